@@ -1,0 +1,283 @@
+"""Python view of the C ABI in include/disco_gpu.h (ctypes).
+
+This mirrors the reference's driver loop (main.c:27-89): parameters come from
+in.par (readpar.c) and module names from Makefile_opt.in; `getmindt()` and
+`timestep(dt)` replace the reference's getmindt/timestep hooks.  All compute
+runs in the native library; if it cannot be loaded or finds no GPU the calls
+raise -- there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import build as _build
+
+_lib = None
+
+
+class DiscoParams(C.Structure):
+    _fields_ = [
+        ("t_min", C.c_double), ("t_max", C.c_double),
+        ("Num_R", C.c_int), ("Num_Z", C.c_int),
+        ("aspect", C.c_double),
+        ("rmin", C.c_double), ("rmax", C.c_double), ("zmin", C.c_double), ("zmax", C.c_double),
+        ("phimax", C.c_double),
+        ("NoBC_Rmin", C.c_int), ("NoBC_Rmax", C.c_int), ("NoBC_Zmin", C.c_int), ("NoBC_Zmax", C.c_int),
+        ("LogZoning", C.c_int), ("R_Periodic", C.c_int), ("Z_Periodic", C.c_int),
+        ("LogRadius", C.c_double),
+        ("Mesh_Motion", C.c_int), ("Riemann_Solver", C.c_int), ("Timestep", C.c_int),
+        ("CFL", C.c_double), ("PLM", C.c_double), ("maxDT", C.c_double),
+        ("Density_Floor", C.c_double), ("Pressure_Floor", C.c_double),
+        ("Exact_Mesh_Omega", C.c_int), ("Exact_Mesh_Omega_Par", C.c_double),
+        ("Energy_Omega", C.c_int), ("Energy_Omega_Par", C.c_double),
+        ("RotFrame", C.c_int), ("RotOmega", C.c_double), ("RotD", C.c_double),
+        ("Adiabatic_Index", C.c_double),
+        ("visc_flag", C.c_int), ("viscosity", C.c_double),
+        ("alpha_flag", C.c_int),
+        ("isothermal_flag", C.c_int),
+        ("Cs2_Profile", C.c_int), ("Cs2_Par", C.c_double),
+        ("Disk_Mach", C.c_double), ("Mass_Ratio", C.c_double),
+        ("grav2D", C.c_int),
+        ("CT", C.c_int),
+        ("metricPar0", C.c_int), ("metricPar1", C.c_double), ("metricPar2", C.c_double),
+        ("metricPar3", C.c_double), ("metricPar4", C.c_double),
+        ("initPar0", C.c_int), ("initPar1", C.c_double), ("initPar2", C.c_double),
+        ("initPar3", C.c_double), ("initPar4", C.c_double), ("initPar5", C.c_double),
+        ("initPar6", C.c_double), ("initPar7", C.c_double), ("initPar8", C.c_double),
+        ("noiseType", C.c_int), ("noiseAbs", C.c_double), ("noiseRel", C.c_double),
+        ("sinkType", C.c_int), ("nozzleType", C.c_int), ("coolType", C.c_int),
+        ("dampInnerType", C.c_int), ("dampOuterType", C.c_int),
+        ("dampUpperType", C.c_int), ("dampLowerType", C.c_int),
+        ("grav_eps", C.c_double),
+        ("read_errors", C.c_int),
+    ]
+
+
+class DiscoModules(C.Structure):
+    _fields_ = [
+        ("hydro", C.c_int), ("initial", C.c_int), ("boundary", C.c_int), ("planets", C.c_int),
+        ("num_c", C.c_int), ("num_n", C.c_int), ("ct_mode", C.c_int),
+        ("initial_name", C.c_char * 64), ("hydro_name", C.c_char * 64),
+        ("boundary_name", C.c_char * 64), ("planets_name", C.c_char * 64),
+    ]
+
+
+class DiscoPlanet(C.Structure):
+    _fields_ = [("r", C.c_double), ("phi", C.c_double), ("M", C.c_double),
+                ("omega", C.c_double), ("vr", C.c_double), ("eps", C.c_double),
+                ("type", C.c_int)]
+
+
+class DiscoHostDomain(C.Structure):
+    _fields_ = [
+        ("par", DiscoParams), ("mod", DiscoModules),
+        ("Nr", C.c_int), ("Nz", C.c_int), ("NgRa", C.c_int), ("NgRb", C.c_int),
+        ("NgZa", C.c_int), ("NgZb", C.c_int),
+        ("num_q", C.c_int), ("num_faces", C.c_int),
+        ("Ncell", C.c_long),
+        ("Np", C.POINTER(C.c_int)), ("ring_off", C.POINTER(C.c_long)),
+        ("r_jph", C.POINTER(C.c_double)), ("z_kph", C.POINTER(C.c_double)),
+        ("phi_max", C.c_double), ("t", C.c_double),
+        ("piph", C.POINTER(C.c_double)), ("dphi", C.POINTER(C.c_double)),
+        ("prim", C.POINTER(C.c_double)),
+        ("Npl", C.c_int),
+        ("planets", DiscoPlanet * 4),
+    ]
+
+
+class DiscoStateView(C.Structure):
+    _fields_ = [("piph", C.POINTER(C.c_double)), ("dphi", C.POINTER(C.c_double)),
+                ("wiph", C.POINTER(C.c_double)), ("prim", C.POINTER(C.c_double)),
+                ("cons", C.POINTER(C.c_double)), ("Phi", C.POINTER(C.c_double)),
+                ("t", C.c_double)]
+
+
+class DiscoGpuErrs(C.Structure):
+    _fields_ = [("nan_cells", C.c_longlong), ("rho_floor_hits", C.c_longlong),
+                ("p_floor_hits", C.c_longlong), ("face_errors", C.c_longlong),
+                ("steps", C.c_longlong)]
+
+
+# Every symbol include/disco_gpu.h declares, with its ctypes signature.
+_P = C.c_void_p
+SIGNATURES = {
+    "disco_params_read": (C.c_int, [C.c_char_p, C.POINTER(DiscoParams)]),
+    "disco_modules_read": (C.c_int, [C.c_char_p, C.POINTER(DiscoModules)]),
+    "disco_host_setup": (C.c_int, [C.POINTER(DiscoParams), C.POINTER(DiscoModules),
+                                   C.POINTER(C.POINTER(DiscoHostDomain))]),
+    "disco_host_free": (None, [C.POINTER(DiscoHostDomain)]),
+    "disco_gpu_create": (C.c_int, [C.POINTER(DiscoHostDomain), C.c_int, C.POINTER(_P)]),
+    "disco_gpu_getmindt": (C.c_int, [_P, C.POINTER(C.c_double)]),
+    "disco_gpu_timestep": (C.c_int, [_P, C.c_double]),
+    "disco_gpu_run": (C.c_int, [_P, C.c_int, C.c_double]),
+    "disco_gpu_download": (C.c_int, [_P, C.POINTER(DiscoStateView)]),
+    "disco_gpu_upload": (C.c_int, [_P, C.POINTER(DiscoStateView)]),
+    "disco_gpu_status": (C.c_int, [_P, C.POINTER(DiscoGpuErrs)]),
+    "disco_gpu_time": (C.c_double, [_P]),
+    "disco_gpu_num_cells": (C.c_long, [_P]),
+    "disco_gpu_num_real_cells": (C.c_long, [_P]),
+    "disco_gpu_free": (None, [_P]),
+    "disco_gpu_launch_count": (C.c_longlong, []),
+    "disco_last_error": (C.c_char_p, []),
+    "disco_abi_version": (C.c_int, []),
+}
+
+
+def lib(build_if_missing: bool = True) -> C.CDLL:
+    """Load libdisco_gb300.so (building it first if needed)."""
+    global _lib
+    if _lib is None:
+        path = _build.LIB
+        if build_if_missing:
+            path = _build.build()
+        if not os.path.exists(path):
+            raise RuntimeError(f"native library missing: {path}")
+        L = C.CDLL(path)
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+class DiscoError(RuntimeError):
+    pass
+
+
+def _check(rc: int, what: str) -> None:
+    if rc != 0:
+        msg = lib().disco_last_error().decode(errors="replace")
+        raise DiscoError(f"{what} failed ({rc}): {msg}")
+
+
+def read_params(in_par: str) -> DiscoParams:
+    p = DiscoParams()
+    _check(lib().disco_params_read(in_par.encode(), C.byref(p)), "disco_params_read")
+    return p
+
+
+def read_modules(makefile_opt: str) -> DiscoModules:
+    m = DiscoModules()
+    _check(lib().disco_modules_read(makefile_opt.encode(), C.byref(m)), "disco_modules_read")
+    return m
+
+
+class HostDomain:
+    """Host-side grid + initial state (disco_host_setup), no GPU needed."""
+
+    def __init__(self, params: DiscoParams, modules: DiscoModules):
+        ptr = C.POINTER(DiscoHostDomain)()
+        _check(lib().disco_host_setup(C.byref(params), C.byref(modules), C.byref(ptr)),
+               "disco_host_setup")
+        self._ptr = ptr
+        d = ptr.contents
+        self.Nr, self.Nz = d.Nr, d.Nz
+        self.NgRa, self.NgRb, self.NgZa, self.NgZb = d.NgRa, d.NgRb, d.NgZa, d.NgZb
+        self.num_q = d.num_q
+        self.Ncell = d.Ncell
+        self.phi_max = d.phi_max
+        self.t = d.t
+        n = self.Ncell
+        self.Np = np.ctypeslib.as_array(d.Np, (self.Nr * self.Nz,)).copy()
+        self.ring_off = np.ctypeslib.as_array(d.ring_off, (self.Nr * self.Nz + 1,)).copy()
+        self.r_jph = np.ctypeslib.as_array(d.r_jph, (self.Nr + 1,)).copy()
+        self.z_kph = np.ctypeslib.as_array(d.z_kph, (self.Nz + 1,)).copy()
+        self.piph = np.ctypeslib.as_array(d.piph, (n,)).copy()
+        self.dphi = np.ctypeslib.as_array(d.dphi, (n,)).copy()
+        self.prim = np.ctypeslib.as_array(d.prim, (self.num_q * n,)).copy().reshape(self.num_q, n)
+
+    def real_mask(self) -> np.ndarray:
+        jk = np.repeat(np.arange(self.Nr * self.Nz), self.Np)
+        j, k = jk % self.Nr, jk // self.Nr
+        return ((j >= self.NgRa) & (j < self.Nr - self.NgRb) &
+                (k >= self.NgZa) & (k < self.Nz - self.NgZb))
+
+    def __del__(self):
+        if getattr(self, "_ptr", None) is not None and _lib is not None:
+            _lib.disco_host_free(self._ptr)
+            self._ptr = None
+
+
+class Domain:
+    """A domain resident on the GPU: the reference's getmindt/timestep pair."""
+
+    def __init__(self, in_par: str, makefile_opt: str, precision: int = 0,
+                 overrides: dict | None = None):
+        self.params = read_params(in_par)
+        for k, v in (overrides or {}).items():
+            setattr(self.params, k, v)
+        self.modules = read_modules(makefile_opt)
+        self.host = HostDomain(self.params, self.modules)
+        g = C.c_void_p()
+        _check(lib().disco_gpu_create(self.host._ptr, int(precision), C.byref(g)), "disco_gpu_create")
+        self._g = g
+        self.precision = precision
+
+    # -- the reference's hot-path entry points -----------------------------
+    def getmindt(self) -> float:
+        dt = C.c_double()
+        _check(lib().disco_gpu_getmindt(self._g, C.byref(dt)), "disco_gpu_getmindt")
+        return dt.value
+
+    def timestep(self, dt: float) -> None:
+        _check(lib().disco_gpu_timestep(self._g, float(dt)), "disco_gpu_timestep")
+
+    def run(self, nsteps: int, t_end: float = 0.0) -> None:
+        _check(lib().disco_gpu_run(self._g, int(nsteps), float(t_end)), "disco_gpu_run")
+
+    @property
+    def t(self) -> float:
+        return lib().disco_gpu_time(self._g)
+
+    @property
+    def num_cells(self) -> int:
+        return lib().disco_gpu_num_cells(self._g)
+
+    @property
+    def num_real_cells(self) -> int:
+        return lib().disco_gpu_num_real_cells(self._g)
+
+    def state(self) -> dict:
+        n = self.num_cells
+        q = self.host.num_q
+        out = {k: np.empty(n) for k in ("piph", "dphi", "wiph")}
+        out["prim"] = np.empty((q, n))
+        out["cons"] = np.empty((q, n))
+        v = DiscoStateView()
+        dp = C.POINTER(C.c_double)
+        for k in ("piph", "dphi", "wiph", "prim", "cons"):
+            setattr(v, k, out[k].ctypes.data_as(dp))
+        _check(lib().disco_gpu_download(self._g, C.byref(v)), "disco_gpu_download")
+        out["t"] = v.t
+        return out
+
+    def upload(self, **arrays) -> None:
+        v = DiscoStateView()
+        dp = C.POINTER(C.c_double)
+        keep = []
+        for k in ("piph", "dphi", "wiph", "prim", "cons"):
+            if k in arrays:
+                a = np.ascontiguousarray(arrays[k], dtype=np.float64)
+                keep.append(a)
+                setattr(v, k, a.ctypes.data_as(dp))
+        _check(lib().disco_gpu_upload(self._g, C.byref(v)), "disco_gpu_upload")
+
+    def status(self) -> dict:
+        e = DiscoGpuErrs()
+        _check(lib().disco_gpu_status(self._g, C.byref(e)), "disco_gpu_status")
+        return {k: getattr(e, k) for k, _ in DiscoGpuErrs._fields_}
+
+    def close(self) -> None:
+        if getattr(self, "_g", None):
+            lib().disco_gpu_free(self._g)
+            self._g = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

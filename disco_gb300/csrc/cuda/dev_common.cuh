@@ -1,0 +1,220 @@
+// Device-side parameters, state arrays and the small geometry / frame /
+// gravity helpers the hot path calls per cell and per face.  Every helper
+// names the reference function it restates; arithmetic follows the same
+// operation order so the FP64 path tracks the reference to rounding.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+#include <math.h>
+
+#define DISCO_HD __host__ __device__
+#define DISCO_D __device__ __forceinline__
+
+namespace disco {
+
+// primitive / conserved component indices (paul.h:4-5)
+enum { RHO = 0, PPP = 1, URR = 2, UPP = 3, UZZ = 4, BRR = 5, BPP = 6, BZZ = 7 };
+enum { DDD = 0, TAU = 1, SRR = 2, LLL = 3, SZZ = 4 };
+enum { PL_POINTMASS = 0, PL_PW = 1, PL_SURFACEGRAV = 2, PL_SPLINE = 3, PL_WEGGC = 4 };
+enum { SOLVER_HLL = 0, SOLVER_HLLC = 1, SOLVER_HLLD = 2, SOLVER_HLLC_DAMP = 3 };
+
+constexpr int MAX_Q = 9;
+constexpr int MAX_PL = 4;
+
+struct DevPlanet {
+  double r, phi, M, omega, vr, eps;
+  int type;
+};
+
+// Hot-path parameters (the module-static values the reference pushes with
+// set*Params, domain.c:259-270), passed by value to every kernel.
+struct DevParams {
+  int Nr, Nz, NgRa, NgRb, NgZa, NgZb;
+  long long Ncell;
+  int num_q, num_c;
+  double phi_max;
+  // Hydro/euler.c:6-27 and Hydro/mhd.c:6-22
+  double gamma_law, rho_floor, p_floor, explicit_viscosity, mach;
+  int include_viscosity, isothermal, alpha_flag, polar_sources;
+  // riemann.c:7-10, misc.c, plm.c
+  int riemann_solver, mesh_motion;
+  double PLM, CFL, maxDT;
+  // omega.c:4-38
+  int meshOmChoice, enOmChoice, cs2Choice;
+  double Omega0, om_M, om_r1, om_H0, eps;
+  // rotframe.c:4-12
+  int rot_flag;
+  double rot_omega, rot_d;
+  // planet.c:4-35
+  int grav2D, polar_r, polar_p;
+  int Npl;
+  // initial / boundary plugins
+  int initial_id, boundary_id;
+  double ic[8];
+  double t_end;
+};
+
+// ---- cylindrical geometry: Geometry/cylindrical.c ------------------------
+DISCO_HD inline double get_dp(double phip, double phim, double phi_max) {
+  double dp = phip - phim;                       // cylindrical.c:10-15
+  while (dp < 0.0) dp += phi_max;
+  while (dp > phi_max) dp -= phi_max;
+  return dp;
+}
+DISCO_HD inline double get_signed_dp(double phip, double phim, double phi_max) {
+  double dp = phip - phim;                       // cylindrical.c:17-22
+  while (dp < -.5 * phi_max) dp += phi_max;
+  while (dp > .5 * phi_max) dp -= phi_max;
+  return dp;
+}
+DISCO_HD inline double centroid_r(double xp, double xm) {
+  return 2.0 * (xp * xp + xp * xm + xm * xm) / (3.0 * (xp + xm));  // cylindrical.c:24-30
+}
+DISCO_HD inline double centroid_z(double xp, double xm) { return 0.5 * (xp + xm); }
+
+// ---- omega.c ----------------------------------------------------------------
+template <typename R>
+DISCO_D R mesh_om(const DevParams& P, R r) {           // omega.c:56-74
+  r = sqrt(r * r + (R)P.eps * (R)P.eps);
+  if (P.meshOmChoice == 1) return (R)1.0;
+  if (P.meshOmChoice == 2) return pow(r, (R)-1.5);
+  if (P.meshOmChoice == 3) { R n = 4.0; return (R)1. / pow(pow(r, (R)1.5 * n) + (R)1., (R)1. / n); }
+  return (R)0.0;
+}
+template <typename R>
+DISCO_D R get_om(const DevParams& P, R r) {            // omega.c:76-100
+  if (P.enOmChoice == 0) return (R)0.0 - (R)P.Omega0;
+  r = sqrt(r * r + (R)P.eps * (R)P.eps);
+  if (P.enOmChoice == 1) return (R)1.0 - (R)P.Omega0;
+  if (P.enOmChoice == 2) return (R)1.0 / pow(r, (R)1.5) - (R)P.Omega0;
+  if (P.enOmChoice == 3) { R n = 8.0; return (R)1. / pow(pow(r, (R)1.5 * n) + (R)1., (R)1. / n) - (R)P.Omega0; }
+  if (P.enOmChoice == 4) return (R)10. * exp((R)-.5 * r * r) - (R)P.Omega0;
+  return (R)0.0 - (R)P.Omega0;
+}
+template <typename R>
+DISCO_D R get_om1(const DevParams& P, R r) {           // omega.c:102-126
+  if (P.enOmChoice == 0 || P.enOmChoice == 1) return (R)0.0;
+  r = sqrt(r * r + (R)P.eps * (R)P.eps);
+  if (P.enOmChoice == 2) return (R)-1.5 / pow(r, (R)2.5);
+  if (P.enOmChoice == 3) {
+    R n = 8.0;
+    return (R)-1.5 * pow(r, (R)-1 + (R)1.5 * n) / pow(pow(r, (R)1.5 * n) + (R)1., (R)1.0 + (R)1. / n);
+  }
+  if (P.enOmChoice == 4) return (R)10. * r * exp((R)-.5 * r * r);
+  return (R)0.0;
+}
+
+// ---- planet.c ---------------------------------------------------------------
+template <typename R>
+DISCO_D R phigrav(R M, R r, R eps, int type) {          // planet.c:37-73 (point mass)
+  if (type == PL_POINTMASS) {
+    R n = 2.0;
+    return M / pow(pow(r, n) + pow(eps, n), (R)1. / n);
+  }
+  return (R)0.0;
+}
+template <typename R>
+DISCO_D R fgrav(R M, R r, R eps, int type) {            // planet.c:75-112 (point mass)
+  if (type == PL_POINTMASS) {
+    R n = 2.0;
+    return M * pow(r, n - (R)1.) / pow(pow(r, n) + pow(eps, n), (R)1. + (R)1. / n);
+  }
+  if (type == PL_SURFACEGRAV) return M;
+  return (R)0.0;
+}
+
+template <typename R>
+DISCO_D R get_cs2(const DevParams& P, const DevPlanet* pl, R r, R phi) {  // omega.c:157-209
+  if (P.cs2Choice == 1) return (R)1. / ((R)P.mach * (R)P.mach);
+  if (P.cs2Choice == 2) { R nu = .5; return (R).5 / (R)P.mach / (R)P.mach / pow(r, (R)2. * nu); }
+  if (P.cs2Choice == 3) return (R)P.om_M * (R)P.om_H0 * (R)P.om_H0 / ((R)2 * (R)P.om_r1 * (R)P.om_r1 * (R)P.om_r1);
+  if (P.cs2Choice == 4) {
+    r = sqrt(r * r + (R)P.eps * (R)P.eps);
+    R v2 = (R)P.om_M / r;
+    return v2 / ((R)P.mach * (R)P.mach);
+  }
+  if (P.cs2Choice == 5) {
+    R cosp = cos(phi), sinp = sin(phi);
+    R gx = r * cosp, gy = r * sinp;
+    R phip = 0.0;
+    for (int p = 0; p < P.Npl; ++p) {
+      R px = (R)pl[p].r * cos((R)pl[p].phi);
+      R py = (R)pl[p].r * sin((R)pl[p].phi);
+      R pr = (px - gx) * (px - gx) + (py - gy) * (py - gy);
+      phip += phigrav<R>((R)pl[p].M, sqrt(pr), (R)pl[p].eps, pl[p].type);
+    }
+    return phip / ((R)P.mach * (R)P.mach);
+  }
+  return (R)1.0;
+}
+
+// planetaryForce (planet.c:138-188), mode 0.
+template <typename R>
+DISCO_D void planetary_force(const DevParams& P, const DevPlanet& pl, R r, R phi, R z,
+                             R* fr, R* fp, R* fz) {
+  R rp = (R)pl.r, pp = (R)pl.phi;
+  if (P.grav2D == 1) z = 0.0;
+  else if (P.grav2D == 2) { rp = r; pp = phi; z = 1.0; }
+  R cosp = cos(phi), sinp = sin(phi);
+  R dx = r * cosp - rp * cos(pp);
+  R dy = r * sinp - rp * sin(pp);
+  R script_r = sqrt(dx * dx + dy * dy + z * z);
+  R script_r_perp = sqrt(dx * dx + dy * dy);
+  R f1 = -fgrav<R>((R)pl.M, script_r, (R)pl.eps, pl.type);
+  R cosa = dx / script_r_perp, sina = dy / script_r_perp;
+  R cosap = cosa * cosp + sina * sinp;
+  R sinap = sina * cosp - cosa * sinp;
+  if (script_r_perp <= (R)0.0) { cosap = 0.0; sinap = 0.0; }
+  R sint = script_r_perp / script_r;
+  R cost = z / script_r;
+  *fr = cosap * f1 * sint;
+  *fp = sinap * f1 * sint;
+  *fz = f1 * cost;
+}
+
+// planet_src (planet.c:190-234) for one planet, cylindrical coordinates.
+template <typename R>
+DISCO_D void planet_src(const DevParams& P, const DevPlanet& pl, const R* prim, double* cons,
+                        const double* xp, const double* xm, double dVdt) {
+  R rho = prim[RHO], vr = prim[URR], vz = prim[UZZ], omega = prim[UPP];
+  double dphi = get_dp(xp[1], xm[1], P.phi_max);
+  double phi = xm[1] + 0.5 * dphi;
+  R x0 = (R)centroid_r(xp[0], xm[0]);
+  R x2 = (R)centroid_z(xp[2], xm[2]);
+  R F0, F1, F2;
+  planetary_force<R>(P, pl, x0, (R)phi, x2, &F0, &F1, &F2);
+  R hr = 1.0, hp = x0, hz = 1.0;
+  if (P.polar_r || P.polar_p) {
+    // geom_polar_vec_adjust, cylindrical.c:175-183
+    double dp = get_dp(xp[1], xm[1], P.phi_max);
+    R adjust = (R)(sin(0.5 * dp) / (0.5 * dp));
+    if (P.polar_r) F0 *= adjust;
+    if (P.polar_p) F1 *= adjust;
+  }
+  cons[SRR] += (double)(rho * hr * F0 * (R)dVdt);
+  cons[LLL] += (double)(rho * hp * F1 * (R)dVdt);
+  cons[SZZ] += (double)(rho * hz * F2 * (R)dVdt);
+  cons[TAU] += (double)(rho * (hr * F0 * vr + hz * F2 * vz + hp * F1 * omega) * (R)dVdt);
+}
+
+// get_height_om (omega.c:132-155): sqrt(sum_p fgrav / script_r).
+template <typename R>
+DISCO_D R get_height_om(const DevParams& P, const DevPlanet* pl, R r, R phi) {
+  R omtot2 = 0.0;
+  R gx = r * cos(phi), gy = r * sin(phi);
+  for (int p = 0; p < P.Npl; ++p) {
+    R px = (R)pl[p].r * cos((R)pl[p].phi);
+    R py = (R)pl[p].r * sin((R)pl[p].phi);
+    R sr = sqrt((px - gx) * (px - gx) + (py - gy) * (py - gy));
+    R f1 = fgrav<R>((R)pl[p].M, sr, (R)pl[p].eps, pl[p].type);
+    omtot2 += f1 / (sr + (R)0.0625 * (R)pl[p].eps);
+  }
+  return sqrt(omtot2);
+}
+
+// Health counters written by kernels (never trap).
+struct DevErrs {
+  unsigned long long nan_cells, rho_floor_hits, p_floor_hits, face_errors, steps;
+};
+
+}  // namespace disco

@@ -1,0 +1,878 @@
+// Kernels of one RK substep (onestep.c:86-186) on ragged SoA ring arrays.
+//
+// Layout in HBM (N = cells incl. ghosts, ring jk = j + Nr*k):
+//   cell c of ring jk lives at ring_off[jk] + i;  per-component arrays are
+//   SoA: prim[q*N + c] (R), cons/RKcons[q*N + c] (FP64), gradp/gradr/gradz
+//   [q*N + c] (R), piph/dphi/wiph[c] (FP64).
+//   Sheared r (dim 1) and z (dim 2) faces are stored per ring pair in a
+//   static block face_off[pair] .. face_off[pair+1] (the count Np_L + Np_R
+//   never changes, faces_alt.c:87-100); only their contents are rebuilt.
+#pragma once
+#include "dev_common.cuh"
+#include "riemann.cuh"
+#include "../plugins/ic_vortex_gauss.h"
+#include "../plugins/ic_disks.h"
+
+namespace disco {
+
+template <typename R>
+struct DevState {
+  int N;                       // cells incl. ghosts
+  const int* cell_ring;        // [N] ring id of each cell
+  const int* ring_off;         // [Nr*Nz+1]
+  const double* r_jph;         // [Nr+1], index shifted: r_jph[j+1] = reference r_jph[j]
+  const double* z_kph;         // [Nz+1]
+  const double* piph;          // [N] current positions
+  double* piph_out;            // [N] positions after move_cells (first substep)
+  double* dphi;                // [N]
+  double* wiph;                // [N]
+  R* prim;                     // [NQ*N]
+  double* cons;                // [NQ*N]
+  double* RKcons;              // [NQ*N]
+  R* gradp;                    // [NQ*N]
+  R* gradr;                    // [NQ*N]
+  R* gradz;                    // [NQ*N]
+  R* fphi;                     // [NQ*N]  (F - wU*) dA dt of the phi face i|i+1
+  // ring anchors (faces_alt.c:57-79)
+  int* anchor;                 // [Nr*Nz]
+  // sheared faces, index d = 0 (r) / 1 (z)
+  const int* face_off[2];      // [npairs+1]
+  int* fL[2];                  // [Nf] global cell id
+  int* fR[2];
+  signed char* fLR[2];         // LRtype
+  double* fphic[2];            // cm[1]
+  double* fdA[2];              // dA
+  R* fflux[2];                 // [NQ*Nf] (F - wU*) dA dt
+  int* run_up_s[2];            // per cell: first face where the cell is L (pair above)
+  int* run_up_e[2];
+  int* run_dn_s[2];            // per cell: first face where the cell is R (pair below)
+  int* run_dn_e[2];
+  int nf[2];
+  DevPlanet* planets;          // [Npl], device copy (moves for analytic orbits)
+  double* scal;                // [0] dt, [1] t, [2] min-dt accumulator (bits)
+  DevErrs* errs;
+};
+
+enum { SC_DT = 0, SC_T = 1, SC_MIN = 2, SC_COUNT = 4 };
+
+DISCO_D bool is_real(const DevParams& P, int j, int k) {
+  return j >= P.NgRa && j < P.Nr - P.NgRb && k >= P.NgZa && k < P.Nz - P.NgZb;
+}
+
+// ---- initial() dispatch (plugin chosen by Makefile_opt.in INITIAL) --------
+DISCO_D void initial_eval(const DevParams& P, double* prim, const double* x) {
+  if (P.initial_id == 0) {
+    disco_ic_vortex_gauss V{P.ic[0], P.ic[1], P.ic[2], P.ic[3], P.ic[4], P.gamma_law};
+    disco_ic_vortex_gauss_eval(&V, prim, x, P.num_c, P.num_q);
+  } else {
+    disco_ic_disk D;
+    disco_ic_disk_from_params(&D, P.gamma_law, P.mach, P.ic[0], P.ic[1], P.ic[2], P.ic[3],
+                              P.ic[4], P.ic[5]);
+    if (P.initial_id == 1) disco_ic_disk_mhd_eval(&D, prim, x, P.num_c, P.num_q);
+    else disco_ic_disk_planet_eval(&D, prim, x, P.num_c, P.num_q);
+  }
+  if (P.rot_flag) prim[UPP] -= P.rot_omega;   // subtract_omega, rotframe.c:15
+}
+
+// ---- set_wcell, misc.c:101-168 --------------------------------------------
+template <typename R, int NQ>
+__global__ void k_wcell(DevParams P, DevState<R> S) {
+  int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= S.N) return;
+  int jk = S.cell_ring[c];
+  int j = jk % P.Nr, k = jk / P.Nr;
+  int off = S.ring_off[jk], Np = S.ring_off[jk + 1] - off;
+  int i = c - off;
+  double w = 0.0;
+  if (P.mesh_motion == 4) {
+    double r = centroid_r(S.r_jph[j + 1], S.r_jph[j]);
+    w = (double)mesh_om<double>(P, r);
+  } else if (P.mesh_motion) {
+    int ip = (i + 1) % Np;
+    double wL = (double)S.prim[UPP * S.N + c];        // get_omega: prim[UPP]
+    double wR = (double)S.prim[UPP * S.N + off + ip];
+    w = .5 * (wL + wR);
+  }
+  (void)k;
+  S.wiph[c] = w;
+}
+
+// Mesh_Motion 3: ring average of w (misc.c:138-152), one block per ring.
+template <typename R>
+__global__ void k_wcell_avg(DevParams P, DevState<R> S) {
+  int jk = blockIdx.x;
+  int off = S.ring_off[jk], Np = S.ring_off[jk + 1] - off;
+  __shared__ double red[256];
+  double s = 0.0;
+  for (int i = threadIdx.x; i < Np; i += blockDim.x) s += S.wiph[off + i];
+  red[threadIdx.x] = s;
+  __syncthreads();
+  for (int h = blockDim.x / 2; h > 0; h >>= 1) {
+    if ((int)threadIdx.x < h) red[threadIdx.x] += red[threadIdx.x + h];
+    __syncthreads();
+  }
+  double w = red[0] / (double)Np;
+  for (int i = threadIdx.x; i < Np; i += blockDim.x) S.wiph[off + i] = w;
+}
+
+// ---- plm_phi, plm.c:6-51 ------------------------------------------------
+template <typename R>
+DISCO_D R minmod(R a, R b, R c) {
+  R m = a;
+  if (a * b < (R)0.0) m = 0.0;
+  if (fabs(b) < fabs(m)) m = b;
+  if (b * c < (R)0.0) m = 0.0;
+  if (fabs(c) < fabs(m)) m = c;
+  return m;
+}
+
+template <typename R, int NQ>
+__global__ void k_plm_phi(DevParams P, DevState<R> S) {
+  int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= S.N) return;
+  int jk = S.cell_ring[c];
+  int off = S.ring_off[jk], Np = S.ring_off[jk + 1] - off;
+  int i = c - off;
+  int cm = off + (i == 0 ? Np - 1 : i - 1);
+  int cp = off + (i + 1 == Np ? 0 : i + 1);
+  R dpL = (R)S.dphi[cm], dpC = (R)S.dphi[c], dpR = (R)S.dphi[cp];
+  R PLM = (R)P.PLM;
+  const int N = S.N;
+#pragma unroll
+  for (int q = 0; q < NQ; ++q) {
+    R pL = S.prim[q * N + cm], pC = S.prim[q * N + c], pR = S.prim[q * N + cp];
+    R sL = pC - pL;
+    sL /= (R).5 * (dpC + dpL);
+    R sR = pR - pC;
+    sR /= (R).5 * (dpR + dpC);
+    R sC = pR - pL;
+    sC /= (R).5 * (dpL + dpR) + dpC;
+    S.gradp[q * N + c] = minmod<R>(PLM * sL, sC, PLM * sR);
+  }
+}
+
+// ---- ring anchors, faces_alt.c:57-79 -----------------------------------------
+// Quadrant tests of sin/cos(piph * 2pi/Pmax) done as exact comparisons of the
+// double theta against the doubles bracketing pi/2, pi, 3pi/2, 2pi: the sign
+// of sin/cos of a double is fixed by which side of those irrationals it lies.
+DISCO_D int quadrant_q1(double th) {  // sin > 0 && cos > 0
+  const double PI_2_LO = 1.5707963267948965579989817342720925807952880859375;   // < pi/2
+  const double TWO_PI_LO = 6.28318530717958623199592693708837032318115234375;    // < 2pi
+  return (th > 0.0 && th <= PI_2_LO) || (th > TWO_PI_LO);
+}
+DISCO_D int quadrant_q4(double th) {  // sin < 0 && cos > 0
+  const double THREE_PI_2_LO = 4.71238898038468967399694520281627774238586425781250;  // < 3pi/2
+  const double TWO_PI_LO = 6.28318530717958623199592693708837032318115234375;
+  return th > THREE_PI_2_LO && th <= TWO_PI_LO;
+}
+
+// One warp per ring: I0 = first Q1 cell after the first Q4 cell, else 0.
+template <typename R>
+__global__ void k_anchor(DevParams P, DevState<R> S, int nring) {
+  int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  int lane = threadIdx.x & 31;
+  if (warp >= nring) return;
+  int off = S.ring_off[warp], Np = S.ring_off[warp + 1] - off;
+  double convert = 2. * M_PI / P.phi_max;
+  int firstQ4 = 0x7fffffff;
+  for (int i = lane; i < Np; i += 32)
+    if (quadrant_q4(S.piph[off + i] * convert)) { firstQ4 = min(firstQ4, i); }
+  for (int o = 16; o > 0; o >>= 1) firstQ4 = min(firstQ4, __shfl_xor_sync(0xffffffffu, firstQ4, o));
+  int I0 = 0x7fffffff;
+  for (int i = lane; i < Np; i += 32)
+    if (i > firstQ4 && quadrant_q1(S.piph[off + i] * convert)) { I0 = min(I0, i); }
+  for (int o = 16; o > 0; o >>= 1) I0 = min(I0, __shfl_xor_sync(0xffffffffu, I0, o));
+  if (lane == 0) S.anchor[warp] = (I0 == 0x7fffffff) ? 0 : I0;
+}
+
+// ---- sheared faces, faces_alt.c:36-179 ---------------------------------------
+// One block per ring pair.  The reference walks both rings from their anchors,
+// advancing the ring whose upper cell edge comes first (ties advance L).  That
+// walk is a merge of the two circular sequences; face n sits at merge-path
+// state (a, b), a + b = n.  Each thread binary-searches the state at the start
+// of its chunk using exact (lap, phi) keys, then walks the chunk with the
+// reference's own wrapped comparison.
+struct PairInfo {
+  int L, R, jL, kL;  // ring ids and (j, k) of the L ring
+};
+
+DISCO_D PairInfo pair_info(const DevParams& P, int dim, int pair) {
+  PairInfo pi;
+  if (dim == 1) {
+    int j = pair % (P.Nr - 1), k = pair / (P.Nr - 1);
+    pi.L = j + P.Nr * k; pi.R = j + 1 + P.Nr * k; pi.jL = j; pi.kL = k;
+  } else {
+    int j = pair % P.Nr, k = pair / P.Nr;
+    pi.L = j + P.Nr * k; pi.R = j + P.Nr * (k + 1); pi.jL = j; pi.kL = k;
+  }
+  return pi;
+}
+
+template <typename R>
+__global__ void k_faces(DevParams P, DevState<R> S, int dim) {
+  extern __shared__ double smem[];
+  const int d = dim - 1;
+  int pair = blockIdx.x;
+  PairInfo pi = pair_info(P, dim, pair);
+  int offL = S.ring_off[pi.L], NL = S.ring_off[pi.L + 1] - offL;
+  int offR = S.ring_off[pi.R], NR = S.ring_off[pi.R + 1] - offR;
+  int I0L = S.anchor[pi.L], I0R = S.anchor[pi.R];
+  int Nf = NL + NR;
+  int base = S.face_off[d][pair];
+  double* sL = smem;
+  double* sR = smem + NL;
+  signed char* sLR = (signed char*)(smem + NL + NR);
+  const double Pmax = P.phi_max;
+
+  for (int m = threadIdx.x; m < NL; m += blockDim.x) sL[m] = S.piph[offL + (I0L + m) % NL];
+  for (int m = threadIdx.x; m < NR; m += blockDim.x) sR[m] = S.piph[offR + (I0R + m) % NR];
+  __syncthreads();
+
+  // lap offset of R relative to L from the anchors' wrapped comparison
+  int offlap = 0;
+  {
+    double raw = sL[0] - sR[0];
+    if (raw > .5 * Pmax) offlap = 1;
+    else if (raw < -.5 * Pmax) offlap = -1;
+  }
+  const double A0 = sL[0], B0 = sR[0];
+  auto keyL = [&](int a, int& lap, double& ph) {
+    int m = a % NL;
+    ph = sL[m];
+    lap = a / NL + ((m > 0 && ph < A0) ? 1 : 0);
+  };
+  auto keyR = [&](int b, int& lap, double& ph) {
+    int m = b % NR;
+    ph = sR[m];
+    lap = b / NR + ((m > 0 && ph < B0) ? 1 : 0) + offlap;
+  };
+
+  int j = pi.jL, k = pi.kL;
+  const double* rj = S.r_jph + 1;  // rj[j] == reference r_jph[j]
+  const double* zk = S.z_kph + 1;
+
+  int chunk = (Nf + blockDim.x - 1) / blockDim.x;
+  int n0 = threadIdx.x * chunk;
+  int n1 = min(n0 + chunk, Nf);
+  if (n0 < Nf) {
+    int lo = 0, hi = n0;
+    while (lo < hi) {
+      int mid = (lo + hi) >> 1;
+      int la, lb; double pa, pb;
+      keyL(mid, la, pa);
+      keyR(n0 - 1 - mid, lb, pb);
+      bool le = (la < lb) || (la == lb && pa <= pb);
+      if (le) lo = mid + 1; else hi = mid;
+    }
+    int a = lo, b = n0 - lo;
+    for (int n = n0; n < n1; ++n) {
+      int iL = offL + (I0L + a) % NL;
+      int iR = offR + (I0R + b) % NR;
+      double pL = S.piph[iL], pR = S.piph[iR];
+      double dL = S.dphi[iL], dR = S.dphi[iR];
+      double dphi = pL - pR;
+      while (dphi > .5 * Pmax) dphi -= Pmax;
+      while (dphi < -.5 * Pmax) dphi += Pmax;
+      int LR = dphi > 0. ? 1 : 0;
+      dphi = pL - dL - pR + dR;
+      while (dphi > .5 * Pmax) dphi -= Pmax;
+      while (dphi < -.5 * Pmax) dphi += Pmax;
+      int LR_back = dphi < 0. ? 1 : 0;
+      double xp1 = LR == 0 ? pL : pR;
+      double xm1 = LR_back == 0 ? pL - dL : pR - dR;
+      // addFace, faces_alt.c:10-34
+      double dp = get_dp(xp1, xm1, Pmax);
+      double phic = get_dp(xp1, .5 * dp, Pmax);
+      double dA;
+      if (dim == 1) dA = (.5 * (rj[j] + rj[j])) * dp * (zk[k] - zk[k - 1]);
+      else dA = (.5 * (rj[j] + rj[j - 1])) * (rj[j] - rj[j - 1]) * dp;
+      int gf = base + n;
+      S.fL[d][gf] = iL;
+      S.fR[d][gf] = iR;
+      S.fLR[d][gf] = (signed char)LR;
+      S.fphic[d][gf] = phic;
+      S.fdA[d][gf] = dA;
+      sLR[n] = (signed char)LR;
+      if (LR == 0) ++a; else ++b;
+    }
+    if (n1 == Nf && (a != NL || b != NR)) atomicAdd(&S.errs->face_errors, 1ull);
+  }
+  __syncthreads();
+  // runs: face n starts L's run if the previous face advanced L (circularly)
+  for (int n = n0; n < n1; ++n) {
+    int gf = base + n;
+    int prev = sLR[(n + Nf - 1) % Nf];
+    int cur = sLR[n];
+    int iL = S.fL[d][gf], iR = S.fR[d][gf];
+    if (prev == 0) S.run_up_s[d][iL] = gf;
+    if (cur == 0) S.run_up_e[d][iL] = gf;
+    if (prev == 1) S.run_dn_s[d][iR] = gf;
+    if (cur == 1) S.run_dn_e[d][iR] = gf;
+  }
+}
+
+// Iterate the faces of a circular run [s, e] of a pair block [base, base+Nf)
+// in ascending face order (the reference's loop order).
+template <typename F>
+DISCO_D void for_run(int s, int e, int base, int Nf, F&& fn) {
+  if (s <= e) {
+    for (int f = s; f <= e; ++f) fn(f);
+  } else {
+    for (int f = base; f <= e; ++f) fn(f);
+    for (int f = s; f < base + Nf; ++f) fn(f);
+  }
+}
+
+DISCO_D int pair_above(const DevParams& P, int dim, int j, int k) {
+  if (dim == 1) return (j < P.Nr - 1) ? j + (P.Nr - 1) * k : -1;
+  return (k < P.Nz - 1) ? j + P.Nr * k : -1;
+}
+DISCO_D int pair_below(const DevParams& P, int dim, int j, int k) {
+  if (dim == 1) return (j > 0) ? (j - 1) + (P.Nr - 1) * k : -1;
+  return (k > 0) ? j + P.Nr * (k - 1) : -1;
+}
+
+// pair spacing dxL + dxR (faces_alt.c:112-135)
+DISCO_D void pair_dx(const DevParams& P, const double* r_jph, const double* z_kph, int dim,
+                     int pair, double* dxL, double* dxR) {
+  const double* rj = r_jph + 1;
+  const double* zk = z_kph + 1;
+  if (dim == 1) {
+    int j = pair % (P.Nr - 1);
+    double rm = centroid_r(rj[j], rj[j - 1]);
+    double rp = centroid_r(rj[j + 1], rj[j]);
+    *dxL = rj[j] - rm;
+    *dxR = rp - rj[j];
+  } else {
+    int k = pair / P.Nr;
+    double zm = centroid_z(zk[k], zk[k - 1]);
+    double zp = centroid_z(zk[k + 1], zk[k]);
+    *dxL = zk[k] - zm;
+    *dxR = zp - zk[k];
+  }
+}
+
+// ---- plm_trans, plm.c:56-195 (per-cell gather over the cell's faces) ---------
+// Sum S dA over the cell's faces, divide by the total area, then limit.  The
+// reference limiter loop (plm.c:146-179) reduces to: zero if any face slope
+// has the opposite sign (or is zero), else the smallest of |g| and |PLM S|,
+// which is independent of face order; it is evaluated in one pass here.
+template <typename R, int NQ>
+__global__ void k_plm_trans(DevParams P, DevState<R> S, int dim) {
+  int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= S.N) return;
+  const int d = dim - 1;
+  const int N = S.N;
+  int jk = S.cell_ring[c];
+  int j = jk % P.Nr, k = jk / P.Nr;
+  R* grad = dim == 1 ? S.gradr : S.gradz;
+  const double Pmax = P.phi_max;
+  R PLM = (R)P.PLM;
+  if (P.PLM == 0.0) {
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) grad[q * N + c] = 0;
+    return;
+  }
+  R sum[NQ], minpos[NQ], maxneg[NQ];
+  unsigned anypos = 0, anyneg = 0, anyzero = 0;
+#pragma unroll
+  for (int q = 0; q < NQ; ++q) { sum[q] = 0; minpos[q] = 0; maxneg[q] = 0; }
+
+  R pc[NQ], gpc[NQ];
+#pragma unroll
+  for (int q = 0; q < NQ; ++q) { pc[q] = S.prim[q * N + c]; gpc[q] = S.gradp[q * N + c]; }
+  double phic_c = S.piph[c] - .5 * S.dphi[c];
+
+  auto visit = [&](int f, int other, bool self_is_L, double dxs) {
+    double phi = S.fphic[d][f];
+    double phiO = S.piph[other] - .5 * S.dphi[other];
+    R dpL, dpR;
+    if (self_is_L) {
+      dpL = (R)get_signed_dp(phi, phic_c, Pmax);
+      dpR = (R)get_signed_dp(phiO, phi, Pmax);
+    } else {
+      dpL = (R)get_signed_dp(phi, phiO, Pmax);
+      dpR = (R)get_signed_dp(phic_c, phi, Pmax);
+    }
+    R dA = (R)S.fdA[d][f];
+    R dxsum = (R)dxs;
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) {
+      R po = S.prim[q * N + other], gpo = S.gradp[q * N + other];
+      R WL, WR;
+      if (self_is_L) { WL = pc[q] + dpL * gpc[q]; WR = po - dpR * gpo; }
+      else { WL = po + dpL * gpo; WR = pc[q] - dpR * gpc[q]; }
+      R Sl = (WR - WL) / dxsum;
+      sum[q] += Sl * dA;
+      R ps = PLM * Sl;
+      if (Sl > (R)0) {
+        if (!(anypos >> q & 1u) || ps < minpos[q]) minpos[q] = ps;
+        anypos |= 1u << q;
+      } else if (Sl < (R)0) {
+        if (!(anyneg >> q & 1u) || ps > maxneg[q]) maxneg[q] = ps;
+        anyneg |= 1u << q;
+      } else {
+        anyzero |= 1u << q;
+      }
+    }
+  };
+
+  int pb = pair_below(P, dim, j, k);
+  int pa = pair_above(P, dim, j, k);
+  if (pb >= 0) {
+    int base = S.face_off[d][pb], Nf = S.face_off[d][pb + 1] - base;
+    double dxL, dxR;
+    pair_dx(P, S.r_jph, S.z_kph, dim, pb, &dxL, &dxR);
+    double dxs = dxR + dxL;
+    for_run(S.run_dn_s[d][c], S.run_dn_e[d][c], base, Nf,
+            [&](int f) { visit(f, S.fL[d][f], false, dxs); });
+  }
+  if (pa >= 0) {
+    int base = S.face_off[d][pa], Nf = S.face_off[d][pa + 1] - base;
+    double dxL, dxR;
+    pair_dx(P, S.r_jph, S.z_kph, dim, pa, &dxL, &dxR);
+    double dxs = dxR + dxL;
+    for_run(S.run_up_s[d][c], S.run_up_e[d][c], base, Nf,
+            [&](int f) { visit(f, S.fR[d][f], true, dxs); });
+  }
+
+  // total weight, plm.c:113-143
+  const double* rj = S.r_jph + 1;
+  const double* zk = S.z_kph + 1;
+  double phip = S.piph[c], phim = phip - S.dphi[c];
+  double dph = get_dp(phip, phim, Pmax);
+  double dAp, dAm;
+  if (dim == 1) {
+    double dz = zk[k] - zk[k - 1];
+    dAp = (.5 * (rj[j] + rj[j])) * dph * dz;
+    dAm = (.5 * (rj[j - 1] + rj[j - 1])) * dph * dz;
+  } else {
+    double dr = rj[j] - rj[j - 1];
+    double r = .5 * (rj[j] + rj[j - 1]);
+    dAp = r * dr * dph;
+    dAm = r * dr * dph;
+  }
+  double dAtot = dAp + dAm;
+  int idx = dim == 1 ? j : k;
+  int nmax = dim == 1 ? P.Nr : P.Nz;
+  if (idx == 0) dAtot = dAp;
+  if (idx == nmax - 1) dAtot = dAm;
+  R dAt = (R)dAtot;
+
+  bool geom_bd = (dim == 1 && j == 0 && P.NgRa == 0);
+  R rcen = (R)centroid_r(rj[j], rj[j - 1]);
+#pragma unroll
+  for (int q = 0; q < NQ; ++q) {
+    R g = sum[q] / dAt;
+    if (g > (R)0) {
+      if ((anyneg >> q & 1u) || (anyzero >> q & 1u)) g = 0;
+      else if ((anypos >> q & 1u) && minpos[q] < g) g = minpos[q];
+    } else if (g < (R)0) {
+      if ((anypos >> q & 1u) || (anyzero >> q & 1u)) g = 0;
+      else if ((anyneg >> q & 1u) && maxneg[q] > g) g = maxneg[q];
+    }
+    if (geom_bd) {  // plm_geom_boundary + geom_grad, cylindrical.c:141-173
+      if (q == URR || (P.num_c > BZZ && q == BRR)) {
+        R SL = pc[q] / rcen;
+        if (g * SL < (R)0) g = 0;
+        else if (fabs(PLM * SL) < fabs(g)) g = PLM * SL;
+      } else {
+        g = 0;
+      }
+    }
+    grad[q * N + c] = g;
+  }
+}
+
+// ---- phi fluxes, misc.c:378-436 + riemann_phi, riemann.c:39-112 -------------
+template <typename Phys, typename R, int NQ>
+__global__ void k_flux_phi(DevParams P, DevState<R> S, double fac) {
+  int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= S.N) return;
+  int jk = S.cell_ring[c];
+  int j = jk % P.Nr, k = jk / P.Nr;
+  if (!is_real(P, j, k)) return;
+  const int N = S.N;
+  int off = S.ring_off[jk], Np = S.ring_off[jk + 1] - off;
+  int i = c - off;
+  int cp = off + (i < Np - 1 ? i + 1 : 0);
+  const double* rj = S.r_jph + 1;
+  const double* zk = S.z_kph + 1;
+  double rp = rj[j], rm = rj[j - 1], zp = zk[k], zm = zk[k - 1];
+  double r = centroid_r(rp, rm);
+  double phi = S.piph[c];
+  double dA = (rp - rm) * (zp - zm);         // get_dA(.., 0) = dr dz
+  double dAdt = dA * (fac * S.scal[SC_DT]);
+  R primL[NQ], primR[NQ], gp[NQ], gLr[NQ], gLz[NQ], gRr[NQ], gRz[NQ];
+  R dL = (R)S.dphi[c], dR = (R)S.dphi[cp];
+#pragma unroll
+  for (int q = 0; q < NQ; ++q) {
+    R pL = S.prim[q * N + c], pR = S.prim[q * N + cp];
+    primL[q] = pL + (R).5 * S.gradp[q * N + c] * dL;
+    primR[q] = pR - (R).5 * S.gradp[q * N + cp] * dR;
+    gp[q] = (pR - pL) / ((R)0.5 * (dR + dL));
+  }
+  if (P.include_viscosity) {
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) {
+      gLr[q] = S.gradr[q * N + c]; gLz[q] = S.gradz[q * N + c];
+      gRr[q] = S.gradr[q * N + cp]; gRz[q] = S.gradz[q * N + cp];
+    }
+  }
+  if (Phys::MHD) {
+    R Bp = (R).5 * (primL[BPP] + primR[BPP]);
+    primL[BPP] = Bp; primR[BPP] = Bp;
+  }
+  R n[3] = {0, 1, 0};
+  R hn = (R)r;
+  R w = hn * (R)S.wiph[c];
+  R Fw[NQ];
+  solve_riemann<Phys, R, NQ>(P, S.planets, primL, primR, gLr, gp, gLz, gRr, gp, gRz, (R)r,
+                             (R)phi, n, w, Fw, nullptr, nullptr);
+#pragma unroll
+  for (int q = 0; q < NQ; ++q) S.fphi[q * N + c] = (R)((double)Fw[q] * dAdt);
+}
+
+// ---- r/z fluxes, misc.c:441-519 + riemann_trans, riemann.c:114-214 ----------
+// Grid: x = pair within the active range, y = chunk of 256 faces.
+template <typename Phys, typename R, int NQ>
+__global__ void k_flux_trans(DevParams P, DevState<R> S, int dim, int jmin, int jcount, int kmin,
+                             double fac) {
+  const int d = dim - 1;
+  int pj = jmin + (int)blockIdx.x % jcount;
+  int pk = kmin + (int)blockIdx.x / jcount;
+  int pair = dim == 1 ? pj + (P.Nr - 1) * pk : pj + P.Nr * pk;
+  int base = S.face_off[d][pair], Nf = S.face_off[d][pair + 1] - base;
+  int n = blockIdx.y * blockDim.x + threadIdx.x;
+  if (n >= Nf) return;
+  int f = base + n;
+  const int N = S.N;
+  double dxL, dxR;
+  pair_dx(P, S.r_jph, S.z_kph, dim, pair, &dxL, &dxR);
+  int cL = S.fL[d][f], cR = S.fR[d][f];
+  double phi = S.fphic[d][f];
+  double dAdt = S.fdA[d][f] * (fac * S.scal[SC_DT]);
+  const double Pmax = P.phi_max;
+  double phiL = S.piph[cL] - .5 * S.dphi[cL];
+  double phiR = S.piph[cR] - .5 * S.dphi[cR];
+  R dpL = (R)get_signed_dp(phi, phiL, Pmax);
+  R dpR = (R)get_signed_dp(phiR, phi, Pmax);
+  const R* gradL = (dim == 1 ? S.gradr : S.gradz);
+  R primL[NQ], primR[NQ], grad[NQ];
+  R gLp[NQ], gRp[NQ], gLo[NQ], gRo[NQ];
+  R rdxL = (R)dxL, rdxR = (R)dxR;
+#pragma unroll
+  for (int q = 0; q < NQ; ++q) {
+    R pL = S.prim[q * N + cL], pR = S.prim[q * N + cR];
+    R gpL = S.gradp[q * N + cL], gpR = S.gradp[q * N + cR];
+    primL[q] = pL + gradL[q * N + cL] * rdxL + gpL * dpL;
+    primR[q] = pR - gradL[q * N + cR] * rdxR - gpR * dpR;
+    grad[q] = ((pR - gpR * dpR) - (pL + gpL * dpL)) / (rdxL + rdxR);
+    gLp[q] = gpL; gRp[q] = gpR;
+  }
+  if (P.include_viscosity) {
+    const R* go = dim == 1 ? S.gradz : S.gradr;
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) { gLo[q] = go[q * N + cL]; gRo[q] = go[q * N + cR]; }
+  }
+  R n3[3] = {0, 0, 0};
+  if (dim == 1) n3[0] = 1; else n3[2] = 1;
+  if (Phys::MHD) {
+    int BT = dim == 1 ? BRR : BZZ;
+    R Bavg = (R).5 * (primL[BT] + primR[BT]);
+    primL[BT] = Bavg; primR[BT] = Bavg;
+  }
+  // face x = cm: r is the face radius for r faces, the centroid for z faces
+  const double* rj = S.r_jph + 1;
+  int pjL = pair % (dim == 1 ? (P.Nr - 1) : P.Nr);
+  double r = dim == 1 ? .5 * (rj[pjL] + rj[pjL]) : centroid_r(rj[pjL], rj[pjL - 1]);
+  R Fw[NQ];
+  if (dim == 1)
+    solve_riemann<Phys, R, NQ>(P, S.planets, primL, primR, grad, gLp, gLo, grad, gRp, gRo, (R)r,
+                               (R)phi, n3, (R)0.0, Fw, nullptr, nullptr);
+  else
+    solve_riemann<Phys, R, NQ>(P, S.planets, primL, primR, gLo, gLp, grad, gRo, gRp, grad, (R)r,
+                               (R)phi, n3, (R)0.0, Fw, nullptr, nullptr);
+  R* out = S.fflux[d];
+  const int NF = S.nf[d];
+#pragma unroll
+  for (int q = 0; q < NQ; ++q) out[q * NF + f] = (R)((double)Fw[q] * dAdt);
+}
+
+// ---- conserved update + sources + move + cons2prim -----------------------------
+// adjust_RK_cons (misc.c:226), flux scatter (riemann.c:314-317) as a gather in
+// the reference's order, add_source (misc.c:550), move_cells/clean_pi/calc_dp
+// (misc.c:266, :8, :281), calc_prim (misc.c:300).
+template <typename Phys, typename R, int NQ>
+__global__ void k_update(DevParams P, DevState<R> S, double RK, double fac, int first) {
+  int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= S.N) return;
+  const int N = S.N;
+  int jk = S.cell_ring[c];
+  int j = jk % P.Nr, k = jk / P.Nr;
+  int off = S.ring_off[jk], Np = S.ring_off[jk + 1] - off;
+  int i = c - off;
+  const double* rj = S.r_jph + 1;
+  const double* zk = S.z_kph + 1;
+  const double Pmax = P.phi_max;
+  double dt = fac * S.scal[SC_DT];
+  bool real = is_real(P, j, k);
+
+  double piph = S.piph[c], dphi = S.dphi[c];
+  if (real) {
+    double U[NQ];
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) {
+      double u = S.cons[q * N + c];
+      if (first) {
+        S.RKcons[q * N + c] = u;
+      } else {
+        u = (1. - RK) * u + RK * S.RKcons[q * N + c];
+      }
+      U[q] = u;
+    }
+    // phi faces: cell i receives +F_{i-1} then -F_i (for i = 0: -F_0, +F_{Np-1})
+    int cm = off + (i == 0 ? Np - 1 : i - 1);
+    if (i == 0) {
+#pragma unroll
+      for (int q = 0; q < NQ; ++q) { U[q] -= (double)S.fphi[q * N + c]; U[q] += (double)S.fphi[q * N + cm]; }
+    } else {
+#pragma unroll
+      for (int q = 0; q < NQ; ++q) { U[q] += (double)S.fphi[q * N + cm]; U[q] -= (double)S.fphi[q * N + c]; }
+    }
+    // r then z faces: lower pair (cell is R: +=) then upper pair (cell is L: -=)
+#pragma unroll
+    for (int dim = 1; dim <= 2; ++dim) {
+      if (dim == 1 && P.Nr <= 1) continue;
+      if (dim == 2 && P.Nz <= 1) continue;
+      const int d = dim - 1;
+      const R* Fb = S.fflux[d];
+      const int NF = S.nf[d];
+      int pb = pair_below(P, dim, j, k);
+      int pa = pair_above(P, dim, j, k);
+      if (pb >= 0) {
+        int base = S.face_off[d][pb], Nf = S.face_off[d][pb + 1] - base;
+        for_run(S.run_dn_s[d][c], S.run_dn_e[d][c], base, Nf, [&](int f) {
+#pragma unroll
+          for (int q = 0; q < NQ; ++q) U[q] += (double)Fb[q * NF + f];
+        });
+      }
+      if (pa >= 0) {
+        int base = S.face_off[d][pa], Nf = S.face_off[d][pa + 1] - base;
+        for_run(S.run_up_s[d][c], S.run_up_e[d][c], base, Nf, [&](int f) {
+#pragma unroll
+          for (int q = 0; q < NQ; ++q) U[q] -= (double)Fb[q * NF + f];
+        });
+      }
+    }
+    // sources (misc.c:569-590) at the pre-move geometry
+    double xp[3] = {rj[j], piph, zk[k]};
+    double xm[3] = {rj[j - 1], piph - dphi, zk[k - 1]};
+    double dV = (.5 * (xp[0] + xm[0])) * (xp[0] - xm[0]) * get_dp(xp[1], xm[1], Pmax) * (xp[2] - xm[2]);
+    double dVdt = dV * dt;
+    R pr[NQ];
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) pr[q] = S.prim[q * N + c];
+    Phys::source(P, pr, U, xp, xm, dVdt);
+    for (int p = 0; p < P.Npl; ++p)
+      if (S.planets[p].M != 0.0) planet_src<R>(P, S.planets[p], pr, U, xp, xm, dVdt);
+    if (P.include_viscosity) {
+      R gr[NQ], gp[NQ], gz[NQ];
+#pragma unroll
+      for (int q = 0; q < NQ; ++q) {
+        gr[q] = S.gradr[q * N + c]; gp[q] = S.gradp[q * N + c]; gz[q] = S.gradz[q * N + c];
+      }
+      Phys::visc_source(P, S.planets, pr, gr, gp, gz, U, xp, xm, dVdt);
+    }
+    if (P.rot_flag) {  // omega_src, rotframe.c:32-80
+      double r = centroid_r(xp[0], xm[0]);
+      double ph = .5 * (xp[1] + xm[1]);
+      double rho = pr[RHO];
+      double v0 = pr[URR], v1 = (double)pr[UPP] * r, v2 = pr[UZZ];
+      double vr = v0, vom = v1 / r;
+      double Rr = r - P.rot_d * cos(ph), Rp = P.rot_d * sin(ph);
+      double f0 = P.rot_omega * P.rot_omega * Rr + 2. * P.rot_omega * r * vom;
+      double f1 = P.rot_omega * P.rot_omega * Rp - 2. * P.rot_omega * vr;
+      double f2 = 0.0;
+      v1 -= r * (double)get_om<double>(P, r);
+      double vf = v0 * f0 + v1 * f1 + v2 * f2;
+      f1 *= r;
+      U[SRR] += rho * f0 * dVdt;
+      U[LLL] += rho * f1 * dVdt;
+      U[SZZ] += rho * f2 * dVdt;
+      U[TAU] += rho * vf * dVdt;
+    }
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) S.cons[q * N + c] = U[q];
+  }
+
+  // move_cells + clean_pi + calc_dp (first substep only)
+  if (first) {
+    int cm = off + (i == 0 ? Np - 1 : i - 1);
+    double pn = piph + S.wiph[c] * dt;
+    while (pn > Pmax) pn -= Pmax;
+    while (pn < 0.0) pn += Pmax;
+    double pm = S.piph[cm] + S.wiph[cm] * dt;
+    while (pm > Pmax) pm -= Pmax;
+    while (pm < 0.0) pm += Pmax;
+    piph = pn;
+    dphi = get_dp(pn, pm, Pmax);
+    S.piph_out[c] = piph;
+    S.dphi[c] = dphi;
+  }
+
+  if (real) {  // calc_prim at the post-move geometry
+    double rp = rj[j], rm = rj[j - 1], zp = zk[k], zm = zk[k - 1];
+    double phim = piph - dphi;
+    double xp1 = piph;
+    double dV = (.5 * (rp + rm)) * (rp - rm) * get_dp(xp1, phim, Pmax) * (zp - zm);
+    double r = centroid_r(rp, rm);
+    double U[NQ];
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) U[q] = S.cons[q * N + c];
+    R pr[NQ];
+    int hits = Phys::cons2prim(P, S.planets, U, pr, r, .5 * (phim + piph), dV);
+    bool bad = false;
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) {
+      S.prim[q * N + c] = pr[q];
+      if (!isfinite((double)pr[q])) bad = true;
+    }
+    if (bad) atomicAdd(&S.errs->nan_cells, 1ull);
+    if (hits & 1) atomicAdd(&S.errs->rho_floor_hits, 1ull);
+    if (hits & 2) atomicAdd(&S.errs->p_floor_hits, 1ull);
+  }
+}
+
+// ---- ghost rings: boundary_trans of Boundary/fixed.c and Boundary/fixed3d.c ----
+// fixed.c:11-46 evaluates initial() at the arithmetic-mean radius on r ghosts
+// only; fixed3d.c uses set_cell_init (boundary_functions.c:21) on r and z
+// ghosts.  The state after the prim update is position-dependent only.
+template <typename R, int NQ>
+__global__ void k_boundary(DevParams P, DevState<R> S) {
+  int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= S.N) return;
+  int jk = S.cell_ring[c];
+  int j = jk % P.Nr, k = jk / P.Nr;
+  bool rghost = (j < P.NgRa) || (j >= P.Nr - P.NgRb);
+  bool zghost = (k < P.NgZa) || (k >= P.Nz - P.NgZb);
+  const double* rj = S.r_jph + 1;
+  const double* zk = S.z_kph + 1;
+  double x[3];
+  if (P.boundary_id == 0) {          // Boundary/fixed.c
+    if (!rghost || P.Nr <= 1) return;
+    x[0] = .5 * (rj[j] + rj[j - 1]);
+    x[1] = S.piph[c] - .5 * S.dphi[c];
+    x[2] = .5 * (zk[k] + zk[k - 1]);
+  } else if (P.boundary_id == 1) {   // Boundary/fixed3d.c -> set_cell_init
+    if (!((rghost && P.Nr > 1) || (zghost && P.Nz > 1))) return;
+    double xp1 = S.piph[c], xm1 = S.piph[c] - S.dphi[c];
+    x[0] = centroid_r(rj[j], rj[j - 1]);
+    x[1] = .5 * (xp1 + xm1);
+    x[2] = centroid_z(zk[k], zk[k - 1]);
+  } else {
+    return;
+  }
+  double prim[MAX_Q];
+  initial_eval(P, prim, x);
+#pragma unroll
+  for (int q = 0; q < NQ; ++q) S.prim[q * S.N + c] = (R)prim[q];
+}
+
+// ---- getmindt, misc.c:39-84 -------------------------------------------------
+template <typename Phys, typename R, int NQ>
+__global__ void k_mindt(DevParams P, DevState<R> S) {
+  int c = blockIdx.x * blockDim.x + threadIdx.x;
+  double dtc = 1.0e300;
+  if (c < S.N) {
+    int jk = S.cell_ring[c];
+    int j = jk % P.Nr, k = jk / P.Nr;
+    if (is_real(P, j, k)) {
+      int off = S.ring_off[jk], Np = S.ring_off[jk + 1] - off;
+      int i = c - off;
+      const double* rj = S.r_jph + 1;
+      const double* zk = S.z_kph + 1;
+      double phip = S.piph[c], phim = phip - S.dphi[c];
+      double xp[3] = {rj[j], phip, zk[k]};
+      double xm[3] = {rj[j - 1], phim, zk[k - 1]};
+      int im = off + (i == 0 ? Np - 1 : i - 1);
+      double w = .5 * (S.wiph[im] + S.wiph[c]);
+      R pr[NQ];
+#pragma unroll
+      for (int q = 0; q < NQ; ++q) pr[q] = S.prim[q * S.N + c];
+      dtc = Phys::mindt(P, S.planets, pr, w, xp, xm);
+    }
+  }
+  // dt > 0: its IEEE bits order like unsigned integers; NaN sorts above.
+  unsigned long long b = __double_as_longlong(dtc);
+  for (int o = 16; o > 0; o >>= 1) b = min(b, __shfl_xor_sync(0xffffffffu, b, o));
+  __shared__ unsigned long long red[32];
+  int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) red[wid] = b;
+  __syncthreads();
+  if (wid == 0) {
+    b = lane < (int)(blockDim.x >> 5) ? red[lane] : ~0ull;
+    for (int o = 16; o > 0; o >>= 1) b = min(b, __shfl_xor_sync(0xffffffffu, b, o));
+    if (lane == 0) atomicMin((unsigned long long*)&S.scal[SC_MIN], b);
+  }
+}
+
+// dt = CFL * min (misc.c:52-78); clamp to T_End (check_dt, domain.c:433).
+__global__ void k_dt_finalize(DevParams P, double* scal) {
+  double m = __longlong_as_double(*(long long*)&scal[SC_MIN]);
+  double dt0 = P.maxDT / P.CFL;
+  if (dt0 <= 0.0) dt0 = 1.0e100;
+  double dt = dt0 < m ? dt0 : m;
+  dt *= P.CFL;
+  if (P.t_end > 0.0 && scal[SC_T] + dt > P.t_end) dt = P.t_end - scal[SC_T];
+  scal[SC_DT] = dt;
+  *(unsigned long long*)&scal[SC_MIN] = 0x7ff0000000000000ull;   // +inf
+}
+
+// After the first substep: t += dt (timestep.c:136), analytic planet motion
+// (Planets/circular.c:44-46), clean_pi on planets (misc.c:27-34).
+__global__ void k_after_first(DevParams P, double* scal, DevPlanet* pl, int planets_id,
+                              DevErrs* errs) {
+  double dt = scal[SC_DT];
+  scal[SC_T] += dt;
+  if (planets_id == 2 && P.Npl > 1) pl[1].phi += pl[1].omega * dt;
+  for (int p = 0; p < P.Npl; ++p) {
+    double phi = pl[p].phi;
+    while (phi > P.phi_max) phi -= P.phi_max;
+    while (phi < 0.0) phi += P.phi_max;
+    pl[p].phi = phi;
+  }
+  errs->steps += 1;
+}
+
+// ---- set-up: prim2cons + cons2prim for real cells (domain.c:349, :379) ---------
+template <typename Phys, typename R, int NQ>
+__global__ void k_init_cells(DevParams P, DevState<R> S, const double* prim0) {
+  int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= S.N) return;
+  const int N = S.N;
+  int jk = S.cell_ring[c];
+  int j = jk % P.Nr, k = jk / P.Nr;
+  if (!is_real(P, j, k)) {
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) { S.prim[q * N + c] = (R)0; S.cons[q * N + c] = 0; }
+    return;
+  }
+  const double* rj = S.r_jph + 1;
+  const double* zk = S.z_kph + 1;
+  double piph = S.piph[c], dphi = S.dphi[c];
+  double rp = rj[j], rm = rj[j - 1], zp = zk[k], zm = zk[k - 1];
+  double dV = (.5 * (rp + rm)) * (rp - rm) * get_dp(piph, piph - dphi, P.phi_max) * (zp - zm);
+  double r = centroid_r(rp, rm);
+  double pr[NQ], U[NQ];
+#pragma unroll
+  for (int q = 0; q < NQ; ++q) pr[q] = prim0[q * N + c];
+  using Phys64 = typename Phys::template Rebind<double>;
+  Phys64::template prim2cons<double>(P, pr, U, r, dV);
+  R out[NQ];
+  Phys::cons2prim(P, S.planets, U, out, r, piph - .5 * dphi, dV);
+#pragma unroll
+  for (int q = 0; q < NQ; ++q) { S.cons[q * N + c] = U[q]; S.prim[q * N + c] = out[q]; }
+}
+
+}  // namespace disco

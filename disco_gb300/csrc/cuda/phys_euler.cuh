@@ -1,0 +1,243 @@
+// Newtonian hydro hooks of Hydro/euler.c, restated as device functions
+// templated on the arithmetic type R (double for the plain path, float for
+// the mixed path).  Same hook set as hydro.h:6-35: prim2cons, getUstar,
+// cons2prim, flux, source, visc_flux, visc_source, vel, mindt.
+#pragma once
+#include "dev_common.cuh"
+
+namespace disco {
+
+template <typename R, int NQ>
+struct Euler {
+  static constexpr int NC = 5;
+  static constexpr bool MHD = false;
+  template <typename T>
+  using Rebind = Euler<T, NQ>;
+
+  // prim2cons, euler.c:37-63.  x = (r, phi, z); only r enters.
+  template <typename T>
+  DISCO_D static void prim2cons(const DevParams& P, const R* prim, T* cons, R r, R dV) {
+    R rho = prim[RHO], Pp = prim[PPP], vr = prim[URR];
+    R vp = prim[UPP] * r, vz = prim[UZZ];
+    R om = get_om<R>(P, r);
+    R vp_off = vp - om * r;
+    R v2 = vr * vr + vp_off * vp_off + vz * vz;
+    R rhoe = Pp / ((R)P.gamma_law - (R)1.);
+    cons[DDD] = rho * dV;
+    cons[TAU] = ((R).5 * rho * v2 + rhoe) * dV;
+    cons[SRR] = rho * vr * dV;
+    cons[LLL] = r * rho * vp * dV;
+    cons[SZZ] = rho * vz * dV;
+#pragma unroll
+    for (int q = NC; q < NQ; ++q) cons[q] = prim[q] * (R)cons[DDD];
+  }
+
+  // getUstar, euler.c:65-101 (HLLC star state).
+  DISCO_D static void getUstar(const DevParams& P, const R* prim, R* Ustar, R r, R Sk, R Ss,
+                               const R* n, const R* Bpack) {
+    R rho = prim[RHO], vr = prim[URR], vp = prim[UPP] * r, vz = prim[UZZ], Pp = prim[PPP];
+    R om = get_om<R>(P, r);
+    R vp_off = vp - om * r;
+    R v2 = vr * vr + vp_off * vp_off + vz * vz;
+    R vn = vr * n[0] + vp * n[1] + vz * n[2];
+    R vn_off = vn - om * r * n[1];
+    R Ss_off = Ss + vn_off - vn;
+    R rhoe = Pp / ((R)P.gamma_law - (R)1.);
+    R rhostar = rho * (Sk - vn) / (Sk - Ss);
+    R Pstar = Pp * (Ss - vn) / (Sk - Ss);
+    R Us = rhoe * (Sk - vn) / (Sk - Ss);
+    Ustar[DDD] = rhostar;
+    Ustar[SRR] = rhostar * (vr + (Ss - vn) * n[0]);
+    Ustar[LLL] = r * rhostar * (vp + (Ss - vn) * n[1]);
+    Ustar[SZZ] = rhostar * (vz + (Ss - vn) * n[2]);
+    Ustar[TAU] = (R).5 * rhostar * v2 + Us + rhostar * Ss_off * (Ss - vn) + Pstar;
+#pragma unroll
+    for (int q = NC; q < NQ; ++q) Ustar[q] = prim[q] * Ustar[DDD];
+  }
+
+  // cons2prim, euler.c:103-140.  cons in FP64 (conserved accumulation),
+  // prim in R.  Returns a floor-hit bit mask (1 = density, 2 = pressure).
+  DISCO_D static int cons2prim(const DevParams& P, const DevPlanet* pl, const double* cons, R* prim,
+                               double r, double phi, double dV) {
+    int hits = 0;
+    R rho = (R)(cons[DDD] / dV);
+    if (rho < (R)P.rho_floor) { rho = (R)P.rho_floor; hits |= 1; }
+    R Sr = (R)(cons[SRR] / dV);
+    R Sp = (R)(cons[LLL] / dV / r);
+    R Sz = (R)(cons[SZZ] / dV);
+    R E = (R)(cons[TAU] / dV);
+    R rr = (R)r;
+    R om = get_om<R>(P, rr);
+    R vr = Sr / rho;
+    R vp = Sp / rho;
+    R vp_off = vp - om * rr;
+    R vz = Sz / rho;
+    R KE = (R).5 * (Sr * vr + rho * vp_off * vp_off + Sz * vz);
+    R rhoe = E - KE;
+    R Pp = ((R)P.gamma_law - (R)1.) * rhoe;
+    if (Pp < (R)P.p_floor * rho) { Pp = (R)P.p_floor * rho; hits |= 2; }
+    if (P.isothermal) {
+      R cs2 = get_cs2<R>(P, pl, rr, (R)phi);
+      Pp = cs2 * rho / (R)P.gamma_law;
+    }
+    prim[RHO] = rho;
+    prim[PPP] = Pp;
+    prim[URR] = vr;
+    prim[UPP] = vp / rr;
+    prim[UZZ] = vz;
+#pragma unroll
+    for (int q = NC; q < NQ; ++q) prim[q] = (R)(cons[q] / cons[DDD]);
+    return hits;
+  }
+
+  // flux, euler.c:142-170.
+  DISCO_D static void flux(const DevParams& P, const R* prim, R* f, R r, const R* n) {
+    R rho = prim[RHO], Pp = prim[PPP], vr = prim[URR], vp = prim[UPP] * r, vz = prim[UZZ];
+    R om = get_om<R>(P, r);
+    R vn = vr * n[0] + vp * n[1] + vz * n[2];
+    R wn = om * r * n[1];
+    R vp_off = vp - om * r;
+    R rhoe = Pp / ((R)P.gamma_law - (R)1.);
+    R v2 = vr * vr + vp_off * vp_off + vz * vz;
+    f[DDD] = rho * vn;
+    f[SRR] = rho * vr * vn + Pp * n[0];
+    f[LLL] = r * (rho * vp * vn + Pp * n[1]);
+    f[SZZ] = rho * vz * vn + Pp * n[2];
+    f[TAU] = ((R).5 * rho * v2 + rhoe + Pp) * vn - Pp * wn;
+#pragma unroll
+    for (int q = NC; q < NQ; ++q) f[q] = prim[q] * f[DDD];
+  }
+
+  // vel, euler.c:301-326: HLLC wave-speed estimates.
+  DISCO_D static void vel(const DevParams& P, const R* p1, const R* p2, R* Sl, R* Sr, R* Ss,
+                          const R* n, R r, R* Bpack) {
+    R P1 = p1[PPP], rho1 = p1[RHO];
+    R vn1 = p1[URR] * n[0] + p1[UPP] * n[1] * r + p1[UZZ] * n[2];
+    R cs1 = sqrt((R)P.gamma_law * P1 / rho1);
+    R P2 = p2[PPP], rho2 = p2[RHO];
+    R vn2 = p2[URR] * n[0] + p2[UPP] * n[1] * r + p2[UZZ] * n[2];
+    R cs2 = sqrt((R)P.gamma_law * P2 / rho2);
+    *Ss = (P2 - P1 + rho1 * vn1 * (-cs1) - rho2 * vn2 * cs2) / (rho1 * (-cs1) - rho2 * cs2);
+    *Sr = cs1 + vn1;
+    *Sl = -cs1 + vn1;
+    if (*Sr < cs2 + vn2) *Sr = cs2 + vn2;
+    if (*Sl > -cs2 + vn2) *Sl = -cs2 + vn2;
+  }
+
+  // source, euler.c:172-213 (geometric + energy-frame source).
+  DISCO_D static void source(const DevParams& P, const R* prim, double* cons, const double* xp,
+                             const double* xm, double dVdt) {
+    double rp = xp[0], rm = xm[0];
+    R rho = prim[RHO], Pp = prim[PPP];
+    R r = (R)centroid_r(rp, rm);
+    R r_1 = (R)(.5 * (rp + rm));
+    R vr = prim[URR], omega = prim[UPP], vz = prim[UZZ];
+    R centrifugal = rho * omega * omega * r;
+    if (P.polar_sources) {
+      double dp = get_dp(xp[1], xm[1], P.phi_max);
+      centrifugal *= (R)(sin(0.5 * dp) / (0.5 * dp));
+    }
+    R press_bal = Pp / r_1;
+    cons[SRR] += dVdt * (double)(centrifugal + press_bal);
+    R om = get_om<R>(P, r);
+    R om_r = get_om1<R>(P, r);
+    R om_z = 0.0;
+    cons[TAU] += (dVdt * (double)rho) * (double)(r * vr * om * om - r * r * (omega - om) * (vr * om_r + vz * om_z));
+  }
+
+  // nu for viscosity: explicit, or alpha c^2 / get_height_om (euler.c:220-226).
+  DISCO_D static R visc_nu(const DevParams& P, const DevPlanet* pl, const R* prim, R r, R phi) {
+    R nu = (R)P.explicit_viscosity;
+    if (P.alpha_flag) {
+      R alpha = (R)P.explicit_viscosity;
+      R c2 = (R)P.gamma_law * prim[PPP] / prim[RHO];
+      nu = alpha * c2 / get_height_om<R>(P, pl, r, phi);
+    }
+    return nu;
+  }
+
+  // visc_flux, euler.c:215-256.
+  DISCO_D static void visc_flux(const DevParams& P, const DevPlanet* pl, const R* prim,
+                                const R* gradr, const R* gradp, const R* gradz, R* f, R r,
+                                R phi, const R* n) {
+    R nu = visc_nu(P, pl, prim, r, phi);
+    R rho = prim[RHO], vr = prim[URR], om = prim[UPP];
+    R om_off = om - get_om<R>(P, r);
+    R vz = prim[UZZ];
+    R divV_o_d = (gradr[URR] + gradp[UPP] + gradz[UZZ] + vr / r) / (R)3.0;
+    R srr = gradr[URR] - divV_o_d;
+    R spp = r * (r * gradp[UPP] + vr - r * divV_o_d);
+    R szz = gradz[UZZ] - divV_o_d;
+    R srp = (R)0.5 * (r * r * gradr[UPP] + gradp[URR]);
+    R srz = (R)0.5 * (gradr[UZZ] + gradz[URR]);
+    R spz = (R)0.5 * (gradp[UZZ] + r * r * gradz[UPP]);
+    R nc0 = n[0], nc1 = n[1] / r, nc2 = n[2];
+    R srn = srr * nc0 + srp * nc1 + srz * nc2;
+    R spn = srp * nc0 + spp * nc1 + spz * nc2;
+    R szn = srz * nc0 + spz * nc1 + szz * nc2;
+    f[SRR] = (R)-2 * nu * rho * srn;
+    f[LLL] = (R)-2 * nu * rho * spn;
+    f[SZZ] = (R)-2 * nu * rho * szn;
+    f[TAU] = (R)-2 * nu * rho * (vr * srn + om_off * spn + vz * szn);
+  }
+
+  // visc_source, euler.c:258-291.
+  DISCO_D static void visc_source(const DevParams& P, const DevPlanet* pl, const R* prim,
+                                  const R* gradr, const R* gradp, const R* gradz, double* cons,
+                                  const double* xp, const double* xm, double dVdt) {
+    R r = (R)centroid_r(xp[0], xm[0]);
+    R phi = (R)(0.5 * (xp[1] + xm[1]));
+    R nu = visc_nu(P, pl, prim, r, phi);
+    R rho = prim[RHO], vr = prim[URR];
+    R divV_o_d = (gradr[URR] + gradp[UPP] + gradz[UZZ] + vr / r) / (R)3.0;
+    R spp = (r * gradp[UPP] + vr - r * divV_o_d) / (r * r * r);
+    cons[SRR] += (double)(((R)-2 * r * rho * nu * spp) * (R)dVdt);
+    R srp = (R)0.5 * (r * r * gradr[UPP] + gradp[URR]);
+    R spz = (R)0.5 * (gradp[UZZ] + r * r * gradz[UPP]);
+    R om_r = get_om1<R>(P, r);
+    R om_z = 0.0;
+    cons[TAU] += (double)(((R)2 * rho * nu * (srp * om_r + spz * om_z)) * (R)dVdt);
+  }
+
+  // HLLD is rejected for hydro at set-up (riemann.c:19-22); never reached.
+  DISCO_D static void hlld(const DevParams&, R, const R*, const R*, R* F, R* U, R, const R*) {
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) { F[q] = 0; U[q] = 0; }
+  }
+
+  // mindt, euler.c:328-377.
+  DISCO_D static double mindt(const DevParams& P, const DevPlanet* pl, const R* prim, double w,
+                              const double* xp, const double* xm) {
+    double r = centroid_r(xp[0], xm[0]);
+    R Pp = prim[PPP], rho = prim[RHO];
+    R vp = (R)((double)prim[UPP] - w) * (R)r;
+    R vr = prim[URR], vz = prim[UZZ];
+    R cs = sqrt((R)P.gamma_law * Pp / rho);
+    R maxvr = cs + fabs(vr), maxvp = cs + fabs(vp), maxvz = cs + fabs(vz);
+    double dL1 = xp[0] - xm[0];
+    double dL0 = .5 * (xp[0] + xm[0]) * get_dp(xp[1], xm[1], P.phi_max);
+    double dL2 = xp[2] - xm[2];
+    double dtr = dL1 / (double)maxvr;
+    double dtp = dL0 / (double)maxvp;
+    double dtz = dL2 / (double)maxvz;
+    double dt = dtr;
+    if (dt > dtp) dt = dtp;
+    if (dt > dtz) dt = dtz;
+    if (P.include_viscosity) {
+      double dx = dL0;
+      if (dx > dL1) dx = dL1;
+      if (dx > dL2) dx = dL2;
+      R nu = (R)P.explicit_viscosity;
+      if (P.alpha_flag) {
+        R c2 = (R)P.gamma_law * prim[PPP] / prim[RHO];
+        nu = (R)P.explicit_viscosity * c2 /
+             get_height_om<R>(P, pl, (R)r, (R)(0.5 * (xp[1] + xm[1])));
+      }
+      double dt_visc = 0.5 * dx * dx / (double)nu;
+      if (dt > dt_visc) dt = dt_visc;
+    }
+    return dt;
+  }
+};
+
+}  // namespace disco

@@ -1,0 +1,26 @@
+/* Internal declarations shared by the host C set-up and the CUDA driver. */
+#ifndef DISCO_HOST_INTERNAL_H
+#define DISCO_HOST_INTERNAL_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct disco_rand_state {
+   uint32_t r[34];
+   int pos;
+} disco_rand_state;
+
+void disco_rand_seed(disco_rand_state *st, unsigned int seed);
+int disco_rand_next(disco_rand_state *st);
+void disco_set_error(const char *msg);
+
+/* Exposed for tests of the glibc-rand restatement. */
+int disco_rand_sequence(unsigned int seed, int n, int *out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,66 @@
+"""CHECKER INFRASTRUCTURE (oracle): ctypes binding of oracle/port/disco_port.c.
+
+Runs the plain-C restatement of the reference hot path on a domain produced
+by the product's host set-up (itself checked bit-for-bit against the
+reference)."""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from .build_oracle import build_port
+
+_L = None
+_dp = C.POINTER(C.c_double)
+
+
+def _lib():
+    global _L
+    if _L is None:
+        L = C.CDLL(build_port())
+        L.disco_port_create.restype = C.c_void_p
+        L.disco_port_create.argtypes = [C.c_void_p]
+        L.disco_port_run.argtypes = [C.c_void_p, C.c_int]
+        L.disco_port_step.restype = C.c_double
+        L.disco_port_step.argtypes = [C.c_void_p]
+        L.disco_port_state.argtypes = [C.c_void_p, _dp, _dp, _dp, _dp, _dp]
+        L.disco_port_num_real.restype = C.c_long
+        L.disco_port_num_real.argtypes = [C.c_void_p]
+        L.disco_port_free.argtypes = [C.c_void_p]
+        _L = L
+    return _L
+
+
+class PortDomain:
+    def __init__(self, host):
+        """host: disco_gb300.HostDomain"""
+        self.host = host
+        self._d = _lib().disco_port_create(C.cast(host._ptr, C.c_void_p))
+        if not self._d:
+            raise RuntimeError("oracle port: unsupported module combination")
+
+    def run(self, n: int) -> None:
+        _lib().disco_port_run(self._d, int(n))
+
+    def step(self) -> float:
+        return _lib().disco_port_step(self._d)
+
+    @property
+    def num_real(self) -> int:
+        return _lib().disco_port_num_real(self._d)
+
+    def state(self) -> dict:
+        N, nq = self.host.Ncell, self.host.num_q
+        s = {"piph": np.empty(N), "dphi": np.empty(N), "prim": np.empty((nq, N)),
+             "cons": np.empty((nq, N))}
+        t = C.c_double()
+        _lib().disco_port_state(self._d, *(s[k].ctypes.data_as(_dp) for k in ("piph", "dphi", "prim", "cons")),
+                                C.byref(t))
+        s["t"] = t.value
+        return s
+
+    def __del__(self):
+        if getattr(self, "_d", None):
+            _lib().disco_port_free(self._d)
+            self._d = None

@@ -1,0 +1,88 @@
+"""Generate the golden fixtures in tests/golden/ from the reference itself.
+
+The reference sources are compiled (unmodified, read in place) together with
+the harness main by oracle/ref/Makefile into oracle/_ref/<config>/disco_ref;
+each case below runs that binary on a small in.par and stores its output as
+a compressed .npz.  Run from the repository root:
+
+    python tests/golden/make_golden.py [REFERENCE_DIR]
+
+The GPU tests compare the device path against these files, so they can run
+where the reference sources are not available.
+"""
+from __future__ import annotations
+
+import os
+import re
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, HERE)
+from dumpio import read_dump  # noqa: E402
+
+# name -> (config dir, in.par overrides, number of steps)
+CASES = {
+    "cfg1_n24": ("configs/cfg1_vortex", {"Num_R": 24}, 10),
+}
+
+
+def patch_par(text: str, overrides: dict) -> str:
+    for k, v in overrides.items():
+        pat = re.compile(rf"^{re.escape(k)}\b.*$", re.M)
+        line = f"{k}\t{v}"
+        text, n = pat.subn(line, text)
+        if n == 0:
+            text += f"\n{line}\n"
+    return text
+
+
+def build_ref(cfg: str, ref: str) -> str:
+    subprocess.run(["make", "-s", "-f", "oracle/ref/Makefile", f"CFG={cfg}", f"REF={ref}"],
+                   cwd=ROOT, check=True)
+    return os.path.join(ROOT, "oracle", "_ref", os.path.basename(cfg), "disco_ref")
+
+
+def run_case(name: str, ref: str) -> None:
+    cfg, over, nsteps = CASES[name]
+    exe = build_ref(cfg, ref)
+    with open(os.path.join(ROOT, cfg, "in.par")) as f:
+        par = patch_par(f.read(), over)
+    with tempfile.TemporaryDirectory() as td:
+        with open(os.path.join(td, "in.par"), "w") as f:
+            f.write(par)
+        for mode, args in (("init", ["init", "init.bin"]), ("grad", ["grad", "grad.bin"]),
+                           ("run", ["run", str(nsteps), "run.bin"])):
+            subprocess.run([exe, *args], cwd=td, check=True, capture_output=True)
+        ini = read_dump(os.path.join(td, "init.bin"))
+        grd = read_dump(os.path.join(td, "grad.bin"))
+        run = read_dump(os.path.join(td, "run.bin"))
+    out = {"par_text": np.array(par), "nsteps": nsteps,
+           "Np": ini["Np"], "r_jph": ini["r_jph"], "z_kph": ini["z_kph"], "real": ini["real"],
+           "init_piph": ini["piph"], "init_dphi": ini["dphi"], "init_prim": ini["prim"],
+           "init_cons": ini["cons"], "init_wiph": ini["wiph"],
+           "grad_gradp": grd["gradp"], "grad_gradr": grd["gradr"], "grad_gradz": grd["gradz"],
+           "run_piph": run["piph"], "run_dphi": run["dphi"], "run_wiph": run["wiph"],
+           "run_prim": run["prim"], "run_cons": run["cons"], "run_t": run["t"]}
+    for key in ("r", "z"):
+        fc = grd.get(f"faces_{key}")
+        if fc is None:
+            continue
+        out[f"faces_{key}_fIndex"] = fc["fIndex"]
+        out[f"faces_{key}_L"] = fc["L"]
+        out[f"faces_{key}_R"] = fc["R"]
+        out[f"faces_{key}_LRtype"] = fc["LRtype"]
+        out[f"faces_{key}_phic"] = fc["cm"][:, 1]
+        out[f"faces_{key}_dA"] = fc["dA"]
+    np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **out)
+    print(f"wrote {name}.npz")
+
+
+if __name__ == "__main__":
+    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    for n in CASES:
+        run_case(n, ref)

@@ -1,0 +1,90 @@
+"""Host C set-up (grid, ring phases, initial state, in.par reader) against
+the reference's own output -- no GPU needed."""
+import ctypes
+import ctypes.util
+import os
+
+import numpy as np
+import pytest
+
+from helpers import ROOT, load_golden, write_par
+
+
+def _dg():
+    import disco_gb300 as dg
+    return dg
+
+
+def test_grid_and_phases_bit_exact():
+    dg = _dg()
+    g = load_golden("cfg1_n24")
+    p = dg.read_params(write_par(g["par_text"]))
+    m = dg.read_modules(os.path.join(ROOT, "configs/cfg1_vortex/Makefile_opt.in"))
+    h = dg.HostDomain(p, m)
+    assert np.array_equal(h.Np, g["Np"])
+    assert np.array_equal(h.r_jph, g["r_jph"])
+    assert np.array_equal(h.z_kph, g["z_kph"])
+    assert np.array_equal(h.piph, g["init_piph"])
+    assert np.array_equal(h.dphi, g["init_dphi"])
+    real = g["real"].astype(bool)
+    assert np.array_equal(h.real_mask(), real)
+    # initial() prims vs the reference's prims after its prim2cons/cons2prim
+    assert np.max(np.abs(h.prim[:, real] - g["init_prim"][:, real])) < 1e-14
+
+
+def test_rand_restatement_matches_libc():
+    """The restated glibc rand() stream equals the C library's (where the
+    host C library is glibc)."""
+    dg = _dg()
+    libc_path = ctypes.util.find_library("c")
+    libc = ctypes.CDLL(libc_path)
+    try:
+        libc.gnu_get_libc_version
+    except AttributeError:
+        pytest.skip("host C library is not glibc")
+    n = 5000
+    out = (ctypes.c_int * n)()
+    L = dg.lib()
+    L.disco_rand_sequence.argtypes = [ctypes.c_uint, ctypes.c_int, ctypes.POINTER(ctypes.c_int)]
+    L.disco_rand_sequence(314159, n, out)
+    libc.srand(314159)
+    ref = [libc.rand() for _ in range(n)]
+    assert list(out) == ref
+
+
+def test_cell_count_full_vortex_config():
+    """72,398 interior cells for the 2D vortex configuration (Np from the
+    outer-edge radius, gridsetup.c:132-139)."""
+    dg = _dg()
+    p = dg.read_params(os.path.join(ROOT, "configs/cfg1_vortex/in.par"))
+    m = dg.read_modules(os.path.join(ROOT, "configs/cfg1_vortex/Makefile_opt.in"))
+    h = dg.HostDomain(p, m)
+    assert int(h.Np[h.NgRa:h.Nr - h.NgRb].sum()) == 72398
+    assert h.Np[h.NgRa:h.Nr - h.NgRb].min() == 167 and h.Np[h.NgRa:h.Nr - h.NgRb].max() == 965
+
+
+def test_readvar_semantics(tmp_path):
+    """readpar.c:6-42: first matching line wins, value after any of
+    '\\t :=>_', absent keys read as 0 and are counted, x2pi scalings."""
+    dg = _dg()
+    f = tmp_path / "in.par"
+    f.write_text("//comment\nNum_R = 12\nNum_R 99\naspect =>_ 2.5\naspect_x 7\nPhi_Max 1.0\n"
+                 "P_Times_2pi 1\nT_End 3\nT_Times_2pi 1\nR_Min\t0.25 // trailing\n")
+    p = dg.read_params(str(f))
+    assert p.Num_R == 12
+    assert p.aspect == 2.5
+    assert p.phimax == 2.0 * np.pi
+    assert p.t_max == 6.0 * np.pi
+    assert p.rmin == 0.25
+    assert p.Num_Z == 0 and p.read_errors > 50
+
+
+def test_missing_files_and_modules_fail_loudly(tmp_path):
+    dg = _dg()
+    with pytest.raises(dg.DiscoError):
+        dg.read_params(str(tmp_path / "nope.par"))
+    mk = tmp_path / "Makefile_opt.in"
+    mk.write_text("INITIAL = vortex_gauss\nHYDRO = grmhd2\nGEOMETRY = cylindrical\n"
+                  "BOUNDARY = fixed\nPLANETS = none\nNUM_C = 5\nNUM_N = 1\nCT_MODE = 0\n")
+    with pytest.raises(dg.DiscoError, match="HYDRO=grmhd2"):
+        dg.read_modules(str(mk))

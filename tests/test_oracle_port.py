@@ -1,0 +1,59 @@
+"""Pin the CPU oracle (oracle/port, a plain-C restatement of the hot path)
+against the reference: bit-for-bit equal to the golden fixture made by the
+reference binary, and -- where the reference sources are present -- to a
+fresh reference run at another size."""
+import os
+import shutil
+import subprocess
+import tempfile
+
+import numpy as np
+import pytest
+
+from helpers import ROOT, load_golden, write_par
+
+
+def _port_run(par_path, mk, nsteps):
+    import disco_gb300 as dg
+    from oracle.port import PortDomain
+    h = dg.HostDomain(dg.read_params(par_path), dg.read_modules(mk))
+    d = PortDomain(h)
+    d.run(nsteps)
+    return h, d.state()
+
+
+def test_port_bit_exact_vs_golden():
+    g = load_golden("cfg1_n24")
+    h, s = _port_run(write_par(g["par_text"]), os.path.join(ROOT, "configs/cfg1_vortex/Makefile_opt.in"),
+                     int(g["nsteps"]))
+    real = g["real"].astype(bool)
+    assert s["t"] == float(g["run_t"])
+    assert np.array_equal(s["piph"], g["run_piph"])
+    assert np.array_equal(s["dphi"], g["run_dphi"])
+    assert np.array_equal(s["cons"][:, real], g["run_cons"][:, real])
+    assert np.array_equal(s["prim"], g["run_prim"]) or np.array_equal(s["prim"][:, real], g["run_prim"][:, real])
+
+
+REF = "/root/reference"
+
+
+@pytest.mark.skipif(not os.path.isdir(REF), reason="reference sources not present")
+def test_port_bit_exact_vs_reference_binary():
+    sys_path_golden = os.path.join(ROOT, "tests", "golden")
+    import sys
+    sys.path.insert(0, sys_path_golden)
+    from make_golden import build_ref, patch_par
+    from dumpio import read_dump
+    exe = build_ref("configs/cfg1_vortex", REF)
+    par = patch_par(open(os.path.join(ROOT, "configs/cfg1_vortex/in.par")).read(),
+                    {"Num_R": 40, "PLM": 1.2, "Riemann_Solver": 0})
+    td = tempfile.mkdtemp()
+    with open(os.path.join(td, "in.par"), "w") as f:
+        f.write(par)
+    subprocess.run([exe, "run", "7", "out.bin"], cwd=td, check=True, capture_output=True)
+    ref = read_dump(os.path.join(td, "out.bin"))
+    h, s = _port_run(os.path.join(td, "in.par"), os.path.join(ROOT, "configs/cfg1_vortex/Makefile_opt.in"), 7)
+    real = ref["real"].astype(bool)
+    assert np.array_equal(s["piph"], ref["piph"])
+    assert np.array_equal(s["cons"][:, real], ref["cons"][:, real])
+    shutil.rmtree(td)
