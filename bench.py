@@ -1,0 +1,353 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 RK substep cycle: zone-updates/s on one GB300.
+
+A "step" is one full RK2 timestep (timestep.c:7 -> two onestep() substeps)
+of every interior cell, preceded by the CFL reduction (getmindt).  The metric
+is zone-updates/s = interior cells x steps / seconds.  The chosen path is the
+mixed-precision one (FP32 reconstruction, Riemann fluxes and sources; FP64
+positions, face geometry, conserved accumulation, dt); the plain FP64 path is
+measured beside it, with the relative L1 error of the chosen path against it.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+--impl reference times the reference algorithm on the host CPU (the C
+restatement in oracle/, pinned bit-for-bit to the reference build).
+Under torchrun (N>1) every rank advances an independent replica (the domain
+is not decomposed across GPUs); rank 0 prints one JSON line.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOADS = {
+    "vortex2d": {"dir": "configs/cfg1_vortex",
+                 "desc": "2D cylindrical Newtonian hydro, Gaussian isentropic vortex, "
+                         "Nr=128 on r in [0.5,3], HLLC, PLM 1.5, RK2, CFL 0.5"},
+}
+DEFAULT_WORKLOAD = "vortex2d"
+L2_BYTES = 126 * 1024 * 1024
+
+
+def _peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            pk = json.load(f)
+        return float(pk["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle sampling during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.idx = gpu_index
+        self.proc = None
+        self.lines = []
+        self.t = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.idx}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def wait_first(self, timeout=3.0):
+        t0 = time.time()
+        while self.proc is not None and not self.lines and time.time() - t0 < timeout:
+            time.sleep(0.02)
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def kernel_bytes(name: str, N: int, nf: dict, nq: int, sw: int) -> float:
+    """Algorithmic (compulsory) HBM bytes of one launch of each kernel: every
+    input and output array element moved once.  N = cells incl. ghosts,
+    nf[d] = faces of dimension d, sw = bytes of a reconstruction-type value."""
+    idx = 4
+    f8 = 8
+    if name == "plm_phi":
+        return N * (2 * nq * sw + f8)
+    if name.startswith("plm_trans"):
+        d = "r" if name.endswith("_r") else "z"
+        return N * (3 * nq * sw + 2 * f8 + 4 * idx) + nf[d] * (2 * f8 + 2 * idx)
+    if name == "flux_phi":
+        return N * (3 * nq * sw + 3 * f8)
+    if name.startswith("flux_"):
+        d = name[-1]
+        return N * (3 * nq * sw + 2 * f8) + nf[d] * (2 * f8 + 2 * idx + nq * sw)
+    if name == "update":
+        fb = sum(nf[d] * nq * sw for d in nf)
+        return N * (4 * nq * f8 + 2 * nq * sw + 5 * f8 + 8 * idx) + fb
+    if name == "faces_r" or name == "faces_z":
+        d = name[-1]
+        return N * 2 * f8 + nf[d] * (2 * idx + 1 + 2 * f8) + N * 4 * idx
+    if name == "mindt":
+        return N * (nq * sw + 3 * f8)
+    return 0.0
+
+
+def measure_ours(args, wl, rank):
+    import torch
+    import disco_gb300 as dg
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    cfg = os.path.join(ROOT, wl["dir"])
+    par, mk = os.path.join(cfg, "in.par"), os.path.join(cfg, "Makefile_opt.in")
+    res = {}
+    doms = {}
+    for prec in (1, 0):
+        d = dg.Domain(par, mk, precision=prec)
+        doms[prec] = d
+        cells = d.num_real_cells
+        N = d.num_cells
+        nq = d.host.num_q
+        sw = 4 if prec else 8
+        state_bytes = N * nq * (4 * 8 + 4 * sw)
+        flush = 2 * L2_BYTES if state_bytes < 4 * L2_BYTES else 0
+        d.run(args.warmup)
+        torch.cuda.synchronize()
+        clk = ClockSampler(dev) if prec == 1 else None
+        if clk:
+            clk.start()
+            clk.wait_first()
+        l0 = dg.lib().disco_gpu_launch_count()
+        ms = d.run_timed(args.steps, flush_bytes=flush)
+        launches = dg.lib().disco_gpu_launch_count() - l0
+        if clk:
+            time.sleep(0.25)
+        clocks = clk.stop() if clk else None
+        res[prec] = {"ms": ms, "cells": cells, "N": N, "nq": nq, "sw": sw, "flush": flush,
+                     "launches": launches, "clocks": clocks,
+                     "value": cells * args.steps / (ms / 1e3)}
+    # accuracy of the chosen path against plain FP64 after the same steps
+    s1, s0 = doms[1].state(), doms[0].state()
+    real = doms[0].host.real_mask()
+    err = 0.0
+    for q in range(s0["cons"].shape[0]):
+        den = np.abs(s0["cons"][q, real]).sum()
+        if den > 0:
+            err = max(err, float(np.abs(s1["cons"][q, real] - s0["cons"][q, real]).sum() / den))
+    res["l1_err"] = err
+    # per-kernel breakdown of the chosen path (events around each launch)
+    prof = doms[1].profile(3)
+    res["profile"] = prof
+    # e2e through the C ABI with host buffers: upload from pinned host memory,
+    # K x (getmindt -> dt to host, timestep(dt) -> dt to device), download.
+    d = doms[1]
+    st = d.state()
+    pin = {k: torch.empty(st[k].shape, dtype=torch.float64, pin_memory=True).numpy()
+           for k in ("piph", "dphi", "wiph", "prim", "cons")}
+    for k in pin:
+        pin[k][...] = st[k]
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    d.upload(**pin)
+    for _ in range(args.steps):
+        d.timestep(d.getmindt())
+    out = d.state()
+    t1 = time.perf_counter()
+    up = sum(pin[k].nbytes for k in pin)
+    down = sum(out[k].nbytes for k in ("piph", "dphi", "wiph", "prim", "cons"))
+    res["e2e"] = {"value": res[1]["cells"] * args.steps / (t1 - t0), "unit": "zone-updates/s",
+                  "h2d_bytes_per_step": int(up / args.steps + 8),
+                  "d2h_bytes_per_step": int(down / args.steps + 8),
+                  "timed": "upload of the full state, K x (getmindt, timestep), download"}
+    for dd in doms.values():
+        dd.close()
+    return res
+
+
+def cpu_baseline(wl, target_s=12.0):
+    """The oracle (plain-C restatement, bit-exact with the reference build),
+    single thread on the host, on the full workload domain for a bounded
+    number of steps."""
+    import disco_gb300 as dg
+    from oracle.port import PortDomain
+    cfg = os.path.join(ROOT, wl["dir"])
+    h = dg.HostDomain(dg.read_params(os.path.join(cfg, "in.par")),
+                      dg.read_modules(os.path.join(cfg, "Makefile_opt.in")))
+    o = PortDomain(h)
+    cells = o.num_real
+    t0 = time.perf_counter()
+    o.step()
+    one = time.perf_counter() - t0
+    n = max(1, int(target_s / max(one, 1e-6)))
+    t0 = time.perf_counter()
+    o.run(n)
+    dt = time.perf_counter() - t0
+    return {"value": cells * n / dt, "unit": "zone-updates/s", "cores": 1, "kind": "port",
+            "sample": f"{n} RK2 steps of the full {cells}-cell domain, 1 thread"}
+
+
+def run_reference(args, wl, rank, world):
+    if rank != 0:
+        return
+    import disco_gb300 as dg
+    from oracle.port import PortDomain
+    cfg = os.path.join(ROOT, wl["dir"])
+    h = dg.HostDomain(dg.read_params(os.path.join(cfg, "in.par")),
+                      dg.read_modules(os.path.join(cfg, "Makefile_opt.in")))
+    o = PortDomain(h)
+    cells = o.num_real
+    o.run(args.warmup)
+    t0 = time.perf_counter()
+    o.run(args.steps)
+    sec = time.perf_counter() - t0
+    v = cells * args.steps / sec
+    line = {"metric": "zone-updates/s", "value": v, "unit": "zone-updates/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": sec * 1e3 / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "impl": "reference",
+            "config": {"workload": wl["desc"], "cells": cells},
+            "cpu_baseline": {"value": v, "unit": "zone-updates/s", "cores": 1, "kind": "port",
+                             "sample": f"{args.steps} RK2 steps of the full {cells}-cell domain "
+                                       "(C restatement pinned bit-for-bit to the reference build; "
+                                       "the reference sources are not on this host)"},
+            "e2e": {"value": v, "unit": "zone-updates/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default=DEFAULT_WORKLOAD, choices=list(WORKLOADS))
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    wl = WORKLOADS[args.workload]
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+
+    if args.impl == "reference":
+        run_reference(args, wl, rank, world)
+        return
+
+    import torch
+    import __graft_entry__
+    __graft_entry__.build()
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        dist.init_process_group("nccl")
+        pg = dist
+        dist.barrier()
+    res = measure_ours(args, wl, rank)
+    ms = res[1]["ms"]
+    if pg is not None:
+        t = torch.tensor([ms], device="cuda", dtype=torch.float64)
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        ms = float(t.item())
+        pg.barrier()
+    if rank != 0:
+        if pg is not None:
+            pg.destroy_process_group()
+        return
+    cells = res[1]["cells"]
+    value = world * cells * args.steps / (ms / 1e3)
+    hbm, peak_kind = _peaks()
+    # dominant kernel of the chosen path, from the per-launch CUDA-event profile
+    N, nq, sw = res[1]["N"], res[1]["nq"], res[1]["sw"]
+    import disco_gb300 as dg  # noqa: F401
+    from disco_gb300.api import Domain  # noqa: F401
+    nf = {"r": 0, "z": 0}
+    hd = dg.HostDomain(dg.read_params(os.path.join(ROOT, wl["dir"], "in.par")),
+                       dg.read_modules(os.path.join(ROOT, wl["dir"], "Makefile_opt.in")))
+    Np = hd.Np.reshape(hd.Nz, hd.Nr)
+    if hd.Nr > 1:
+        nf["r"] = int((Np[:, :-1] + Np[:, 1:]).sum())
+    if hd.Nz > 1:
+        nf["z"] = int((Np[:-1, :] + Np[1:, :]).sum())
+    prof = sorted(res["profile"], key=lambda x: -x[2])
+    tot_prof = sum(p[2] for p in prof)
+    top = prof[0]
+    top_bytes = kernel_bytes(top[0], N, nf, nq, sw)
+    top_avg_s = top[2] / top[1] / 1e3
+    achieved = top_bytes / top_avg_s / 1e9
+    roof = {"bound": "hbm", "kernel": top[0], "achieved": achieved, "peak": hbm, "unit": "GB/s",
+            "frac": achieved / hbm, "peak_kind": peak_kind, "traffic": None,
+            "algorithmic_bytes_per_launch": top_bytes,
+            "share_of_step": top[2] / tot_prof}
+    bz = nq * (4 * sw + 6 * 8) + 6 * 8   # fused-RK2 compulsory bytes per zone-update
+    whole = {"algorithmic_bytes_per_zone_update": bz, "achieved_GBps": bz * value / 1e9,
+             "frac_of_hbm": bz * value / 1e9 / hbm}
+    line = {
+        "metric": "zone-updates/s", "value": value, "unit": "zone-updates/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 reconstruction/fluxes, f64 positions/accumulation",
+        "data": "synthetic",
+        "config": {"workload": wl["desc"], "cells": cells, "precision": "mixed",
+                   "l2": "flushed between steps" if res[1]["flush"] else "inputs larger than L2",
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "fp64": {"value": world * res[0]["cells"] * args.steps / (res[0]["ms"] / 1e3),
+                 "ms_per_step": res[0]["ms"] / args.steps},
+        "l1_err_vs_fp64": res["l1_err"],
+        "roofline": roof,
+        "step_hbm": whole,
+        "kernels_ms_per_step": {p[0]: p[2] / 3 for p in prof},
+        "e2e": res["e2e"],
+        "gpu_launches": int(res[1]["launches"]),
+        "clocks": res[1]["clocks"],
+    }
+    if world == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(wl)
+    print(json.dumps(line), flush=True)
+    if pg is not None:
+        pg.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

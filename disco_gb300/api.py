@@ -95,6 +95,10 @@ class DiscoStateView(C.Structure):
                 ("t", C.c_double)]
 
 
+class DiscoKernelTime(C.Structure):
+    _fields_ = [("name", C.c_char * 48), ("launches", C.c_longlong), ("ms", C.c_double)]
+
+
 class DiscoGpuErrs(C.Structure):
     _fields_ = [("nan_cells", C.c_longlong), ("rho_floor_hits", C.c_longlong),
                 ("p_floor_hits", C.c_longlong), ("face_errors", C.c_longlong),
@@ -116,6 +120,9 @@ SIGNATURES = {
     "disco_gpu_download": (C.c_int, [_P, C.POINTER(DiscoStateView)]),
     "disco_gpu_upload": (C.c_int, [_P, C.POINTER(DiscoStateView)]),
     "disco_gpu_status": (C.c_int, [_P, C.POINTER(DiscoGpuErrs)]),
+    "disco_gpu_run_timed": (C.c_int, [_P, C.c_int, C.c_double, C.c_size_t, C.POINTER(C.c_double)]),
+    "disco_gpu_profile": (C.c_int, [_P, C.c_int, C.POINTER(DiscoKernelTime), C.c_int,
+                                    C.POINTER(C.c_int)]),
     "disco_gpu_time": (C.c_double, [_P]),
     "disco_gpu_num_cells": (C.c_long, [_P]),
     "disco_gpu_num_real_cells": (C.c_long, [_P]),
@@ -228,6 +235,20 @@ class Domain:
 
     def run(self, nsteps: int, t_end: float = 0.0) -> None:
         _check(lib().disco_gpu_run(self._g, int(nsteps), float(t_end)), "disco_gpu_run")
+
+    def run_timed(self, nsteps: int, t_end: float = 0.0, flush_bytes: int = 0) -> float:
+        """Run n steps; returns summed device milliseconds (CUDA events)."""
+        ms = C.c_double()
+        _check(lib().disco_gpu_run_timed(self._g, int(nsteps), float(t_end), int(flush_bytes),
+                                         C.byref(ms)), "disco_gpu_run_timed")
+        return ms.value
+
+    def profile(self, nsteps: int) -> list:
+        """Per-kernel (name, launches, ms) over n steps launched without graphs."""
+        out = (DiscoKernelTime * 64)()
+        n = C.c_int()
+        _check(lib().disco_gpu_profile(self._g, int(nsteps), out, 64, C.byref(n)), "disco_gpu_profile")
+        return [(out[i].name.decode(), out[i].launches, out[i].ms) for i in range(n.value)]
 
     @property
     def t(self) -> float:

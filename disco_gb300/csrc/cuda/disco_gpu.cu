@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <atomic>
+#include <string>
 #include <cstdio>
 #include <cstring>
 #include <vector>
@@ -40,6 +41,8 @@ struct InstanceBase {
   virtual int download(disco_state_view* v) = 0;
   virtual int upload(const disco_state_view* v) = 0;
   virtual int status(disco_gpu_errs* e) = 0;
+  virtual int run_timed(int n, double t_end, size_t flush_bytes, double* ms) = 0;
+  virtual int profile(int n, disco_kernel_time* out, int maxo, int* nout) = 0;
   virtual double time() = 0;
   long N = 0, Nreal = 0;
 };
@@ -56,8 +59,39 @@ static int dalloc(T** p, size_t n, std::vector<void*>& keep) {
   return 0;
 }
 
+struct KTimer {
+  bool on = false;
+  cudaStream_t st = nullptr;
+  struct Rec { const char* name; cudaEvent_t a, b; };
+  std::vector<Rec> recs;
+  cudaEvent_t cur_a = nullptr;
+  void begin() {
+    if (!on) return;
+    cudaEventCreate(&cur_a);
+    cudaEventRecord(cur_a, st);
+  }
+  void end(const char* name) {
+    if (!on) return;
+    cudaEvent_t b;
+    cudaEventCreate(&b);
+    cudaEventRecord(b, st);
+    recs.push_back({name, cur_a, b});
+  }
+};
+
+#define LAUNCH(NAME, ...)            \
+  do {                               \
+    kt.begin();                      \
+    __VA_ARGS__;                     \
+    kt.end(NAME);                    \
+    ++g_launches;                    \
+  } while (0)
+
 template <class Phys, typename R, int NQ>
 struct Instance : InstanceBase {
+  KTimer kt;
+  void* flush_buf = nullptr;
+  size_t flush_size = 0;
   DevParams P{};
   DevState<R> S{};
   std::vector<void*> keep;
@@ -72,6 +106,7 @@ struct Instance : InstanceBase {
   double host_t = 0;
 
   ~Instance() override {
+    if (flush_buf) cudaFree(flush_buf);
     for (int i = 0; i < 2; ++i)
       if (graph[i]) cudaGraphExecDestroy(graph[i]);
     if (st) cudaStreamDestroy(st);
@@ -228,39 +263,32 @@ struct Instance : InstanceBase {
 
   // ---- launch helpers -----------------------------------------------------
   void launch_wcell() {
-    k_wcell<R, NQ><<<blocks(N), 256, 0, st>>>(P, S);
-    ++g_launches;
-    if (P.mesh_motion == 3) { k_wcell_avg<R><<<nring, 256, 0, st>>>(P, S); ++g_launches; }
+    LAUNCH("wcell", (k_wcell<R, NQ><<<blocks(N), 256, 0, st>>>(P, S)));
+    if (P.mesh_motion == 3) LAUNCH("wcell_avg", (k_wcell_avg<R><<<nring, 256, 0, st>>>(P, S)));
   }
   void launch_boundary() {
-    k_boundary<R, NQ><<<blocks(N), 256, 0, st>>>(P, S);
-    ++g_launches;
+    LAUNCH("boundary", (k_boundary<R, NQ><<<blocks(N), 256, 0, st>>>(P, S)));
   }
   void launch_faces() {
     if (npair[0] == 0 && npair[1] == 0) return;
-    k_anchor<R><<<blocks((long)nring * 32), 256, 0, st>>>(P, S, nring);
-    ++g_launches;
+    LAUNCH("anchor", (k_anchor<R><<<blocks((long)nring * 32), 256, 0, st>>>(P, S, nring)));
     for (int d = 0; d < 2; ++d) {
       if (!npair[d]) continue;
       size_t sm = (size_t)maxNf[d] * 9 + 64;
-      k_faces<R><<<npair[d], 256, sm, st>>>(P, S, d + 1);
-      ++g_launches;
+      LAUNCH(d == 0 ? "faces_r" : "faces_z", (k_faces<R><<<npair[d], 256, sm, st>>>(P, S, d + 1)));
     }
   }
   void launch_mindt() {
-    k_mindt<Phys, R, NQ><<<blocks(N), 256, 0, st>>>(P, S);
-    k_dt_finalize<<<1, 1, 0, st>>>(P, S.scal);
-    g_launches += 2;
+    LAUNCH("mindt", (k_mindt<Phys, R, NQ><<<blocks(N), 256, 0, st>>>(P, S)));
+    LAUNCH("dt_finalize", (k_dt_finalize<<<1, 1, 0, st>>>(P, S.scal)));
   }
   // one onestep (onestep.c:86-186)
   void substep(double RK, double fac, int first) {
     if (first) launch_wcell();
-    k_plm_phi<R, NQ><<<blocks(N), 256, 0, st>>>(P, S);
-    ++g_launches;
-    if (Nr > 1) { k_plm_trans<R, NQ><<<blocks(N), 256, 0, st>>>(P, S, 1); ++g_launches; }
-    if (Nz > 1) { k_plm_trans<R, NQ><<<blocks(N), 256, 0, st>>>(P, S, 2); ++g_launches; }
-    k_flux_phi<Phys, R, NQ><<<blocks(N), 256, 0, st>>>(P, S, fac);
-    ++g_launches;
+    LAUNCH("plm_phi", (k_plm_phi<R, NQ><<<blocks(N), 256, 0, st>>>(P, S)));
+    if (Nr > 1) LAUNCH("plm_trans_r", (k_plm_trans<R, NQ><<<blocks(N), 256, 0, st>>>(P, S, 1)));
+    if (Nz > 1) LAUNCH("plm_trans_z", (k_plm_trans<R, NQ><<<blocks(N), 256, 0, st>>>(P, S, 2)));
+    LAUNCH("flux_phi", (k_flux_phi<Phys, R, NQ><<<blocks(N), 256, 0, st>>>(P, S, fac)));
     for (int d = 0; d < 2; ++d) {
       if (!npair[d]) continue;
       int dim = d + 1;
@@ -277,16 +305,14 @@ struct Instance : InstanceBase {
       int jc = jmax - jmin, kc = kmax - kmin;
       if (jc <= 0 || kc <= 0) continue;
       dim3 grid(jc * kc, (maxNf[d] + 255) / 256);
-      k_flux_trans<Phys, R, NQ><<<grid, 256, 0, st>>>(P, S, dim, jmin, jc, kmin, fac);
-      ++g_launches;
+      LAUNCH(dim == 1 ? "flux_r" : "flux_z",
+             (k_flux_trans<Phys, R, NQ><<<grid, 256, 0, st>>>(P, S, dim, jmin, jc, kmin, fac)));
     }
-    k_update<Phys, R, NQ><<<blocks(N), 256, 0, st>>>(P, S, RK, fac, first);
-    ++g_launches;
+    LAUNCH("update", (k_update<Phys, R, NQ><<<blocks(N), 256, 0, st>>>(P, S, RK, fac, first)));
     if (first) {
       parity ^= 1;
       set_piph(parity);
-      k_after_first<<<1, 1, 0, st>>>(P, S.scal, S.planets, planets_id, S.errs);
-      ++g_launches;
+      LAUNCH("after_first", (k_after_first<<<1, 1, 0, st>>>(P, S.scal, S.planets, planets_id, S.errs)));
     }
     launch_boundary();
     if (first) launch_faces();
@@ -350,6 +376,82 @@ struct Instance : InstanceBase {
     P.t_end = 0.0;
     CK(cudaStreamSynchronize(st));
     CK(cudaGetLastError());
+    double sc[SC_COUNT];
+    CK(cudaMemcpy(sc, S.scal, sizeof sc, cudaMemcpyDeviceToHost));
+    host_t = sc[SC_T];
+    return 0;
+  }
+  int run_timed(int n, double t_end, size_t flush_bytes, double* ms) override {
+    if (graph_t_end != t_end) {
+      for (int i = 0; i < 2; ++i) if (graph[i]) { cudaGraphExecDestroy(graph[i]); graph[i] = nullptr; }
+      graph_t_end = t_end;
+    }
+    for (int i = 0; i < 2; ++i)
+      if (!graph[i]) { int rc = build_graph(i, t_end); if (rc) return rc; }
+    if (flush_bytes > flush_size) {
+      if (flush_buf) cudaFree(flush_buf);
+      flush_buf = nullptr; flush_size = 0;
+      CK(cudaMalloc(&flush_buf, flush_bytes));
+      flush_size = flush_bytes;
+    }
+    std::vector<cudaEvent_t> ev(2 * (size_t)n);
+    for (auto& e : ev) CK(cudaEventCreate(&e));
+    for (int s = 0; s < n; ++s) {
+      if (flush_bytes) CK(cudaMemsetAsync(flush_buf, s & 0xff, flush_bytes, st));
+      CK(cudaEventRecord(ev[2 * s], st));
+      CK(cudaGraphLaunch(graph[parity], st));
+      CK(cudaEventRecord(ev[2 * s + 1], st));
+      g_launches += graph_nodes;
+      parity ^= 1;
+    }
+    set_piph(parity);
+    CK(cudaStreamSynchronize(st));
+    double tot = 0;
+    for (int s = 0; s < n; ++s) {
+      float t;
+      CK(cudaEventElapsedTime(&t, ev[2 * s], ev[2 * s + 1]));
+      tot += t;
+    }
+    for (auto& e : ev) cudaEventDestroy(e);
+    *ms = tot;
+    double sc[SC_COUNT];
+    CK(cudaMemcpy(sc, S.scal, sizeof sc, cudaMemcpyDeviceToHost));
+    host_t = sc[SC_T];
+    return 0;
+  }
+  int profile(int n, disco_kernel_time* out, int maxo, int* nout) override {
+    kt.on = true;
+    kt.st = st;
+    kt.recs.clear();
+    for (int s = 0; s < n; ++s) {
+      P.t_end = 0.0;
+      launch_mindt();
+      step_kernels();
+    }
+    kt.on = false;
+    CK(cudaStreamSynchronize(st));
+    std::vector<std::string> names;
+    std::vector<long long> cnt;
+    std::vector<double> ms;
+    for (auto& r : kt.recs) {
+      float t = 0;
+      cudaEventElapsedTime(&t, r.a, r.b);
+      cudaEventDestroy(r.a);
+      cudaEventDestroy(r.b);
+      size_t i = 0;
+      for (; i < names.size(); ++i) if (names[i] == r.name) break;
+      if (i == names.size()) { names.push_back(r.name); cnt.push_back(0); ms.push_back(0); }
+      cnt[i] += 1;
+      ms[i] += t;
+    }
+    kt.recs.clear();
+    int k = 0;
+    for (size_t i = 0; i < names.size() && k < maxo; ++i, ++k) {
+      snprintf(out[k].name, sizeof out[k].name, "%s", names[i].c_str());
+      out[k].launches = cnt[i];
+      out[k].ms = ms[i];
+    }
+    *nout = k;
     double sc[SC_COUNT];
     CK(cudaMemcpy(sc, S.scal, sizeof sc, cudaMemcpyDeviceToHost));
     host_t = sc[SC_T];
@@ -464,6 +566,14 @@ int disco_gpu_download(disco_gpu* g, disco_state_view* v) {
 int disco_gpu_upload(disco_gpu* g, const disco_state_view* v) {
   if (!g || !v) { disco_set_error("null argument"); return DISCO_E_ARG; }
   return g->impl->upload(v);
+}
+int disco_gpu_run_timed(disco_gpu* g, int nsteps, double t_end, size_t flush_bytes, double* ms) {
+  if (!g || nsteps < 0 || !ms) { disco_set_error("bad argument"); return DISCO_E_ARG; }
+  return g->impl->run_timed(nsteps, t_end, flush_bytes, ms);
+}
+int disco_gpu_profile(disco_gpu* g, int nsteps, disco_kernel_time* out, int max_out, int* n_out) {
+  if (!g || !out || !n_out || nsteps < 0) { disco_set_error("bad argument"); return DISCO_E_ARG; }
+  return g->impl->profile(nsteps, out, max_out, n_out);
 }
 int disco_gpu_status(disco_gpu* g, disco_gpu_errs* e) {
   if (!g || !e) { disco_set_error("null argument"); return DISCO_E_ARG; }

@@ -192,6 +192,25 @@ int disco_gpu_download(disco_gpu *g, disco_state_view *v);
  * NULL to keep the device copy); used to resume from a checkpoint. */
 int disco_gpu_upload(disco_gpu *g, const disco_state_view *v);
 
+/* Timed variant of disco_gpu_run for benchmarking: each of the n steps is
+ * one CUDA-graph launch bracketed by CUDA events on the library's stream;
+ * if flush_bytes > 0 a scratch buffer of that size is overwritten before
+ * each step, outside the timed interval, to evict L2.  *ms_total receives
+ * the summed device time of the steps. */
+int disco_gpu_run_timed(disco_gpu *g, int nsteps, double t_end,
+                        size_t flush_bytes, double *ms_total);
+
+/* Per-kernel device time: runs n steps without graphs, each kernel launch
+ * bracketed by CUDA events, and reports per kernel name the launch count
+ * and summed milliseconds (at most max_out entries). */
+typedef struct disco_kernel_time {
+   char name[48];
+   long long launches;
+   double ms;
+} disco_kernel_time;
+int disco_gpu_profile(disco_gpu *g, int nsteps, disco_kernel_time *out,
+                      int max_out, int *n_out);
+
 int disco_gpu_status(disco_gpu *g, disco_gpu_errs *errs);
 double disco_gpu_time(disco_gpu *g);
 long disco_gpu_num_cells(disco_gpu *g);       /* total incl. ghosts */
