@@ -15,7 +15,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
 PORT_SRC = os.path.join(HERE, "port", "disco_port.c")
 PORT_LIB = os.path.join(HERE, "_build", "libdisco_port.so")
-REF_CONFIGS = ["configs/cfg1_vortex"]
+REF_CONFIGS = ["configs/cfg1_vortex", "configs/cfg2_mhd_disk"]
 
 
 def build_port(force: bool = False) -> str:

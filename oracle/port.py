@@ -28,6 +28,7 @@ def _lib():
         L.disco_port_num_real.restype = C.c_long
         L.disco_port_num_real.argtypes = [C.c_void_p]
         L.disco_port_free.argtypes = [C.c_void_p]
+        L.disco_port_phi.argtypes = [C.c_void_p, _dp]
         _L = L
     return _L
 
@@ -58,6 +59,9 @@ class PortDomain:
         _lib().disco_port_state(self._d, *(s[k].ctypes.data_as(_dp) for k in ("piph", "dphi", "prim", "cons")),
                                 C.byref(t))
         s["t"] = t.value
+        if self.host.num_q == 9:
+            s["Phi"] = np.empty((5, N))
+            _lib().disco_port_phi(self._d, s["Phi"].ctypes.data_as(_dp))
         return s
 
     def __del__(self):

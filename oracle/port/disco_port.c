@@ -2,17 +2,18 @@
  * CHECKER INFRASTRUCTURE (oracle) -- not product code.
  *
  * Plain-C restatement of the reference's RK substep cycle (timestep.c:7 ->
- * onestep.c:86) for the Newtonian hydro module (Hydro/euler.c), run serially
- * on the CPU over the same ring layout.  It follows the reference loop by
- * loop -- sequential face walk (faces_alt.c:36-179), scatter updates in face
- * order (riemann.c:314-317), limiter (plm.c:146-179) -- so that compiled
- * with gcc it reproduces the reference's numbers.  It is pinned against the
- * reference binary (oracle/ref) by tests/test_oracle_port.py, and used
- *   - as the checker of the GPU path at sizes beyond the golden fixtures,
- *   - as the timed CPU baseline ("port") in bench.py.
+ * onestep.c:86) for the Newtonian hydro (Hydro/euler.c) and MHD
+ * (Hydro/mhd.c + hlld.c + bfields.c constrained transport) modules, run
+ * serially on the CPU.  It keeps the reference's per-cell records, face
+ * records with cell pointers, loop orders and scatter updates, so compiled
+ * with gcc (no FMA contraction) it reproduces the reference's numbers
+ * bit-for-bit; tests/test_oracle_port.py pins that against the reference
+ * binary built from the reference's own sources (oracle/ref).
  *
- * Input: the host-set-up domain (grid, ring phases, initial primitives) of
- * include/disco_gpu.h, which tests check bit-for-bit against the reference.
+ * Used as the checker of the GPU path at sizes beyond the golden fixtures
+ * and as the timed CPU baseline ("port") in bench.py.  Input: the host-set-up
+ * domain of include/disco_gpu.h (grid, ring phases, initial primitives),
+ * itself checked bit-for-bit against the reference.
  */
 #include <math.h>
 #include <stdio.h>
@@ -23,51 +24,59 @@
 #include "../../disco_gb300/csrc/plugins/ic_vortex_gauss.h"
 #include "../../disco_gb300/csrc/plugins/ic_disks.h"
 
-enum { RHO, PPP, URR, UPP, UZZ };
+enum { RHO, PPP, URR, UPP, UZZ, BRR, BPP, BZZ };
 enum { DDD, TAU, SRR, LLL, SZZ };
 #define MAXQ 9
+#define TOL_HLLD 1e-10
 
-typedef struct {
-   int L, R;            /* global cell ids */
-   double dxL, dxR, cm[3], dphi, dA;
-   int LRtype;
+typedef struct pcell {
+   double prim[MAXQ], cons[MAXQ], RKcons[MAXQ];
+   double gradr[MAXQ], gradp[MAXQ], gradz[MAXQ];
+   double piph, dphi, wiph;
+   double E[8], B[8], E_phi[4], Phi[5], RK_Phi[5];
+   double tempDoub;
+   int real;
+} pcell;
+
+typedef struct pface {
+   pcell *L, *R;
+   double dxL, dxR, cm[3], dphi, dl, dA, E, B;
+   int LRtype, flip_flag;
 } pface;
 
 typedef struct port_domain {
    disco_params par;
    disco_modules mod;
-   int Nr, Nz, NgRa, NgRb, NgZa, NgZb, nq, nc, Npl;
+   int Nr, Nz, NgRa, NgRb, NgZa, NgZb, nq, nc, Npl, mhd, ct;
    long N;
    int *Np;
    long *off;
-   double *rj, *zk;      /* rj[j] = reference r_jph[j] for j = -1..Nr-1 */
+   pcell *cells;
+   pcell **ring;          /* ring[jk] = cells + off[jk] */
+   double *rj, *zk;       /* rj[j] = reference r_jph[j], j = -1..Nr-1 */
    double Pmax, t;
-   double *piph, *dphi, *wiph;
-   double *prim, *cons, *RKcons, *gradp, *gradr, *gradz;   /* [c*nq + q] */
    pface *faces[2];
    int *fI[2];
-   int nfaces[2];
+   int ntracks[2];
    disco_planet pl[DISCO_MAX_PLANETS];
-   /* physics */
-   double gamma_law, rho_floor, p_floor;
+   double gam;
 } port_domain;
 
-#define P(d, c) ((d)->prim + (size_t)(c)*(d)->nq)
-#define U(d, c) ((d)->cons + (size_t)(c)*(d)->nq)
+static port_domain *D;   /* the domain being advanced (module statics in the reference) */
 
 /* ---- geometry: Geometry/cylindrical.c:10-75 ---------------------------- */
-static double get_dp(const port_domain *d, double phip, double phim)
+static double get_dp(double phip, double phim)
 {
    double dp = phip - phim;
-   while(dp < 0.0) dp += d->Pmax;
-   while(dp > d->Pmax) dp -= d->Pmax;
+   while(dp < 0.0) dp += D->Pmax;
+   while(dp > D->Pmax) dp -= D->Pmax;
    return dp;
 }
-static double get_signed_dp(const port_domain *d, double phip, double phim)
+static double get_signed_dp(double phip, double phim)
 {
    double dp = phip - phim;
-   while(dp < -.5*d->Pmax) dp += d->Pmax;
-   while(dp > .5*d->Pmax) dp -= d->Pmax;
+   while(dp < -.5*D->Pmax) dp += D->Pmax;
+   while(dp > .5*D->Pmax) dp -= D->Pmax;
    return dp;
 }
 static double centroid(double xp, double xm, int dim)
@@ -75,67 +84,134 @@ static double centroid(double xp, double xm, int dim)
    if(dim == 1) return 2.0*(xp*xp + xp*xm + xm*xm)/(3.0*(xp + xm));
    return 0.5*(xp + xm);
 }
-static double get_dA(const port_domain *d, const double *xp, const double *xm, int dim)
+static void centroid_arr(const double *xp, const double *xm, double *x)
+{
+   x[0] = centroid(xp[0], xm[0], 1);
+   x[1] = centroid(xp[1], xm[1], 0);
+   x[2] = centroid(xp[2], xm[2], 2);
+}
+static double get_dL(const double *xp, const double *xm, int dim)
+{
+   double r = .5*(xp[0] + xm[0]);
+   double dphi = get_dp(xp[1], xm[1]);
+   if(dim == 0) return r*dphi;
+   if(dim == 1) return xp[0] - xm[0];
+   return xp[2] - xm[2];
+}
+static double get_dA(const double *xp, const double *xm, int dim)
 {
    double r = .5*(xp[0] + xm[0]), dr = xp[0] - xm[0];
-   double dphi = get_dp(d, xp[1], xm[1]), dz = xp[2] - xm[2];
+   double dphi = get_dp(xp[1], xm[1]), dz = xp[2] - xm[2];
    if(dim == 0) return dr*dz;
    if(dim == 1) return r*dphi*dz;
    return r*dr*dphi;
 }
-static double get_dV(const port_domain *d, const double *xp, const double *xm)
+static double get_dV(const double *xp, const double *xm)
 {
    double r = .5*(xp[0] + xm[0]), dr = xp[0] - xm[0];
-   double dphi = get_dp(d, xp[1], xm[1]), dz = xp[2] - xm[2];
+   double dphi = get_dp(xp[1], xm[1]), dz = xp[2] - xm[2];
    return r*dr*dphi*dz;
 }
 
-/* ---- omega.c (Energy_Omega 0: om = -RotOmega) ---------------------------- */
-static double get_om(const port_domain *d, const double *x)
+/* ---- omega.c ------------------------------------------------------------ */
+static double get_om(const double *x)
 {
-   double r = sqrt(x[0]*x[0] + d->par.grav_eps*d->par.grav_eps);
-   switch(d->par.Energy_Omega) {
-   case 1: return 1.0 - d->par.RotOmega;
-   case 2: return 1.0/pow(r, 1.5) - d->par.RotOmega;
-   default: return 0.0 - d->par.RotOmega;
+   double r = sqrt(x[0]*x[0] + D->par.grav_eps*D->par.grav_eps);
+   switch(D->par.Energy_Omega) {
+   case 1: return 1.0 - D->par.RotOmega;
+   case 2: return 1.0/pow(r, 1.5) - D->par.RotOmega;
+   default: return 0.0 - D->par.RotOmega;
    }
 }
-static double get_om1(const port_domain *d, const double *x)
+static double get_om1(const double *x)
 {
-   double r = sqrt(x[0]*x[0] + d->par.grav_eps*d->par.grav_eps);
-   if(d->par.Energy_Omega == 2) return -1.5/pow(r, 2.5);
+   double r = sqrt(x[0]*x[0] + D->par.grav_eps*D->par.grav_eps);
+   if(D->par.Energy_Omega == 2) return -1.5/pow(r, 2.5);
    return 0.0;
 }
+static double get_cs2(const double *x)
+{
+   double r = x[0];
+   if(D->par.Cs2_Profile == 1) return 1./(D->par.Disk_Mach*D->par.Disk_Mach);
+   if(D->par.Cs2_Profile == 4) {
+      r = sqrt(r*r + D->par.grav_eps*D->par.grav_eps);
+      double v2 = D->par.metricPar2/r;
+      return v2/(D->par.Disk_Mach*D->par.Disk_Mach);
+   }
+   return 1.0;
+}
 
-/* ---- Hydro/euler.c ------------------------------------------------------- */
-static void prim2cons(const port_domain *d, const double *prim, double *cons,
-                      const double *x, double dV)
+/* ---- planet.c (point masses) ---------------------------------------------- */
+static double fgrav(double M, double r, double eps)
+{
+   double n = 2.0;
+   return M*pow(r, n - 1.)/pow(pow(r, n) + pow(eps, n), 1. + 1./n);
+}
+static void planetary_force(const disco_planet *pl, double r, double phi, double z,
+                            double *fr, double *fp, double *fz)
+{
+   double rp = pl->r, pp = pl->phi;
+   if(D->par.grav2D == 1) z = 0.0;
+   else if(D->par.grav2D == 2) { rp = r; pp = phi; z = 1.0; }
+   double cosp = cos(phi), sinp = sin(phi);
+   double dx = r*cosp - rp*cos(pp);
+   double dy = r*sinp - rp*sin(pp);
+   double script_r = sqrt(dx*dx + dy*dy + z*z);
+   double script_r_perp = sqrt(dx*dx + dy*dy);
+   double f1 = -fgrav(pl->M, script_r, pl->eps);
+   double cosa = dx/script_r_perp, sina = dy/script_r_perp;
+   double cosap = cosa*cosp + sina*sinp;
+   double sinap = sina*cosp - cosa*sinp;
+   if(script_r_perp <= 0.0) { cosap = 0.0; sinap = 0.0; }
+   double sint = script_r_perp/script_r, cost = z/script_r;
+   *fr = cosap*f1*sint;
+   *fp = sinap*f1*sint;
+   *fz = f1*cost;
+}
+static void planet_src(const disco_planet *pl, const double *prim, double *cons,
+                       const double *xp, const double *xm, double dVdt)
+{
+   double rho = prim[RHO], vr = prim[URR], vz = prim[UZZ], omega = prim[UPP];
+   double dphi = get_dp(xp[1], xm[1]);
+   double phi = xm[1] + 0.5*dphi;
+   double x[3] = {centroid(xp[0], xm[0], 1), phi, centroid(xp[2], xm[2], 2)};
+   double F[3];
+   planetary_force(pl, x[0], x[1], x[2], &F[0], &F[1], &F[2]);
+   double hr = 1.0, hp = x[0], hz = 1.0;
+   cons[SRR] += rho*hr*F[0]*dVdt;
+   cons[LLL] += rho*hp*F[1]*dVdt;
+   cons[SZZ] += rho*hz*F[2]*dVdt;
+   cons[TAU] += rho*(hr*F[0]*vr + hz*F[2]*vz + hp*F[1]*omega)*dVdt;
+}
+
+/* ---- Hydro/euler.c -------------------------------------------------------- */
+static void e_prim2cons(const double *prim, double *cons, const double *x, double dV)
 {
    double r = x[0], rho = prim[RHO], Pp = prim[PPP], vr = prim[URR];
    double vp = prim[UPP]*r, vz = prim[UZZ];
-   double om = get_om(d, x);
+   double om = get_om(x);
    double vp_off = vp - om*r;
    double v2 = vr*vr + vp_off*vp_off + vz*vz;
-   double rhoe = Pp/(d->gamma_law - 1.);
+   double rhoe = Pp/(D->gam - 1.);
    cons[DDD] = rho*dV;
    cons[TAU] = (.5*rho*v2 + rhoe)*dV;
    cons[SRR] = rho*vr*dV;
    cons[LLL] = r*rho*vp*dV;
    cons[SZZ] = rho*vz*dV;
-   for(int q = d->nc; q < d->nq; q++) cons[q] = prim[q]*cons[DDD];
+   for(int q = D->nc; q < D->nq; q++) cons[q] = prim[q]*cons[DDD];
 }
-static void getUstar(const port_domain *d, const double *prim, double *Ustar,
-                     const double *x, double Sk, double Ss, const double *n)
+static void e_getUstar(const double *prim, double *Ustar, const double *x, double Sk, double Ss,
+                       const double *n)
 {
    double r = x[0], rho = prim[RHO], vr = prim[URR], vp = prim[UPP]*r;
    double vz = prim[UZZ], Pp = prim[PPP];
-   double om = get_om(d, x);
+   double om = get_om(x);
    double vp_off = vp - om*r;
    double v2 = vr*vr + vp_off*vp_off + vz*vz;
    double vn = vr*n[0] + vp*n[1] + vz*n[2];
    double vn_off = vn - om*r*n[1];
    double Ss_off = Ss + vn_off - vn;
-   double rhoe = Pp/(d->gamma_law - 1.);
+   double rhoe = Pp/(D->gam - 1.);
    double rhostar = rho*(Sk - vn)/(Sk - Ss);
    double Pstar = Pp*(Ss - vn)/(Sk - Ss);
    double Us = rhoe*(Sk - vn)/(Sk - Ss);
@@ -144,67 +220,59 @@ static void getUstar(const port_domain *d, const double *prim, double *Ustar,
    Ustar[LLL] = r*rhostar*(vp + (Ss - vn)*n[1]);
    Ustar[SZZ] = rhostar*(vz + (Ss - vn)*n[2]);
    Ustar[TAU] = .5*rhostar*v2 + Us + rhostar*Ss_off*(Ss - vn) + Pstar;
-   for(int q = d->nc; q < d->nq; q++) Ustar[q] = prim[q]*Ustar[DDD];
+   for(int q = D->nc; q < D->nq; q++) Ustar[q] = prim[q]*Ustar[DDD];
 }
-static void cons2prim(const port_domain *d, const double *cons, double *prim,
-                      const double *x, double dV)
+static void e_cons2prim(const double *cons, double *prim, const double *x, double dV)
 {
    double r = x[0];
    double rho = cons[DDD]/dV;
-   if(rho < d->rho_floor) rho = d->rho_floor;
+   if(rho < D->par.Density_Floor) rho = D->par.Density_Floor;
    double Sr = cons[SRR]/dV, Sp = cons[LLL]/dV/r, Sz = cons[SZZ]/dV, E = cons[TAU]/dV;
-   double om = get_om(d, x);
+   double om = get_om(x);
    double vr = Sr/rho, vp = Sp/rho, vp_off = vp - om*r, vz = Sz/rho;
    double KE = .5*(Sr*vr + rho*vp_off*vp_off + Sz*vz);
    double rhoe = E - KE;
-   double Pp = (d->gamma_law - 1.)*rhoe;
-   if(Pp < d->p_floor*rho) Pp = d->p_floor*rho;
-   if(d->par.isothermal_flag) {
-      double rr = sqrt(r*r + d->par.grav_eps*d->par.grav_eps);
-      double cs2 = 1.0;
-      if(d->par.Cs2_Profile == 1) cs2 = 1./(d->par.Disk_Mach*d->par.Disk_Mach);
-      else if(d->par.Cs2_Profile == 4) cs2 = (d->par.metricPar2/rr)/(d->par.Disk_Mach*d->par.Disk_Mach);
-      Pp = cs2*rho/d->gamma_law;
-   }
+   double Pp = (D->gam - 1.)*rhoe;
+   if(Pp < D->par.Pressure_Floor*rho) Pp = D->par.Pressure_Floor*rho;
+   if(D->par.isothermal_flag) Pp = get_cs2(x)*rho/D->gam;
    prim[RHO] = rho; prim[PPP] = Pp; prim[URR] = vr; prim[UPP] = vp/r; prim[UZZ] = vz;
-   for(int q = d->nc; q < d->nq; q++) prim[q] = cons[q]/cons[DDD];
+   for(int q = D->nc; q < D->nq; q++) prim[q] = cons[q]/cons[DDD];
 }
-static void flux(const port_domain *d, const double *prim, double *f, const double *x,
-                 const double *n)
+static void e_flux(const double *prim, double *f, const double *x, const double *n)
 {
    double r = x[0], rho = prim[RHO], Pp = prim[PPP], vr = prim[URR];
    double vp = prim[UPP]*r, vz = prim[UZZ];
-   double om = get_om(d, x);
+   double om = get_om(x);
    double vn = vr*n[0] + vp*n[1] + vz*n[2];
    double wn = om*r*n[1];
    double vp_off = vp - om*r;
-   double rhoe = Pp/(d->gamma_law - 1.);
+   double rhoe = Pp/(D->gam - 1.);
    double v2 = vr*vr + vp_off*vp_off + vz*vz;
    f[DDD] = rho*vn;
    f[SRR] = rho*vr*vn + Pp*n[0];
    f[LLL] = r*(rho*vp*vn + Pp*n[1]);
    f[SZZ] = rho*vz*vn + Pp*n[2];
    f[TAU] = (.5*rho*v2 + rhoe + Pp)*vn - Pp*wn;
-   for(int q = d->nc; q < d->nq; q++) f[q] = prim[q]*f[DDD];
+   for(int q = D->nc; q < D->nq; q++) f[q] = prim[q]*f[DDD];
 }
-static void vel(const port_domain *d, const double *p1, const double *p2, double *Sl,
-                double *Sr, double *Ss, const double *n, const double *x)
+static void e_vel(const double *p1, const double *p2, double *Sl, double *Sr, double *Ss,
+                  const double *n, const double *x)
 {
    double r = x[0];
    double P1 = p1[PPP], rho1 = p1[RHO];
    double vn1 = p1[URR]*n[0] + p1[UPP]*n[1]*r + p1[UZZ]*n[2];
-   double cs1 = sqrt(d->gamma_law*P1/rho1);
+   double cs1 = sqrt(D->gam*P1/rho1);
    double P2 = p2[PPP], rho2 = p2[RHO];
    double vn2 = p2[URR]*n[0] + p2[UPP]*n[1]*r + p2[UZZ]*n[2];
-   double cs2 = sqrt(d->gamma_law*P2/rho2);
+   double cs2 = sqrt(D->gam*P2/rho2);
    *Ss = (P2 - P1 + rho1*vn1*(-cs1) - rho2*vn2*cs2)/(rho1*(-cs1) - rho2*cs2);
    *Sr = cs1 + vn1;
    *Sl = -cs1 + vn1;
    if(*Sr < cs2 + vn2) *Sr = cs2 + vn2;
    if(*Sl > -cs2 + vn2) *Sl = -cs2 + vn2;
 }
-static void source(const port_domain *d, const double *prim, double *cons,
-                   const double *xp, const double *xm, double dVdt)
+static void e_source(const double *prim, double *cons, const double *xp, const double *xm,
+                     double dVdt)
 {
    double rp = xp[0], rm = xm[0];
    double rho = prim[RHO], Pp = prim[PPP];
@@ -215,82 +283,406 @@ static void source(const port_domain *d, const double *prim, double *cons,
    double centrifugal = rho*omega*omega*r;
    double press_bal = Pp/r_1;
    cons[SRR] += dVdt*(centrifugal + press_bal);
-   double om = get_om(d, x), om_r = get_om1(d, x), om_z = 0.0;
+   double om = get_om(x), om_r = get_om1(x), om_z = 0.0;
    cons[TAU] += dVdt*rho*(r*vr*om*om - r*r*(omega - om)*(vr*om_r + vz*om_z));
 }
-static double mindt(const port_domain *d, const double *prim, double w,
-                    const double *xp, const double *xm)
+static double e_mindt(const double *prim, double w, const double *xp, const double *xm)
 {
    double r = centroid(xp[0], xm[0], 1);
    double Pp = prim[PPP], rho = prim[RHO];
    double vp = (prim[UPP] - w)*r, vr = prim[URR], vz = prim[UZZ];
-   double cs = sqrt(d->gamma_law*Pp/rho);
+   double cs = sqrt(D->gam*Pp/rho);
    double maxvr = cs + fabs(vr), maxvp = cs + fabs(vp), maxvz = cs + fabs(vz);
-   double dtr = (xp[0] - xm[0])/maxvr;
-   double dtp = (.5*(xp[0] + xm[0])*get_dp(d, xp[1], xm[1]))/maxvp;
-   double dtz = (xp[2] - xm[2])/maxvz;
+   double dtr = get_dL(xp, xm, 1)/maxvr;
+   double dtp = get_dL(xp, xm, 0)/maxvp;
+   double dtz = get_dL(xp, xm, 2)/maxvz;
    double dt = dtr;
    if(dt > dtp) dt = dtp;
    if(dt > dtz) dt = dtz;
    return dt;
 }
 
-/* ---- Riemann solver: riemann.c:216-320 (HLL / HLLC) ------------------------- */
-static void solve_riemann(port_domain *d, const double *primL, const double *primR,
-                          double *consL, double *consR, const double *x, const double *n,
-                          double w, double dAdt)
+/* ---- Hydro/mhd.c ----------------------------------------------------------- */
+static void m_prim2cons(const double *prim, double *cons, const double *x, double dV)
 {
-   int nq = d->nq, q;
+   double r = x[0], rho = prim[RHO], Pp = prim[PPP], vr = prim[URR];
+   double vp = prim[UPP]*r, vz = prim[UZZ];
+   double om = get_om(x);
+   double vp_off = vp - om*r;
+   double Br = prim[BRR], Bp = prim[BPP], Bz = prim[BZZ];
+   double v2 = vr*vr + vp_off*vp_off + vz*vz;
+   double B2 = Br*Br + Bp*Bp + Bz*Bz;
+   double rhoe = Pp/(D->gam - 1.);
+   cons[DDD] = rho*dV;
+   cons[TAU] = (.5*rho*v2 + rhoe + .5*B2)*dV;
+   cons[SRR] = rho*vr*dV;
+   cons[LLL] = r*rho*vp*dV;
+   cons[SZZ] = rho*vz*dV;
+   cons[BRR] = Br*dV*(1.0/r);
+   cons[BPP] = Bp*dV/r;
+   cons[BZZ] = Bz*dV;
+   for(int q = D->nc; q < D->nq; q++) cons[q] = prim[q]*cons[DDD];
+}
+static void m_cons2prim(const double *cons, double *prim, const double *x, double dV)
+{
+   double r = x[0];
+   double rho = cons[DDD]/dV;
+   if(rho < D->par.Density_Floor) rho = D->par.Density_Floor;
+   double Sr = cons[SRR]/dV, Sp = cons[LLL]/dV/r, Sz = cons[SZZ]/dV, E = cons[TAU]/dV;
+   double om = get_om(x);
+   double vr = Sr/rho, vp = Sp/rho, vp_off = vp - om*r, vz = Sz/rho;
+   double Br = cons[BRR]/(dV*(1.0/r));
+   double Bp = cons[BPP]/dV*r;
+   double Bz = cons[BZZ]/dV;
+   double B2 = Br*Br + Bp*Bp + Bz*Bz;
+   double KE = .5*(Sr*vr + rho*vp_off*vp_off + Sz*vz);
+   double rhoe = E - KE - .5*B2;
+   double Pp = (D->gam - 1.)*rhoe;
+   if(Pp < D->par.Pressure_Floor*rho) Pp = D->par.Pressure_Floor*rho;
+   if(D->par.isothermal_flag) Pp = get_cs2(x)*rho/D->gam;
+   prim[RHO] = rho; prim[PPP] = Pp; prim[URR] = vr; prim[UPP] = vp/r; prim[UZZ] = vz;
+   prim[BRR] = Br; prim[BPP] = Bp; prim[BZZ] = Bz;
+   for(int q = D->nc; q < D->nq; q++) prim[q] = cons[q]/cons[DDD];
+}
+static void m_flux(const double *prim, double *f, const double *x, const double *n)
+{
+   double r = x[0], rho = prim[RHO], Pp = prim[PPP], vr = prim[URR];
+   double vp = prim[UPP]*r, vz = prim[UZZ];
+   double Br = prim[BRR], Bp = prim[BPP], Bz = prim[BZZ];
+   double vn = vr*n[0] + vp*n[1] + vz*n[2];
+   double Bn = Br*n[0] + Bp*n[1] + Bz*n[2];
+   double vB = vr*Br + vp*Bp + vz*Bz;
+   double rhoe = Pp/(D->gam - 1.);
+   double v2 = vr*vr + vp*vp + vz*vz;
+   double B2 = Br*Br + Bp*Bp + Bz*Bz;
+   f[DDD] = rho*vn;
+   f[SRR] = rho*vr*vn + (Pp + .5*B2)*n[0] - Br*Bn;
+   f[LLL] = r*(rho*vp*vn + (Pp + .5*B2)*n[1] - Bp*Bn);
+   f[SZZ] = rho*vz*vn + (Pp + .5*B2)*n[2] - Bz*Bn;
+   f[TAU] = (.5*rho*v2 + rhoe + Pp + B2)*vn - vB*Bn;
+   f[BRR] = (Br*vn - vr*Bn)*(1.0/r);
+   f[BPP] = (Bp*vn - vp*Bn)/r;
+   f[BZZ] = Bz*vn - vz*Bn;
+   for(int q = D->nc; q < D->nq; q++) f[q] = prim[q]*f[DDD];
+}
+static void m_source(const double *prim, double *cons, const double *xp, const double *xm,
+                     double dVdt)
+{
+   double rp = xp[0], rm = xm[0];
+   double dphi = get_dp(xp[1], xm[1]);
+   double rho = prim[RHO], Pp = prim[PPP];
+   double r_1 = .5*(rp + rm);
+   double r2_3 = (rp*rp + rp*rm + rm*rm)/3.;
+   double vr = prim[URR], omega = prim[UPP];
+   double r = centroid(rp, rm, 1), z = centroid(xp[2], xm[2], 2);
+   double x[3] = {r, 0.5*(xm[1] + xp[1]), z};
+   double Br = prim[BRR], Bp = prim[BPP], Bz = prim[BZZ];
+   double B2 = Br*Br + Bp*Bp + Bz*Bz;
+   double centrifugal;
+   if(D->NgRa == 0) {
+      centrifugal = (rho*omega*omega*r2_3)/r_1*sin(.5*dphi)/(.5*dphi);
+      centrifugal -= Bp*Bp/r_1;
+   } else {
+      centrifugal = rho*omega*omega*r - Bp*Bp/r;
+   }
+   double press_bal = (Pp + .5*B2)/r_1;
+   cons[SRR] += dVdt*(centrifugal + press_bal);
+   double om = get_om(x), om1 = get_om1(x);
+   cons[TAU] += dVdt*rho*vr*(om*om*r2_3/r_1 - om1*(omega - om)*r2_3);
+   if(D->par.visc_flag) cons[SRR] += -dVdt*D->par.viscosity*rho*vr/(r_1*r_1);
+}
+static void m_flux_to_E(const double *Flux, const double *Ustr, const double *x,
+                        double *E1, double *B1, double *E2, double *B2, int dim)
+{
+   double r = x[0];
+   double irfac = 1.0/(1.0/x[0]);
+   if(dim == 0) {
+      *E1 = Flux[BRR]*irfac; *B1 = Ustr[BRR]*irfac; *E2 = -Flux[BZZ]; *B2 = Ustr[BZZ];
+   } else if(dim == 1) {
+      *E1 = -Flux[BPP]*r; *B1 = Ustr[BRR]*irfac; *E2 = Flux[BZZ];
+   } else {
+      *E1 = Flux[BPP]*r; *B1 = Ustr[BZZ]; *E2 = -Flux[BRR]*irfac;
+   }
+}
+static double m_mindt(const double *prim, double w, const double *xp, const double *xm)
+{
+   double r = centroid(xp[0], xm[0], 1);
+   double Pp = prim[PPP], rho = prim[RHO];
+   double vp = (prim[UPP] - w)*r, vr = prim[URR], vz = prim[UZZ];
+   double cs = sqrt(D->gam*Pp/rho);
+   double Br = prim[BRR], Bp = prim[BPP], Bz = prim[BZZ];
+   double b2 = (Br*Br + Bp*Bp + Bz*Bz)/rho;
+   double cf = sqrt(cs*cs + b2);
+   double maxvr = cf + fabs(vr), maxvp = cf + fabs(vp), maxvz = cf + fabs(vz);
+   double dtr = get_dL(xp, xm, 1)/maxvr;
+   double dtp = get_dL(xp, xm, 0)/maxvp;
+   double dtz = get_dL(xp, xm, 2)/maxvz;
+   double dt = dtr;
+   if(dt > dtp) dt = dtp;
+   if(dt > dtz) dt = dtz;
+   return dt;
+}
+
+/* ---- hlld.c: 5-wave solver with face speed w ------------------------------ */
+static void h_velocities(const double *pL, const double *pR, const double *n, double *vel,
+                         double *Pt_star)
+{
+   double gam = D->gam;
+   double rho_L = pL[RHO], P_L = pL[PPP];
+   double u_L = pL[URR]*n[0] + pL[UPP]*n[1] + pL[UZZ]*n[2];
+   double Bn_L = pL[BRR]*n[0] + pL[BPP]*n[1] + pL[BZZ]*n[2];
+   double B2_L = pL[BRR]*pL[BRR] + pL[BPP]*pL[BPP] + pL[BZZ]*pL[BZZ];
+   double Pt_L = P_L + .5*B2_L;
+   double rho_R = pR[RHO], P_R = pR[PPP];
+   double u_R = pR[URR]*n[0] + pR[UPP]*n[1] + pR[UZZ]*n[2];
+   double Bn_R = pR[BRR]*n[0] + pR[BPP]*n[1] + pR[BZZ]*n[2];
+   double B2_R = pR[BRR]*pR[BRR] + pR[BPP]*pR[BPP] + pR[BZZ]*pR[BZZ];
+   double Pt_R = P_R + .5*B2_R;
+   double Bn = .5*(Bn_L + Bn_R);
+   double aL = gam*P_L + B2_L, aR = gam*P_R + B2_R;
+   double cf2_L = .5*(gam*P_L + B2_L + sqrt(fabs(aL*aL - 4.*gam*P_L*Bn_L*Bn_L)))/rho_L;
+   double cf2_R = .5*(gam*P_R + B2_R + sqrt(fabs(aR*aR - 4.*gam*P_R*Bn_R*Bn_R)))/rho_R;
+   double cf2 = cf2_L > cf2_R ? cf2_L : cf2_R;
+   double umin, umax;
+   if(u_L < u_R) { umin = u_L; umax = u_R; } else { umin = u_R; umax = u_L; }
+   double S_R = umax + sqrt(fabs(cf2));
+   double S_L = umin - sqrt(fabs(cf2));
+   double S_M = ((S_R - u_R)*rho_R*u_R - (S_L - u_L)*rho_L*u_L - Pt_R + Pt_L)/
+                ((S_R - u_R)*rho_R - (S_L - u_L)*rho_L);
+   double rhostar_L = rho_L*(S_L - u_L)/(S_L - S_M);
+   double rhostar_R = rho_R*(S_R - u_R)/(S_R - S_M);
+   vel[0] = S_L;
+   vel[1] = S_M - fabs(Bn)/sqrt(rhostar_L);
+   vel[2] = S_M;
+   vel[3] = S_M + fabs(Bn)/sqrt(rhostar_R);
+   vel[4] = S_R;
+   double num = (S_R - u_R)*rho_R*Pt_L - (S_L - u_L)*rho_L*Pt_R +
+                rho_L*rho_R*(S_R - u_R)*(S_L - u_L)*(u_R - u_L);
+   double denom = (S_R - u_R)*rho_R - (S_L - u_L)*rho_L;
+   *Pt_star = num/denom;
+}
+static void h_prim_to_cons(const double *prim, double *cons)
+{
+   double rho = prim[RHO], Pp = prim[PPP], vx = prim[URR], vy = prim[UPP], vz = prim[UZZ];
+   double Bx = prim[BRR], By = prim[BPP], Bz = prim[BZZ];
+   double v2 = vx*vx + vy*vy + vz*vz;
+   double rhoe = Pp/(D->gam - 1.);
+   double B2 = Bx*Bx + By*By + Bz*Bz;
+   cons[DDD] = rho; cons[SRR] = rho*vx; cons[LLL] = rho*vy; cons[SZZ] = rho*vz;
+   cons[TAU] = (.5*rho*v2 + rhoe + .5*B2);
+   cons[BRR] = Bx; cons[BPP] = By; cons[BZZ] = Bz;
+}
+static void h_flux(const double *prim, double *flux, const double *n)
+{
+   double rho = prim[RHO], Pp = prim[PPP], vx = prim[URR], vy = prim[UPP], vz = prim[UZZ];
+   double Bx = prim[BRR], By = prim[BPP], Bz = prim[BZZ];
+   double v2 = vx*vx + vy*vy + vz*vz;
+   double vB = vx*Bx + vy*By + vz*Bz;
+   double B2 = Bx*Bx + By*By + Bz*Bz;
+   double vn = vx*n[0] + vy*n[1] + vz*n[2];
+   double Bn = Bx*n[0] + By*n[1] + Bz*n[2];
+   double rhoe = Pp/(D->gam - 1.);
+   flux[DDD] = rho*vn;
+   flux[SRR] = rho*vx*vn + (Pp + .5*B2)*n[0] - Bx*Bn;
+   flux[LLL] = rho*vy*vn + (Pp + .5*B2)*n[1] - By*Bn;
+   flux[SZZ] = rho*vz*vn + (Pp + .5*B2)*n[2] - Bz*Bn;
+   flux[TAU] = (.5*rho*v2 + rhoe + Pp + B2)*vn - vB*Bn;
+   flux[BRR] = Bx*vn - vx*Bn;
+   flux[BPP] = By*vn - vy*Bn;
+   flux[BZZ] = Bz*vn - vz*Bn;
+}
+static void h_single_star(const double *prim, double *Us, double S_K, double S_M,
+                          double Pt_star, const double *n)
+{
+   double rho = prim[RHO], vx = prim[URR], vy = prim[UPP], vz = prim[UZZ], Pp = prim[PPP];
+   double Bx = prim[BRR], By = prim[BPP], Bz = prim[BZZ];
+   double u_K = vx*n[0] + vy*n[1] + vz*n[2];
+   double Bn = Bx*n[0] + By*n[1] + Bz*n[2];
+   double vdotB = vx*Bx + vy*By + vz*Bz;
+   double v2 = vx*vx + vy*vy + vz*vz;
+   double B2 = Bx*Bx + By*By + Bz*Bz;
+   double Pt = Pp + .5*B2;
+   double e = .5*rho*v2 + Pp/(D->gam - 1.) + .5*B2;
+   double rhostar = rho*(S_K - u_K)/(S_K - S_M);
+   double denom = rho*(S_K - u_K)*(S_K - S_M) - Bn*Bn;
+   if(fabs(denom) < TOL_HLLD) denom = TOL_HLLD;
+   double vx_s = vx - Bn*Bx*(S_M - u_K)/denom;
+   double vy_s = vy - Bn*By*(S_M - u_K)/denom;
+   double vz_s = vz - Bn*Bz*(S_M - u_K)/denom;
+   double sq = (S_K - u_K)*(S_K - u_K);
+   double Bx_s = Bx*(rho*sq - Bn*Bn)/denom;
+   double By_s = By*(rho*sq - Bn*Bn)/denom;
+   double Bz_s = Bz*(rho*sq - Bn*Bn)/denom;
+   double vn_s = vx_s*n[0] + vy_s*n[1] + vz_s*n[2];
+   double Bn_s = Bx_s*n[0] + By_s*n[1] + Bz_s*n[2];
+   vx_s += (S_M - vn_s)*n[0]; vy_s += (S_M - vn_s)*n[1]; vz_s += (S_M - vn_s)*n[2];
+   Bx_s += (Bn - Bn_s)*n[0]; By_s += (Bn - Bn_s)*n[1]; Bz_s += (Bn - Bn_s)*n[2];
+   double vB_s = vx_s*Bx_s + vy_s*By_s + vz_s*Bz_s;
+   double e_s = ((S_K - u_K)*e - Pt*u_K + Pt_star*S_M + Bn*(vdotB - vB_s))/(S_K - S_M);
+   Us[DDD] = rhostar; Us[SRR] = rhostar*vx_s; Us[LLL] = rhostar*vy_s; Us[SZZ] = rhostar*vz_s;
+   Us[TAU] = e_s; Us[BRR] = Bx_s; Us[BPP] = By_s; Us[BZZ] = Bz_s;
+}
+static void h_double_star(const double *UsL, const double *UsR, double *Uss, const double *vel,
+                          const double *n, int LR)
+{
+   double rho_L = UsL[DDD], rho_R = UsR[DDD];
+   double rhostar_K = LR == 0 ? rho_L : rho_R;
+   double rrh_L = sqrt(rho_L), rrh_R = sqrt(rho_R), rrh_K = sqrt(rhostar_K);
+   double vx_L = UsL[SRR]/rho_L, vy_L = UsL[LLL]/rho_L, vz_L = UsL[SZZ]/rho_L;
+   double Bx_L = UsL[BRR], By_L = UsL[BPP], Bz_L = UsL[BZZ];
+   double vx_R = UsR[SRR]/rho_R, vy_R = UsR[LLL]/rho_R, vz_R = UsR[SZZ]/rho_R;
+   double Bx_R = UsR[BRR], By_R = UsR[BPP], Bz_R = UsR[BZZ];
+   double Bn_L = Bx_L*n[0] + By_L*n[1] + Bz_L*n[2];
+   double Bn_R = Bx_R*n[0] + By_R*n[1] + Bz_R*n[2];
+   double Bn = .5*(Bn_L + Bn_R);
+   double sB = Bn > 0.0 ? 1.0 : -1.0;
+   double den = rrh_L + rrh_R;
+   double vx = (rrh_L*vx_L + rrh_R*vx_R + (Bx_R - Bx_L)*sB)/den;
+   double vy = (rrh_L*vy_L + rrh_R*vy_R + (By_R - By_L)*sB)/den;
+   double vz = (rrh_L*vz_L + rrh_R*vz_R + (Bz_R - Bz_L)*sB)/den;
+   double vn = vx*n[0] + vy*n[1] + vz*n[2];
+   vx += (vel[2] - vn)*n[0]; vy += (vel[2] - vn)*n[1]; vz += (vel[2] - vn)*n[2];
+   double Bx = (rrh_L*Bx_R + rrh_R*Bx_L + rrh_L*rrh_R*(vx_R - vx_L)*sB)/den;
+   double By = (rrh_L*By_R + rrh_R*By_L + rrh_L*rrh_R*(vy_R - vy_L)*sB)/den;
+   double Bz = (rrh_L*Bz_R + rrh_R*Bz_L + rrh_L*rrh_R*(vz_R - vz_L)*sB)/den;
+   double Bns = Bx*n[0] + By*n[1] + Bz*n[2];
+   Bx += (Bn - Bns)*n[0]; By += (Bn - Bns)*n[1]; Bz += (Bn - Bns)*n[2];
+   double vB_ss = vx*Bx + vy*By + vz*Bz;
+   double vBstar, e_star;
+   if(LR == 0) { vBstar = vx_L*Bx_L + vy_L*By_L + vz_L*Bz_L; e_star = UsL[TAU]; }
+   else { vBstar = vx_R*Bx_R + vy_R*By_R + vz_R*Bz_R; e_star = UsR[TAU]; }
+   double pm = LR == 1 ? 1.0 : -1.0;
+   double e_ss = e_star + pm*rrh_K*(vBstar - vB_ss)*sB;
+   Uss[DDD] = rhostar_K; Uss[SRR] = rhostar_K*vx; Uss[LLL] = rhostar_K*vy; Uss[SZZ] = rhostar_K*vz;
+   Uss[TAU] = e_ss; Uss[BRR] = Bx; Uss[BPP] = By; Uss[BZZ] = Bz;
+}
+static void h_ustar(double w, const double *primL, const double *primR, double *F, double *U,
+                    const double *x, const double *n)
+{
+   double vel[5], Pt_star;
+   double hr = 1.0, hp = x[0], hz = 1.0;
+   double pL[MAXQ], pR[MAXQ];
+   int q, nq = D->nq;
+   memcpy(pL, primL, nq*sizeof(double));
+   memcpy(pR, primR, nq*sizeof(double));
+   pL[URR] *= hr; pR[URR] *= hr;
+   pL[UPP] *= hp; pR[UPP] *= hp;
+   pL[UZZ] *= hz; pR[UZZ] *= hz;
+   h_velocities(pL, pR, n, vel, &Pt_star);
+   if(w < vel[2]) {
+      double UL[8];
+      h_flux(pL, F, n);
+      h_prim_to_cons(pL, UL);
+      if(w < vel[0]) {
+         h_prim_to_cons(pL, U);
+      } else if(w < vel[1]) {
+         h_single_star(pL, U, vel[0], vel[2], Pt_star, n);
+         for(q = 0; q < 8; q++) F[q] += vel[0]*(U[q] - UL[q]);
+      } else {
+         double UsL[8], UsR[8];
+         h_single_star(pL, UsL, vel[0], vel[2], Pt_star, n);
+         h_single_star(pR, UsR, vel[4], vel[2], Pt_star, n);
+         h_double_star(UsL, UsR, U, vel, n, 0);
+         for(q = 0; q < 8; q++) F[q] += vel[1]*(U[q] - UsL[q]) + vel[0]*(UsL[q] - UL[q]);
+      }
+      for(q = 8; q < nq; q++) { U[q] = pL[q]*U[DDD]; F[q] = pL[q]*F[DDD]; }
+   } else {
+      double UR[8];
+      h_flux(pR, F, n);
+      h_prim_to_cons(pR, UR);
+      if(w > vel[4]) {
+         h_prim_to_cons(pR, U);
+      } else if(w > vel[3]) {
+         h_single_star(pR, U, vel[4], vel[2], Pt_star, n);
+         for(q = 0; q < 8; q++) F[q] += vel[4]*(U[q] - UR[q]);
+      } else {
+         double UsL[8], UsR[8];
+         h_single_star(pL, UsL, vel[0], vel[2], Pt_star, n);
+         h_single_star(pR, UsR, vel[4], vel[2], Pt_star, n);
+         h_double_star(UsL, UsR, U, vel, n, 1);
+         for(q = 0; q < 8; q++) F[q] += vel[3]*(U[q] - UsR[q]) + vel[4]*(UsR[q] - UR[q]);
+      }
+      for(q = 8; q < nq; q++) { U[q] = pR[q]*U[DDD]; F[q] = pR[q]*F[DDD]; }
+   }
+   double brfac = 1.0/x[0], bpfac = 1.0, bzfac = 1.0;
+   F[SRR] *= hr; F[LLL] *= hp; F[SZZ] *= hz;
+   F[BRR] *= brfac/hr; F[BPP] *= bpfac/hp; F[BZZ] *= bzfac/hz;
+   U[SRR] *= hr; U[LLL] *= hp; U[SZZ] *= hz;
+   U[BRR] *= brfac/hr; U[BPP] *= bpfac/hp; U[BZZ] *= bzfac/hz;
+}
+
+/* ---- module dispatch --------------------------------------------------------- */
+static void prim2cons(const double *p, double *c, const double *x, double dV)
+{ if(D->mhd) m_prim2cons(p, c, x, dV); else e_prim2cons(p, c, x, dV); }
+static void cons2prim(const double *c, double *p, const double *x, double dV)
+{ if(D->mhd) m_cons2prim(c, p, x, dV); else e_cons2prim(c, p, x, dV); }
+static void flux(const double *p, double *f, const double *x, const double *n)
+{ if(D->mhd) m_flux(p, f, x, n); else e_flux(p, f, x, n); }
+static double mindt(const double *p, double w, const double *xp, const double *xm)
+{ return D->mhd ? m_mindt(p, w, xp, xm) : e_mindt(p, w, xp, xm); }
+
+/* ---- riemann.c:216-320 ------------------------------------------------------- */
+static void solve_riemann(const double *primL, const double *primR, double *consL, double *consR,
+                          const double *x, const double *n, double w, double dAdt, int dim,
+                          double *E1, double *B1, double *E2, double *B2)
+{
+   int nq = D->nq, q;
    double Flux[MAXQ] = {0}, Ustr[MAXQ] = {0};
-   double Sl, Sr, Ss;
-   vel(d, primL, primR, &Sl, &Sr, &Ss, n, x);
-   if(w < Sl) {
-      flux(d, primL, Flux, x, n);
-      prim2cons(d, primL, Ustr, x, 1.0);
-   } else if(w > Sr) {
-      flux(d, primR, Flux, x, n);
-      prim2cons(d, primR, Ustr, x, 1.0);
-   } else if(d->par.Riemann_Solver == 0) {
-      double Fl[MAXQ], Fr[MAXQ], Ul[MAXQ], Ur[MAXQ];
-      double aL = Sr, aR = -Sl;
-      prim2cons(d, primL, Ul, x, 1.0);
-      prim2cons(d, primR, Ur, x, 1.0);
-      flux(d, primL, Fl, x, n);
-      flux(d, primR, Fr, x, n);
-      for(q = 0; q < nq; q++) {
-         Flux[q] = (aL*Fl[q] + aR*Fr[q] + aL*aR*(Ul[q] - Ur[q]))/(aL + aR);
-         Ustr[q] = (aR*Ul[q] + aL*Ur[q] + Fl[q] - Fr[q])/(aL + aR);
+   int solver = D->par.Riemann_Solver;
+   if(solver == 0 || solver == 1) {
+      double Sl, Sr, Ss;
+      e_vel(primL, primR, &Sl, &Sr, &Ss, n, x);
+      if(w < Sl) {
+         flux(primL, Flux, x, n);
+         prim2cons(primL, Ustr, x, 1.0);
+      } else if(w > Sr) {
+         flux(primR, Flux, x, n);
+         prim2cons(primR, Ustr, x, 1.0);
+      } else if(solver == 0) {
+         double Fl[MAXQ], Fr[MAXQ], Ul[MAXQ], Ur[MAXQ];
+         double aL = Sr, aR = -Sl;
+         prim2cons(primL, Ul, x, 1.0);
+         prim2cons(primR, Ur, x, 1.0);
+         flux(primL, Fl, x, n);
+         flux(primR, Fr, x, n);
+         for(q = 0; q < nq; q++) {
+            Flux[q] = (aL*Fl[q] + aR*Fr[q] + aL*aR*(Ul[q] - Ur[q]))/(aL + aR);
+            Ustr[q] = (aR*Ul[q] + aL*Ur[q] + Fl[q] - Fr[q])/(aL + aR);
+         }
+      } else {
+         double Uk[MAXQ], Fk[MAXQ];
+         if(w < Ss) {
+            prim2cons(primL, Uk, x, 1.0);
+            e_getUstar(primL, Ustr, x, Sl, Ss, n);
+            flux(primL, Fk, x, n);
+            for(q = 0; q < nq; q++) Flux[q] = Fk[q] + Sl*(Ustr[q] - Uk[q]);
+         } else {
+            prim2cons(primR, Uk, x, 1.0);
+            e_getUstar(primR, Ustr, x, Sr, Ss, n);
+            flux(primR, Fk, x, n);
+            for(q = 0; q < nq; q++) Flux[q] = Fk[q] + Sr*(Ustr[q] - Uk[q]);
+         }
       }
    } else {
-      double Uk[MAXQ], Fk[MAXQ];
-      if(w < Ss) {
-         prim2cons(d, primL, Uk, x, 1.0);
-         getUstar(d, primL, Ustr, x, Sl, Ss, n);
-         flux(d, primL, Fk, x, n);
-         for(q = 0; q < nq; q++) Flux[q] = Fk[q] + Sl*(Ustr[q] - Uk[q]);
-      } else {
-         prim2cons(d, primR, Uk, x, 1.0);
-         getUstar(d, primR, Ustr, x, Sr, Ss, n);
-         flux(d, primR, Fk, x, n);
-         for(q = 0; q < nq; q++) Flux[q] = Fk[q] + Sr*(Ustr[q] - Uk[q]);
-      }
+      h_ustar(w, primL, primR, Flux, Ustr, x, n);
    }
    for(q = 0; q < nq; q++) {
       consL[q] -= (Flux[q] - w*Ustr[q])*dAdt;
       consR[q] += (Flux[q] - w*Ustr[q])*dAdt;
    }
+   if(D->mhd) m_flux_to_E(Flux, Ustr, x, E1, B1, E2, B2, dim);
 }
 
-/* ---- faces: faces_alt.c:36-179 (sequential walk) ---------------------------- */
-static void build_faces(port_domain *d, int dim)
+/* ---- faces: faces_alt.c:36-179 (sequential walk) ------------------------------ */
+static void build_faces(int dim)
 {
-   int Nr = d->Nr, Nz = d->Nz, j, k, i, jk;
+   int Nr = D->Nr, Nz = D->Nz, j, k, i, jk;
    int *I0 = (int *)malloc(sizeof(int)*Nr*Nz);
-   double convert = 2.*M_PI/d->Pmax;
    for(jk = 0; jk < Nr*Nz; jk++) {
       int found = 0, quad_prev = 0;
-      for(i = 0; i < d->Np[jk] && !found; i++) {
-         double ph = d->piph[d->off[jk] + i];
+      for(i = 0; i < D->Np[jk] && !found; i++) {
+         double convert = 2.*M_PI/D->Pmax;
+         double ph = D->ring[jk][i].piph;
          double sn = sin(ph*convert), cs = cos(ph*convert);
          if(sn > 0. && cs > 0. && quad_prev) { found = 1; I0[jk] = i; }
          else if(sn < 0. && cs > 0.) quad_prev = 1;
@@ -299,19 +691,17 @@ static void build_faces(port_domain *d, int dim)
    }
    int Nrmax = dim == 1 ? Nr - 1 : Nr;
    int Nzmax = dim == 1 ? Nz : Nz - 1;
-   int d0 = dim - 1;
-   int n = 0;
+   int d0 = dim - 1, n = 0;
    for(k = 0; k < Nzmax; k++) for(j = 0; j < Nrmax; j++) {
-      int JK = j + Nrmax*k;
       int L = j + Nr*k, R = dim == 1 ? j + 1 + Nr*k : j + Nr*(k + 1);
-      d->fI[d0][JK] = n;
-      n += d->Np[L] + d->Np[R];
+      D->fI[d0][j + Nrmax*k] = n;
+      n += D->Np[L] + D->Np[R];
    }
-   d->fI[d0][Nrmax*Nzmax] = n;
-   d->nfaces[d0] = n;
-   free(d->faces[d0]);
-   d->faces[d0] = (pface *)malloc(sizeof(pface)*(n > 0 ? n : 1));
-   const double *rj = d->rj, *zk = d->zk;
+   D->fI[d0][Nrmax*Nzmax] = n;
+   D->ntracks[d0] = Nrmax*Nzmax;
+   free(D->faces[d0]);
+   D->faces[d0] = (pface *)malloc(sizeof(pface)*(n > 0 ? n : 1));
+   const double *rj = D->rj, *zk = D->zk;
    n = 0;
    for(k = 0; k < Nzmax; k++) for(j = 0; j < Nrmax; j++) {
       int jkL = j + Nr*k, jkR = dim == 1 ? j + 1 + Nr*k : j + Nr*(k + 1);
@@ -326,36 +716,36 @@ static void build_faces(port_domain *d, int dim)
       double xp[3] = {rj[j], 0.0, zk[k]}, xm[3] = {rj[j], 0.0, zk[k - 1]};
       if(dim == 2) { xm[0] = rj[j - 1]; xm[2] = zk[k]; }
       int a = I0[jkL], b = I0[jkR], f;
-      for(f = 0; f < d->Np[jkL] + d->Np[jkR]; f++) {
-         long cL = d->off[jkL] + a, cR = d->off[jkR] + b;
-         double dphi = d->piph[cL] - d->piph[cR];
-         while(dphi > .5*d->Pmax) dphi -= d->Pmax;
-         while(dphi < -.5*d->Pmax) dphi += d->Pmax;
+      for(f = 0; f < D->Np[jkL] + D->Np[jkR]; f++) {
+         pcell *cL = &D->ring[jkL][a], *cR = &D->ring[jkR][b];
+         double dphi = cL->piph - cR->piph;
+         while(dphi > .5*D->Pmax) dphi -= D->Pmax;
+         while(dphi < -.5*D->Pmax) dphi += D->Pmax;
          int LR = dphi > 0. ? 1 : 0;
-         dphi = d->piph[cL] - d->dphi[cL] - d->piph[cR] + d->dphi[cR];
-         while(dphi > .5*d->Pmax) dphi -= d->Pmax;
-         while(dphi < -.5*d->Pmax) dphi += d->Pmax;
+         dphi = cL->piph - cL->dphi - cR->piph + cR->dphi;
+         while(dphi > .5*D->Pmax) dphi -= D->Pmax;
+         while(dphi < -.5*D->Pmax) dphi += D->Pmax;
          int LR_back = dphi < 0. ? 1 : 0;
-         xp[1] = LR == 0 ? d->piph[cL] : d->piph[cR];
-         xm[1] = LR_back == 0 ? d->piph[cL] - d->dphi[cL] : d->piph[cR] - d->dphi[cR];
-         /* addFace, faces_alt.c:10-34 */
-         pface *F = &d->faces[d0][n];
-         double dp = get_dp(d, xp[1], xm[1]);
-         double phic = get_dp(d, xp[1], .5*dp);
+         xp[1] = LR == 0 ? cL->piph : cR->piph;
+         xm[1] = LR_back == 0 ? cL->piph - cL->dphi : cR->piph - cR->dphi;
+         pface *F = &D->faces[d0][n];
+         double dp = get_dp(xp[1], xm[1]);
          F->cm[0] = dim == 1 ? 0.5*(xp[0] + xm[0]) : centroid(xp[0], xm[0], 1);
-         F->cm[1] = phic;
+         F->cm[1] = get_dp(xp[1], .5*dp);
          F->cm[2] = dim == 2 ? 0.5*(xp[2] + xm[2]) : centroid(xp[2], xm[2], 2);
-         F->L = (int)cL; F->R = (int)cR; F->dxL = dxL; F->dxR = dxR;
-         F->dphi = dp; F->dA = get_dA(d, xp, xm, dim); F->LRtype = LR;
+         F->L = cL; F->R = cR; F->dxL = dxL; F->dxR = dxR;
+         F->dphi = dp; F->dA = get_dA(xp, xm, dim);
+         F->dl = get_dL(xp, xm, 3 - dim);
+         F->E = 0.0; F->B = 0.0; F->LRtype = LR; F->flip_flag = 0;
          n++;
-         if(LR == 0) { a++; if(a == d->Np[jkL]) a = 0; }
-         else { b++; if(b == d->Np[jkR]) b = 0; }
+         if(LR == 0) { a++; if(a == D->Np[jkL]) a = 0; }
+         else { b++; if(b == D->Np[jkR]) b = 0; }
       }
    }
    free(I0);
 }
 
-/* ---- reconstruction: plm.c ---------------------------------------------------- */
+/* ---- reconstruction: plm.c ----------------------------------------------------- */
 static double minmod(double a, double b, double c)
 {
    double m = a;
@@ -365,311 +755,712 @@ static double minmod(double a, double b, double c)
    if(fabs(c) < fabs(m)) m = c;
    return m;
 }
-static void plm_phi(port_domain *d)
+static void plm_phi(void)
 {
-   int jk, i, q, nq = d->nq;
-   double PLM = d->par.PLM;
-   for(jk = 0; jk < d->Nr*d->Nz; jk++) {
-      long o = d->off[jk];
-      int Np = d->Np[jk];
-      for(i = 0; i < Np; i++) {
-         long c = o + i, cl = o + (i == 0 ? Np - 1 : i - 1), cr = o + (i + 1)%Np;
-         double dpL = d->dphi[cl], dpC = d->dphi[c], dpR = d->dphi[cr];
-         for(q = 0; q < nq; q++) {
-            double pL = P(d, cl)[q], pC = P(d, c)[q], pR = P(d, cr)[q];
+   double PLM = D->par.PLM;
+   for(int jk = 0; jk < D->Nr*D->Nz; jk++) {
+      int Np = D->Np[jk];
+      for(int i = 0; i < Np; i++) {
+         pcell *c = &D->ring[jk][i], *cL = &D->ring[jk][i == 0 ? Np - 1 : i - 1];
+         pcell *cR = &D->ring[jk][(i + 1)%Np];
+         double dpL = cL->dphi, dpC = c->dphi, dpR = cR->dphi;
+         for(int q = 0; q < D->nq; q++) {
+            double pL = cL->prim[q], pC = c->prim[q], pR = cR->prim[q];
             double sL = pC - pL; sL /= .5*(dpC + dpL);
             double sR = pR - pC; sR /= .5*(dpR + dpC);
             double sC = pR - pL; sC /= .5*(dpL + dpR) + dpC;
-            d->gradp[c*nq + q] = minmod(PLM*sL, sC, PLM*sR);
+            c->gradp[q] = minmod(PLM*sL, sC, PLM*sR);
          }
       }
    }
 }
-static void plm_trans(port_domain *d, int dim)
+static double *gsel(pcell *c, int dim) { return dim == 1 ? c->gradr : c->gradz; }
+static void plm_trans(int dim)
 {
-   int nq = d->nq, q, n;
-   long c;
-   double *G = dim == 1 ? d->gradr : d->gradz;
-   memset(G, 0, sizeof(double)*nq*d->N);
-   double PLM = d->par.PLM;
+   int nq = D->nq, q, n, j, k, i;
+   for(j = 0; j < D->Nr; j++) for(k = 0; k < D->Nz; k++) {
+      int jk = j + D->Nr*k;
+      for(i = 0; i < D->Np[jk]; i++) memset(gsel(&D->ring[jk][i], dim), 0, sizeof(double)*MAXQ);
+   }
+   double PLM = D->par.PLM;
    if(PLM == 0.0) return;
-   pface *Fs = d->faces[dim - 1];
-   int Nf = d->nfaces[dim - 1];
+   pface *Fs = D->faces[dim - 1];
+   int Nf = D->fI[dim - 1][D->ntracks[dim - 1]];
    for(n = 0; n < Nf; n++) {
       pface *f = &Fs[n];
       double phi = f->cm[1];
-      double phiL = d->piph[f->L] - .5*d->dphi[f->L], phiR = d->piph[f->R] - .5*d->dphi[f->R];
-      double dpL = get_signed_dp(d, phi, phiL), dpR = get_signed_dp(d, phiR, phi);
+      double phiL = f->L->piph - .5*f->L->dphi, phiR = f->R->piph - .5*f->R->dphi;
+      double dpL = get_signed_dp(phi, phiL), dpR = get_signed_dp(phiR, phi);
+      double *gL = gsel(f->L, dim), *gR = gsel(f->R, dim);
       for(q = 0; q < nq; q++) {
-         double WL = P(d, f->L)[q] + dpL*d->gradp[(size_t)f->L*nq + q];
-         double WR = P(d, f->R)[q] - dpR*d->gradp[(size_t)f->R*nq + q];
+         double WL = f->L->prim[q] + dpL*f->L->gradp[q];
+         double WR = f->R->prim[q] - dpR*f->R->gradp[q];
          double S = (WR - WL)/(f->dxR + f->dxL);
-         G[(size_t)f->L*nq + q] += S*f->dA;
-         G[(size_t)f->R*nq + q] += S*f->dA;
+         gL[q] += S*f->dA;
+         gR[q] += S*f->dA;
       }
    }
-   int j, k, i;
-   for(j = 0; j < d->Nr; j++) for(k = 0; k < d->Nz; k++) {
-      int jk = j + d->Nr*k;
-      for(i = 0; i < d->Np[jk]; i++) {
-         c = d->off[jk] + i;
-         double phip = d->piph[c], phim = phip - d->dphi[c];
-         double xp[3] = {d->rj[j], phip, d->zk[k]}, xm[3] = {d->rj[j - 1], phim, d->zk[k - 1]};
-         if(dim == 1) xm[0] = d->rj[j]; else xm[2] = d->zk[k];
-         double dAp = get_dA(d, xp, xm, dim);
-         if(dim == 1) { xp[0] = d->rj[j - 1]; xm[0] = d->rj[j - 1]; }
-         else { xp[2] = d->zk[k - 1]; xm[2] = d->zk[k - 1]; }
-         double dAm = get_dA(d, xp, xm, dim);
+   for(j = 0; j < D->Nr; j++) for(k = 0; k < D->Nz; k++) {
+      int jk = j + D->Nr*k;
+      for(i = 0; i < D->Np[jk]; i++) {
+         pcell *c = &D->ring[jk][i];
+         double phip = c->piph, phim = phip - c->dphi;
+         double xp[3] = {D->rj[j], phip, D->zk[k]}, xm[3] = {D->rj[j - 1], phim, D->zk[k - 1]};
+         if(dim == 1) xm[0] = D->rj[j]; else xm[2] = D->zk[k];
+         double dAp = get_dA(xp, xm, dim);
+         if(dim == 1) { xp[0] = D->rj[j - 1]; xm[0] = D->rj[j - 1]; }
+         else { xp[2] = D->zk[k - 1]; xm[2] = D->zk[k - 1]; }
+         double dAm = get_dA(xp, xm, dim);
          double dAtot = dAp + dAm;
          if((dim == 1 && j == 0) || (dim == 2 && k == 0)) dAtot = dAp;
-         if((dim == 1 && j == d->Nr - 1) || (dim == 2 && k == d->Nz - 1)) dAtot = dAm;
-         for(q = 0; q < nq; q++) G[c*nq + q] /= dAtot;
+         if((dim == 1 && j == D->Nr - 1) || (dim == 2 && k == D->Nz - 1)) dAtot = dAm;
+         double *g = gsel(c, dim);
+         for(q = 0; q < nq; q++) g[q] /= dAtot;
       }
    }
    for(n = 0; n < Nf; n++) {
       pface *f = &Fs[n];
       double phi = f->cm[1];
-      double phiL = d->piph[f->L] - .5*d->dphi[f->L], phiR = d->piph[f->R] - .5*d->dphi[f->R];
-      double dpL = get_signed_dp(d, phi, phiL), dpR = get_signed_dp(d, phiR, phi);
+      double phiL = f->L->piph - .5*f->L->dphi, phiR = f->R->piph - .5*f->R->dphi;
+      double dpL = get_signed_dp(phi, phiL), dpR = get_signed_dp(phiR, phi);
+      double *gL = gsel(f->L, dim), *gR = gsel(f->R, dim);
       for(q = 0; q < nq; q++) {
-         double WL = P(d, f->L)[q] + dpL*d->gradp[(size_t)f->L*nq + q];
-         double WR = P(d, f->R)[q] - dpR*d->gradp[(size_t)f->R*nq + q];
+         double WL = f->L->prim[q] + dpL*f->L->gradp[q];
+         double WR = f->R->prim[q] - dpR*f->R->gradp[q];
          double S = (WR - WL)/(f->dxR + f->dxL);
-         double *gL = &G[(size_t)f->L*nq + q], *gR = &G[(size_t)f->R*nq + q];
-         if(S*(*gL) < 0.0) *gL = 0.0; else if(fabs(PLM*S) < fabs(*gL)) *gL = PLM*S;
-         if(S*(*gR) < 0.0) *gR = 0.0; else if(fabs(PLM*S) < fabs(*gR)) *gR = PLM*S;
+         if(S*gL[q] < 0.0) gL[q] = 0.0; else if(fabs(PLM*S) < fabs(gL[q])) gL[q] = PLM*S;
+         if(S*gR[q] < 0.0) gR[q] = 0.0; else if(fabs(PLM*S) < fabs(gR[q])) gR[q] = PLM*S;
       }
    }
 }
 
-/* ---- fluxes: misc.c:378-519, riemann.c:39-214 --------------------------------- */
-static void phi_flux(port_domain *d, double dt)
+/* ---- fluxes: misc.c:378-519, riemann.c:39-214 ------------------------------------- */
+static void riemann_phi(pcell *cL, pcell *cR, double *x, double dAdt)
 {
-   int j, k, i, q, nq = d->nq;
-   for(k = d->NgZa; k < d->Nz - d->NgZb; k++) {
-      double zp = d->zk[k], zm = d->zk[k - 1], z = centroid(zp, zm, 2);
-      for(j = d->NgRa; j < d->Nr - d->NgRb; j++) {
-         double rp = d->rj[j], rm = d->rj[j - 1], r = centroid(rp, rm, 1);
-         int jk = j + d->Nr*k, Np = d->Np[jk];
-         long o = d->off[jk];
-         for(i = 0; i < Np; i++) {
-            long cl = o + i, cr = o + (i < Np - 1 ? i + 1 : 0);
-            double phi = d->piph[cl];
-            double xp[3] = {rp, phi, zp}, xm[3] = {rm, phi, zm};
-            double dA = get_dA(d, xp, xm, 0);
-            double x[3] = {r, phi, z};
-            double primL[MAXQ], primR[MAXQ];
-            for(q = 0; q < nq; q++) {
-               primL[q] = P(d, cl)[q] + .5*d->gradp[cl*nq + q]*d->dphi[cl];
-               primR[q] = P(d, cr)[q] - .5*d->gradp[cr*nq + q]*d->dphi[cr];
-            }
-            double n[3] = {0.0, 1.0, 0.0};
-            double hn = x[0];
-            solve_riemann(d, primL, primR, U(d, cl), U(d, cr), x, n, hn*d->wiph[cl], dA*dt);
-         }
-      }
+   double primL[MAXQ], primR[MAXQ];
+   int q;
+   for(q = 0; q < D->nq; q++) {
+      primL[q] = cL->prim[q] + .5*cL->gradp[q]*cL->dphi;
+      primR[q] = cR->prim[q] - .5*cR->gradp[q]*cR->dphi;
+   }
+   double n[3] = {0.0, 1.0, 0.0};
+   double hn = x[0];
+   if(D->mhd) { double Bp = .5*(primL[BPP] + primR[BPP]); primL[BPP] = Bp; primR[BPP] = Bp; }
+   double Er = 0, Ez = 0, Br = 0, Bz = 0;
+   solve_riemann(primL, primR, cL->cons, cR->cons, x, n, hn*cL->wiph, dAdt, 0, &Ez, &Br, &Er, &Bz);
+   if(D->mhd && D->ct) {   /* NUM_EDGES == 8 */
+      cL->E[0] = .5*Ez; cL->E[1] = .5*Ez; cR->E[2] = .5*Ez; cR->E[3] = .5*Ez;
+      cL->B[0] = .5*Br; cL->B[1] = .5*Br; cR->B[2] = .5*Br; cR->B[3] = .5*Br;
+      cL->E[4] = .5*Er; cL->E[5] = .5*Er; cR->E[6] = .5*Er; cR->E[7] = .5*Er;
+      cL->B[4] = .5*Bz; cL->B[5] = .5*Bz; cR->B[6] = .5*Bz; cR->B[7] = .5*Bz;
    }
 }
-static void trans_flux(port_domain *d, double dt, int dim)
+static void riemann_trans(pface *F, double dt, int dim)
 {
-   int jmin, jmax, kmin, kmax, Nfr, j, k, q, nq = d->nq;
+   pcell *cL = F->L, *cR = F->R;
+   double dAdt = F->dA*dt, phi = F->cm[1];
+   double primL[MAXQ], primR[MAXQ];
+   double phiL = cL->piph - .5*cL->dphi, phiR = cR->piph - .5*cR->dphi;
+   double dpL = get_signed_dp(phi, phiL), dpR = get_signed_dp(phiR, phi);
+   double *gL = gsel(cL, dim), *gR = gsel(cR, dim);
+   int q;
+   for(q = 0; q < D->nq; q++) {
+      primL[q] = cL->prim[q] + gL[q]*F->dxL + cL->gradp[q]*dpL;
+      primR[q] = cR->prim[q] - gR[q]*F->dxR - cR->gradp[q]*dpR;
+   }
+   double n[3] = {0.0, 0.0, 0.0};
+   if(dim == 1) n[0] = 1.0; else n[2] = 1.0;
+   if(D->mhd) {
+      int BT = dim == 1 ? BRR : BZZ;
+      double Bavg = .5*(primL[BT] + primR[BT]);
+      primL[BT] = Bavg; primR[BT] = Bavg;
+   }
+   double Erz = 0, Brz = 0, Ephi = 0;
+   solve_riemann(primL, primR, cL->cons, cR->cons, F->cm, n, 0.0, dAdt, dim, &Erz, &Brz, &Ephi, NULL);
+   if(!(D->mhd && D->ct)) return;
+   double fracL = F->dphi/cL->dphi, fracR = F->dphi/cR->dphi;
    if(dim == 1) {
-      Nfr = d->Nr - 1;
-      jmin = d->NgRa == 0 ? 0 : d->NgRa - 1; jmax = d->NgRb == 0 ? d->Nr - 1 : d->Nr - d->NgRb;
-      kmin = d->NgZa; kmax = d->Nz - d->NgZb;
+      cL->E[1] += .5*Erz*fracL; cL->E[3] += .5*Erz*fracL;
+      cR->E[0] += .5*Erz*fracR; cR->E[2] += .5*Erz*fracR;
+      cL->B[1] += .5*Brz*fracL; cL->B[3] += .5*Brz*fracL;
+      cR->B[0] += .5*Brz*fracR; cR->B[2] += .5*Brz*fracR;
+      if(F->LRtype == 0) cL->E_phi[1] = Ephi; else cR->E_phi[0] = Ephi;
    } else {
-      Nfr = d->Nr;
-      jmin = d->NgRa; jmax = d->Nr - d->NgRb;
-      kmin = d->NgZa == 0 ? 0 : d->NgZa - 1; kmax = d->NgZb == 0 ? d->Nz - 1 : d->Nz - d->NgZb;
+      cL->E[5] += .5*Erz*fracL; cL->E[7] += .5*Erz*fracL;
+      cR->E[4] += .5*Erz*fracR; cR->E[6] += .5*Erz*fracR;
+      cL->B[5] += .5*Brz*fracL; cL->B[7] += .5*Brz*fracL;
+      cR->B[4] += .5*Brz*fracR; cR->B[6] += .5*Brz*fracR;
+      if(F->LRtype == 0) cL->E_phi[3] = Ephi; else cR->E_phi[2] = Ephi;
    }
-   pface *Fs = d->faces[dim - 1];
-   int *fI = d->fI[dim - 1];
-   for(k = kmin; k < kmax; k++) for(j = jmin; j < jmax; j++) {
-      int JK = j + Nfr*k, f;
-      for(f = fI[JK]; f < fI[JK + 1]; f++) {
-         pface *F = &Fs[f];
-         double *gL = (dim == 1 ? d->gradr : d->gradz) + (size_t)F->L*nq;
-         double *gR = (dim == 1 ? d->gradr : d->gradz) + (size_t)F->R*nq;
-         double phiL = d->piph[F->L] - .5*d->dphi[F->L], phiR = d->piph[F->R] - .5*d->dphi[F->R];
-         double dpL = get_signed_dp(d, F->cm[1], phiL), dpR = get_signed_dp(d, phiR, F->cm[1]);
-         double primL[MAXQ], primR[MAXQ];
-         for(q = 0; q < nq; q++) {
-            primL[q] = P(d, F->L)[q] + gL[q]*F->dxL + d->gradp[(size_t)F->L*nq + q]*dpL;
-            primR[q] = P(d, F->R)[q] - gR[q]*F->dxR - d->gradp[(size_t)F->R*nq + q]*dpR;
+}
+static void phi_flux(double dt)
+{
+   int jmin, jmax, kmin, kmax, j, k, i;
+   if(D->mhd && D->ct) {
+      jmin = D->NgRa == 0 ? 0 : D->NgRa - 1; jmax = D->NgRb == 0 ? D->Nr : D->Nr - D->NgRb + 1;
+      kmin = D->NgZa == 0 ? 0 : D->NgZa - 1; kmax = D->NgZb == 0 ? D->Nz : D->Nz - D->NgZb + 1;
+   } else {
+      jmin = D->NgRa; jmax = D->Nr - D->NgRb; kmin = D->NgZa; kmax = D->Nz - D->NgZb;
+   }
+   for(k = kmin; k < kmax; k++) {
+      double zp = D->zk[k], zm = D->zk[k - 1], z = centroid(zp, zm, 2);
+      for(j = jmin; j < jmax; j++) {
+         double rp = D->rj[j], rm = D->rj[j - 1], r = centroid(rp, rm, 1);
+         int jk = j + D->Nr*k, Np = D->Np[jk];
+         pcell *cp = D->ring[jk];
+         for(i = 0; i < Np; i++) {
+            int ip = i < Np - 1 ? i + 1 : 0;
+            double phi = cp[i].piph;
+            double xp[3] = {rp, phi, zp}, xm[3] = {rm, phi, zm};
+            double dA = get_dA(xp, xm, 0);
+            double x[3] = {r, phi, z};
+            riemann_phi(&cp[i], &cp[ip], x, dA*dt);
          }
-         double n[3] = {0.0, 0.0, 0.0};
-         if(dim == 1) n[0] = 1.0; else n[2] = 1.0;
-         solve_riemann(d, primL, primR, U(d, F->L), U(d, F->R), F->cm, n, 0.0, F->dA*dt);
+      }
+   }
+}
+static void trans_flux(double dt, int dim)
+{
+   int jmin, jmax, kmin, kmax, Nfr, j, k;
+   int ctx = D->mhd && D->ct;
+   if(dim == 1) {
+      Nfr = D->Nr - 1;
+      jmin = D->NgRa == 0 ? 0 : D->NgRa - 1; jmax = D->NgRb == 0 ? D->Nr - 1 : D->Nr - D->NgRb;
+      if(ctx) { kmin = D->NgZa == 0 ? 0 : D->NgZa - 1; kmax = D->NgZb == 0 ? D->Nz : D->Nz - D->NgZb + 1; }
+      else { kmin = D->NgZa; kmax = D->Nz - D->NgZb; }
+   } else {
+      Nfr = D->Nr;
+      if(ctx) { jmin = D->NgRa == 0 ? 0 : D->NgRa - 1; jmax = D->NgRb == 0 ? D->Nr : D->Nr - D->NgRb + 1; }
+      else { jmin = D->NgRa; jmax = D->Nr - D->NgRb; }
+      kmin = D->NgZa == 0 ? 0 : D->NgZa - 1; kmax = D->NgZb == 0 ? D->Nz - 1 : D->Nz - D->NgZb;
+   }
+   int *fI = D->fI[dim - 1];
+   for(k = kmin; k < kmax; k++) for(j = jmin; j < jmax; j++) {
+      int JK = j + Nfr*k;
+      for(int f = fI[JK]; f < fI[JK + 1]; f++) riemann_trans(&D->faces[dim - 1][f], dt, dim);
+   }
+}
+
+/* ---- constrained transport: bfields.c ------------------------------------------ */
+static void B_faces_to_cells(int type)
+{
+   int Nr = D->Nr, Nz = D->Nz, j, k, i, n;
+   for(j = 0; j < Nr; j++) for(k = 0; k < Nz; k++) {
+      int jk = j + Nr*k;
+      for(i = 0; i < D->Np[jk]; i++) {
+         pcell *c = &D->ring[jk][i];
+         c->tempDoub = 0.0;
+         if(type == 0) { c->prim[BRR] = 0.0; c->prim[BPP] = 0.0; c->prim[BZZ] = 0.0; }
+         else { c->cons[BRR] = 0.0; c->cons[BPP] = 0.0; c->cons[BZZ] = 0.0; }
+      }
+   }
+   int Nf = D->fI[0][D->ntracks[0]];
+   for(n = 0; n < Nf; n++) {
+      pface *f = &D->faces[0][n];
+      double Phi = f->LRtype == 0 ? f->L->Phi[2] : f->R->Phi[1];
+      f->L->tempDoub += f->dA;
+      f->R->tempDoub += f->dA;
+      if(type == 0) { f->L->prim[BRR] += Phi; f->R->prim[BRR] += Phi; }
+      else { f->L->cons[BRR] += Phi; f->R->cons[BRR] += Phi; }
+   }
+   for(j = 0; j < Nr; j++) for(k = 0; k < Nz; k++) {
+      int jk = j + Nr*k;
+      for(i = 0; i < D->Np[jk]; i++) {
+         int im = i == 0 ? D->Np[jk] - 1 : i - 1;
+         pcell *c = &D->ring[jk][i], *cm = &D->ring[jk][im];
+         double xp[3] = {D->rj[j], c->piph, D->zk[k]}, xm[3] = {D->rj[j - 1], cm->piph, D->zk[k - 1]};
+         double x[3];
+         centroid_arr(xp, xm, x);
+         double dA = get_dA(xp, xm, 0), dV = get_dV(xp, xm);
+         if(type == 0) {
+            c->prim[BRR] /= c->tempDoub;
+            c->prim[BPP] = .5*(c->Phi[0] + cm->Phi[0])/dA;
+         } else {
+            double rfac = 1.0/x[0], hr = 1.0, hp = x[0];
+            c->cons[BRR] *= dV*rfac/(c->tempDoub*hr);
+            c->cons[BPP] = .5*(c->Phi[0] + cm->Phi[0])*dV/(dA*hp);
+         }
+      }
+   }
+   if(Nz > 1) {
+      for(j = 0; j < Nr; j++) for(k = 0; k < Nz; k++) {
+         int jk = j + Nr*k;
+         for(i = 0; i < D->Np[jk]; i++) D->ring[jk][i].tempDoub = 0.0;
+      }
+      int Nfz = D->fI[1][D->ntracks[1]];
+      for(n = 0; n < Nfz; n++) {
+         pface *f = &D->faces[1][n];
+         double Phi = f->LRtype == 0 ? f->L->Phi[4] : f->R->Phi[3];
+         f->L->tempDoub += f->dA;
+         f->R->tempDoub += f->dA;
+         if(type == 0) { f->L->prim[BZZ] += Phi; f->R->prim[BZZ] += Phi; }
+         else { f->L->cons[BZZ] += Phi; f->R->cons[BZZ] += Phi; }
+      }
+      for(j = 0; j < Nr; j++) for(k = 0; k < Nz; k++) {
+         int jk = j + Nr*k;
+         for(i = 0; i < D->Np[jk]; i++) {
+            int im = i == 0 ? D->Np[jk] - 1 : i - 1;
+            pcell *c = &D->ring[jk][i], *cm = &D->ring[jk][im];
+            double xp[3] = {D->rj[j], c->piph, D->zk[k]}, xm[3] = {D->rj[j - 1], cm->piph, D->zk[k - 1]};
+            double dV = get_dV(xp, xm);
+            if(type == 0) c->prim[BZZ] /= c->tempDoub;
+            else c->cons[BZZ] *= dV*1.0/(c->tempDoub*1.0);
+         }
       }
    }
 }
 
-/* ---- cell loops: misc.c ---------------------------------------------------------- */
-static void set_wcell(port_domain *d)
+static void initial(double *prim, const double *x);
+
+static void set_B_fields(void)
 {
-   int jk, i;
-   for(jk = 0; jk < d->Nr*d->Nz; jk++) {
-      long o = d->off[jk];
-      int Np = d->Np[jk];
-      for(i = 0; i < Np; i++) {
-         double w = 0.0;
-         if(d->par.Mesh_Motion) w = .5*(P(d, o + i)[UPP] + P(d, o + (i + 1)%Np)[UPP]);
-         d->wiph[o + i] = w;
+   int i, j, k, n;
+   for(k = 0; k < D->Nz; k++) {
+      double z = centroid(D->zk[k], D->zk[k - 1], 2);
+      for(j = 0; j < D->Nr; j++) {
+         double r = centroid(D->rj[j], D->rj[j - 1], 1);
+         int jk = j + D->Nr*k;
+         for(i = 0; i < D->Np[jk]; i++) {
+            pcell *c = &D->ring[jk][i];
+            double phip = c->piph, phim = phip - c->dphi;
+            double xp[3] = {D->rj[j], phip, D->zk[k]}, xm[3] = {D->rj[j - 1], phim, D->zk[k - 1]};
+            double x[3] = {r, phip, z};
+            double prim[MAXQ];
+            initial(prim, x);
+            c->Phi[0] = prim[BPP]*get_dA(xp, xm, 0);
+         }
       }
-      if(d->par.Mesh_Motion == 3) {
+   }
+   build_faces(1);
+   for(n = 0; n < D->fI[0][D->ntracks[0]]; n++) {
+      pface *f = &D->faces[0][n];
+      double prim[MAXQ];
+      initial(prim, f->cm);
+      double Phi = prim[BRR]*f->dA;
+      if(f->LRtype == 0) f->L->Phi[2] = Phi; else f->R->Phi[1] = Phi;
+   }
+   if(D->Nz > 1) {
+      build_faces(2);
+      for(n = 0; n < D->fI[1][D->ntracks[1]]; n++) {
+         pface *f = &D->faces[1][n];
+         double prim[MAXQ];
+         initial(prim, f->cm);
+         double Phi = prim[BZZ]*f->dA;
+         if(f->LRtype == 0) f->L->Phi[4] = Phi; else f->R->Phi[3] = Phi;
+      }
+   }
+   B_faces_to_cells(0);
+   B_faces_to_cells(1);
+}
+
+static void avg_Efields(void)
+{
+   int Nr = D->Nr, Nz = D->Nz, j, k, i, n, d;
+   for(j = 0; j < Nr; j++) for(k = 0; k < Nz; k++) {
+      int jk = j + Nr*k;
+      for(i = 0; i < D->Np[jk]; i++) {
+         pcell *c = &D->ring[jk][i], *cp = &D->ring[jk][(i + 1)%D->Np[jk]];
+         for(int h = 0; h < 2; h++) {
+            int a = 4*h;
+            double El = .5*(c->E[a + 0] + cp->E[a + 2]), Er = .5*(c->E[a + 1] + cp->E[a + 3]);
+            c->E[a + 0] = El; c->E[a + 1] = Er; cp->E[a + 2] = El; cp->E[a + 3] = Er;
+            double Bl = .5*(c->B[a + 0] + cp->B[a + 2]), Br = .5*(c->B[a + 1] + cp->B[a + 3]);
+            c->B[a + 0] = Bl; c->B[a + 1] = Br; cp->B[a + 2] = Bl; cp->B[a + 3] = Br;
+         }
+      }
+   }
+   for(d = 0; d < 2; d++) {
+      if(d == 1 && Nz <= 1) break;
+      int a = 4*d;
+      int Nf = D->fI[d][D->ntracks[d]];
+      pface *Fs = D->faces[d];
+      for(n = 0; n < Nf; n++) {
+         pface *f = &Fs[n];
+         pcell *c1 = f->LRtype == 0 ? f->L : f->R, *c2 = f->LRtype == 0 ? f->R : f->L;
+         double dp1 = get_dp(c2->piph, c1->piph);
+         double dp2 = c2->dphi - dp1;
+         if(f->LRtype == 0) {
+            double Eavg = (dp2*c2->E[a + 0] + dp1*c2->E[a + 2])/(dp1 + dp2);
+            double Bavg = (dp2*c2->B[a + 0] + dp1*c2->B[a + 2])/(dp1 + dp2);
+            f->E = .5*(f->L->E[a + 1] + Eavg);
+            f->B = .5*(f->L->B[a + 1] + Bavg);
+         } else {
+            double Eavg = (dp2*c2->E[a + 1] + dp1*c2->E[a + 3])/(dp1 + dp2);
+            double Bavg = (dp2*c2->B[a + 1] + dp1*c2->B[a + 3])/(dp1 + dp2);
+            f->E = .5*(f->R->E[a + 0] + Eavg);
+            f->B = .5*(f->R->B[a + 0] + Bavg);
+         }
+      }
+      for(n = 0; n < Nf; n++) {
+         pface *f = &Fs[n];
+         if(f->LRtype == 0) { f->L->E[a + 1] = f->E; f->L->B[a + 1] = f->B; }
+         else { f->R->E[a + 0] = f->E; f->R->B[a + 0] = f->B; }
+         f->E = 0.0; f->B = 0.0;
+      }
+   }
+   for(j = 0; j < Nr; j++) for(k = 0; k < Nz; k++) {
+      int jk = j + Nr*k;
+      for(i = 0; i < D->Np[jk]; i++) {
+         pcell *c = &D->ring[jk][i], *cp = &D->ring[jk][(i + 1)%D->Np[jk]];
+         cp->E[2] = c->E[0]; cp->E[3] = c->E[1]; cp->B[2] = c->B[0]; cp->B[3] = c->B[1];
+         cp->E[6] = c->E[4]; cp->E[7] = c->E[5]; cp->B[6] = c->B[4]; cp->B[7] = c->B[5];
+      }
+   }
+}
+static void subtract_advective_B_fluxes(void)
+{
+   for(int k = 0; k < D->Nz; k++) for(int j = 0; j < D->Nr; j++) {
+      int jk = j + D->Nr*k;
+      double xp[3] = {D->rj[j], 0.0, D->zk[k]}, xm[3] = {D->rj[j - 1], 0.0, D->zk[k - 1]};
+      double xc[3];
+      centroid_arr(xp, xm, xc);
+      double hL = xm[0], hR = xp[0], hD = xc[0], hU = xc[0];
+      for(int i = 0; i < D->Np[jk]; i++) {
+         pcell *c = &D->ring[jk][i];
+         double wm = c->wiph, wp = c->wiph;
+         c->E[0] -= hL*wm*c->B[0];
+         c->E[1] -= hR*wp*c->B[1];
+         c->E[4] += hD*wm*c->B[4];
+         c->E[5] += hU*wp*c->B[5];
+      }
+   }
+}
+static int phi_switch(double dphi, int mode)
+{
+   while(dphi > .5*D->Pmax) dphi -= D->Pmax;
+   while(dphi < -.5*D->Pmax) dphi += D->Pmax;
+   if(mode == 1) dphi = -dphi;
+   return dphi > 0. ? 1 : 0;
+}
+static int get_which4(double phi, double phiR, double phiU, double phiUR, int *LR_alt,
+                      int *UD_alt, int mode)
+{
+   int LR_D = phi_switch(phi - phiR, mode);
+   int LR_U = phi_switch(phiU - phiUR, mode);
+   double phi1 = LR_D ? phiR : phi, phi2 = LR_U ? phiUR : phiU;
+   int UD = phi_switch(phi1 - phi2, mode);
+   int w4 = UD == 0 ? (LR_D == 0 ? 0 : 1) : (LR_U == 0 ? 2 : 3);
+   if(mode == 0) {
+      *LR_alt = (w4 == 0 || w4 == 1) ? LR_U : LR_D;
+      if(w4 == 0 || w4 == 2) *UD_alt = phi_switch(phiR - phiUR, mode);
+      else *UD_alt = phi_switch(phi - phiU, mode);
+   }
+   return w4;
+}
+static void make_edge_adjust(double dt)
+{
+   int Nr = D->Nr, Nz = D->Nz, i, j, k, jk;
+   int *I0 = (int *)malloc(sizeof(int)*Nr*Nz);
+   for(jk = 0; jk < Nr*Nz; jk++) {
+      int found = 0, quad_prev = 0;
+      for(i = 0; i < D->Np[jk] && !found; i++) {
+         double convert = 2.*M_PI/D->Pmax;
+         double ph = D->ring[jk][i].piph;
+         double sn = sin(ph*convert), cs = cos(ph*convert);
+         if(sn > 0. && cs > 0. && quad_prev) { found = 1; I0[jk] = i; }
+         else if(sn < 0. && cs > 0.) quad_prev = 1;
+      }
+      if(!found) I0[jk] = 0;
+   }
+   for(k = 0; k < Nz - 1; k++) for(j = 0; j < Nr - 1; j++) {
+      int a = j + Nr*k, b = j + 1 + Nr*k, u = j + Nr*(k + 1), ur = j + 1 + Nr*(k + 1);
+      double xp[3] = {D->rj[j], 0.0, D->zk[k]}, xm[3] = {D->rj[j], 0.0, D->zk[k]};
+      int i0 = I0[a], iR = I0[b], iU = I0[u], iUR = I0[ur];
+      int Ne = D->Np[a] + D->Np[b] + D->Np[u] + D->Np[ur];
+      for(int e = 0; e < Ne; e++) {
+         pcell *c = &D->ring[a][i0], *cR = &D->ring[b][iR], *cU = &D->ring[u][iU], *cUR = &D->ring[ur][iUR];
+         int LR_alt, UD_alt;
+         int w4 = get_which4(c->piph, cR->piph, cU->piph, cUR->piph, &LR_alt, &UD_alt, 0);
+         int w4b = get_which4(c->piph - c->dphi, cR->piph - cR->dphi, cU->piph - cU->dphi,
+                              cUR->piph - cUR->dphi, NULL, NULL, 1);
+         double *PhiL, *PhiR, *PhiU, *PhiD, E;
+         if(w4 == 0) {
+            PhiL = c->Phi + 4; PhiD = c->Phi + 2;
+            E = .25*(c->E_phi[3] + c->E_phi[1]);
+            if(LR_alt == 0) { PhiU = cU->Phi + 2; E += .25*cU->E_phi[1]; }
+            else { PhiU = cUR->Phi + 1; E += .25*cUR->E_phi[0]; }
+            if(UD_alt == 0) { PhiR = cR->Phi + 4; E += .25*cR->E_phi[3]; }
+            else { PhiR = cUR->Phi + 3; E += .25*cUR->E_phi[2]; }
+         } else if(w4 == 1) {
+            PhiR = cR->Phi + 4; PhiD = cR->Phi + 1;
+            E = .25*(cR->E_phi[3] + cR->E_phi[0]);
+            if(LR_alt == 0) { PhiU = cU->Phi + 2; E += .25*cU->E_phi[1]; }
+            else { PhiU = cUR->Phi + 1; E += .25*cUR->E_phi[0]; }
+            if(UD_alt == 0) { PhiL = c->Phi + 4; E += .25*c->E_phi[3]; }
+            else { PhiL = cU->Phi + 3; E += .25*cU->E_phi[2]; }
+         } else if(w4 == 2) {
+            PhiL = cU->Phi + 3; PhiU = cU->Phi + 2;
+            E = .25*(cU->E_phi[2] + cU->E_phi[1]);
+            if(LR_alt == 0) { PhiD = c->Phi + 2; E += .25*c->E_phi[1]; }
+            else { PhiD = cR->Phi + 1; E += .25*cR->E_phi[0]; }
+            if(UD_alt == 0) { PhiR = cR->Phi + 4; E += .25*cR->E_phi[3]; }
+            else { PhiR = cUR->Phi + 3; E += .25*cUR->E_phi[2]; }
+         } else {
+            PhiR = cUR->Phi + 3; PhiU = cUR->Phi + 1;
+            E = .25*(cUR->E_phi[2] + cUR->E_phi[0]);
+            if(LR_alt == 0) { PhiD = c->Phi + 2; E += .25*c->E_phi[1]; }
+            else { PhiD = cR->Phi + 1; E += .25*cR->E_phi[0]; }
+            if(UD_alt == 0) { PhiL = c->Phi + 4; E += .25*c->E_phi[3]; }
+            else { PhiL = cU->Phi + 3; E += .25*cU->E_phi[2]; }
+         }
+         pcell *top = w4 == 0 ? c : w4 == 1 ? cR : w4 == 2 ? cU : cUR;
+         pcell *bot = w4b == 0 ? c : w4b == 1 ? cR : w4b == 2 ? cU : cUR;
+         xp[1] = top->piph;
+         xm[1] = bot->piph - bot->dphi;
+         double Edldt = E*get_dL(xp, xm, 0)*dt;
+         *PhiL -= Edldt; *PhiR += Edldt; *PhiU -= Edldt; *PhiD += Edldt;
+         if(w4 == 0) { if(++i0 == D->Np[a]) i0 = 0; }
+         else if(w4 == 1) { if(++iR == D->Np[b]) iR = 0; }
+         else if(w4 == 2) { if(++iU == D->Np[u]) iU = 0; }
+         else { if(++iUR == D->Np[ur]) iUR = 0; }
+      }
+   }
+   free(I0);
+}
+static void update_B_fluxes(double dt)
+{
+   for(int d = 0; d < 2; d++) {
+      if(d == 1 && D->Nz <= 1) break;
+      pface *Fs = D->faces[d];
+      int *Nf = D->fI[d];
+      int n0 = 0;
+      for(int jk = 0; jk < D->ntracks[d]; jk++) {
+         int cnt = Nf[jk] - n0;
+         for(int n = 0; n < cnt; n++) {
+            pface *f = Fs + n0 + n, *fp = Fs + n0 + (n + 1 == cnt ? 0 : n + 1);
+            double E, dl = f->dl;
+            if(d == 0) {
+               if(f->LRtype == 0) { E = f->L->E[1]; f->L->Phi[2] -= E*dl*dt; f->L->Phi[0] += E*dl*dt; }
+               else { E = f->R->E[0]; f->R->Phi[1] -= E*dl*dt; f->R->Phi[0] -= E*dl*dt; }
+               if(fp->LRtype == 0) fp->L->Phi[2] += E*dl*dt; else fp->R->Phi[1] += E*dl*dt;
+            } else {
+               if(f->LRtype == 0) { E = f->L->E[5]; f->L->Phi[4] += E*dl*dt; f->L->Phi[0] -= E*dl*dt; }
+               else { E = f->R->E[4]; f->R->Phi[3] += E*dl*dt; f->R->Phi[0] += E*dl*dt; }
+               if(fp->LRtype == 0) fp->L->Phi[4] -= E*dl*dt; else fp->R->Phi[3] -= E*dl*dt;
+            }
+         }
+         n0 = Nf[jk];
+      }
+   }
+   if(D->Nz > 1) make_edge_adjust(dt);
+}
+static void check_flipped(int d)
+{
+   pface *Fs = D->faces[d];
+   int *fI = D->fI[d], n0 = 0;
+   for(int jk = 0; jk < D->ntracks[d]; jk++) {
+      int cnt = fI[jk] - n0;
+      for(int n = 0; n < cnt; n++) {
+         pface *f = Fs + n0 + n, *fp = Fs + n0 + (n + 1 == cnt ? 0 : n + 1);
+         double pm = f->LRtype == 0 ? f->L->piph : f->R->piph;
+         double pp = fp->LRtype == 0 ? fp->L->piph : fp->R->piph;
+         if(get_signed_dp(pp, pm) < 0.) fp->flip_flag = 1;
+      }
+      n0 = fI[jk];
+   }
+}
+static void phi_ptr(pface *f, double **P, double **RK, int d)
+{
+   int lo = d == 0 ? 2 : 4, hi = d == 0 ? 1 : 3;
+   if(f->LRtype == 0) { *P = &f->L->Phi[lo]; *RK = &f->L->RK_Phi[lo]; }
+   else { *P = &f->R->Phi[hi]; *RK = &f->R->RK_Phi[hi]; }
+}
+static void flip_fluxes(int d)
+{
+   pface *Fs = D->faces[d];
+   int *fI = D->fI[d], n0 = 0;
+   for(int jk = 0; jk < D->ntracks[d]; jk++) {
+      int cnt = fI[jk] - n0;
+      for(int n = 0; n < cnt; n++) {
+         pface *f = Fs + n0 + n;
+         if(!f->flip_flag) continue;
+         pface *fp = Fs + n0 + (n + 1 == cnt ? 0 : n + 1);
+         pface *fm = Fs + n0 + (n == 0 ? cnt - 1 : n - 1);
+         double *P, *Pm, *Pp, *RP, *RPm, *RPp;
+         phi_ptr(f, &P, &RP, d);
+         phi_ptr(fm, &Pm, &RPm, d);
+         phi_ptr(fp, &Pp, &RPp, d);
+         double Phi = *P, RPhi = *RP;
+         *P = *Pm + Phi; *RP = *RPm + RPhi;
+         *Pm = -Phi; *RPm = -RPhi;
+         *Pp = *Pp + Phi; *RPp = *RPp + RPhi;
+         f->LRtype = !f->LRtype;
+         fm->LRtype = !fm->LRtype;
+      }
+      n0 = fI[jk];
+   }
+}
+
+/* ---- cell loops: misc.c ------------------------------------------------------------- */
+static void set_wcell(void)
+{
+   for(int jk = 0; jk < D->Nr*D->Nz; jk++) {
+      int Np = D->Np[jk];
+      for(int i = 0; i < Np; i++) {
          double w = 0.0;
-         for(i = 0; i < Np; i++) w += d->wiph[o + i];
+         if(D->par.Mesh_Motion) w = .5*(D->ring[jk][i].prim[UPP] + D->ring[jk][(i + 1)%Np].prim[UPP]);
+         D->ring[jk][i].wiph = w;
+      }
+      if(D->par.Mesh_Motion == 3) {
+         double w = 0.0;
+         for(int i = 0; i < Np; i++) w += D->ring[jk][i].wiph;
          w /= (double)Np;
-         for(i = 0; i < Np; i++) d->wiph[o + i] = w;
+         for(int i = 0; i < Np; i++) D->ring[jk][i].wiph = w;
       }
    }
 }
-static void calc_dp(port_domain *d)
+static void calc_dp(void)
 {
-   int jk, i;
-   for(jk = 0; jk < d->Nr*d->Nz; jk++) {
-      long o = d->off[jk];
-      int Np = d->Np[jk];
-      for(i = 0; i < Np; i++) {
-         int im = i == 0 ? Np - 1 : i - 1;
-         d->dphi[o + i] = get_dp(d, d->piph[o + i], d->piph[o + im]);
-      }
+   for(int jk = 0; jk < D->Nr*D->Nz; jk++) {
+      int Np = D->Np[jk];
+      for(int i = 0; i < Np; i++)
+         D->ring[jk][i].dphi = get_dp(D->ring[jk][i].piph, D->ring[jk][i == 0 ? Np - 1 : i - 1].piph);
    }
 }
-static void calc_prim(port_domain *d)
+static void calc_prim(void)
 {
-   int j, k, i;
-   for(k = d->NgZa; k < d->Nz - d->NgZb; k++) {
-      double zm = d->zk[k - 1], zp = d->zk[k], z = centroid(zp, zm, 2);
-      for(j = d->NgRa; j < d->Nr - d->NgRb; j++) {
-         int jk = j + d->Nr*k;
-         double rm = d->rj[j - 1], rp = d->rj[j], r = centroid(rp, rm, 1);
-         for(i = 0; i < d->Np[jk]; i++) {
-            long c = d->off[jk] + i;
-            double phip = d->piph[c], phim = phip - d->dphi[c];
+   for(int k = D->NgZa; k < D->Nz - D->NgZb; k++) {
+      double zm = D->zk[k - 1], zp = D->zk[k], z = centroid(zp, zm, 2);
+      for(int j = D->NgRa; j < D->Nr - D->NgRb; j++) {
+         int jk = j + D->Nr*k;
+         double rm = D->rj[j - 1], rp = D->rj[j], r = centroid(rp, rm, 1);
+         for(int i = 0; i < D->Np[jk]; i++) {
+            pcell *c = &D->ring[jk][i];
+            double phip = c->piph, phim = phip - c->dphi;
             double xp[3] = {rp, phip, zp}, xm[3] = {rm, phim, zm};
-            double dV = get_dV(d, xp, xm);
             double x[3] = {r, 0.5*(phim + phip), z};
-            cons2prim(d, U(d, c), P(d, c), x, dV);
+            cons2prim(c->cons, c->prim, x, get_dV(xp, xm));
          }
       }
    }
 }
-static void initial(const port_domain *d, double *prim, const double *x)
+static void initial(double *prim, const double *x)
 {
-   const disco_params *p = &d->par;
-   if(d->mod.initial == DISCO_IC_VORTEX_GAUSS) {
+   const disco_params *p = &D->par;
+   if(D->mod.initial == DISCO_IC_VORTEX_GAUSS) {
       struct disco_ic_vortex_gauss V = {p->initPar1, p->initPar2, p->initPar3, p->initPar4,
                                         p->initPar5, p->Adiabatic_Index};
-      disco_ic_vortex_gauss_eval(&V, prim, x, d->nc, d->nq);
+      disco_ic_vortex_gauss_eval(&V, prim, x, D->nc, D->nq);
    } else {
-      struct disco_ic_disk D;
-      disco_ic_disk_from_params(&D, p->Adiabatic_Index, p->Disk_Mach, p->initPar1, p->initPar2,
+      struct disco_ic_disk Dk;
+      disco_ic_disk_from_params(&Dk, p->Adiabatic_Index, p->Disk_Mach, p->initPar1, p->initPar2,
                                 p->initPar3, p->initPar4, p->initPar5, p->initPar6);
-      if(d->mod.initial == DISCO_IC_DISK_MHD) disco_ic_disk_mhd_eval(&D, prim, x, d->nc, d->nq);
-      else disco_ic_disk_planet_eval(&D, prim, x, d->nc, d->nq);
+      if(D->mod.initial == DISCO_IC_DISK_MHD) disco_ic_disk_mhd_eval(&Dk, prim, x, D->nc, D->nq);
+      else disco_ic_disk_planet_eval(&Dk, prim, x, D->nc, D->nq);
    }
    if(p->RotFrame) prim[UPP] -= p->RotOmega;
 }
 /* Boundary/fixed.c:11-46 (r ghosts) and fixed3d.c via set_cell_init. */
-static void boundary(port_domain *d)
+static void boundary(void)
 {
-   int j, k, i;
-   for(k = 0; k < d->Nz; k++) for(j = 0; j < d->Nr; j++) {
-      int rg = j < d->NgRa || j >= d->Nr - d->NgRb;
-      int zg = k < d->NgZa || k >= d->Nz - d->NgZb;
-      int jk = j + d->Nr*k;
-      for(i = 0; i < d->Np[jk]; i++) {
-         long c = d->off[jk] + i;
+   for(int k = 0; k < D->Nz; k++) for(int j = 0; j < D->Nr; j++) {
+      int rg = j < D->NgRa || j >= D->Nr - D->NgRb;
+      int zg = k < D->NgZa || k >= D->Nz - D->NgZb;
+      int jk = j + D->Nr*k;
+      for(int i = 0; i < D->Np[jk]; i++) {
+         pcell *c = &D->ring[jk][i];
          double x[3];
-         if(d->mod.boundary == DISCO_BC_FIXED) {
-            if(!rg || d->Nr <= 1) continue;
-            x[0] = .5*(d->rj[j] + d->rj[j - 1]);
-            x[1] = d->piph[c] - .5*d->dphi[c];
-            x[2] = .5*(d->zk[k] + d->zk[k - 1]);
+         if(D->mod.boundary == DISCO_BC_FIXED) {
+            if(!rg || D->Nr <= 1) continue;
+            x[0] = .5*(D->rj[j] + D->rj[j - 1]);
+            x[1] = c->piph - .5*c->dphi;
+            x[2] = .5*(D->zk[k] + D->zk[k - 1]);
          } else {
-            if(!((rg && d->Nr > 1) || (zg && d->Nz > 1))) continue;
-            x[0] = centroid(d->rj[j], d->rj[j - 1], 1);
-            x[1] = .5*(d->piph[c] + d->piph[c] - d->dphi[c]);
-            x[2] = centroid(d->zk[k], d->zk[k - 1], 2);
+            if(!((rg && D->Nr > 1) || (zg && D->Nz > 1))) continue;
+            double xp[3] = {D->rj[j], c->piph, D->zk[k]}, xm[3] = {D->rj[j - 1], c->piph - c->dphi, D->zk[k - 1]};
+            centroid_arr(xp, xm, x);
          }
-         initial(d, P(d, c), x);
+         initial(c->prim, x);
       }
    }
 }
-static void add_source(port_domain *d, double dt)
+static void add_source(double dt)
 {
-   int j, k, i;
-   for(k = d->NgZa; k < d->Nz - d->NgZb; k++) for(j = d->NgRa; j < d->Nr - d->NgRb; j++) {
-      int jk = j + d->Nr*k;
-      for(i = 0; i < d->Np[jk]; i++) {
-         long c = d->off[jk] + i;
-         double phip = d->piph[c], phim = d->piph[c] - d->dphi[c];
-         double xp[3] = {d->rj[j], phip, d->zk[k]}, xm[3] = {d->rj[j - 1], phim, d->zk[k - 1]};
-         double dV = get_dV(d, xp, xm);
-         source(d, P(d, c), U(d, c), xp, xm, dV*dt);
+   for(int k = D->NgZa; k < D->Nz - D->NgZb; k++) for(int j = D->NgRa; j < D->Nr - D->NgRb; j++) {
+      int jk = j + D->Nr*k;
+      for(int i = 0; i < D->Np[jk]; i++) {
+         pcell *c = &D->ring[jk][i];
+         double phip = c->piph, phim = c->piph - c->dphi;
+         double xp[3] = {D->rj[j], phip, D->zk[k]}, xm[3] = {D->rj[j - 1], phim, D->zk[k - 1]};
+         double dV = get_dV(xp, xm);
+         if(D->mhd) m_source(c->prim, c->cons, xp, xm, dV*dt);
+         else e_source(c->prim, c->cons, xp, xm, dV*dt);
+         for(int p = 0; p < D->Npl; p++) planet_src(&D->pl[p], c->prim, c->cons, xp, xm, dV*dt);
       }
    }
 }
 
-static void onestep(port_domain *d, double RK, double dt, int first)
+static void onestep(double RK, double dt, int first)
 {
    long c;
-   int q, nq = d->nq;
-   if(first) set_wcell(d);
-   for(c = 0; c < d->N; c++)
-      for(q = 0; q < nq; q++) U(d, c)[q] = (1. - RK)*U(d, c)[q] + RK*d->RKcons[c*nq + q];
-   plm_phi(d);
-   if(d->Nr > 1) plm_trans(d, 1);
-   if(d->Nz > 1) plm_trans(d, 2);
-   phi_flux(d, dt);
-   if(d->Nr > 1) trans_flux(d, dt, 1);
-   if(d->Nz > 1) trans_flux(d, dt, 2);
-   add_source(d, dt);
-   if(first) for(c = 0; c < d->N; c++) d->piph[c] += d->wiph[c]*dt;
-   for(c = 0; c < d->N; c++) {    /* clean_pi, misc.c:8-26 */
-      double phi = d->piph[c];
-      while(phi > d->Pmax) phi -= d->Pmax;
-      while(phi < 0.0) phi += d->Pmax;
-      d->piph[c] = phi;
+   int q;
+   if(first) set_wcell();
+   for(c = 0; c < D->N; c++) {
+      pcell *x = &D->cells[c];
+      for(q = 0; q < D->nq; q++) x->cons[q] = (1. - RK)*x->cons[q] + RK*x->RKcons[q];
+      if(D->mhd) for(q = 0; q < 5; q++) x->Phi[q] = (1. - RK)*x->Phi[q] + RK*x->RK_Phi[q];
    }
-   calc_dp(d);
-   calc_prim(d);
-   boundary(d);
+   plm_phi();
+   if(D->Nr > 1) { build_faces(1); plm_trans(1); }
+   if(D->Nz > 1) { build_faces(2); plm_trans(2); }
+   phi_flux(dt);
+   if(D->Nr > 1) trans_flux(dt, 1);
+   if(D->Nz > 1) trans_flux(dt, 2);
+   if(D->mhd) { avg_Efields(); subtract_advective_B_fluxes(); update_B_fluxes(dt); }
+   add_source(dt);
+   if(first) {
+      for(c = 0; c < D->N; c++) D->cells[c].piph += D->cells[c].wiph*dt;
+      if(D->mhd) {
+         check_flipped(0); flip_fluxes(0);
+         if(D->Nz > 1) { check_flipped(1); flip_fluxes(1); }
+      }
+   }
+   for(c = 0; c < D->N; c++) {
+      double phi = D->cells[c].piph;
+      while(phi > D->Pmax) phi -= D->Pmax;
+      while(phi < 0.0) phi += D->Pmax;
+      D->cells[c].piph = phi;
+   }
+   calc_dp();
+   if(D->mhd && D->ct) B_faces_to_cells(1);
+   calc_prim();
+   boundary();
 }
 
-static double getmindt(port_domain *d)
+static double getmindt(void)
 {
-   double dt = d->par.maxDT/d->par.CFL;
+   double dt = D->par.maxDT/D->par.CFL;
    if(dt <= 0.0) dt = 1.0e100;
-   int j, k, i;
-   for(k = d->NgZa; k < d->Nz - d->NgZb; k++) for(j = d->NgRa; j < d->Nr - d->NgRb; j++) {
-      int jk = j + d->Nr*k, Np = d->Np[jk];
-      for(i = 0; i < Np; i++) {
-         long c = d->off[jk] + i;
-         double phip = d->piph[c], phim = phip - d->dphi[c];
-         double xp[3] = {d->rj[j], phip, d->zk[k]}, xm[3] = {d->rj[j - 1], phim, d->zk[k - 1]};
-         long cm = d->off[jk] + (i == 0 ? Np - 1 : i - 1);
-         double w = .5*(d->wiph[cm] + d->wiph[c]);
-         double t = mindt(d, P(d, c), w, xp, xm);
+   for(int k = D->NgZa; k < D->Nz - D->NgZb; k++) for(int j = D->NgRa; j < D->Nr - D->NgRb; j++) {
+      int jk = j + D->Nr*k, Np = D->Np[jk];
+      for(int i = 0; i < Np; i++) {
+         pcell *c = &D->ring[jk][i];
+         if(!c->real) continue;
+         double phip = c->piph, phim = phip - c->dphi;
+         double xp[3] = {D->rj[j], phip, D->zk[k]}, xm[3] = {D->rj[j - 1], phim, D->zk[k - 1]};
+         double w = .5*(D->ring[jk][i == 0 ? Np - 1 : i - 1].wiph + c->wiph);
+         double t = mindt(c->prim, w, xp, xm);
          if(dt > t) dt = t;
       }
    }
-   return dt*d->par.CFL;
+   return dt*D->par.CFL;
 }
 
-/* ---- public checker API ------------------------------------------------------- */
+/* ---- public checker API --------------------------------------------------------- */
 port_domain *disco_port_create(const disco_host_domain *h)
 {
-   if(h->mod.hydro != DISCO_HYDRO_EULER) return NULL;
    port_domain *d = (port_domain *)calloc(1, sizeof(*d));
+   D = d;
    d->par = h->par; d->mod = h->mod;
    d->Nr = h->Nr; d->Nz = h->Nz; d->NgRa = h->NgRa; d->NgRb = h->NgRb;
    d->NgZa = h->NgZa; d->NgZb = h->NgZb; d->nq = h->num_q; d->nc = h->mod.num_c;
+   d->mhd = h->mod.hydro == DISCO_HYDRO_MHD;
+   d->ct = d->mhd && h->mod.ct_mode == 2 && h->par.CT;
+   if(d->mhd && (!d->ct || h->par.Riemann_Solver != 2 || h->NgRa == 0 || h->NgRb == 0 ||
+                 h->NgZa == 0 || h->NgZb == 0)) { free(d); return NULL; }
    d->N = h->Ncell; d->Pmax = h->phi_max; d->t = h->t; d->Npl = h->Npl;
+   d->gam = h->par.Adiabatic_Index;
    memcpy(d->pl, h->planets, sizeof d->pl);
-   d->gamma_law = h->par.Adiabatic_Index;
-   d->rho_floor = h->par.Density_Floor; d->p_floor = h->par.Pressure_Floor;
    int R = d->Nr*d->Nz;
    d->Np = (int *)malloc(sizeof(int)*R); memcpy(d->Np, h->Np, sizeof(int)*R);
    d->off = (long *)malloc(sizeof(long)*(R + 1)); memcpy(d->off, h->ring_off, sizeof(long)*(R + 1));
@@ -678,20 +1469,14 @@ port_domain *disco_port_create(const disco_host_domain *h)
    memcpy(rj, h->r_jph, sizeof(double)*(d->Nr + 1));
    memcpy(zk, h->z_kph, sizeof(double)*(d->Nz + 1));
    d->rj = rj + 1; d->zk = zk + 1;
-   long N = d->N;
-   int nq = d->nq;
-   d->piph = (double *)malloc(sizeof(double)*N); memcpy(d->piph, h->piph, sizeof(double)*N);
-   d->dphi = (double *)malloc(sizeof(double)*N); memcpy(d->dphi, h->dphi, sizeof(double)*N);
-   d->wiph = (double *)calloc(N, sizeof(double));
-   d->prim = (double *)calloc((size_t)nq*N, sizeof(double));
-   d->cons = (double *)calloc((size_t)nq*N, sizeof(double));
-   d->RKcons = (double *)calloc((size_t)nq*N, sizeof(double));
-   d->gradp = (double *)calloc((size_t)nq*N, sizeof(double));
-   d->gradr = (double *)calloc((size_t)nq*N, sizeof(double));
-   d->gradz = (double *)calloc((size_t)nq*N, sizeof(double));
+   d->cells = (pcell *)calloc(d->N, sizeof(pcell));
+   d->ring = (pcell **)malloc(sizeof(pcell *)*R);
+   for(int jk = 0; jk < R; jk++) d->ring[jk] = d->cells + d->off[jk];
    d->fI[0] = (int *)malloc(sizeof(int)*((d->Nr - 1)*d->Nz + 2));
    d->fI[1] = (int *)malloc(sizeof(int)*(d->Nr*(d->Nz > 1 ? d->Nz - 1 : 0) + 2));
-   /* setupCells: prim2cons then cons2prim for real cells (domain.c:319-382) */
+   long c;
+   for(c = 0; c < d->N; c++) { d->cells[c].piph = h->piph[c]; d->cells[c].dphi = h->dphi[c]; }
+   /* setupCells (domain.c:283-385) */
    int j, k, i, q;
    for(k = d->NgZa; k < d->Nz - d->NgZb; k++) {
       double z = centroid(d->zk[k], d->zk[k - 1], 2);
@@ -699,34 +1484,48 @@ port_domain *disco_port_create(const disco_host_domain *h)
          double r = centroid(d->rj[j], d->rj[j - 1], 1);
          int jk = j + d->Nr*k;
          for(i = 0; i < d->Np[jk]; i++) {
-            long c = d->off[jk] + i;
-            double phip = d->piph[c], phim = phip - d->dphi[c];
+            pcell *x = &d->ring[jk][i];
+            double phip = x->piph, phim = phip - x->dphi;
             double xp[3] = {d->rj[j], phip, d->zk[k]}, xm[3] = {d->rj[j - 1], phim, d->zk[k - 1]};
-            double dV = get_dV(d, xp, xm);
-            double x[3] = {r, d->piph[c] - .5*d->dphi[c], z};
-            for(q = 0; q < nq; q++) P(d, c)[q] = h->prim[(size_t)q*N + c];
-            prim2cons(d, P(d, c), U(d, c), x, dV);
-            cons2prim(d, U(d, c), P(d, c), x, dV);
+            double X[3] = {r, x->piph - .5*x->dphi, z};
+            for(q = 0; q < d->nq; q++) x->prim[q] = h->prim[(size_t)q*d->N + (x - d->cells)];
+            prim2cons(x->prim, x->cons, X, get_dV(xp, xm));
+            x->real = 1;
          }
       }
    }
-   set_wcell(d);
-   boundary(d);
+   if(d->ct) set_B_fields();
+   for(k = d->NgZa; k < d->Nz - d->NgZb; k++) {
+      double z = centroid(d->zk[k], d->zk[k - 1], 2);
+      for(j = d->NgRa; j < d->Nr - d->NgRb; j++) {
+         double r = centroid(d->rj[j], d->rj[j - 1], 1);
+         int jk = j + d->Nr*k;
+         for(i = 0; i < d->Np[jk]; i++) {
+            pcell *x = &d->ring[jk][i];
+            double phip = x->piph, phim = phip - x->dphi;
+            double xp[3] = {d->rj[j], phip, d->zk[k]}, xm[3] = {d->rj[j - 1], phim, d->zk[k - 1]};
+            double X[3] = {r, x->piph - .5*x->dphi, z};
+            cons2prim(x->cons, x->prim, X, get_dV(xp, xm));
+         }
+      }
+   }
+   set_wcell();
+   boundary();
    return d;
 }
 
 /* timestep.c:7-54 (Timestep 0), preceded by getmindt (main.c:70). */
 double disco_port_step(port_domain *d)
 {
-   double dt = getmindt(d);
-   memcpy(d->RKcons, d->cons, sizeof(double)*d->nq*d->N);
-   if(d->Nr > 1) build_faces(d, 1);
-   if(d->Nz > 1) build_faces(d, 2);
-   onestep(d, 0.0, dt, 1);
+   D = d;
+   double dt = getmindt();
+   for(long c = 0; c < d->N; c++) {
+      memcpy(d->cells[c].RKcons, d->cells[c].cons, sizeof(double)*MAXQ);
+      memcpy(d->cells[c].RK_Phi, d->cells[c].Phi, sizeof(double)*5);
+   }
+   onestep(0.0, dt, 1);
    d->t += dt;
-   if(d->Nr > 1) build_faces(d, 1);
-   if(d->Nz > 1) build_faces(d, 2);
-   onestep(d, 0.5, 0.5*dt, 0);
+   onestep(0.5, 0.5*dt, 0);
    return dt;
 }
 
@@ -736,19 +1535,28 @@ int disco_port_run(port_domain *d, int nsteps)
    return 0;
 }
 
-/* SoA download, same layout as disco_gpu_download. */
+/* SoA download, same layout as disco_gpu_download; Phi may be NULL. */
 void disco_port_state(const port_domain *d, double *piph, double *dphi, double *prim,
                       double *cons, double *t)
 {
    long N = d->N, c;
-   int q, nq = d->nq;
-   if(piph) memcpy(piph, d->piph, sizeof(double)*N);
-   if(dphi) memcpy(dphi, d->dphi, sizeof(double)*N);
-   for(c = 0; c < N; c++) for(q = 0; q < nq; q++) {
-      if(prim) prim[(size_t)q*N + c] = d->prim[c*nq + q];
-      if(cons) cons[(size_t)q*N + c] = d->cons[c*nq + q];
+   for(c = 0; c < N; c++) {
+      const pcell *x = &d->cells[c];
+      if(piph) piph[c] = x->piph;
+      if(dphi) dphi[c] = x->dphi;
+      for(int q = 0; q < d->nq; q++) {
+         if(prim) prim[(size_t)q*N + c] = x->prim[q];
+         if(cons) cons[(size_t)q*N + c] = x->cons[q];
+      }
    }
    if(t) *t = d->t;
+}
+
+void disco_port_phi(const port_domain *d, double *Phi)
+/* per-cell face fluxes Phi[0..4], SoA [5*N] */
+{
+   for(long c = 0; c < d->N; c++)
+      for(int q = 0; q < 5; q++) Phi[(size_t)q*d->N + c] = d->cells[c].Phi[q];
 }
 
 long disco_port_num_real(const port_domain *d)
@@ -763,8 +1571,7 @@ void disco_port_free(port_domain *d)
 {
    if(!d) return;
    free(d->Np); free(d->off); free(d->rj - 1); free(d->zk - 1);
-   free(d->piph); free(d->dphi); free(d->wiph); free(d->prim); free(d->cons);
-   free(d->RKcons); free(d->gradp); free(d->gradr); free(d->gradz);
+   free(d->cells); free(d->ring);
    free(d->faces[0]); free(d->faces[1]); free(d->fI[0]); free(d->fI[1]);
    free(d);
 }

@@ -28,6 +28,7 @@ from dumpio import read_dump  # noqa: E402
 # name -> (config dir, in.par overrides, number of steps)
 CASES = {
     "cfg1_n24": ("configs/cfg1_vortex", {"Num_R": 24}, 10),
+    "cfg2_n12": ("configs/cfg2_mhd_disk", {"Num_R": 12, "Num_Z": 6}, 5),
 }
 
 
@@ -67,7 +68,8 @@ def run_case(name: str, ref: str) -> None:
            "init_cons": ini["cons"], "init_wiph": ini["wiph"],
            "grad_gradp": grd["gradp"], "grad_gradr": grd["gradr"], "grad_gradz": grd["gradz"],
            "run_piph": run["piph"], "run_dphi": run["dphi"], "run_wiph": run["wiph"],
-           "run_prim": run["prim"], "run_cons": run["cons"], "run_t": run["t"]}
+           "run_prim": run["prim"], "run_cons": run["cons"], "run_t": run["t"],
+           "init_Phi": ini["Phi"], "run_Phi": run["Phi"]}
     for key in ("r", "z"):
         fc = grd.get(f"faces_{key}")
         if fc is None:

@@ -57,3 +57,16 @@ def test_port_bit_exact_vs_reference_binary():
     assert np.array_equal(s["piph"], ref["piph"])
     assert np.array_equal(s["cons"][:, real], ref["cons"][:, real])
     shutil.rmtree(td)
+
+
+def test_port_mhd_ct_bit_exact_vs_golden():
+    """3D MHD disk with HLLD and constrained transport: the oracle equals the
+    reference bit for bit (conserved variables, face fluxes, positions)."""
+    g = load_golden("cfg2_n12")
+    h, s = _port_run(write_par(g["par_text"]), os.path.join(ROOT, "configs/cfg2_mhd_disk/Makefile_opt.in"),
+                     int(g["nsteps"]))
+    real = g["real"].astype(bool)
+    assert s["t"] == float(g["run_t"])
+    assert np.array_equal(s["piph"], g["run_piph"])
+    assert np.array_equal(s["cons"][:, real], g["run_cons"][:, real])
+    assert np.array_equal(s["prim"][:, real], g["run_prim"][:, real])
