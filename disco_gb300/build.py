@@ -26,7 +26,7 @@ NVCC_FLAGS = ["-std=c++17", "-O3", GENCODE, "-lineinfo", "-Xcompiler", "-fPIC",
 CC_FLAGS = ["-std=gnu11", "-O2", "-fPIC", "-Wall", "-ffp-contract=off"]
 
 HOST_SOURCES = ["host/disco_host.c"]
-CUDA_SOURCES = ["cuda/disco_gpu.cu"]
+CUDA_SOURCES = ["cuda/disco_gpu.cu", "cuda/disco_gpu_euler.cu", "cuda/disco_gpu_mhd.cu"]
 
 
 def _nvcc() -> str:

@@ -1,0 +1,495 @@
+// Constrained transport (bfields.c) on the device.
+//
+// Per cell: Eraw/Braw[8] edge EMFs and fields (E[8], B[8] of struct cell),
+// Ephi[4] azimuthal-edge EMFs (E_phi), Phi/RKPhi[5] face fluxes (FP64).
+// Face flux ownership follows the reference exactly: the r face ending at
+// cell L's upper phi edge (LRtype 0) stores its flux in L.Phi[2], the one
+// ending at R's upper edge (LRtype 1) in R.Phi[1]; z faces use Phi[4]/[3].
+// Every cell owns exactly one face on each side, the last face of its run
+// in that pair (run_up_e / run_dn_e), so the reference's scatter updates
+// become per-cell gathers.
+#pragma once
+#include "kernels.cuh"
+
+namespace disco {
+
+struct CtState {
+  double* Phi;      // [5*N]
+  double* RKPhi;    // [5*N]
+  double* Efin;     // [4*N]: E0, E1, E4, E5 after averaging and advective subtraction
+  double* Ephi;     // [4*N]
+  unsigned long long* errs;  // [0] edge-order mismatches
+  int last_pair[2]; // index of the last pair of each dimension (skipped by update_B_fluxes)
+};
+
+// ---- RK adjust of Phi + edge gathers (riemann.c:172-212) --------------------
+template <typename R>
+__global__ void k_ct_gather(DevParams P, DevState<R> S, CtState C, double RK, int first) {
+  int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= S.N) return;
+  const int N = S.N;
+#pragma unroll
+  for (int q = 0; q < 5; ++q) {
+    double ph = C.Phi[q * N + c];
+    if (first) C.RKPhi[q * N + c] = ph;
+    else C.Phi[q * N + c] = (1. - RK) * ph + RK * C.RKPhi[q * N + c];
+  }
+  int jk = S.cell_ring[c];
+  int j = jk % P.Nr, k = jk / P.Nr;
+  if (!ring_in_phi_range(P, j, k)) return;
+  double dphic = S.dphi[c];
+  for (int dim = 1; dim <= 2; ++dim) {
+    if (dim == 1 && P.Nr <= 1) continue;
+    if (dim == 2 && P.Nz <= 1) continue;
+    const int d = dim - 1;
+    const int a = 4 * d;
+    int pb = pair_below(P, dim, j, k), pa = pair_above(P, dim, j, k);
+    if (pb >= 0 && pair_in_flux_range(P, dim, pb)) {
+      double e0 = S.Eraw[(a + 0) * N + c], e2 = S.Eraw[(a + 2) * N + c];
+      double b0 = S.Braw[(a + 0) * N + c], b2 = S.Braw[(a + 2) * N + c];
+      int base = S.face_off[d][pb], Nf = S.face_off[d][pb + 1] - base;
+      for_run(S.run_dn_s[d][c], S.run_dn_e[d][c], base, Nf, [&](int f) {
+        double fr = S.fdphi[d][f] / dphic;
+        e0 += .5 * S.fErz[d][f] * fr; e2 += .5 * S.fErz[d][f] * fr;
+        b0 += .5 * S.fBrz[d][f] * fr; b2 += .5 * S.fBrz[d][f] * fr;
+      });
+      S.Eraw[(a + 0) * N + c] = e0; S.Eraw[(a + 2) * N + c] = e2;
+      S.Braw[(a + 0) * N + c] = b0; S.Braw[(a + 2) * N + c] = b2;
+      C.Ephi[(2 * d + 0) * N + c] = S.fEphi[d][S.run_dn_e[d][c]];
+    }
+    if (pa >= 0 && pair_in_flux_range(P, dim, pa)) {
+      double e1 = S.Eraw[(a + 1) * N + c], e3 = S.Eraw[(a + 3) * N + c];
+      double b1 = S.Braw[(a + 1) * N + c], b3 = S.Braw[(a + 3) * N + c];
+      int base = S.face_off[d][pa], Nf = S.face_off[d][pa + 1] - base;
+      for_run(S.run_up_s[d][c], S.run_up_e[d][c], base, Nf, [&](int f) {
+        double fr = S.fdphi[d][f] / dphic;
+        e1 += .5 * S.fErz[d][f] * fr; e3 += .5 * S.fErz[d][f] * fr;
+        b1 += .5 * S.fBrz[d][f] * fr; b3 += .5 * S.fBrz[d][f] * fr;
+      });
+      S.Eraw[(a + 1) * N + c] = e1; S.Eraw[(a + 3) * N + c] = e3;
+      S.Braw[(a + 1) * N + c] = b1; S.Braw[(a + 3) * N + c] = b3;
+      C.Ephi[(2 * d + 1) * N + c] = S.fEphi[d][S.run_up_e[d][c]];
+    }
+  }
+}
+
+// ---- avg_Efields (bfields.c:392-644) + subtract_advective_B_fluxes (:646-690)
+// d1: neighbour average along phi; d2: face average with the interpolated
+// value from the overlapping cell of the other ring; then E -= h w B.
+template <typename R>
+DISCO_D double edge_avg(const CtState& C, const DevState<R>& S, const double* A, int e, int x) {
+  // value of slot e of cell x after the phi-neighbour averaging pass
+  const int N = S.N;
+  int jk = S.cell_ring[x];
+  int off = S.ring_off[jk], Np = S.ring_off[jk + 1] - off;
+  int i = x - off;
+  int xp = off + (i + 1 == Np ? 0 : i + 1), xm = off + (i == 0 ? Np - 1 : i - 1);
+  int h = e & 4, s = e & 3;
+  if (s == 0) return .5 * (A[(h + 0) * N + x] + A[(h + 2) * N + xp]);
+  if (s == 1) return .5 * (A[(h + 1) * N + x] + A[(h + 3) * N + xp]);
+  if (s == 2) return .5 * (A[(h + 0) * N + xm] + A[(h + 2) * N + x]);
+  return .5 * (A[(h + 1) * N + xm] + A[(h + 3) * N + x]);
+}
+
+template <typename R>
+__global__ void k_ct_avg(DevParams P, DevState<R> S, CtState C) {
+  int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= S.N) return;
+  const int N = S.N;
+  int jk = S.cell_ring[c];
+  int j = jk % P.Nr, k = jk / P.Nr;
+  double outE[4], outB[4];
+  // slots: 0 -> E0 (r lower), 1 -> E1 (r upper), 2 -> E4 (z lower), 3 -> E5 (z upper)
+  const int slot_e[4] = {0, 1, 4, 5};
+  for (int s = 0; s < 4; ++s) {
+    outE[s] = edge_avg(C, S, S.Eraw, slot_e[s], c);
+    outB[s] = edge_avg(C, S, S.Braw, slot_e[s], c);
+  }
+  for (int dim = 1; dim <= 2; ++dim) {
+    if (dim == 1 && P.Nr <= 1) continue;
+    if (dim == 2 && P.Nz <= 1) continue;
+    const int d = dim - 1, a = 4 * d;
+    int pa = pair_above(P, dim, j, k), pb = pair_below(P, dim, j, k);
+    if (pa >= 0) {   // LRtype 0 face owned by c (c = L = c1, c2 = R)
+      int f = S.run_up_e[d][c];
+      int c2 = S.fR[d][f];
+      double dp1 = get_dp(S.piph[c2], S.piph[c], P.phi_max);
+      double dp2 = S.dphi[c2] - dp1;
+      double Eavg = (dp2 * edge_avg(C, S, S.Eraw, a + 0, c2) + dp1 * edge_avg(C, S, S.Eraw, a + 2, c2)) / (dp1 + dp2);
+      double Bavg = (dp2 * edge_avg(C, S, S.Braw, a + 0, c2) + dp1 * edge_avg(C, S, S.Braw, a + 2, c2)) / (dp1 + dp2);
+      outE[2 * d + 1] = .5 * (outE[2 * d + 1] + Eavg);
+      outB[2 * d + 1] = .5 * (outB[2 * d + 1] + Bavg);
+    }
+    if (pb >= 0) {   // LRtype 1 face owned by c (c = R = c1, c2 = L)
+      int f = S.run_dn_e[d][c];
+      int c2 = S.fL[d][f];
+      double dp1 = get_dp(S.piph[c2], S.piph[c], P.phi_max);
+      double dp2 = S.dphi[c2] - dp1;
+      double Eavg = (dp2 * edge_avg(C, S, S.Eraw, a + 1, c2) + dp1 * edge_avg(C, S, S.Eraw, a + 3, c2)) / (dp1 + dp2);
+      double Bavg = (dp2 * edge_avg(C, S, S.Braw, a + 1, c2) + dp1 * edge_avg(C, S, S.Braw, a + 3, c2)) / (dp1 + dp2);
+      outE[2 * d + 0] = .5 * (outE[2 * d + 0] + Eavg);
+      outB[2 * d + 0] = .5 * (outB[2 * d + 0] + Bavg);
+    }
+  }
+  const double* rj = S.r_jph + 1;
+  const double* zk = S.z_kph + 1;
+  double hL = rj[j - 1], hR = rj[j];
+  double hC = centroid_r(rj[j], rj[j - 1]);
+  double w = S.wiph[c];
+  C.Efin[0 * N + c] = outE[0] - hL * w * outB[0];
+  C.Efin[1 * N + c] = outE[1] - hR * w * outB[1];
+  C.Efin[2 * N + c] = outE[2] + hC * w * outB[2];
+  C.Efin[3 * N + c] = outE[3] + hC * w * outB[3];
+  (void)zk;
+}
+
+// ---- update_B_fluxes (bfields.c:313-382): Stokes circulation per face --------
+// The reference's loop skips the last pair of each dimension (it visits pair
+// jk-1 at index jk, jk < N_ftracks); that is reproduced.
+template <typename R>
+DISCO_D double face_emf(const DevState<R>& S, const CtState& C, int d, int f) {
+  const int N = S.N;
+  if (S.fLR[d][f] == 0) return C.Efin[(2 * d + 1) * N + S.fL[d][f]];
+  return C.Efin[(2 * d + 0) * N + S.fR[d][f]];
+}
+
+template <typename R>
+__global__ void k_ct_bflux(DevParams P, DevState<R> S, CtState C, double fac) {
+  int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= S.N) return;
+  const int N = S.N;
+  int jk = S.cell_ring[c];
+  int j = jk % P.Nr, k = jk / P.Nr;
+  double dt = fac * S.scal[SC_DT];
+  const double* rj = S.r_jph + 1;
+  const double* zk = S.z_kph + 1;
+  double ph0 = C.Phi[0 * N + c];
+  for (int dim = 1; dim <= 2; ++dim) {
+    if (dim == 1 && P.Nr <= 1) continue;
+    if (dim == 2 && P.Nz <= 1) continue;
+    const int d = dim - 1;
+    double dl = dim == 1 ? (zk[k] - zk[k - 1]) : (rj[j] - rj[j - 1]);
+    double sgn = dim == 1 ? 1.0 : -1.0;   // z faces circulate with the opposite sign
+    int pb = pair_below(P, dim, j, k), pa = pair_above(P, dim, j, k);
+    // lower pair: c is R, owns the LRtype-1 face run_dn_e (slot Phi[1] or Phi[3])
+    if (pb >= 0 && pb != C.last_pair[d]) {
+      int base = S.face_off[d][pb], Nf = S.face_off[d][pb + 1] - base;
+      int f = S.run_dn_e[d][c];
+      int g = f == base ? base + Nf - 1 : f - 1;
+      double Ef = C.Efin[(2 * d + 0) * N + c];
+      double Eg = face_emf(S, C, d, g);
+      int slot = dim == 1 ? 1 : 3;
+      double v = C.Phi[slot * N + c];
+      if (dim == 1) {
+        if (f == base) { v -= Ef * dl * dt; v += Eg * dl * dt; }
+        else { v += Eg * dl * dt; v -= Ef * dl * dt; }
+        ph0 -= Ef * dl * dt;
+      } else {
+        if (f == base) { v += Ef * dl * dt; v -= Eg * dl * dt; }
+        else { v -= Eg * dl * dt; v += Ef * dl * dt; }
+      }
+      C.Phi[slot * N + c] = v;
+      if (dim == 2) ph0 += Ef * dl * dt;
+    }
+    if (pa >= 0 && pa != C.last_pair[d]) {
+      int base = S.face_off[d][pa], Nf = S.face_off[d][pa + 1] - base;
+      int f = S.run_up_e[d][c];
+      int g = f == base ? base + Nf - 1 : f - 1;
+      double Ef = C.Efin[(2 * d + 1) * N + c];
+      double Eg = face_emf(S, C, d, g);
+      int slot = dim == 1 ? 2 : 4;
+      double v = C.Phi[slot * N + c];
+      if (dim == 1) {
+        if (f == base) { v -= Ef * dl * dt; v += Eg * dl * dt; }
+        else { v += Eg * dl * dt; v -= Ef * dl * dt; }
+        ph0 += Ef * dl * dt;
+      } else {
+        if (f == base) { v += Ef * dl * dt; v -= Eg * dl * dt; }
+        else { v -= Eg * dl * dt; v += Ef * dl * dt; }
+        ph0 -= Ef * dl * dt;
+      }
+      C.Phi[slot * N + c] = v;
+    }
+    (void)sgn;
+  }
+  C.Phi[0 * N + c] = ph0;
+}
+
+// ---- make_edge_adjust (bfields.c:888-1127) -------------------------------------
+// The reference walks, for each corner line (r_j, z_k), the four rings around
+// it in phi order (a 4-way merge of their upper cell edges, ties ordered
+// c < cR < cU < cUR) and adds E_phi dl dt to the four faces meeting there.
+// Every walk event advances exactly one cell, so events map one-to-one onto
+// the cells of the four rings: here each thread takes one cell, finds the
+// heads of the other three rings by binary search, and evaluates that event.
+// Contributions from different events to one face are summed with FP64
+// atomics (order may differ from the reference at rounding level).
+DISCO_D int phi_switch(double dphi, double Pmax, int mode) {
+  while (dphi > .5 * Pmax) dphi -= Pmax;
+  while (dphi < -.5 * Pmax) dphi += Pmax;
+  if (mode == 1) dphi = -dphi;
+  return dphi > 0. ? 1 : 0;
+}
+DISCO_D int get_which4(double phi, double phiR, double phiU, double phiUR, int* LR_alt, int* UD_alt,
+                       int mode, double Pmax) {
+  int LR_D = phi_switch(phi - phiR, Pmax, mode);
+  int LR_U = phi_switch(phiU - phiUR, Pmax, mode);
+  double phi1 = LR_D ? phiR : phi, phi2 = LR_U ? phiUR : phiU;
+  int UD = phi_switch(phi1 - phi2, Pmax, mode);
+  int w4 = UD == 0 ? (LR_D == 0 ? 0 : 1) : (LR_U == 0 ? 2 : 3);
+  if (mode == 0) {
+    *LR_alt = (w4 == 0 || w4 == 1) ? LR_U : LR_D;
+    if (w4 == 0 || w4 == 2) *UD_alt = phi_switch(phiR - phiUR, Pmax, mode);
+    else *UD_alt = phi_switch(phi - phiU, Pmax, mode);
+  }
+  return w4;
+}
+
+template <typename R>
+__global__ void k_ct_edge(DevParams P, DevState<R> S, CtState C, double fac) {
+  extern __shared__ double sm[];
+  int q = blockIdx.x;   // quad (j, k): rings j, j+1 at layers k, k+1
+  int j = q % (P.Nr - 1), k = q / (P.Nr - 1);
+  const int N = S.N;
+  int ring[4] = {j + P.Nr * k, j + 1 + P.Nr * k, j + P.Nr * (k + 1), j + 1 + P.Nr * (k + 1)};
+  int off[4], np[4], I0[4], base[4];
+  int tot = 0;
+#pragma unroll
+  for (int x = 0; x < 4; ++x) {
+    off[x] = S.ring_off[ring[x]];
+    np[x] = S.ring_off[ring[x] + 1] - off[x];
+    I0[x] = S.anchor[ring[x]];
+    base[x] = tot;
+    tot += np[x];
+  }
+  double* sp = sm;   // rotated piph of the four rings
+  for (int x = 0; x < 4; ++x)
+    for (int m = threadIdx.x; m < np[x]; m += blockDim.x) sp[base[x] + m] = S.piph[off[x] + (I0[x] + m) % np[x]];
+  __syncthreads();
+  const double Pmax = P.phi_max;
+  int lapoff[4];
+  lapoff[0] = 0;
+#pragma unroll
+  for (int x = 1; x < 4; ++x) {
+    double raw = sp[base[0]] - sp[base[x]];
+    lapoff[x] = raw > .5 * Pmax ? 1 : (raw < -.5 * Pmax ? -1 : 0);
+  }
+  auto key = [&](int x, int m, int& lap, double& ph) {
+    int mm = m % np[x];
+    ph = sp[base[x] + mm];
+    lap = m / np[x] + ((mm > 0 && ph < sp[base[x]]) ? 1 : 0) + lapoff[x];
+  };
+  double dt = fac * S.scal[SC_DT];
+  const double rjj = S.r_jph[j + 1];
+  for (int t = threadIdx.x; t < tot; t += blockDim.x) {
+    int rx = t >= base[3] ? 3 : t >= base[2] ? 2 : t >= base[1] ? 1 : 0;
+    int m = t - base[rx];
+    int lx; double px;
+    key(rx, m, lx, px);
+    int head[4];
+    head[rx] = m;
+#pragma unroll
+    for (int y = 0; y < 4; ++y) {
+      if (y == rx) continue;
+      // number of Y elements ordered before X[m]: (lap, phi, rank) lexicographic
+      int lo = 0, hi = np[y];
+      while (lo < hi) {
+        int mid = (lo + hi) >> 1;
+        int ly; double py;
+        key(y, mid, ly, py);
+        bool before = (ly < lx) || (ly == lx && (py < px || (py == px && y < rx)));
+        if (before) lo = mid + 1; else hi = mid;
+      }
+      head[y] = lo;
+    }
+    int cid[4];
+#pragma unroll
+    for (int y = 0; y < 4; ++y) cid[y] = off[y] + (I0[y] + head[y]) % np[y];
+    double pp[4], pb[4];
+#pragma unroll
+    for (int y = 0; y < 4; ++y) { pp[y] = S.piph[cid[y]]; pb[y] = pp[y] - S.dphi[cid[y]]; }
+    int LR_alt, UD_alt;
+    int w4 = get_which4(pp[0], pp[1], pp[2], pp[3], &LR_alt, &UD_alt, 0, Pmax);
+    int w4b = get_which4(pb[0], pb[1], pb[2], pb[3], nullptr, nullptr, 1, Pmax);
+    if (w4 != rx) { atomicAdd(C.errs, 1ull); continue; }
+    int c = cid[0], cR = cid[1], cU = cid[2], cUR = cid[3];
+    const double* Ep = C.Ephi;
+    double E;
+    double *PhiL, *PhiR, *PhiU, *PhiD;
+    double* Ph = C.Phi;
+    if (w4 == 0) {
+      PhiL = Ph + 4 * N + c; PhiD = Ph + 2 * N + c;
+      E = .25 * (Ep[3 * N + c] + Ep[1 * N + c]);
+      if (LR_alt == 0) { PhiU = Ph + 2 * N + cU; E += .25 * Ep[1 * N + cU]; }
+      else { PhiU = Ph + 1 * N + cUR; E += .25 * Ep[0 * N + cUR]; }
+      if (UD_alt == 0) { PhiR = Ph + 4 * N + cR; E += .25 * Ep[3 * N + cR]; }
+      else { PhiR = Ph + 3 * N + cUR; E += .25 * Ep[2 * N + cUR]; }
+    } else if (w4 == 1) {
+      PhiR = Ph + 4 * N + cR; PhiD = Ph + 1 * N + cR;
+      E = .25 * (Ep[3 * N + cR] + Ep[0 * N + cR]);
+      if (LR_alt == 0) { PhiU = Ph + 2 * N + cU; E += .25 * Ep[1 * N + cU]; }
+      else { PhiU = Ph + 1 * N + cUR; E += .25 * Ep[0 * N + cUR]; }
+      if (UD_alt == 0) { PhiL = Ph + 4 * N + c; E += .25 * Ep[3 * N + c]; }
+      else { PhiL = Ph + 3 * N + cU; E += .25 * Ep[2 * N + cU]; }
+    } else if (w4 == 2) {
+      PhiL = Ph + 3 * N + cU; PhiU = Ph + 2 * N + cU;
+      E = .25 * (Ep[2 * N + cU] + Ep[1 * N + cU]);
+      if (LR_alt == 0) { PhiD = Ph + 2 * N + c; E += .25 * Ep[1 * N + c]; }
+      else { PhiD = Ph + 1 * N + cR; E += .25 * Ep[0 * N + cR]; }
+      if (UD_alt == 0) { PhiR = Ph + 4 * N + cR; E += .25 * Ep[3 * N + cR]; }
+      else { PhiR = Ph + 3 * N + cUR; E += .25 * Ep[2 * N + cUR]; }
+    } else {
+      PhiR = Ph + 3 * N + cUR; PhiU = Ph + 1 * N + cUR;
+      E = .25 * (Ep[2 * N + cUR] + Ep[0 * N + cUR]);
+      if (LR_alt == 0) { PhiD = Ph + 2 * N + c; E += .25 * Ep[1 * N + c]; }
+      else { PhiD = Ph + 1 * N + cR; E += .25 * Ep[0 * N + cR]; }
+      if (UD_alt == 0) { PhiL = Ph + 4 * N + c; E += .25 * Ep[3 * N + c]; }
+      else { PhiL = Ph + 3 * N + cU; E += .25 * Ep[2 * N + cU]; }
+    }
+    double xp1 = pp[w4], xm1 = pb[w4b];
+    double dl = (.5 * (rjj + rjj)) * get_dp(xp1, xm1, Pmax);
+    double Edldt = E * dl * dt;
+    atomicAdd(PhiL, -Edldt);
+    atomicAdd(PhiR, Edldt);
+    atomicAdd(PhiU, -Edldt);
+    atomicAdd(PhiD, Edldt);
+  }
+}
+
+// ---- check_flipped + flip_fluxes (bfields.c:693-814), first substep --------------
+// One block per pair; flags in parallel, then the sequential repair (rare).
+template <typename R>
+__global__ void k_ct_flip(DevParams P, DevState<R> S, CtState C, int dim) {
+  extern __shared__ unsigned char fsm[];
+  const int d = dim - 1;
+  int pair = blockIdx.x;
+  if (pair == C.last_pair[d]) return;   // the reference loops skip the last pair
+  int base = S.face_off[d][pair], Nf = S.face_off[d][pair + 1] - base;
+  signed char* lr = (signed char*)fsm;
+  unsigned char* flag = fsm + Nf;
+  for (int n = threadIdx.x; n < Nf; n += blockDim.x) { lr[n] = S.fLR[d][base + n]; flag[n] = 0; }
+  __syncthreads();
+  for (int n = threadIdx.x; n < Nf; n += blockDim.x) {
+    int f = base + n, np = n + 1 == Nf ? 0 : n + 1, fp = base + np;
+    double pm = lr[n] == 0 ? S.piph[S.fL[d][f]] : S.piph[S.fR[d][f]];
+    double pp = lr[np] == 0 ? S.piph[S.fL[d][fp]] : S.piph[S.fR[d][fp]];
+    if (get_signed_dp(pp, pm, P.phi_max) < 0.) flag[np] = 1;
+  }
+  __syncthreads();
+  if (threadIdx.x != 0) return;
+  const int N = S.N;
+  int lo = d == 0 ? 2 : 4, hi = d == 0 ? 1 : 3;
+  auto slot = [&](int n) -> long long {
+    int f = base + n;
+    return lr[n] == 0 ? (long long)lo * N + S.fL[d][f] : (long long)hi * N + S.fR[d][f];
+  };
+  bool any = false;
+  for (int n = 0; n < Nf; ++n) {
+    if (!flag[n]) continue;
+    any = true;
+    int np = n + 1 == Nf ? 0 : n + 1, nm = n == 0 ? Nf - 1 : n - 1;
+    long long s = slot(n), sm_ = slot(nm), sp = slot(np);
+    double Phi = C.Phi[s], RPhi = C.RKPhi[s];
+    C.Phi[s] = C.Phi[sm_] + Phi; C.RKPhi[s] = C.RKPhi[sm_] + RPhi;
+    C.Phi[sm_] = -Phi; C.RKPhi[sm_] = -RPhi;
+    C.Phi[sp] = C.Phi[sp] + Phi; C.RKPhi[sp] = C.RKPhi[sp] + RPhi;
+    lr[n] = !lr[n];
+    lr[nm] = !lr[nm];
+  }
+  if (any)
+    for (int n = 0; n < Nf; ++n) S.fLR[d][base + n] = lr[n];
+}
+
+// ---- B_faces_to_cells type 1 (bfields.c:88-309): cell B from face fluxes ---------
+template <typename R, int NQ>
+__global__ void k_ct_b2c(DevParams P, DevState<R> S, CtState C, int prim_out) {
+  int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= S.N) return;
+  const int N = S.N;
+  int jk = S.cell_ring[c];
+  int j = jk % P.Nr, k = jk / P.Nr;
+  if (!prim_out && !is_real(P, j, k)) return;
+  int off = S.ring_off[jk], Np = S.ring_off[jk + 1] - off;
+  int i = c - off;
+  int cm = off + (i == 0 ? Np - 1 : i - 1);
+  const double* rj = S.r_jph + 1;
+  const double* zk = S.z_kph + 1;
+  double xp0 = rj[j], xm0 = rj[j - 1], xp2 = zk[k], xm2 = zk[k - 1];
+  double xp1 = S.piph[c], xm1 = S.piph[cm];
+  double x0 = centroid_r(xp0, xm0);
+  double dA = (xp0 - xm0) * (xp2 - xm2);
+  double dV = (.5 * (xp0 + xm0)) * (xp0 - xm0) * get_dp(xp1, xm1, P.phi_max) * (xp2 - xm2);
+  double sums[2] = {0, 0}, areas[2] = {0, 0};
+  for (int dim = 1; dim <= 2; ++dim) {
+    if (dim == 1 && P.Nr <= 1) continue;
+    if (dim == 2 && P.Nz <= 1) continue;
+    const int d = dim - 1;
+    int lo = d == 0 ? 2 : 4, hi = d == 0 ? 1 : 3;
+    int pb = pair_below(P, dim, j, k), pa = pair_above(P, dim, j, k);
+    auto visit = [&](int f) {
+      double ph = S.fLR[d][f] == 0 ? C.Phi[lo * N + S.fL[d][f]] : C.Phi[hi * N + S.fR[d][f]];
+      areas[d] += S.fdA[d][f];
+      sums[d] += ph;
+    };
+    if (pb >= 0) {
+      int base = S.face_off[d][pb], Nf = S.face_off[d][pb + 1] - base;
+      for_run(S.run_dn_s[d][c], S.run_dn_e[d][c], base, Nf, visit);
+    }
+    if (pa >= 0) {
+      int base = S.face_off[d][pa], Nf = S.face_off[d][pa + 1] - base;
+      for_run(S.run_up_s[d][c], S.run_up_e[d][c], base, Nf, visit);
+    }
+  }
+  double Bphi = .5 * (C.Phi[c] + C.Phi[cm]);
+  if (prim_out) {   // type 0 (primitive B), used once at set-up
+    S.prim[BRR * N + c] = (R)(sums[0] / areas[0]);
+    S.prim[BPP * N + c] = (R)(Bphi / dA);
+    if (P.Nz > 1) S.prim[BZZ * N + c] = (R)(sums[1] / areas[1]);
+  } else {
+    double rfac = 1.0 / x0, hr = 1.0, hp = x0;
+    S.cons[BRR * N + c] = sums[0] * (dV * rfac / (areas[0] * hr));
+    S.cons[BPP * N + c] = Bphi * dV / (dA * hp);
+    if (P.Nz > 1) S.cons[BZZ * N + c] = sums[1] * (dV * 1.0 / (areas[1] * 1.0));
+  }
+}
+
+// ---- set_B_fields (bfields.c:13-86): face fluxes of the initial field ------------
+template <typename R>
+__global__ void k_ct_init_phi0(DevParams P, DevState<R> S, CtState C) {
+  int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= S.N) return;
+  int jk = S.cell_ring[c];
+  int j = jk % P.Nr, k = jk / P.Nr;
+  const double* rj = S.r_jph + 1;
+  const double* zk = S.z_kph + 1;
+  double x[3] = {centroid_r(rj[j], rj[j - 1]), S.piph[c], centroid_z(zk[k], zk[k - 1])};
+  double prim[MAX_Q];
+  initial_eval(P, prim, x);
+  double dA = (rj[j] - rj[j - 1]) * (zk[k] - zk[k - 1]);
+  C.Phi[c] = prim[BPP] * dA;
+}
+
+template <typename R>
+__global__ void k_ct_init_face_phi(DevParams P, DevState<R> S, CtState C, int dim) {
+  const int d = dim - 1;
+  int f = blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= S.nf[d]) return;
+  // face centre cm = (r, phic, z) of its pair
+  int cL = S.fL[d][f];
+  int jk = S.cell_ring[cL];
+  int j = jk % P.Nr, k = jk / P.Nr;
+  const double* rj = S.r_jph + 1;
+  const double* zk = S.z_kph + 1;
+  double x[3];
+  if (dim == 1) { x[0] = .5 * (rj[j] + rj[j]); x[2] = centroid_z(zk[k], zk[k - 1]); }
+  else { x[0] = centroid_r(rj[j], rj[j - 1]); x[2] = .5 * (zk[k] + zk[k]); }
+  x[1] = S.fphic[d][f];
+  double prim[MAX_Q];
+  initial_eval(P, prim, x);
+  double Phi = (dim == 1 ? prim[BRR] : prim[BZZ]) * S.fdA[d][f];
+  const int N = S.N;
+  if (S.fLR[d][f] == 0) C.Phi[(dim == 1 ? 2 : 4) * N + cL] = Phi;
+  else C.Phi[(dim == 1 ? 1 : 3) * N + S.fR[d][f]] = Phi;
+}
+
+}  // namespace disco

@@ -1,519 +1,16 @@
-// C-ABI driver of the GB300 RK substep cycle: owns the device arrays of one
-// domain, launches the kernels of kernels.cuh in onestep.c order, and
-// captures whole timesteps in CUDA graphs for disco_gpu_run().
-#include <cuda_runtime.h>
+// C-ABI entry points of the GB300 RK substep cycle.  The per-module
+// instances live in disco_gpu_euler.cu / disco_gpu_mhd.cu.
+#include "instance.cuh"
 
-#include <atomic>
-#include <string>
-#include <cstdio>
-#include <cstring>
-#include <vector>
-
-#include "disco_gpu.h"
-#include "../host/disco_host_internal.h"
-#include "kernels.cuh"
-#include "phys_euler.cuh"
-
-using namespace disco;
-
-static std::atomic<long long> g_launches{0};
+std::atomic<long long> g_launches{0};
 long long disco_gpu_launch_count(void) { return g_launches.load(); }
 
-#define CK(x)                                                                  \
-  do {                                                                         \
-    cudaError_t e_ = (x);                                                      \
-    if (e_ != cudaSuccess) {                                                   \
-      char b_[256];                                                            \
-      snprintf(b_, sizeof b_, "CUDA %s at %s:%d", cudaGetErrorString(e_),      \
-               __FILE__, __LINE__);                                            \
-      disco_set_error(b_);                                                     \
-      return DISCO_E_CUDA;                                                     \
-    }                                                                          \
-  } while (0)
-
-namespace {
-
-struct InstanceBase {
-  virtual ~InstanceBase() {}
-  virtual int getmindt(double* dt) = 0;
-  virtual int timestep(double dt) = 0;
-  virtual int run(int n, double t_end) = 0;
-  virtual int download(disco_state_view* v) = 0;
-  virtual int upload(const disco_state_view* v) = 0;
-  virtual int status(disco_gpu_errs* e) = 0;
-  virtual int run_timed(int n, double t_end, size_t flush_bytes, double* ms) = 0;
-  virtual int profile(int n, disco_kernel_time* out, int maxo, int* nout) = 0;
-  virtual double time() = 0;
-  long N = 0, Nreal = 0;
-};
-
-template <typename T>
-static int dalloc(T** p, size_t n, std::vector<void*>& keep) {
-  if (n == 0) n = 1;
-  cudaError_t e = cudaMalloc((void**)p, n * sizeof(T));
-  if (e != cudaSuccess) {
-    disco_set_error("cudaMalloc failed");
-    return DISCO_E_NOMEM;
-  }
-  keep.push_back((void*)*p);
-  return 0;
+namespace disco_impl {
+InstanceBase* make_euler(const disco_host_domain* dom, int precision, int* rc);
+InstanceBase* make_mhd(const disco_host_domain* dom, int precision, int* rc);
 }
+using namespace disco_impl;
 
-struct KTimer {
-  bool on = false;
-  cudaStream_t st = nullptr;
-  struct Rec { const char* name; cudaEvent_t a, b; };
-  std::vector<Rec> recs;
-  cudaEvent_t cur_a = nullptr;
-  void begin() {
-    if (!on) return;
-    cudaEventCreate(&cur_a);
-    cudaEventRecord(cur_a, st);
-  }
-  void end(const char* name) {
-    if (!on) return;
-    cudaEvent_t b;
-    cudaEventCreate(&b);
-    cudaEventRecord(b, st);
-    recs.push_back({name, cur_a, b});
-  }
-};
-
-#define LAUNCH(NAME, ...)            \
-  do {                               \
-    kt.begin();                      \
-    __VA_ARGS__;                     \
-    kt.end(NAME);                    \
-    ++g_launches;                    \
-  } while (0)
-
-template <class Phys, typename R, int NQ>
-struct Instance : InstanceBase {
-  KTimer kt;
-  void* flush_buf = nullptr;
-  size_t flush_size = 0;
-  DevParams P{};
-  DevState<R> S{};
-  std::vector<void*> keep;
-  cudaStream_t st = nullptr;
-  int Nr = 0, Nz = 0, nring = 0, npair[2] = {0, 0};
-  int maxNf[2] = {0, 0};
-  double* piph_buf[2] = {nullptr, nullptr};
-  int parity = 0;  // which piph buffer is current
-  int planets_id = 0;
-  cudaGraphExec_t graph[2] = {nullptr, nullptr};
-  int graph_nodes = 0;
-  double host_t = 0;
-
-  ~Instance() override {
-    if (flush_buf) cudaFree(flush_buf);
-    for (int i = 0; i < 2; ++i)
-      if (graph[i]) cudaGraphExecDestroy(graph[i]);
-    if (st) cudaStreamDestroy(st);
-    for (void* p : keep) cudaFree(p);
-  }
-
-  int blocks(long n, int b = 256) const { return (int)((n + b - 1) / b); }
-
-  void set_piph(int par) {
-    S.piph = piph_buf[par];
-    S.piph_out = piph_buf[par ^ 1];
-  }
-
-  int create(const disco_host_domain* dom) {
-    const disco_params& p = dom->par;
-    CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
-    Nr = dom->Nr; Nz = dom->Nz; nring = Nr * Nz;
-    N = dom->Ncell;
-    if (N > 0x7fffffffL) { disco_set_error("too many cells for int32 indexing"); return DISCO_E_ARG; }
-    // ---- parameters (set*Params pushes, domain.c:259-270)
-    P.Nr = Nr; P.Nz = Nz; P.NgRa = dom->NgRa; P.NgRb = dom->NgRb; P.NgZa = dom->NgZa; P.NgZb = dom->NgZb;
-    P.Ncell = N; P.num_q = dom->num_q; P.num_c = dom->mod.num_c; P.phi_max = dom->phi_max;
-    P.gamma_law = p.Adiabatic_Index; P.rho_floor = p.Density_Floor; P.p_floor = p.Pressure_Floor;
-    P.explicit_viscosity = p.viscosity; P.mach = p.Disk_Mach;
-    P.include_viscosity = p.visc_flag; P.isothermal = p.isothermal_flag; P.alpha_flag = p.alpha_flag;
-    P.polar_sources = dom->mod.hydro == DISCO_HYDRO_EULER ? (p.NoBC_Rmin == 1) : (dom->NgRa == 0);
-    P.riemann_solver = p.Riemann_Solver; P.mesh_motion = p.Mesh_Motion;
-    P.PLM = p.PLM; P.CFL = p.CFL; P.maxDT = p.maxDT;
-    P.meshOmChoice = p.Exact_Mesh_Omega; P.enOmChoice = p.Energy_Omega; P.cs2Choice = p.Cs2_Profile;
-    P.Omega0 = p.RotOmega; P.om_M = p.metricPar2; P.om_r1 = p.initPar2; P.om_H0 = p.initPar4;
-    P.eps = p.grav_eps;
-    P.rot_flag = p.RotFrame; P.rot_omega = p.RotOmega; P.rot_d = p.RotD;
-    P.grav2D = p.grav2D;
-    P.polar_r = P.polar_p = (p.NoBC_Rmin == 1);    // planet.c:13-18 (cylindrical)
-    P.Npl = dom->Npl;
-    P.initial_id = dom->mod.initial; P.boundary_id = dom->mod.boundary;
-    double icp[8] = {p.initPar1, p.initPar2, p.initPar3, p.initPar4, p.initPar5, p.initPar6, p.initPar7, p.initPar8};
-    for (int i = 0; i < 8; ++i) P.ic[i] = icp[i];
-    P.t_end = 0.0;
-    planets_id = dom->mod.planets;
-    if (!Phys::MHD && P.riemann_solver == SOLVER_HLLD) {
-      disco_set_error("Riemann_Solver = HLLD with a hydro module (riemann.c:19-22)");
-      return DISCO_E_MODULE;
-    }
-    if (p.sinkType || p.nozzleType || p.coolType || p.dampInnerType || p.dampOuterType ||
-        p.dampUpperType || p.dampLowerType) {
-      disco_set_error("sink/nozzle/cooling/damping source terms are not built");
-      return DISCO_E_MODULE;
-    }
-    if (p.Timestep != 0) {
-      disco_set_error("only Timestep 0 (RK2) is built");
-      return DISCO_E_MODULE;
-    }
-    if (dom->mod.boundary > 1) {
-      disco_set_error("zero-gradient boundaries are not built");
-      return DISCO_E_MODULE;
-    }
-
-    // ---- index arrays
-    std::vector<int> ring_off(nring + 1), cell_ring(N);
-    for (int jk = 0; jk <= nring; ++jk) ring_off[jk] = (int)dom->ring_off[jk];
-    for (int jk = 0; jk < nring; ++jk)
-      for (int c = ring_off[jk]; c < ring_off[jk + 1]; ++c) cell_ring[c] = jk;
-    Nreal = 0;
-    for (int k = dom->NgZa; k < Nz - dom->NgZb; ++k)
-      for (int j = dom->NgRa; j < Nr - dom->NgRb; ++j) Nreal += dom->Np[j + Nr * k];
-
-    int rc;
-    int *d_ring_off, *d_cell_ring;
-    double *d_r, *d_z;
-#define A(ptr, n) if ((rc = dalloc(ptr, (size_t)(n), keep))) return rc
-    A(&d_ring_off, nring + 1); A(&d_cell_ring, N); A(&d_r, Nr + 1); A(&d_z, Nz + 1);
-    CK(cudaMemcpy(d_ring_off, ring_off.data(), sizeof(int) * (nring + 1), cudaMemcpyHostToDevice));
-    CK(cudaMemcpy(d_cell_ring, cell_ring.data(), sizeof(int) * N, cudaMemcpyHostToDevice));
-    CK(cudaMemcpy(d_r, dom->r_jph, sizeof(double) * (Nr + 1), cudaMemcpyHostToDevice));
-    CK(cudaMemcpy(d_z, dom->z_kph, sizeof(double) * (Nz + 1), cudaMemcpyHostToDevice));
-    S.N = (int)N; S.cell_ring = d_cell_ring; S.ring_off = d_ring_off; S.r_jph = d_r; S.z_kph = d_z;
-    A(&piph_buf[0], N); A(&piph_buf[1], N);
-    A(&S.dphi, N); A(&S.wiph, N);
-    A(&S.prim, (size_t)NQ * N); A(&S.cons, (size_t)NQ * N); A(&S.RKcons, (size_t)NQ * N);
-    A(&S.gradp, (size_t)NQ * N); A(&S.gradr, (size_t)NQ * N); A(&S.gradz, (size_t)NQ * N);
-    A(&S.fphi, (size_t)NQ * N);
-    A(&S.anchor, nring);
-    CK(cudaMemset(S.gradr, 0, sizeof(R) * NQ * N));
-    CK(cudaMemset(S.gradz, 0, sizeof(R) * NQ * N));
-    CK(cudaMemset(S.wiph, 0, sizeof(double) * N));
-    // faces per dimension
-    for (int d = 0; d < 2; ++d) {
-      int dim = d + 1;
-      int np = 0;
-      if (dim == 1 && Nr > 1) np = (Nr - 1) * Nz;
-      if (dim == 2 && Nz > 1) np = Nr * (Nz - 1);
-      npair[d] = np;
-      std::vector<int> off(np + 1, 0);
-      int mx = 0;
-      for (int pr = 0; pr < np; ++pr) {
-        int L, Rr;
-        if (dim == 1) { int j = pr % (Nr - 1), k = pr / (Nr - 1); L = j + Nr * k; Rr = j + 1 + Nr * k; }
-        else { int j = pr % Nr, k = pr / Nr; L = j + Nr * k; Rr = j + Nr * (k + 1); }
-        int nf = dom->Np[L] + dom->Np[Rr];
-        off[pr + 1] = off[pr] + nf;
-        if (nf > mx) mx = nf;
-      }
-      maxNf[d] = mx;
-      int nf = off[np];
-      S.nf[d] = nf;
-      int* d_off;
-      A(&d_off, np + 1);
-      CK(cudaMemcpy(d_off, off.data(), sizeof(int) * (np + 1), cudaMemcpyHostToDevice));
-      S.face_off[d] = d_off;
-      A(&S.fL[d], nf); A(&S.fR[d], nf); A(&S.fLR[d], nf); A(&S.fphic[d], nf); A(&S.fdA[d], nf);
-      A(&S.fflux[d], (size_t)NQ * nf);
-      A(&S.run_up_s[d], N); A(&S.run_up_e[d], N); A(&S.run_dn_s[d], N); A(&S.run_dn_e[d], N);
-      if (np > 0 && mx * 9 > 48 * 1024) {
-        CK(cudaFuncSetAttribute(k_faces<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx * 9 + 64));
-      }
-    }
-    A(&S.planets, MAX_PL); A(&S.scal, SC_COUNT); A(&S.errs, 1);
-#undef A
-    std::vector<DevPlanet> pl(MAX_PL);
-    for (int i = 0; i < dom->Npl && i < MAX_PL; ++i) {
-      pl[i].r = dom->planets[i].r; pl[i].phi = dom->planets[i].phi; pl[i].M = dom->planets[i].M;
-      pl[i].omega = dom->planets[i].omega; pl[i].vr = dom->planets[i].vr;
-      pl[i].eps = dom->planets[i].eps; pl[i].type = dom->planets[i].type;
-    }
-    CK(cudaMemcpy(S.planets, pl.data(), sizeof(DevPlanet) * MAX_PL, cudaMemcpyHostToDevice));
-    double scal[SC_COUNT] = {0, dom->t, 0, 0};
-    unsigned long long inf = 0x7ff0000000000000ull;
-    memcpy(&scal[SC_MIN], &inf, 8);
-    CK(cudaMemcpy(S.scal, scal, sizeof scal, cudaMemcpyHostToDevice));
-    CK(cudaMemset(S.errs, 0, sizeof(DevErrs)));
-    host_t = dom->t;
-
-    // ---- state upload + set-up kernels (setupCells, domain.c:283-385)
-    CK(cudaMemcpy(piph_buf[0], dom->piph, sizeof(double) * N, cudaMemcpyHostToDevice));
-    CK(cudaMemcpy(S.dphi, dom->dphi, sizeof(double) * N, cudaMemcpyHostToDevice));
-    parity = 0;
-    set_piph(0);
-    double* d_prim0;
-    CK(cudaMalloc(&d_prim0, sizeof(double) * NQ * N));
-    CK(cudaMemcpy(d_prim0, dom->prim, sizeof(double) * NQ * N, cudaMemcpyHostToDevice));
-    k_init_cells<Phys, R, NQ><<<blocks(N), 256, 0, st>>>(P, S, d_prim0);
-    ++g_launches;
-    CK(cudaGetLastError());
-    CK(cudaStreamSynchronize(st));
-    cudaFree(d_prim0);
-    launch_boundary();
-    launch_wcell();
-    launch_faces();
-    CK(cudaGetLastError());
-    CK(cudaStreamSynchronize(st));
-    return 0;
-  }
-
-  // ---- launch helpers -----------------------------------------------------
-  void launch_wcell() {
-    LAUNCH("wcell", (k_wcell<R, NQ><<<blocks(N), 256, 0, st>>>(P, S)));
-    if (P.mesh_motion == 3) LAUNCH("wcell_avg", (k_wcell_avg<R><<<nring, 256, 0, st>>>(P, S)));
-  }
-  void launch_boundary() {
-    LAUNCH("boundary", (k_boundary<R, NQ><<<blocks(N), 256, 0, st>>>(P, S)));
-  }
-  void launch_faces() {
-    if (npair[0] == 0 && npair[1] == 0) return;
-    LAUNCH("anchor", (k_anchor<R><<<blocks((long)nring * 32), 256, 0, st>>>(P, S, nring)));
-    for (int d = 0; d < 2; ++d) {
-      if (!npair[d]) continue;
-      size_t sm = (size_t)maxNf[d] * 9 + 64;
-      LAUNCH(d == 0 ? "faces_r" : "faces_z", (k_faces<R><<<npair[d], 256, sm, st>>>(P, S, d + 1)));
-    }
-  }
-  void launch_mindt() {
-    LAUNCH("mindt", (k_mindt<Phys, R, NQ><<<blocks(N), 256, 0, st>>>(P, S)));
-    LAUNCH("dt_finalize", (k_dt_finalize<<<1, 1, 0, st>>>(P, S.scal)));
-  }
-  // one onestep (onestep.c:86-186)
-  void substep(double RK, double fac, int first) {
-    if (first) launch_wcell();
-    LAUNCH("plm_phi", (k_plm_phi<R, NQ><<<blocks(N), 256, 0, st>>>(P, S)));
-    if (Nr > 1) LAUNCH("plm_trans_r", (k_plm_trans<R, NQ><<<blocks(N), 256, 0, st>>>(P, S, 1)));
-    if (Nz > 1) LAUNCH("plm_trans_z", (k_plm_trans<R, NQ><<<blocks(N), 256, 0, st>>>(P, S, 2)));
-    LAUNCH("flux_phi", (k_flux_phi<Phys, R, NQ><<<blocks(N), 256, 0, st>>>(P, S, fac)));
-    for (int d = 0; d < 2; ++d) {
-      if (!npair[d]) continue;
-      int dim = d + 1;
-      int jmin, jmax, kmin, kmax;
-      if (dim == 1) {
-        jmin = P.NgRa == 0 ? 0 : P.NgRa - 1;
-        jmax = P.NgRb == 0 ? Nr - 1 : Nr - P.NgRb;
-        kmin = P.NgZa; kmax = Nz - P.NgZb;
-      } else {
-        jmin = P.NgRa; jmax = Nr - P.NgRb;
-        kmin = P.NgZa == 0 ? 0 : P.NgZa - 1;
-        kmax = P.NgZb == 0 ? Nz - 1 : Nz - P.NgZb;
-      }
-      int jc = jmax - jmin, kc = kmax - kmin;
-      if (jc <= 0 || kc <= 0) continue;
-      dim3 grid(jc * kc, (maxNf[d] + 255) / 256);
-      LAUNCH(dim == 1 ? "flux_r" : "flux_z",
-             (k_flux_trans<Phys, R, NQ><<<grid, 256, 0, st>>>(P, S, dim, jmin, jc, kmin, fac)));
-    }
-    LAUNCH("update", (k_update<Phys, R, NQ><<<blocks(N), 256, 0, st>>>(P, S, RK, fac, first)));
-    if (first) {
-      parity ^= 1;
-      set_piph(parity);
-      LAUNCH("after_first", (k_after_first<<<1, 1, 0, st>>>(P, S.scal, S.planets, planets_id, S.errs)));
-    }
-    launch_boundary();
-    if (first) launch_faces();
-  }
-  // timestep.c:7-54 with Timestep 0 (RK2)
-  void step_kernels() {
-    substep(0.0, 1.0, 1);
-    substep(0.5, 0.5, 0);
-  }
-
-  int getmindt(double* dt) override {
-    P.t_end = 0.0;
-    launch_mindt();
-    CK(cudaMemcpyAsync(dt, &S.scal[SC_DT], sizeof(double), cudaMemcpyDeviceToHost, st));
-    CK(cudaStreamSynchronize(st));
-    CK(cudaGetLastError());
-    return 0;
-  }
-  int timestep(double dt) override {
-    CK(cudaMemcpyAsync(&S.scal[SC_DT], &dt, sizeof(double), cudaMemcpyHostToDevice, st));
-    step_kernels();
-    CK(cudaGetLastError());
-    CK(cudaStreamSynchronize(st));
-    host_t += dt;
-    return 0;
-  }
-  int build_graph(int par, double t_end) {
-    // capture one full step starting from piph parity `par`
-    int save = parity;
-    parity = par;
-    set_piph(par);
-    P.t_end = t_end;
-    long long before = g_launches.load();
-    CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-    launch_mindt();
-    step_kernels();
-    cudaGraph_t g;
-    CK(cudaStreamEndCapture(st, &g));
-    graph_nodes = (int)(g_launches.load() - before);
-    g_launches -= graph_nodes;  // counted again on each replay
-    CK(cudaGraphInstantiate(&graph[par], g, 0));
-    cudaGraphDestroy(g);
-    parity = save;
-    set_piph(save);
-    return 0;
-  }
-  double graph_t_end = -1.0;
-  int run(int n, double t_end) override {
-    if (graph_t_end != t_end) {
-      for (int i = 0; i < 2; ++i) if (graph[i]) { cudaGraphExecDestroy(graph[i]); graph[i] = nullptr; }
-      graph_t_end = t_end;
-    }
-    for (int i = 0; i < 2; ++i)
-      if (!graph[i]) { int rc = build_graph(i, t_end); if (rc) return rc; }
-    for (int s = 0; s < n; ++s) {
-      CK(cudaGraphLaunch(graph[parity], st));
-      g_launches += graph_nodes;
-      parity ^= 1;
-    }
-    set_piph(parity);
-    P.t_end = 0.0;
-    CK(cudaStreamSynchronize(st));
-    CK(cudaGetLastError());
-    double sc[SC_COUNT];
-    CK(cudaMemcpy(sc, S.scal, sizeof sc, cudaMemcpyDeviceToHost));
-    host_t = sc[SC_T];
-    return 0;
-  }
-  int run_timed(int n, double t_end, size_t flush_bytes, double* ms) override {
-    if (graph_t_end != t_end) {
-      for (int i = 0; i < 2; ++i) if (graph[i]) { cudaGraphExecDestroy(graph[i]); graph[i] = nullptr; }
-      graph_t_end = t_end;
-    }
-    for (int i = 0; i < 2; ++i)
-      if (!graph[i]) { int rc = build_graph(i, t_end); if (rc) return rc; }
-    if (flush_bytes > flush_size) {
-      if (flush_buf) cudaFree(flush_buf);
-      flush_buf = nullptr; flush_size = 0;
-      CK(cudaMalloc(&flush_buf, flush_bytes));
-      flush_size = flush_bytes;
-    }
-    std::vector<cudaEvent_t> ev(2 * (size_t)n);
-    for (auto& e : ev) CK(cudaEventCreate(&e));
-    for (int s = 0; s < n; ++s) {
-      if (flush_bytes) CK(cudaMemsetAsync(flush_buf, s & 0xff, flush_bytes, st));
-      CK(cudaEventRecord(ev[2 * s], st));
-      CK(cudaGraphLaunch(graph[parity], st));
-      CK(cudaEventRecord(ev[2 * s + 1], st));
-      g_launches += graph_nodes;
-      parity ^= 1;
-    }
-    set_piph(parity);
-    CK(cudaStreamSynchronize(st));
-    double tot = 0;
-    for (int s = 0; s < n; ++s) {
-      float t;
-      CK(cudaEventElapsedTime(&t, ev[2 * s], ev[2 * s + 1]));
-      tot += t;
-    }
-    for (auto& e : ev) cudaEventDestroy(e);
-    *ms = tot;
-    double sc[SC_COUNT];
-    CK(cudaMemcpy(sc, S.scal, sizeof sc, cudaMemcpyDeviceToHost));
-    host_t = sc[SC_T];
-    return 0;
-  }
-  int profile(int n, disco_kernel_time* out, int maxo, int* nout) override {
-    kt.on = true;
-    kt.st = st;
-    kt.recs.clear();
-    for (int s = 0; s < n; ++s) {
-      P.t_end = 0.0;
-      launch_mindt();
-      step_kernels();
-    }
-    kt.on = false;
-    CK(cudaStreamSynchronize(st));
-    std::vector<std::string> names;
-    std::vector<long long> cnt;
-    std::vector<double> ms;
-    for (auto& r : kt.recs) {
-      float t = 0;
-      cudaEventElapsedTime(&t, r.a, r.b);
-      cudaEventDestroy(r.a);
-      cudaEventDestroy(r.b);
-      size_t i = 0;
-      for (; i < names.size(); ++i) if (names[i] == r.name) break;
-      if (i == names.size()) { names.push_back(r.name); cnt.push_back(0); ms.push_back(0); }
-      cnt[i] += 1;
-      ms[i] += t;
-    }
-    kt.recs.clear();
-    int k = 0;
-    for (size_t i = 0; i < names.size() && k < maxo; ++i, ++k) {
-      snprintf(out[k].name, sizeof out[k].name, "%s", names[i].c_str());
-      out[k].launches = cnt[i];
-      out[k].ms = ms[i];
-    }
-    *nout = k;
-    double sc[SC_COUNT];
-    CK(cudaMemcpy(sc, S.scal, sizeof sc, cudaMemcpyDeviceToHost));
-    host_t = sc[SC_T];
-    return 0;
-  }
-  int download(disco_state_view* v) override {
-    CK(cudaStreamSynchronize(st));
-    if (v->piph) CK(cudaMemcpy(v->piph, S.piph, sizeof(double) * N, cudaMemcpyDeviceToHost));
-    if (v->dphi) CK(cudaMemcpy(v->dphi, S.dphi, sizeof(double) * N, cudaMemcpyDeviceToHost));
-    if (v->wiph) CK(cudaMemcpy(v->wiph, S.wiph, sizeof(double) * N, cudaMemcpyDeviceToHost));
-    if (v->cons) CK(cudaMemcpy(v->cons, S.cons, sizeof(double) * NQ * N, cudaMemcpyDeviceToHost));
-    if (v->prim) {
-      if (sizeof(R) == sizeof(double)) {
-        CK(cudaMemcpy(v->prim, S.prim, sizeof(double) * NQ * N, cudaMemcpyDeviceToHost));
-      } else {
-        std::vector<R> tmp((size_t)NQ * N);
-        CK(cudaMemcpy(tmp.data(), S.prim, sizeof(R) * NQ * N, cudaMemcpyDeviceToHost));
-        for (size_t i = 0; i < tmp.size(); ++i) v->prim[i] = (double)tmp[i];
-      }
-    }
-    double sc[SC_COUNT];
-    CK(cudaMemcpy(sc, S.scal, sizeof sc, cudaMemcpyDeviceToHost));
-    v->t = sc[SC_T];
-    return 0;
-  }
-  int upload(const disco_state_view* v) override {
-    CK(cudaStreamSynchronize(st));
-    if (v->piph) CK(cudaMemcpy((void*)S.piph, v->piph, sizeof(double) * N, cudaMemcpyHostToDevice));
-    if (v->dphi) CK(cudaMemcpy(S.dphi, v->dphi, sizeof(double) * N, cudaMemcpyHostToDevice));
-    if (v->wiph) CK(cudaMemcpy(S.wiph, v->wiph, sizeof(double) * N, cudaMemcpyHostToDevice));
-    if (v->cons) CK(cudaMemcpy(S.cons, v->cons, sizeof(double) * NQ * N, cudaMemcpyHostToDevice));
-    if (v->prim) {
-      std::vector<R> tmp((size_t)NQ * N);
-      for (size_t i = 0; i < tmp.size(); ++i) tmp[i] = (R)v->prim[i];
-      CK(cudaMemcpy(S.prim, tmp.data(), sizeof(R) * NQ * N, cudaMemcpyHostToDevice));
-    }
-    if (v->piph || v->dphi) { launch_faces(); CK(cudaStreamSynchronize(st)); }
-    return 0;
-  }
-  int status(disco_gpu_errs* e) override {
-    DevErrs h;
-    CK(cudaStreamSynchronize(st));
-    CK(cudaMemcpy(&h, S.errs, sizeof h, cudaMemcpyDeviceToHost));
-    e->nan_cells = (long long)h.nan_cells;
-    e->rho_floor_hits = (long long)h.rho_floor_hits;
-    e->p_floor_hits = (long long)h.p_floor_hits;
-    e->face_errors = (long long)h.face_errors;
-    e->steps = (long long)h.steps;
-    return 0;
-  }
-  double time() override { return host_t; }
-};
-
-template <class Phys, typename R, int NQ>
-InstanceBase* make_instance(const disco_host_domain* dom, int* rc) {
-  auto* x = new Instance<Phys, R, NQ>();
-  *rc = x->create(dom);
-  if (*rc) { delete x; return nullptr; }
-  return x;
-}
-
-}  // namespace
 
 struct disco_gpu {
   InstanceBase* impl;
@@ -529,18 +26,8 @@ int disco_gpu_create(const disco_host_domain* dom, int precision, disco_gpu** ou
     return DISCO_E_NODEV;
   }
   int rc = 0;
-  InstanceBase* impl = nullptr;
-  int nq = dom->num_q;
-  if (dom->mod.hydro == DISCO_HYDRO_EULER) {
-    if (nq == 5) impl = precision ? make_instance<Euler<float, 5>, float, 5>(dom, &rc)
-                                  : make_instance<Euler<double, 5>, double, 5>(dom, &rc);
-    else if (nq == 6) impl = precision ? make_instance<Euler<float, 6>, float, 6>(dom, &rc)
-                                       : make_instance<Euler<double, 6>, double, 6>(dom, &rc);
-    else { disco_set_error("euler: NUM_Q must be 5 or 6"); return DISCO_E_MODULE; }
-  } else {
-    disco_set_error("HYDRO=mhd is not built in this library");
-    return DISCO_E_MODULE;
-  }
+  InstanceBase* impl = dom->mod.hydro == DISCO_HYDRO_EULER ? make_euler(dom, precision, &rc)
+                                                           : make_mhd(dom, precision, &rc);
   if (!impl) return rc ? rc : DISCO_E_CUDA;
   *out = new disco_gpu{impl};
   return 0;

@@ -48,6 +48,14 @@ struct DevState {
   int* run_dn_s[2];            // per cell: first face where the cell is R (pair below)
   int* run_dn_e[2];
   int nf[2];
+  // constrained transport (MHD): edge EMFs written by the flux kernels
+  int ct;
+  double* Eraw;                // [8*N] E[8] of the reference cell
+  double* Braw;                // [8*N] B[8]
+  double* fdphi[2];            // face dphi
+  double* fErz[2];             // per face flux_to_E outputs
+  double* fBrz[2];
+  double* fEphi[2];
   DevPlanet* planets;          // [Npl], device copy (moves for analytic orbits)
   double* scal;                // [0] dt, [1] t, [2] min-dt accumulator (bits)
   DevErrs* errs;
@@ -57,6 +65,26 @@ enum { SC_DT = 0, SC_T = 1, SC_MIN = 2, SC_COUNT = 4 };
 
 DISCO_D bool is_real(const DevParams& P, int j, int k) {
   return j >= P.NgRa && j < P.Nr - P.NgRb && k >= P.NgZa && k < P.Nz - P.NgZb;
+}
+
+// CT sweep ranges (misc.c:393-407, :464-500): one ring beyond the interior.
+DISCO_D bool ring_in_phi_range(const DevParams& P, int j, int k) {
+  int jmin = P.NgRa == 0 ? 0 : P.NgRa - 1, jmax = P.NgRb == 0 ? P.Nr : P.Nr - P.NgRb + 1;
+  int kmin = P.NgZa == 0 ? 0 : P.NgZa - 1, kmax = P.NgZb == 0 ? P.Nz : P.Nz - P.NgZb + 1;
+  return j >= jmin && j < jmax && k >= kmin && k < kmax;
+}
+DISCO_D bool pair_in_flux_range(const DevParams& P, int dim, int pair) {
+  int j, k, jmin, jmax, kmin, kmax;
+  if (dim == 1) {
+    j = pair % (P.Nr - 1); k = pair / (P.Nr - 1);
+    jmin = P.NgRa == 0 ? 0 : P.NgRa - 1; jmax = P.NgRb == 0 ? P.Nr - 1 : P.Nr - P.NgRb;
+    kmin = P.NgZa == 0 ? 0 : P.NgZa - 1; kmax = P.NgZb == 0 ? P.Nz : P.Nz - P.NgZb + 1;
+  } else {
+    j = pair % P.Nr; k = pair / P.Nr;
+    jmin = P.NgRa == 0 ? 0 : P.NgRa - 1; jmax = P.NgRb == 0 ? P.Nr : P.Nr - P.NgRb + 1;
+    kmin = P.NgZa == 0 ? 0 : P.NgZa - 1; kmax = P.NgZb == 0 ? P.Nz - 1 : P.Nz - P.NgZb;
+  }
+  return j >= jmin && j < jmax && k >= kmin && k < kmax;
 }
 
 // ---- initial() dispatch (plugin chosen by Makefile_opt.in INITIAL) --------
@@ -292,6 +320,7 @@ __global__ void k_faces(DevParams P, DevState<R> S, int dim) {
       S.fLR[d][gf] = (signed char)LR;
       S.fphic[d][gf] = phic;
       S.fdA[d][gf] = dA;
+      if (S.fdphi[d]) S.fdphi[d][gf] = dp;
       sLR[n] = (signed char)LR;
       if (LR == 0) ++a; else ++b;
     }
@@ -491,7 +520,7 @@ __global__ void k_flux_phi(DevParams P, DevState<R> S, double fac) {
   if (c >= S.N) return;
   int jk = S.cell_ring[c];
   int j = jk % P.Nr, k = jk / P.Nr;
-  if (!is_real(P, j, k)) return;
+  if (S.ct ? !ring_in_phi_range(P, j, k) : !is_real(P, j, k)) return;
   const int N = S.N;
   int off = S.ring_off[jk], Np = S.ring_off[jk + 1] - off;
   int i = c - off;
@@ -526,11 +555,20 @@ __global__ void k_flux_phi(DevParams P, DevState<R> S, double fac) {
   R n[3] = {0, 1, 0};
   R hn = (R)r;
   R w = hn * (R)S.wiph[c];
-  R Fw[NQ];
+  R Fw[NQ], Fl[NQ], Us[NQ];
   solve_riemann<Phys, R, NQ>(P, S.planets, primL, primR, gLr, gp, gLz, gRr, gp, gRz, (R)r,
-                             (R)phi, n, w, Fw, nullptr, nullptr);
+                             (R)phi, n, w, Fw, Fl, Us);
 #pragma unroll
   for (int q = 0; q < NQ; ++q) S.fphi[q * N + c] = (R)((double)Fw[q] * dAdt);
+  if (S.ct) {   // riemann.c:86-111 (NUM_EDGES == 8)
+    R Ez, Br, Er, Bz;
+    Phys::flux_to_E(Fl, Us, (R)r, &Ez, &Br, &Er, &Bz, 0);
+    double hEz = .5 * (double)Ez, hBr = .5 * (double)Br, hEr = .5 * (double)Er, hBz = .5 * (double)Bz;
+    S.Eraw[0 * N + c] = hEz; S.Eraw[1 * N + c] = hEz; S.Eraw[2 * N + cp] = hEz; S.Eraw[3 * N + cp] = hEz;
+    S.Braw[0 * N + c] = hBr; S.Braw[1 * N + c] = hBr; S.Braw[2 * N + cp] = hBr; S.Braw[3 * N + cp] = hBr;
+    S.Eraw[4 * N + c] = hEr; S.Eraw[5 * N + c] = hEr; S.Eraw[6 * N + cp] = hEr; S.Eraw[7 * N + cp] = hEr;
+    S.Braw[4 * N + c] = hBz; S.Braw[5 * N + c] = hBz; S.Braw[6 * N + cp] = hBz; S.Braw[7 * N + cp] = hBz;
+  }
 }
 
 // ---- r/z fluxes, misc.c:441-519 + riemann_trans, riemann.c:114-214 ----------
@@ -586,17 +624,22 @@ __global__ void k_flux_trans(DevParams P, DevState<R> S, int dim, int jmin, int 
   const double* rj = S.r_jph + 1;
   int pjL = pair % (dim == 1 ? (P.Nr - 1) : P.Nr);
   double r = dim == 1 ? .5 * (rj[pjL] + rj[pjL]) : centroid_r(rj[pjL], rj[pjL - 1]);
-  R Fw[NQ];
+  R Fw[NQ], Fl[NQ], Us[NQ];
   if (dim == 1)
     solve_riemann<Phys, R, NQ>(P, S.planets, primL, primR, grad, gLp, gLo, grad, gRp, gRo, (R)r,
-                               (R)phi, n3, (R)0.0, Fw, nullptr, nullptr);
+                               (R)phi, n3, (R)0.0, Fw, Fl, Us);
   else
     solve_riemann<Phys, R, NQ>(P, S.planets, primL, primR, gLo, gLp, grad, gRo, gRp, grad, (R)r,
-                               (R)phi, n3, (R)0.0, Fw, nullptr, nullptr);
+                               (R)phi, n3, (R)0.0, Fw, Fl, Us);
   R* out = S.fflux[d];
   const int NF = S.nf[d];
 #pragma unroll
   for (int q = 0; q < NQ; ++q) out[q * NF + f] = (R)((double)Fw[q] * dAdt);
+  if (S.ct) {
+    R E1, B1, E2, B2;
+    Phys::flux_to_E(Fl, Us, (R)r, &E1, &B1, &E2, &B2, dim);
+    S.fErz[d][f] = (double)E1; S.fBrz[d][f] = (double)B1; S.fEphi[d][f] = (double)E2;
+  }
 }
 
 // ---- conserved update + sources + move + cons2prim -----------------------------
@@ -604,7 +647,7 @@ __global__ void k_flux_trans(DevParams P, DevState<R> S, int dim, int jmin, int 
 // the reference's order, add_source (misc.c:550), move_cells/clean_pi/calc_dp
 // (misc.c:266, :8, :281), calc_prim (misc.c:300).
 template <typename Phys, typename R, int NQ>
-__global__ void k_update(DevParams P, DevState<R> S, double RK, double fac, int first) {
+__global__ void k_update(DevParams P, DevState<R> S, double RK, double fac, int first, int do_c2p) {
   int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= S.N) return;
   const int N = S.N;
@@ -721,7 +764,7 @@ __global__ void k_update(DevParams P, DevState<R> S, double RK, double fac, int 
     S.dphi[c] = dphi;
   }
 
-  if (real) {  // calc_prim at the post-move geometry
+  if (real && do_c2p) {  // calc_prim at the post-move geometry
     double rp = rj[j], rm = rj[j - 1], zp = zk[k], zm = zk[k - 1];
     double phim = piph - dphi;
     double xp1 = piph;
@@ -818,7 +861,7 @@ __global__ void k_mindt(DevParams P, DevState<R> S) {
 }
 
 // dt = CFL * min (misc.c:52-78); clamp to T_End (check_dt, domain.c:433).
-__global__ void k_dt_finalize(DevParams P, double* scal) {
+static __global__ void k_dt_finalize(DevParams P, double* scal) {
   double m = __longlong_as_double(*(long long*)&scal[SC_MIN]);
   double dt0 = P.maxDT / P.CFL;
   if (dt0 <= 0.0) dt0 = 1.0e100;
@@ -831,7 +874,7 @@ __global__ void k_dt_finalize(DevParams P, double* scal) {
 
 // After the first substep: t += dt (timestep.c:136), analytic planet motion
 // (Planets/circular.c:44-46), clean_pi on planets (misc.c:27-34).
-__global__ void k_after_first(DevParams P, double* scal, DevPlanet* pl, int planets_id,
+static __global__ void k_after_first(DevParams P, double* scal, DevPlanet* pl, int planets_id,
                               DevErrs* errs) {
   double dt = scal[SC_DT];
   scal[SC_T] += dt;
@@ -845,9 +888,41 @@ __global__ void k_after_first(DevParams P, double* scal, DevPlanet* pl, int plan
   errs->steps += 1;
 }
 
+// ---- calc_prim (misc.c:300-335) as its own pass (after B_faces_to_cells) --------
+template <typename Phys, typename R, int NQ>
+__global__ void k_c2p(DevParams P, DevState<R> S) {
+  int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= S.N) return;
+  const int N = S.N;
+  int jk = S.cell_ring[c];
+  int j = jk % P.Nr, k = jk / P.Nr;
+  if (!is_real(P, j, k)) return;
+  const double* rj = S.r_jph + 1;
+  const double* zk = S.z_kph + 1;
+  double piph = S.piph[c], dphi = S.dphi[c];
+  double rp = rj[j], rm = rj[j - 1], zp = zk[k], zm = zk[k - 1];
+  double phim = piph - dphi;
+  double dV = (.5 * (rp + rm)) * (rp - rm) * get_dp(piph, phim, P.phi_max) * (zp - zm);
+  double r = centroid_r(rp, rm);
+  double U[NQ];
+#pragma unroll
+  for (int q = 0; q < NQ; ++q) U[q] = S.cons[q * N + c];
+  R pr[NQ];
+  int hits = Phys::cons2prim(P, S.planets, U, pr, r, .5 * (phim + piph), dV);
+  bool bad = false;
+#pragma unroll
+  for (int q = 0; q < NQ; ++q) {
+    S.prim[q * N + c] = pr[q];
+    if (!isfinite((double)pr[q])) bad = true;
+  }
+  if (bad) atomicAdd(&S.errs->nan_cells, 1ull);
+  if (hits & 1) atomicAdd(&S.errs->rho_floor_hits, 1ull);
+  if (hits & 2) atomicAdd(&S.errs->p_floor_hits, 1ull);
+}
+
 // ---- set-up: prim2cons + cons2prim for real cells (domain.c:349, :379) ---------
 template <typename Phys, typename R, int NQ>
-__global__ void k_init_cells(DevParams P, DevState<R> S, const double* prim0) {
+__global__ void k_init_cells(DevParams P, DevState<R> S, const double* prim0, int do_c2p) {
   int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= S.N) return;
   const int N = S.N;
@@ -870,7 +945,8 @@ __global__ void k_init_cells(DevParams P, DevState<R> S, const double* prim0) {
   using Phys64 = typename Phys::template Rebind<double>;
   Phys64::template prim2cons<double>(P, pr, U, r, dV);
   R out[NQ];
-  Phys::cons2prim(P, S.planets, U, out, r, piph - .5 * dphi, dV);
+  if (do_c2p) Phys::cons2prim(P, S.planets, U, out, r, piph - .5 * dphi, dV);
+  else for (int q = 0; q < NQ; ++q) out[q] = (R)pr[q];
 #pragma unroll
   for (int q = 0; q < NQ; ++q) { S.cons[q * N + c] = U[q]; S.prim[q * N + c] = out[q]; }
 }

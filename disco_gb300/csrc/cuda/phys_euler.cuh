@@ -199,6 +199,9 @@ struct Euler {
     cons[TAU] += (double)(((R)2 * rho * nu * (srp * om_r + spz * om_z)) * (R)dVdt);
   }
 
+  // flux_to_E, euler.c:293-299: no magnetic field, nothing to do.
+  DISCO_D static void flux_to_E(const R*, const R*, R, R*, R*, R*, R*, int) {}
+
   // HLLD is rejected for hydro at set-up (riemann.c:19-22); never reached.
   DISCO_D static void hlld(const DevParams&, R, const R*, const R*, R* F, R* U, R, const R*) {
 #pragma unroll

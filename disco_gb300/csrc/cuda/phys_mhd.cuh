@@ -1,0 +1,357 @@
+// Newtonian MHD hooks of Hydro/mhd.c and the HLLD solver of hlld.c as device
+// functions templated on the arithmetic type R.  Magnetic field primitives
+// are B^r, B^phi (orthonormal), B^z; conserved B^r is scaled by 1/r
+// (bfield_scale_factor, mhd.c:518).
+#pragma once
+#include "dev_common.cuh"
+
+namespace disco {
+
+template <typename R, int NQ>
+struct Mhd {
+  static constexpr int NC = 8;
+  static constexpr bool MHD = true;
+  template <typename T>
+  using Rebind = Mhd<T, NQ>;
+
+  // prim2cons, mhd.c:35-69
+  template <typename T>
+  DISCO_D static void prim2cons(const DevParams& P, const R* prim, T* cons, R r, R dV) {
+    R rho = prim[RHO], Pp = prim[PPP], vr = prim[URR], vp = prim[UPP] * r, vz = prim[UZZ];
+    R om = get_om<R>(P, r);
+    R vp_off = vp - om * r;
+    R Br = prim[BRR], Bp = prim[BPP], Bz = prim[BZZ];
+    R v2 = vr * vr + vp_off * vp_off + vz * vz;
+    R B2 = Br * Br + Bp * Bp + Bz * Bz;
+    R rhoe = Pp / ((R)P.gamma_law - (R)1.);
+    cons[DDD] = rho * dV;
+    cons[TAU] = ((R).5 * rho * v2 + rhoe + (R).5 * B2) * dV;
+    cons[SRR] = rho * vr * dV;
+    cons[LLL] = r * rho * vp * dV;
+    cons[SZZ] = rho * vz * dV;
+    cons[BRR] = Br * dV * ((R)1.0 / r);
+    cons[BPP] = Bp * dV / r;
+    cons[BZZ] = Bz * dV;
+#pragma unroll
+    for (int q = NC; q < NQ; ++q) cons[q] = prim[q] * (R)cons[DDD];
+  }
+
+  // cons2prim, mhd.c:138-185 (FP64 conserved in, R primitives out)
+  DISCO_D static int cons2prim(const DevParams& P, const DevPlanet* pl, const double* cons, R* prim,
+                               double r, double phi, double dV) {
+    int hits = 0;
+    R rho = (R)(cons[DDD] / dV);
+    if (rho < (R)P.rho_floor) { rho = (R)P.rho_floor; hits |= 1; }
+    R Sr = (R)(cons[SRR] / dV);
+    R Sp = (R)(cons[LLL] / dV / r);
+    R Sz = (R)(cons[SZZ] / dV);
+    R E = (R)(cons[TAU] / dV);
+    R rr = (R)r;
+    R om = get_om<R>(P, rr);
+    R vr = Sr / rho, vp = Sp / rho, vp_off = vp - om * rr, vz = Sz / rho;
+    R Br = (R)(cons[BRR] / (dV * (1.0 / r)));
+    R Bp = (R)(cons[BPP] / dV * r);
+    R Bz = (R)(cons[BZZ] / dV);
+    R B2 = Br * Br + Bp * Bp + Bz * Bz;
+    R KE = (R).5 * (Sr * vr + rho * vp_off * vp_off + Sz * vz);
+    R rhoe = E - KE - (R).5 * B2;
+    R Pp = ((R)P.gamma_law - (R)1.) * rhoe;
+    if (Pp < (R)P.p_floor * rho) { Pp = (R)P.p_floor * rho; hits |= 2; }
+    if (P.isothermal) {
+      R cs2 = get_cs2<R>(P, pl, rr, (R)phi);
+      Pp = cs2 * rho / (R)P.gamma_law;
+    }
+    prim[RHO] = rho; prim[PPP] = Pp; prim[URR] = vr; prim[UPP] = vp / rr; prim[UZZ] = vz;
+    prim[BRR] = Br; prim[BPP] = Bp; prim[BZZ] = Bz;
+#pragma unroll
+    for (int q = NC; q < NQ; ++q) prim[q] = (R)(cons[q] / cons[DDD]);
+    return hits;
+  }
+
+  // flux, mhd.c:187-223
+  DISCO_D static void flux(const DevParams& P, const R* prim, R* f, R r, const R* n) {
+    R rho = prim[RHO], Pp = prim[PPP], vr = prim[URR], vp = prim[UPP] * r, vz = prim[UZZ];
+    R Br = prim[BRR], Bp = prim[BPP], Bz = prim[BZZ];
+    R vn = vr * n[0] + vp * n[1] + vz * n[2];
+    R Bn = Br * n[0] + Bp * n[1] + Bz * n[2];
+    R vB = vr * Br + vp * Bp + vz * Bz;
+    R rhoe = Pp / ((R)P.gamma_law - (R)1.);
+    R v2 = vr * vr + vp * vp + vz * vz;
+    R B2 = Br * Br + Bp * Bp + Bz * Bz;
+    f[DDD] = rho * vn;
+    f[SRR] = rho * vr * vn + (Pp + (R).5 * B2) * n[0] - Br * Bn;
+    f[LLL] = r * (rho * vp * vn + (Pp + (R).5 * B2) * n[1] - Bp * Bn);
+    f[SZZ] = rho * vz * vn + (Pp + (R).5 * B2) * n[2] - Bz * Bn;
+    f[TAU] = ((R).5 * rho * v2 + rhoe + Pp + B2) * vn - vB * Bn;
+    f[BRR] = (Br * vn - vr * Bn) * ((R)1.0 / r);
+    f[BPP] = (Bp * vn - vp * Bn) / r;
+    f[BZZ] = Bz * vn - vz * Bn;
+#pragma unroll
+    for (int q = NC; q < NQ; ++q) f[q] = prim[q] * f[DDD];
+  }
+
+  // source, mhd.c:225-262
+  DISCO_D static void source(const DevParams& P, const R* prim, double* cons, const double* xp,
+                             const double* xm, double dVdt) {
+    double rp = xp[0], rm = xm[0];
+    double dphi = get_dp(xp[1], xm[1], P.phi_max);
+    R rho = prim[RHO], Pp = prim[PPP];
+    R r_1 = (R)(.5 * (rp + rm));
+    R r2_3 = (R)((rp * rp + rp * rm + rm * rm) / 3.);
+    R vr = prim[URR], omega = prim[UPP];
+    R r = (R)centroid_r(rp, rm);
+    R Br = prim[BRR], Bp = prim[BPP], Bz = prim[BZZ];
+    R B2 = Br * Br + Bp * Bp + Bz * Bz;
+    R centrifugal;
+    if (P.polar_sources) {
+      centrifugal = (rho * omega * omega * r2_3) / r_1 * (R)sin(.5 * dphi) / (R)(.5 * dphi);
+      centrifugal -= Bp * Bp / r_1;
+    } else {
+      centrifugal = rho * omega * omega * r - Bp * Bp / r;
+    }
+    R press_bal = (Pp + (R).5 * B2) / r_1;
+    cons[SRR] += dVdt * (double)(centrifugal + press_bal);
+    R om = get_om<R>(P, r), om1 = get_om1<R>(P, r);
+    cons[TAU] += ((dVdt * (double)rho) * (double)vr) * (double)(om * om * r2_3 / r_1 - om1 * (omega - om) * r2_3);
+    if (P.include_viscosity)
+      cons[SRR] += -dVdt * P.explicit_viscosity * (double)rho * (double)vr / (double)(r_1 * r_1);
+  }
+
+  // mhd.c defines neither visc_flux nor visc_source with content.
+  DISCO_D static void visc_flux(const DevParams&, const DevPlanet*, const R*, const R*, const R*,
+                                const R*, R*, R, R, const R*) {}
+  DISCO_D static void visc_source(const DevParams&, const DevPlanet*, const R*, const R*, const R*,
+                                  const R*, double*, const double*, const double*, double) {}
+
+  // flux_to_E, mhd.c:293-316: edge EMFs from the face flux / star state.
+  DISCO_D static void flux_to_E(const R* Flux, const R* Ustr, R r, R* E1, R* B1, R* E2, R* B2,
+                                int dim) {
+    R irfac = (R)1.0 / ((R)1.0 / r);
+    if (dim == 0) {
+      *E1 = Flux[BRR] * irfac; *B1 = Ustr[BRR] * irfac; *E2 = -Flux[BZZ]; *B2 = Ustr[BZZ];
+    } else if (dim == 1) {
+      *E1 = -Flux[BPP] * r; *B1 = Ustr[BRR] * irfac; *E2 = Flux[BZZ];
+    } else {
+      *E1 = Flux[BPP] * r; *B1 = Ustr[BZZ]; *E2 = -Flux[BRR] * irfac;
+    }
+  }
+
+  // HLL/HLLC paths of solve_riemann are not used with this module here
+  // (configurations select HLLD, Riemann_Solver 2); rejected at set-up.
+  DISCO_D static void vel(const DevParams&, const R*, const R*, R* Sl, R* Sr, R* Ss, const R*, R,
+                          R*) { *Sl = -1; *Sr = 1; *Ss = 0; }
+  DISCO_D static void getUstar(const DevParams&, const R*, R* U, R, R, R, const R*, const R*) {
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) U[q] = 0;
+  }
+
+  // ---- hlld.c ----------------------------------------------------------------
+  DISCO_D static void h_velocities(R gam, const R* pL, const R* pR, const R* n, R* vel, R* Pt_star) {
+    R rho_L = pL[RHO], P_L = pL[PPP];
+    R u_L = pL[URR] * n[0] + pL[UPP] * n[1] + pL[UZZ] * n[2];
+    R Bn_L = pL[BRR] * n[0] + pL[BPP] * n[1] + pL[BZZ] * n[2];
+    R B2_L = pL[BRR] * pL[BRR] + pL[BPP] * pL[BPP] + pL[BZZ] * pL[BZZ];
+    R Pt_L = P_L + (R).5 * B2_L;
+    R rho_R = pR[RHO], P_R = pR[PPP];
+    R u_R = pR[URR] * n[0] + pR[UPP] * n[1] + pR[UZZ] * n[2];
+    R Bn_R = pR[BRR] * n[0] + pR[BPP] * n[1] + pR[BZZ] * n[2];
+    R B2_R = pR[BRR] * pR[BRR] + pR[BPP] * pR[BPP] + pR[BZZ] * pR[BZZ];
+    R Pt_R = P_R + (R).5 * B2_R;
+    R Bn = (R).5 * (Bn_L + Bn_R);
+    R aL = gam * P_L + B2_L, aR = gam * P_R + B2_R;
+    R cf2_L = (R).5 * (gam * P_L + B2_L + sqrt(fabs(aL * aL - (R)4. * gam * P_L * Bn_L * Bn_L))) / rho_L;
+    R cf2_R = (R).5 * (gam * P_R + B2_R + sqrt(fabs(aR * aR - (R)4. * gam * P_R * Bn_R * Bn_R))) / rho_R;
+    R cf2 = cf2_L > cf2_R ? cf2_L : cf2_R;
+    R umin, umax;
+    if (u_L < u_R) { umin = u_L; umax = u_R; } else { umin = u_R; umax = u_L; }
+    R S_R = umax + sqrt(fabs(cf2));
+    R S_L = umin - sqrt(fabs(cf2));
+    R S_M = ((S_R - u_R) * rho_R * u_R - (S_L - u_L) * rho_L * u_L - Pt_R + Pt_L) /
+            ((S_R - u_R) * rho_R - (S_L - u_L) * rho_L);
+    R rhostar_L = rho_L * (S_L - u_L) / (S_L - S_M);
+    R rhostar_R = rho_R * (S_R - u_R) / (S_R - S_M);
+    vel[0] = S_L;
+    vel[1] = S_M - fabs(Bn) / sqrt(rhostar_L);
+    vel[2] = S_M;
+    vel[3] = S_M + fabs(Bn) / sqrt(rhostar_R);
+    vel[4] = S_R;
+    R num = (S_R - u_R) * rho_R * Pt_L - (S_L - u_L) * rho_L * Pt_R +
+            rho_L * rho_R * (S_R - u_R) * (S_L - u_L) * (u_R - u_L);
+    R denom = (S_R - u_R) * rho_R - (S_L - u_L) * rho_L;
+    *Pt_star = num / denom;
+  }
+  DISCO_D static void h_prim_to_cons(R gam, const R* p, R* c) {
+    R rho = p[RHO], Pp = p[PPP], vx = p[URR], vy = p[UPP], vz = p[UZZ];
+    R Bx = p[BRR], By = p[BPP], Bz = p[BZZ];
+    R v2 = vx * vx + vy * vy + vz * vz;
+    R rhoe = Pp / (gam - (R)1.);
+    R B2 = Bx * Bx + By * By + Bz * Bz;
+    c[DDD] = rho; c[SRR] = rho * vx; c[LLL] = rho * vy; c[SZZ] = rho * vz;
+    c[TAU] = ((R).5 * rho * v2 + rhoe + (R).5 * B2);
+    c[BRR] = Bx; c[BPP] = By; c[BZZ] = Bz;
+  }
+  DISCO_D static void h_flux(R gam, const R* p, R* f, const R* n) {
+    R rho = p[RHO], Pp = p[PPP], vx = p[URR], vy = p[UPP], vz = p[UZZ];
+    R Bx = p[BRR], By = p[BPP], Bz = p[BZZ];
+    R v2 = vx * vx + vy * vy + vz * vz;
+    R vB = vx * Bx + vy * By + vz * Bz;
+    R B2 = Bx * Bx + By * By + Bz * Bz;
+    R vn = vx * n[0] + vy * n[1] + vz * n[2];
+    R Bn = Bx * n[0] + By * n[1] + Bz * n[2];
+    R rhoe = Pp / (gam - (R)1.);
+    f[DDD] = rho * vn;
+    f[SRR] = rho * vx * vn + (Pp + (R).5 * B2) * n[0] - Bx * Bn;
+    f[LLL] = rho * vy * vn + (Pp + (R).5 * B2) * n[1] - By * Bn;
+    f[SZZ] = rho * vz * vn + (Pp + (R).5 * B2) * n[2] - Bz * Bn;
+    f[TAU] = ((R).5 * rho * v2 + rhoe + Pp + B2) * vn - vB * Bn;
+    f[BRR] = Bx * vn - vx * Bn;
+    f[BPP] = By * vn - vy * Bn;
+    f[BZZ] = Bz * vn - vz * Bn;
+  }
+  DISCO_D static void h_single_star(R gam, const R* p, R* Us, R S_K, R S_M, R Pt_star, const R* n) {
+    R rho = p[RHO], vx = p[URR], vy = p[UPP], vz = p[UZZ], Pp = p[PPP];
+    R Bx = p[BRR], By = p[BPP], Bz = p[BZZ];
+    R u_K = vx * n[0] + vy * n[1] + vz * n[2];
+    R Bn = Bx * n[0] + By * n[1] + Bz * n[2];
+    R vdotB = vx * Bx + vy * By + vz * Bz;
+    R v2 = vx * vx + vy * vy + vz * vz;
+    R B2 = Bx * Bx + By * By + Bz * Bz;
+    R Pt = Pp + (R).5 * B2;
+    R e = (R).5 * rho * v2 + Pp / (gam - (R)1.) + (R).5 * B2;
+    R rhostar = rho * (S_K - u_K) / (S_K - S_M);
+    R denom = rho * (S_K - u_K) * (S_K - S_M) - Bn * Bn;
+    if (fabs(denom) < (R)1e-10) denom = (R)1e-10;   // hlld.c:12 TOL
+    R vx_s = vx - Bn * Bx * (S_M - u_K) / denom;
+    R vy_s = vy - Bn * By * (S_M - u_K) / denom;
+    R vz_s = vz - Bn * Bz * (S_M - u_K) / denom;
+    R sq = (S_K - u_K) * (S_K - u_K);
+    R Bx_s = Bx * (rho * sq - Bn * Bn) / denom;
+    R By_s = By * (rho * sq - Bn * Bn) / denom;
+    R Bz_s = Bz * (rho * sq - Bn * Bn) / denom;
+    R vn_s = vx_s * n[0] + vy_s * n[1] + vz_s * n[2];
+    R Bn_s = Bx_s * n[0] + By_s * n[1] + Bz_s * n[2];
+    vx_s += (S_M - vn_s) * n[0]; vy_s += (S_M - vn_s) * n[1]; vz_s += (S_M - vn_s) * n[2];
+    Bx_s += (Bn - Bn_s) * n[0]; By_s += (Bn - Bn_s) * n[1]; Bz_s += (Bn - Bn_s) * n[2];
+    R vB_s = vx_s * Bx_s + vy_s * By_s + vz_s * Bz_s;
+    R e_s = ((S_K - u_K) * e - Pt * u_K + Pt_star * S_M + Bn * (vdotB - vB_s)) / (S_K - S_M);
+    Us[DDD] = rhostar; Us[SRR] = rhostar * vx_s; Us[LLL] = rhostar * vy_s; Us[SZZ] = rhostar * vz_s;
+    Us[TAU] = e_s; Us[BRR] = Bx_s; Us[BPP] = By_s; Us[BZZ] = Bz_s;
+  }
+  DISCO_D static void h_double_star(const R* UsL, const R* UsR, R* Uss, const R* vel, const R* n, int LR) {
+    R rho_L = UsL[DDD], rho_R = UsR[DDD];
+    R rhostar_K = LR == 0 ? rho_L : rho_R;
+    R rrh_L = sqrt(rho_L), rrh_R = sqrt(rho_R), rrh_K = sqrt(rhostar_K);
+    R vx_L = UsL[SRR] / rho_L, vy_L = UsL[LLL] / rho_L, vz_L = UsL[SZZ] / rho_L;
+    R Bx_L = UsL[BRR], By_L = UsL[BPP], Bz_L = UsL[BZZ];
+    R vx_R = UsR[SRR] / rho_R, vy_R = UsR[LLL] / rho_R, vz_R = UsR[SZZ] / rho_R;
+    R Bx_R = UsR[BRR], By_R = UsR[BPP], Bz_R = UsR[BZZ];
+    R Bn_L = Bx_L * n[0] + By_L * n[1] + Bz_L * n[2];
+    R Bn_R = Bx_R * n[0] + By_R * n[1] + Bz_R * n[2];
+    R Bn = (R).5 * (Bn_L + Bn_R);
+    R sB = Bn > (R)0.0 ? (R)1.0 : (R)-1.0;
+    R den = rrh_L + rrh_R;
+    R vx = (rrh_L * vx_L + rrh_R * vx_R + (Bx_R - Bx_L) * sB) / den;
+    R vy = (rrh_L * vy_L + rrh_R * vy_R + (By_R - By_L) * sB) / den;
+    R vz = (rrh_L * vz_L + rrh_R * vz_R + (Bz_R - Bz_L) * sB) / den;
+    R vn = vx * n[0] + vy * n[1] + vz * n[2];
+    vx += (vel[2] - vn) * n[0]; vy += (vel[2] - vn) * n[1]; vz += (vel[2] - vn) * n[2];
+    R Bx = (rrh_L * Bx_R + rrh_R * Bx_L + rrh_L * rrh_R * (vx_R - vx_L) * sB) / den;
+    R By = (rrh_L * By_R + rrh_R * By_L + rrh_L * rrh_R * (vy_R - vy_L) * sB) / den;
+    R Bz = (rrh_L * Bz_R + rrh_R * Bz_L + rrh_L * rrh_R * (vz_R - vz_L) * sB) / den;
+    R Bns = Bx * n[0] + By * n[1] + Bz * n[2];
+    Bx += (Bn - Bns) * n[0]; By += (Bn - Bns) * n[1]; Bz += (Bn - Bns) * n[2];
+    R vB_ss = vx * Bx + vy * By + vz * Bz;
+    R vBstar, e_star;
+    if (LR == 0) { vBstar = vx_L * Bx_L + vy_L * By_L + vz_L * Bz_L; e_star = UsL[TAU]; }
+    else { vBstar = vx_R * Bx_R + vy_R * By_R + vz_R * Bz_R; e_star = UsR[TAU]; }
+    R pm = LR == 1 ? (R)1.0 : (R)-1.0;
+    R e_ss = e_star + pm * rrh_K * (vBstar - vB_ss) * sB;
+    Uss[DDD] = rhostar_K; Uss[SRR] = rhostar_K * vx; Uss[LLL] = rhostar_K * vy; Uss[SZZ] = rhostar_K * vz;
+    Uss[TAU] = e_ss; Uss[BRR] = Bx; Uss[BPP] = By; Uss[BZZ] = Bz;
+  }
+  // get_Ustar_HLLD, hlld.c:282-401
+  DISCO_D static void hlld(const DevParams& P, R w, const R* primL, const R* primR, R* F, R* U, R r,
+                           const R* n) {
+    R gam = (R)P.gamma_law;
+    R vel[5], Pt_star;
+    R hr = 1.0, hp = r, hz = 1.0;
+    R pL[NQ], pR[NQ];
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) { pL[q] = primL[q]; pR[q] = primR[q]; }
+    pL[URR] *= hr; pR[URR] *= hr;
+    pL[UPP] *= hp; pR[UPP] *= hp;
+    pL[UZZ] *= hz; pR[UZZ] *= hz;
+    h_velocities(gam, pL, pR, n, vel, &Pt_star);
+    if (w < vel[2]) {
+      R UL[8];
+      h_flux(gam, pL, F, n);
+      h_prim_to_cons(gam, pL, UL);
+      if (w < vel[0]) {
+        h_prim_to_cons(gam, pL, U);
+      } else if (w < vel[1]) {
+        h_single_star(gam, pL, U, vel[0], vel[2], Pt_star, n);
+#pragma unroll
+        for (int q = 0; q < 8; ++q) F[q] += vel[0] * (U[q] - UL[q]);
+      } else {
+        R UsL[8], UsR[8];
+        h_single_star(gam, pL, UsL, vel[0], vel[2], Pt_star, n);
+        h_single_star(gam, pR, UsR, vel[4], vel[2], Pt_star, n);
+        h_double_star(UsL, UsR, U, vel, n, 0);
+#pragma unroll
+        for (int q = 0; q < 8; ++q) F[q] += vel[1] * (U[q] - UsL[q]) + vel[0] * (UsL[q] - UL[q]);
+      }
+#pragma unroll
+      for (int q = 8; q < NQ; ++q) { U[q] = pL[q] * U[DDD]; F[q] = pL[q] * F[DDD]; }
+    } else {
+      R UR[8];
+      h_flux(gam, pR, F, n);
+      h_prim_to_cons(gam, pR, UR);
+      if (w > vel[4]) {
+        h_prim_to_cons(gam, pR, U);
+      } else if (w > vel[3]) {
+        h_single_star(gam, pR, U, vel[4], vel[2], Pt_star, n);
+#pragma unroll
+        for (int q = 0; q < 8; ++q) F[q] += vel[4] * (U[q] - UR[q]);
+      } else {
+        R UsL[8], UsR[8];
+        h_single_star(gam, pL, UsL, vel[0], vel[2], Pt_star, n);
+        h_single_star(gam, pR, UsR, vel[4], vel[2], Pt_star, n);
+        h_double_star(UsL, UsR, U, vel, n, 1);
+#pragma unroll
+        for (int q = 0; q < 8; ++q) F[q] += vel[3] * (U[q] - UsR[q]) + vel[4] * (UsR[q] - UR[q]);
+      }
+#pragma unroll
+      for (int q = 8; q < NQ; ++q) { U[q] = pR[q] * U[DDD]; F[q] = pR[q] * F[DDD]; }
+    }
+    R brfac = (R)1.0 / r, bpfac = 1.0, bzfac = 1.0;
+    F[SRR] *= hr; F[LLL] *= hp; F[SZZ] *= hz;
+    F[BRR] *= brfac / hr; F[BPP] *= bpfac / hp; F[BZZ] *= bzfac / hz;
+    U[SRR] *= hr; U[LLL] *= hp; U[SZZ] *= hz;
+    U[BRR] *= brfac / hr; U[BPP] *= bpfac / hp; U[BZZ] *= bzfac / hz;
+  }
+
+  // mindt, mhd.c:452-483
+  DISCO_D static double mindt(const DevParams& P, const DevPlanet*, const R* prim, double w,
+                              const double* xp, const double* xm) {
+    double r = centroid_r(xp[0], xm[0]);
+    R Pp = prim[PPP], rho = prim[RHO];
+    R vp = (R)((double)prim[UPP] - w) * (R)r;
+    R vr = prim[URR], vz = prim[UZZ];
+    R cs = sqrt((R)P.gamma_law * Pp / rho);
+    R Br = prim[BRR], Bp = prim[BPP], Bz = prim[BZZ];
+    R b2 = (Br * Br + Bp * Bp + Bz * Bz) / rho;
+    R cf = sqrt(cs * cs + b2);
+    R maxvr = cf + fabs(vr), maxvp = cf + fabs(vp), maxvz = cf + fabs(vz);
+    double dL1 = xp[0] - xm[0];
+    double dL0 = .5 * (xp[0] + xm[0]) * get_dp(xp[1], xm[1], P.phi_max);
+    double dL2 = xp[2] - xm[2];
+    double dt = dL1 / (double)maxvr;
+    double dtp = dL0 / (double)maxvp;
+    double dtz = dL2 / (double)maxvz;
+    if (dt > dtp) dt = dtp;
+    if (dt > dtz) dt = dtz;
+    return dt;
+  }
+};
+
+}  // namespace disco
