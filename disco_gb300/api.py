@@ -123,6 +123,8 @@ SIGNATURES = {
     "disco_gpu_run_timed": (C.c_int, [_P, C.c_int, C.c_double, C.c_size_t, C.POINTER(C.c_double)]),
     "disco_gpu_profile": (C.c_int, [_P, C.c_int, C.POINTER(DiscoKernelTime), C.c_int,
                                     C.POINTER(C.c_int)]),
+    "disco_gpu_debug_ct": (C.c_int, [_P, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                     C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     "disco_gpu_time": (C.c_double, [_P]),
     "disco_gpu_num_cells": (C.c_long, [_P]),
     "disco_gpu_num_real_cells": (C.c_long, [_P]),
@@ -270,8 +272,11 @@ class Domain:
         out["cons"] = np.empty((q, n))
         v = DiscoStateView()
         dp = C.POINTER(C.c_double)
-        for k in ("piph", "dphi", "wiph", "prim", "cons"):
-            setattr(v, k, out[k].ctypes.data_as(dp))
+        if self.host.num_q >= 8:
+            out["Phi"] = np.zeros((5, n))
+        for k in ("piph", "dphi", "wiph", "prim", "cons", "Phi"):
+            if k in out:
+                setattr(v, k, out[k].ctypes.data_as(dp))
         _check(lib().disco_gpu_download(self._g, C.byref(v)), "disco_gpu_download")
         out["t"] = v.t
         return out

@@ -26,7 +26,13 @@ NVCC_FLAGS = ["-std=c++17", "-O3", GENCODE, "-lineinfo", "-Xcompiler", "-fPIC",
 CC_FLAGS = ["-std=gnu11", "-O2", "-fPIC", "-Wall", "-ffp-contract=off"]
 
 HOST_SOURCES = ["host/disco_host.c"]
-CUDA_SOURCES = ["cuda/disco_gpu.cu", "cuda/disco_gpu_euler.cu", "cuda/disco_gpu_mhd.cu"]
+# (source, extra nvcc flags): the plain-FP64 instances are compiled without
+# FMA contraction so their FP64 arithmetic rounds like the reference's C build.
+CUDA_SOURCES = [("cuda/disco_gpu.cu", []),
+                ("cuda/inst_euler_f64.cu", ["--fmad=false"]),
+                ("cuda/inst_euler_f32.cu", []),
+                ("cuda/inst_mhd_f64.cu", ["--fmad=false"]),
+                ("cuda/inst_mhd_f32.cu", [])]
 
 
 def _nvcc() -> str:
@@ -64,9 +70,9 @@ def build(force: bool = False, verbose: bool = False) -> str:
         obj = os.path.join(LIBDIR, "obj", os.path.basename(src) + ".o")
         jobs.append(["gcc", *CC_FLAGS, f"-I{INCLUDE}", "-c", os.path.join(CSRC, src), "-o", obj])
         objs.append(obj)
-    for src in CUDA_SOURCES:
+    for src, extra in CUDA_SOURCES:
         obj = os.path.join(LIBDIR, "obj", os.path.basename(src) + ".o")
-        jobs.append([nvcc, *NVCC_FLAGS, f"-I{INCLUDE}", "-c", os.path.join(CSRC, src), "-o", obj])
+        jobs.append([nvcc, *NVCC_FLAGS, *extra, f"-I{INCLUDE}", "-c", os.path.join(CSRC, src), "-o", obj])
         objs.append(obj)
     with cf.ThreadPoolExecutor(max_workers=len(jobs)) as ex:
         for cmd, fut in [(c, ex.submit(_run, c)) for c in jobs]:

@@ -1,13 +1,16 @@
 // C-ABI entry points of the GB300 RK substep cycle.  The per-module
 // instances live in disco_gpu_euler.cu / disco_gpu_mhd.cu.
 #include "instance.cuh"
+#include "disco_gpu_debug.h"
 
 std::atomic<long long> g_launches{0};
 long long disco_gpu_launch_count(void) { return g_launches.load(); }
 
 namespace disco_impl {
-InstanceBase* make_euler(const disco_host_domain* dom, int precision, int* rc);
-InstanceBase* make_mhd(const disco_host_domain* dom, int precision, int* rc);
+InstanceBase* make_euler_double(const disco_host_domain* dom, int* rc);
+InstanceBase* make_euler_float(const disco_host_domain* dom, int* rc);
+InstanceBase* make_mhd_double(const disco_host_domain* dom, int* rc);
+InstanceBase* make_mhd_float(const disco_host_domain* dom, int* rc);
 }
 using namespace disco_impl;
 
@@ -26,8 +29,11 @@ int disco_gpu_create(const disco_host_domain* dom, int precision, disco_gpu** ou
     return DISCO_E_NODEV;
   }
   int rc = 0;
-  InstanceBase* impl = dom->mod.hydro == DISCO_HYDRO_EULER ? make_euler(dom, precision, &rc)
-                                                           : make_mhd(dom, precision, &rc);
+  InstanceBase* impl;
+  if (dom->mod.hydro == DISCO_HYDRO_EULER)
+    impl = precision ? make_euler_float(dom, &rc) : make_euler_double(dom, &rc);
+  else
+    impl = precision ? make_mhd_float(dom, &rc) : make_mhd_double(dom, &rc);
   if (!impl) return rc ? rc : DISCO_E_CUDA;
   *out = new disco_gpu{impl};
   return 0;
@@ -65,6 +71,10 @@ int disco_gpu_profile(disco_gpu* g, int nsteps, disco_kernel_time* out, int max_
 int disco_gpu_status(disco_gpu* g, disco_gpu_errs* e) {
   if (!g || !e) { disco_set_error("null argument"); return DISCO_E_ARG; }
   return g->impl->status(e);
+}
+int disco_gpu_debug_ct(disco_gpu* g, int stage, double* E, double* B, double* Ephi, double* Phi) {
+  if (!g || stage < 0 || stage > 4) { disco_set_error("bad argument"); return DISCO_E_ARG; }
+  return g->impl->debug_ct(stage, E, B, Ephi, Phi);
 }
 double disco_gpu_time(disco_gpu* g) { return g ? g->impl->time() : 0.0; }
 long disco_gpu_num_cells(disco_gpu* g) { return g ? g->impl->N : 0; }

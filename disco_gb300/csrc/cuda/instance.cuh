@@ -45,6 +45,7 @@ struct InstanceBase {
   virtual int run_timed(int n, double t_end, size_t flush_bytes, double* ms) = 0;
   virtual int profile(int n, disco_kernel_time* out, int maxo, int* nout) = 0;
   virtual double time() = 0;
+  virtual int debug_ct(int stage, double* E, double* B, double* Ephi, double* Phi) = 0;
   long N = 0, Nreal = 0;
 };
 
@@ -106,6 +107,7 @@ struct Instance : InstanceBase {
   int planets_id = 0;
   cudaGraphExec_t graph[2] = {nullptr, nullptr};
   size_t edge_smem = 0;
+  int maxring = 0;
   int graph_nodes = 0;
   double host_t = 0;
 
@@ -188,6 +190,9 @@ struct Instance : InstanceBase {
       return DISCO_E_MODULE;
     }
 
+    for (int jk = 0; jk < nring; ++jk) maxring = std::max(maxring, dom->Np[jk]);
+    if ((maxring + 1) * 8 > 48 * 1024)
+      CK(cudaFuncSetAttribute(k_wcell_avg<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (maxring + 1) * 8));
     // ---- index arrays
     std::vector<int> ring_off(nring + 1), cell_ring(N);
     for (int jk = 0; jk <= nring; ++jk) ring_off[jk] = (int)dom->ring_off[jk];
@@ -260,8 +265,6 @@ struct Instance : InstanceBase {
       CK(cudaMemset(S.Eraw, 0, sizeof(double) * 8 * N)); CK(cudaMemset(S.Braw, 0, sizeof(double) * 8 * N));
       CK(cudaMemset(C.Phi, 0, sizeof(double) * 5 * N)); CK(cudaMemset(C.RKPhi, 0, sizeof(double) * 5 * N));
       CK(cudaMemset(C.Ephi, 0, sizeof(double) * 4 * N)); CK(cudaMemset(C.errs, 0, 8));
-      int maxring = 0;
-      for (int jk = 0; jk < nring; ++jk) maxring = std::max(maxring, dom->Np[jk]);
       edge_smem = (size_t)4 * maxring * 8;
       if (edge_smem > 48 * 1024)
         CK(cudaFuncSetAttribute(k_ct_edge<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)edge_smem));
@@ -313,7 +316,8 @@ struct Instance : InstanceBase {
   // ---- launch helpers -----------------------------------------------------
   void launch_wcell() {
     LAUNCH("wcell", (k_wcell<R, NQ><<<blocks(N), 256, 0, st>>>(P, S)));
-    if (P.mesh_motion == 3) LAUNCH("wcell_avg", (k_wcell_avg<R><<<nring, 256, 0, st>>>(P, S)));
+    if (P.mesh_motion == 3)
+      LAUNCH("wcell_avg", (k_wcell_avg<R><<<nring, 256, (maxring + 1) * sizeof(double), st>>>(P, S)));
   }
   void launch_boundary() {
     LAUNCH("boundary", (k_boundary<R, NQ><<<blocks(N), 256, 0, st>>>(P, S)));
@@ -331,23 +335,20 @@ struct Instance : InstanceBase {
     LAUNCH("mindt", (k_mindt<Phys, R, NQ><<<blocks(N), 256, 0, st>>>(P, S)));
     LAUNCH("dt_finalize", (k_dt_finalize<<<1, 1, 0, st>>>(P, S.scal)));
   }
-  // one onestep (onestep.c:86-186)
-  void substep(double RK, double fac, int first) {
-    if (first) launch_wcell();
-    LAUNCH("plm_phi", (k_plm_phi<R, NQ><<<blocks(N), 256, 0, st>>>(P, S)));
-    if (Nr > 1) LAUNCH("plm_trans_r", (k_plm_trans<R, NQ><<<blocks(N), 256, 0, st>>>(P, S, 1)));
-    if (Nz > 1) LAUNCH("plm_trans_z", (k_plm_trans<R, NQ><<<blocks(N), 256, 0, st>>>(P, S, 2)));
-    LAUNCH("flux_phi", (k_flux_phi<Phys, R, NQ><<<blocks(N), 256, 0, st>>>(P, S, fac)));
+  void launch_trans_fluxes(double fac) {
     for (int d = 0; d < 2; ++d) {
       if (!npair[d]) continue;
       int dim = d + 1;
       int jmin, jmax, kmin, kmax;
+      // misc.c:464-500; with CT one more layer across the other dimension
       if (dim == 1) {
         jmin = P.NgRa == 0 ? 0 : P.NgRa - 1;
         jmax = P.NgRb == 0 ? Nr - 1 : Nr - P.NgRb;
-        kmin = P.NgZa; kmax = Nz - P.NgZb;
+        if (ct) { kmin = P.NgZa == 0 ? 0 : P.NgZa - 1; kmax = P.NgZb == 0 ? Nz : Nz - P.NgZb + 1; }
+        else { kmin = P.NgZa; kmax = Nz - P.NgZb; }
       } else {
-        jmin = P.NgRa; jmax = Nr - P.NgRb;
+        if (ct) { jmin = P.NgRa == 0 ? 0 : P.NgRa - 1; jmax = P.NgRb == 0 ? Nr : Nr - P.NgRb + 1; }
+        else { jmin = P.NgRa; jmax = Nr - P.NgRb; }
         kmin = P.NgZa == 0 ? 0 : P.NgZa - 1;
         kmax = P.NgZb == 0 ? Nz - 1 : Nz - P.NgZb;
       }
@@ -357,6 +358,15 @@ struct Instance : InstanceBase {
       LAUNCH(dim == 1 ? "flux_r" : "flux_z",
              (k_flux_trans<Phys, R, NQ><<<grid, 256, 0, st>>>(P, S, dim, jmin, jc, kmin, fac)));
     }
+  }
+  // one onestep (onestep.c:86-186)
+  void substep(double RK, double fac, int first) {
+    if (first) launch_wcell();
+    LAUNCH("plm_phi", (k_plm_phi<R, NQ><<<blocks(N), 256, 0, st>>>(P, S)));
+    if (Nr > 1) LAUNCH("plm_trans_r", (k_plm_trans<R, NQ><<<blocks(N), 256, 0, st>>>(P, S, 1)));
+    if (Nz > 1) LAUNCH("plm_trans_z", (k_plm_trans<R, NQ><<<blocks(N), 256, 0, st>>>(P, S, 2)));
+    LAUNCH("flux_phi", (k_flux_phi<Phys, R, NQ><<<blocks(N), 256, 0, st>>>(P, S, fac)));
+    launch_trans_fluxes(fac);
     if (ct) {   // avg_Efields, subtract_advective_B_fluxes, update_B_fluxes (onestep.c:261-265)
       LAUNCH("ct_gather", (k_ct_gather<R><<<blocks(N), 256, 0, st>>>(P, S, C, RK, first)));
       LAUNCH("ct_avg", (k_ct_avg<R><<<blocks(N), 256, 0, st>>>(P, S, C)));
@@ -520,12 +530,49 @@ struct Instance : InstanceBase {
     host_t = sc[SC_T];
     return 0;
   }
+  int debug_ct(int stage, double* E, double* B, double* Ephi, double* Phi) override {
+    if (!ct) { disco_set_error("debug_ct: not a CT instance"); return DISCO_E_STATE; }
+    P.t_end = 0.0;
+    launch_mindt();
+    const double RK = 0.0, fac = 1.0;
+    const int first = 1;
+    launch_wcell();
+    LAUNCH("plm_phi", (k_plm_phi<R, NQ><<<blocks(N), 256, 0, st>>>(P, S)));
+    if (Nr > 1) LAUNCH("plm_trans_r", (k_plm_trans<R, NQ><<<blocks(N), 256, 0, st>>>(P, S, 1)));
+    if (Nz > 1) LAUNCH("plm_trans_z", (k_plm_trans<R, NQ><<<blocks(N), 256, 0, st>>>(P, S, 2)));
+    LAUNCH("flux_phi", (k_flux_phi<Phys, R, NQ><<<blocks(N), 256, 0, st>>>(P, S, fac)));
+    if (stage >= 1) {
+      launch_trans_fluxes(fac);
+      LAUNCH("ct_gather", (k_ct_gather<R><<<blocks(N), 256, 0, st>>>(P, S, C, RK, first)));
+    }
+    if (stage >= 2) LAUNCH("ct_avg", (k_ct_avg<R><<<blocks(N), 256, 0, st>>>(P, S, C)));
+    if (stage >= 3) LAUNCH("ct_bflux", (k_ct_bflux<R><<<blocks(N), 256, 0, st>>>(P, S, C, fac)));
+    if (stage >= 4 && Nz > 1)
+      LAUNCH("ct_edge", (k_ct_edge<R><<<(Nr - 1) * (Nz - 1), 256, edge_smem, st>>>(P, S, C, fac)));
+    CK(cudaStreamSynchronize(st));
+    CK(cudaGetLastError());
+    if (stage == 2) {
+      if (E) {
+        std::vector<double> t((size_t)4 * N);
+        CK(cudaMemcpy(t.data(), C.Efin, sizeof(double) * 4 * N, cudaMemcpyDeviceToHost));
+        const int slot[4] = {0, 1, 4, 5};
+        for (int q = 0; q < 4; ++q) memcpy(E + (size_t)slot[q] * N, t.data() + (size_t)q * N, sizeof(double) * N);
+      }
+    } else {
+      if (E) CK(cudaMemcpy(E, S.Eraw, sizeof(double) * 8 * N, cudaMemcpyDeviceToHost));
+      if (B) CK(cudaMemcpy(B, S.Braw, sizeof(double) * 8 * N, cudaMemcpyDeviceToHost));
+    }
+    if (Ephi) CK(cudaMemcpy(Ephi, C.Ephi, sizeof(double) * 4 * N, cudaMemcpyDeviceToHost));
+    if (Phi) CK(cudaMemcpy(Phi, C.Phi, sizeof(double) * 5 * N, cudaMemcpyDeviceToHost));
+    return 0;
+  }
   int download(disco_state_view* v) override {
     CK(cudaStreamSynchronize(st));
     if (v->piph) CK(cudaMemcpy(v->piph, S.piph, sizeof(double) * N, cudaMemcpyDeviceToHost));
     if (v->dphi) CK(cudaMemcpy(v->dphi, S.dphi, sizeof(double) * N, cudaMemcpyDeviceToHost));
     if (v->wiph) CK(cudaMemcpy(v->wiph, S.wiph, sizeof(double) * N, cudaMemcpyDeviceToHost));
     if (v->cons) CK(cudaMemcpy(v->cons, S.cons, sizeof(double) * NQ * N, cudaMemcpyDeviceToHost));
+    if (v->Phi && ct) CK(cudaMemcpy(v->Phi, C.Phi, sizeof(double) * 5 * N, cudaMemcpyDeviceToHost));
     if (v->prim) {
       if (sizeof(R) == sizeof(double)) {
         CK(cudaMemcpy(v->prim, S.prim, sizeof(double) * NQ * N, cudaMemcpyDeviceToHost));
@@ -563,6 +610,11 @@ struct Instance : InstanceBase {
     e->p_floor_hits = (long long)h.p_floor_hits;
     e->face_errors = (long long)h.face_errors;
     e->steps = (long long)h.steps;
+    if (ct) {
+      unsigned long long ce = 0;
+      CK(cudaMemcpy(&ce, C.errs, 8, cudaMemcpyDeviceToHost));
+      e->face_errors += (long long)ce;
+    }
     return 0;
   }
   double time() override { return host_t; }

@@ -125,21 +125,24 @@ __global__ void k_wcell(DevParams P, DevState<R> S) {
   S.wiph[c] = w;
 }
 
-// Mesh_Motion 3: ring average of w (misc.c:138-152), one block per ring.
+// Mesh_Motion 3: ring average of w (misc.c:138-152), one block per ring.  The
+// ring is staged in shared memory and summed by one thread in the
+// reference's order, so the mesh speed rounds exactly like the reference's
+// (it can coincide with a contact speed, where HLLD branches on equality).
 template <typename R>
 __global__ void k_wcell_avg(DevParams P, DevState<R> S) {
+  extern __shared__ double wsm[];
   int jk = blockIdx.x;
   int off = S.ring_off[jk], Np = S.ring_off[jk + 1] - off;
-  __shared__ double red[256];
-  double s = 0.0;
-  for (int i = threadIdx.x; i < Np; i += blockDim.x) s += S.wiph[off + i];
-  red[threadIdx.x] = s;
+  for (int i = threadIdx.x; i < Np; i += blockDim.x) wsm[i] = S.wiph[off + i];
   __syncthreads();
-  for (int h = blockDim.x / 2; h > 0; h >>= 1) {
-    if ((int)threadIdx.x < h) red[threadIdx.x] += red[threadIdx.x + h];
-    __syncthreads();
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (int i = 0; i < Np; ++i) s += wsm[i];
+    wsm[Np] = s / (double)Np;
   }
-  double w = red[0] / (double)Np;
+  __syncthreads();
+  double w = wsm[Np];
   for (int i = threadIdx.x; i < Np; i += blockDim.x) S.wiph[off + i] = w;
 }
 

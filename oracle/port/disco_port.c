@@ -1217,7 +1217,13 @@ static void make_edge_adjust(double dt)
    }
    free(I0);
 }
+static void update_B_fluxes_core(double dt);
 static void update_B_fluxes(double dt)
+{
+   update_B_fluxes_core(dt);
+   if(D->Nz > 1) make_edge_adjust(dt);
+}
+static void update_B_fluxes_core(double dt)
 {
    for(int d = 0; d < 2; d++) {
       if(d == 1 && D->Nz <= 1) break;
@@ -1242,7 +1248,6 @@ static void update_B_fluxes(double dt)
          n0 = Nf[jk];
       }
    }
-   if(D->Nz > 1) make_edge_adjust(dt);
 }
 static void check_flipped(int d)
 {
@@ -1574,4 +1579,33 @@ void disco_port_free(port_domain *d)
    free(d->cells); free(d->ring);
    free(d->faces[0]); free(d->faces[1]); free(d->fI[0]); free(d->fI[1]);
    free(d);
+}
+
+/* Stage dumps of the CT chain of the first substep (see disco_gpu_debug_ct). */
+int disco_port_debug_ct(port_domain *d, int stage, double *E, double *B, double *Ephi, double *Phi)
+{
+   D = d;
+   double dt = getmindt();
+   for(long c = 0; c < d->N; c++) {
+      memcpy(d->cells[c].RKcons, d->cells[c].cons, sizeof(double)*MAXQ);
+      memcpy(d->cells[c].RK_Phi, d->cells[c].Phi, sizeof(double)*5);
+   }
+   set_wcell();
+   plm_phi();
+   if(d->Nr > 1) { build_faces(1); plm_trans(1); }
+   if(d->Nz > 1) { build_faces(2); plm_trans(2); }
+   phi_flux(dt);
+   if(stage >= 1 && d->Nr > 1) trans_flux(dt, 1);
+   if(stage >= 1 && d->Nz > 1) trans_flux(dt, 2);
+   if(stage >= 2) { avg_Efields(); subtract_advective_B_fluxes(); }
+   if(stage >= 3) update_B_fluxes_core(dt);
+   if(stage >= 4 && d->Nz > 1) make_edge_adjust(dt);
+   long N = d->N;
+   for(long c = 0; c < N; c++) {
+      pcell *x = &d->cells[c];
+      for(int q = 0; q < 8; q++) { if(E) E[q*N + c] = x->E[q]; if(B) B[q*N + c] = x->B[q]; }
+      for(int q = 0; q < 4; q++) if(Ephi) Ephi[q*N + c] = x->E_phi[q];
+      for(int q = 0; q < 5; q++) if(Phi) Phi[q*N + c] = x->Phi[q];
+   }
+   return 0;
 }
