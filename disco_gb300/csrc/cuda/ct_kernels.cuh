@@ -13,18 +13,19 @@
 
 namespace disco {
 
-struct CtState {
-  double* Phi;      // [5*N]
+template <typename R>
+struct CtStateT {
+  double* Phi;      // [5*N] face fluxes: conserved, FP64 in both paths
   double* RKPhi;    // [5*N]
-  double* Efin;     // [4*N]: E0, E1, E4, E5 after averaging and advective subtraction
-  double* Ephi;     // [4*N]
+  R* Efin;          // [4*N]: E0, E1, E4, E5 after averaging and advective subtraction
+  R* Ephi;          // [4*N]
   unsigned long long* errs;  // [0] edge-order mismatches
   int last_pair[2]; // index of the last pair of each dimension (skipped by update_B_fluxes)
 };
 
 // ---- RK adjust of Phi + edge gathers (riemann.c:172-212) --------------------
 template <typename R>
-__global__ void k_ct_gather(DevParams P, DevState<R> S, CtState C, double RK, int first) {
+__global__ void k_ct_gather(DevParams P, DevState<R> S, CtStateT<R> C, double RK, int first) {
   int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= S.N) return;
   const int N = S.N;
@@ -37,7 +38,6 @@ __global__ void k_ct_gather(DevParams P, DevState<R> S, CtState C, double RK, in
   int jk = S.cell_ring[c];
   int j = jk % P.Nr, k = jk / P.Nr;
   if (!ring_in_phi_range(P, j, k)) return;
-  double dphic = S.dphi[c];
   for (int dim = 1; dim <= 2; ++dim) {
     if (dim == 1 && P.Nr <= 1) continue;
     if (dim == 2 && P.Nz <= 1) continue;
@@ -45,26 +45,26 @@ __global__ void k_ct_gather(DevParams P, DevState<R> S, CtState C, double RK, in
     const int a = 4 * d;
     int pb = pair_below(P, dim, j, k), pa = pair_above(P, dim, j, k);
     if (pb >= 0 && pair_in_flux_range(P, dim, pb)) {
-      double e0 = S.Eraw[(a + 0) * N + c], e2 = S.Eraw[(a + 2) * N + c];
-      double b0 = S.Braw[(a + 0) * N + c], b2 = S.Braw[(a + 2) * N + c];
+      R e0 = S.Eraw[(a + 0) * N + c], e2 = S.Eraw[(a + 2) * N + c];
+      R b0 = S.Braw[(a + 0) * N + c], b2 = S.Braw[(a + 2) * N + c];
       int base = S.face_off[d][pb], Nf = S.face_off[d][pb + 1] - base;
       for_run(S.run_dn_s[d][c], S.run_dn_e[d][c], base, Nf, [&](int f) {
-        double fr = S.fdphi[d][f] / dphic;
-        e0 += .5 * S.fErz[d][f] * fr; e2 += .5 * S.fErz[d][f] * fr;
-        b0 += .5 * S.fBrz[d][f] * fr; b2 += .5 * S.fBrz[d][f] * fr;
+        R fr = S.ffrR[d][f];
+        e0 += (R).5 * S.fErz[d][f] * fr; e2 += (R).5 * S.fErz[d][f] * fr;
+        b0 += (R).5 * S.fBrz[d][f] * fr; b2 += (R).5 * S.fBrz[d][f] * fr;
       });
       S.Eraw[(a + 0) * N + c] = e0; S.Eraw[(a + 2) * N + c] = e2;
       S.Braw[(a + 0) * N + c] = b0; S.Braw[(a + 2) * N + c] = b2;
       C.Ephi[(2 * d + 0) * N + c] = S.fEphi[d][S.run_dn_e[d][c]];
     }
     if (pa >= 0 && pair_in_flux_range(P, dim, pa)) {
-      double e1 = S.Eraw[(a + 1) * N + c], e3 = S.Eraw[(a + 3) * N + c];
-      double b1 = S.Braw[(a + 1) * N + c], b3 = S.Braw[(a + 3) * N + c];
+      R e1 = S.Eraw[(a + 1) * N + c], e3 = S.Eraw[(a + 3) * N + c];
+      R b1 = S.Braw[(a + 1) * N + c], b3 = S.Braw[(a + 3) * N + c];
       int base = S.face_off[d][pa], Nf = S.face_off[d][pa + 1] - base;
       for_run(S.run_up_s[d][c], S.run_up_e[d][c], base, Nf, [&](int f) {
-        double fr = S.fdphi[d][f] / dphic;
-        e1 += .5 * S.fErz[d][f] * fr; e3 += .5 * S.fErz[d][f] * fr;
-        b1 += .5 * S.fBrz[d][f] * fr; b3 += .5 * S.fBrz[d][f] * fr;
+        R fr = S.ffrL[d][f];
+        e1 += (R).5 * S.fErz[d][f] * fr; e3 += (R).5 * S.fErz[d][f] * fr;
+        b1 += (R).5 * S.fBrz[d][f] * fr; b3 += (R).5 * S.fBrz[d][f] * fr;
       });
       S.Eraw[(a + 1) * N + c] = e1; S.Eraw[(a + 3) * N + c] = e3;
       S.Braw[(a + 1) * N + c] = b1; S.Braw[(a + 3) * N + c] = b3;
@@ -77,7 +77,7 @@ __global__ void k_ct_gather(DevParams P, DevState<R> S, CtState C, double RK, in
 // d1: neighbour average along phi; d2: face average with the interpolated
 // value from the overlapping cell of the other ring; then E -= h w B.
 template <typename R>
-DISCO_D double edge_avg(const CtState& C, const DevState<R>& S, const double* A, int e, int x) {
+DISCO_D R edge_avg(const DevState<R>& S, const R* A, int e, int x) {
   // value of slot e of cell x after the phi-neighbour averaging pass
   const int N = S.N;
   int jk = S.cell_ring[x];
@@ -85,25 +85,25 @@ DISCO_D double edge_avg(const CtState& C, const DevState<R>& S, const double* A,
   int i = x - off;
   int xp = off + (i + 1 == Np ? 0 : i + 1), xm = off + (i == 0 ? Np - 1 : i - 1);
   int h = e & 4, s = e & 3;
-  if (s == 0) return .5 * (A[(h + 0) * N + x] + A[(h + 2) * N + xp]);
-  if (s == 1) return .5 * (A[(h + 1) * N + x] + A[(h + 3) * N + xp]);
-  if (s == 2) return .5 * (A[(h + 0) * N + xm] + A[(h + 2) * N + x]);
-  return .5 * (A[(h + 1) * N + xm] + A[(h + 3) * N + x]);
+  if (s == 0) return (R).5 * (A[(h + 0) * N + x] + A[(h + 2) * N + xp]);
+  if (s == 1) return (R).5 * (A[(h + 1) * N + x] + A[(h + 3) * N + xp]);
+  if (s == 2) return (R).5 * (A[(h + 0) * N + xm] + A[(h + 2) * N + x]);
+  return (R).5 * (A[(h + 1) * N + xm] + A[(h + 3) * N + x]);
 }
 
 template <typename R>
-__global__ void k_ct_avg(DevParams P, DevState<R> S, CtState C) {
+__global__ void k_ct_avg(DevParams P, DevState<R> S, CtStateT<R> C) {
   int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= S.N) return;
   const int N = S.N;
   int jk = S.cell_ring[c];
   int j = jk % P.Nr, k = jk / P.Nr;
-  double outE[4], outB[4];
+  R outE[4], outB[4];
   // slots: 0 -> E0 (r lower), 1 -> E1 (r upper), 2 -> E4 (z lower), 3 -> E5 (z upper)
   const int slot_e[4] = {0, 1, 4, 5};
   for (int s = 0; s < 4; ++s) {
-    outE[s] = edge_avg(C, S, S.Eraw, slot_e[s], c);
-    outB[s] = edge_avg(C, S, S.Braw, slot_e[s], c);
+    outE[s] = edge_avg(S, S.Eraw, slot_e[s], c);
+    outB[s] = edge_avg(S, S.Braw, slot_e[s], c);
   }
   for (int dim = 1; dim <= 2; ++dim) {
     if (dim == 1 && P.Nr <= 1) continue;
@@ -113,48 +113,44 @@ __global__ void k_ct_avg(DevParams P, DevState<R> S, CtState C) {
     if (pa >= 0) {   // LRtype 0 face owned by c (c = L = c1, c2 = R)
       int f = S.run_up_e[d][c];
       int c2 = S.fR[d][f];
-      double dp1 = get_dp(S.piph[c2], S.piph[c], P.phi_max);
-      double dp2 = S.dphi[c2] - dp1;
-      double Eavg = (dp2 * edge_avg(C, S, S.Eraw, a + 0, c2) + dp1 * edge_avg(C, S, S.Eraw, a + 2, c2)) / (dp1 + dp2);
-      double Bavg = (dp2 * edge_avg(C, S, S.Braw, a + 0, c2) + dp1 * edge_avg(C, S, S.Braw, a + 2, c2)) / (dp1 + dp2);
-      outE[2 * d + 1] = .5 * (outE[2 * d + 1] + Eavg);
-      outB[2 * d + 1] = .5 * (outB[2 * d + 1] + Bavg);
+      R dp1 = S.fdp1[d][f], dp2 = S.fdp2[d][f];
+      R Eavg = (dp2 * edge_avg(S, S.Eraw, a + 0, c2) + dp1 * edge_avg(S, S.Eraw, a + 2, c2)) / (dp1 + dp2);
+      R Bavg = (dp2 * edge_avg(S, S.Braw, a + 0, c2) + dp1 * edge_avg(S, S.Braw, a + 2, c2)) / (dp1 + dp2);
+      outE[2 * d + 1] = (R).5 * (outE[2 * d + 1] + Eavg);
+      outB[2 * d + 1] = (R).5 * (outB[2 * d + 1] + Bavg);
     }
     if (pb >= 0) {   // LRtype 1 face owned by c (c = R = c1, c2 = L)
       int f = S.run_dn_e[d][c];
       int c2 = S.fL[d][f];
-      double dp1 = get_dp(S.piph[c2], S.piph[c], P.phi_max);
-      double dp2 = S.dphi[c2] - dp1;
-      double Eavg = (dp2 * edge_avg(C, S, S.Eraw, a + 1, c2) + dp1 * edge_avg(C, S, S.Eraw, a + 3, c2)) / (dp1 + dp2);
-      double Bavg = (dp2 * edge_avg(C, S, S.Braw, a + 1, c2) + dp1 * edge_avg(C, S, S.Braw, a + 3, c2)) / (dp1 + dp2);
-      outE[2 * d + 0] = .5 * (outE[2 * d + 0] + Eavg);
-      outB[2 * d + 0] = .5 * (outB[2 * d + 0] + Bavg);
+      R dp1 = S.fdp1[d][f], dp2 = S.fdp2[d][f];
+      R Eavg = (dp2 * edge_avg(S, S.Eraw, a + 1, c2) + dp1 * edge_avg(S, S.Eraw, a + 3, c2)) / (dp1 + dp2);
+      R Bavg = (dp2 * edge_avg(S, S.Braw, a + 1, c2) + dp1 * edge_avg(S, S.Braw, a + 3, c2)) / (dp1 + dp2);
+      outE[2 * d + 0] = (R).5 * (outE[2 * d + 0] + Eavg);
+      outB[2 * d + 0] = (R).5 * (outB[2 * d + 0] + Bavg);
     }
   }
   const double* rj = S.r_jph + 1;
-  const double* zk = S.z_kph + 1;
   double hL = rj[j - 1], hR = rj[j];
   double hC = centroid_r(rj[j], rj[j - 1]);
   double w = S.wiph[c];
-  C.Efin[0 * N + c] = outE[0] - hL * w * outB[0];
-  C.Efin[1 * N + c] = outE[1] - hR * w * outB[1];
-  C.Efin[2 * N + c] = outE[2] + hC * w * outB[2];
-  C.Efin[3 * N + c] = outE[3] + hC * w * outB[3];
-  (void)zk;
+  C.Efin[0 * N + c] = outE[0] - (R)(hL * w) * outB[0];
+  C.Efin[1 * N + c] = outE[1] - (R)(hR * w) * outB[1];
+  C.Efin[2 * N + c] = outE[2] + (R)(hC * w) * outB[2];
+  C.Efin[3 * N + c] = outE[3] + (R)(hC * w) * outB[3];
 }
 
 // ---- update_B_fluxes (bfields.c:313-382): Stokes circulation per face --------
 // The reference's loop skips the last pair of each dimension (it visits pair
 // jk-1 at index jk, jk < N_ftracks); that is reproduced.
 template <typename R>
-DISCO_D double face_emf(const DevState<R>& S, const CtState& C, int d, int f) {
+DISCO_D R face_emf(const DevState<R>& S, const CtStateT<R>& C, int d, int f) {
   const int N = S.N;
   if (S.fLR[d][f] == 0) return C.Efin[(2 * d + 1) * N + S.fL[d][f]];
   return C.Efin[(2 * d + 0) * N + S.fR[d][f]];
 }
 
 template <typename R>
-__global__ void k_ct_bflux(DevParams P, DevState<R> S, CtState C, double fac) {
+__global__ void k_ct_bflux(DevParams P, DevState<R> S, CtStateT<R> C, double fac) {
   int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= S.N) return;
   const int N = S.N;
@@ -176,8 +172,8 @@ __global__ void k_ct_bflux(DevParams P, DevState<R> S, CtState C, double fac) {
       int base = S.face_off[d][pb], Nf = S.face_off[d][pb + 1] - base;
       int f = S.run_dn_e[d][c];
       int g = f == base ? base + Nf - 1 : f - 1;
-      double Ef = C.Efin[(2 * d + 0) * N + c];
-      double Eg = face_emf(S, C, d, g);
+      double Ef = (double)C.Efin[(2 * d + 0) * N + c];
+      double Eg = (double)face_emf(S, C, d, g);
       int slot = dim == 1 ? 1 : 3;
       double v = C.Phi[slot * N + c];
       if (dim == 1) {
@@ -195,8 +191,8 @@ __global__ void k_ct_bflux(DevParams P, DevState<R> S, CtState C, double fac) {
       int base = S.face_off[d][pa], Nf = S.face_off[d][pa + 1] - base;
       int f = S.run_up_e[d][c];
       int g = f == base ? base + Nf - 1 : f - 1;
-      double Ef = C.Efin[(2 * d + 1) * N + c];
-      double Eg = face_emf(S, C, d, g);
+      double Ef = (double)C.Efin[(2 * d + 1) * N + c];
+      double Eg = (double)face_emf(S, C, d, g);
       int slot = dim == 1 ? 2 : 4;
       double v = C.Phi[slot * N + c];
       if (dim == 1) {
@@ -246,7 +242,7 @@ DISCO_D int get_which4(double phi, double phiR, double phiU, double phiUR, int* 
 }
 
 template <typename R>
-__global__ void k_ct_edge(DevParams P, DevState<R> S, CtState C, double fac) {
+__global__ void k_ct_edge(DevParams P, DevState<R> S, CtStateT<R> C, double fac) {
   extern __shared__ double sm[];
   int q = blockIdx.x;   // quad (j, k): rings j, j+1 at layers k, k+1
   int j = q % (P.Nr - 1), k = q / (P.Nr - 1);
@@ -262,19 +258,23 @@ __global__ void k_ct_edge(DevParams P, DevState<R> S, CtState C, double fac) {
     base[x] = tot;
     tot += np[x];
   }
-  double* sp = sm;   // rotated piph of the four rings
+  // rotated piph of the four rings as IEEE bit patterns: positions are
+  // non-negative, so integer order equals numeric order and the merge-order
+  // search runs on the integer pipe.
+  long long* sp = (long long*)sm;
   for (int x = 0; x < 4; ++x)
-    for (int m = threadIdx.x; m < np[x]; m += blockDim.x) sp[base[x] + m] = S.piph[off[x] + (I0[x] + m) % np[x]];
+    for (int m = threadIdx.x; m < np[x]; m += blockDim.x)
+      sp[base[x] + m] = __double_as_longlong(S.piph[off[x] + (I0[x] + m) % np[x]]);
   __syncthreads();
   const double Pmax = P.phi_max;
   int lapoff[4];
   lapoff[0] = 0;
 #pragma unroll
   for (int x = 1; x < 4; ++x) {
-    double raw = sp[base[0]] - sp[base[x]];
+    double raw = __longlong_as_double(sp[base[0]]) - __longlong_as_double(sp[base[x]]);
     lapoff[x] = raw > .5 * Pmax ? 1 : (raw < -.5 * Pmax ? -1 : 0);
   }
-  auto key = [&](int x, int m, int& lap, double& ph) {
+  auto key = [&](int x, int m, int& lap, long long& ph) {
     int mm = m % np[x];
     ph = sp[base[x] + mm];
     lap = m / np[x] + ((mm > 0 && ph < sp[base[x]]) ? 1 : 0) + lapoff[x];
@@ -284,7 +284,7 @@ __global__ void k_ct_edge(DevParams P, DevState<R> S, CtState C, double fac) {
   for (int t = threadIdx.x; t < tot; t += blockDim.x) {
     int rx = t >= base[3] ? 3 : t >= base[2] ? 2 : t >= base[1] ? 1 : 0;
     int m = t - base[rx];
-    int lx; double px;
+    int lx; long long px;
     key(rx, m, lx, px);
     int head[4];
     head[rx] = m;
@@ -295,7 +295,7 @@ __global__ void k_ct_edge(DevParams P, DevState<R> S, CtState C, double fac) {
       int lo = 0, hi = np[y];
       while (lo < hi) {
         int mid = (lo + hi) >> 1;
-        int ly; double py;
+        int ly; long long py;
         key(y, mid, ly, py);
         bool before = (ly < lx) || (ly == lx && (py < px || (py == px && y < rx)));
         if (before) lo = mid + 1; else hi = mid;
@@ -313,42 +313,42 @@ __global__ void k_ct_edge(DevParams P, DevState<R> S, CtState C, double fac) {
     int w4b = get_which4(pb[0], pb[1], pb[2], pb[3], nullptr, nullptr, 1, Pmax);
     if (w4 != rx) { atomicAdd(C.errs, 1ull); continue; }
     int c = cid[0], cR = cid[1], cU = cid[2], cUR = cid[3];
-    const double* Ep = C.Ephi;
-    double E;
+    const R* Ep = C.Ephi;
+    R E;
     double *PhiL, *PhiR, *PhiU, *PhiD;
     double* Ph = C.Phi;
     if (w4 == 0) {
       PhiL = Ph + 4 * N + c; PhiD = Ph + 2 * N + c;
-      E = .25 * (Ep[3 * N + c] + Ep[1 * N + c]);
-      if (LR_alt == 0) { PhiU = Ph + 2 * N + cU; E += .25 * Ep[1 * N + cU]; }
-      else { PhiU = Ph + 1 * N + cUR; E += .25 * Ep[0 * N + cUR]; }
-      if (UD_alt == 0) { PhiR = Ph + 4 * N + cR; E += .25 * Ep[3 * N + cR]; }
-      else { PhiR = Ph + 3 * N + cUR; E += .25 * Ep[2 * N + cUR]; }
+      E = (R).25 * (Ep[3 * N + c] + Ep[1 * N + c]);
+      if (LR_alt == 0) { PhiU = Ph + 2 * N + cU; E += (R).25 * Ep[1 * N + cU]; }
+      else { PhiU = Ph + 1 * N + cUR; E += (R).25 * Ep[0 * N + cUR]; }
+      if (UD_alt == 0) { PhiR = Ph + 4 * N + cR; E += (R).25 * Ep[3 * N + cR]; }
+      else { PhiR = Ph + 3 * N + cUR; E += (R).25 * Ep[2 * N + cUR]; }
     } else if (w4 == 1) {
       PhiR = Ph + 4 * N + cR; PhiD = Ph + 1 * N + cR;
-      E = .25 * (Ep[3 * N + cR] + Ep[0 * N + cR]);
-      if (LR_alt == 0) { PhiU = Ph + 2 * N + cU; E += .25 * Ep[1 * N + cU]; }
-      else { PhiU = Ph + 1 * N + cUR; E += .25 * Ep[0 * N + cUR]; }
-      if (UD_alt == 0) { PhiL = Ph + 4 * N + c; E += .25 * Ep[3 * N + c]; }
-      else { PhiL = Ph + 3 * N + cU; E += .25 * Ep[2 * N + cU]; }
+      E = (R).25 * (Ep[3 * N + cR] + Ep[0 * N + cR]);
+      if (LR_alt == 0) { PhiU = Ph + 2 * N + cU; E += (R).25 * Ep[1 * N + cU]; }
+      else { PhiU = Ph + 1 * N + cUR; E += (R).25 * Ep[0 * N + cUR]; }
+      if (UD_alt == 0) { PhiL = Ph + 4 * N + c; E += (R).25 * Ep[3 * N + c]; }
+      else { PhiL = Ph + 3 * N + cU; E += (R).25 * Ep[2 * N + cU]; }
     } else if (w4 == 2) {
       PhiL = Ph + 3 * N + cU; PhiU = Ph + 2 * N + cU;
-      E = .25 * (Ep[2 * N + cU] + Ep[1 * N + cU]);
-      if (LR_alt == 0) { PhiD = Ph + 2 * N + c; E += .25 * Ep[1 * N + c]; }
-      else { PhiD = Ph + 1 * N + cR; E += .25 * Ep[0 * N + cR]; }
-      if (UD_alt == 0) { PhiR = Ph + 4 * N + cR; E += .25 * Ep[3 * N + cR]; }
-      else { PhiR = Ph + 3 * N + cUR; E += .25 * Ep[2 * N + cUR]; }
+      E = (R).25 * (Ep[2 * N + cU] + Ep[1 * N + cU]);
+      if (LR_alt == 0) { PhiD = Ph + 2 * N + c; E += (R).25 * Ep[1 * N + c]; }
+      else { PhiD = Ph + 1 * N + cR; E += (R).25 * Ep[0 * N + cR]; }
+      if (UD_alt == 0) { PhiR = Ph + 4 * N + cR; E += (R).25 * Ep[3 * N + cR]; }
+      else { PhiR = Ph + 3 * N + cUR; E += (R).25 * Ep[2 * N + cUR]; }
     } else {
       PhiR = Ph + 3 * N + cUR; PhiU = Ph + 1 * N + cUR;
-      E = .25 * (Ep[2 * N + cUR] + Ep[0 * N + cUR]);
-      if (LR_alt == 0) { PhiD = Ph + 2 * N + c; E += .25 * Ep[1 * N + c]; }
-      else { PhiD = Ph + 1 * N + cR; E += .25 * Ep[0 * N + cR]; }
-      if (UD_alt == 0) { PhiL = Ph + 4 * N + c; E += .25 * Ep[3 * N + c]; }
-      else { PhiL = Ph + 3 * N + cU; E += .25 * Ep[2 * N + cU]; }
+      E = (R).25 * (Ep[2 * N + cUR] + Ep[0 * N + cUR]);
+      if (LR_alt == 0) { PhiD = Ph + 2 * N + c; E += (R).25 * Ep[1 * N + c]; }
+      else { PhiD = Ph + 1 * N + cR; E += (R).25 * Ep[0 * N + cR]; }
+      if (UD_alt == 0) { PhiL = Ph + 4 * N + c; E += (R).25 * Ep[3 * N + c]; }
+      else { PhiL = Ph + 3 * N + cU; E += (R).25 * Ep[2 * N + cU]; }
     }
     double xp1 = pp[w4], xm1 = pb[w4b];
     double dl = (.5 * (rjj + rjj)) * get_dp(xp1, xm1, Pmax);
-    double Edldt = E * dl * dt;
+    double Edldt = (double)E * dl * dt;
     atomicAdd(PhiL, -Edldt);
     atomicAdd(PhiR, Edldt);
     atomicAdd(PhiU, -Edldt);
@@ -359,7 +359,7 @@ __global__ void k_ct_edge(DevParams P, DevState<R> S, CtState C, double fac) {
 // ---- check_flipped + flip_fluxes (bfields.c:693-814), first substep --------------
 // One block per pair; flags in parallel, then the sequential repair (rare).
 template <typename R>
-__global__ void k_ct_flip(DevParams P, DevState<R> S, CtState C, int dim) {
+__global__ void k_ct_flip(DevParams P, DevState<R> S, CtStateT<R> C, int dim) {
   extern __shared__ unsigned char fsm[];
   const int d = dim - 1;
   int pair = blockIdx.x;
@@ -402,7 +402,7 @@ __global__ void k_ct_flip(DevParams P, DevState<R> S, CtState C, int dim) {
 
 // ---- B_faces_to_cells type 1 (bfields.c:88-309): cell B from face fluxes ---------
 template <typename R, int NQ>
-__global__ void k_ct_b2c(DevParams P, DevState<R> S, CtState C, int prim_out) {
+__global__ void k_ct_b2c(DevParams P, DevState<R> S, CtStateT<R> C, int prim_out) {
   int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= S.N) return;
   const int N = S.N;
@@ -428,7 +428,7 @@ __global__ void k_ct_b2c(DevParams P, DevState<R> S, CtState C, int prim_out) {
     int pb = pair_below(P, dim, j, k), pa = pair_above(P, dim, j, k);
     auto visit = [&](int f) {
       double ph = S.fLR[d][f] == 0 ? C.Phi[lo * N + S.fL[d][f]] : C.Phi[hi * N + S.fR[d][f]];
-      areas[d] += S.fdA[d][f];
+      areas[d] += (double)S.fdA[d][f];
       sums[d] += ph;
     };
     if (pb >= 0) {
@@ -455,7 +455,7 @@ __global__ void k_ct_b2c(DevParams P, DevState<R> S, CtState C, int prim_out) {
 
 // ---- set_B_fields (bfields.c:13-86): face fluxes of the initial field ------------
 template <typename R>
-__global__ void k_ct_init_phi0(DevParams P, DevState<R> S, CtState C) {
+__global__ void k_ct_init_phi0(DevParams P, DevState<R> S, CtStateT<R> C) {
   int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= S.N) return;
   int jk = S.cell_ring[c];
@@ -470,7 +470,7 @@ __global__ void k_ct_init_phi0(DevParams P, DevState<R> S, CtState C) {
 }
 
 template <typename R>
-__global__ void k_ct_init_face_phi(DevParams P, DevState<R> S, CtState C, int dim) {
+__global__ void k_ct_init_face_phi(DevParams P, DevState<R> S, CtStateT<R> C, int dim) {
   const int d = dim - 1;
   int f = blockIdx.x * blockDim.x + threadIdx.x;
   if (f >= S.nf[d]) return;
@@ -486,7 +486,7 @@ __global__ void k_ct_init_face_phi(DevParams P, DevState<R> S, CtState C, int di
   x[1] = S.fphic[d][f];
   double prim[MAX_Q];
   initial_eval(P, prim, x);
-  double Phi = (dim == 1 ? prim[BRR] : prim[BZZ]) * S.fdA[d][f];
+  double Phi = (dim == 1 ? prim[BRR] : prim[BZZ]) * (double)S.fdA[d][f];
   const int N = S.N;
   if (S.fLR[d][f] == 0) C.Phi[(dim == 1 ? 2 : 4) * N + cL] = Phi;
   else C.Phi[(dim == 1 ? 1 : 3) * N + S.fR[d][f]] = Phi;

@@ -96,7 +96,7 @@ struct Instance : InstanceBase {
   size_t flush_size = 0;
   DevParams P{};
   DevState<R> S{};
-  CtState C{};
+  CtStateT<R> C{};
   bool ct = false;
   std::vector<void*> keep;
   cudaStream_t st = nullptr;
@@ -246,10 +246,13 @@ struct Instance : InstanceBase {
       CK(cudaMemcpy(d_off, off.data(), sizeof(int) * (np + 1), cudaMemcpyHostToDevice));
       S.face_off[d] = d_off;
       A(&S.fL[d], nf); A(&S.fR[d], nf); A(&S.fLR[d], nf); A(&S.fphic[d], nf); A(&S.fdA[d], nf);
+      A(&S.fdpL[d], nf); A(&S.fdpR[d], nf);
+      A(&S.pdxL[d], np); A(&S.pdxR[d], np); A(&S.pdxs[d], np); A(&S.prad[d], np);
       A(&S.fflux[d], (size_t)NQ * nf);
       A(&S.run_up_s[d], N); A(&S.run_up_e[d], N); A(&S.run_dn_s[d], N); A(&S.run_dn_e[d], N);
       if (ct) {
         A(&S.fdphi[d], nf); A(&S.fErz[d], nf); A(&S.fBrz[d], nf); A(&S.fEphi[d], nf);
+        A(&S.ffrL[d], nf); A(&S.ffrR[d], nf); A(&S.fdp1[d], nf); A(&S.fdp2[d], nf);
       }
       C.last_pair[d] = np - 1;
       if (np > 0 && mx * 9 > 48 * 1024) {
@@ -262,9 +265,9 @@ struct Instance : InstanceBase {
       A(&S.Eraw, (size_t)8 * N); A(&S.Braw, (size_t)8 * N);
       A(&C.Phi, (size_t)5 * N); A(&C.RKPhi, (size_t)5 * N); A(&C.Efin, (size_t)4 * N);
       A(&C.Ephi, (size_t)4 * N); A(&C.errs, 1);
-      CK(cudaMemset(S.Eraw, 0, sizeof(double) * 8 * N)); CK(cudaMemset(S.Braw, 0, sizeof(double) * 8 * N));
+      CK(cudaMemset(S.Eraw, 0, sizeof(R) * 8 * N)); CK(cudaMemset(S.Braw, 0, sizeof(R) * 8 * N));
       CK(cudaMemset(C.Phi, 0, sizeof(double) * 5 * N)); CK(cudaMemset(C.RKPhi, 0, sizeof(double) * 5 * N));
-      CK(cudaMemset(C.Ephi, 0, sizeof(double) * 4 * N)); CK(cudaMemset(C.errs, 0, 8));
+      CK(cudaMemset(C.Ephi, 0, sizeof(R) * 4 * N)); CK(cudaMemset(C.errs, 0, 8));
       edge_smem = (size_t)4 * maxring * 8;
       if (edge_smem > 48 * 1024)
         CK(cudaFuncSetAttribute(k_ct_edge<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)edge_smem));
@@ -284,6 +287,8 @@ struct Instance : InstanceBase {
     CK(cudaMemset(S.errs, 0, sizeof(DevErrs)));
     host_t = dom->t;
 
+    for (int d = 0; d < 2; ++d)
+      if (npair[d]) LAUNCH("pair_geom", (k_pair_geom<R><<<blocks(npair[d]), 256, 0, st>>>(P, S, d + 1, npair[d])));
     // ---- state upload + set-up kernels (setupCells, domain.c:283-385)
     CK(cudaMemcpy(piph_buf[0], dom->piph, sizeof(double) * N, cudaMemcpyHostToDevice));
     CK(cudaMemcpy(S.dphi, dom->dphi, sizeof(double) * N, cudaMemcpyHostToDevice));
@@ -551,18 +556,25 @@ struct Instance : InstanceBase {
       LAUNCH("ct_edge", (k_ct_edge<R><<<(Nr - 1) * (Nz - 1), 256, edge_smem, st>>>(P, S, C, fac)));
     CK(cudaStreamSynchronize(st));
     CK(cudaGetLastError());
+    auto fetch = [&](double* dst, const R* src, size_t n) -> int {
+      std::vector<R> t(n);
+      CK(cudaMemcpy(t.data(), src, sizeof(R) * n, cudaMemcpyDeviceToHost));
+      for (size_t i = 0; i < n; ++i) dst[i] = (double)t[i];
+      return 0;
+    };
+    int rc2 = 0;
     if (stage == 2) {
       if (E) {
         std::vector<double> t((size_t)4 * N);
-        CK(cudaMemcpy(t.data(), C.Efin, sizeof(double) * 4 * N, cudaMemcpyDeviceToHost));
+        if ((rc2 = fetch(t.data(), C.Efin, (size_t)4 * N))) return rc2;
         const int slot[4] = {0, 1, 4, 5};
         for (int q = 0; q < 4; ++q) memcpy(E + (size_t)slot[q] * N, t.data() + (size_t)q * N, sizeof(double) * N);
       }
     } else {
-      if (E) CK(cudaMemcpy(E, S.Eraw, sizeof(double) * 8 * N, cudaMemcpyDeviceToHost));
-      if (B) CK(cudaMemcpy(B, S.Braw, sizeof(double) * 8 * N, cudaMemcpyDeviceToHost));
+      if (E && (rc2 = fetch(E, S.Eraw, (size_t)8 * N))) return rc2;
+      if (B && (rc2 = fetch(B, S.Braw, (size_t)8 * N))) return rc2;
     }
-    if (Ephi) CK(cudaMemcpy(Ephi, C.Ephi, sizeof(double) * 4 * N, cudaMemcpyDeviceToHost));
+    if (Ephi && (rc2 = fetch(Ephi, C.Ephi, (size_t)4 * N))) return rc2;
     if (Phi) CK(cudaMemcpy(Phi, C.Phi, sizeof(double) * 5 * N, cudaMemcpyDeviceToHost));
     return 0;
   }

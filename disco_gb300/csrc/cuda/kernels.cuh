@@ -41,7 +41,17 @@ struct DevState {
   int* fR[2];
   signed char* fLR[2];         // LRtype
   double* fphic[2];            // cm[1]
-  double* fdA[2];              // dA
+  R* fdA[2];                   // dA
+  R* fdpL[2];                  // signed phi offset face centre - L cell centre
+  R* fdpR[2];                  // signed phi offset R cell centre - face centre
+  R* ffrL[2];                  // face dphi / L cell dphi (edge EMF weight, CT)
+  R* ffrR[2];                  // face dphi / R cell dphi
+  R* fdp1[2];                  // avg_Efields interpolation weights (CT)
+  R* fdp2[2];
+  R* pdxL[2];                  // per pair: dxL, dxR, dxL + dxR, face radius
+  R* pdxR[2];
+  R* pdxs[2];
+  R* prad[2];
   R* fflux[2];                 // [NQ*Nf] (F - wU*) dA dt
   int* run_up_s[2];            // per cell: first face where the cell is L (pair above)
   int* run_up_e[2];
@@ -50,12 +60,12 @@ struct DevState {
   int nf[2];
   // constrained transport (MHD): edge EMFs written by the flux kernels
   int ct;
-  double* Eraw;                // [8*N] E[8] of the reference cell
-  double* Braw;                // [8*N] B[8]
-  double* fdphi[2];            // face dphi
-  double* fErz[2];             // per face flux_to_E outputs
-  double* fBrz[2];
-  double* fEphi[2];
+  R* Eraw;                     // [8*N] E[8] of the reference cell
+  R* Braw;                     // [8*N] B[8]
+  double* fdphi[2];            // face dphi (FP64, CT initial fluxes)
+  R* fErz[2];                  // per face flux_to_E outputs
+  R* fBrz[2];
+  R* fEphi[2];
   DevPlanet* planets;          // [Npl], device copy (moves for analytic orbits)
   double* scal;                // [0] dt, [1] t, [2] min-dt accumulator (bits)
   DevErrs* errs;
@@ -322,8 +332,20 @@ __global__ void k_faces(DevParams P, DevState<R> S, int dim) {
       S.fR[d][gf] = iR;
       S.fLR[d][gf] = (signed char)LR;
       S.fphic[d][gf] = phic;
-      S.fdA[d][gf] = dA;
-      if (S.fdphi[d]) S.fdphi[d][gf] = dp;
+      S.fdA[d][gf] = (R)dA;
+      // plm.c:93-96 / riemann.c:127-130 offsets, fixed until the next rebuild
+      S.fdpL[d][gf] = (R)get_signed_dp(phic, pL - .5 * dL, Pmax);
+      S.fdpR[d][gf] = (R)get_signed_dp(pR - .5 * dR, phic, Pmax);
+      if (S.ct) {
+        S.fdphi[d][gf] = dp;
+        S.ffrL[d][gf] = (R)(dp / dL);   // riemann.c:172-173
+        S.ffrR[d][gf] = (R)(dp / dR);
+        // avg_Efields weights (bfields.c:461-465): c1 owns the face's end edge
+        double p1 = LR == 0 ? pL : pR, p2 = LR == 0 ? pR : pL, dc2 = LR == 0 ? dR : dL;
+        double dp1 = get_dp(p2, p1, Pmax);
+        S.fdp1[d][gf] = (R)dp1;
+        S.fdp2[d][gf] = (R)(dc2 - dp1);
+      }
       sLR[n] = (signed char)LR;
       if (LR == 0) ++a; else ++b;
     }
@@ -384,6 +406,23 @@ DISCO_D void pair_dx(const DevParams& P, const double* r_jph, const double* z_kp
   }
 }
 
+// Static per-pair geometry (faces_alt.c:112-135, the face radius cm[0]).
+template <typename R>
+__global__ void k_pair_geom(DevParams P, DevState<R> S, int dim, int npair) {
+  int pair = blockIdx.x * blockDim.x + threadIdx.x;
+  if (pair >= npair) return;
+  const int d = dim - 1;
+  double dxL, dxR;
+  pair_dx(P, S.r_jph, S.z_kph, dim, pair, &dxL, &dxR);
+  const double* rj = S.r_jph + 1;
+  int pj = pair % (dim == 1 ? (P.Nr - 1) : P.Nr);
+  double r = dim == 1 ? .5 * (rj[pj] + rj[pj]) : centroid_r(rj[pj], rj[pj - 1]);
+  S.pdxL[d][pair] = (R)dxL;
+  S.pdxR[d][pair] = (R)dxR;
+  S.pdxs[d][pair] = (R)(dxR + dxL);
+  S.prad[d][pair] = (R)r;
+}
+
 // ---- plm_trans, plm.c:56-195 (per-cell gather over the cell's faces) ---------
 // Sum S dA over the cell's faces, divide by the total area, then limit.  The
 // reference limiter loop (plm.c:146-179) reduces to: zero if any face slope
@@ -413,21 +452,10 @@ __global__ void k_plm_trans(DevParams P, DevState<R> S, int dim) {
   R pc[NQ], gpc[NQ];
 #pragma unroll
   for (int q = 0; q < NQ; ++q) { pc[q] = S.prim[q * N + c]; gpc[q] = S.gradp[q * N + c]; }
-  double phic_c = S.piph[c] - .5 * S.dphi[c];
 
-  auto visit = [&](int f, int other, bool self_is_L, double dxs) {
-    double phi = S.fphic[d][f];
-    double phiO = S.piph[other] - .5 * S.dphi[other];
-    R dpL, dpR;
-    if (self_is_L) {
-      dpL = (R)get_signed_dp(phi, phic_c, Pmax);
-      dpR = (R)get_signed_dp(phiO, phi, Pmax);
-    } else {
-      dpL = (R)get_signed_dp(phi, phiO, Pmax);
-      dpR = (R)get_signed_dp(phic_c, phi, Pmax);
-    }
-    R dA = (R)S.fdA[d][f];
-    R dxsum = (R)dxs;
+  auto visit = [&](int f, int other, bool self_is_L, R dxsum) {
+    R dpL = S.fdpL[d][f], dpR = S.fdpR[d][f];
+    R dA = S.fdA[d][f];
 #pragma unroll
     for (int q = 0; q < NQ; ++q) {
       R po = S.prim[q * N + other], gpo = S.gradp[q * N + other];
@@ -453,17 +481,13 @@ __global__ void k_plm_trans(DevParams P, DevState<R> S, int dim) {
   int pa = pair_above(P, dim, j, k);
   if (pb >= 0) {
     int base = S.face_off[d][pb], Nf = S.face_off[d][pb + 1] - base;
-    double dxL, dxR;
-    pair_dx(P, S.r_jph, S.z_kph, dim, pb, &dxL, &dxR);
-    double dxs = dxR + dxL;
+    R dxs = S.pdxs[d][pb];
     for_run(S.run_dn_s[d][c], S.run_dn_e[d][c], base, Nf,
             [&](int f) { visit(f, S.fL[d][f], false, dxs); });
   }
   if (pa >= 0) {
     int base = S.face_off[d][pa], Nf = S.face_off[d][pa + 1] - base;
-    double dxL, dxR;
-    pair_dx(P, S.r_jph, S.z_kph, dim, pa, &dxL, &dxR);
-    double dxs = dxR + dxL;
+    R dxs = S.pdxs[d][pa];
     for_run(S.run_up_s[d][c], S.run_up_e[d][c], base, Nf,
             [&](int f) { visit(f, S.fR[d][f], true, dxs); });
   }
@@ -566,7 +590,7 @@ __global__ void k_flux_phi(DevParams P, DevState<R> S, double fac) {
   if (S.ct) {   // riemann.c:86-111 (NUM_EDGES == 8)
     R Ez, Br, Er, Bz;
     Phys::flux_to_E(Fl, Us, (R)r, &Ez, &Br, &Er, &Bz, 0);
-    double hEz = .5 * (double)Ez, hBr = .5 * (double)Br, hEr = .5 * (double)Er, hBz = .5 * (double)Bz;
+    R hEz = (R).5 * Ez, hBr = (R).5 * Br, hEr = (R).5 * Er, hBz = (R).5 * Bz;
     S.Eraw[0 * N + c] = hEz; S.Eraw[1 * N + c] = hEz; S.Eraw[2 * N + cp] = hEz; S.Eraw[3 * N + cp] = hEz;
     S.Braw[0 * N + c] = hBr; S.Braw[1 * N + c] = hBr; S.Braw[2 * N + cp] = hBr; S.Braw[3 * N + cp] = hBr;
     S.Eraw[4 * N + c] = hEr; S.Eraw[5 * N + c] = hEr; S.Eraw[6 * N + cp] = hEr; S.Eraw[7 * N + cp] = hEr;
@@ -588,20 +612,13 @@ __global__ void k_flux_trans(DevParams P, DevState<R> S, int dim, int jmin, int 
   if (n >= Nf) return;
   int f = base + n;
   const int N = S.N;
-  double dxL, dxR;
-  pair_dx(P, S.r_jph, S.z_kph, dim, pair, &dxL, &dxR);
   int cL = S.fL[d][f], cR = S.fR[d][f];
-  double phi = S.fphic[d][f];
-  double dAdt = S.fdA[d][f] * (fac * S.scal[SC_DT]);
-  const double Pmax = P.phi_max;
-  double phiL = S.piph[cL] - .5 * S.dphi[cL];
-  double phiR = S.piph[cR] - .5 * S.dphi[cR];
-  R dpL = (R)get_signed_dp(phi, phiL, Pmax);
-  R dpR = (R)get_signed_dp(phiR, phi, Pmax);
+  R phi = (R)S.fphic[d][f];
+  R dpL = S.fdpL[d][f], dpR = S.fdpR[d][f];
+  R rdxL = S.pdxL[d][pair], rdxR = S.pdxR[d][pair];
   const R* gradL = (dim == 1 ? S.gradr : S.gradz);
   R primL[NQ], primR[NQ], grad[NQ];
   R gLp[NQ], gRp[NQ], gLo[NQ], gRo[NQ];
-  R rdxL = (R)dxL, rdxR = (R)dxR;
 #pragma unroll
   for (int q = 0; q < NQ; ++q) {
     R pL = S.prim[q * N + cL], pR = S.prim[q * N + cR];
@@ -624,24 +641,23 @@ __global__ void k_flux_trans(DevParams P, DevState<R> S, int dim, int jmin, int 
     primL[BT] = Bavg; primR[BT] = Bavg;
   }
   // face x = cm: r is the face radius for r faces, the centroid for z faces
-  const double* rj = S.r_jph + 1;
-  int pjL = pair % (dim == 1 ? (P.Nr - 1) : P.Nr);
-  double r = dim == 1 ? .5 * (rj[pjL] + rj[pjL]) : centroid_r(rj[pjL], rj[pjL - 1]);
+  R r = S.prad[d][pair];
   R Fw[NQ], Fl[NQ], Us[NQ];
   if (dim == 1)
     solve_riemann<Phys, R, NQ>(P, S.planets, primL, primR, grad, gLp, gLo, grad, gRp, gRo, (R)r,
-                               (R)phi, n3, (R)0.0, Fw, Fl, Us);
+                               phi, n3, (R)0.0, Fw, Fl, Us);
   else
     solve_riemann<Phys, R, NQ>(P, S.planets, primL, primR, gLo, gLp, grad, gRo, gRp, grad, (R)r,
-                               (R)phi, n3, (R)0.0, Fw, Fl, Us);
+                               phi, n3, (R)0.0, Fw, Fl, Us);
   R* out = S.fflux[d];
   const int NF = S.nf[d];
+  R dAdt = S.fdA[d][f] * (R)(fac * S.scal[SC_DT]);
 #pragma unroll
-  for (int q = 0; q < NQ; ++q) out[q * NF + f] = (R)((double)Fw[q] * dAdt);
+  for (int q = 0; q < NQ; ++q) out[q * NF + f] = Fw[q] * dAdt;
   if (S.ct) {
     R E1, B1, E2, B2;
-    Phys::flux_to_E(Fl, Us, (R)r, &E1, &B1, &E2, &B2, dim);
-    S.fErz[d][f] = (double)E1; S.fBrz[d][f] = (double)B1; S.fEphi[d][f] = (double)E2;
+    Phys::flux_to_E(Fl, Us, r, &E1, &B1, &E2, &B2, dim);
+    S.fErz[d][f] = E1; S.fBrz[d][f] = B1; S.fEphi[d][f] = E2;
   }
 }
 
@@ -677,14 +693,22 @@ __global__ void k_update(DevParams P, DevState<R> S, double RK, double fac, int 
       }
       U[q] = u;
     }
+    // Mixed path: fluxes and sources are summed in R (FP32) into dU, and dU
+    // is added once to the FP64 conserved state.  The FP64 path adds every
+    // term to U directly, in the reference's order.
+    constexpr bool MIX = sizeof(R) < sizeof(double);
+    R dU[NQ];
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) dU[q] = 0;
+    auto add = [&](int q, R v) { if (MIX) dU[q] += v; else U[q] += (double)v; };
     // phi faces: cell i receives +F_{i-1} then -F_i (for i = 0: -F_0, +F_{Np-1})
     int cm = off + (i == 0 ? Np - 1 : i - 1);
     if (i == 0) {
 #pragma unroll
-      for (int q = 0; q < NQ; ++q) { U[q] -= (double)S.fphi[q * N + c]; U[q] += (double)S.fphi[q * N + cm]; }
+      for (int q = 0; q < NQ; ++q) { add(q, -S.fphi[q * N + c]); add(q, S.fphi[q * N + cm]); }
     } else {
 #pragma unroll
-      for (int q = 0; q < NQ; ++q) { U[q] += (double)S.fphi[q * N + cm]; U[q] -= (double)S.fphi[q * N + c]; }
+      for (int q = 0; q < NQ; ++q) { add(q, S.fphi[q * N + cm]); add(q, -S.fphi[q * N + c]); }
     }
     // r then z faces: lower pair (cell is R: +=) then upper pair (cell is L: -=)
 #pragma unroll
@@ -700,16 +724,20 @@ __global__ void k_update(DevParams P, DevState<R> S, double RK, double fac, int 
         int base = S.face_off[d][pb], Nf = S.face_off[d][pb + 1] - base;
         for_run(S.run_dn_s[d][c], S.run_dn_e[d][c], base, Nf, [&](int f) {
 #pragma unroll
-          for (int q = 0; q < NQ; ++q) U[q] += (double)Fb[q * NF + f];
+          for (int q = 0; q < NQ; ++q) add(q, Fb[q * NF + f]);
         });
       }
       if (pa >= 0) {
         int base = S.face_off[d][pa], Nf = S.face_off[d][pa + 1] - base;
         for_run(S.run_up_s[d][c], S.run_up_e[d][c], base, Nf, [&](int f) {
 #pragma unroll
-          for (int q = 0; q < NQ; ++q) U[q] -= (double)Fb[q * NF + f];
+          for (int q = 0; q < NQ; ++q) add(q, -Fb[q * NF + f]);
         });
       }
+    }
+    if (MIX) {
+#pragma unroll
+      for (int q = 0; q < NQ; ++q) { U[q] += (double)dU[q]; dU[q] = 0; }
     }
     // sources (misc.c:569-590) at the pre-move geometry
     double xp[3] = {rj[j], piph, zk[k]};

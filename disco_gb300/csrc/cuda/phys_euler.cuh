@@ -60,13 +60,17 @@ struct Euler {
   DISCO_D static int cons2prim(const DevParams& P, const DevPlanet* pl, const double* cons, R* prim,
                                double r, double phi, double dV) {
     int hits = 0;
-    R rho = (R)(cons[DDD] / dV);
-    if (rho < (R)P.rho_floor) { rho = (R)P.rho_floor; hits |= 1; }
-    R Sr = (R)(cons[SRR] / dV);
-    R Sp = (R)(cons[LLL] / dV / r);
-    R Sz = (R)(cons[SZZ] / dV);
-    R E = (R)(cons[TAU] / dV);
+    R rho, Sr, Sp, Sz, E;
     R rr = (R)r;
+    if (sizeof(R) < sizeof(double)) {   // mixed path: one reciprocal, FP32 products
+      R idV = (R)1 / (R)dV;
+      rho = (R)cons[DDD] * idV; Sr = (R)cons[SRR] * idV; Sp = (R)cons[LLL] * idV / rr;
+      Sz = (R)cons[SZZ] * idV; E = (R)cons[TAU] * idV;
+    } else {
+      rho = (R)(cons[DDD] / dV); Sr = (R)(cons[SRR] / dV); Sp = (R)(cons[LLL] / dV / r);
+      Sz = (R)(cons[SZZ] / dV); E = (R)(cons[TAU] / dV);
+    }
+    if (rho < (R)P.rho_floor) { rho = (R)P.rho_floor; hits |= 1; }
     R om = get_om<R>(P, rr);
     R vr = Sr / rho;
     R vp = Sp / rho;
@@ -86,7 +90,8 @@ struct Euler {
     prim[UPP] = vp / rr;
     prim[UZZ] = vz;
 #pragma unroll
-    for (int q = NC; q < NQ; ++q) prim[q] = (R)(cons[q] / cons[DDD]);
+    for (int q = NC; q < NQ; ++q)
+      prim[q] = sizeof(R) < sizeof(double) ? (R)cons[q] / (R)cons[DDD] : (R)(cons[q] / cons[DDD]);
     return hits;
   }
 
@@ -220,9 +225,12 @@ struct Euler {
     double dL1 = xp[0] - xm[0];
     double dL0 = .5 * (xp[0] + xm[0]) * get_dp(xp[1], xm[1], P.phi_max);
     double dL2 = xp[2] - xm[2];
-    double dtr = dL1 / (double)maxvr;
-    double dtp = dL0 / (double)maxvp;
-    double dtz = dL2 / (double)maxvz;
+    double dtr, dtp, dtz;
+    if (sizeof(R) < sizeof(double)) {
+      dtr = (double)((R)dL1 / maxvr); dtp = (double)((R)dL0 / maxvp); dtz = (double)((R)dL2 / maxvz);
+    } else {
+      dtr = dL1 / (double)maxvr; dtp = dL0 / (double)maxvp; dtz = dL2 / (double)maxvz;
+    }
     double dt = dtr;
     if (dt > dtp) dt = dtp;
     if (dt > dtz) dt = dtz;

@@ -40,18 +40,21 @@ struct Mhd {
   DISCO_D static int cons2prim(const DevParams& P, const DevPlanet* pl, const double* cons, R* prim,
                                double r, double phi, double dV) {
     int hits = 0;
-    R rho = (R)(cons[DDD] / dV);
-    if (rho < (R)P.rho_floor) { rho = (R)P.rho_floor; hits |= 1; }
-    R Sr = (R)(cons[SRR] / dV);
-    R Sp = (R)(cons[LLL] / dV / r);
-    R Sz = (R)(cons[SZZ] / dV);
-    R E = (R)(cons[TAU] / dV);
+    R rho, Sr, Sp, Sz, E, Br, Bp, Bz;
     R rr = (R)r;
+    if (sizeof(R) < sizeof(double)) {   // mixed path: one reciprocal, FP32 products
+      R idV = (R)1 / (R)dV;
+      rho = (R)cons[DDD] * idV; Sr = (R)cons[SRR] * idV; Sp = (R)cons[LLL] * idV / rr;
+      Sz = (R)cons[SZZ] * idV; E = (R)cons[TAU] * idV;
+      Br = (R)cons[BRR] * idV * rr; Bp = (R)cons[BPP] * idV * rr; Bz = (R)cons[BZZ] * idV;
+    } else {
+      rho = (R)(cons[DDD] / dV); Sr = (R)(cons[SRR] / dV); Sp = (R)(cons[LLL] / dV / r);
+      Sz = (R)(cons[SZZ] / dV); E = (R)(cons[TAU] / dV);
+      Br = (R)(cons[BRR] / (dV * (1.0 / r))); Bp = (R)(cons[BPP] / dV * r); Bz = (R)(cons[BZZ] / dV);
+    }
+    if (rho < (R)P.rho_floor) { rho = (R)P.rho_floor; hits |= 1; }
     R om = get_om<R>(P, rr);
     R vr = Sr / rho, vp = Sp / rho, vp_off = vp - om * rr, vz = Sz / rho;
-    R Br = (R)(cons[BRR] / (dV * (1.0 / r)));
-    R Bp = (R)(cons[BPP] / dV * r);
-    R Bz = (R)(cons[BZZ] / dV);
     R B2 = Br * Br + Bp * Bp + Bz * Bz;
     R KE = (R).5 * (Sr * vr + rho * vp_off * vp_off + Sz * vz);
     R rhoe = E - KE - (R).5 * B2;
@@ -64,7 +67,8 @@ struct Mhd {
     prim[RHO] = rho; prim[PPP] = Pp; prim[URR] = vr; prim[UPP] = vp / rr; prim[UZZ] = vz;
     prim[BRR] = Br; prim[BPP] = Bp; prim[BZZ] = Bz;
 #pragma unroll
-    for (int q = NC; q < NQ; ++q) prim[q] = (R)(cons[q] / cons[DDD]);
+    for (int q = NC; q < NQ; ++q)
+      prim[q] = sizeof(R) < sizeof(double) ? (R)cons[q] / (R)cons[DDD] : (R)(cons[q] / cons[DDD]);
     return hits;
   }
 
@@ -345,9 +349,12 @@ struct Mhd {
     double dL1 = xp[0] - xm[0];
     double dL0 = .5 * (xp[0] + xm[0]) * get_dp(xp[1], xm[1], P.phi_max);
     double dL2 = xp[2] - xm[2];
-    double dt = dL1 / (double)maxvr;
-    double dtp = dL0 / (double)maxvp;
-    double dtz = dL2 / (double)maxvz;
+    double dt, dtp, dtz;
+    if (sizeof(R) < sizeof(double)) {
+      dt = (double)((R)dL1 / maxvr); dtp = (double)((R)dL0 / maxvp); dtz = (double)((R)dL2 / maxvz);
+    } else {
+      dt = dL1 / (double)maxvr; dtp = dL0 / (double)maxvp; dtz = dL2 / (double)maxvz;
+    }
     if (dt > dtp) dt = dtp;
     if (dt > dtz) dt = dtz;
     return dt;
