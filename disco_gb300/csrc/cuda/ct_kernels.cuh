@@ -131,7 +131,7 @@ __global__ void k_ct_avg(DevParams P, DevState<R> S, CtStateT<R> C) {
   }
   const double* rj = S.r_jph + 1;
   double hL = rj[j - 1], hR = rj[j];
-  double hC = centroid_r(rj[j], rj[j - 1]);
+  double hC = S.ring_rc[jk];
   double w = S.wiph[c];
   C.Efin[0 * N + c] = outE[0] - (R)(hL * w) * outB[0];
   C.Efin[1 * N + c] = outE[1] - (R)(hR * w) * outB[1];
@@ -274,10 +274,12 @@ __global__ void k_ct_edge(DevParams P, DevState<R> S, CtStateT<R> C, double fac)
     double raw = __longlong_as_double(sp[base[0]]) - __longlong_as_double(sp[base[x]]);
     lapoff[x] = raw > .5 * Pmax ? 1 : (raw < -.5 * Pmax ? -1 : 0);
   }
+  // m is in [0, np[x]]: one wrap at most, no integer division needed
   auto key = [&](int x, int m, int& lap, long long& ph) {
-    int mm = m % np[x];
+    int wrap = m >= np[x] ? 1 : 0;
+    int mm = m - wrap * np[x];
     ph = sp[base[x] + mm];
-    lap = m / np[x] + ((mm > 0 && ph < sp[base[x]]) ? 1 : 0) + lapoff[x];
+    lap = wrap + ((mm > 0 && ph < sp[base[x]]) ? 1 : 0) + lapoff[x];
   };
   double dt = fac * S.scal[SC_DT];
   const double rjj = S.r_jph[j + 1];
@@ -304,7 +306,12 @@ __global__ void k_ct_edge(DevParams P, DevState<R> S, CtStateT<R> C, double fac)
     }
     int cid[4];
 #pragma unroll
-    for (int y = 0; y < 4; ++y) cid[y] = off[y] + (I0[y] + head[y]) % np[y];
+    for (int y = 0; y < 4; ++y) {
+      int t2 = I0[y] + head[y];
+      t2 -= t2 >= np[y] ? np[y] : 0;
+      t2 -= t2 >= np[y] ? np[y] : 0;
+      cid[y] = off[y] + t2;
+    }
     double pp[4], pb[4];
 #pragma unroll
     for (int y = 0; y < 4; ++y) { pp[y] = S.piph[cid[y]]; pb[y] = pp[y] - S.dphi[cid[y]]; }
@@ -369,14 +376,17 @@ __global__ void k_ct_flip(DevParams P, DevState<R> S, CtStateT<R> C, int dim) {
   unsigned char* flag = fsm + Nf;
   for (int n = threadIdx.x; n < Nf; n += blockDim.x) { lr[n] = S.fLR[d][base + n]; flag[n] = 0; }
   __syncthreads();
+  __shared__ int nflag;
+  if (threadIdx.x == 0) nflag = 0;
+  __syncthreads();
   for (int n = threadIdx.x; n < Nf; n += blockDim.x) {
     int f = base + n, np = n + 1 == Nf ? 0 : n + 1, fp = base + np;
     double pm = lr[n] == 0 ? S.piph[S.fL[d][f]] : S.piph[S.fR[d][f]];
     double pp = lr[np] == 0 ? S.piph[S.fL[d][fp]] : S.piph[S.fR[d][fp]];
-    if (get_signed_dp(pp, pm, P.phi_max) < 0.) flag[np] = 1;
+    if (get_signed_dp(pp, pm, P.phi_max) < 0.) { flag[np] = 1; atomicAdd(&nflag, 1); }
   }
   __syncthreads();
-  if (threadIdx.x != 0) return;
+  if (threadIdx.x != 0 || nflag == 0) return;
   const int N = S.N;
   int lo = d == 0 ? 2 : 4, hi = d == 0 ? 1 : 3;
   auto slot = [&](int n) -> long long {
@@ -416,7 +426,7 @@ __global__ void k_ct_b2c(DevParams P, DevState<R> S, CtStateT<R> C, int prim_out
   const double* zk = S.z_kph + 1;
   double xp0 = rj[j], xm0 = rj[j - 1], xp2 = zk[k], xm2 = zk[k - 1];
   double xp1 = S.piph[c], xm1 = S.piph[cm];
-  double x0 = centroid_r(xp0, xm0);
+  double x0 = S.ring_rc[jk];
   double dA = (xp0 - xm0) * (xp2 - xm2);
   double dV = (.5 * (xp0 + xm0)) * (xp0 - xm0) * get_dp(xp1, xm1, P.phi_max) * (xp2 - xm2);
   double sums[2] = {0, 0}, areas[2] = {0, 0};
@@ -462,7 +472,7 @@ __global__ void k_ct_init_phi0(DevParams P, DevState<R> S, CtStateT<R> C) {
   int j = jk % P.Nr, k = jk / P.Nr;
   const double* rj = S.r_jph + 1;
   const double* zk = S.z_kph + 1;
-  double x[3] = {centroid_r(rj[j], rj[j - 1]), S.piph[c], centroid_z(zk[k], zk[k - 1])};
+  double x[3] = {S.ring_rc[jk], S.piph[c], centroid_z(zk[k], zk[k - 1])};
   double prim[MAX_Q];
   initial_eval(P, prim, x);
   double dA = (rj[j] - rj[j - 1]) * (zk[k] - zk[k - 1]);

@@ -175,11 +175,11 @@ DISCO_D void planetary_force(const DevParams& P, const DevPlanet& pl, R r, R phi
 // planet_src (planet.c:190-234) for one planet, cylindrical coordinates.
 template <typename R>
 DISCO_D void planet_src(const DevParams& P, const DevPlanet& pl, const R* prim, double* cons,
-                        const double* xp, const double* xm, double dVdt) {
+                        const double* xp, const double* xm, double dVdt, double rc) {
   R rho = prim[RHO], vr = prim[URR], vz = prim[UZZ], omega = prim[UPP];
   double dphi = get_dp(xp[1], xm[1], P.phi_max);
   double phi = xm[1] + 0.5 * dphi;
-  R x0 = (R)centroid_r(xp[0], xm[0]);
+  R x0 = (R)rc;
   R x2 = (R)centroid_z(xp[2], xm[2]);
   R F0, F1, F2;
   planetary_force<R>(P, pl, x0, (R)phi, x2, &F0, &F1, &F2);

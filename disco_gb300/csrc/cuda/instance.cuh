@@ -212,6 +212,7 @@ struct Instance : InstanceBase {
     CK(cudaMemcpy(d_r, dom->r_jph, sizeof(double) * (Nr + 1), cudaMemcpyHostToDevice));
     CK(cudaMemcpy(d_z, dom->z_kph, sizeof(double) * (Nz + 1), cudaMemcpyHostToDevice));
     S.N = (int)N; S.cell_ring = d_cell_ring; S.ring_off = d_ring_off; S.r_jph = d_r; S.z_kph = d_z;
+    A(&S.ring_rc, nring); A(&S.ring_r23, nring);
     A(&piph_buf[0], N); A(&piph_buf[1], N);
     A(&S.dphi, N); A(&S.wiph, N);
     A(&S.prim, (size_t)NQ * N); A(&S.cons, (size_t)NQ * N); A(&S.RKcons, (size_t)NQ * N);
@@ -255,8 +256,8 @@ struct Instance : InstanceBase {
         A(&S.ffrL[d], nf); A(&S.ffrR[d], nf); A(&S.fdp1[d], nf); A(&S.fdp2[d], nf);
       }
       C.last_pair[d] = np - 1;
-      if (np > 0 && mx * 9 > 48 * 1024) {
-        CK(cudaFuncSetAttribute(k_faces<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx * 9 + 64));
+      if (np > 0 && mx * 13 + 64 > 48 * 1024) {
+        CK(cudaFuncSetAttribute(k_faces<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx * 13 + 64));
       }
     }
     A(&S.planets, MAX_PL); A(&S.scal, SC_COUNT); A(&S.errs, 1);
@@ -287,6 +288,7 @@ struct Instance : InstanceBase {
     CK(cudaMemset(S.errs, 0, sizeof(DevErrs)));
     host_t = dom->t;
 
+    LAUNCH("ring_geom", (k_ring_geom<R><<<blocks(nring), 256, 0, st>>>(P, S, nring)));
     for (int d = 0; d < 2; ++d)
       if (npair[d]) LAUNCH("pair_geom", (k_pair_geom<R><<<blocks(npair[d]), 256, 0, st>>>(P, S, d + 1, npair[d])));
     // ---- state upload + set-up kernels (setupCells, domain.c:283-385)
@@ -322,7 +324,7 @@ struct Instance : InstanceBase {
   void launch_wcell() {
     LAUNCH("wcell", (k_wcell<R, NQ><<<blocks(N), 256, 0, st>>>(P, S)));
     if (P.mesh_motion == 3)
-      LAUNCH("wcell_avg", (k_wcell_avg<R><<<nring, 256, (maxring + 1) * sizeof(double), st>>>(P, S)));
+      LAUNCH("wcell_avg", (k_wcell_avg<R><<<nring, 64, (maxring + 1) * sizeof(double), st>>>(P, S)));
   }
   void launch_boundary() {
     LAUNCH("boundary", (k_boundary<R, NQ><<<blocks(N), 256, 0, st>>>(P, S)));
@@ -332,7 +334,7 @@ struct Instance : InstanceBase {
     LAUNCH("anchor", (k_anchor<R><<<blocks((long)nring * 32), 256, 0, st>>>(P, S, nring)));
     for (int d = 0; d < 2; ++d) {
       if (!npair[d]) continue;
-      size_t sm = (size_t)maxNf[d] * 9 + 64;
+      size_t sm = (size_t)maxNf[d] * 13 + 64;
       LAUNCH(d == 0 ? "faces_r" : "faces_z", (k_faces<R><<<npair[d], 256, sm, st>>>(P, S, d + 1)));
     }
   }

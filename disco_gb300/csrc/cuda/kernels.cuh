@@ -48,6 +48,8 @@ struct DevState {
   R* ffrR[2];                  // face dphi / R cell dphi
   R* fdp1[2];                  // avg_Efields interpolation weights (CT)
   R* fdp2[2];
+  double* ring_rc;             // per ring: centroid radius (cylindrical.c:24)
+  double* ring_r23;            // per ring: (rp^2 + rp rm + rm^2) / 3 (mhd.c:239)
   R* pdxL[2];                  // per pair: dxL, dxR, dxL + dxR, face radius
   R* pdxR[2];
   R* pdxs[2];
@@ -262,7 +264,8 @@ __global__ void k_faces(DevParams P, DevState<R> S, int dim) {
   int base = S.face_off[d][pair];
   double* sL = smem;
   double* sR = smem + NL;
-  signed char* sLR = (signed char*)(smem + NL + NR);
+  int* sA = (int*)(smem + NL + NR);
+  signed char* sLR = (signed char*)(sA + NL + NR);
   const double Pmax = P.phi_max;
 
   for (int m = threadIdx.x; m < NL; m += blockDim.x) sL[m] = S.piph[offL + (I0L + m) % NL];
@@ -292,68 +295,74 @@ __global__ void k_faces(DevParams P, DevState<R> S, int dim) {
   const double* rj = S.r_jph + 1;  // rj[j] == reference r_jph[j]
   const double* zk = S.z_kph + 1;
 
-  int chunk = (Nf + blockDim.x - 1) / blockDim.x;
-  int n0 = threadIdx.x * chunk;
-  int n1 = min(n0 + chunk, Nf);
-  if (n0 < Nf) {
-    int lo = 0, hi = n0;
+  // Each face n is found independently: merge-path state (a, b), a + b = n,
+  // by binary search on the exact keys; consecutive threads take consecutive
+  // faces so every output array is written coalesced.
+  int nerr = 0;
+  for (int n = threadIdx.x; n < Nf; n += blockDim.x) {
+    int lo = 0, hi = n;
     while (lo < hi) {
       int mid = (lo + hi) >> 1;
       int la, lb; double pa, pb;
       keyL(mid, la, pa);
-      keyR(n0 - 1 - mid, lb, pb);
+      keyR(n - 1 - mid, lb, pb);
       bool le = (la < lb) || (la == lb && pa <= pb);
       if (le) lo = mid + 1; else hi = mid;
     }
-    int a = lo, b = n0 - lo;
-    for (int n = n0; n < n1; ++n) {
-      int iL = offL + (I0L + a) % NL;
-      int iR = offR + (I0R + b) % NR;
-      double pL = S.piph[iL], pR = S.piph[iR];
-      double dL = S.dphi[iL], dR = S.dphi[iR];
-      double dphi = pL - pR;
-      while (dphi > .5 * Pmax) dphi -= Pmax;
-      while (dphi < -.5 * Pmax) dphi += Pmax;
-      int LR = dphi > 0. ? 1 : 0;
-      dphi = pL - dL - pR + dR;
-      while (dphi > .5 * Pmax) dphi -= Pmax;
-      while (dphi < -.5 * Pmax) dphi += Pmax;
-      int LR_back = dphi < 0. ? 1 : 0;
-      double xp1 = LR == 0 ? pL : pR;
-      double xm1 = LR_back == 0 ? pL - dL : pR - dR;
-      // addFace, faces_alt.c:10-34
-      double dp = get_dp(xp1, xm1, Pmax);
-      double phic = get_dp(xp1, .5 * dp, Pmax);
-      double dA;
-      if (dim == 1) dA = (.5 * (rj[j] + rj[j])) * dp * (zk[k] - zk[k - 1]);
-      else dA = (.5 * (rj[j] + rj[j - 1])) * (rj[j] - rj[j - 1]) * dp;
-      int gf = base + n;
-      S.fL[d][gf] = iL;
-      S.fR[d][gf] = iR;
-      S.fLR[d][gf] = (signed char)LR;
-      S.fphic[d][gf] = phic;
-      S.fdA[d][gf] = (R)dA;
-      // plm.c:93-96 / riemann.c:127-130 offsets, fixed until the next rebuild
-      S.fdpL[d][gf] = (R)get_signed_dp(phic, pL - .5 * dL, Pmax);
-      S.fdpR[d][gf] = (R)get_signed_dp(pR - .5 * dR, phic, Pmax);
-      if (S.ct) {
-        S.fdphi[d][gf] = dp;
-        S.ffrL[d][gf] = (R)(dp / dL);   // riemann.c:172-173
-        S.ffrR[d][gf] = (R)(dp / dR);
-        // avg_Efields weights (bfields.c:461-465): c1 owns the face's end edge
-        double p1 = LR == 0 ? pL : pR, p2 = LR == 0 ? pR : pL, dc2 = LR == 0 ? dR : dL;
-        double dp1 = get_dp(p2, p1, Pmax);
-        S.fdp1[d][gf] = (R)dp1;
-        S.fdp2[d][gf] = (R)(dc2 - dp1);
-      }
-      sLR[n] = (signed char)LR;
-      if (LR == 0) ++a; else ++b;
+    int a = lo, b = n - lo;
+    int am = a - (a >= NL ? NL : 0), bm = b - (b >= NR ? NR : 0);
+    if (am >= NL || bm >= NR) { ++nerr; continue; }
+    int iL = offL + (I0L + am) % NL;
+    int iR = offR + (I0R + bm) % NR;
+    double pL = sL[am], pR = sR[bm];
+    double dL = S.dphi[iL], dR = S.dphi[iR];
+    double dphi = pL - pR;
+    while (dphi > .5 * Pmax) dphi -= Pmax;
+    while (dphi < -.5 * Pmax) dphi += Pmax;
+    int LR = dphi > 0. ? 1 : 0;
+    dphi = pL - dL - pR + dR;
+    while (dphi > .5 * Pmax) dphi -= Pmax;
+    while (dphi < -.5 * Pmax) dphi += Pmax;
+    int LR_back = dphi < 0. ? 1 : 0;
+    double xp1 = LR == 0 ? pL : pR;
+    double xm1 = LR_back == 0 ? pL - dL : pR - dR;
+    // addFace, faces_alt.c:10-34
+    double dp = get_dp(xp1, xm1, Pmax);
+    double phic = get_dp(xp1, .5 * dp, Pmax);
+    double dA;
+    if (dim == 1) dA = (.5 * (rj[j] + rj[j])) * dp * (zk[k] - zk[k - 1]);
+    else dA = (.5 * (rj[j] + rj[j - 1])) * (rj[j] - rj[j - 1]) * dp;
+    int gf = base + n;
+    S.fL[d][gf] = iL;
+    S.fR[d][gf] = iR;
+    S.fLR[d][gf] = (signed char)LR;
+    S.fphic[d][gf] = phic;
+    S.fdA[d][gf] = (R)dA;
+    // plm.c:93-96 / riemann.c:127-130 offsets, fixed until the next rebuild
+    S.fdpL[d][gf] = (R)get_signed_dp(phic, pL - .5 * dL, Pmax);
+    S.fdpR[d][gf] = (R)get_signed_dp(pR - .5 * dR, phic, Pmax);
+    if (S.ct) {
+      S.fdphi[d][gf] = dp;
+      S.ffrL[d][gf] = (R)(dp / dL);   // riemann.c:172-173
+      S.ffrR[d][gf] = (R)(dp / dR);
+      // avg_Efields weights (bfields.c:461-465): c1 owns the face's end edge
+      double p1 = LR == 0 ? pL : pR, p2 = LR == 0 ? pR : pL, dc2 = LR == 0 ? dR : dL;
+      double dp1 = get_dp(p2, p1, Pmax);
+      S.fdp1[d][gf] = (R)dp1;
+      S.fdp2[d][gf] = (R)(dc2 - dp1);
     }
-    if (n1 == Nf && (a != NL || b != NR)) atomicAdd(&S.errs->face_errors, 1ull);
+    sLR[n] = (signed char)LR;
+    sA[n] = a;
   }
   __syncthreads();
+  // the walk must end with both rings consumed exactly once (a = NL, b = NR)
+  if (threadIdx.x == 0) {
+    int alast = sA[Nf - 1] + (sLR[Nf - 1] == 0 ? 1 : 0);
+    if (alast != NL) ++nerr;
+  }
+  if (nerr) atomicAdd(&S.errs->face_errors, (unsigned long long)nerr);
   // runs: face n starts L's run if the previous face advanced L (circularly)
-  for (int n = n0; n < n1; ++n) {
+  for (int n = threadIdx.x; n < Nf; n += blockDim.x) {
     int gf = base + n;
     int prev = sLR[(n + Nf - 1) % Nf];
     int cur = sLR[n];
@@ -404,6 +413,17 @@ DISCO_D void pair_dx(const DevParams& P, const double* r_jph, const double* z_kp
     *dxL = zk[k] - zm;
     *dxR = zp - zk[k];
   }
+}
+
+// Static per-ring radii, computed once with the path's rounding.
+template <typename R>
+__global__ void k_ring_geom(DevParams P, DevState<R> S, int nring) {
+  int jk = blockIdx.x * blockDim.x + threadIdx.x;
+  if (jk >= nring) return;
+  int j = jk % P.Nr;
+  double rp = S.r_jph[j + 1], rm = S.r_jph[j];
+  S.ring_rc[jk] = centroid_r(rp, rm);
+  S.ring_r23[jk] = (rp * rp + rp * rm + rm * rm) / 3.;
 }
 
 // Static per-pair geometry (faces_alt.c:112-135, the face radius cm[0]).
@@ -516,7 +536,7 @@ __global__ void k_plm_trans(DevParams P, DevState<R> S, int dim) {
   R dAt = (R)dAtot;
 
   bool geom_bd = (dim == 1 && j == 0 && P.NgRa == 0);
-  R rcen = (R)centroid_r(rj[j], rj[j - 1]);
+  R rcen = (R)S.ring_rc[jk];
 #pragma unroll
   for (int q = 0; q < NQ; ++q) {
     R g = sum[q] / dAt;
@@ -555,7 +575,7 @@ __global__ void k_flux_phi(DevParams P, DevState<R> S, double fac) {
   const double* rj = S.r_jph + 1;
   const double* zk = S.z_kph + 1;
   double rp = rj[j], rm = rj[j - 1], zp = zk[k], zm = zk[k - 1];
-  double r = centroid_r(rp, rm);
+  double r = S.ring_rc[jk];
   double phi = S.piph[c];
   double dA = (rp - rm) * (zp - zm);         // get_dA(.., 0) = dr dz
   double dAdt = dA * (fac * S.scal[SC_DT]);
@@ -747,9 +767,9 @@ __global__ void k_update(DevParams P, DevState<R> S, double RK, double fac, int 
     R pr[NQ];
 #pragma unroll
     for (int q = 0; q < NQ; ++q) pr[q] = S.prim[q * N + c];
-    Phys::source(P, pr, U, xp, xm, dVdt);
+    Phys::source(P, pr, U, xp, xm, dVdt, S.ring_rc[jk], S.ring_r23[jk]);
     for (int p = 0; p < P.Npl; ++p)
-      if (S.planets[p].M != 0.0) planet_src<R>(P, S.planets[p], pr, U, xp, xm, dVdt);
+      if (S.planets[p].M != 0.0) planet_src<R>(P, S.planets[p], pr, U, xp, xm, dVdt, S.ring_rc[jk]);
     if (P.include_viscosity) {
       R gr[NQ], gp[NQ], gz[NQ];
 #pragma unroll
@@ -759,7 +779,7 @@ __global__ void k_update(DevParams P, DevState<R> S, double RK, double fac, int 
       Phys::visc_source(P, S.planets, pr, gr, gp, gz, U, xp, xm, dVdt);
     }
     if (P.rot_flag) {  // omega_src, rotframe.c:32-80
-      double r = centroid_r(xp[0], xm[0]);
+      double r = S.ring_rc[jk];
       double ph = .5 * (xp[1] + xm[1]);
       double rho = pr[RHO];
       double v0 = pr[URR], v1 = (double)pr[UPP] * r, v2 = pr[UZZ];
@@ -800,7 +820,7 @@ __global__ void k_update(DevParams P, DevState<R> S, double RK, double fac, int 
     double phim = piph - dphi;
     double xp1 = piph;
     double dV = (.5 * (rp + rm)) * (rp - rm) * get_dp(xp1, phim, Pmax) * (zp - zm);
-    double r = centroid_r(rp, rm);
+    double r = S.ring_rc[jk];
     double U[NQ];
 #pragma unroll
     for (int q = 0; q < NQ; ++q) U[q] = S.cons[q * N + c];
@@ -874,7 +894,7 @@ __global__ void k_mindt(DevParams P, DevState<R> S) {
       R pr[NQ];
 #pragma unroll
       for (int q = 0; q < NQ; ++q) pr[q] = S.prim[q * S.N + c];
-      dtc = Phys::mindt(P, S.planets, pr, w, xp, xm);
+      dtc = Phys::mindt(P, S.planets, pr, w, xp, xm, S.ring_rc[jk]);
     }
   }
   // dt > 0: its IEEE bits order like unsigned integers; NaN sorts above.
@@ -934,7 +954,7 @@ __global__ void k_c2p(DevParams P, DevState<R> S) {
   double rp = rj[j], rm = rj[j - 1], zp = zk[k], zm = zk[k - 1];
   double phim = piph - dphi;
   double dV = (.5 * (rp + rm)) * (rp - rm) * get_dp(piph, phim, P.phi_max) * (zp - zm);
-  double r = centroid_r(rp, rm);
+  double r = S.ring_rc[jk];
   double U[NQ];
 #pragma unroll
   for (int q = 0; q < NQ; ++q) U[q] = S.cons[q * N + c];

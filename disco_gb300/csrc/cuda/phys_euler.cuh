@@ -131,10 +131,10 @@ struct Euler {
 
   // source, euler.c:172-213 (geometric + energy-frame source).
   DISCO_D static void source(const DevParams& P, const R* prim, double* cons, const double* xp,
-                             const double* xm, double dVdt) {
+                             const double* xm, double dVdt, double rc, double r23) {
     double rp = xp[0], rm = xm[0];
     R rho = prim[RHO], Pp = prim[PPP];
-    R r = (R)centroid_r(rp, rm);
+    R r = (R)rc;
     R r_1 = (R)(.5 * (rp + rm));
     R vr = prim[URR], omega = prim[UPP], vz = prim[UZZ];
     R centrifugal = rho * omega * omega * r;
@@ -215,8 +215,7 @@ struct Euler {
 
   // mindt, euler.c:328-377.
   DISCO_D static double mindt(const DevParams& P, const DevPlanet* pl, const R* prim, double w,
-                              const double* xp, const double* xm) {
-    double r = centroid_r(xp[0], xm[0]);
+                              const double* xp, const double* xm, double r) {
     R Pp = prim[PPP], rho = prim[RHO];
     R vp = (R)((double)prim[UPP] - w) * (R)r;
     R vr = prim[URR], vz = prim[UZZ];

@@ -96,14 +96,14 @@ struct Mhd {
 
   // source, mhd.c:225-262
   DISCO_D static void source(const DevParams& P, const R* prim, double* cons, const double* xp,
-                             const double* xm, double dVdt) {
+                             const double* xm, double dVdt, double rc, double r23) {
     double rp = xp[0], rm = xm[0];
     double dphi = get_dp(xp[1], xm[1], P.phi_max);
     R rho = prim[RHO], Pp = prim[PPP];
     R r_1 = (R)(.5 * (rp + rm));
-    R r2_3 = (R)((rp * rp + rp * rm + rm * rm) / 3.);
+    R r2_3 = (R)r23;
     R vr = prim[URR], omega = prim[UPP];
-    R r = (R)centroid_r(rp, rm);
+    R r = (R)rc;
     R Br = prim[BRR], Bp = prim[BPP], Bz = prim[BZZ];
     R B2 = Br * Br + Bp * Bp + Bz * Bz;
     R centrifugal;
@@ -336,8 +336,7 @@ struct Mhd {
 
   // mindt, mhd.c:452-483
   DISCO_D static double mindt(const DevParams& P, const DevPlanet*, const R* prim, double w,
-                              const double* xp, const double* xm) {
-    double r = centroid_r(xp[0], xm[0]);
+                              const double* xp, const double* xm, double r) {
     R Pp = prim[PPP], rho = prim[RHO];
     R vp = (R)((double)prim[UPP] - w) * (R)r;
     R vr = prim[URR], vz = prim[UZZ];
