@@ -130,13 +130,22 @@ __global__ void k_ct_avg(DevParams P, DevState<R> S, CtStateT<R> C) {
     }
   }
   const double* rj = S.r_jph + 1;
-  double hL = rj[j - 1], hR = rj[j];
-  double hC = S.ring_rc[jk];
-  double w = S.wiph[c];
-  C.Efin[0 * N + c] = outE[0] - (R)(hL * w) * outB[0];
-  C.Efin[1 * N + c] = outE[1] - (R)(hR * w) * outB[1];
-  C.Efin[2 * N + c] = outE[2] + (R)(hC * w) * outB[2];
-  C.Efin[3 * N + c] = outE[3] + (R)(hC * w) * outB[3];
+  if constexpr (kMix<R>) {
+    R w = (R)S.wiph[c];
+    R hL = (R)rj[j - 1], hR = (R)rj[j], hC = S.ring_rc_r[jk];
+    C.Efin[0 * N + c] = outE[0] - (hL * w) * outB[0];
+    C.Efin[1 * N + c] = outE[1] - (hR * w) * outB[1];
+    C.Efin[2 * N + c] = outE[2] + (hC * w) * outB[2];
+    C.Efin[3 * N + c] = outE[3] + (hC * w) * outB[3];
+  } else {
+    double hL = rj[j - 1], hR = rj[j];
+    double hC = S.ring_rc[jk];
+    double w = S.wiph[c];
+    C.Efin[0 * N + c] = outE[0] - (R)(hL * w) * outB[0];
+    C.Efin[1 * N + c] = outE[1] - (R)(hR * w) * outB[1];
+    C.Efin[2 * N + c] = outE[2] + (R)(hC * w) * outB[2];
+    C.Efin[3 * N + c] = outE[3] + (R)(hC * w) * outB[3];
+  }
 }
 
 // ---- update_B_fluxes (bfields.c:313-382): Stokes circulation per face --------
@@ -149,10 +158,56 @@ DISCO_D R face_emf(const DevState<R>& S, const CtStateT<R>& C, int d, int f) {
   return C.Efin[(2 * d + 0) * N + S.fR[d][f]];
 }
 
+// Mixed path: each slot's circulation E dl dt is formed in R and added to
+// the FP64 flux once (the FP64 path below keeps the reference's terms).
+template <typename R>
+DISCO_D void ct_bflux_mixed(const DevParams& P, const DevState<R>& S, const CtStateT<R>& C,
+                            double fac, int c) {
+  const int N = S.N;
+  int jk = S.cell_ring[c];
+  int j = jk % P.Nr, k = jk / P.Nr;
+  R dtf = (R)fac * dt_r<R>(S.scal);
+  R dph0 = 0;
+  for (int dim = 1; dim <= 2; ++dim) {
+    if (dim == 1 && P.Nr <= 1) continue;
+    if (dim == 2 && P.Nz <= 1) continue;
+    const int d = dim - 1;
+    R dldt = S.ring_dl_r[d][jk] * dtf;
+    int pb = pair_below(P, dim, j, k), pa = pair_above(P, dim, j, k);
+    if (pb >= 0 && pb != C.last_pair[d]) {
+      int base = S.face_off[d][pb], Nf = S.face_off[d][pb + 1] - base;
+      int f = S.run_dn_e[d][c];
+      int g = f == base ? base + Nf - 1 : f - 1;
+      R Ef = C.Efin[(2 * d + 0) * N + c];
+      R Eg = face_emf(S, C, d, g);
+      int slot = dim == 1 ? 1 : 3;
+      R dv = dim == 1 ? (Eg - Ef) * dldt : (Ef - Eg) * dldt;
+      C.Phi[slot * N + c] += (double)dv;
+      dph0 += dim == 1 ? -Ef * dldt : Ef * dldt;
+    }
+    if (pa >= 0 && pa != C.last_pair[d]) {
+      int base = S.face_off[d][pa], Nf = S.face_off[d][pa + 1] - base;
+      int f = S.run_up_e[d][c];
+      int g = f == base ? base + Nf - 1 : f - 1;
+      R Ef = C.Efin[(2 * d + 1) * N + c];
+      R Eg = face_emf(S, C, d, g);
+      int slot = dim == 1 ? 2 : 4;
+      R dv = dim == 1 ? (Eg - Ef) * dldt : (Ef - Eg) * dldt;
+      C.Phi[slot * N + c] += (double)dv;
+      dph0 += dim == 1 ? Ef * dldt : -Ef * dldt;
+    }
+  }
+  C.Phi[0 * N + c] += (double)dph0;
+}
+
 template <typename R>
 __global__ void k_ct_bflux(DevParams P, DevState<R> S, CtStateT<R> C, double fac) {
   int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= S.N) return;
+  if constexpr (kMix<R>) {
+    ct_bflux_mixed<R>(P, S, C, fac, c);
+    return;
+  }
   const int N = S.N;
   int jk = S.cell_ring[c];
   int j = jk % P.Nr, k = jk / P.Nr;
@@ -274,35 +329,37 @@ __global__ void k_ct_edge(DevParams P, DevState<R> S, CtStateT<R> C, double fac)
     double raw = __longlong_as_double(sp[base[0]]) - __longlong_as_double(sp[base[x]]);
     lapoff[x] = raw > .5 * Pmax ? 1 : (raw < -.5 * Pmax ? -1 : 0);
   }
-  // m is in [0, np[x]]: one wrap at most, no integer division needed
+  // m is in [-1, np[x]]: one wrap at most, no integer division needed
+  // (x may be a runtime ring index: selects keep the small arrays in registers)
+  auto pick = [](const int* a, int x) { return x == 0 ? a[0] : x == 1 ? a[1] : x == 2 ? a[2] : a[3]; };
   auto key = [&](int x, int m, int& lap, long long& ph) {
-    int wrap = m >= np[x] ? 1 : 0;
-    int mm = m - wrap * np[x];
-    ph = sp[base[x] + mm];
-    lap = wrap + ((mm > 0 && ph < sp[base[x]]) ? 1 : 0) + lapoff[x];
+    int npx = pick(np, x), bx = pick(base, x);
+    int wrap = m >= npx ? 1 : (m < 0 ? -1 : 0);
+    int mm = m - wrap * npx;
+    ph = sp[bx + mm];
+    lap = wrap + ((mm > 0 && ph < sp[bx]) ? 1 : 0) + pick(lapoff, x);
   };
   double dt = fac * S.scal[SC_DT];
   const double rjj = S.r_jph[j + 1];
+  R dlfac = 0;
+  if constexpr (kMix<R>) dlfac = (R)rjj * ((R)fac * dt_r<R>(S.scal));
   for (int t = threadIdx.x; t < tot; t += blockDim.x) {
     int rx = t >= base[3] ? 3 : t >= base[2] ? 2 : t >= base[1] ? 1 : 0;
-    int m = t - base[rx];
+    int m = t - pick(base, rx);
     int lx; long long px;
     key(rx, m, lx, px);
     int head[4];
-    head[rx] = m;
 #pragma unroll
     for (int y = 0; y < 4; ++y) {
-      if (y == rx) continue;
-      // number of Y elements ordered before X[m]: (lap, phi, rank) lexicographic
-      int lo = 0, hi = np[y];
-      while (lo < hi) {
-        int mid = (lo + hi) >> 1;
+      if (y == rx) { head[y] = m; continue; }
+      // number of Y elements ordered before X[m]: (lap, phi, rank)
+      // lexicographic, searched from the proportional position
+      int hint = __float2int_rn((float)m * ((float)np[y] / (float)pick(np, rx)));
+      head[y] = gallop_search(0, np[y], hint, [&](int mid) {
         int ly; long long py;
         key(y, mid, ly, py);
-        bool before = (ly < lx) || (ly == lx && (py < px || (py == px && y < rx)));
-        if (before) lo = mid + 1; else hi = mid;
-      }
-      head[y] = lo;
+        return (ly < lx) || (ly == lx && (py < px || (py == px && y < rx)));
+      });
     }
     int cid[4];
 #pragma unroll
@@ -312,12 +369,46 @@ __global__ void k_ct_edge(DevParams P, DevState<R> S, CtStateT<R> C, double fac)
       t2 -= t2 >= np[y] ? np[y] : 0;
       cid[y] = off[y] + t2;
     }
+    int LR_alt, UD_alt, w4, w4b;
     double pp[4], pb[4];
+    double xp1, xm1;
+    if constexpr (kMix<R>) {
+      // get_which4 on the merge keys: the heads' upper edges, and the
+      // predecessors' upper edges for the lower edges ("after" = strictly
+      // later in the (lap, phi) order, the wrapped comparison's meaning)
+      int hl[4], bl[4];
+      long long hk[4], bk[4];
 #pragma unroll
-    for (int y = 0; y < 4; ++y) { pp[y] = S.piph[cid[y]]; pb[y] = pp[y] - S.dphi[cid[y]]; }
-    int LR_alt, UD_alt;
-    int w4 = get_which4(pp[0], pp[1], pp[2], pp[3], &LR_alt, &UD_alt, 0, Pmax);
-    int w4b = get_which4(pb[0], pb[1], pb[2], pb[3], nullptr, nullptr, 1, Pmax);
+      for (int y = 0; y < 4; ++y) { key(y, head[y], hl[y], hk[y]); key(y, head[y] - 1, bl[y], bk[y]); }
+      auto after = [](int la, long long pa, int lb, long long pb_) {
+        return la > lb || (la == lb && pa > pb_);
+      };
+      // (selects instead of runtime indices keep the arrays in registers)
+      int LR_D = after(hl[0], hk[0], hl[1], hk[1]);
+      int LR_U = after(hl[2], hk[2], hl[3], hk[3]);
+      int l1 = LR_D ? hl[1] : hl[0], l2 = LR_U ? hl[3] : hl[2];
+      long long k1 = LR_D ? hk[1] : hk[0], k2 = LR_U ? hk[3] : hk[2];
+      int UD = after(l1, k1, l2, k2);
+      w4 = UD == 0 ? (LR_D == 0 ? 0 : 1) : (LR_U == 0 ? 2 : 3);
+      LR_alt = (w4 == 0 || w4 == 1) ? LR_U : LR_D;
+      UD_alt = (w4 == 0 || w4 == 2) ? after(hl[1], hk[1], hl[3], hk[3]) : after(hl[0], hk[0], hl[2], hk[2]);
+      int LB_D = after(bl[1], bk[1], bl[0], bk[0]);
+      int LB_U = after(bl[3], bk[3], bl[2], bk[2]);
+      int m1 = LB_D ? bl[1] : bl[0], m2 = LB_U ? bl[3] : bl[2];
+      long long n1 = LB_D ? bk[1] : bk[0], n2 = LB_U ? bk[3] : bk[2];
+      int UB = after(m2, n2, m1, n1);
+      w4b = UB == 0 ? (LB_D == 0 ? 0 : 1) : (LB_U == 0 ? 2 : 3);
+      xp1 = phi_unkey(UD == 0 ? k1 : k2);
+      xm1 = phi_unkey(UB == 0 ? n1 : n2);
+      (void)pp; (void)pb;
+    } else {
+#pragma unroll
+      for (int y = 0; y < 4; ++y) { pp[y] = S.piph[cid[y]]; pb[y] = pp[y] - S.dphi[cid[y]]; }
+      w4 = get_which4(pp[0], pp[1], pp[2], pp[3], &LR_alt, &UD_alt, 0, Pmax);
+      w4b = get_which4(pb[0], pb[1], pb[2], pb[3], nullptr, nullptr, 1, Pmax);
+      xp1 = w4 == 0 ? pp[0] : w4 == 1 ? pp[1] : w4 == 2 ? pp[2] : pp[3];
+      xm1 = w4b == 0 ? pb[0] : w4b == 1 ? pb[1] : w4b == 2 ? pb[2] : pb[3];
+    }
     if (w4 != rx) { atomicAdd(C.errs, 1ull); continue; }
     int c = cid[0], cR = cid[1], cU = cid[2], cUR = cid[3];
     const R* Ep = C.Ephi;
@@ -353,9 +444,13 @@ __global__ void k_ct_edge(DevParams P, DevState<R> S, CtStateT<R> C, double fac)
       if (UD_alt == 0) { PhiL = Ph + 4 * N + c; E += (R).25 * Ep[3 * N + c]; }
       else { PhiL = Ph + 3 * N + cU; E += (R).25 * Ep[2 * N + cU]; }
     }
-    double xp1 = pp[w4], xm1 = pb[w4b];
-    double dl = (.5 * (rjj + rjj)) * get_dp(xp1, xm1, Pmax);
-    double Edldt = (double)E * dl * dt;
+    double Edldt;
+    if constexpr (kMix<R>) {
+      Edldt = (double)(E * (dlfac * wrap_dp<R>((R)(xp1 - xm1), (R)Pmax)));
+    } else {
+      double dl = (.5 * (rjj + rjj)) * get_dp(xp1, xm1, Pmax);
+      Edldt = (double)E * dl * dt;
+    }
     atomicAdd(PhiL, -Edldt);
     atomicAdd(PhiR, Edldt);
     atomicAdd(PhiU, -Edldt);
@@ -422,6 +517,43 @@ __global__ void k_ct_b2c(DevParams P, DevState<R> S, CtStateT<R> C, int prim_out
   int off = S.ring_off[jk], Np = S.ring_off[jk + 1] - off;
   int i = c - off;
   int cm = off + (i == 0 ? Np - 1 : i - 1);
+  if constexpr (kMix<R>) {   // face fluxes summed in R
+    R sums[2] = {0, 0}, areas[2] = {0, 0};
+    for (int dim = 1; dim <= 2; ++dim) {
+      if (dim == 1 && P.Nr <= 1) continue;
+      if (dim == 2 && P.Nz <= 1) continue;
+      const int d = dim - 1;
+      int lo = d == 0 ? 2 : 4, hi = d == 0 ? 1 : 3;
+      int pb = pair_below(P, dim, j, k), pa = pair_above(P, dim, j, k);
+      auto visit = [&](int f) {
+        double ph = S.fLR[d][f] == 0 ? C.Phi[lo * N + S.fL[d][f]] : C.Phi[hi * N + S.fR[d][f]];
+        areas[d] += S.fdA[d][f];
+        sums[d] += (R)ph;
+      };
+      if (pb >= 0) {
+        int base = S.face_off[d][pb], Nf = S.face_off[d][pb + 1] - base;
+        for_run(S.run_dn_s[d][c], S.run_dn_e[d][c], base, Nf, visit);
+      }
+      if (pa >= 0) {
+        int base = S.face_off[d][pa], Nf = S.face_off[d][pa + 1] - base;
+        for_run(S.run_up_s[d][c], S.run_up_e[d][c], base, Nf, visit);
+      }
+    }
+    R Bphi = (R).5 * (R)(C.Phi[c] + C.Phi[cm]);
+    R dA = S.ring_dA_r[jk];
+    R x0 = S.ring_rc_r[jk];
+    if (prim_out) {
+      S.prim[BRR * N + c] = sums[0] / areas[0];
+      S.prim[BPP * N + c] = Bphi / dA;
+      if (P.Nz > 1) S.prim[BZZ * N + c] = sums[1] / areas[1];
+    } else {
+      R dV = S.ring_vol_r[jk] * S.dphi_r[c];
+      S.cons[BRR * N + c] = (double)(sums[0] * (dV / (areas[0] * x0)));
+      S.cons[BPP * N + c] = (double)(Bphi * dV / (dA * x0));
+      if (P.Nz > 1) S.cons[BZZ * N + c] = (double)(sums[1] * (dV / areas[1]));
+    }
+    return;
+  }
   const double* rj = S.r_jph + 1;
   const double* zk = S.z_kph + 1;
   double xp0 = rj[j], xm0 = rj[j - 1], xp2 = zk[k], xm2 = zk[k - 1];

@@ -172,29 +172,27 @@ DISCO_D void planetary_force(const DevParams& P, const DevPlanet& pl, R r, R phi
   *fz = f1 * cost;
 }
 
-// planet_src (planet.c:190-234) for one planet, cylindrical coordinates.
-template <typename R>
-DISCO_D void planet_src(const DevParams& P, const DevPlanet& pl, const R* prim, double* cons,
-                        const double* xp, const double* xm, double dVdt, double rc) {
+// planet_src (planet.c:190-234) for one planet, cylindrical coordinates, at
+// the cell centre (rc, phi, z) of a cell of width dphi; T is the accumulator
+// type (FP64 conserved state, or the R sum of the mixed path).
+template <typename R, typename T>
+DISCO_D void planet_src(const DevParams& P, const DevPlanet& pl, const R* prim, T* cons, R phi,
+                        R x2, T dVdt, R rc, R dphi) {
   R rho = prim[RHO], vr = prim[URR], vz = prim[UZZ], omega = prim[UPP];
-  double dphi = get_dp(xp[1], xm[1], P.phi_max);
-  double phi = xm[1] + 0.5 * dphi;
-  R x0 = (R)rc;
-  R x2 = (R)centroid_z(xp[2], xm[2]);
+  R x0 = rc;
   R F0, F1, F2;
-  planetary_force<R>(P, pl, x0, (R)phi, x2, &F0, &F1, &F2);
+  planetary_force<R>(P, pl, x0, phi, x2, &F0, &F1, &F2);
   R hr = 1.0, hp = x0, hz = 1.0;
   if (P.polar_r || P.polar_p) {
     // geom_polar_vec_adjust, cylindrical.c:175-183
-    double dp = get_dp(xp[1], xm[1], P.phi_max);
-    R adjust = (R)(sin(0.5 * dp) / (0.5 * dp));
+    R adjust = (R)(sin((R)0.5 * dphi) / ((R)0.5 * dphi));
     if (P.polar_r) F0 *= adjust;
     if (P.polar_p) F1 *= adjust;
   }
-  cons[SRR] += (double)(rho * hr * F0 * (R)dVdt);
-  cons[LLL] += (double)(rho * hp * F1 * (R)dVdt);
-  cons[SZZ] += (double)(rho * hz * F2 * (R)dVdt);
-  cons[TAU] += (double)(rho * (hr * F0 * vr + hz * F2 * vz + hp * F1 * omega) * (R)dVdt);
+  cons[SRR] += (T)(rho * hr * F0 * (R)dVdt);
+  cons[LLL] += (T)(rho * hp * F1 * (R)dVdt);
+  cons[SZZ] += (T)(rho * hz * F2 * (R)dVdt);
+  cons[TAU] += (T)(rho * (hr * F0 * vr + hz * F2 * vz + hp * F1 * omega) * (R)dVdt);
 }
 
 // get_height_om (omega.c:132-155): sqrt(sum_p fgrav / script_r).

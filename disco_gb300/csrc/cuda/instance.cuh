@@ -205,7 +205,7 @@ struct Instance : InstanceBase {
     int rc;
     int *d_ring_off, *d_cell_ring;
     double *d_r, *d_z;
-#define A(ptr, n) if ((rc = dalloc(ptr, (size_t)(n), keep))) return rc
+#define A(ptr, n) do { if ((rc = dalloc(ptr, (size_t)(n), keep))) return rc; } while (0)
     A(&d_ring_off, nring + 1); A(&d_cell_ring, N); A(&d_r, Nr + 1); A(&d_z, Nz + 1);
     CK(cudaMemcpy(d_ring_off, ring_off.data(), sizeof(int) * (nring + 1), cudaMemcpyHostToDevice));
     CK(cudaMemcpy(d_cell_ring, cell_ring.data(), sizeof(int) * N, cudaMemcpyHostToDevice));
@@ -213,8 +213,16 @@ struct Instance : InstanceBase {
     CK(cudaMemcpy(d_z, dom->z_kph, sizeof(double) * (Nz + 1), cudaMemcpyHostToDevice));
     S.N = (int)N; S.cell_ring = d_cell_ring; S.ring_off = d_ring_off; S.r_jph = d_r; S.z_kph = d_z;
     A(&S.ring_rc, nring); A(&S.ring_r23, nring);
+    A(&S.ring_rc_r, nring); A(&S.ring_r1_r, nring); A(&S.ring_vol_r, nring); A(&S.ring_dA_r, nring);
+    A(&S.ring_r23_r, nring); A(&S.ring_zc_r, nring);
+    for (int d = 0; d < 2; ++d) { A(&S.ring_At_r[d], nring); A(&S.ring_dl_r[d], nring); }
     A(&piph_buf[0], N); A(&piph_buf[1], N);
     A(&S.dphi, N); A(&S.wiph, N);
+    if (kMix<R>) {
+      A(&S.dphi_r, N);
+    } else {
+      S.dphi_r = (R*)S.dphi;
+    }
     A(&S.prim, (size_t)NQ * N); A(&S.cons, (size_t)NQ * N); A(&S.RKcons, (size_t)NQ * N);
     A(&S.gradp, (size_t)NQ * N); A(&S.gradr, (size_t)NQ * N); A(&S.gradz, (size_t)NQ * N);
     A(&S.fphi, (size_t)NQ * N);
@@ -249,6 +257,7 @@ struct Instance : InstanceBase {
       A(&S.fL[d], nf); A(&S.fR[d], nf); A(&S.fLR[d], nf); A(&S.fphic[d], nf); A(&S.fdA[d], nf);
       A(&S.fdpL[d], nf); A(&S.fdpR[d], nf);
       A(&S.pdxL[d], np); A(&S.pdxR[d], np); A(&S.pdxs[d], np); A(&S.prad[d], np);
+      A(&S.pidxs[d], np); A(&S.pdA[d], np);
       A(&S.fflux[d], (size_t)NQ * nf);
       A(&S.run_up_s[d], N); A(&S.run_up_e[d], N); A(&S.run_dn_s[d], N); A(&S.run_dn_e[d], N);
       if (ct) {
@@ -294,6 +303,7 @@ struct Instance : InstanceBase {
     // ---- state upload + set-up kernels (setupCells, domain.c:283-385)
     CK(cudaMemcpy(piph_buf[0], dom->piph, sizeof(double) * N, cudaMemcpyHostToDevice));
     CK(cudaMemcpy(S.dphi, dom->dphi, sizeof(double) * N, cudaMemcpyHostToDevice));
+    sync_dphi_r();
     parity = 0;
     set_piph(0);
     double* d_prim0;
@@ -321,7 +331,14 @@ struct Instance : InstanceBase {
   }
 
   // ---- launch helpers -----------------------------------------------------
+  void sync_dphi_r() {
+    if (kMix<R>) LAUNCH("dphi_r", (k_dphi_r<R><<<blocks(N), 256, 0, st>>>(S)));
+  }
   void launch_wcell() {
+    if (kMix<R> && P.mesh_motion == 3) {
+      LAUNCH("wcell_ring", (k_wcell_ring<R><<<nring, 256, 0, st>>>(P, S)));
+      return;
+    }
     LAUNCH("wcell", (k_wcell<R, NQ><<<blocks(N), 256, 0, st>>>(P, S)));
     if (P.mesh_motion == 3)
       LAUNCH("wcell_avg", (k_wcell_avg<R><<<nring, 64, (maxring + 1) * sizeof(double), st>>>(P, S)));
@@ -412,7 +429,11 @@ struct Instance : InstanceBase {
     return 0;
   }
   int timestep(double dt) override {
+    double slot[1] = {0};
+    float dtf = (float)dt;
+    memcpy(slot, &dtf, sizeof dtf);
     CK(cudaMemcpyAsync(&S.scal[SC_DT], &dt, sizeof(double), cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(&S.scal[SC_DTF], slot, sizeof(double), cudaMemcpyHostToDevice, st));
     step_kernels();
     CK(cudaGetLastError());
     CK(cudaStreamSynchronize(st));
@@ -612,7 +633,10 @@ struct Instance : InstanceBase {
       for (size_t i = 0; i < tmp.size(); ++i) tmp[i] = (R)v->prim[i];
       CK(cudaMemcpy(S.prim, tmp.data(), sizeof(R) * NQ * N, cudaMemcpyHostToDevice));
     }
-    if (v->piph || v->dphi) { launch_faces(); CK(cudaStreamSynchronize(st)); }
+    if (v->dphi) sync_dphi_r();
+    if (v->piph || v->dphi) launch_faces();
+    CK(cudaStreamSynchronize(st));
+    CK(cudaGetLastError());
     return 0;
   }
   int status(disco_gpu_errs* e) override {

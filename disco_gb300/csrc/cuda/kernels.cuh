@@ -50,10 +50,25 @@ struct DevState {
   R* fdp2[2];
   double* ring_rc;             // per ring: centroid radius (cylindrical.c:24)
   double* ring_r23;            // per ring: (rp^2 + rp rm + rm^2) / 3 (mhd.c:239)
+  // Per-ring constants in R for the mixed path (the FP64 path evaluates the
+  // reference's own expressions instead): centroid radius, .5 (rp + rm),
+  // dV / dphi, phi-face area, total r / z face area per unit dphi
+  // (plm.c:113-143), r / z face edge length (bfields.c:338-356).
+  R* ring_rc_r;
+  R* ring_r1_r;
+  R* ring_vol_r;
+  R* ring_dA_r;
+  R* ring_r23_r;
+  R* ring_zc_r;
+  R* ring_At_r[2];
+  R* ring_dl_r[2];
+  R* dphi_r;                   // [N] dphi in R (the same array as dphi when R is double)
   R* pdxL[2];                  // per pair: dxL, dxR, dxL + dxR, face radius
   R* pdxR[2];
   R* pdxs[2];
   R* prad[2];
+  R* pidxs[2];                 // per pair: 1 / (dxL + dxR)
+  R* pdA[2];                   // per pair: face area per unit dphi
   R* fflux[2];                 // [NQ*Nf] (F - wU*) dA dt
   int* run_up_s[2];            // per cell: first face where the cell is L (pair above)
   int* run_up_e[2];
@@ -73,7 +88,47 @@ struct DevState {
   DevErrs* errs;
 };
 
-enum { SC_DT = 0, SC_T = 1, SC_MIN = 2, SC_COUNT = 4 };
+// scal: [SC_DT] dt (FP64), [SC_T] t, [SC_MIN] min-dt accumulator (bits),
+// [SC_DTF] dt rounded to FP32, stored in the first 4 bytes of the slot.
+enum { SC_DT = 0, SC_T = 1, SC_MIN = 2, SC_DTF = 3, SC_COUNT = 4 };
+
+// The mixed path (R = float) keeps positions, conserved sums and face
+// fluxes of B in FP64 but does every other product in R.
+template <typename R>
+constexpr bool kMix = sizeof(R) < sizeof(double);
+
+// dt in R: the FP32 copy on the mixed path, the FP64 value otherwise.
+template <typename R>
+DISCO_D R dt_r(const double* scal) {
+  if constexpr (kMix<R>) return *(const float*)&scal[SC_DTF];
+  else return scal[SC_DT];
+}
+
+// Wrap a phi difference into [0, Pmax] (get_dp) / [-Pmax/2, Pmax/2]
+// (get_signed_dp) in R, for differences already formed in FP64.
+template <typename R>
+DISCO_D R wrap_dp(R dp, R Pmax) {
+  while (dp < (R)0) dp += Pmax;
+  while (dp > Pmax) dp -= Pmax;
+  return dp;
+}
+template <typename R>
+DISCO_D R wrap_signed(R dp, R Pmax) {
+  while (dp < (R)-.5 * Pmax) dp += Pmax;
+  while (dp > (R).5 * Pmax) dp -= Pmax;
+  return dp;
+}
+
+// Order-preserving integer key of a double: integer comparison of keys
+// equals IEEE comparison of the values (and +0 == -0), so phi orderings run
+// on the integer pipe.
+DISCO_D long long phi_key(double v) {
+  long long b = __double_as_longlong(v);
+  return b >= 0 ? b : -(b & 0x7fffffffffffffffLL);
+}
+DISCO_D double phi_unkey(long long k) {
+  return k >= 0 ? __longlong_as_double(k) : __longlong_as_double((-k) | (long long)0x8000000000000000ULL);
+}
 
 DISCO_D bool is_real(const DevParams& P, int j, int k) {
   return j >= P.NgRa && j < P.Nr - P.NgRb && k >= P.NgZa && k < P.Nz - P.NgZb;
@@ -137,6 +192,31 @@ __global__ void k_wcell(DevParams P, DevState<R> S) {
   S.wiph[c] = w;
 }
 
+// Mixed path, Mesh_Motion 3: the ring average of .5 (w_i + w_i+1) is the
+// ring average of w_i = prim[UPP]; one block per ring sums it as an FP64
+// tree (the mesh speed enters F - wU, where its rounding is amplified) and
+// writes the mean to every cell of the ring.
+template <typename R>
+__global__ void k_wcell_ring(DevParams P, DevState<R> S) {
+  __shared__ double part[32];
+  int jk = blockIdx.x;
+  int off = S.ring_off[jk], Np = S.ring_off[jk + 1] - off;
+  double s = 0;
+  for (int i = threadIdx.x; i < Np; i += blockDim.x) s += (double)S.prim[UPP * S.N + off + i];
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) part[wid] = s;
+  __syncthreads();
+  if (wid == 0) {
+    s = lane < (int)(blockDim.x >> 5) ? part[lane] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (lane == 0) part[0] = s / (double)Np;
+  }
+  __syncthreads();
+  double w = part[0];
+  for (int i = threadIdx.x; i < Np; i += blockDim.x) S.wiph[off + i] = w;
+}
+
 // Mesh_Motion 3: ring average of w (misc.c:138-152), one block per ring.  The
 // ring is staged in shared memory and summed by one thread in the
 // reference's order, so the mesh speed rounds exactly like the reference's
@@ -156,6 +236,13 @@ __global__ void k_wcell_avg(DevParams P, DevState<R> S) {
   __syncthreads();
   double w = wsm[Np];
   for (int i = threadIdx.x; i < Np; i += blockDim.x) S.wiph[off + i] = w;
+}
+
+// dphi in R for the mixed path (after an upload or at set-up).
+template <typename R>
+__global__ void k_dphi_r(DevState<R> S) {
+  int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c < S.N) S.dphi_r[c] = (R)S.dphi[c];
 }
 
 // ---- plm_phi, plm.c:6-51 ------------------------------------------------
@@ -178,18 +265,26 @@ __global__ void k_plm_phi(DevParams P, DevState<R> S) {
   int i = c - off;
   int cm = off + (i == 0 ? Np - 1 : i - 1);
   int cp = off + (i + 1 == Np ? 0 : i + 1);
-  R dpL = (R)S.dphi[cm], dpC = (R)S.dphi[c], dpR = (R)S.dphi[cp];
+  R dpL = S.dphi_r[cm], dpC = S.dphi_r[c], dpR = S.dphi_r[cp];
   R PLM = (R)P.PLM;
   const int N = S.N;
+  R iL = 0, iR = 0, iC = 0;
+  if constexpr (kMix<R>) {   // three reciprocals instead of 3 NQ divisions
+    iL = (R)1 / ((R).5 * (dpC + dpL));
+    iR = (R)1 / ((R).5 * (dpR + dpC));
+    iC = (R)1 / ((R).5 * (dpL + dpR) + dpC);
+  }
 #pragma unroll
   for (int q = 0; q < NQ; ++q) {
     R pL = S.prim[q * N + cm], pC = S.prim[q * N + c], pR = S.prim[q * N + cp];
-    R sL = pC - pL;
-    sL /= (R).5 * (dpC + dpL);
-    R sR = pR - pC;
-    sR /= (R).5 * (dpR + dpC);
-    R sC = pR - pL;
-    sC /= (R).5 * (dpL + dpR) + dpC;
+    R sL = pC - pL, sR = pR - pC, sC = pR - pL;
+    if constexpr (kMix<R>) {
+      sL *= iL; sR *= iR; sC *= iC;
+    } else {
+      sL /= (R).5 * (dpC + dpL);
+      sR /= (R).5 * (dpR + dpC);
+      sC /= (R).5 * (dpL + dpR) + dpC;
+    }
     S.gradp[q * N + c] = minmod<R>(PLM * sL, sC, PLM * sR);
   }
 }
@@ -251,9 +346,42 @@ DISCO_D PairInfo pair_info(const DevParams& P, int dim, int pair) {
   return pi;
 }
 
+// First index in [lo0, hi0] at which the monotone predicate (true ... true,
+// false ... false) is false, searched outward from the hint h with doubling
+// steps and finished by bisection: O(log |answer - h|) predicate calls.
+template <typename F>
+DISCO_D int gallop_search(int lo0, int hi0, int h, F&& pred) {
+  if (hi0 <= lo0) return lo0;
+  if (h < lo0) h = lo0;
+  if (h > hi0 - 1) h = hi0 - 1;
+  int lo, hi;
+  if (pred(h)) {
+    lo = h + 1; hi = hi0;
+    for (int step = 1;; step <<= 1) {
+      int p = h + step;
+      if (p >= hi0) break;
+      if (!pred(p)) { hi = p; break; }
+      lo = p + 1;
+    }
+  } else {
+    lo = lo0; hi = h;
+    for (int step = 1;; step <<= 1) {
+      int p = h - step;
+      if (p < lo0) break;
+      if (pred(p)) { lo = p + 1; break; }
+      hi = p;
+    }
+  }
+  while (lo < hi) {
+    int mid = (lo + hi) >> 1;
+    if (pred(mid)) lo = mid + 1; else hi = mid;
+  }
+  return lo;
+}
+
 template <typename R>
 __global__ void k_faces(DevParams P, DevState<R> S, int dim) {
-  extern __shared__ double smem[];
+  extern __shared__ long long fkeys[];
   const int d = dim - 1;
   int pair = blockIdx.x;
   PairInfo pi = pair_info(P, dim, pair);
@@ -262,60 +390,73 @@ __global__ void k_faces(DevParams P, DevState<R> S, int dim) {
   int I0L = S.anchor[pi.L], I0R = S.anchor[pi.R];
   int Nf = NL + NR;
   int base = S.face_off[d][pair];
-  double* sL = smem;
-  double* sR = smem + NL;
-  int* sA = (int*)(smem + NL + NR);
+  // anchor-rotated upper cell edges of both rings as integer keys
+  long long* sL = fkeys;
+  long long* sR = fkeys + NL;
+  int* sA = (int*)(fkeys + NL + NR);
   signed char* sLR = (signed char*)(sA + NL + NR);
   const double Pmax = P.phi_max;
 
-  for (int m = threadIdx.x; m < NL; m += blockDim.x) sL[m] = S.piph[offL + (I0L + m) % NL];
-  for (int m = threadIdx.x; m < NR; m += blockDim.x) sR[m] = S.piph[offR + (I0R + m) % NR];
+  for (int m = threadIdx.x; m < NL; m += blockDim.x) {
+    int t = I0L + m; t -= t >= NL ? NL : 0;
+    sL[m] = phi_key(S.piph[offL + t]);
+  }
+  for (int m = threadIdx.x; m < NR; m += blockDim.x) {
+    int t = I0R + m; t -= t >= NR ? NR : 0;
+    sR[m] = phi_key(S.piph[offR + t]);
+  }
   __syncthreads();
 
   // lap offset of R relative to L from the anchors' wrapped comparison
   int offlap = 0;
   {
-    double raw = sL[0] - sR[0];
+    double raw = phi_unkey(sL[0]) - phi_unkey(sR[0]);
     if (raw > .5 * Pmax) offlap = 1;
     else if (raw < -.5 * Pmax) offlap = -1;
   }
-  const double A0 = sL[0], B0 = sR[0];
-  auto keyL = [&](int a, int& lap, double& ph) {
-    int m = a % NL;
+  const long long A0 = sL[0], B0 = sR[0];
+  // key of merge index a (any a >= 0: lap counts completed turns)
+  auto keyL = [&](int a, int& lap, long long& ph) {
+    int m = a;
+    lap = 0;
+    while (m >= NL) { m -= NL; ++lap; }
     ph = sL[m];
-    lap = a / NL + ((m > 0 && ph < A0) ? 1 : 0);
+    lap += (m > 0 && ph < A0) ? 1 : 0;
   };
-  auto keyR = [&](int b, int& lap, double& ph) {
-    int m = b % NR;
+  auto keyR = [&](int b, int& lap, long long& ph) {
+    int m = b;
+    lap = offlap;
+    while (m >= NR) { m -= NR; ++lap; }
     ph = sR[m];
-    lap = b / NR + ((m > 0 && ph < B0) ? 1 : 0) + offlap;
+    lap += (m > 0 && ph < B0) ? 1 : 0;
   };
 
   int j = pi.jL, k = pi.kL;
   const double* rj = S.r_jph + 1;  // rj[j] == reference r_jph[j]
   const double* zk = S.z_kph + 1;
+  const float ratio = (float)NL / (float)Nf;
 
   // Each face n is found independently: merge-path state (a, b), a + b = n,
-  // by binary search on the exact keys; consecutive threads take consecutive
-  // faces so every output array is written coalesced.
+  // searched from the proportional guess a ~ n NL / Nf; consecutive threads
+  // take consecutive faces so every output array is written coalesced.
   int nerr = 0;
   for (int n = threadIdx.x; n < Nf; n += blockDim.x) {
-    int lo = 0, hi = n;
-    while (lo < hi) {
-      int mid = (lo + hi) >> 1;
-      int la, lb; double pa, pb;
+    int a = gallop_search(0, n, __float2int_rn((float)n * ratio), [&](int mid) {
+      int la, lb; long long pa, pb;
       keyL(mid, la, pa);
       keyR(n - 1 - mid, lb, pb);
-      bool le = (la < lb) || (la == lb && pa <= pb);
-      if (le) lo = mid + 1; else hi = mid;
-    }
-    int a = lo, b = n - lo;
+      return (la < lb) || (la == lb && pa <= pb);
+    });
+    int b = n - a;
     int am = a - (a >= NL ? NL : 0), bm = b - (b >= NR ? NR : 0);
     if (am >= NL || bm >= NR) { ++nerr; continue; }
-    int iL = offL + (I0L + am) % NL;
-    int iR = offR + (I0R + bm) % NR;
-    double pL = sL[am], pR = sR[bm];
+    int tL = I0L + am; tL -= tL >= NL ? NL : 0;
+    int tR = I0R + bm; tR -= tR >= NR ? NR : 0;
+    int iL = offL + tL;
+    int iR = offR + tR;
+    double pL = phi_unkey(sL[am]), pR = phi_unkey(sR[bm]);
     double dL = S.dphi[iL], dR = S.dphi[iR];
+    // LRtype and the face's lower edge: the reference's FP64 comparisons
     double dphi = pL - pR;
     while (dphi > .5 * Pmax) dphi -= Pmax;
     while (dphi < -.5 * Pmax) dphi += Pmax;
@@ -329,27 +470,44 @@ __global__ void k_faces(DevParams P, DevState<R> S, int dim) {
     // addFace, faces_alt.c:10-34
     double dp = get_dp(xp1, xm1, Pmax);
     double phic = get_dp(xp1, .5 * dp, Pmax);
-    double dA;
-    if (dim == 1) dA = (.5 * (rj[j] + rj[j])) * dp * (zk[k] - zk[k - 1]);
-    else dA = (.5 * (rj[j] + rj[j - 1])) * (rj[j] - rj[j - 1]) * dp;
     int gf = base + n;
     S.fL[d][gf] = iL;
     S.fR[d][gf] = iR;
     S.fLR[d][gf] = (signed char)LR;
     S.fphic[d][gf] = phic;
-    S.fdA[d][gf] = (R)dA;
-    // plm.c:93-96 / riemann.c:127-130 offsets, fixed until the next rebuild
-    S.fdpL[d][gf] = (R)get_signed_dp(phic, pL - .5 * dL, Pmax);
-    S.fdpR[d][gf] = (R)get_signed_dp(pR - .5 * dR, phic, Pmax);
-    if (S.ct) {
-      S.fdphi[d][gf] = dp;
-      S.ffrL[d][gf] = (R)(dp / dL);   // riemann.c:172-173
-      S.ffrR[d][gf] = (R)(dp / dR);
-      // avg_Efields weights (bfields.c:461-465): c1 owns the face's end edge
-      double p1 = LR == 0 ? pL : pR, p2 = LR == 0 ? pR : pL, dc2 = LR == 0 ? dR : dL;
-      double dp1 = get_dp(p2, p1, Pmax);
-      S.fdp1[d][gf] = (R)dp1;
-      S.fdp2[d][gf] = (R)(dc2 - dp1);
+    if constexpr (kMix<R>) {
+      // offsets from FP64 differences of nearby positions, the rest in R
+      const R Pm = (R)Pmax;
+      R dpr = (R)dp, dLr = S.dphi_r[iL], dRr = S.dphi_r[iR];
+      S.fdA[d][gf] = S.pdA[d][pair] * dpr;
+      S.fdpL[d][gf] = wrap_signed<R>((R)(phic - pL) + (R).5 * dLr, Pm);
+      S.fdpR[d][gf] = wrap_signed<R>((R)(pR - phic) - (R).5 * dRr, Pm);
+      if (S.ct) {
+        S.fdphi[d][gf] = dp;
+        S.ffrL[d][gf] = dpr / dLr;
+        S.ffrR[d][gf] = dpr / dRr;
+        R dp1 = wrap_dp<R>(LR == 0 ? (R)(pR - pL) : (R)(pL - pR), Pm);
+        S.fdp1[d][gf] = dp1;
+        S.fdp2[d][gf] = (LR == 0 ? dRr : dLr) - dp1;
+      }
+    } else {
+      double dA;
+      if (dim == 1) dA = (.5 * (rj[j] + rj[j])) * dp * (zk[k] - zk[k - 1]);
+      else dA = (.5 * (rj[j] + rj[j - 1])) * (rj[j] - rj[j - 1]) * dp;
+      S.fdA[d][gf] = (R)dA;
+      // plm.c:93-96 / riemann.c:127-130 offsets, fixed until the next rebuild
+      S.fdpL[d][gf] = (R)get_signed_dp(phic, pL - .5 * dL, Pmax);
+      S.fdpR[d][gf] = (R)get_signed_dp(pR - .5 * dR, phic, Pmax);
+      if (S.ct) {
+        S.fdphi[d][gf] = dp;
+        S.ffrL[d][gf] = (R)(dp / dL);   // riemann.c:172-173
+        S.ffrR[d][gf] = (R)(dp / dR);
+        // avg_Efields weights (bfields.c:461-465): c1 owns the face's end edge
+        double p1 = LR == 0 ? pL : pR, p2 = LR == 0 ? pR : pL, dc2 = LR == 0 ? dR : dL;
+        double dp1 = get_dp(p2, p1, Pmax);
+        S.fdp1[d][gf] = (R)dp1;
+        S.fdp2[d][gf] = (R)(dc2 - dp1);
+      }
     }
     sLR[n] = (signed char)LR;
     sA[n] = a;
@@ -364,7 +522,7 @@ __global__ void k_faces(DevParams P, DevState<R> S, int dim) {
   // runs: face n starts L's run if the previous face advanced L (circularly)
   for (int n = threadIdx.x; n < Nf; n += blockDim.x) {
     int gf = base + n;
-    int prev = sLR[(n + Nf - 1) % Nf];
+    int prev = sLR[n == 0 ? Nf - 1 : n - 1];
     int cur = sLR[n];
     int iL = S.fL[d][gf], iR = S.fR[d][gf];
     if (prev == 0) S.run_up_s[d][iL] = gf;
@@ -420,10 +578,27 @@ template <typename R>
 __global__ void k_ring_geom(DevParams P, DevState<R> S, int nring) {
   int jk = blockIdx.x * blockDim.x + threadIdx.x;
   if (jk >= nring) return;
-  int j = jk % P.Nr;
+  int j = jk % P.Nr, k = jk / P.Nr;
   double rp = S.r_jph[j + 1], rm = S.r_jph[j];
+  double zp = S.z_kph[k + 1], zm = S.z_kph[k];
   S.ring_rc[jk] = centroid_r(rp, rm);
   S.ring_r23[jk] = (rp * rp + rp * rm + rm * rm) / 3.;
+  double r1 = .5 * (rp + rm), dr = rp - rm, dz = zp - zm;
+  S.ring_rc_r[jk] = (R)centroid_r(rp, rm);
+  S.ring_r1_r[jk] = (R)r1;
+  S.ring_vol_r[jk] = (R)(r1 * dr * dz);
+  S.ring_dA_r[jk] = (R)(dr * dz);
+  S.ring_r23_r[jk] = (R)((rp * rp + rp * rm + rm * rm) / 3.);
+  S.ring_zc_r[jk] = (R)centroid_z(zp, zm);
+  // total face area per unit dphi, one side only at the domain's edge rings
+  double atr = (rp + rm) * dz, atz = 2. * r1 * dr;
+  if (j == 0) atr = rp * dz;
+  if (j == P.Nr - 1) atr = rm * dz;
+  if (k == 0 || k == P.Nz - 1) atz = r1 * dr;
+  S.ring_At_r[0][jk] = (R)atr;
+  S.ring_At_r[1][jk] = (R)atz;
+  S.ring_dl_r[0][jk] = (R)dz;
+  S.ring_dl_r[1][jk] = (R)dr;
 }
 
 // Static per-pair geometry (faces_alt.c:112-135, the face radius cm[0]).
@@ -441,6 +616,12 @@ __global__ void k_pair_geom(DevParams P, DevState<R> S, int dim, int npair) {
   S.pdxR[d][pair] = (R)dxR;
   S.pdxs[d][pair] = (R)(dxR + dxL);
   S.prad[d][pair] = (R)r;
+  S.pidxs[d][pair] = (R)1 / (R)(dxR + dxL);
+  int pk = pair / (dim == 1 ? (P.Nr - 1) : P.Nr);
+  const double* zk = S.z_kph + 1;
+  double a = dim == 1 ? (.5 * (rj[pj] + rj[pj])) * (zk[pk] - zk[pk - 1])
+                      : (.5 * (rj[pj] + rj[pj - 1])) * (rj[pj] - rj[pj - 1]);
+  S.pdA[d][pair] = (R)a;
 }
 
 // ---- plm_trans, plm.c:56-195 (per-cell gather over the cell's faces) ---------
@@ -458,6 +639,7 @@ __global__ void k_plm_trans(DevParams P, DevState<R> S, int dim) {
   int j = jk % P.Nr, k = jk / P.Nr;
   R* grad = dim == 1 ? S.gradr : S.gradz;
   const double Pmax = P.phi_max;
+  (void)Pmax;
   R PLM = (R)P.PLM;
   if (P.PLM == 0.0) {
 #pragma unroll
@@ -473,7 +655,7 @@ __global__ void k_plm_trans(DevParams P, DevState<R> S, int dim) {
 #pragma unroll
   for (int q = 0; q < NQ; ++q) { pc[q] = S.prim[q * N + c]; gpc[q] = S.gradp[q * N + c]; }
 
-  auto visit = [&](int f, int other, bool self_is_L, R dxsum) {
+  auto visit = [&](int f, int other, bool self_is_L, R dxsum, R idxsum) {
     R dpL = S.fdpL[d][f], dpR = S.fdpR[d][f];
     R dA = S.fdA[d][f];
 #pragma unroll
@@ -482,7 +664,9 @@ __global__ void k_plm_trans(DevParams P, DevState<R> S, int dim) {
       R WL, WR;
       if (self_is_L) { WL = pc[q] + dpL * gpc[q]; WR = po - dpR * gpo; }
       else { WL = po + dpL * gpo; WR = pc[q] - dpR * gpc[q]; }
-      R Sl = (WR - WL) / dxsum;
+      R Sl;
+      if constexpr (kMix<R>) Sl = (WR - WL) * idxsum;
+      else Sl = (WR - WL) / dxsum;
       sum[q] += Sl * dA;
       R ps = PLM * Sl;
       if (Sl > (R)0) {
@@ -501,45 +685,53 @@ __global__ void k_plm_trans(DevParams P, DevState<R> S, int dim) {
   int pa = pair_above(P, dim, j, k);
   if (pb >= 0) {
     int base = S.face_off[d][pb], Nf = S.face_off[d][pb + 1] - base;
-    R dxs = S.pdxs[d][pb];
+    R dxs = S.pdxs[d][pb], idxs = kMix<R> ? S.pidxs[d][pb] : (R)0;
     for_run(S.run_dn_s[d][c], S.run_dn_e[d][c], base, Nf,
-            [&](int f) { visit(f, S.fL[d][f], false, dxs); });
+            [&](int f) { visit(f, S.fL[d][f], false, dxs, idxs); });
   }
   if (pa >= 0) {
     int base = S.face_off[d][pa], Nf = S.face_off[d][pa + 1] - base;
-    R dxs = S.pdxs[d][pa];
+    R dxs = S.pdxs[d][pa], idxs = kMix<R> ? S.pidxs[d][pa] : (R)0;
     for_run(S.run_up_s[d][c], S.run_up_e[d][c], base, Nf,
-            [&](int f) { visit(f, S.fR[d][f], true, dxs); });
+            [&](int f) { visit(f, S.fR[d][f], true, dxs, idxs); });
   }
 
   // total weight, plm.c:113-143
-  const double* rj = S.r_jph + 1;
-  const double* zk = S.z_kph + 1;
-  double phip = S.piph[c], phim = phip - S.dphi[c];
-  double dph = get_dp(phip, phim, Pmax);
-  double dAp, dAm;
-  if (dim == 1) {
-    double dz = zk[k] - zk[k - 1];
-    dAp = (.5 * (rj[j] + rj[j])) * dph * dz;
-    dAm = (.5 * (rj[j - 1] + rj[j - 1])) * dph * dz;
+  R dAt, idAt = 0;
+  if constexpr (kMix<R>) {
+    dAt = S.ring_At_r[d][jk] * S.dphi_r[c];
+    idAt = (R)1 / dAt;
   } else {
-    double dr = rj[j] - rj[j - 1];
-    double r = .5 * (rj[j] + rj[j - 1]);
-    dAp = r * dr * dph;
-    dAm = r * dr * dph;
+    const double* rj = S.r_jph + 1;
+    const double* zk = S.z_kph + 1;
+    double phip = S.piph[c], phim = phip - S.dphi[c];
+    double dph = get_dp(phip, phim, Pmax);
+    double dAp, dAm;
+    if (dim == 1) {
+      double dz = zk[k] - zk[k - 1];
+      dAp = (.5 * (rj[j] + rj[j])) * dph * dz;
+      dAm = (.5 * (rj[j - 1] + rj[j - 1])) * dph * dz;
+    } else {
+      double dr = rj[j] - rj[j - 1];
+      double r = .5 * (rj[j] + rj[j - 1]);
+      dAp = r * dr * dph;
+      dAm = r * dr * dph;
+    }
+    double dAtot = dAp + dAm;
+    int idx = dim == 1 ? j : k;
+    int nmax = dim == 1 ? P.Nr : P.Nz;
+    if (idx == 0) dAtot = dAp;
+    if (idx == nmax - 1) dAtot = dAm;
+    dAt = (R)dAtot;
   }
-  double dAtot = dAp + dAm;
-  int idx = dim == 1 ? j : k;
-  int nmax = dim == 1 ? P.Nr : P.Nz;
-  if (idx == 0) dAtot = dAp;
-  if (idx == nmax - 1) dAtot = dAm;
-  R dAt = (R)dAtot;
 
   bool geom_bd = (dim == 1 && j == 0 && P.NgRa == 0);
-  R rcen = (R)S.ring_rc[jk];
+  R rcen = kMix<R> ? S.ring_rc_r[jk] : (R)S.ring_rc[jk];
 #pragma unroll
   for (int q = 0; q < NQ; ++q) {
-    R g = sum[q] / dAt;
+    R g;
+    if constexpr (kMix<R>) g = sum[q] * idAt;
+    else g = sum[q] / dAt;
     if (g > (R)0) {
       if ((anyneg >> q & 1u) || (anyzero >> q & 1u)) g = 0;
       else if ((anypos >> q & 1u) && minpos[q] < g) g = minpos[q];
@@ -572,15 +764,22 @@ __global__ void k_flux_phi(DevParams P, DevState<R> S, double fac) {
   int off = S.ring_off[jk], Np = S.ring_off[jk + 1] - off;
   int i = c - off;
   int cp = off + (i < Np - 1 ? i + 1 : 0);
-  const double* rj = S.r_jph + 1;
-  const double* zk = S.z_kph + 1;
-  double rp = rj[j], rm = rj[j - 1], zp = zk[k], zm = zk[k - 1];
-  double r = S.ring_rc[jk];
+  R r, dAdt_r = 0;
+  double dAdt = 0;
+  if constexpr (kMix<R>) {
+    r = S.ring_rc_r[jk];
+    dAdt_r = S.ring_dA_r[jk] * ((R)fac * dt_r<R>(S.scal));
+  } else {
+    const double* rj = S.r_jph + 1;
+    const double* zk = S.z_kph + 1;
+    double rp = rj[j], rm = rj[j - 1], zp = zk[k], zm = zk[k - 1];
+    r = S.ring_rc[jk];
+    double dA = (rp - rm) * (zp - zm);         // get_dA(.., 0) = dr dz
+    dAdt = dA * (fac * S.scal[SC_DT]);
+  }
   double phi = S.piph[c];
-  double dA = (rp - rm) * (zp - zm);         // get_dA(.., 0) = dr dz
-  double dAdt = dA * (fac * S.scal[SC_DT]);
   R primL[NQ], primR[NQ], gp[NQ], gLr[NQ], gLz[NQ], gRr[NQ], gRz[NQ];
-  R dL = (R)S.dphi[c], dR = (R)S.dphi[cp];
+  R dL = S.dphi_r[c], dR = S.dphi_r[cp];
 #pragma unroll
   for (int q = 0; q < NQ; ++q) {
     R pL = S.prim[q * N + c], pR = S.prim[q * N + cp];
@@ -605,8 +804,13 @@ __global__ void k_flux_phi(DevParams P, DevState<R> S, double fac) {
   R Fw[NQ], Fl[NQ], Us[NQ];
   solve_riemann<Phys, R, NQ>(P, S.planets, primL, primR, gLr, gp, gLz, gRr, gp, gRz, (R)r,
                              (R)phi, n, w, Fw, Fl, Us);
+  if constexpr (kMix<R>) {
 #pragma unroll
-  for (int q = 0; q < NQ; ++q) S.fphi[q * N + c] = (R)((double)Fw[q] * dAdt);
+    for (int q = 0; q < NQ; ++q) S.fphi[q * N + c] = Fw[q] * dAdt_r;
+  } else {
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) S.fphi[q * N + c] = (R)((double)Fw[q] * dAdt);
+  }
   if (S.ct) {   // riemann.c:86-111 (NUM_EDGES == 8)
     R Ez, Br, Er, Bz;
     Phys::flux_to_E(Fl, Us, (R)r, &Ez, &Br, &Er, &Bz, 0);
@@ -636,6 +840,7 @@ __global__ void k_flux_trans(DevParams P, DevState<R> S, int dim, int jmin, int 
   R phi = (R)S.fphic[d][f];
   R dpL = S.fdpL[d][f], dpR = S.fdpR[d][f];
   R rdxL = S.pdxL[d][pair], rdxR = S.pdxR[d][pair];
+  R ridxs = kMix<R> ? S.pidxs[d][pair] : (R)0;
   const R* gradL = (dim == 1 ? S.gradr : S.gradz);
   R primL[NQ], primR[NQ], grad[NQ];
   R gLp[NQ], gRp[NQ], gLo[NQ], gRo[NQ];
@@ -645,7 +850,8 @@ __global__ void k_flux_trans(DevParams P, DevState<R> S, int dim, int jmin, int 
     R gpL = S.gradp[q * N + cL], gpR = S.gradp[q * N + cR];
     primL[q] = pL + gradL[q * N + cL] * rdxL + gpL * dpL;
     primR[q] = pR - gradL[q * N + cR] * rdxR - gpR * dpR;
-    grad[q] = ((pR - gpR * dpR) - (pL + gpL * dpL)) / (rdxL + rdxR);
+    if constexpr (kMix<R>) grad[q] = ((pR - gpR * dpR) - (pL + gpL * dpL)) * ridxs;
+    else grad[q] = ((pR - gpR * dpR) - (pL + gpL * dpL)) / (rdxL + rdxR);
     gLp[q] = gpL; gRp[q] = gpR;
   }
   if (P.include_viscosity) {
@@ -671,7 +877,9 @@ __global__ void k_flux_trans(DevParams P, DevState<R> S, int dim, int jmin, int 
                                phi, n3, (R)0.0, Fw, Fl, Us);
   R* out = S.fflux[d];
   const int NF = S.nf[d];
-  R dAdt = S.fdA[d][f] * (R)(fac * S.scal[SC_DT]);
+  R dAdt;
+  if constexpr (kMix<R>) dAdt = S.fdA[d][f] * ((R)fac * dt_r<R>(S.scal));
+  else dAdt = S.fdA[d][f] * (R)(fac * S.scal[SC_DT]);
 #pragma unroll
   for (int q = 0; q < NQ; ++q) out[q * NF + f] = Fw[q] * dAdt;
   if (S.ct) {
@@ -701,6 +909,8 @@ __global__ void k_update(DevParams P, DevState<R> S, double RK, double fac, int 
   bool real = is_real(P, j, k);
 
   double piph = S.piph[c], dphi = S.dphi[c];
+  constexpr bool MIX = kMix<R>;
+  double Ukeep[MIX ? NQ : 1];
   if (real) {
     double U[NQ];
 #pragma unroll
@@ -716,7 +926,6 @@ __global__ void k_update(DevParams P, DevState<R> S, double RK, double fac, int 
     // Mixed path: fluxes and sources are summed in R (FP32) into dU, and dU
     // is added once to the FP64 conserved state.  The FP64 path adds every
     // term to U directly, in the reference's order.
-    constexpr bool MIX = sizeof(R) < sizeof(double);
     R dU[NQ];
 #pragma unroll
     for (int q = 0; q < NQ; ++q) dU[q] = 0;
@@ -755,21 +964,42 @@ __global__ void k_update(DevParams P, DevState<R> S, double RK, double fac, int 
         });
       }
     }
-    if (MIX) {
-#pragma unroll
-      for (int q = 0; q < NQ; ++q) { U[q] += (double)dU[q]; dU[q] = 0; }
-    }
     // sources (misc.c:569-590) at the pre-move geometry
-    double xp[3] = {rj[j], piph, zk[k]};
-    double xm[3] = {rj[j - 1], piph - dphi, zk[k - 1]};
-    double dV = (.5 * (xp[0] + xm[0])) * (xp[0] - xm[0]) * get_dp(xp[1], xm[1], Pmax) * (xp[2] - xm[2]);
-    double dVdt = dV * dt;
     R pr[NQ];
 #pragma unroll
     for (int q = 0; q < NQ; ++q) pr[q] = S.prim[q * N + c];
-    Phys::source(P, pr, U, xp, xm, dVdt, S.ring_rc[jk], S.ring_r23[jk]);
-    for (int p = 0; p < P.Npl; ++p)
-      if (S.planets[p].M != 0.0) planet_src<R>(P, S.planets[p], pr, U, xp, xm, dVdt, S.ring_rc[jk]);
+    double xp[3] = {rj[j], piph, zk[k]};
+    double xm[3] = {rj[j - 1], piph - dphi, zk[k - 1]};
+    double dVdt = 0;
+    if constexpr (MIX) {   // sources summed in R into dU with the flux terms
+      R dph = S.dphi_r[c];
+      R dVdt_r = S.ring_vol_r[jk] * dph * ((R)fac * dt_r<R>(S.scal));
+      R rc = S.ring_rc_r[jk];
+      Phys::template source<R>(P, pr, dU, dVdt_r, S.ring_r1_r[jk], S.ring_r23_r[jk], rc, dph);
+      if (P.Npl) {
+        R phc = (R)piph - (R).5 * dph;
+        for (int p = 0; p < P.Npl; ++p)
+          if (S.planets[p].M != 0.0)
+            planet_src<R, R>(P, S.planets[p], pr, dU, phc, S.ring_zc_r[jk], dVdt_r, rc, dph);
+      }
+#pragma unroll
+      for (int q = 0; q < NQ; ++q) U[q] += (double)dU[q];
+      if (P.include_viscosity || P.rot_flag) {
+        double dV = (.5 * (xp[0] + xm[0])) * (xp[0] - xm[0]) * get_dp(xp[1], xm[1], Pmax) * (xp[2] - xm[2]);
+        dVdt = dV * dt;
+      }
+    } else {
+      double dV = (.5 * (xp[0] + xm[0])) * (xp[0] - xm[0]) * get_dp(xp[1], xm[1], Pmax) * (xp[2] - xm[2]);
+      dVdt = dV * dt;
+      double dph = get_dp(xp[1], xm[1], Pmax);
+      double rc = S.ring_rc[jk];
+      Phys::template source<double>(P, pr, U, dVdt, (R)(.5 * (xp[0] + xm[0])), (R)S.ring_r23[jk], (R)rc,
+                                    (R)dph);
+      for (int p = 0; p < P.Npl; ++p)
+        if (S.planets[p].M != 0.0)
+          planet_src<R, double>(P, S.planets[p], pr, U, (R)(xm[1] + 0.5 * dph),
+                                (R)centroid_z(xp[2], xm[2]), dVdt, (R)rc, (R)dph);
+    }
     if (P.include_viscosity) {
       R gr[NQ], gp[NQ], gz[NQ];
 #pragma unroll
@@ -798,6 +1028,10 @@ __global__ void k_update(DevParams P, DevState<R> S, double RK, double fac, int 
     }
 #pragma unroll
     for (int q = 0; q < NQ; ++q) S.cons[q * N + c] = U[q];
+    if constexpr (MIX) {
+#pragma unroll
+      for (int q = 0; q < NQ; ++q) Ukeep[q] = U[q];
+    }
   }
 
   // move_cells + clean_pi + calc_dp (first substep only)
@@ -813,19 +1047,27 @@ __global__ void k_update(DevParams P, DevState<R> S, double RK, double fac, int 
     dphi = get_dp(pn, pm, Pmax);
     S.piph_out[c] = piph;
     S.dphi[c] = dphi;
+    if constexpr (MIX) S.dphi_r[c] = (R)dphi;
   }
 
   if (real && do_c2p) {  // calc_prim at the post-move geometry
-    double rp = rj[j], rm = rj[j - 1], zp = zk[k], zm = zk[k - 1];
-    double phim = piph - dphi;
-    double xp1 = piph;
-    double dV = (.5 * (rp + rm)) * (rp - rm) * get_dp(xp1, phim, Pmax) * (zp - zm);
-    double r = S.ring_rc[jk];
-    double U[NQ];
-#pragma unroll
-    for (int q = 0; q < NQ; ++q) U[q] = S.cons[q * N + c];
     R pr[NQ];
-    int hits = Phys::cons2prim(P, S.planets, U, pr, r, .5 * (phim + piph), dV);
+    int hits;
+    if constexpr (MIX) {
+      R dph = first ? (R)dphi : S.dphi_r[c];
+      R dV = S.ring_vol_r[jk] * dph;
+      hits = Phys::cons2prim(P, S.planets, Ukeep, pr, S.ring_rc_r[jk], (R)piph - (R).5 * dph, dV);
+    } else {
+      double rp = rj[j], rm = rj[j - 1], zp = zk[k], zm = zk[k - 1];
+      double phim = piph - dphi;
+      double xp1 = piph;
+      double dV = (.5 * (rp + rm)) * (rp - rm) * get_dp(xp1, phim, Pmax) * (zp - zm);
+      double r = S.ring_rc[jk];
+      double U[NQ];
+#pragma unroll
+      for (int q = 0; q < NQ; ++q) U[q] = S.cons[q * N + c];
+      hits = Phys::cons2prim(P, S.planets, U, pr, r, .5 * (phim + piph), dV);
+    }
     bool bad = false;
 #pragma unroll
     for (int q = 0; q < NQ; ++q) {
@@ -878,30 +1120,46 @@ template <typename Phys, typename R, int NQ>
 __global__ void k_mindt(DevParams P, DevState<R> S) {
   int c = blockIdx.x * blockDim.x + threadIdx.x;
   double dtc = 1.0e300;
+  float dtf = 3.0e38f;
   if (c < S.N) {
     int jk = S.cell_ring[c];
     int j = jk % P.Nr, k = jk / P.Nr;
     if (is_real(P, j, k)) {
       int off = S.ring_off[jk], Np = S.ring_off[jk + 1] - off;
       int i = c - off;
-      const double* rj = S.r_jph + 1;
-      const double* zk = S.z_kph + 1;
-      double phip = S.piph[c], phim = phip - S.dphi[c];
-      double xp[3] = {rj[j], phip, zk[k]};
-      double xm[3] = {rj[j - 1], phim, zk[k - 1]};
       int im = off + (i == 0 ? Np - 1 : i - 1);
-      double w = .5 * (S.wiph[im] + S.wiph[c]);
       R pr[NQ];
 #pragma unroll
       for (int q = 0; q < NQ; ++q) pr[q] = S.prim[q * S.N + c];
-      dtc = Phys::mindt(P, S.planets, pr, w, xp, xm, S.ring_rc[jk]);
+      if constexpr (kMix<R>) {
+        R w = (R).5 * ((R)S.wiph[im] + (R)S.wiph[c]);
+        R dph = S.dphi_r[c];
+        dtf = Phys::mindt_r(P, S.planets, pr, w, S.ring_r1_r[jk] * dph, S.ring_dl_r[1][jk],
+                            S.ring_dl_r[0][jk], S.ring_rc_r[jk], (R)S.piph[c] - (R).5 * dph);
+      } else {
+        const double* rj = S.r_jph + 1;
+        const double* zk = S.z_kph + 1;
+        double phip = S.piph[c], phim = phip - S.dphi[c];
+        double xp[3] = {rj[j], phip, zk[k]};
+        double xm[3] = {rj[j - 1], phim, zk[k - 1]};
+        double w = .5 * (S.wiph[im] + S.wiph[c]);
+        dtc = Phys::mindt(P, S.planets, pr, w, xp, xm, S.ring_rc[jk]);
+      }
     }
   }
   // dt > 0: its IEEE bits order like unsigned integers; NaN sorts above.
-  unsigned long long b = __double_as_longlong(dtc);
-  for (int o = 16; o > 0; o >>= 1) b = min(b, __shfl_xor_sync(0xffffffffu, b, o));
   __shared__ unsigned long long red[32];
   int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  unsigned long long b;
+  if constexpr (kMix<R>) {   // reduce FP32 bits, widen once per warp
+    unsigned u = __float_as_uint(dtf);
+    for (int o = 16; o > 0; o >>= 1) u = min(u, __shfl_xor_sync(0xffffffffu, u, o));
+    b = __double_as_longlong(u >= 0x7f000000u ? 1.0e300 : (double)__uint_as_float(u));
+  } else {
+    b = __double_as_longlong(dtc);
+    for (int o = 16; o > 0; o >>= 1) b = min(b, __shfl_xor_sync(0xffffffffu, b, o));
+  }
+  (void)dtc; (void)dtf;
   if (lane == 0) red[wid] = b;
   __syncthreads();
   if (wid == 0) {
@@ -920,6 +1178,7 @@ static __global__ void k_dt_finalize(DevParams P, double* scal) {
   dt *= P.CFL;
   if (P.t_end > 0.0 && scal[SC_T] + dt > P.t_end) dt = P.t_end - scal[SC_T];
   scal[SC_DT] = dt;
+  *(float*)&scal[SC_DTF] = (float)dt;
   *(unsigned long long*)&scal[SC_MIN] = 0x7ff0000000000000ull;   // +inf
 }
 
@@ -948,18 +1207,25 @@ __global__ void k_c2p(DevParams P, DevState<R> S) {
   int jk = S.cell_ring[c];
   int j = jk % P.Nr, k = jk / P.Nr;
   if (!is_real(P, j, k)) return;
-  const double* rj = S.r_jph + 1;
-  const double* zk = S.z_kph + 1;
-  double piph = S.piph[c], dphi = S.dphi[c];
-  double rp = rj[j], rm = rj[j - 1], zp = zk[k], zm = zk[k - 1];
-  double phim = piph - dphi;
-  double dV = (.5 * (rp + rm)) * (rp - rm) * get_dp(piph, phim, P.phi_max) * (zp - zm);
-  double r = S.ring_rc[jk];
   double U[NQ];
 #pragma unroll
   for (int q = 0; q < NQ; ++q) U[q] = S.cons[q * N + c];
   R pr[NQ];
-  int hits = Phys::cons2prim(P, S.planets, U, pr, r, .5 * (phim + piph), dV);
+  int hits;
+  if constexpr (kMix<R>) {
+    R dph = S.dphi_r[c];
+    hits = Phys::cons2prim(P, S.planets, U, pr, S.ring_rc_r[jk], (R)S.piph[c] - (R).5 * dph,
+                           S.ring_vol_r[jk] * dph);
+  } else {
+    const double* rj = S.r_jph + 1;
+    const double* zk = S.z_kph + 1;
+    double piph = S.piph[c], dphi = S.dphi[c];
+    double rp = rj[j], rm = rj[j - 1], zp = zk[k], zm = zk[k - 1];
+    double phim = piph - dphi;
+    double dV = (.5 * (rp + rm)) * (rp - rm) * get_dp(piph, phim, P.phi_max) * (zp - zm);
+    double r = S.ring_rc[jk];
+    hits = Phys::cons2prim(P, S.planets, U, pr, r, .5 * (phim + piph), dV);
+  }
   bool bad = false;
 #pragma unroll
   for (int q = 0; q < NQ; ++q) {

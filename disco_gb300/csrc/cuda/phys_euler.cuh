@@ -58,7 +58,7 @@ struct Euler {
   // cons2prim, euler.c:103-140.  cons in FP64 (conserved accumulation),
   // prim in R.  Returns a floor-hit bit mask (1 = density, 2 = pressure).
   DISCO_D static int cons2prim(const DevParams& P, const DevPlanet* pl, const double* cons, R* prim,
-                               double r, double phi, double dV) {
+                               R r, R phi, R dV) {
     int hits = 0;
     R rho, Sr, Sp, Sz, E;
     R rr = (R)r;
@@ -129,25 +129,23 @@ struct Euler {
     if (*Sl > -cs2 + vn2) *Sl = -cs2 + vn2;
   }
 
-  // source, euler.c:172-213 (geometric + energy-frame source).
-  DISCO_D static void source(const DevParams& P, const R* prim, double* cons, const double* xp,
-                             const double* xm, double dVdt, double rc, double r23) {
-    double rp = xp[0], rm = xm[0];
+  // source, euler.c:172-213 (geometric + energy-frame source).  T is the
+  // accumulator type; r_1 = .5 (rp + rm), rc = centroid radius, dphi = cell
+  // width (r23 is unused by this module).
+  template <typename T>
+  DISCO_D static void source(const DevParams& P, const R* prim, T* cons, T dVdt, R r_1, R r23,
+                             R r, R dphi) {
+    (void)r23;
     R rho = prim[RHO], Pp = prim[PPP];
-    R r = (R)rc;
-    R r_1 = (R)(.5 * (rp + rm));
     R vr = prim[URR], omega = prim[UPP], vz = prim[UZZ];
     R centrifugal = rho * omega * omega * r;
-    if (P.polar_sources) {
-      double dp = get_dp(xp[1], xm[1], P.phi_max);
-      centrifugal *= (R)(sin(0.5 * dp) / (0.5 * dp));
-    }
+    if (P.polar_sources) centrifugal *= (R)(sin((R)0.5 * dphi) / ((R)0.5 * dphi));
     R press_bal = Pp / r_1;
-    cons[SRR] += dVdt * (double)(centrifugal + press_bal);
+    cons[SRR] += dVdt * (T)(centrifugal + press_bal);
     R om = get_om<R>(P, r);
     R om_r = get_om1<R>(P, r);
     R om_z = 0.0;
-    cons[TAU] += (dVdt * (double)rho) * (double)(r * vr * om * om - r * r * (omega - om) * (vr * om_r + vz * om_z));
+    cons[TAU] += (dVdt * (T)rho) * (T)(r * vr * om * om - r * r * (omega - om) * (vr * om_r + vz * om_z));
   }
 
   // nu for viscosity: explicit, or alpha c^2 / get_height_om (euler.c:220-226).
@@ -211,6 +209,32 @@ struct Euler {
   DISCO_D static void hlld(const DevParams&, R, const R*, const R*, R* F, R* U, R, const R*) {
 #pragma unroll
     for (int q = 0; q < NQ; ++q) { F[q] = 0; U[q] = 0; }
+  }
+
+  // mindt of the mixed path: the same bound in R, with the cell extents
+  // dL0 = r dphi, dL1 = dr, dL2 = dz given.
+  DISCO_D static R mindt_r(const DevParams& P, const DevPlanet* pl, const R* prim, R w, R dL0, R dL1,
+                           R dL2, R r, R phi) {
+    R Pp = prim[PPP], rho = prim[RHO];
+    R vp = (prim[UPP] - w) * r;
+    R vr = prim[URR], vz = prim[UZZ];
+    R cs = sqrt((R)P.gamma_law * Pp / rho);
+    R dt = dL1 / (cs + fabs(vr)), dtp = dL0 / (cs + fabs(vp)), dtz = dL2 / (cs + fabs(vz));
+    if (dt > dtp) dt = dtp;
+    if (dt > dtz) dt = dtz;
+    if (P.include_viscosity) {
+      R dx = dL0;
+      if (dx > dL1) dx = dL1;
+      if (dx > dL2) dx = dL2;
+      R nu = (R)P.explicit_viscosity;
+      if (P.alpha_flag) {
+        R c2 = (R)P.gamma_law * prim[PPP] / prim[RHO];
+        nu = (R)P.explicit_viscosity * c2 / get_height_om<R>(P, pl, r, phi);
+      }
+      R dt_visc = (R)0.5 * dx * dx / nu;
+      if (dt > dt_visc) dt = dt_visc;
+    }
+    return dt;
   }
 
   // mindt, euler.c:328-377.

@@ -38,7 +38,7 @@ struct Mhd {
 
   // cons2prim, mhd.c:138-185 (FP64 conserved in, R primitives out)
   DISCO_D static int cons2prim(const DevParams& P, const DevPlanet* pl, const double* cons, R* prim,
-                               double r, double phi, double dV) {
+                               R r, R phi, R dV) {
     int hits = 0;
     R rho, Sr, Sp, Sz, E, Br, Bp, Bz;
     R rr = (R)r;
@@ -94,31 +94,29 @@ struct Mhd {
     for (int q = NC; q < NQ; ++q) f[q] = prim[q] * f[DDD];
   }
 
-  // source, mhd.c:225-262
-  DISCO_D static void source(const DevParams& P, const R* prim, double* cons, const double* xp,
-                             const double* xm, double dVdt, double rc, double r23) {
-    double rp = xp[0], rm = xm[0];
-    double dphi = get_dp(xp[1], xm[1], P.phi_max);
+  // source, mhd.c:225-262.  T is the accumulator type (FP64 conserved
+  // state, or the R sum of the mixed path); r_1 = .5 (rp + rm),
+  // r23 = (rp^2 + rp rm + rm^2) / 3, rc = centroid radius, dphi = cell width.
+  template <typename T>
+  DISCO_D static void source(const DevParams& P, const R* prim, T* cons, T dVdt, R r_1, R r2_3,
+                             R r, R dphi) {
     R rho = prim[RHO], Pp = prim[PPP];
-    R r_1 = (R)(.5 * (rp + rm));
-    R r2_3 = (R)r23;
     R vr = prim[URR], omega = prim[UPP];
-    R r = (R)rc;
     R Br = prim[BRR], Bp = prim[BPP], Bz = prim[BZZ];
     R B2 = Br * Br + Bp * Bp + Bz * Bz;
     R centrifugal;
     if (P.polar_sources) {
-      centrifugal = (rho * omega * omega * r2_3) / r_1 * (R)sin(.5 * dphi) / (R)(.5 * dphi);
+      centrifugal = (rho * omega * omega * r2_3) / r_1 * (R)sin((R).5 * dphi) / (R)((R).5 * dphi);
       centrifugal -= Bp * Bp / r_1;
     } else {
       centrifugal = rho * omega * omega * r - Bp * Bp / r;
     }
     R press_bal = (Pp + (R).5 * B2) / r_1;
-    cons[SRR] += dVdt * (double)(centrifugal + press_bal);
+    cons[SRR] += dVdt * (T)(centrifugal + press_bal);
     R om = get_om<R>(P, r), om1 = get_om1<R>(P, r);
-    cons[TAU] += ((dVdt * (double)rho) * (double)vr) * (double)(om * om * r2_3 / r_1 - om1 * (omega - om) * r2_3);
+    cons[TAU] += ((dVdt * (T)rho) * (T)vr) * (T)(om * om * r2_3 / r_1 - om1 * (omega - om) * r2_3);
     if (P.include_viscosity)
-      cons[SRR] += -dVdt * P.explicit_viscosity * (double)rho * (double)vr / (double)(r_1 * r_1);
+      cons[SRR] += -dVdt * (T)P.explicit_viscosity * (T)rho * (T)vr / (T)(r_1 * r_1);
   }
 
   // mhd.c defines neither visc_flux nor visc_source with content.
@@ -332,6 +330,24 @@ struct Mhd {
     F[BRR] *= brfac / hr; F[BPP] *= bpfac / hp; F[BZZ] *= bzfac / hz;
     U[SRR] *= hr; U[LLL] *= hp; U[SZZ] *= hz;
     U[BRR] *= brfac / hr; U[BPP] *= bpfac / hp; U[BZZ] *= bzfac / hz;
+  }
+
+  // mindt of the mixed path: the same bound in R, with the cell extents
+  // dL0 = r dphi, dL1 = dr, dL2 = dz given.
+  DISCO_D static R mindt_r(const DevParams& P, const DevPlanet*, const R* prim, R w, R dL0, R dL1,
+                           R dL2, R r, R phi) {
+    (void)phi;
+    R Pp = prim[PPP], rho = prim[RHO];
+    R vp = (prim[UPP] - w) * r;
+    R vr = prim[URR], vz = prim[UZZ];
+    R cs = sqrt((R)P.gamma_law * Pp / rho);
+    R Br = prim[BRR], Bp = prim[BPP], Bz = prim[BZZ];
+    R b2 = (Br * Br + Bp * Bp + Bz * Bz) / rho;
+    R cf = sqrt(cs * cs + b2);
+    R dt = dL1 / (cf + fabs(vr)), dtp = dL0 / (cf + fabs(vp)), dtz = dL2 / (cf + fabs(vz));
+    if (dt > dtp) dt = dtp;
+    if (dt > dtz) dt = dtz;
+    return dt;
   }
 
   // mindt, mhd.c:452-483
