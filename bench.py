@@ -115,30 +115,53 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def kernel_bytes(name: str, N: int, nf: dict, nq: int, sw: int) -> float:
+def kernel_bytes(name: str, N: int, nf: dict, nq: int, sw: int, ct: bool) -> float:
     """Algorithmic (compulsory) HBM bytes of one launch of each kernel: every
-    input and output array element moved once.  N = cells incl. ghosts,
-    nf[d] = faces of dimension d, sw = bytes of a reconstruction-type value."""
-    idx = 4
-    f8 = 8
+    array element the kernel must read or write, moved once (neighbour and
+    face re-reads are assumed served on chip).  N = cells incl. ghosts,
+    nf[d] = faces of dimension d ("r", "z"), sw = bytes of a reconstruction
+    value (4 mixed, 8 FP64), index = 4 bytes, positions/conserved = 8 bytes.
+    The same table is written out, per unit, in the design doc."""
+    ix, f8 = 4, 8
+    nfa = nf["r"] + nf["z"]
+    c = 1 if ct else 0
     if name == "plm_phi":
-        return N * (2 * nq * sw + f8)
+        return N * (2 * nq * sw + sw)
     if name.startswith("plm_trans"):
-        d = "r" if name.endswith("_r") else "z"
-        return N * (3 * nq * sw + 2 * f8 + 4 * idx) + nf[d] * (2 * f8 + 2 * idx)
+        d = name[-1]
+        return N * (3 * nq * sw + sw + 4 * ix) + nf[d] * (3 * sw + 2 * ix)
     if name == "flux_phi":
-        return N * (3 * nq * sw + 3 * f8)
-    if name.startswith("flux_"):
+        return N * (3 * nq * sw + sw + 2 * f8 + c * 16 * sw)
+    if name in ("flux_r", "flux_z"):
         d = name[-1]
-        return N * (3 * nq * sw + 2 * f8) + nf[d] * (2 * f8 + 2 * idx + nq * sw)
+        return N * 3 * nq * sw + nf[d] * (2 * ix + f8 + 3 * sw + nq * sw + c * 3 * sw)
+    if name == "ct_gather":
+        return N * (15 * f8 + 36 * sw + 4 * ix) + nfa * 5 * sw
+    if name == "ct_avg":
+        return N * (20 * sw + f8 + 4 * ix) + nfa * 2 * sw
+    if name == "ct_bflux":
+        return N * (4 * sw + 10 * f8 + 4 * ix)
+    if name == "ct_edge":
+        return N * (f8 + 4 * sw + 10 * f8)
+    if name == "ct_flip":
+        return N * f8 + nfa * (1 + 2 * ix)
+    if name == "ct_b2c":
+        return N * (5 * f8 + 3 * f8 + sw + 4 * ix) + nfa * (sw + 1 + 2 * ix)
+    if name == "c2p":
+        return N * (nq * f8 + nq * sw + sw + f8)
     if name == "update":
-        fb = sum(nf[d] * nq * sw for d in nf)
-        return N * (4 * nq * f8 + 2 * nq * sw + 5 * f8 + 8 * idx) + fb
-    if name == "faces_r" or name == "faces_z":
+        return N * (3 * nq * f8 + 2 * nq * sw + 5 * f8 + sw + 8 * ix) + nfa * nq * sw
+    if name in ("faces_r", "faces_z"):
         d = name[-1]
-        return N * 2 * f8 + nf[d] * (2 * idx + 1 + 2 * f8) + N * 4 * idx
+        return N * (2 * f8 + 4 * ix) + nf[d] * (2 * ix + 1 + f8 + 3 * sw + c * (f8 + 4 * sw))
     if name == "mindt":
-        return N * (nq * sw + 3 * f8)
+        return N * (nq * sw + 2 * f8 + sw)
+    if name in ("wcell_ring", "wcell", "wcell_avg"):
+        return N * (sw + f8)
+    if name == "boundary":
+        return N * 2 * f8
+    if name == "anchor":
+        return N * f8
     return 0.0
 
 
@@ -358,14 +381,17 @@ def main():
     prof = sorted(res["profile"], key=lambda x: -x[2])
     tot_prof = sum(p[2] for p in prof)
     top = prof[0]
-    top_bytes = kernel_bytes(top[0], N, nf, nq, sw)
+    ct = nq >= 8
+    top_bytes = kernel_bytes(top[0], N, nf, nq, sw, ct)
     top_avg_s = top[2] / top[1] / 1e3
     achieved = top_bytes / top_avg_s / 1e9
     roof = {"bound": "hbm", "kernel": top[0], "achieved": achieved, "peak": hbm, "unit": "GB/s",
             "frac": achieved / hbm, "peak_kind": peak_kind, "traffic": None,
             "algorithmic_bytes_per_launch": top_bytes,
             "share_of_step": top[2] / tot_prof}
-    bz = nq * (4 * sw + 6 * 8) + 6 * 8   # fused-RK2 compulsory bytes per zone-update
+    # fused-RK2 compulsory bytes per zone-update: NQ (4 s_W + 6 s_U) + 6 x 8,
+    # plus 25 x 8 for the face fluxes Phi / RK_Phi of constrained transport
+    bz = nq * (4 * sw + 6 * 8) + 6 * 8 + (200 if ct else 0)
     whole = {"algorithmic_bytes_per_zone_update": bz, "achieved_GBps": bz * value / 1e9,
              "frac_of_hbm": bz * value / 1e9 / hbm}
     line = {
@@ -385,7 +411,10 @@ def main():
                              "after warmup+steps RK2 steps from the same initial state",
         "roofline": roof,
         "step_hbm": whole,
-        "kernels_ms_per_step": {p[0]: p[2] / 3 for p in prof},
+        "kernels": {p[0]: {"ms_per_step": p[2] / 3,
+                           "GBps": (kernel_bytes(p[0], N, nf, nq, sw, ct) * p[1] / (p[2] / 1e3) / 1e9
+                                    if p[2] > 0 else None)}
+                    for p in prof},
         "e2e": res["e2e"],
         "gpu_launches": int(res[1]["launches"]),
         "clocks": res[1]["clocks"],

@@ -48,9 +48,14 @@ __global__ void k_ct_gather(DevParams P, DevState<R> S, CtStateT<R> C, double RK
       R e0 = S.Eraw[(a + 0) * N + c], e2 = S.Eraw[(a + 2) * N + c];
       R b0 = S.Braw[(a + 0) * N + c], b2 = S.Braw[(a + 2) * N + c];
       int base = S.face_off[d][pb], Nf = S.face_off[d][pb + 1] - base;
+      // mixed path: the face EMF was solved in the L ring's frame; this cell
+      // (R) stores it relative to its own ring's frame
+      R cX = kMix<R> ? S.pcX[d][pb] : (R)0;
       for_run(S.run_dn_s[d][c], S.run_dn_e[d][c], base, Nf, [&](int f) {
         R fr = S.ffrR[d][f];
-        e0 += (R).5 * S.fErz[d][f] * fr; e2 += (R).5 * S.fErz[d][f] * fr;
+        R ef = S.fErz[d][f];
+        if constexpr (kMix<R>) ef += cX * S.fBrz[d][f];
+        e0 += (R).5 * ef * fr; e2 += (R).5 * ef * fr;
         b0 += (R).5 * S.fBrz[d][f] * fr; b2 += (R).5 * S.fBrz[d][f] * fr;
       });
       S.Eraw[(a + 0) * N + c] = e0; S.Eraw[(a + 2) * N + c] = e2;
@@ -99,11 +104,16 @@ __global__ void k_ct_avg(DevParams P, DevState<R> S, CtStateT<R> C) {
   int jk = S.cell_ring[c];
   int j = jk % P.Nr, k = jk / P.Nr;
   R outE[4], outB[4];
+  // mixed path: the B average split by the ring whose frame the EMFs were
+  // stored in (own ring / the neighbouring ring across the face)
+  R ownB[4], othB[4], dOmo[4];
+  bool has[4] = {false, false, false, false};
   // slots: 0 -> E0 (r lower), 1 -> E1 (r upper), 2 -> E4 (z lower), 3 -> E5 (z upper)
   const int slot_e[4] = {0, 1, 4, 5};
   for (int s = 0; s < 4; ++s) {
     outE[s] = edge_avg(S, S.Eraw, slot_e[s], c);
     outB[s] = edge_avg(S, S.Braw, slot_e[s], c);
+    ownB[s] = outB[s]; othB[s] = 0; dOmo[s] = 0;
   }
   for (int dim = 1; dim <= 2; ++dim) {
     if (dim == 1 && P.Nr <= 1) continue;
@@ -116,8 +126,11 @@ __global__ void k_ct_avg(DevParams P, DevState<R> S, CtStateT<R> C) {
       R dp1 = S.fdp1[d][f], dp2 = S.fdp2[d][f];
       R Eavg = (dp2 * edge_avg(S, S.Eraw, a + 0, c2) + dp1 * edge_avg(S, S.Eraw, a + 2, c2)) / (dp1 + dp2);
       R Bavg = (dp2 * edge_avg(S, S.Braw, a + 0, c2) + dp1 * edge_avg(S, S.Braw, a + 2, c2)) / (dp1 + dp2);
-      outE[2 * d + 1] = (R).5 * (outE[2 * d + 1] + Eavg);
-      outB[2 * d + 1] = (R).5 * (outB[2 * d + 1] + Bavg);
+      const int s = 2 * d + 1;
+      outE[s] = (R).5 * (outE[s] + Eavg);
+      outB[s] = (R).5 * (outB[s] + Bavg);
+      has[s] = true; othB[s] = Bavg;
+      if constexpr (kMix<R>) dOmo[s] = S.pdOm[d][pa];
     }
     if (pb >= 0) {   // LRtype 1 face owned by c (c = R = c1, c2 = L)
       int f = S.run_dn_e[d][c];
@@ -125,19 +138,28 @@ __global__ void k_ct_avg(DevParams P, DevState<R> S, CtStateT<R> C) {
       R dp1 = S.fdp1[d][f], dp2 = S.fdp2[d][f];
       R Eavg = (dp2 * edge_avg(S, S.Eraw, a + 1, c2) + dp1 * edge_avg(S, S.Eraw, a + 3, c2)) / (dp1 + dp2);
       R Bavg = (dp2 * edge_avg(S, S.Braw, a + 1, c2) + dp1 * edge_avg(S, S.Braw, a + 3, c2)) / (dp1 + dp2);
-      outE[2 * d + 0] = (R).5 * (outE[2 * d + 0] + Eavg);
-      outB[2 * d + 0] = (R).5 * (outB[2 * d + 0] + Bavg);
+      const int s = 2 * d + 0;
+      outE[s] = (R).5 * (outE[s] + Eavg);
+      outB[s] = (R).5 * (outB[s] + Bavg);
+      has[s] = true; othB[s] = Bavg;
+      if constexpr (kMix<R>) dOmo[s] = -S.pdOm[d][pb];
     }
   }
   const double* rj = S.r_jph + 1;
   if constexpr (kMix<R>) {
-    R w = (R)S.wiph[c];
+    // E_lab - h w B = X + s h ((w - Om_own) B_own + (w - Om_other) B_other),
+    // all frame differences small and exact to FP32 rounding
+    R wrel = (R)(S.wiph[c] - S.ring_Om[jk]);
     R hL = (R)rj[j - 1], hR = (R)rj[j], hC = S.ring_rc_r[jk];
-    C.Efin[0 * N + c] = outE[0] - (hL * w) * outB[0];
-    C.Efin[1 * N + c] = outE[1] - (hR * w) * outB[1];
-    C.Efin[2 * N + c] = outE[2] + (hC * w) * outB[2];
-    C.Efin[3 * N + c] = outE[3] + (hC * w) * outB[3];
+    const R h[4] = {hL, hR, hC, hC};
+    const R sg[4] = {(R)-1, (R)-1, (R)1, (R)1};
+#pragma unroll
+    for (int s = 0; s < 4; ++s) {
+      R bt = has[s] ? (R).5 * (wrel * ownB[s] + (wrel - dOmo[s]) * othB[s]) : wrel * ownB[s];
+      C.Efin[s * N + c] = outE[s] + sg[s] * h[s] * bt;
+    }
   } else {
+    (void)ownB; (void)othB; (void)dOmo; (void)has;
     double hL = rj[j - 1], hR = rj[j];
     double hC = S.ring_rc[jk];
     double w = S.wiph[c];

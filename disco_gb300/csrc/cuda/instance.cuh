@@ -110,6 +110,8 @@ struct Instance : InstanceBase {
   int maxring = 0;
   int graph_nodes = 0;
   double host_t = 0;
+  std::vector<double> ring_Om_h;   // ring frames (host copy)
+  std::vector<int> cell_ring_h;
 
   ~Instance() override {
     if (flush_buf) cudaFree(flush_buf);
@@ -215,6 +217,8 @@ struct Instance : InstanceBase {
     A(&S.ring_rc, nring); A(&S.ring_r23, nring);
     A(&S.ring_rc_r, nring); A(&S.ring_r1_r, nring); A(&S.ring_vol_r, nring); A(&S.ring_dA_r, nring);
     A(&S.ring_r23_r, nring); A(&S.ring_zc_r, nring);
+    A(&S.ring_Om, nring); A(&S.ring_Om_r, nring); A(&S.ring_Lsh, nring);
+    A(&S.ring_gL_r, nring); A(&S.ring_gR_r, nring);
     for (int d = 0; d < 2; ++d) { A(&S.ring_At_r[d], nring); A(&S.ring_dl_r[d], nring); }
     A(&piph_buf[0], N); A(&piph_buf[1], N);
     A(&S.dphi, N); A(&S.wiph, N);
@@ -257,7 +261,7 @@ struct Instance : InstanceBase {
       A(&S.fL[d], nf); A(&S.fR[d], nf); A(&S.fLR[d], nf); A(&S.fphic[d], nf); A(&S.fdA[d], nf);
       A(&S.fdpL[d], nf); A(&S.fdpR[d], nf);
       A(&S.pdxL[d], np); A(&S.pdxR[d], np); A(&S.pdxs[d], np); A(&S.prad[d], np);
-      A(&S.pidxs[d], np); A(&S.pdA[d], np);
+      A(&S.pidxs[d], np); A(&S.pdA[d], np); A(&S.pdOm[d], np); A(&S.pcX[d], np);
       A(&S.fflux[d], (size_t)NQ * nf);
       A(&S.run_up_s[d], N); A(&S.run_up_e[d], N); A(&S.run_dn_s[d], N); A(&S.run_dn_e[d], N);
       if (ct) {
@@ -297,6 +301,25 @@ struct Instance : InstanceBase {
     CK(cudaMemset(S.errs, 0, sizeof(DevErrs)));
     host_t = dom->t;
 
+    // ring frames of the mixed path (0 on the FP64 path): the ring mean of
+    // the initial omega of the real rings, the nearest real ring's for ghosts
+    ring_Om_h.assign(nring, 0.0);
+    if (kMix<R>) {
+      const int NgRa = dom->NgRa, NgRb = dom->NgRb, NgZa = dom->NgZa, NgZb = dom->NgZb;
+      for (int jk = 0; jk < nring; ++jk) {
+        int j = jk % Nr, k = jk / Nr;
+        int jr = std::min(std::max(j, NgRa), Nr - NgRb - 1);
+        int kr = std::min(std::max(k, NgZa), Nz - NgZb - 1);
+        int src = jr + Nr * kr;
+        double sum = 0;
+        for (long c = dom->ring_off[src]; c < dom->ring_off[src + 1]; ++c)
+          sum += dom->prim[(long)UPP * N + c];
+        long np_ = dom->ring_off[src + 1] - dom->ring_off[src];
+        ring_Om_h[jk] = np_ > 0 ? sum / (double)np_ : 0.0;
+      }
+    }
+    CK(cudaMemcpy(S.ring_Om, ring_Om_h.data(), sizeof(double) * nring, cudaMemcpyHostToDevice));
+    cell_ring_h = cell_ring;
     LAUNCH("ring_geom", (k_ring_geom<R><<<blocks(nring), 256, 0, st>>>(P, S, nring)));
     for (int d = 0; d < 2; ++d)
       if (npair[d]) LAUNCH("pair_geom", (k_pair_geom<R><<<blocks(npair[d]), 256, 0, st>>>(P, S, d + 1, npair[d])));
@@ -615,6 +638,7 @@ struct Instance : InstanceBase {
         std::vector<R> tmp((size_t)NQ * N);
         CK(cudaMemcpy(tmp.data(), S.prim, sizeof(R) * NQ * N, cudaMemcpyDeviceToHost));
         for (size_t i = 0; i < tmp.size(); ++i) v->prim[i] = (double)tmp[i];
+        for (long c = 0; c < N; ++c) v->prim[(size_t)UPP * N + c] += ring_Om_h[cell_ring_h[c]];
       }
     }
     double sc[SC_COUNT];
@@ -631,6 +655,9 @@ struct Instance : InstanceBase {
     if (v->prim) {
       std::vector<R> tmp((size_t)NQ * N);
       for (size_t i = 0; i < tmp.size(); ++i) tmp[i] = (R)v->prim[i];
+      if (kMix<R>)
+        for (long c = 0; c < N; ++c)
+          tmp[(size_t)UPP * N + c] = (R)(v->prim[(size_t)UPP * N + c] - ring_Om_h[cell_ring_h[c]]);
       CK(cudaMemcpy(S.prim, tmp.data(), sizeof(R) * NQ * N, cudaMemcpyHostToDevice));
     }
     if (v->dphi) sync_dphi_r();

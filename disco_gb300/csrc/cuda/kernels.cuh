@@ -63,6 +63,16 @@ struct DevState {
   R* ring_At_r[2];
   R* ring_dl_r[2];
   R* dphi_r;                   // [N] dphi in R (the same array as dphi when R is double)
+  // Ring frame of the mixed path: there prim[UPP] holds omega - Om of the
+  // cell's ring, so the FP32 value keeps the precision of the motion
+  // relative to the mesh (Om is fixed at set-up; 0 on the FP64 path).
+  double* ring_Om;             // per ring: Om
+  R* ring_Om_r;                // Om in R
+  double* ring_Lsh;            // Om rc^2: angular momentum per unit mass of the frame
+  R* ring_gL_r;                // Om (rc - r_lower), Om (rc - r_upper): EMF frame terms
+  R* ring_gR_r;
+  R* pdOm[2];                  // per pair: Om(R ring) - Om(L ring)
+  R* pcX[2];                   // per pair: EMF frame term of the R cell, +-(Om_R - Om_L) r
   R* pdxL[2];                  // per pair: dxL, dxR, dxL + dxR, face radius
   R* pdxR[2];
   R* pdxs[2];
@@ -187,6 +197,7 @@ __global__ void k_wcell(DevParams P, DevState<R> S) {
     double wL = (double)S.prim[UPP * S.N + c];        // get_omega: prim[UPP]
     double wR = (double)S.prim[UPP * S.N + off + ip];
     w = .5 * (wL + wR);
+    if constexpr (kMix<R>) w += S.ring_Om[jk];          // ring frame -> lab
   }
   (void)k;
   S.wiph[c] = w;
@@ -210,7 +221,7 @@ __global__ void k_wcell_ring(DevParams P, DevState<R> S) {
   if (wid == 0) {
     s = lane < (int)(blockDim.x >> 5) ? part[lane] : 0.0;
     for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-    if (lane == 0) part[0] = s / (double)Np;
+    if (lane == 0) part[0] = s / (double)Np + S.ring_Om[jk];   // ring frame -> lab
   }
   __syncthreads();
   double w = part[0];
@@ -590,6 +601,11 @@ __global__ void k_ring_geom(DevParams P, DevState<R> S, int nring) {
   S.ring_dA_r[jk] = (R)(dr * dz);
   S.ring_r23_r[jk] = (R)((rp * rp + rp * rm + rm * rm) / 3.);
   S.ring_zc_r[jk] = (R)centroid_z(zp, zm);
+  double Om = S.ring_Om[jk], rc = centroid_r(rp, rm);
+  S.ring_Om_r[jk] = (R)Om;
+  S.ring_Lsh[jk] = Om * rc * rc;
+  S.ring_gL_r[jk] = (R)(Om * (rc - rm));
+  S.ring_gR_r[jk] = (R)(Om * (rc - rp));
   // total face area per unit dphi, one side only at the domain's edge rings
   double atr = (rp + rm) * dz, atz = 2. * r1 * dr;
   if (j == 0) atr = rp * dz;
@@ -622,6 +638,10 @@ __global__ void k_pair_geom(DevParams P, DevState<R> S, int dim, int npair) {
   double a = dim == 1 ? (.5 * (rj[pj] + rj[pj])) * (zk[pk] - zk[pk - 1])
                       : (.5 * (rj[pj] + rj[pj - 1])) * (rj[pj] - rj[pj - 1]);
   S.pdA[d][pair] = (R)a;
+  PairInfo pi = pair_info(P, dim, pair);
+  double dOm = S.ring_Om[pi.R] - S.ring_Om[pi.L];
+  S.pdOm[d][pair] = (R)dOm;
+  S.pcX[d][pair] = (R)((dim == 1 ? -dOm : dOm) * r);
 }
 
 // ---- plm_trans, plm.c:56-195 (per-cell gather over the cell's faces) ---------
@@ -655,7 +675,7 @@ __global__ void k_plm_trans(DevParams P, DevState<R> S, int dim) {
 #pragma unroll
   for (int q = 0; q < NQ; ++q) { pc[q] = S.prim[q * N + c]; gpc[q] = S.gradp[q * N + c]; }
 
-  auto visit = [&](int f, int other, bool self_is_L, R dxsum, R idxsum) {
+  auto visit = [&](int f, int other, bool self_is_L, R dxsum, R idxsum, R dOm) {
     R dpL = S.fdpL[d][f], dpR = S.fdpR[d][f];
     R dA = S.fdA[d][f];
 #pragma unroll
@@ -665,7 +685,7 @@ __global__ void k_plm_trans(DevParams P, DevState<R> S, int dim) {
       if (self_is_L) { WL = pc[q] + dpL * gpc[q]; WR = po - dpR * gpo; }
       else { WL = po + dpL * gpo; WR = pc[q] - dpR * gpc[q]; }
       R Sl;
-      if constexpr (kMix<R>) Sl = (WR - WL) * idxsum;
+      if constexpr (kMix<R>) Sl = ((WR - WL) + (q == UPP ? dOm : (R)0)) * idxsum;   // frames of the rings
       else Sl = (WR - WL) / dxsum;
       sum[q] += Sl * dA;
       R ps = PLM * Sl;
@@ -686,14 +706,16 @@ __global__ void k_plm_trans(DevParams P, DevState<R> S, int dim) {
   if (pb >= 0) {
     int base = S.face_off[d][pb], Nf = S.face_off[d][pb + 1] - base;
     R dxs = S.pdxs[d][pb], idxs = kMix<R> ? S.pidxs[d][pb] : (R)0;
+    R dOm = kMix<R> ? S.pdOm[d][pb] : (R)0;
     for_run(S.run_dn_s[d][c], S.run_dn_e[d][c], base, Nf,
-            [&](int f) { visit(f, S.fL[d][f], false, dxs, idxs); });
+            [&](int f) { visit(f, S.fL[d][f], false, dxs, idxs, dOm); });
   }
   if (pa >= 0) {
     int base = S.face_off[d][pa], Nf = S.face_off[d][pa + 1] - base;
     R dxs = S.pdxs[d][pa], idxs = kMix<R> ? S.pidxs[d][pa] : (R)0;
+    R dOm = kMix<R> ? S.pdOm[d][pa] : (R)0;
     for_run(S.run_up_s[d][c], S.run_up_e[d][c], base, Nf,
-            [&](int f) { visit(f, S.fR[d][f], true, dxs, idxs); });
+            [&](int f) { visit(f, S.fR[d][f], true, dxs, idxs, dOm); });
   }
 
   // total weight, plm.c:113-143
@@ -800,14 +822,25 @@ __global__ void k_flux_phi(DevParams P, DevState<R> S, double fac) {
   }
   R n[3] = {0, 1, 0};
   R hn = (R)r;
-  R w = hn * (R)S.wiph[c];
   R Fw[NQ], Fl[NQ], Us[NQ];
-  solve_riemann<Phys, R, NQ>(P, S.planets, primL, primR, gLr, gp, gLz, gRr, gp, gRz, (R)r,
-                             (R)phi, n, w, Fw, Fl, Us);
   if constexpr (kMix<R>) {
+    // Riemann problem in the ring frame: mesh speed and energy frame
+    // relative to Om, then Fw back to the lab (the mass flux through the
+    // moving face is frame invariant; L and, for the total energy of the
+    // MHD module, TAU pick up the frame's share).
+    R Om = S.ring_Om_r[jk];
+    R w = hn * (R)(S.wiph[c] - S.ring_Om[jk]);
+    solve_riemann<Phys, R, NQ>(P, S.planets, primL, primR, gLr, gp, gLz, gRr, gp, gRz, r,
+                               (R)phi, n, w, Fw, Fl, Us, Om);
+    R Omr2 = Om * r * r;
+    if (Phys::MHD) Fw[TAU] += Om * Fw[LLL] + (R).5 * Om * Omr2 * Fw[DDD];
+    Fw[LLL] += Omr2 * Fw[DDD];
 #pragma unroll
     for (int q = 0; q < NQ; ++q) S.fphi[q * N + c] = Fw[q] * dAdt_r;
   } else {
+    R w = hn * (R)S.wiph[c];
+    solve_riemann<Phys, R, NQ>(P, S.planets, primL, primR, gLr, gp, gLz, gRr, gp, gRz, (R)r,
+                               (R)phi, n, w, Fw, Fl, Us);
 #pragma unroll
     for (int q = 0; q < NQ; ++q) S.fphi[q * N + c] = (R)((double)Fw[q] * dAdt);
   }
@@ -815,7 +848,14 @@ __global__ void k_flux_phi(DevParams P, DevState<R> S, double fac) {
     R Ez, Br, Er, Bz;
     Phys::flux_to_E(Fl, Us, (R)r, &Ez, &Br, &Er, &Bz, 0);
     R hEz = (R).5 * Ez, hBr = (R).5 * Br, hEr = (R).5 * Er, hBz = (R).5 * Bz;
-    S.Eraw[0 * N + c] = hEz; S.Eraw[1 * N + c] = hEz; S.Eraw[2 * N + cp] = hEz; S.Eraw[3 * N + cp] = hEz;
+    if constexpr (kMix<R>) {
+      // ring-frame EMFs X = E + s h Om B (s = -1 on r edges, +1 on z edges);
+      // the Er slots reduce to the frame-relative value exactly
+      R hEzL = (R).5 * (Ez + S.ring_gL_r[jk] * Br), hEzR = (R).5 * (Ez + S.ring_gR_r[jk] * Br);
+      S.Eraw[0 * N + c] = hEzL; S.Eraw[1 * N + c] = hEzR; S.Eraw[2 * N + cp] = hEzL; S.Eraw[3 * N + cp] = hEzR;
+    } else {
+      S.Eraw[0 * N + c] = hEz; S.Eraw[1 * N + c] = hEz; S.Eraw[2 * N + cp] = hEz; S.Eraw[3 * N + cp] = hEz;
+    }
     S.Braw[0 * N + c] = hBr; S.Braw[1 * N + c] = hBr; S.Braw[2 * N + cp] = hBr; S.Braw[3 * N + cp] = hBr;
     S.Eraw[4 * N + c] = hEr; S.Eraw[5 * N + c] = hEr; S.Eraw[6 * N + cp] = hEr; S.Eraw[7 * N + cp] = hEr;
     S.Braw[4 * N + c] = hBz; S.Braw[5 * N + c] = hBz; S.Braw[6 * N + cp] = hBz; S.Braw[7 * N + cp] = hBz;
@@ -854,6 +894,13 @@ __global__ void k_flux_trans(DevParams P, DevState<R> S, int dim, int jmin, int 
     else grad[q] = ((pR - gpR * dpR) - (pL + gpL * dpL)) / (rdxL + rdxR);
     gLp[q] = gpL; gRp[q] = gpR;
   }
+  R OmL = 0;
+  if constexpr (kMix<R>) {   // the R cell's omega into the L ring's frame
+    R dOm = S.pdOm[d][pair];
+    primR[UPP] += dOm;
+    grad[UPP] += dOm * ridxs;
+    OmL = S.ring_Om_r[S.cell_ring[cL]];
+  }
   if (P.include_viscosity) {
     const R* go = dim == 1 ? S.gradz : S.gradr;
 #pragma unroll
@@ -871,10 +918,15 @@ __global__ void k_flux_trans(DevParams P, DevState<R> S, int dim, int jmin, int 
   R Fw[NQ], Fl[NQ], Us[NQ];
   if (dim == 1)
     solve_riemann<Phys, R, NQ>(P, S.planets, primL, primR, grad, gLp, gLo, grad, gRp, gRo, (R)r,
-                               phi, n3, (R)0.0, Fw, Fl, Us);
+                               phi, n3, (R)0.0, Fw, Fl, Us, OmL);
   else
     solve_riemann<Phys, R, NQ>(P, S.planets, primL, primR, gLo, gLp, grad, gRo, gRp, grad, (R)r,
-                               phi, n3, (R)0.0, Fw, Fl, Us);
+                               phi, n3, (R)0.0, Fw, Fl, Us, OmL);
+  if constexpr (kMix<R>) {   // back to the lab frame (fixed face: F = Fw)
+    R Omr2 = OmL * r * r;
+    if (Phys::MHD) Fw[TAU] += OmL * Fw[LLL] + (R).5 * OmL * Omr2 * Fw[DDD];
+    Fw[LLL] += Omr2 * Fw[DDD];
+  }
   R* out = S.fflux[d];
   const int NF = S.nf[d];
   R dAdt;
@@ -972,6 +1024,7 @@ __global__ void k_update(DevParams P, DevState<R> S, double RK, double fac, int 
     double xm[3] = {rj[j - 1], piph - dphi, zk[k - 1]};
     double dVdt = 0;
     if constexpr (MIX) {   // sources summed in R into dU with the flux terms
+      pr[UPP] += S.ring_Om_r[jk];   // lab omega for the source terms
       R dph = S.dphi_r[c];
       R dVdt_r = S.ring_vol_r[jk] * dph * ((R)fac * dt_r<R>(S.scal));
       R rc = S.ring_rc_r[jk];
@@ -1056,7 +1109,8 @@ __global__ void k_update(DevParams P, DevState<R> S, double RK, double fac, int 
     if constexpr (MIX) {
       R dph = first ? (R)dphi : S.dphi_r[c];
       R dV = S.ring_vol_r[jk] * dph;
-      hits = Phys::cons2prim(P, S.planets, Ukeep, pr, S.ring_rc_r[jk], (R)piph - (R).5 * dph, dV);
+      hits = Phys::cons2prim(P, S.planets, Ukeep, pr, S.ring_rc_r[jk], (R)piph - (R).5 * dph, dV,
+                             S.ring_Lsh[jk], S.ring_Om_r[jk]);
     } else {
       double rp = rj[j], rm = rj[j - 1], zp = zk[k], zm = zk[k - 1];
       double phim = piph - dphi;
@@ -1111,6 +1165,7 @@ __global__ void k_boundary(DevParams P, DevState<R> S) {
   }
   double prim[MAX_Q];
   initial_eval(P, prim, x);
+  if constexpr (kMix<R>) prim[UPP] -= S.ring_Om[jk];   // ring frame
 #pragma unroll
   for (int q = 0; q < NQ; ++q) S.prim[q * S.N + c] = (R)prim[q];
 }
@@ -1132,7 +1187,7 @@ __global__ void k_mindt(DevParams P, DevState<R> S) {
 #pragma unroll
       for (int q = 0; q < NQ; ++q) pr[q] = S.prim[q * S.N + c];
       if constexpr (kMix<R>) {
-        R w = (R).5 * ((R)S.wiph[im] + (R)S.wiph[c]);
+        R w = (R)(.5 * (S.wiph[im] + S.wiph[c]) - S.ring_Om[jk]);   // relative to the ring frame
         R dph = S.dphi_r[c];
         dtf = Phys::mindt_r(P, S.planets, pr, w, S.ring_r1_r[jk] * dph, S.ring_dl_r[1][jk],
                             S.ring_dl_r[0][jk], S.ring_rc_r[jk], (R)S.piph[c] - (R).5 * dph);
@@ -1215,7 +1270,7 @@ __global__ void k_c2p(DevParams P, DevState<R> S) {
   if constexpr (kMix<R>) {
     R dph = S.dphi_r[c];
     hits = Phys::cons2prim(P, S.planets, U, pr, S.ring_rc_r[jk], (R)S.piph[c] - (R).5 * dph,
-                           S.ring_vol_r[jk] * dph);
+                           S.ring_vol_r[jk] * dph, S.ring_Lsh[jk], S.ring_Om_r[jk]);
   } else {
     const double* rj = S.r_jph + 1;
     const double* zk = S.z_kph + 1;
@@ -1262,8 +1317,12 @@ __global__ void k_init_cells(DevParams P, DevState<R> S, const double* prim0, in
   using Phys64 = typename Phys::template Rebind<double>;
   Phys64::template prim2cons<double>(P, pr, U, r, dV);
   R out[NQ];
-  if (do_c2p) Phys::cons2prim(P, S.planets, U, out, r, piph - .5 * dphi, dV);
-  else for (int q = 0; q < NQ; ++q) out[q] = (R)pr[q];
+  if (do_c2p) {
+    Phys::cons2prim(P, S.planets, U, out, r, piph - .5 * dphi, dV, S.ring_Lsh[jk], (R)S.ring_Om[jk]);
+  } else {
+    for (int q = 0; q < NQ; ++q) out[q] = (R)pr[q];
+    if constexpr (kMix<R>) out[UPP] = (R)(pr[UPP] - S.ring_Om[jk]);   // ring frame
+  }
 #pragma unroll
   for (int q = 0; q < NQ; ++q) { S.cons[q * N + c] = U[q]; S.prim[q * N + c] = out[q]; }
 }

@@ -15,11 +15,13 @@ struct Euler {
   using Rebind = Euler<T, NQ>;
 
   // prim2cons, euler.c:37-63.  x = (r, phi, z); only r enters.
+  // omf: angular velocity of the frame the velocities are given in (0 in
+  // the lab frame); the energy frame get_om moves with it.
   template <typename T>
-  DISCO_D static void prim2cons(const DevParams& P, const R* prim, T* cons, R r, R dV) {
+  DISCO_D static void prim2cons(const DevParams& P, const R* prim, T* cons, R r, R dV, R omf = 0) {
     R rho = prim[RHO], Pp = prim[PPP], vr = prim[URR];
     R vp = prim[UPP] * r, vz = prim[UZZ];
-    R om = get_om<R>(P, r);
+    R om = get_om<R>(P, r) - omf;
     R vp_off = vp - om * r;
     R v2 = vr * vr + vp_off * vp_off + vz * vz;
     R rhoe = Pp / ((R)P.gamma_law - (R)1.);
@@ -34,9 +36,9 @@ struct Euler {
 
   // getUstar, euler.c:65-101 (HLLC star state).
   DISCO_D static void getUstar(const DevParams& P, const R* prim, R* Ustar, R r, R Sk, R Ss,
-                               const R* n, const R* Bpack) {
+                               const R* n, const R* Bpack, R omf = 0) {
     R rho = prim[RHO], vr = prim[URR], vp = prim[UPP] * r, vz = prim[UZZ], Pp = prim[PPP];
-    R om = get_om<R>(P, r);
+    R om = get_om<R>(P, r) - omf;
     R vp_off = vp - om * r;
     R v2 = vr * vr + vp_off * vp_off + vz * vz;
     R vn = vr * n[0] + vp * n[1] + vz * n[2];
@@ -57,24 +59,30 @@ struct Euler {
 
   // cons2prim, euler.c:103-140.  cons in FP64 (conserved accumulation),
   // prim in R.  Returns a floor-hit bit mask (1 = density, 2 = pressure).
+  // Mixed path (R = float): the angular momentum is taken relative to the
+  // ring frame Om in FP64 (Lsh = Om r^2), so prim[UPP] comes out as
+  // omega - Om with the precision of the motion relative to that frame.
   DISCO_D static int cons2prim(const DevParams& P, const DevPlanet* pl, const double* cons, R* prim,
-                               R r, R phi, R dV) {
+                               R r, R phi, R dV, double Lsh = 0, R Om = 0) {
     int hits = 0;
     R rho, Sr, Sp, Sz, E;
     R rr = (R)r;
     if (sizeof(R) < sizeof(double)) {   // mixed path: one reciprocal, FP32 products
       R idV = (R)1 / (R)dV;
-      rho = (R)cons[DDD] * idV; Sr = (R)cons[SRR] * idV; Sp = (R)cons[LLL] * idV / rr;
+      rho = (R)cons[DDD] * idV; Sr = (R)cons[SRR] * idV;
+      Sp = (R)(cons[LLL] - cons[DDD] * Lsh) * idV / rr;
       Sz = (R)cons[SZZ] * idV; E = (R)cons[TAU] * idV;
     } else {
       rho = (R)(cons[DDD] / dV); Sr = (R)(cons[SRR] / dV); Sp = (R)(cons[LLL] / dV / r);
       Sz = (R)(cons[SZZ] / dV); E = (R)(cons[TAU] / dV);
     }
+    R rho0 = rho;
     if (rho < (R)P.rho_floor) { rho = (R)P.rho_floor; hits |= 1; }
     R om = get_om<R>(P, rr);
     R vr = Sr / rho;
-    R vp = Sp / rho;
-    R vp_off = vp - om * rr;
+    R vp = Sp / rho;                       // relative to the frame
+    if (rho != rho0) vp += Om * rr * (rho0 / rho - (R)1);
+    R vp_off = vp + (Om - om) * rr;
     R vz = Sz / rho;
     R KE = (R).5 * (Sr * vr + rho * vp_off * vp_off + Sz * vz);
     R rhoe = E - KE;
@@ -96,9 +104,9 @@ struct Euler {
   }
 
   // flux, euler.c:142-170.
-  DISCO_D static void flux(const DevParams& P, const R* prim, R* f, R r, const R* n) {
+  DISCO_D static void flux(const DevParams& P, const R* prim, R* f, R r, const R* n, R omf = 0) {
     R rho = prim[RHO], Pp = prim[PPP], vr = prim[URR], vp = prim[UPP] * r, vz = prim[UZZ];
-    R om = get_om<R>(P, r);
+    R om = get_om<R>(P, r) - omf;
     R vn = vr * n[0] + vp * n[1] + vz * n[2];
     R wn = om * r * n[1];
     R vp_off = vp - om * r;
@@ -162,10 +170,10 @@ struct Euler {
   // visc_flux, euler.c:215-256.
   DISCO_D static void visc_flux(const DevParams& P, const DevPlanet* pl, const R* prim,
                                 const R* gradr, const R* gradp, const R* gradz, R* f, R r,
-                                R phi, const R* n) {
+                                R phi, const R* n, R omf = 0) {
     R nu = visc_nu(P, pl, prim, r, phi);
     R rho = prim[RHO], vr = prim[URR], om = prim[UPP];
-    R om_off = om - get_om<R>(P, r);
+    R om_off = om - (get_om<R>(P, r) - omf);
     R vz = prim[UZZ];
     R divV_o_d = (gradr[URR] + gradp[UPP] + gradz[UZZ] + vr / r) / (R)3.0;
     R srr = gradr[URR] - divV_o_d;

@@ -16,9 +16,9 @@ struct Mhd {
 
   // prim2cons, mhd.c:35-69
   template <typename T>
-  DISCO_D static void prim2cons(const DevParams& P, const R* prim, T* cons, R r, R dV) {
+  DISCO_D static void prim2cons(const DevParams& P, const R* prim, T* cons, R r, R dV, R omf = 0) {
     R rho = prim[RHO], Pp = prim[PPP], vr = prim[URR], vp = prim[UPP] * r, vz = prim[UZZ];
-    R om = get_om<R>(P, r);
+    R om = get_om<R>(P, r) - omf;
     R vp_off = vp - om * r;
     R Br = prim[BRR], Bp = prim[BPP], Bz = prim[BZZ];
     R v2 = vr * vr + vp_off * vp_off + vz * vz;
@@ -37,14 +37,17 @@ struct Mhd {
   }
 
   // cons2prim, mhd.c:138-185 (FP64 conserved in, R primitives out)
+  // Mixed path: prim[UPP] relative to the ring frame Om (Lsh = Om r^2), as
+  // in the hydro module.
   DISCO_D static int cons2prim(const DevParams& P, const DevPlanet* pl, const double* cons, R* prim,
-                               R r, R phi, R dV) {
+                               R r, R phi, R dV, double Lsh = 0, R Om = 0) {
     int hits = 0;
     R rho, Sr, Sp, Sz, E, Br, Bp, Bz;
     R rr = (R)r;
     if (sizeof(R) < sizeof(double)) {   // mixed path: one reciprocal, FP32 products
       R idV = (R)1 / (R)dV;
-      rho = (R)cons[DDD] * idV; Sr = (R)cons[SRR] * idV; Sp = (R)cons[LLL] * idV / rr;
+      rho = (R)cons[DDD] * idV; Sr = (R)cons[SRR] * idV;
+      Sp = (R)(cons[LLL] - cons[DDD] * Lsh) * idV / rr;
       Sz = (R)cons[SZZ] * idV; E = (R)cons[TAU] * idV;
       Br = (R)cons[BRR] * idV * rr; Bp = (R)cons[BPP] * idV * rr; Bz = (R)cons[BZZ] * idV;
     } else {
@@ -52,9 +55,12 @@ struct Mhd {
       Sz = (R)(cons[SZZ] / dV); E = (R)(cons[TAU] / dV);
       Br = (R)(cons[BRR] / (dV * (1.0 / r))); Bp = (R)(cons[BPP] / dV * r); Bz = (R)(cons[BZZ] / dV);
     }
+    R rho0 = rho;
     if (rho < (R)P.rho_floor) { rho = (R)P.rho_floor; hits |= 1; }
     R om = get_om<R>(P, rr);
-    R vr = Sr / rho, vp = Sp / rho, vp_off = vp - om * rr, vz = Sz / rho;
+    R vr = Sr / rho, vp = Sp / rho, vz = Sz / rho;   // vp relative to the frame
+    if (rho != rho0) vp += Om * rr * (rho0 / rho - (R)1);
+    R vp_off = vp + (Om - om) * rr;
     R B2 = Br * Br + Bp * Bp + Bz * Bz;
     R KE = (R).5 * (Sr * vr + rho * vp_off * vp_off + Sz * vz);
     R rhoe = E - KE - (R).5 * B2;
@@ -73,7 +79,9 @@ struct Mhd {
   }
 
   // flux, mhd.c:187-223
-  DISCO_D static void flux(const DevParams& P, const R* prim, R* f, R r, const R* n) {
+  // (omf is accepted for the common hook signature: this flux has no energy frame)
+  DISCO_D static void flux(const DevParams& P, const R* prim, R* f, R r, const R* n, R omf = 0) {
+    (void)omf;
     R rho = prim[RHO], Pp = prim[PPP], vr = prim[URR], vp = prim[UPP] * r, vz = prim[UZZ];
     R Br = prim[BRR], Bp = prim[BPP], Bz = prim[BZZ];
     R vn = vr * n[0] + vp * n[1] + vz * n[2];
@@ -121,7 +129,7 @@ struct Mhd {
 
   // mhd.c defines neither visc_flux nor visc_source with content.
   DISCO_D static void visc_flux(const DevParams&, const DevPlanet*, const R*, const R*, const R*,
-                                const R*, R*, R, R, const R*) {}
+                                const R*, R*, R, R, const R*, R = 0) {}
   DISCO_D static void visc_source(const DevParams&, const DevPlanet*, const R*, const R*, const R*,
                                   const R*, double*, const double*, const double*, double) {}
 
@@ -142,7 +150,7 @@ struct Mhd {
   // (configurations select HLLD, Riemann_Solver 2); rejected at set-up.
   DISCO_D static void vel(const DevParams&, const R*, const R*, R* Sl, R* Sr, R* Ss, const R*, R,
                           R*) { *Sl = -1; *Sr = 1; *Ss = 0; }
-  DISCO_D static void getUstar(const DevParams&, const R*, R* U, R, R, R, const R*, const R*) {
+  DISCO_D static void getUstar(const DevParams&, const R*, R* U, R, R, R, const R*, const R*, R = 0) {
 #pragma unroll
     for (int q = 0; q < NQ; ++q) U[q] = 0;
   }

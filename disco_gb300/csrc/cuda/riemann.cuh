@@ -11,7 +11,7 @@ template <typename Phys, typename R, int NQ>
 DISCO_D void solve_riemann(const DevParams& P, const DevPlanet* pl, const R* primL, const R* primR,
                            const R* gLr, const R* gLp, const R* gLz, const R* gRr, const R* gRp,
                            const R* gRz, R r, R phi, const R* n, R w, R* Fw, R* Flux_out,
-                           R* Ustr_out) {
+                           R* Ustr_out, R omf = 0) {
   R Flux[NQ], Ustr[NQ];
 #pragma unroll
   for (int q = 0; q < NQ; ++q) { Flux[q] = 0; Ustr[q] = 0; }
@@ -22,19 +22,19 @@ DISCO_D void solve_riemann(const DevParams& P, const DevPlanet* pl, const R* pri
     R Bpack[5];
     Phys::vel(P, primL, primR, &Sl, &Sr, &Ss, n, r, Bpack);
     if (w < Sl) {
-      Phys::flux(P, primL, Flux, r, n);
-      Phys::template prim2cons<R>(P, primL, Ustr, r, (R)1.0);
+      Phys::flux(P, primL, Flux, r, n, omf);
+      Phys::template prim2cons<R>(P, primL, Ustr, r, (R)1.0, omf);
     } else if (w > Sr) {
-      Phys::flux(P, primR, Flux, r, n);
-      Phys::template prim2cons<R>(P, primR, Ustr, r, (R)1.0);
+      Phys::flux(P, primR, Flux, r, n, omf);
+      Phys::template prim2cons<R>(P, primR, Ustr, r, (R)1.0, omf);
     } else {
       if (P.riemann_solver == SOLVER_HLL || (r < (R)0.1 && P.riemann_solver == SOLVER_HLLC_DAMP)) {
         R Fl[NQ], Fr[NQ], Ul[NQ], Ur[NQ];
         R aL = Sr, aR = -Sl;
-        Phys::template prim2cons<R>(P, primL, Ul, r, (R)1.0);
-        Phys::template prim2cons<R>(P, primR, Ur, r, (R)1.0);
-        Phys::flux(P, primL, Fl, r, n);
-        Phys::flux(P, primR, Fr, r, n);
+        Phys::template prim2cons<R>(P, primL, Ul, r, (R)1.0, omf);
+        Phys::template prim2cons<R>(P, primR, Ur, r, (R)1.0, omf);
+        Phys::flux(P, primL, Fl, r, n, omf);
+        Phys::flux(P, primR, Fr, r, n, omf);
 #pragma unroll
         for (int q = 0; q < NQ; ++q) {
           Flux[q] = (aL * Fl[q] + aR * Fr[q] + aL * aR * (Ul[q] - Ur[q])) / (aL + aR);
@@ -43,15 +43,15 @@ DISCO_D void solve_riemann(const DevParams& P, const DevPlanet* pl, const R* pri
       } else {
         R Uk[NQ], Fk[NQ];
         if (w < Ss) {
-          Phys::template prim2cons<R>(P, primL, Uk, r, (R)1.0);
-          Phys::getUstar(P, primL, Ustr, r, Sl, Ss, n, Bpack);
-          Phys::flux(P, primL, Fk, r, n);
+          Phys::template prim2cons<R>(P, primL, Uk, r, (R)1.0, omf);
+          Phys::getUstar(P, primL, Ustr, r, Sl, Ss, n, Bpack, omf);
+          Phys::flux(P, primL, Fk, r, n, omf);
 #pragma unroll
           for (int q = 0; q < NQ; ++q) Flux[q] = Fk[q] + Sl * (Ustr[q] - Uk[q]);
         } else {
-          Phys::template prim2cons<R>(P, primR, Uk, r, (R)1.0);
-          Phys::getUstar(P, primR, Ustr, r, Sr, Ss, n, Bpack);
-          Phys::flux(P, primR, Fk, r, n);
+          Phys::template prim2cons<R>(P, primR, Uk, r, (R)1.0, omf);
+          Phys::getUstar(P, primR, Ustr, r, Sr, Ss, n, Bpack, omf);
+          Phys::flux(P, primR, Fk, r, n, omf);
 #pragma unroll
           for (int q = 0; q < NQ; ++q) Flux[q] = Fk[q] + Sr * (Ustr[q] - Uk[q]);
         }
@@ -71,7 +71,7 @@ DISCO_D void solve_riemann(const DevParams& P, const DevPlanet* pl, const R* pri
       gz[q] = (R).5 * (gLz[q] + gRz[q]);
       vFlux[q] = 0.0;
     }
-    Phys::visc_flux(P, pl, prim, gr, gp, gz, vFlux, r, phi, n);
+    Phys::visc_flux(P, pl, prim, gr, gp, gz, vFlux, r, phi, n, omf);
 #pragma unroll
     for (int q = 0; q < NQ; ++q) Flux[q] += vFlux[q];
   }
