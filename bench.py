@@ -38,6 +38,13 @@ WORKLOADS = {
                    # bounded CPU samples: same physics at reduced resolution
                    "cpu_sample": {"Num_R": 64, "Num_Z": 16},
                    "ref_sample": {"Num_R": 32, "Num_Z": 8}},
+    # the same disk at 64 x 16 rings (1.4 M cells, 0.4 GB of state, still
+    # larger than L2): the small case for full ncu captures
+    "mhd_disk3d_small": {"dir": "configs/cfg2_mhd_disk",
+                         "desc": "3D Newtonian MHD Keplerian disk at Nr=64 x Nz=16 (profiling case)",
+                         "overrides": {"Num_R": 64, "Num_Z": 16},
+                         "cpu_sample": {"Num_R": 32, "Num_Z": 8},
+                         "ref_sample": {"Num_R": 32, "Num_Z": 8}},
     "vortex2d": {"dir": "configs/cfg1_vortex",
                  "desc": "2D cylindrical Newtonian hydro, Gaussian isentropic vortex, "
                          "Nr=128 on r in [0.5,3], HLLC, PLM 1.5, RK2, CFL 0.5",
@@ -175,7 +182,7 @@ def measure_ours(args, wl, rank):
     res = {}
     doms = {}
     for prec in (1, 0):
-        d = dg.Domain(par, mk, precision=prec)
+        d = dg.Domain(par, mk, precision=prec, overrides=wl.get("overrides"))
         doms[prec] = d
         cells = d.num_real_cells
         N = d.num_cells
@@ -371,7 +378,10 @@ def main():
     import disco_gb300 as dg  # noqa: F401
     from disco_gb300.api import Domain  # noqa: F401
     nf = {"r": 0, "z": 0}
-    hd = dg.HostDomain(dg.read_params(os.path.join(ROOT, wl["dir"], "in.par")),
+    hp = dg.read_params(os.path.join(ROOT, wl["dir"], "in.par"))
+    for k, v in (wl.get("overrides") or {}).items():
+        setattr(hp, k, v)
+    hd = dg.HostDomain(hp,
                        dg.read_modules(os.path.join(ROOT, wl["dir"], "Makefile_opt.in")))
     Np = hd.Np.reshape(hd.Nz, hd.Nr)
     if hd.Nr > 1:
