@@ -105,7 +105,7 @@ class DiscoGpuErrs(C.Structure):
                 ("steps", C.c_longlong)]
 
 
-# Every symbol include/disco_gpu.h declares, with its ctypes signature.
+# Every symbol include/*.h declares, with its ctypes signature.
 _P = C.c_void_p
 SIGNATURES = {
     "disco_params_read": (C.c_int, [C.c_char_p, C.POINTER(DiscoParams)]),
@@ -125,6 +125,7 @@ SIGNATURES = {
                                     C.POINTER(C.c_int)]),
     "disco_gpu_debug_ct": (C.c_int, [_P, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double),
                                      C.POINTER(C.c_double), C.POINTER(C.c_double)]),
+    "disco_gpu_getmindt_noalloc": (C.c_int, [_P, C.POINTER(C.c_double)]),
     "disco_gpu_time": (C.c_double, [_P]),
     "disco_gpu_num_cells": (C.c_long, [_P]),
     "disco_gpu_num_real_cells": (C.c_long, [_P]),
@@ -230,6 +231,12 @@ class Domain:
     def getmindt(self) -> float:
         dt = C.c_double()
         _check(lib().disco_gpu_getmindt(self._g, C.byref(dt)), "disco_gpu_getmindt")
+        return dt.value
+
+    def getmindt_noalloc(self) -> float:
+        """getmindt through the no-allocation entry point (static scratch)."""
+        dt = C.c_double()
+        _check(lib().disco_gpu_getmindt_noalloc(self._g, C.byref(dt)), "disco_gpu_getmindt_noalloc")
         return dt.value
 
     def timestep(self, dt: float) -> None:

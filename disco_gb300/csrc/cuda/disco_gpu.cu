@@ -2,6 +2,7 @@
 // instances live in disco_gpu_euler.cu / disco_gpu_mhd.cu.
 #include "instance.cuh"
 #include "disco_gpu_debug.h"
+#include "disco_gpu_noalloc.h"
 
 std::atomic<long long> g_launches{0};
 long long disco_gpu_launch_count(void) { return g_launches.load(); }
@@ -75,6 +76,10 @@ int disco_gpu_status(disco_gpu* g, disco_gpu_errs* e) {
 int disco_gpu_debug_ct(disco_gpu* g, int stage, double* E, double* B, double* Ephi, double* Phi) {
   if (!g || stage < 0 || stage > 4) { disco_set_error("bad argument"); return DISCO_E_ARG; }
   return g->impl->debug_ct(stage, E, B, Ephi, Phi);
+}
+int disco_gpu_getmindt_noalloc(disco_gpu* g, double* dt) {
+  if (!g || !dt) { disco_set_error("null argument"); return DISCO_E_ARG; }
+  return g->impl->getmindt_noalloc(dt);
 }
 double disco_gpu_time(disco_gpu* g) { return g ? g->impl->time() : 0.0; }
 long disco_gpu_num_cells(disco_gpu* g) { return g ? g->impl->N : 0; }

@@ -15,6 +15,7 @@
 #include "../host/disco_host_internal.h"
 #include "kernels.cuh"
 #include "ct_kernels.cuh"
+#include "noalloc.cuh"
 
 using namespace disco;
 
@@ -46,6 +47,7 @@ struct InstanceBase {
   virtual int profile(int n, disco_kernel_time* out, int maxo, int* nout) = 0;
   virtual double time() = 0;
   virtual int debug_ct(int stage, double* E, double* B, double* Ephi, double* Phi) = 0;
+  virtual int getmindt_noalloc(double* dt) = 0;
   long N = 0, Nreal = 0;
 };
 
@@ -683,6 +685,29 @@ struct Instance : InstanceBase {
     return 0;
   }
   double time() override { return host_t; }
+
+  // CFL dt with partial minima in the library's static scratch array: no
+  // device allocation, no write to the instance (disco_gpu_noalloc.h).
+  int getmindt_noalloc(double* dt) override {
+    long nb = blocks(N, kNoallocBlock);
+    if (N > DISCO_NOALLOC_MAX_CELLS || nb > kNoallocMaxBlocks) {
+      disco_set_error("getmindt_noalloc: instance larger than the static scratch (DISCO_NOALLOC_MAX_CELLS)");
+      return DISCO_E_ARG;
+    }
+    int dev = 0;
+    CK(cudaGetDevice(&dev));
+    unsigned long long* part = noalloc_scratch(dev);
+    if (!part) { disco_set_error("getmindt_noalloc: scratch symbol not available"); return DISCO_E_CUDA; }
+    DevParams Pn = P;
+    Pn.t_end = 0.0;
+    k_mindt_blocks<Phys, R, NQ><<<(int)nb, kNoallocBlock, 0, st>>>(Pn, S, part);
+    k_mindt_final<<<1, 1024, 0, st>>>(Pn, part, (int)nb);
+    g_launches += 2;
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(dt, part + kNoallocMaxBlocks, sizeof(double), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    return 0;
+  }
 };
 
 template <class Phys, typename R, int NQ>
