@@ -160,7 +160,7 @@ def kernel_bytes(name: str, N: int, nf: dict, nq: int, sw: int, ct: bool) -> flo
         return N * (3 * nq * f8 + 2 * nq * sw + 5 * f8 + sw + 8 * ix) + nfa * nq * sw
     if name in ("faces_r", "faces_z"):
         d = name[-1]
-        return N * (2 * f8 + 4 * ix) + nf[d] * (2 * ix + 1 + f8 + 3 * sw + c * (f8 + 4 * sw))
+        return N * (2 * f8 + 4 * ix) + nf[d] * (2 * ix + 1 + f8 + 3 * sw + c * 4 * sw)
     if name == "mindt":
         return N * (nq * sw + 2 * f8 + sw)
     if name in ("wcell_ring", "wcell", "wcell_avg"):

@@ -28,11 +28,15 @@ CC_FLAGS = ["-std=gnu11", "-O2", "-fPIC", "-Wall", "-ffp-contract=off"]
 HOST_SOURCES = ["host/disco_host.c"]
 # (source, extra nvcc flags): the plain-FP64 instances are compiled without
 # FMA contraction so their FP64 arithmetic rounds like the reference's C build.
+# FP64 path: no FMA contraction (it must round like the reference build).
+# Mixed path: FP32 division and square root need not be correctly rounded
+# (they only touch FP32 values; FP64 arithmetic is unaffected).
+F32_FLAGS = ["-prec-div=false", "-prec-sqrt=false"]
 CUDA_SOURCES = [("cuda/disco_gpu.cu", []),
                 ("cuda/inst_euler_f64.cu", ["--fmad=false"]),
-                ("cuda/inst_euler_f32.cu", []),
+                ("cuda/inst_euler_f32.cu", F32_FLAGS),
                 ("cuda/inst_mhd_f64.cu", ["--fmad=false"]),
-                ("cuda/inst_mhd_f32.cu", [])]
+                ("cuda/inst_mhd_f32.cu", F32_FLAGS)]
 
 
 def _nvcc() -> str:

@@ -468,7 +468,7 @@ __global__ void k_ct_edge(DevParams P, DevState<R> S, CtStateT<R> C, double fac)
     }
     double Edldt;
     if constexpr (kMix<R>) {
-      Edldt = (double)(E * (dlfac * wrap_dp<R>((R)(xp1 - xm1), (R)Pmax)));
+      Edldt = (double)(E * (dlfac * (R)get_dp(xp1, xm1, Pmax)));   // wrapped in FP64, then R
     } else {
       double dl = (.5 * (rjj + rjj)) * get_dp(xp1, xm1, Pmax);
       Edldt = (double)E * dl * dt;
@@ -489,31 +489,50 @@ __global__ void k_ct_flip(DevParams P, DevState<R> S, CtStateT<R> C, int dim) {
   int pair = blockIdx.x;
   if (pair == C.last_pair[d]) return;   // the reference loops skip the last pair
   int base = S.face_off[d][pair], Nf = S.face_off[d][pair + 1] - base;
+  // shared: lr[Nf] (int8), then the ascending list of flagged faces (int)
   signed char* lr = (signed char*)fsm;
-  unsigned char* flag = fsm + Nf;
-  for (int n = threadIdx.x; n < Nf; n += blockDim.x) { lr[n] = S.fLR[d][base + n]; flag[n] = 0; }
+  int* list = (int*)(fsm + ((Nf + 15) & ~15));
+  __shared__ int cnt[256];
+  for (int n = threadIdx.x; n < Nf; n += blockDim.x) lr[n] = S.fLR[d][base + n];
   __syncthreads();
-  __shared__ int nflag;
-  if (threadIdx.x == 0) nflag = 0;
-  __syncthreads();
-  for (int n = threadIdx.x; n < Nf; n += blockDim.x) {
-    int f = base + n, np = n + 1 == Nf ? 0 : n + 1, fp = base + np;
+  // each thread flags a contiguous chunk, so a prefix over the per-thread
+  // counts lists the flagged faces in ascending order
+  const int chunk = (Nf + blockDim.x - 1) / blockDim.x;
+  const int n0 = threadIdx.x * chunk, n1 = min(Nf, n0 + chunk);
+  unsigned long long bits = 0;   // chunk <= 64 (Nf <= 16384)
+  int mine = 0;
+  for (int n = n0; n < n1; ++n) {
+    int np = n + 1 == Nf ? 0 : n + 1;   // face np is flagged when its end edge precedes face n's
+    int f = base + n, fp = base + np;
     double pm = lr[n] == 0 ? S.piph[S.fL[d][f]] : S.piph[S.fR[d][f]];
     double pp = lr[np] == 0 ? S.piph[S.fL[d][fp]] : S.piph[S.fR[d][fp]];
-    if (get_signed_dp(pp, pm, P.phi_max) < 0.) { flag[np] = 1; atomicAdd(&nflag, 1); }
+    if (get_signed_dp(pp, pm, P.phi_max) < 0.) { bits |= 1ull << (n - n0); ++mine; }
+  }
+  cnt[threadIdx.x] = mine;
+  __syncthreads();
+  if (threadIdx.x == 0) {   // exclusive scan of 256 counts (cheap, one thread)
+    int acc = 0;
+    for (int t = 0; t < (int)blockDim.x; ++t) { int v = cnt[t]; cnt[t] = acc; acc += v; }
+    list[Nf] = acc;
   }
   __syncthreads();
+  {
+    int w = cnt[threadIdx.x];
+    for (int n = n0; n < n1; ++n)
+      if (bits >> (n - n0) & 1ull) list[w++] = n + 1 == Nf ? 0 : n + 1;
+  }
+  __syncthreads();
+  int nflag = list[Nf];
   if (threadIdx.x != 0 || nflag == 0) return;
+  // flip_fluxes in ascending face order (the list holds n + 1 for each n;
+  // the wrap-around face 0 comes from the last chunk, so visit it first)
   const int N = S.N;
   int lo = d == 0 ? 2 : 4, hi = d == 0 ? 1 : 3;
   auto slot = [&](int n) -> long long {
     int f = base + n;
     return lr[n] == 0 ? (long long)lo * N + S.fL[d][f] : (long long)hi * N + S.fR[d][f];
   };
-  bool any = false;
-  for (int n = 0; n < Nf; ++n) {
-    if (!flag[n]) continue;
-    any = true;
+  auto repair = [&](int n) {
     int np = n + 1 == Nf ? 0 : n + 1, nm = n == 0 ? Nf - 1 : n - 1;
     long long s = slot(n), sm_ = slot(nm), sp = slot(np);
     double Phi = C.Phi[s], RPhi = C.RKPhi[s];
@@ -522,9 +541,11 @@ __global__ void k_ct_flip(DevParams P, DevState<R> S, CtStateT<R> C, int dim) {
     C.Phi[sp] = C.Phi[sp] + Phi; C.RKPhi[sp] = C.RKPhi[sp] + RPhi;
     lr[n] = !lr[n];
     lr[nm] = !lr[nm];
-  }
-  if (any)
-    for (int n = 0; n < Nf; ++n) S.fLR[d][base + n] = lr[n];
+  };
+  if (list[nflag - 1] == 0) repair(0);
+  for (int t = 0; t < nflag; ++t)
+    if (list[t] != 0) repair(list[t]);
+  for (int n = 0; n < Nf; ++n) S.fLR[d][base + n] = lr[n];
 }
 
 // ---- B_faces_to_cells type 1 (bfields.c:88-309): cell B from face fluxes ---------

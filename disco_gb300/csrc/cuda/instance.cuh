@@ -124,6 +124,8 @@ struct Instance : InstanceBase {
   }
 
   int blocks(long n, int b = 256) const { return (int)((n + b - 1) / b); }
+  // k_ct_flip: LRtype bytes (padded to 16) + the flagged-face list (Nf + 1 ints)
+  size_t flip_smem(int d) const { return (size_t)((maxNf[d] + 15) & ~15) + 4 * ((size_t)maxNf[d] + 1); }
 
   void set_piph(int par) {
     S.piph = piph_buf[par];
@@ -267,7 +269,7 @@ struct Instance : InstanceBase {
       A(&S.fflux[d], (size_t)NQ * nf);
       A(&S.run_up_s[d], N); A(&S.run_up_e[d], N); A(&S.run_dn_s[d], N); A(&S.run_dn_e[d], N);
       if (ct) {
-        A(&S.fdphi[d], nf); A(&S.fErz[d], nf); A(&S.fBrz[d], nf); A(&S.fEphi[d], nf);
+        A(&S.fErz[d], nf); A(&S.fBrz[d], nf); A(&S.fEphi[d], nf);
         A(&S.ffrL[d], nf); A(&S.ffrR[d], nf); A(&S.fdp1[d], nf); A(&S.fdp2[d], nf);
       }
       C.last_pair[d] = np - 1;
@@ -284,6 +286,13 @@ struct Instance : InstanceBase {
       CK(cudaMemset(S.Eraw, 0, sizeof(R) * 8 * N)); CK(cudaMemset(S.Braw, 0, sizeof(R) * 8 * N));
       CK(cudaMemset(C.Phi, 0, sizeof(double) * 5 * N)); CK(cudaMemset(C.RKPhi, 0, sizeof(double) * 5 * N));
       CK(cudaMemset(C.Ephi, 0, sizeof(R) * 4 * N)); CK(cudaMemset(C.errs, 0, 8));
+      if (std::max(maxNf[0], maxNf[1]) > 64 * 256) {
+        disco_set_error("CT flip repair handles at most 16384 faces per ring pair");
+        return DISCO_E_ARG;
+      }
+      for (int d = 0; d < 2; ++d)
+        if (flip_smem(d) > 48 * 1024)
+          CK(cudaFuncSetAttribute(k_ct_flip<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)flip_smem(d)));
       edge_smem = (size_t)4 * maxring * 8;
       if (edge_smem > 48 * 1024)
         CK(cudaFuncSetAttribute(k_ct_edge<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)edge_smem));
@@ -412,8 +421,8 @@ struct Instance : InstanceBase {
   void substep(double RK, double fac, int first) {
     if (first) launch_wcell();
     LAUNCH("plm_phi", (k_plm_phi<R, NQ><<<blocks(N), 256, 0, st>>>(P, S)));
-    if (Nr > 1) LAUNCH("plm_trans_r", (k_plm_trans<R, NQ><<<blocks(N), 256, 0, st>>>(P, S, 1)));
-    if (Nz > 1) LAUNCH("plm_trans_z", (k_plm_trans<R, NQ><<<blocks(N), 256, 0, st>>>(P, S, 2)));
+    if (Nr > 1) LAUNCH("plm_trans_r", (k_plm_trans<R, NQ><<<dim3(blocks(N), plm_groups<NQ>()), 256, 0, st>>>(P, S, 1)));
+    if (Nz > 1) LAUNCH("plm_trans_z", (k_plm_trans<R, NQ><<<dim3(blocks(N), plm_groups<NQ>()), 256, 0, st>>>(P, S, 2)));
     LAUNCH("flux_phi", (k_flux_phi<Phys, R, NQ><<<blocks(N), 256, 0, st>>>(P, S, fac)));
     launch_trans_fluxes(fac);
     if (ct) {   // avg_Efields, subtract_advective_B_fluxes, update_B_fluxes (onestep.c:261-265)
@@ -432,7 +441,7 @@ struct Instance : InstanceBase {
     if (ct) {   // flips (first substep), B_faces_to_cells, calc_prim (onestep.c:270-296)
       if (first)
         for (int d = 0; d < 2; ++d)
-          if (npair[d]) LAUNCH("ct_flip", (k_ct_flip<R><<<npair[d], 256, 2 * maxNf[d] + 16, st>>>(P, S, C, d + 1)));
+          if (npair[d]) LAUNCH("ct_flip", (k_ct_flip<R><<<npair[d], 256, flip_smem(d), st>>>(P, S, C, d + 1)));
       LAUNCH("ct_b2c", (k_ct_b2c<R, NQ><<<blocks(N), 256, 0, st>>>(P, S, C, 0)));
       LAUNCH("c2p", (k_c2p<Phys, R, NQ><<<blocks(N), 256, 0, st>>>(P, S)));
     }
@@ -591,8 +600,8 @@ struct Instance : InstanceBase {
     const int first = 1;
     launch_wcell();
     LAUNCH("plm_phi", (k_plm_phi<R, NQ><<<blocks(N), 256, 0, st>>>(P, S)));
-    if (Nr > 1) LAUNCH("plm_trans_r", (k_plm_trans<R, NQ><<<blocks(N), 256, 0, st>>>(P, S, 1)));
-    if (Nz > 1) LAUNCH("plm_trans_z", (k_plm_trans<R, NQ><<<blocks(N), 256, 0, st>>>(P, S, 2)));
+    if (Nr > 1) LAUNCH("plm_trans_r", (k_plm_trans<R, NQ><<<dim3(blocks(N), plm_groups<NQ>()), 256, 0, st>>>(P, S, 1)));
+    if (Nz > 1) LAUNCH("plm_trans_z", (k_plm_trans<R, NQ><<<dim3(blocks(N), plm_groups<NQ>()), 256, 0, st>>>(P, S, 2)));
     LAUNCH("flux_phi", (k_flux_phi<Phys, R, NQ><<<blocks(N), 256, 0, st>>>(P, S, fac)));
     if (stage >= 1) {
       launch_trans_fluxes(fac);

@@ -89,7 +89,6 @@ struct DevState {
   int ct;
   R* Eraw;                     // [8*N] E[8] of the reference cell
   R* Braw;                     // [8*N] B[8]
-  double* fdphi[2];            // face dphi (FP64, CT initial fluxes)
   R* fErz[2];                  // per face flux_to_E outputs
   R* fBrz[2];
   R* fEphi[2];
@@ -466,42 +465,61 @@ __global__ void k_faces(DevParams P, DevState<R> S, int dim) {
     int iL = offL + tL;
     int iR = offR + tR;
     double pL = phi_unkey(sL[am]), pR = phi_unkey(sR[bm]);
-    double dL = S.dphi[iL], dR = S.dphi[iR];
-    // LRtype and the face's lower edge: the reference's FP64 comparisons
-    double dphi = pL - pR;
-    while (dphi > .5 * Pmax) dphi -= Pmax;
-    while (dphi < -.5 * Pmax) dphi += Pmax;
-    int LR = dphi > 0. ? 1 : 0;
-    dphi = pL - dL - pR + dR;
-    while (dphi > .5 * Pmax) dphi -= Pmax;
-    while (dphi < -.5 * Pmax) dphi += Pmax;
-    int LR_back = dphi < 0. ? 1 : 0;
-    double xp1 = LR == 0 ? pL : pR;
-    double xm1 = LR_back == 0 ? pL - dL : pR - dR;
-    // addFace, faces_alt.c:10-34
-    double dp = get_dp(xp1, xm1, Pmax);
-    double phic = get_dp(xp1, .5 * dp, Pmax);
     int gf = base + n;
     S.fL[d][gf] = iL;
     S.fR[d][gf] = iR;
-    S.fLR[d][gf] = (signed char)LR;
-    S.fphic[d][gf] = phic;
+    int LR;
     if constexpr (kMix<R>) {
-      // offsets from FP64 differences of nearby positions, the rest in R
+      // LRtype from the merge order itself (the face ends at whichever upper
+      // edge comes first; ties advance L); every offset relative to pL in R
+      // from the single FP64 difference pR - pL.
+      int la, lb; long long ka, kb;
+      keyL(a, la, ka);
+      keyR(b, lb, kb);
+      LR = ((la < lb) || (la == lb && ka <= kb)) ? 0 : 1;
       const R Pm = (R)Pmax;
-      R dpr = (R)dp, dLr = S.dphi_r[iL], dRr = S.dphi_r[iR];
+      R dLr = S.dphi_r[iL], dRr = S.dphi_r[iR];
+      // wrapped in FP64 first: across phi = 0 the raw difference is ~2 pi,
+      // where an FP32 rounding would be as large as a sliver face
+      R dLR = (R)get_signed_dp(pR, pL, Pmax);
+      int LR_back = wrap_signed<R>(dRr - dLr - dLR, Pm) < (R)0 ? 1 : 0;
+      R xp = LR == 0 ? (R)0 : dLR;                  // upper edge - pL
+      R xm = LR_back == 0 ? -dLr : dLR - dRr;      // lower edge - pL
+      R dpr = wrap_dp<R>(xp - xm, Pm);
+      R pc = xp - (R).5 * dpr;                     // face centre - pL
+      double phic = pL + (double)pc;
+      while (phic < 0.0) phic += Pmax;
+      while (phic > Pmax) phic -= Pmax;
+      S.fLR[d][gf] = (signed char)LR;
+      S.fphic[d][gf] = phic;
       S.fdA[d][gf] = S.pdA[d][pair] * dpr;
-      S.fdpL[d][gf] = wrap_signed<R>((R)(phic - pL) + (R).5 * dLr, Pm);
-      S.fdpR[d][gf] = wrap_signed<R>((R)(pR - phic) - (R).5 * dRr, Pm);
+      S.fdpL[d][gf] = wrap_signed<R>(pc + (R).5 * dLr, Pm);
+      S.fdpR[d][gf] = wrap_signed<R>(dLR - pc - (R).5 * dRr, Pm);
       if (S.ct) {
-        S.fdphi[d][gf] = dp;
         S.ffrL[d][gf] = dpr / dLr;
         S.ffrR[d][gf] = dpr / dRr;
-        R dp1 = wrap_dp<R>(LR == 0 ? (R)(pR - pL) : (R)(pL - pR), Pm);
+        R dp1 = wrap_dp<R>(LR == 0 ? dLR : -dLR, Pm);
         S.fdp1[d][gf] = dp1;
         S.fdp2[d][gf] = (LR == 0 ? dRr : dLr) - dp1;
       }
     } else {
+      double dL = S.dphi[iL], dR = S.dphi[iR];
+      // LRtype and the face's lower edge: the reference's FP64 comparisons
+      double dphi = pL - pR;
+      while (dphi > .5 * Pmax) dphi -= Pmax;
+      while (dphi < -.5 * Pmax) dphi += Pmax;
+      LR = dphi > 0. ? 1 : 0;
+      dphi = pL - dL - pR + dR;
+      while (dphi > .5 * Pmax) dphi -= Pmax;
+      while (dphi < -.5 * Pmax) dphi += Pmax;
+      int LR_back = dphi < 0. ? 1 : 0;
+      double xp1 = LR == 0 ? pL : pR;
+      double xm1 = LR_back == 0 ? pL - dL : pR - dR;
+      // addFace, faces_alt.c:10-34
+      double dp = get_dp(xp1, xm1, Pmax);
+      double phic = get_dp(xp1, .5 * dp, Pmax);
+      S.fLR[d][gf] = (signed char)LR;
+      S.fphic[d][gf] = phic;
       double dA;
       if (dim == 1) dA = (.5 * (rj[j] + rj[j])) * dp * (zk[k] - zk[k - 1]);
       else dA = (.5 * (rj[j] + rj[j - 1])) * (rj[j] - rj[j - 1]) * dp;
@@ -510,7 +528,6 @@ __global__ void k_faces(DevParams P, DevState<R> S, int dim) {
       S.fdpL[d][gf] = (R)get_signed_dp(phic, pL - .5 * dL, Pmax);
       S.fdpR[d][gf] = (R)get_signed_dp(pR - .5 * dR, phic, Pmax);
       if (S.ct) {
-        S.fdphi[d][gf] = dp;
         S.ffrL[d][gf] = (R)(dp / dL);   // riemann.c:172-173
         S.ffrR[d][gf] = (R)(dp / dR);
         // avg_Efields weights (bfields.c:461-465): c1 owns the face's end edge
@@ -649,54 +666,63 @@ __global__ void k_pair_geom(DevParams P, DevState<R> S, int dim, int npair) {
 // reference limiter loop (plm.c:146-179) reduces to: zero if any face slope
 // has the opposite sign (or is zero), else the smallest of |g| and |PLM S|,
 // which is independent of face order; it is evaluated in one pass here.
+// The components are independent: blockIdx.y selects a group of QPT of them,
+// so a cell's work is spread over several threads with fewer registers each.
+constexpr int kPlmQ = 5;   // components per thread in k_plm_trans
+template <int NQ>
+constexpr int plm_groups() { return (NQ + kPlmQ - 1) / kPlmQ; }
+
 template <typename R, int NQ>
 __global__ void k_plm_trans(DevParams P, DevState<R> S, int dim) {
   int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= S.N) return;
+  constexpr int QPT = kPlmQ;
+  const int q0 = blockIdx.y * QPT;
   const int d = dim - 1;
   const int N = S.N;
   int jk = S.cell_ring[c];
   int j = jk % P.Nr, k = jk / P.Nr;
   R* grad = dim == 1 ? S.gradr : S.gradz;
-  const double Pmax = P.phi_max;
-  (void)Pmax;
   R PLM = (R)P.PLM;
   if (P.PLM == 0.0) {
 #pragma unroll
-    for (int q = 0; q < NQ; ++q) grad[q * N + c] = 0;
+    for (int t = 0; t < QPT; ++t)
+      if (q0 + t < NQ) grad[(q0 + t) * N + c] = 0;
     return;
   }
-  R sum[NQ], minpos[NQ], maxneg[NQ];
+  R sum[QPT], minpos[QPT], maxneg[QPT];
   unsigned anypos = 0, anyneg = 0, anyzero = 0;
+  R pc[QPT], gpc[QPT];
 #pragma unroll
-  for (int q = 0; q < NQ; ++q) { sum[q] = 0; minpos[q] = 0; maxneg[q] = 0; }
-
-  R pc[NQ], gpc[NQ];
-#pragma unroll
-  for (int q = 0; q < NQ; ++q) { pc[q] = S.prim[q * N + c]; gpc[q] = S.gradp[q * N + c]; }
+  for (int t = 0; t < QPT; ++t) {
+    sum[t] = 0; minpos[t] = 0; maxneg[t] = 0; pc[t] = 0; gpc[t] = 0;
+    if (q0 + t < NQ) { pc[t] = S.prim[(q0 + t) * N + c]; gpc[t] = S.gradp[(q0 + t) * N + c]; }
+  }
 
   auto visit = [&](int f, int other, bool self_is_L, R dxsum, R idxsum, R dOm) {
     R dpL = S.fdpL[d][f], dpR = S.fdpR[d][f];
     R dA = S.fdA[d][f];
 #pragma unroll
-    for (int q = 0; q < NQ; ++q) {
+    for (int t = 0; t < QPT; ++t) {
+      const int q = q0 + t;
+      if (q >= NQ) break;
       R po = S.prim[q * N + other], gpo = S.gradp[q * N + other];
       R WL, WR;
-      if (self_is_L) { WL = pc[q] + dpL * gpc[q]; WR = po - dpR * gpo; }
-      else { WL = po + dpL * gpo; WR = pc[q] - dpR * gpc[q]; }
+      if (self_is_L) { WL = pc[t] + dpL * gpc[t]; WR = po - dpR * gpo; }
+      else { WL = po + dpL * gpo; WR = pc[t] - dpR * gpc[t]; }
       R Sl;
       if constexpr (kMix<R>) Sl = ((WR - WL) + (q == UPP ? dOm : (R)0)) * idxsum;   // frames of the rings
       else Sl = (WR - WL) / dxsum;
-      sum[q] += Sl * dA;
+      sum[t] += Sl * dA;
       R ps = PLM * Sl;
       if (Sl > (R)0) {
-        if (!(anypos >> q & 1u) || ps < minpos[q]) minpos[q] = ps;
-        anypos |= 1u << q;
+        if (!(anypos >> t & 1u) || ps < minpos[t]) minpos[t] = ps;
+        anypos |= 1u << t;
       } else if (Sl < (R)0) {
-        if (!(anyneg >> q & 1u) || ps > maxneg[q]) maxneg[q] = ps;
-        anyneg |= 1u << q;
+        if (!(anyneg >> t & 1u) || ps > maxneg[t]) maxneg[t] = ps;
+        anyneg |= 1u << t;
       } else {
-        anyzero |= 1u << q;
+        anyzero |= 1u << t;
       }
     }
   };
@@ -724,6 +750,7 @@ __global__ void k_plm_trans(DevParams P, DevState<R> S, int dim) {
     dAt = S.ring_At_r[d][jk] * S.dphi_r[c];
     idAt = (R)1 / dAt;
   } else {
+    const double Pmax = P.phi_max;
     const double* rj = S.r_jph + 1;
     const double* zk = S.z_kph + 1;
     double phip = S.piph[c], phim = phip - S.dphi[c];
@@ -750,20 +777,22 @@ __global__ void k_plm_trans(DevParams P, DevState<R> S, int dim) {
   bool geom_bd = (dim == 1 && j == 0 && P.NgRa == 0);
   R rcen = kMix<R> ? S.ring_rc_r[jk] : (R)S.ring_rc[jk];
 #pragma unroll
-  for (int q = 0; q < NQ; ++q) {
+  for (int t = 0; t < QPT; ++t) {
+    const int q = q0 + t;
+    if (q >= NQ) break;
     R g;
-    if constexpr (kMix<R>) g = sum[q] * idAt;
-    else g = sum[q] / dAt;
+    if constexpr (kMix<R>) g = sum[t] * idAt;
+    else g = sum[t] / dAt;
     if (g > (R)0) {
-      if ((anyneg >> q & 1u) || (anyzero >> q & 1u)) g = 0;
-      else if ((anypos >> q & 1u) && minpos[q] < g) g = minpos[q];
+      if ((anyneg >> t & 1u) || (anyzero >> t & 1u)) g = 0;
+      else if ((anypos >> t & 1u) && minpos[t] < g) g = minpos[t];
     } else if (g < (R)0) {
-      if ((anypos >> q & 1u) || (anyzero >> q & 1u)) g = 0;
-      else if ((anyneg >> q & 1u) && maxneg[q] > g) g = maxneg[q];
+      if ((anypos >> t & 1u) || (anyzero >> t & 1u)) g = 0;
+      else if ((anyneg >> t & 1u) && maxneg[t] > g) g = maxneg[t];
     }
     if (geom_bd) {  // plm_geom_boundary + geom_grad, cylindrical.c:141-173
       if (q == URR || (P.num_c > BZZ && q == BRR)) {
-        R SL = pc[q] / rcen;
+        R SL = pc[t] / rcen;
         if (g * SL < (R)0) g = 0;
         else if (fabs(PLM * SL) < fabs(g)) g = PLM * SL;
       } else {
@@ -962,19 +991,36 @@ __global__ void k_update(DevParams P, DevState<R> S, double RK, double fac, int 
 
   double piph = S.piph[c], dphi = S.dphi[c];
   constexpr bool MIX = kMix<R>;
-  double Ukeep[MIX ? NQ : 1];
+  // move_cells + clean_pi + calc_dp (first substep only): new positions
+  double piph_new = piph, dphi_new = dphi;
+  if (first) {
+    int cm = off + (i == 0 ? Np - 1 : i - 1);
+    double pn = piph + S.wiph[c] * dt;
+    while (pn > Pmax) pn -= Pmax;
+    while (pn < 0.0) pn += Pmax;
+    double pm = S.piph[cm] + S.wiph[cm] * dt;
+    while (pm > Pmax) pm -= Pmax;
+    while (pm < 0.0) pm += Pmax;
+    piph_new = pn;
+    dphi_new = get_dp(pn, pm, Pmax);
+  }
   if (real) {
     double U[NQ];
+    // adjust_RK_cons: before the flux terms on the FP64 path (they are added
+    // to U in order); after the R sums on the mixed path (shorter live range)
+    auto load_rk = [&]() {
 #pragma unroll
-    for (int q = 0; q < NQ; ++q) {
-      double u = S.cons[q * N + c];
-      if (first) {
-        S.RKcons[q * N + c] = u;
-      } else {
-        u = (1. - RK) * u + RK * S.RKcons[q * N + c];
+      for (int q = 0; q < NQ; ++q) {
+        double u = S.cons[q * N + c];
+        if (first) {
+          S.RKcons[q * N + c] = u;
+        } else {
+          u = (1. - RK) * u + RK * S.RKcons[q * N + c];
+        }
+        U[q] = u;
       }
-      U[q] = u;
-    }
+    };
+    if constexpr (!MIX) load_rk();
     // Mixed path: fluxes and sources are summed in R (FP32) into dU, and dU
     // is added once to the FP64 conserved state.  The FP64 path adds every
     // term to U directly, in the reference's order.
@@ -1035,6 +1081,7 @@ __global__ void k_update(DevParams P, DevState<R> S, double RK, double fac, int 
           if (S.planets[p].M != 0.0)
             planet_src<R, R>(P, S.planets[p], pr, dU, phc, S.ring_zc_r[jk], dVdt_r, rc, dph);
       }
+      load_rk();
 #pragma unroll
       for (int q = 0; q < NQ; ++q) U[q] += (double)dU[q];
       if (P.include_viscosity || P.rot_flag) {
@@ -1082,36 +1129,37 @@ __global__ void k_update(DevParams P, DevState<R> S, double RK, double fac, int 
 #pragma unroll
     for (int q = 0; q < NQ; ++q) S.cons[q * N + c] = U[q];
     if constexpr (MIX) {
+      if (do_c2p) {   // calc_prim at the post-move geometry, from U in registers
+        R pr2[NQ];
+        R dph = first ? (R)dphi_new : S.dphi_r[c];
+        int hits = Phys::cons2prim(P, S.planets, U, pr2, S.ring_rc_r[jk],
+                                   (R)piph_new - (R).5 * dph, S.ring_vol_r[jk] * dph,
+                                   S.ring_Lsh[jk], S.ring_Om_r[jk]);
+        bool bad = false;
 #pragma unroll
-      for (int q = 0; q < NQ; ++q) Ukeep[q] = U[q];
+        for (int q = 0; q < NQ; ++q) {
+          S.prim[q * N + c] = pr2[q];
+          if (!isfinite((double)pr2[q])) bad = true;
+        }
+        if (bad) atomicAdd(&S.errs->nan_cells, 1ull);
+        if (hits & 1) atomicAdd(&S.errs->rho_floor_hits, 1ull);
+        if (hits & 2) atomicAdd(&S.errs->p_floor_hits, 1ull);
+      }
     }
   }
 
-  // move_cells + clean_pi + calc_dp (first substep only)
   if (first) {
-    int cm = off + (i == 0 ? Np - 1 : i - 1);
-    double pn = piph + S.wiph[c] * dt;
-    while (pn > Pmax) pn -= Pmax;
-    while (pn < 0.0) pn += Pmax;
-    double pm = S.piph[cm] + S.wiph[cm] * dt;
-    while (pm > Pmax) pm -= Pmax;
-    while (pm < 0.0) pm += Pmax;
-    piph = pn;
-    dphi = get_dp(pn, pm, Pmax);
+    piph = piph_new;
+    dphi = dphi_new;
     S.piph_out[c] = piph;
     S.dphi[c] = dphi;
     if constexpr (MIX) S.dphi_r[c] = (R)dphi;
   }
 
-  if (real && do_c2p) {  // calc_prim at the post-move geometry
+  if (!MIX && real && do_c2p) {  // calc_prim at the post-move geometry
     R pr[NQ];
     int hits;
-    if constexpr (MIX) {
-      R dph = first ? (R)dphi : S.dphi_r[c];
-      R dV = S.ring_vol_r[jk] * dph;
-      hits = Phys::cons2prim(P, S.planets, Ukeep, pr, S.ring_rc_r[jk], (R)piph - (R).5 * dph, dV,
-                             S.ring_Lsh[jk], S.ring_Om_r[jk]);
-    } else {
+    {
       double rp = rj[j], rm = rj[j - 1], zp = zk[k], zm = zk[k - 1];
       double phim = piph - dphi;
       double xp1 = piph;
