@@ -114,31 +114,77 @@ static double get_dV(const double *xp, const double *xm)
 }
 
 /* ---- omega.c ------------------------------------------------------------ */
-static double get_om(const double *x)
+static double get_om(const double *x)   /* omega.c:76-100 */
 {
+   double O0 = D->par.RotOmega;
+   if(D->par.Energy_Omega == 0) return 0.0 - O0;
    double r = sqrt(x[0]*x[0] + D->par.grav_eps*D->par.grav_eps);
    switch(D->par.Energy_Omega) {
-   case 1: return 1.0 - D->par.RotOmega;
-   case 2: return 1.0/pow(r, 1.5) - D->par.RotOmega;
-   default: return 0.0 - D->par.RotOmega;
+   case 1: return 1.0 - O0;
+   case 2: return 1.0/pow(r, 1.5) - O0;
+   case 3: { double n = 8.0; return 1./pow(pow(r, 1.5*n) + 1., 1./n) - O0; }
+   case 4: return 10.*exp(-.5*r*r) - O0;
+   default: return 0.0 - O0;
    }
 }
-static double get_om1(const double *x)
+static double get_om1(const double *x)  /* omega.c:102-126 */
 {
+   int ch = D->par.Energy_Omega;
+   if(ch == 0 || ch == 1) return 0.0;
    double r = sqrt(x[0]*x[0] + D->par.grav_eps*D->par.grav_eps);
-   if(D->par.Energy_Omega == 2) return -1.5/pow(r, 2.5);
+   if(ch == 2) return -1.5/pow(r, 2.5);
+   if(ch == 3) { double n = 8.0; return -1.5*pow(r, -1 + 1.5*n)/pow(pow(r, 1.5*n) + 1., 1.0 + 1./n); }
+   if(ch == 4) return 10.*r*exp(-.5*r*r);
    return 0.0;
 }
-static double get_cs2(const double *x)
+static double mesh_om(const double *x)  /* omega.c:56-74 */
 {
-   double r = x[0];
-   if(D->par.Cs2_Profile == 1) return 1./(D->par.Disk_Mach*D->par.Disk_Mach);
+   double r = sqrt(x[0]*x[0] + D->par.grav_eps*D->par.grav_eps);
+   if(D->par.Exact_Mesh_Omega == 1) return 1.0;
+   if(D->par.Exact_Mesh_Omega == 2) return pow(r, -1.5);
+   if(D->par.Exact_Mesh_Omega == 3) { double n = 4.0; return 1./pow(pow(r, 1.5*n) + 1., 1./n); }
+   return 0.0;
+}
+static double fgrav(double M, double r, double eps);
+static double phigrav(double M, double r, double eps)
+{
+   double n = 2.0;
+   return M/pow(pow(r, n) + pow(eps, n), 1./n);
+}
+static double get_cs2(const double *x)  /* omega.c:157-209 */
+{
+   double r = x[0], M = D->par.Disk_Mach;
+   if(D->par.Cs2_Profile == 1) return 1./(M*M);
+   if(D->par.Cs2_Profile == 2) { double nu = .5; return .5/M/M/pow(r, 2.*nu); }
+   if(D->par.Cs2_Profile == 3)
+      return D->par.metricPar2*D->par.initPar4*D->par.initPar4/(2*D->par.initPar2*D->par.initPar2*D->par.initPar2);
    if(D->par.Cs2_Profile == 4) {
       r = sqrt(r*r + D->par.grav_eps*D->par.grav_eps);
       double v2 = D->par.metricPar2/r;
-      return v2/(D->par.Disk_Mach*D->par.Disk_Mach);
+      return v2/(M*M);
+   }
+   if(D->par.Cs2_Profile == 5) {
+      double gx = r*cos(x[1]), gy = r*sin(x[1]), phip = 0.0;
+      for(int p = 0; p < D->Npl; p++) {
+         double px = D->pl[p].r*cos(D->pl[p].phi), py = D->pl[p].r*sin(D->pl[p].phi);
+         double pr = (px - gx)*(px - gx) + (py - gy)*(py - gy);
+         phip += phigrav(D->pl[p].M, sqrt(pr), D->pl[p].eps);
+      }
+      return phip/(M*M);
    }
    return 1.0;
+}
+static double get_height_om(const double *x)  /* omega.c:132-155 */
+{
+   double omtot2 = 0.0, r = x[0], phi = x[1];
+   double gx = r*cos(phi), gy = r*sin(phi);
+   for(int p = 0; p < D->Npl; p++) {
+      double px = D->pl[p].r*cos(D->pl[p].phi), py = D->pl[p].r*sin(D->pl[p].phi);
+      double sr = sqrt((px - gx)*(px - gx) + (py - gy)*(py - gy));
+      double f1 = fgrav(D->pl[p].M, sr, D->pl[p].eps);
+      omtot2 += f1/(sr + 0.0625*D->pl[p].eps);
+   }
+   return sqrt(omtot2);
 }
 
 /* ---- planet.c (point masses) ---------------------------------------------- */
@@ -286,6 +332,51 @@ static void e_source(const double *prim, double *cons, const double *xp, const d
    double om = get_om(x), om_r = get_om1(x), om_z = 0.0;
    cons[TAU] += dVdt*rho*(r*vr*om*om - r*r*(omega - om)*(vr*om_r + vz*om_z));
 }
+static double e_visc_nu(const double *prim, const double *x)   /* euler.c:220-226 */
+{
+   double nu = D->par.viscosity;
+   if(D->par.alpha_flag) {
+      double c2 = D->gam*prim[PPP]/prim[RHO];
+      nu = D->par.viscosity*c2/get_height_om(x);
+   }
+   return nu;
+}
+static void e_visc_flux(const double *prim, const double *gr, const double *gp, const double *gz,
+                        double *f, const double *x, const double *n)   /* euler.c:215-256 */
+{
+   double r = x[0], nu = e_visc_nu(prim, x);
+   double rho = prim[RHO], vr = prim[URR], om_off = prim[UPP] - get_om(x), vz = prim[UZZ];
+   double divV_o_d = (gr[URR] + gp[UPP] + gz[UZZ] + vr/r)/3.0;
+   double srr = gr[URR] - divV_o_d;
+   double spp = r*(r*gp[UPP] + vr - r*divV_o_d);
+   double szz = gz[UZZ] - divV_o_d;
+   double srp = 0.5*(r*r*gr[UPP] + gp[URR]);
+   double srz = 0.5*(gr[UZZ] + gz[URR]);
+   double spz = 0.5*(gp[UZZ] + r*r*gz[UPP]);
+   double nc[3] = {n[0], n[1]/r, n[2]};
+   double srn = srr*nc[0] + srp*nc[1] + srz*nc[2];
+   double spn = srp*nc[0] + spp*nc[1] + spz*nc[2];
+   double szn = srz*nc[0] + spz*nc[1] + szz*nc[2];
+   f[SRR] = -2*nu*rho*srn;
+   f[LLL] = -2*nu*rho*spn;
+   f[SZZ] = -2*nu*rho*szn;
+   f[TAU] = -2*nu*rho*(vr*srn + om_off*spn + vz*szn);
+}
+static void e_visc_source(const double *prim, const double *gr, const double *gp, const double *gz,
+                          double *cons, const double *xp, const double *xm, double dVdt)
+{                                                               /* euler.c:258-291 */
+   double x[3];
+   centroid_arr(xp, xm, x);
+   double r = x[0], nu = e_visc_nu(prim, x);
+   double rho = prim[RHO], vr = prim[URR];
+   double divV_o_d = (gr[URR] + gp[UPP] + gz[UZZ] + vr/r)/3.0;
+   double spp = (r*gp[UPP] + vr - r*divV_o_d)/(r*r*r);
+   cons[SRR] += (-2*r*rho*nu*spp)*dVdt;
+   double srp = 0.5*(r*r*gr[UPP] + gp[URR]);
+   double spz = 0.5*(gp[UZZ] + r*r*gz[UPP]);
+   double om_r = get_om1(x), om_z = 0.0;
+   cons[TAU] += (2*rho*nu*(srp*om_r + spz*om_z))*dVdt;
+}
 static double e_mindt(const double *prim, double w, const double *xp, const double *xm)
 {
    double r = centroid(xp[0], xm[0], 1);
@@ -299,6 +390,21 @@ static double e_mindt(const double *prim, double w, const double *xp, const doub
    double dt = dtr;
    if(dt > dtp) dt = dtp;
    if(dt > dtz) dt = dtz;
+   if(D->par.visc_flag) {   /* euler.c:351-373 */
+      double dL0 = get_dL(xp, xm, 0), dL1 = get_dL(xp, xm, 1), dL2 = get_dL(xp, xm, 2);
+      double dx = dL0;
+      if(dx > dL1) dx = dL1;
+      if(dx > dL2) dx = dL2;
+      double nu = D->par.viscosity;
+      if(D->par.alpha_flag) {
+         double x[3];
+         centroid_arr(xp, xm, x);
+         double c2 = D->gam*prim[PPP]/prim[RHO];
+         nu = D->par.viscosity*c2/get_height_om(x);
+      }
+      double dt_visc = 0.5*dx*dx/nu;
+      if(dt > dt_visc) dt = dt_visc;
+   }
    return dt;
 }
 
@@ -623,6 +729,8 @@ static double mindt(const double *p, double w, const double *xp, const double *x
 
 /* ---- riemann.c:216-320 ------------------------------------------------------- */
 static void solve_riemann(const double *primL, const double *primR, double *consL, double *consR,
+                          const double *gLr, const double *gLp, const double *gLz,
+                          const double *gRr, const double *gRp, const double *gRz,
                           const double *x, const double *n, double w, double dAdt, int dim,
                           double *E1, double *B1, double *E2, double *B2)
 {
@@ -665,6 +773,18 @@ static void solve_riemann(const double *primL, const double *primR, double *cons
       }
    } else {
       h_ustar(w, primL, primR, Flux, Ustr, x, n);
+   }
+   if(D->par.visc_flag && !D->mhd) {   /* riemann.c:297-312 (mhd.c has no viscous flux) */
+      double vF[MAXQ], pm[MAXQ], gr[MAXQ], gp[MAXQ], gz[MAXQ];
+      for(q = 0; q < nq; q++) {
+         pm[q] = .5*(primL[q] + primR[q]);
+         gr[q] = .5*(gLr[q] + gRr[q]);
+         gp[q] = .5*(gLp[q] + gRp[q]);
+         gz[q] = .5*(gLz[q] + gRz[q]);
+         vF[q] = 0.0;
+      }
+      e_visc_flux(pm, gr, gp, gz, vF, x, n);
+      for(q = 0; q < nq; q++) Flux[q] += vF[q];
    }
    for(q = 0; q < nq; q++) {
       consL[q] -= (Flux[q] - w*Ustr[q])*dAdt;
@@ -837,17 +957,19 @@ static void plm_trans(int dim)
 /* ---- fluxes: misc.c:378-519, riemann.c:39-214 ------------------------------------- */
 static void riemann_phi(pcell *cL, pcell *cR, double *x, double dAdt)
 {
-   double primL[MAXQ], primR[MAXQ];
+   double primL[MAXQ], primR[MAXQ], gp[MAXQ];
    int q;
    for(q = 0; q < D->nq; q++) {
       primL[q] = cL->prim[q] + .5*cL->gradp[q]*cL->dphi;
       primR[q] = cR->prim[q] - .5*cR->gradp[q]*cR->dphi;
+      gp[q] = (cR->prim[q] - cL->prim[q])/(0.5*(cR->dphi + cL->dphi));
    }
    double n[3] = {0.0, 1.0, 0.0};
    double hn = x[0];
    if(D->mhd) { double Bp = .5*(primL[BPP] + primR[BPP]); primL[BPP] = Bp; primR[BPP] = Bp; }
    double Er = 0, Ez = 0, Br = 0, Bz = 0;
-   solve_riemann(primL, primR, cL->cons, cR->cons, x, n, hn*cL->wiph, dAdt, 0, &Ez, &Br, &Er, &Bz);
+   solve_riemann(primL, primR, cL->cons, cR->cons, cL->gradr, gp, cL->gradz, cR->gradr, gp, cR->gradz,
+                 x, n, hn*cL->wiph, dAdt, 0, &Ez, &Br, &Er, &Bz);
    if(D->mhd && D->ct) {   /* NUM_EDGES == 8 */
       cL->E[0] = .5*Ez; cL->E[1] = .5*Ez; cR->E[2] = .5*Ez; cR->E[3] = .5*Ez;
       cL->B[0] = .5*Br; cL->B[1] = .5*Br; cR->B[2] = .5*Br; cR->B[3] = .5*Br;
@@ -859,7 +981,7 @@ static void riemann_trans(pface *F, double dt, int dim)
 {
    pcell *cL = F->L, *cR = F->R;
    double dAdt = F->dA*dt, phi = F->cm[1];
-   double primL[MAXQ], primR[MAXQ];
+   double primL[MAXQ], primR[MAXQ], grad[MAXQ];
    double phiL = cL->piph - .5*cL->dphi, phiR = cR->piph - .5*cR->dphi;
    double dpL = get_signed_dp(phi, phiL), dpR = get_signed_dp(phiR, phi);
    double *gL = gsel(cL, dim), *gR = gsel(cR, dim);
@@ -867,6 +989,7 @@ static void riemann_trans(pface *F, double dt, int dim)
    for(q = 0; q < D->nq; q++) {
       primL[q] = cL->prim[q] + gL[q]*F->dxL + cL->gradp[q]*dpL;
       primR[q] = cR->prim[q] - gR[q]*F->dxR - cR->gradp[q]*dpR;
+      grad[q] = ((cR->prim[q] - cR->gradp[q]*dpR) - (cL->prim[q] + cL->gradp[q]*dpL))/(F->dxL + F->dxR);
    }
    double n[3] = {0.0, 0.0, 0.0};
    if(dim == 1) n[0] = 1.0; else n[2] = 1.0;
@@ -876,7 +999,12 @@ static void riemann_trans(pface *F, double dt, int dim)
       primL[BT] = Bavg; primR[BT] = Bavg;
    }
    double Erz = 0, Brz = 0, Ephi = 0;
-   solve_riemann(primL, primR, cL->cons, cR->cons, F->cm, n, 0.0, dAdt, dim, &Erz, &Brz, &Ephi, NULL);
+   if(dim == 1)
+      solve_riemann(primL, primR, cL->cons, cR->cons, grad, cL->gradp, cL->gradz,
+                    grad, cR->gradp, cR->gradz, F->cm, n, 0.0, dAdt, dim, &Erz, &Brz, &Ephi, NULL);
+   else
+      solve_riemann(primL, primR, cL->cons, cR->cons, cL->gradr, cL->gradp, grad,
+                    cR->gradr, cR->gradp, grad, F->cm, n, 0.0, dAdt, dim, &Erz, &Brz, &Ephi, NULL);
    if(!(D->mhd && D->ct)) return;
    double fracL = F->dphi/cL->dphi, fracR = F->dphi/cR->dphi;
    if(dim == 1) {
@@ -1312,6 +1440,12 @@ static void set_wcell(void)
          w /= (double)Np;
          for(int i = 0; i < Np; i++) D->ring[jk][i].wiph = w;
       }
+      if(D->par.Mesh_Motion == 4) {   /* misc.c:153-167: exact mesh rotation */
+         int j = jk % D->Nr, k = jk / D->Nr;
+         double x[3] = {centroid(D->rj[j], D->rj[j - 1], 1), 0.0, centroid(D->zk[k], D->zk[k - 1], 2)};
+         double w = mesh_om(x);
+         for(int i = 0; i < Np; i++) D->ring[jk][i].wiph = w;
+      }
    }
 }
 static void calc_dp(void)
@@ -1391,6 +1525,8 @@ static void add_source(double dt)
          if(D->mhd) m_source(c->prim, c->cons, xp, xm, dV*dt);
          else e_source(c->prim, c->cons, xp, xm, dV*dt);
          for(int p = 0; p < D->Npl; p++) planet_src(&D->pl[p], c->prim, c->cons, xp, xm, dV*dt);
+         if(D->par.visc_flag && !D->mhd)
+            e_visc_source(c->prim, c->gradr, c->gradp, c->gradz, c->cons, xp, xm, dV*dt);
       }
    }
 }
@@ -1415,6 +1551,8 @@ static void onestep(double RK, double dt, int first)
    add_source(dt);
    if(first) {
       for(c = 0; c < D->N; c++) D->cells[c].piph += D->cells[c].wiph*dt;
+      /* movePlanets (Planets/circular.c:44-46) for the analytic orbit */
+      if(D->mod.planets == DISCO_PL_CIRCULAR && D->Npl > 1) D->pl[1].phi += D->pl[1].omega*dt;
       if(D->mhd) {
          check_flipped(0); flip_fluxes(0);
          if(D->Nz > 1) { check_flipped(1); flip_fluxes(1); }
@@ -1425,6 +1563,12 @@ static void onestep(double RK, double dt, int first)
       while(phi > D->Pmax) phi -= D->Pmax;
       while(phi < 0.0) phi += D->Pmax;
       D->cells[c].piph = phi;
+   }
+   for(int p = 0; p < D->Npl; p++) {   /* clean_pi on planets, misc.c:27-34 */
+      double phi = D->pl[p].phi;
+      while(phi > D->Pmax) phi -= D->Pmax;
+      while(phi < 0.0) phi += D->Pmax;
+      D->pl[p].phi = phi;
    }
    calc_dp();
    if(D->mhd && D->ct) B_faces_to_cells(1);

@@ -5,7 +5,7 @@ the harness main by oracle/ref/Makefile into oracle/_ref/<config>/disco_ref;
 each case below runs that binary on a small in.par and stores its output as
 a compressed .npz.  Run from the repository root:
 
-    python tests/golden/make_golden.py [REFERENCE_DIR]
+    python tests/golden/make_golden.py [REFERENCE_DIR [CASE ...]]
 
 The GPU tests compare the device path against these files, so they can run
 where the reference sources are not available.
@@ -29,6 +29,14 @@ from dumpio import read_dump  # noqa: E402
 CASES = {
     "cfg1_n24": ("configs/cfg1_vortex", {"Num_R": 24}, 10),
     "cfg2_n12": ("configs/cfg2_mhd_disk", {"Num_R": 12, "Num_Z": 6}, 5),
+    # solver / mesh-motion variants of the vortex: HLL on a static mesh, and
+    # HLLC with the exact Keplerian mesh rotation and a different PLM theta
+    "cfg1_hll_static": ("configs/cfg1_vortex", {"Num_R": 24, "Riemann_Solver": 0, "Mesh_Motion": 0}, 10),
+    "cfg1_exact_mesh": ("configs/cfg1_vortex", {"Num_R": 24, "Mesh_Motion": 4, "Exact_Mesh_Omega": 2,
+                                                 "PLM": 1.0}, 10),
+    # one instance of the planet-disk batch: alpha viscosity, locally
+    # isothermal, a planet on a circular orbit
+    "cfg3_n24": ("configs/cfg3_planet_disk", {"Num_R": 24}, 10),
 }
 
 
@@ -62,7 +70,7 @@ def run_case(name: str, ref: str) -> None:
         ini = read_dump(os.path.join(td, "init.bin"))
         grd = read_dump(os.path.join(td, "grad.bin"))
         run = read_dump(os.path.join(td, "run.bin"))
-    out = {"par_text": np.array(par), "nsteps": nsteps,
+    out = {"par_text": np.array(par), "nsteps": nsteps, "cfg": np.array(cfg),
            "Np": ini["Np"], "r_jph": ini["r_jph"], "z_kph": ini["z_kph"], "real": ini["real"],
            "init_piph": ini["piph"], "init_dphi": ini["dphi"], "init_prim": ini["prim"],
            "init_cons": ini["cons"], "init_wiph": ini["wiph"],
@@ -86,5 +94,6 @@ def run_case(name: str, ref: str) -> None:
 
 if __name__ == "__main__":
     ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
-    for n in CASES:
+    names = sys.argv[2:] or list(CASES)
+    for n in names:
         run_case(n, ref)

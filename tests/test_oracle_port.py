@@ -22,9 +22,12 @@ def _port_run(par_path, mk, nsteps):
     return h, d.state()
 
 
-def test_port_bit_exact_vs_golden():
-    g = load_golden("cfg1_n24")
-    h, s = _port_run(write_par(g["par_text"]), os.path.join(ROOT, "configs/cfg1_vortex/Makefile_opt.in"),
+@pytest.mark.parametrize("name", ["cfg1_n24", "cfg1_hll_static", "cfg1_exact_mesh", "cfg3_n24"])
+def test_port_bit_exact_vs_golden(name):
+    """Hydro cases: HLLC vortex, HLL on a static mesh, exact Keplerian mesh
+    rotation, and the planet disk with alpha viscosity."""
+    g = load_golden(name)
+    h, s = _port_run(write_par(g["par_text"]), os.path.join(ROOT, str(g["cfg"]), "Makefile_opt.in"),
                      int(g["nsteps"]))
     real = g["real"].astype(bool)
     assert s["t"] == float(g["run_t"])
