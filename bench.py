@@ -45,6 +45,16 @@ WORKLOADS = {
                          "overrides": {"Num_R": 64, "Num_Z": 16},
                          "cpu_sample": {"Num_R": 32, "Num_Z": 8},
                          "ref_sample": {"Num_R": 32, "Num_Z": 8}},
+    # 64 independent planet-disk runs in one graph launch per step: Nr drawn
+    # from U{64..512} and the planet mass ratio log-uniform in [1e-5, 1e-3]
+    # by splitmix64 seeded 0..63
+    "planet_batch": {"dir": "configs/cfg3_planet_disk",
+                     "desc": "64 independent 2D locally isothermal disk + planet runs (alpha 1e-3, "
+                             "h/r 0.05, r in [0.4,2.5], Nr ~ U{64..512}, q ~ logU[1e-5,1e-3]), "
+                             "one CUDA graph per step",
+                     "batch": 64,
+                     "cpu_sample": {"Num_R": 128},
+                     "ref_sample": {"Num_R": 64}},
     "vortex2d": {"dir": "configs/cfg1_vortex",
                  "desc": "2D cylindrical Newtonian hydro, Gaussian isentropic vortex, "
                          "Nr=128 on r in [0.5,3], HLLC, PLM 1.5, RK2, CFL 0.5",
@@ -170,6 +180,126 @@ def kernel_bytes(name: str, N: int, nf: dict, nq: int, sw: int, ct: bool) -> flo
     if name == "anchor":
         return N * f8
     return 0.0
+
+
+def splitmix64(x: int):
+    """The splitmix64 generator (Steele, Lea, Flood 2014): returns
+    (next state, 64-bit output)."""
+    M = (1 << 64) - 1
+    x = (x + 0x9E3779B97F4A7C15) & M
+    z = x
+    z = ((z ^ (z >> 30)) * 0xBF58476D1CE4E5B9) & M
+    z = ((z ^ (z >> 27)) * 0x94D049BB133111EB) & M
+    return x, z ^ (z >> 31)
+
+
+def batch_members(n: int):
+    """(Num_R, Mass_Ratio) of batch member i, drawn from splitmix64 seeded i."""
+    out = []
+    for i in range(n):
+        st, a = splitmix64(i)
+        st, b = splitmix64(st)
+        nr = 64 + a % 449
+        q = 10.0 ** (-5.0 + 2.0 * (b / 2.0 ** 64))
+        out.append({"Num_R": int(nr), "Mass_Ratio": float(q)})
+    return out
+
+
+def measure_batch(args, wl):
+    """The batch workload: both precisions as one Batch each, same members."""
+    import torch
+    import disco_gb300 as dg
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    cfg = os.path.join(ROOT, wl["dir"])
+    par, mk = os.path.join(cfg, "in.par"), os.path.join(cfg, "Makefile_opt.in")
+    mem = batch_members(wl["batch"])
+    res, sets, batches = {}, {}, {}
+    for prec in (1, 0):
+        doms = [dg.Domain(par, mk, precision=prec, overrides=m) for m in mem]
+        b = dg.Batch(doms)
+        sets[prec], batches[prec] = doms, b
+        cells = sum(d.num_real_cells for d in doms)
+        N = sum(d.num_cells for d in doms)
+        nq = doms[0].host.num_q
+        sw = 4 if prec else 8
+        state_bytes = N * nq * (4 * 8 + 4 * sw)
+        flush = 2 * L2_BYTES if state_bytes < 4 * L2_BYTES else 0
+        b.run(args.warmup)
+        torch.cuda.synchronize()
+        clk = ClockSampler(dev) if prec == 1 else None
+        if clk:
+            clk.start()
+            clk.wait_first()
+        l0 = dg.lib().disco_gpu_launch_count()
+        ms = b.run_timed(args.steps, flush_bytes=flush)
+        launches = dg.lib().disco_gpu_launch_count() - l0
+        if clk:
+            time.sleep(0.25)
+        clocks = clk.stop() if clk else None
+        res[prec] = {"ms": ms, "cells": cells, "N": N, "nq": nq, "sw": sw, "flush": flush,
+                     "launches": launches, "clocks": clocks,
+                     "value": cells * args.steps / (ms / 1e3)}
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from helpers import cell_radius, grouped_rel_l1
+    worst, worst128, per_member = {}, {}, []
+    for m, d1, d0 in zip(mem, sets[1], sets[0]):
+        s1, s0 = d1.state(), d0.state()
+        h = d0.host
+        real = h.real_mask()
+        r = cell_radius(h.Np, h.r_jph, h.Nr, h.Nz)[real]
+        e = grouped_rel_l1(s1["cons"][:, real], s0["cons"][:, real], r, 5)
+        per_member.append([m["Num_R"], max(e.values())])
+        for k, v in e.items():
+            worst[k] = max(worst.get(k, 0.0), v)
+            if m["Num_R"] >= 128:
+                worst128[k] = max(worst128.get(k, 0.0), v)
+    res["l1_err"] = {"max_over_quantities": max(worst.values()), "per_quantity": worst,
+                     "max_over_quantities_Nr_ge_128": max(worst128.values()) if worst128 else None,
+                     "per_member_Nr_and_max": sorted(per_member),
+                     "note": "maximum over the batch members of the per-member error"}
+    # per-kernel profile of the largest member (its own stream, no graph)
+    big = max(range(len(mem)), key=lambda i: sets[1][i].num_cells)
+    res["profile"] = sets[1][big].profile(3)
+    hb = sets[1][big].host
+    Np = hb.Np.reshape(hb.Nz, hb.Nr)
+    res["profiled"] = {"N": sets[1][big].num_cells,
+                       "nf": {"r": int((Np[:, :-1] + Np[:, 1:]).sum()) if hb.Nr > 1 else 0,
+                              "z": int((Np[:-1, :] + Np[1:, :]).sum()) if hb.Nz > 1 else 0},
+                       "member": big, "Num_R": mem[big]["Num_R"]}
+    # e2e: upload every member's state from pinned host memory, K x (one batch
+    # step, read every member's time to the host), download every member
+    doms = sets[1]
+    pins = []
+    for d in doms:
+        st = d.state()
+        pin = {k: torch.empty(st[k].shape, dtype=torch.float64, pin_memory=True).numpy()
+               for k in ("piph", "dphi", "wiph", "prim", "cons")}
+        for k in pin:
+            pin[k][...] = st[k]
+        pins.append(pin)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for d, pin in zip(doms, pins):
+        d.upload(**pin)
+    for _ in range(args.steps):
+        batches[1].run(1)
+        [d.t for d in doms]
+    outs = [d.state() for d in doms]
+    t1 = time.perf_counter()
+    up = sum(pin[k].nbytes for pin in pins for k in pin)
+    down = sum(o[k].nbytes for o in outs for k in ("piph", "dphi", "wiph", "prim", "cons"))
+    res["e2e"] = {"value": res[1]["cells"] * args.steps / (t1 - t0), "unit": "zone-updates/s",
+                  "h2d_bytes_per_step": int(up / args.steps),
+                  "d2h_bytes_per_step": int(down / args.steps + 8 * len(doms)),
+                  "timed": "upload of every member's state, K x (batch step, members' times "
+                           "to host), download of every member"}
+    for bb in batches.values():
+        bb.close()
+    for ds in sets.values():
+        for d in ds:
+            d.close()
+    return res
 
 
 def measure_ours(args, wl, rank):
@@ -359,7 +489,7 @@ def main():
         dist.init_process_group("nccl")
         pg = dist
         dist.barrier()
-    res = measure_ours(args, wl, rank)
+    res = measure_batch(args, wl) if wl.get("batch") else measure_ours(args, wl, rank)
     ms = res[1]["ms"]
     if pg is not None:
         t = torch.tensor([ms], device="cuda", dtype=torch.float64)
@@ -378,16 +508,19 @@ def main():
     import disco_gb300 as dg  # noqa: F401
     from disco_gb300.api import Domain  # noqa: F401
     nf = {"r": 0, "z": 0}
-    hp = dg.read_params(os.path.join(ROOT, wl["dir"], "in.par"))
-    for k, v in (wl.get("overrides") or {}).items():
-        setattr(hp, k, v)
-    hd = dg.HostDomain(hp,
-                       dg.read_modules(os.path.join(ROOT, wl["dir"], "Makefile_opt.in")))
-    Np = hd.Np.reshape(hd.Nz, hd.Nr)
-    if hd.Nr > 1:
-        nf["r"] = int((Np[:, :-1] + Np[:, 1:]).sum())
-    if hd.Nz > 1:
-        nf["z"] = int((Np[:-1, :] + Np[1:, :]).sum())
+    if "profiled" in res:   # batch: the profile is of its largest member
+        N, nf = res["profiled"]["N"], res["profiled"]["nf"]
+    else:
+        hp = dg.read_params(os.path.join(ROOT, wl["dir"], "in.par"))
+        for k, v in (wl.get("overrides") or {}).items():
+            setattr(hp, k, v)
+        hd = dg.HostDomain(hp,
+                           dg.read_modules(os.path.join(ROOT, wl["dir"], "Makefile_opt.in")))
+        Np = hd.Np.reshape(hd.Nz, hd.Nr)
+        if hd.Nr > 1:
+            nf["r"] = int((Np[:, :-1] + Np[:, 1:]).sum())
+        if hd.Nz > 1:
+            nf["z"] = int((Np[:-1, :] + Np[1:, :]).sum())
     prof = sorted(res["profile"], key=lambda x: -x[2])
     tot_prof = sum(p[2] for p in prof)
     top = prof[0]
@@ -411,6 +544,8 @@ def main():
         "dtype": "f32 reconstruction/fluxes, f64 positions/accumulation",
         "data": "synthetic",
         "config": {"workload": wl["desc"], "cells": cells, "precision": "mixed",
+                   **({"members": wl["batch"], "profiled_member": res["profiled"]}
+                      if "profiled" in res else {}),
                    "l2": "flushed between steps" if res[1]["flush"] else "inputs larger than L2",
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "fp64": {"value": world * res[0]["cells"] * args.steps / (res[0]["ms"] / 1e3),

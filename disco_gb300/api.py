@@ -126,6 +126,10 @@ SIGNATURES = {
     "disco_gpu_debug_ct": (C.c_int, [_P, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double),
                                      C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     "disco_gpu_getmindt_noalloc": (C.c_int, [_P, C.POINTER(C.c_double)]),
+    "disco_batch_create": (C.c_int, [C.POINTER(_P), C.c_int, C.POINTER(_P)]),
+    "disco_batch_run": (C.c_int, [_P, C.c_int]),
+    "disco_batch_run_timed": (C.c_int, [_P, C.c_int, C.c_size_t, C.POINTER(C.c_double)]),
+    "disco_batch_free": (None, [_P]),
     "disco_gpu_time": (C.c_double, [_P]),
     "disco_gpu_num_cells": (C.c_long, [_P]),
     "disco_gpu_num_real_cells": (C.c_long, [_P]),
@@ -308,6 +312,43 @@ class Domain:
         if getattr(self, "_g", None):
             lib().disco_gpu_free(self._g)
             self._g = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Batch:
+    """Independent domains advanced together (disco_gpu_batch.h): each step is
+    one CUDA-graph launch with one branch per member, every member using its
+    own CFL dt.  The members stay usable on their own (state(), status())."""
+
+    def __init__(self, members: list):
+        self.members = list(members)
+        arr = (C.c_void_p * len(self.members))(*[m._g.value for m in self.members])
+        b = C.c_void_p()
+        _check(lib().disco_batch_create(arr, len(self.members), C.byref(b)), "disco_batch_create")
+        self._b = b
+
+    @property
+    def num_real_cells(self) -> int:
+        return sum(m.num_real_cells for m in self.members)
+
+    def run(self, nsteps: int) -> None:
+        _check(lib().disco_batch_run(self._b, int(nsteps)), "disco_batch_run")
+
+    def run_timed(self, nsteps: int, flush_bytes: int = 0) -> float:
+        ms = C.c_double()
+        _check(lib().disco_batch_run_timed(self._b, int(nsteps), int(flush_bytes), C.byref(ms)),
+               "disco_batch_run_timed")
+        return ms.value
+
+    def close(self) -> None:
+        if getattr(self, "_b", None) is not None and self._b.value:
+            lib().disco_batch_free(self._b)
+            self._b = C.c_void_p()
 
     def __del__(self):
         try:

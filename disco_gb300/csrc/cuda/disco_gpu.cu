@@ -3,6 +3,7 @@
 #include "instance.cuh"
 #include "disco_gpu_debug.h"
 #include "disco_gpu_noalloc.h"
+#include "disco_gpu_batch.h"
 
 std::atomic<long long> g_launches{0};
 long long disco_gpu_launch_count(void) { return g_launches.load(); }
@@ -19,6 +20,87 @@ using namespace disco_impl;
 struct disco_gpu {
   InstanceBase* impl;
 };
+
+// A batch: one graph per piph parity, built by stream capture with a
+// fork/join over the members' own streams, so the captured graph has one
+// branch per member.
+struct disco_batch {
+  std::vector<InstanceBase*> m;
+  cudaStream_t root = nullptr;
+  cudaEvent_t fork = nullptr;
+  std::vector<cudaEvent_t> join;
+  cudaGraphExec_t graph[2] = {nullptr, nullptr};
+  long long nodes = 0;          // kernel launches per graph
+  std::vector<long long> per;   // per member
+  int parity = 0;
+  void* flush = nullptr;
+  size_t flush_size = 0;
+  ~disco_batch() {
+    for (auto& g : graph) if (g) cudaGraphExecDestroy(g);
+    for (auto e : join) if (e) cudaEventDestroy(e);
+    if (fork) cudaEventDestroy(fork);
+    if (root) cudaStreamDestroy(root);
+    if (flush) cudaFree(flush);
+  }
+};
+
+static int batch_build(disco_batch* b, int par) {
+  long long before = g_launches.load();
+  CK(cudaStreamBeginCapture(b->root, cudaStreamCaptureModeThreadLocal));
+  CK(cudaEventRecord(b->fork, b->root));
+  b->per.assign(b->m.size(), 0);
+  for (size_t i = 0; i < b->m.size(); ++i) {
+    long long l0 = g_launches.load();
+    CK(cudaStreamWaitEvent(b->m[i]->stream(), b->fork, 0));
+    b->m[i]->launch_step(par);
+    CK(cudaEventRecord(b->join[i], b->m[i]->stream()));
+    CK(cudaStreamWaitEvent(b->root, b->join[i], 0));
+    b->per[i] = g_launches.load() - l0;
+  }
+  cudaGraph_t g;
+  CK(cudaStreamEndCapture(b->root, &g));
+  b->nodes = g_launches.load() - before;
+  g_launches -= b->nodes;   // counted on each replay
+  CK(cudaGraphInstantiate(&b->graph[par], g, 0));
+  cudaGraphDestroy(g);
+  return 0;
+}
+
+static int batch_steps(disco_batch* b, int nsteps, size_t flush_bytes, double* ms) {
+  for (int p = 0; p < 2; ++p)
+    if (!b->graph[p]) { int rc = batch_build(b, p); if (rc) return rc; }
+  if (flush_bytes > b->flush_size) {
+    if (b->flush) cudaFree(b->flush);
+    b->flush = nullptr; b->flush_size = 0;
+    CK(cudaMalloc(&b->flush, flush_bytes));
+    b->flush_size = flush_bytes;
+  }
+  std::vector<cudaEvent_t> ev(ms ? 2 * (size_t)nsteps : 0);
+  for (auto& e : ev) CK(cudaEventCreate(&e));
+  for (int s = 0; s < nsteps; ++s) {
+    if (ms && flush_bytes) CK(cudaMemsetAsync(b->flush, s & 0xff, flush_bytes, b->root));
+    if (ms) CK(cudaEventRecord(ev[2 * s], b->root));
+    CK(cudaGraphLaunch(b->graph[b->parity], b->root));
+    if (ms) CK(cudaEventRecord(ev[2 * s + 1], b->root));
+    b->parity ^= 1;
+  }
+  CK(cudaStreamSynchronize(b->root));
+  if (ms) {
+    double tot = 0;
+    for (int s = 0; s < nsteps; ++s) {
+      float t;
+      CK(cudaEventElapsedTime(&t, ev[2 * s], ev[2 * s + 1]));
+      tot += t;
+    }
+    *ms = tot;
+    for (auto e : ev) cudaEventDestroy(e);
+  }
+  for (size_t i = 0; i < b->m.size(); ++i) {
+    int rc = b->m[i]->after_external_steps(nsteps, b->per[i] * nsteps);
+    if (rc) return rc;
+  }
+  return 0;
+}
 
 extern "C" {
 
@@ -81,6 +163,47 @@ int disco_gpu_getmindt_noalloc(disco_gpu* g, double* dt) {
   if (!g || !dt) { disco_set_error("null argument"); return DISCO_E_ARG; }
   return g->impl->getmindt_noalloc(dt);
 }
+int disco_batch_create(disco_gpu* const* members, int n, disco_batch** out) {
+  if (!members || n <= 0 || !out) { disco_set_error("disco_batch_create: bad argument"); return DISCO_E_ARG; }
+  int par = -1;
+  for (int i = 0; i < n; ++i) {
+    if (!members[i]) { disco_set_error("disco_batch_create: null member"); return DISCO_E_ARG; }
+    int p = members[i]->impl->cur_parity();
+    if (par >= 0 && p != par) {
+      disco_set_error("disco_batch_create: members have taken different step counts (parity)");
+      return DISCO_E_STATE;
+    }
+    par = p;
+  }
+  disco_batch* b = new disco_batch();
+  for (int i = 0; i < n; ++i) b->m.push_back(members[i]->impl);
+  b->parity = par;
+  b->join.assign(n, nullptr);
+  if (cudaStreamCreateWithFlags(&b->root, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming) != cudaSuccess) {
+    delete b;
+    disco_set_error("disco_batch_create: stream/event creation failed");
+    return DISCO_E_CUDA;
+  }
+  for (int i = 0; i < n; ++i)
+    if (cudaEventCreateWithFlags(&b->join[i], cudaEventDisableTiming) != cudaSuccess) {
+      delete b;
+      disco_set_error("disco_batch_create: event creation failed");
+      return DISCO_E_CUDA;
+    }
+  *out = b;
+  return 0;
+}
+int disco_batch_run(disco_batch* b, int nsteps) {
+  if (!b || nsteps < 0) { disco_set_error("bad argument"); return DISCO_E_ARG; }
+  return batch_steps(b, nsteps, 0, nullptr);
+}
+int disco_batch_run_timed(disco_batch* b, int nsteps, size_t flush_bytes, double* ms) {
+  if (!b || nsteps < 0 || !ms) { disco_set_error("bad argument"); return DISCO_E_ARG; }
+  return batch_steps(b, nsteps, flush_bytes, ms);
+}
+void disco_batch_free(disco_batch* b) { delete b; }
+
 double disco_gpu_time(disco_gpu* g) { return g ? g->impl->time() : 0.0; }
 long disco_gpu_num_cells(disco_gpu* g) { return g ? g->impl->N : 0; }
 long disco_gpu_num_real_cells(disco_gpu* g) { return g ? g->impl->Nreal : 0; }

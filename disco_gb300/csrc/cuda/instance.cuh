@@ -48,8 +48,27 @@ struct InstanceBase {
   virtual double time() = 0;
   virtual int debug_ct(int stage, double* E, double* B, double* Ephi, double* Phi) = 0;
   virtual int getmindt_noalloc(double* dt) = 0;
+  // batch support: launch one full step (getmindt + timestep) from piph
+  // parity `par` on the instance's stream, then account for nsteps steps
+  // taken outside the instance's own run()
+  virtual void launch_step(int par) = 0;
+  virtual int cur_parity() const = 0;
+  virtual cudaStream_t stream() const = 0;
+  virtual int after_external_steps(int nsteps, long long nodes) = 0;
   long N = 0, Nreal = 0;
 };
+
+// The dynamic shared-memory limit is an attribute of the kernel function,
+// shared by every instance in the process: only ever raise it, so a smaller
+// instance created later cannot lower the limit a larger one relies on.
+template <typename K>
+static cudaError_t raise_smem_limit(K* kernel, size_t bytes) {
+  cudaFuncAttributes a;
+  cudaError_t e = cudaFuncGetAttributes(&a, kernel);
+  if (e != cudaSuccess) return e;
+  if ((size_t)a.maxDynamicSharedSizeBytes >= bytes) return cudaSuccess;
+  return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+}
 
 template <typename T>
 static int dalloc(T** p, size_t n, std::vector<void*>& keep) {
@@ -198,7 +217,7 @@ struct Instance : InstanceBase {
 
     for (int jk = 0; jk < nring; ++jk) maxring = std::max(maxring, dom->Np[jk]);
     if ((maxring + 1) * 8 > 48 * 1024)
-      CK(cudaFuncSetAttribute(k_wcell_avg<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (maxring + 1) * 8));
+      CK(raise_smem_limit(k_wcell_avg<R>, (size_t)(maxring + 1) * 8));
     // ---- index arrays
     std::vector<int> ring_off(nring + 1), cell_ring(N);
     for (int jk = 0; jk <= nring; ++jk) ring_off[jk] = (int)dom->ring_off[jk];
@@ -274,7 +293,7 @@ struct Instance : InstanceBase {
       }
       C.last_pair[d] = np - 1;
       if (np > 0 && mx * 13 + 64 > 48 * 1024) {
-        CK(cudaFuncSetAttribute(k_faces<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx * 13 + 64));
+        CK(raise_smem_limit(k_faces<R>, (size_t)mx * 13 + 64));
       }
     }
     A(&S.planets, MAX_PL); A(&S.scal, SC_COUNT); A(&S.errs, 1);
@@ -292,10 +311,10 @@ struct Instance : InstanceBase {
       }
       for (int d = 0; d < 2; ++d)
         if (flip_smem(d) > 48 * 1024)
-          CK(cudaFuncSetAttribute(k_ct_flip<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)flip_smem(d)));
+          CK(raise_smem_limit(k_ct_flip<R>, flip_smem(d)));
       edge_smem = (size_t)4 * maxring * 8;
       if (edge_smem > 48 * 1024)
-        CK(cudaFuncSetAttribute(k_ct_edge<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)edge_smem));
+        CK(raise_smem_limit(k_ct_edge<R>, edge_smem));
     }
 #undef A
     std::vector<DevPlanet> pl(MAX_PL);
@@ -694,6 +713,29 @@ struct Instance : InstanceBase {
     return 0;
   }
   double time() override { return host_t; }
+
+  void launch_step(int par) override {
+    int save = parity;
+    parity = par;
+    set_piph(par);
+    P.t_end = 0.0;
+    launch_mindt();
+    step_kernels();
+    parity = save;
+    set_piph(save);
+  }
+  int cur_parity() const override { return parity; }
+  cudaStream_t stream() const override { return st; }
+  int after_external_steps(int nsteps, long long nodes) override {
+    g_launches += nodes;
+    parity ^= (nsteps & 1);
+    set_piph(parity);
+    double sc[SC_COUNT];
+    CK(cudaMemcpyAsync(sc, S.scal, sizeof sc, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    host_t = sc[SC_T];
+    return 0;
+  }
 
   // CFL dt with partial minima in the library's static scratch array: no
   // device allocation, no write to the instance (disco_gpu_noalloc.h).
