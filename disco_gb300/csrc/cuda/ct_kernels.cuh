@@ -36,7 +36,7 @@ __global__ void k_ct_gather(DevParams P, DevState<R> S, CtStateT<R> C, double RK
     else C.Phi[q * N + c] = (1. - RK) * ph + RK * C.RKPhi[q * N + c];
   }
   int jk = S.cell_ring[c];
-  int j = jk % P.Nr, k = jk / P.Nr;
+  int k = div_fast(jk, P.mul_nr), j = jk - k * P.Nr;
   if (!ring_in_phi_range(P, j, k)) return;
   for (int dim = 1; dim <= 2; ++dim) {
     if (dim == 1 && P.Nr <= 1) continue;
@@ -102,7 +102,7 @@ __global__ void k_ct_avg(DevParams P, DevState<R> S, CtStateT<R> C) {
   if (c >= S.N) return;
   const int N = S.N;
   int jk = S.cell_ring[c];
-  int j = jk % P.Nr, k = jk / P.Nr;
+  int k = div_fast(jk, P.mul_nr), j = jk - k * P.Nr;
   R outE[4], outB[4];
   // mixed path: the B average split by the ring whose frame the EMFs were
   // stored in (own ring / the neighbouring ring across the face)
@@ -187,7 +187,7 @@ DISCO_D void ct_bflux_mixed(const DevParams& P, const DevState<R>& S, const CtSt
                             double fac, int c) {
   const int N = S.N;
   int jk = S.cell_ring[c];
-  int j = jk % P.Nr, k = jk / P.Nr;
+  int k = div_fast(jk, P.mul_nr), j = jk - k * P.Nr;
   R dtf = (R)fac * dt_r<R>(S.scal);
   R dph0 = 0;
   for (int dim = 1; dim <= 2; ++dim) {
@@ -232,7 +232,7 @@ __global__ void k_ct_bflux(DevParams P, DevState<R> S, CtStateT<R> C, double fac
   }
   const int N = S.N;
   int jk = S.cell_ring[c];
-  int j = jk % P.Nr, k = jk / P.Nr;
+  int k = div_fast(jk, P.mul_nr), j = jk - k * P.Nr;
   double dt = fac * S.scal[SC_DT];
   const double* rj = S.r_jph + 1;
   const double* zk = S.z_kph + 1;
@@ -322,7 +322,7 @@ template <typename R>
 __global__ void k_ct_edge(DevParams P, DevState<R> S, CtStateT<R> C, double fac) {
   extern __shared__ double sm[];
   int q = blockIdx.x;   // quad (j, k): rings j, j+1 at layers k, k+1
-  int j = q % (P.Nr - 1), k = q / (P.Nr - 1);
+  int k = div_fast(q, P.mul_nr1), j = q - k * (P.Nr - 1);
   const int N = S.N;
   int ring[4] = {j + P.Nr * k, j + 1 + P.Nr * k, j + P.Nr * (k + 1), j + 1 + P.Nr * (k + 1)};
   int off[4], np[4], I0[4], base[4];
@@ -555,7 +555,7 @@ __global__ void k_ct_b2c(DevParams P, DevState<R> S, CtStateT<R> C, int prim_out
   if (c >= S.N) return;
   const int N = S.N;
   int jk = S.cell_ring[c];
-  int j = jk % P.Nr, k = jk / P.Nr;
+  int k = div_fast(jk, P.mul_nr), j = jk - k * P.Nr;
   if (!prim_out && !is_real(P, j, k)) return;
   int off = S.ring_off[jk], Np = S.ring_off[jk + 1] - off;
   int i = c - off;
@@ -644,7 +644,7 @@ __global__ void k_ct_init_phi0(DevParams P, DevState<R> S, CtStateT<R> C) {
   int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= S.N) return;
   int jk = S.cell_ring[c];
-  int j = jk % P.Nr, k = jk / P.Nr;
+  int k = div_fast(jk, P.mul_nr), j = jk - k * P.Nr;
   const double* rj = S.r_jph + 1;
   const double* zk = S.z_kph + 1;
   double x[3] = {S.ring_rc[jk], S.piph[c], centroid_z(zk[k], zk[k - 1])};
@@ -662,7 +662,7 @@ __global__ void k_ct_init_face_phi(DevParams P, DevState<R> S, CtStateT<R> C, in
   // face centre cm = (r, phic, z) of its pair
   int cL = S.fL[d][f];
   int jk = S.cell_ring[cL];
-  int j = jk % P.Nr, k = jk / P.Nr;
+  int k = div_fast(jk, P.mul_nr), j = jk - k * P.Nr;
   const double* rj = S.r_jph + 1;
   const double* zk = S.z_kph + 1;
   double x[3];

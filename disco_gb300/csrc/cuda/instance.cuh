@@ -177,6 +177,12 @@ struct Instance : InstanceBase {
     double icp[8] = {p.initPar1, p.initPar2, p.initPar3, p.initPar4, p.initPar5, p.initPar6, p.initPar7, p.initPar8};
     for (int i = 0; i < 8; ++i) P.ic[i] = icp[i];
     P.t_end = 0.0;
+    if ((long)nring >= (1L << 24) || Nr >= (1 << 16)) {
+      disco_set_error("grid too large for the ring index arithmetic (Nr*Nz < 2^24, Nr < 2^16)");
+      return DISCO_E_ARG;
+    }
+    P.mul_nr = ((1ull << 40) + (unsigned long long)Nr - 1) / (unsigned long long)Nr;
+    P.mul_nr1 = Nr > 1 ? ((1ull << 40) + (unsigned long long)(Nr - 1) - 1) / (unsigned long long)(Nr - 1) : 0;
     planets_id = dom->mod.planets;
     if (!Phys::MHD && P.riemann_solver == SOLVER_HLLD) {
       disco_set_error("Riemann_Solver = HLLD with a hydro module (riemann.c:19-22)");
@@ -296,6 +302,17 @@ struct Instance : InstanceBase {
         CK(raise_smem_limit(k_faces<R>, (size_t)mx * 13 + 64));
       }
     }
+    A(&S.fslope, (size_t)NQ * std::max(S.nf[0], S.nf[1]));
+    {   // chunks of kTileCells consecutive cells of each ring
+      std::vector<int> cr, ci;
+      for (int jk = 0; jk < nring; ++jk)
+        for (int i0 = 0; i0 < dom->Np[jk]; i0 += kTileCells) { cr.push_back(jk); ci.push_back(i0); }
+      int *d_cr, *d_ci;
+      A(&d_cr, cr.size()); A(&d_ci, ci.size());
+      CK(cudaMemcpy(d_cr, cr.data(), sizeof(int) * cr.size(), cudaMemcpyHostToDevice));
+      CK(cudaMemcpy(d_ci, ci.data(), sizeof(int) * ci.size(), cudaMemcpyHostToDevice));
+      S.chunk_ring = d_cr; S.chunk_i0 = d_ci; S.nchunk = (int)cr.size();
+    }
     A(&S.planets, MAX_PL); A(&S.scal, SC_COUNT); A(&S.errs, 1);
     S.ct = ct ? 1 : 0;
     if (ct) {
@@ -408,6 +425,17 @@ struct Instance : InstanceBase {
       LAUNCH(d == 0 ? "faces_r" : "faces_z", (k_faces<R><<<npair[d], 256, sm, st>>>(P, S, d + 1)));
     }
   }
+  // plm_trans per dimension: face slopes, then the per-cell gather
+  void launch_plm_trans() {
+    for (int d = 0; d < 2; ++d) {
+      if (!npair[d]) continue;
+      dim3 grid(npair[d], (maxNf[d] + 255) / 256);
+      LAUNCH(d == 0 ? "plm_slopes_r" : "plm_slopes_z",
+             (k_plm_slopes<R, NQ><<<grid, 256, 0, st>>>(P, S, d + 1)));
+      LAUNCH(d == 0 ? "plm_trans_r" : "plm_trans_z",
+             (k_plm_trans<R, NQ><<<dim3(S.nchunk, plm_groups<NQ>()), kTileCells, 0, st>>>(P, S, d + 1)));
+    }
+  }
   void launch_mindt() {
     LAUNCH("mindt", (k_mindt<Phys, R, NQ><<<blocks(N), 256, 0, st>>>(P, S)));
     LAUNCH("dt_finalize", (k_dt_finalize<<<1, 1, 0, st>>>(P, S.scal)));
@@ -440,8 +468,7 @@ struct Instance : InstanceBase {
   void substep(double RK, double fac, int first) {
     if (first) launch_wcell();
     LAUNCH("plm_phi", (k_plm_phi<R, NQ><<<blocks(N), 256, 0, st>>>(P, S)));
-    if (Nr > 1) LAUNCH("plm_trans_r", (k_plm_trans<R, NQ><<<dim3(blocks(N), plm_groups<NQ>()), 256, 0, st>>>(P, S, 1)));
-    if (Nz > 1) LAUNCH("plm_trans_z", (k_plm_trans<R, NQ><<<dim3(blocks(N), plm_groups<NQ>()), 256, 0, st>>>(P, S, 2)));
+    launch_plm_trans();
     LAUNCH("flux_phi", (k_flux_phi<Phys, R, NQ><<<blocks(N), 256, 0, st>>>(P, S, fac)));
     launch_trans_fluxes(fac);
     if (ct) {   // avg_Efields, subtract_advective_B_fluxes, update_B_fluxes (onestep.c:261-265)
@@ -619,8 +646,7 @@ struct Instance : InstanceBase {
     const int first = 1;
     launch_wcell();
     LAUNCH("plm_phi", (k_plm_phi<R, NQ><<<blocks(N), 256, 0, st>>>(P, S)));
-    if (Nr > 1) LAUNCH("plm_trans_r", (k_plm_trans<R, NQ><<<dim3(blocks(N), plm_groups<NQ>()), 256, 0, st>>>(P, S, 1)));
-    if (Nz > 1) LAUNCH("plm_trans_z", (k_plm_trans<R, NQ><<<dim3(blocks(N), plm_groups<NQ>()), 256, 0, st>>>(P, S, 2)));
+    launch_plm_trans();
     LAUNCH("flux_phi", (k_flux_phi<Phys, R, NQ><<<blocks(N), 256, 0, st>>>(P, S, fac)));
     if (stage >= 1) {
       launch_trans_fluxes(fac);

@@ -80,6 +80,11 @@ struct DevState {
   R* pidxs[2];                 // per pair: 1 / (dxL + dxR)
   R* pdA[2];                   // per pair: face area per unit dphi
   R* fflux[2];                 // [NQ*Nf] (F - wU*) dA dt
+  R* fslope;                   // [NQ*max Nf] face slopes of one dimension (plm_trans)
+  // chunks of kTileCells consecutive cells of one ring (tiled face gathers)
+  const int* chunk_ring;
+  const int* chunk_i0;
+  int nchunk;
   int* run_up_s[2];            // per cell: first face where the cell is L (pair above)
   int* run_up_e[2];
   int* run_dn_s[2];            // per cell: first face where the cell is R (pair below)
@@ -152,11 +157,11 @@ DISCO_D bool ring_in_phi_range(const DevParams& P, int j, int k) {
 DISCO_D bool pair_in_flux_range(const DevParams& P, int dim, int pair) {
   int j, k, jmin, jmax, kmin, kmax;
   if (dim == 1) {
-    j = pair % (P.Nr - 1); k = pair / (P.Nr - 1);
+    k = div_fast(pair, P.mul_nr1); j = pair - k * (P.Nr - 1);
     jmin = P.NgRa == 0 ? 0 : P.NgRa - 1; jmax = P.NgRb == 0 ? P.Nr - 1 : P.Nr - P.NgRb;
     kmin = P.NgZa == 0 ? 0 : P.NgZa - 1; kmax = P.NgZb == 0 ? P.Nz : P.Nz - P.NgZb + 1;
   } else {
-    j = pair % P.Nr; k = pair / P.Nr;
+    k = div_fast(pair, P.mul_nr); j = pair - k * P.Nr;
     jmin = P.NgRa == 0 ? 0 : P.NgRa - 1; jmax = P.NgRb == 0 ? P.Nr : P.Nr - P.NgRb + 1;
     kmin = P.NgZa == 0 ? 0 : P.NgZa - 1; kmax = P.NgZb == 0 ? P.Nz - 1 : P.Nz - P.NgZb;
   }
@@ -184,7 +189,7 @@ __global__ void k_wcell(DevParams P, DevState<R> S) {
   int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= S.N) return;
   int jk = S.cell_ring[c];
-  int j = jk % P.Nr, k = jk / P.Nr;
+  int k = div_fast(jk, P.mul_nr), j = jk - k * P.Nr;
   int off = S.ring_off[jk], Np = S.ring_off[jk + 1] - off;
   int i = c - off;
   double w = 0.0;
@@ -347,10 +352,10 @@ struct PairInfo {
 DISCO_D PairInfo pair_info(const DevParams& P, int dim, int pair) {
   PairInfo pi;
   if (dim == 1) {
-    int j = pair % (P.Nr - 1), k = pair / (P.Nr - 1);
+    int k = div_fast(pair, P.mul_nr1), j = pair - k * (P.Nr - 1);
     pi.L = j + P.Nr * k; pi.R = j + 1 + P.Nr * k; pi.jL = j; pi.kL = k;
   } else {
-    int j = pair % P.Nr, k = pair / P.Nr;
+    int k = div_fast(pair, P.mul_nr), j = pair - k * P.Nr;
     pi.L = j + P.Nr * k; pi.R = j + P.Nr * (k + 1); pi.jL = j; pi.kL = k;
   }
   return pi;
@@ -587,13 +592,13 @@ DISCO_D void pair_dx(const DevParams& P, const double* r_jph, const double* z_kp
   const double* rj = r_jph + 1;
   const double* zk = z_kph + 1;
   if (dim == 1) {
-    int j = pair % (P.Nr - 1);
+    int j = pair - div_fast(pair, P.mul_nr1) * (P.Nr - 1);
     double rm = centroid_r(rj[j], rj[j - 1]);
     double rp = centroid_r(rj[j + 1], rj[j]);
     *dxL = rj[j] - rm;
     *dxR = rp - rj[j];
   } else {
-    int k = pair / P.Nr;
+    int k = div_fast(pair, P.mul_nr);
     double zm = centroid_z(zk[k], zk[k - 1]);
     double zp = centroid_z(zk[k + 1], zk[k]);
     *dxL = zk[k] - zm;
@@ -606,7 +611,7 @@ template <typename R>
 __global__ void k_ring_geom(DevParams P, DevState<R> S, int nring) {
   int jk = blockIdx.x * blockDim.x + threadIdx.x;
   if (jk >= nring) return;
-  int j = jk % P.Nr, k = jk / P.Nr;
+  int k = div_fast(jk, P.mul_nr), j = jk - k * P.Nr;
   double rp = S.r_jph[j + 1], rm = S.r_jph[j];
   double zp = S.z_kph[k + 1], zm = S.z_kph[k];
   S.ring_rc[jk] = centroid_r(rp, rm);
@@ -661,88 +666,135 @@ __global__ void k_pair_geom(DevParams P, DevState<R> S, int dim, int npair) {
   S.pcX[d][pair] = (R)((dim == 1 ? -dOm : dOm) * r);
 }
 
-// ---- plm_trans, plm.c:56-195 (per-cell gather over the cell's faces) ---------
-// Sum S dA over the cell's faces, divide by the total area, then limit.  The
-// reference limiter loop (plm.c:146-179) reduces to: zero if any face slope
-// has the opposite sign (or is zero), else the smallest of |g| and |PLM S|,
-// which is independent of face order; it is evaluated in one pass here.
-// The components are independent: blockIdx.y selects a group of QPT of them,
-// so a cell's work is spread over several threads with fewer registers each.
-constexpr int kPlmQ = 5;   // components per thread in k_plm_trans
+// ---- plm_trans, plm.c:56-195 ------------------------------------------------
+// Two passes, as the reference's own face loop: k_plm_slopes computes every
+// face's slope S = (W_R - W_L) / (dxL + dxR) once (plm.c:87-110), then
+// k_plm_trans gathers each cell's faces in the reference's order: sum S dA,
+// divide by the total area, limit.  The reference limiter loop
+// (plm.c:146-179) reduces to: zero if any face slope has the opposite sign
+// (or is zero), else the smallest of |g| and |PLM S| -- a function of the
+// extremes of PLM S over the faces only, independent of face order.
+template <typename R, int NQ>
+__global__ void k_plm_slopes(DevParams P, DevState<R> S, int dim) {
+  const int d = dim - 1;
+  int pair = blockIdx.x;
+  int base = S.face_off[d][pair], Nf = S.face_off[d][pair + 1] - base;
+  int n = blockIdx.y * blockDim.x + threadIdx.x;
+  if (n >= Nf) return;
+  int f = base + n;
+  const int N = S.N, NF = S.nf[d];
+  int cL = S.fL[d][f], cR = S.fR[d][f];
+  R dpL = S.fdpL[d][f], dpR = S.fdpR[d][f];
+  R dxs = S.pdxs[d][pair];
+  R idxs = kMix<R> ? S.pidxs[d][pair] : (R)0;
+  R dOm = kMix<R> ? S.pdOm[d][pair] : (R)0;
+#pragma unroll
+  for (int q = 0; q < NQ; ++q) {
+    R WL = S.prim[q * N + cL] + dpL * S.gradp[q * N + cL];
+    R WR = S.prim[q * N + cR] - dpR * S.gradp[q * N + cR];
+    R Sl;
+    if constexpr (kMix<R>) Sl = ((WR - WL) + (q == UPP ? dOm : (R)0)) * idxs;   // frames of the rings
+    else Sl = (WR - WL) / dxs;
+    S.fslope[q * NF + f] = Sl;
+  }
+}
+
+// The components are independent: blockIdx.y selects a group of QPT of them.
+constexpr int kPlmQ = 5;        // components per thread in k_plm_trans
+constexpr int kTileCells = 128; // cells per block of a tiled face gather
+constexpr int kTileCap = 4 * kTileCells;   // faces staged per side
 template <int NQ>
 constexpr int plm_groups() { return (NQ + kPlmQ - 1) / kPlmQ; }
 
+// The faces where consecutive cells of a ring are L (or R) form one circular
+// interval of the pair's face block, because the merge walk assigns faces to
+// the cells of each ring in ring order.  A block takes kTileCells consecutive
+// cells of one ring, stages that interval's face data in shared memory with
+// coalesced loads, and each thread then walks its own run in the reference's
+// order from shared memory.
 template <typename R, int NQ>
-__global__ void k_plm_trans(DevParams P, DevState<R> S, int dim) {
-  int c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= S.N) return;
+__global__ void __launch_bounds__(kTileCells) k_plm_trans(DevParams P, DevState<R> S, int dim) {
   constexpr int QPT = kPlmQ;
+  __shared__ R sS[QPT][kTileCap];
+  __shared__ R sA[kTileCap];
+  __shared__ int rng[2];
+  const int item = blockIdx.x;
   const int q0 = blockIdx.y * QPT;
   const int d = dim - 1;
-  const int N = S.N;
-  int jk = S.cell_ring[c];
-  int j = jk % P.Nr, k = jk / P.Nr;
+  const int N = S.N, NF = S.nf[d];
+  const int jk = S.chunk_ring[item], i0 = S.chunk_i0[item];
+  const int off = S.ring_off[jk], Np = S.ring_off[jk + 1] - off;
+  const int i1 = min(Np, i0 + kTileCells);
+  const int i = i0 + threadIdx.x;
+  const bool valid = i < i1;
+  const int c = off + i;
+  const int k = div_fast(jk, P.mul_nr), j = jk - k * P.Nr;
   R* grad = dim == 1 ? S.gradr : S.gradz;
   R PLM = (R)P.PLM;
   if (P.PLM == 0.0) {
+    if (valid)
 #pragma unroll
-    for (int t = 0; t < QPT; ++t)
-      if (q0 + t < NQ) grad[(q0 + t) * N + c] = 0;
+      for (int t = 0; t < QPT; ++t)
+        if (q0 + t < NQ) grad[(q0 + t) * N + c] = 0;
     return;
   }
-  R sum[QPT], minpos[QPT], maxneg[QPT];
-  unsigned anypos = 0, anyneg = 0, anyzero = 0;
-  R pc[QPT], gpc[QPT];
+  // the limiter needs only the extremes of PLM S over the faces: for g > 0 it
+  // is zero if any PLM S <= 0, else min(g, min PLM S); for g < 0 symmetric
+  R sum[QPT], mn[QPT], mx[QPT];
 #pragma unroll
   for (int t = 0; t < QPT; ++t) {
-    sum[t] = 0; minpos[t] = 0; maxneg[t] = 0; pc[t] = 0; gpc[t] = 0;
-    if (q0 + t < NQ) { pc[t] = S.prim[(q0 + t) * N + c]; gpc[t] = S.gradp[(q0 + t) * N + c]; }
+    sum[t] = 0;
+    mn[t] = (R)INFINITY;
+    mx[t] = -(R)INFINITY;
   }
 
-  auto visit = [&](int f, int other, bool self_is_L, R dxsum, R idxsum, R dOm) {
-    R dpL = S.fdpL[d][f], dpR = S.fdpR[d][f];
-    R dA = S.fdA[d][f];
+  for (int side = 0; side < 2; ++side) {   // pair below (cell is R), then above (cell is L)
+    const int p = side == 0 ? pair_below(P, dim, j, k) : pair_above(P, dim, j, k);
+    if (p < 0) continue;                    // uniform over the block (one ring)
+    const int base = S.face_off[d][p], Nf = S.face_off[d][p + 1] - base;
+    const int* rs = side == 0 ? S.run_dn_s[d] : S.run_up_s[d];
+    const int* re = side == 0 ? S.run_dn_e[d] : S.run_up_e[d];
+    if (threadIdx.x == 0) {
+      int st = rs[off + i0], en = re[off + i1 - 1];
+      int dd = en - st;
+      if (dd < 0) dd += Nf;
+      rng[0] = st;
+      rng[1] = dd + 1;
+    }
+    __syncthreads();
+    const int st = rng[0], cnt = rng[1];
+    const bool tiled = cnt <= kTileCap;
+    if (tiled) {
+      for (int t = threadIdx.x; t < cnt; t += kTileCells) {
+        int f = st + t;
+        if (f >= base + Nf) f -= Nf;
+        sA[t] = S.fdA[d][f];
 #pragma unroll
-    for (int t = 0; t < QPT; ++t) {
-      const int q = q0 + t;
-      if (q >= NQ) break;
-      R po = S.prim[q * N + other], gpo = S.gradp[q * N + other];
-      R WL, WR;
-      if (self_is_L) { WL = pc[t] + dpL * gpc[t]; WR = po - dpR * gpo; }
-      else { WL = po + dpL * gpo; WR = pc[t] - dpR * gpc[t]; }
-      R Sl;
-      if constexpr (kMix<R>) Sl = ((WR - WL) + (q == UPP ? dOm : (R)0)) * idxsum;   // frames of the rings
-      else Sl = (WR - WL) / dxsum;
-      sum[t] += Sl * dA;
-      R ps = PLM * Sl;
-      if (Sl > (R)0) {
-        if (!(anypos >> t & 1u) || ps < minpos[t]) minpos[t] = ps;
-        anypos |= 1u << t;
-      } else if (Sl < (R)0) {
-        if (!(anyneg >> t & 1u) || ps > maxneg[t]) maxneg[t] = ps;
-        anyneg |= 1u << t;
-      } else {
-        anyzero |= 1u << t;
+        for (int u = 0; u < QPT; ++u)
+          if (q0 + u < NQ) sS[u][t] = S.fslope[(q0 + u) * NF + f];
       }
     }
-  };
-
-  int pb = pair_below(P, dim, j, k);
-  int pa = pair_above(P, dim, j, k);
-  if (pb >= 0) {
-    int base = S.face_off[d][pb], Nf = S.face_off[d][pb + 1] - base;
-    R dxs = S.pdxs[d][pb], idxs = kMix<R> ? S.pidxs[d][pb] : (R)0;
-    R dOm = kMix<R> ? S.pdOm[d][pb] : (R)0;
-    for_run(S.run_dn_s[d][c], S.run_dn_e[d][c], base, Nf,
-            [&](int f) { visit(f, S.fL[d][f], false, dxs, idxs, dOm); });
+    __syncthreads();
+    if (valid) {
+      for_run(rs[c], re[c], base, Nf, [&](int f) {
+        int o = f - st;
+        if (o < 0) o += Nf;
+        R dA = tiled ? sA[o] : S.fdA[d][f];
+#pragma unroll
+        for (int t = 0; t < QPT; ++t) {
+          const int q = q0 + t;
+          if (q >= NQ) break;
+          R Sl = tiled ? sS[t][o] : S.fslope[q * NF + f];
+          sum[t] += Sl * dA;
+          R ps = PLM * Sl;
+          mn[t] = ps < mn[t] ? ps : mn[t];
+          mx[t] = ps > mx[t] ? ps : mx[t];
+        }
+      });
+    }
+    __syncthreads();
   }
-  if (pa >= 0) {
-    int base = S.face_off[d][pa], Nf = S.face_off[d][pa + 1] - base;
-    R dxs = S.pdxs[d][pa], idxs = kMix<R> ? S.pidxs[d][pa] : (R)0;
-    R dOm = kMix<R> ? S.pdOm[d][pa] : (R)0;
-    for_run(S.run_up_s[d][c], S.run_up_e[d][c], base, Nf,
-            [&](int f) { visit(f, S.fR[d][f], true, dxs, idxs, dOm); });
-  }
+  if (!valid) return;
 
   // total weight, plm.c:113-143
   R dAt, idAt = 0;
@@ -784,15 +836,15 @@ __global__ void k_plm_trans(DevParams P, DevState<R> S, int dim) {
     if constexpr (kMix<R>) g = sum[t] * idAt;
     else g = sum[t] / dAt;
     if (g > (R)0) {
-      if ((anyneg >> t & 1u) || (anyzero >> t & 1u)) g = 0;
-      else if ((anypos >> t & 1u) && minpos[t] < g) g = minpos[t];
+      if (!(mn[t] > (R)0)) g = 0;
+      else if (mn[t] < g) g = mn[t];
     } else if (g < (R)0) {
-      if ((anypos >> t & 1u) || (anyzero >> t & 1u)) g = 0;
-      else if ((anyneg >> t & 1u) && maxneg[t] > g) g = maxneg[t];
+      if (!(mx[t] < (R)0)) g = 0;
+      else if (mx[t] > g) g = mx[t];
     }
     if (geom_bd) {  // plm_geom_boundary + geom_grad, cylindrical.c:141-173
       if (q == URR || (P.num_c > BZZ && q == BRR)) {
-        R SL = pc[t] / rcen;
+        R SL = S.prim[q * N + c] / rcen;
         if (g * SL < (R)0) g = 0;
         else if (fabs(PLM * SL) < fabs(g)) g = PLM * SL;
       } else {
@@ -809,7 +861,7 @@ __global__ void k_flux_phi(DevParams P, DevState<R> S, double fac) {
   int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= S.N) return;
   int jk = S.cell_ring[c];
-  int j = jk % P.Nr, k = jk / P.Nr;
+  int k = div_fast(jk, P.mul_nr), j = jk - k * P.Nr;
   if (S.ct ? !ring_in_phi_range(P, j, k) : !is_real(P, j, k)) return;
   const int N = S.N;
   int off = S.ring_off[jk], Np = S.ring_off[jk + 1] - off;
@@ -980,7 +1032,7 @@ __global__ void k_update(DevParams P, DevState<R> S, double RK, double fac, int 
   if (c >= S.N) return;
   const int N = S.N;
   int jk = S.cell_ring[c];
-  int j = jk % P.Nr, k = jk / P.Nr;
+  int k = div_fast(jk, P.mul_nr), j = jk - k * P.Nr;
   int off = S.ring_off[jk], Np = S.ring_off[jk + 1] - off;
   int i = c - off;
   const double* rj = S.r_jph + 1;
@@ -1191,7 +1243,7 @@ __global__ void k_boundary(DevParams P, DevState<R> S) {
   int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= S.N) return;
   int jk = S.cell_ring[c];
-  int j = jk % P.Nr, k = jk / P.Nr;
+  int k = div_fast(jk, P.mul_nr), j = jk - k * P.Nr;
   bool rghost = (j < P.NgRa) || (j >= P.Nr - P.NgRb);
   bool zghost = (k < P.NgZa) || (k >= P.Nz - P.NgZb);
   const double* rj = S.r_jph + 1;
@@ -1226,7 +1278,7 @@ __global__ void k_mindt(DevParams P, DevState<R> S) {
   float dtf = 3.0e38f;
   if (c < S.N) {
     int jk = S.cell_ring[c];
-    int j = jk % P.Nr, k = jk / P.Nr;
+    int k = div_fast(jk, P.mul_nr), j = jk - k * P.Nr;
     if (is_real(P, j, k)) {
       int off = S.ring_off[jk], Np = S.ring_off[jk + 1] - off;
       int i = c - off;
@@ -1308,7 +1360,7 @@ __global__ void k_c2p(DevParams P, DevState<R> S) {
   if (c >= S.N) return;
   const int N = S.N;
   int jk = S.cell_ring[c];
-  int j = jk % P.Nr, k = jk / P.Nr;
+  int k = div_fast(jk, P.mul_nr), j = jk - k * P.Nr;
   if (!is_real(P, j, k)) return;
   double U[NQ];
 #pragma unroll
@@ -1347,7 +1399,7 @@ __global__ void k_init_cells(DevParams P, DevState<R> S, const double* prim0, in
   if (c >= S.N) return;
   const int N = S.N;
   int jk = S.cell_ring[c];
-  int j = jk % P.Nr, k = jk / P.Nr;
+  int k = div_fast(jk, P.mul_nr), j = jk - k * P.Nr;
   if (!is_real(P, j, k)) {
 #pragma unroll
     for (int q = 0; q < NQ; ++q) { S.prim[q * N + c] = (R)0; S.cons[q * N + c] = 0; }

@@ -44,7 +44,7 @@ __global__ void k_mindt_blocks(DevParams P, DevState<R> S, unsigned long long* p
   float dtf = 3.0e38f;
   if (c < S.N) {
     int jk = S.cell_ring[c];
-    int j = jk % P.Nr, k = jk / P.Nr;
+    int k = div_fast(jk, P.mul_nr), j = jk - k * P.Nr;
     if (is_real(P, j, k)) {
       int off = S.ring_off[jk], Np = S.ring_off[jk + 1] - off;
       int i = c - off;
