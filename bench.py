@@ -166,6 +166,8 @@ def kernel_bytes(name: str, N: int, nf: dict, nq: int, sw: int, ct: bool) -> flo
         return N * (5 * f8 + 3 * f8 + sw + 4 * ix) + nfa * (sw + 1 + 2 * ix)
     if name == "c2p":
         return N * (nq * f8 + nq * sw + sw + f8)
+    if name == "ct_b2c_c2p":
+        return kernel_bytes("ct_b2c", N, nf, nq, sw, ct) + kernel_bytes("c2p", N, nf, nq, sw, ct)
     if name == "update":
         return N * (3 * nq * f8 + 2 * nq * sw + 5 * f8 + sw + 8 * ix) + nfa * nq * sw
     if name in ("faces_r", "faces_z"):

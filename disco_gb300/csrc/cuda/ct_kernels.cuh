@@ -550,9 +550,8 @@ __global__ void k_ct_flip(DevParams P, DevState<R> S, CtStateT<R> C, int dim) {
 
 // ---- B_faces_to_cells type 1 (bfields.c:88-309): cell B from face fluxes ---------
 template <typename R, int NQ>
-__global__ void k_ct_b2c(DevParams P, DevState<R> S, CtStateT<R> C, int prim_out) {
-  int c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= S.N) return;
+DISCO_D void ct_b2c_cell(const DevParams& P, const DevState<R>& S, const CtStateT<R>& C, int c,
+                         int prim_out) {
   const int N = S.N;
   int jk = S.cell_ring[c];
   int k = div_fast(jk, P.mul_nr), j = jk - k * P.Nr;
@@ -636,6 +635,27 @@ __global__ void k_ct_b2c(DevParams P, DevState<R> S, CtStateT<R> C, int prim_out
     S.cons[BPP * N + c] = Bphi * dV / (dA * hp);
     if (P.Nz > 1) S.cons[BZZ * N + c] = sums[1] * (dV * 1.0 / (areas[1] * 1.0));
   }
+}
+
+
+template <typename R, int NQ>
+__global__ void k_ct_b2c(DevParams P, DevState<R> S, CtStateT<R> C, int prim_out) {
+  int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= S.N) return;
+  ct_b2c_cell<R, NQ>(P, S, C, c, prim_out);
+}
+
+// B_faces_to_cells then calc_prim of the same real cell (onestep.c:285-296),
+// one pass over the conserved state instead of two.
+template <typename Phys, typename R, int NQ>
+__global__ void k_ct_b2c_c2p(DevParams P, DevState<R> S, CtStateT<R> C) {
+  int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= S.N) return;
+  int jk = S.cell_ring[c];
+  int k = div_fast(jk, P.mul_nr), j = jk - k * P.Nr;
+  if (!is_real(P, j, k)) return;
+  ct_b2c_cell<R, NQ>(P, S, C, c, 0);
+  c2p_cell<Phys, R, NQ>(P, S, c, jk, j, k);
 }
 
 // ---- set_B_fields (bfields.c:13-86): face fluxes of the initial field ------------

@@ -488,8 +488,7 @@ struct Instance : InstanceBase {
       if (first)
         for (int d = 0; d < 2; ++d)
           if (npair[d]) LAUNCH("ct_flip", (k_ct_flip<R><<<npair[d], 256, flip_smem(d), st>>>(P, S, C, d + 1)));
-      LAUNCH("ct_b2c", (k_ct_b2c<R, NQ><<<blocks(N), 256, 0, st>>>(P, S, C, 0)));
-      LAUNCH("c2p", (k_c2p<Phys, R, NQ><<<blocks(N), 256, 0, st>>>(P, S)));
+      LAUNCH("ct_b2c_c2p", (k_ct_b2c_c2p<Phys, R, NQ><<<blocks(N), 256, 0, st>>>(P, S, C)));
     }
     launch_boundary();
     if (first) launch_faces();

@@ -1355,13 +1355,8 @@ static __global__ void k_after_first(DevParams P, double* scal, DevPlanet* pl, i
 
 // ---- calc_prim (misc.c:300-335) as its own pass (after B_faces_to_cells) --------
 template <typename Phys, typename R, int NQ>
-__global__ void k_c2p(DevParams P, DevState<R> S) {
-  int c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= S.N) return;
+DISCO_D void c2p_cell(const DevParams& P, const DevState<R>& S, int c, int jk, int j, int k) {
   const int N = S.N;
-  int jk = S.cell_ring[c];
-  int k = div_fast(jk, P.mul_nr), j = jk - k * P.Nr;
-  if (!is_real(P, j, k)) return;
   double U[NQ];
 #pragma unroll
   for (int q = 0; q < NQ; ++q) U[q] = S.cons[q * N + c];
@@ -1390,6 +1385,16 @@ __global__ void k_c2p(DevParams P, DevState<R> S) {
   if (bad) atomicAdd(&S.errs->nan_cells, 1ull);
   if (hits & 1) atomicAdd(&S.errs->rho_floor_hits, 1ull);
   if (hits & 2) atomicAdd(&S.errs->p_floor_hits, 1ull);
+}
+
+template <typename Phys, typename R, int NQ>
+__global__ void k_c2p(DevParams P, DevState<R> S) {
+  int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= S.N) return;
+  int jk = S.cell_ring[c];
+  int k = div_fast(jk, P.mul_nr), j = jk - k * P.Nr;
+  if (!is_real(P, j, k)) return;
+  c2p_cell<Phys, R, NQ>(P, S, c, jk, j, k);
 }
 
 // ---- set-up: prim2cons + cons2prim for real cells (domain.c:349, :379) ---------
