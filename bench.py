@@ -64,6 +64,19 @@ DEFAULT_WORKLOAD = "mhd_disk3d"
 L2_BYTES = 126 * 1024 * 1024
 
 
+def _traffic_table() -> dict:
+    """DRAM bytes per launch at full size from the committed ncu summary
+    (lines `traffic <kernel> <bytes>` in profiles/*_dram_per_launch.md)."""
+    out = {}
+    import glob
+    for path in glob.glob(os.path.join(ROOT, "profiles", "*_dram_per_launch.md")):
+        for ln in open(path):
+            parts = ln.split()
+            if len(parts) == 3 and parts[0] == "traffic":
+                out[(os.path.basename(path).split("_dram")[0], parts[1])] = float(parts[2])
+    return out
+
+
 def _peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -144,9 +157,12 @@ def kernel_bytes(name: str, N: int, nf: dict, nq: int, sw: int, ct: bool) -> flo
     c = 1 if ct else 0
     if name == "plm_phi":
         return N * (2 * nq * sw + sw)
-    if name.startswith("plm_trans"):
+    if name.startswith("plm_slopes"):   # per face: indices, offsets, slopes out
         d = name[-1]
-        return N * (3 * nq * sw + sw + 4 * ix) + nf[d] * (3 * sw + 2 * ix)
+        return N * 2 * nq * sw + nf[d] * (2 * ix + 2 * sw + nq * sw)
+    if name.startswith("plm_trans"):    # per cell: runs, gradient out; per face: slopes, area
+        d = name[-1]
+        return N * (nq * sw + sw + 4 * ix) + nf[d] * (nq * sw + sw)
     if name == "flux_phi":
         return N * (3 * nq * sw + sw + 2 * f8 + c * 16 * sw)
     if name in ("flux_r", "flux_z"):
@@ -530,8 +546,11 @@ def main():
     top_bytes = kernel_bytes(top[0], N, nf, nq, sw, ct)
     top_avg_s = top[2] / top[1] / 1e3
     achieved = top_bytes / top_avg_s / 1e9
+    traffic = _traffic_table().get((args.workload, top[0]))
     roof = {"bound": "hbm", "kernel": top[0], "achieved": achieved, "peak": hbm, "unit": "GB/s",
-            "frac": achieved / hbm, "peak_kind": peak_kind, "traffic": None,
+            "frac": achieved / hbm, "peak_kind": peak_kind, "traffic": traffic,
+            "traffic_source": ("ncu dram__bytes_read.sum + dram__bytes_write.sum of one full-size "
+                               "launch, profiles/%s_dram_per_launch.md" % args.workload) if traffic else None,
             "algorithmic_bytes_per_launch": top_bytes,
             "share_of_step": top[2] / tot_prof}
     # fused-RK2 compulsory bytes per zone-update: NQ (4 s_W + 6 s_U) + 6 x 8,
