@@ -736,8 +736,8 @@ static void solve_riemann(const double *primL, const double *primR, double *cons
 {
    int nq = D->nq, q;
    double Flux[MAXQ] = {0}, Ustr[MAXQ] = {0};
-   int solver = D->par.Riemann_Solver;
-   if(solver == 0 || solver == 1) {
+   int solver = D->par.Riemann_Solver;   /* 0 HLL, 1 HLLC, 2 HLLD, 3 HLLC with HLL for r < 0.1 */
+   if(solver == 0 || solver == 1 || solver == 3) {
       double Sl, Sr, Ss;
       e_vel(primL, primR, &Sl, &Sr, &Ss, n, x);
       if(w < Sl) {
@@ -746,7 +746,7 @@ static void solve_riemann(const double *primL, const double *primR, double *cons
       } else if(w > Sr) {
          flux(primR, Flux, x, n);
          prim2cons(primR, Ustr, x, 1.0);
-      } else if(solver == 0) {
+      } else if(solver == 0 || (x[0] < 0.1 && solver == 3)) {
          double Fl[MAXQ], Fr[MAXQ], Ul[MAXQ], Ur[MAXQ];
          double aL = Sr, aR = -Sl;
          prim2cons(primL, Ul, x, 1.0);
@@ -1513,6 +1513,30 @@ static void boundary(void)
       }
    }
 }
+/* rotframe.c:32-80 (cylindrical: the rpz / orthonormal conversions reduce
+ * to the scale factor r on the phi component) */
+static void omega_src(const double *prim, double *cons, const double *xp, const double *xm,
+                      double dVdt)
+{
+   double x[3];
+   centroid_arr(xp, xm, x);
+   double r = x[0], phi = x[1];
+   double O = D->par.RotOmega, d = D->par.RotD;
+   double rho = prim[RHO];
+   double v0 = prim[URR], v1 = prim[UPP]*r, v2 = prim[UZZ];
+   double vr = v0, vom = v1/r;
+   double Rr = r - d*cos(phi), Rp = d*sin(phi);
+   double f0 = O*O*Rr + 2.*O*r*vom;
+   double f1 = O*O*Rp - 2.*O*vr;
+   double f2 = 0.0;
+   v1 -= r*get_om(x);
+   double vf = v0*f0 + v1*f1 + v2*f2;
+   f1 *= r;
+   cons[SRR] += rho*f0*dVdt;
+   cons[LLL] += rho*f1*dVdt;
+   cons[SZZ] += rho*f2*dVdt;
+   cons[TAU] += rho*vf*dVdt;
+}
 static void add_source(double dt)
 {
    for(int k = D->NgZa; k < D->Nz - D->NgZb; k++) for(int j = D->NgRa; j < D->Nr - D->NgRb; j++) {
@@ -1527,6 +1551,7 @@ static void add_source(double dt)
          for(int p = 0; p < D->Npl; p++) planet_src(&D->pl[p], c->prim, c->cons, xp, xm, dV*dt);
          if(D->par.visc_flag && !D->mhd)
             e_visc_source(c->prim, c->gradr, c->gradp, c->gradz, c->cons, xp, xm, dV*dt);
+         if(D->par.RotFrame) omega_src(c->prim, c->cons, xp, xm, dV*dt);
       }
    }
 }

@@ -34,6 +34,10 @@ CASES = {
     "cfg1_hll_static": ("configs/cfg1_vortex", {"Num_R": 24, "Riemann_Solver": 0, "Mesh_Motion": 0}, 10),
     "cfg1_exact_mesh": ("configs/cfg1_vortex", {"Num_R": 24, "Mesh_Motion": 4, "Exact_Mesh_Omega": 2,
                                                  "PLM": 1.0}, 10),
+    # rotating frame with an off-centre axis and a Keplerian energy frame;
+    # HLLC with the small-radius HLL switch
+    "cfg1_rotframe": ("configs/cfg1_vortex", {"Num_R": 24, "RotFrame": 1, "RotOmega": 0.3, "RotD": 0.1,
+                                               "Energy_Omega": 2, "Riemann_Solver": 3}, 10),
     # one instance of the planet-disk batch: alpha viscosity, locally
     # isothermal, a planet on a circular orbit
     "cfg3_n24": ("configs/cfg3_planet_disk", {"Num_R": 24}, 10),

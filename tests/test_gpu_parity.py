@@ -14,6 +14,7 @@ pytestmark = pytest.mark.gpu
 
 CASES = {"cfg1_n24": "configs/cfg1_vortex", "cfg2_n12": "configs/cfg2_mhd_disk",
          "cfg1_hll_static": "configs/cfg1_vortex", "cfg1_exact_mesh": "configs/cfg1_vortex",
+         "cfg1_rotframe": "configs/cfg1_vortex",
          "cfg3_n24": "configs/cfg3_planet_disk"}
 
 

@@ -22,10 +22,12 @@ def _port_run(par_path, mk, nsteps):
     return h, d.state()
 
 
-@pytest.mark.parametrize("name", ["cfg1_n24", "cfg1_hll_static", "cfg1_exact_mesh", "cfg3_n24"])
+@pytest.mark.parametrize("name", ["cfg1_n24", "cfg1_hll_static", "cfg1_exact_mesh", "cfg1_rotframe",
+                                  "cfg3_n24"])
 def test_port_bit_exact_vs_golden(name):
     """Hydro cases: HLLC vortex, HLL on a static mesh, exact Keplerian mesh
-    rotation, and the planet disk with alpha viscosity."""
+    rotation, rotating frame with a Keplerian energy frame (HLLC with the
+    centre switch), and the planet disk with alpha viscosity."""
     g = load_golden(name)
     h, s = _port_run(write_par(g["par_text"]), os.path.join(ROOT, str(g["cfg"]), "Makefile_opt.in"),
                      int(g["nsteps"]))
