@@ -156,7 +156,12 @@ struct Instance : InstanceBase {
     CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
     Nr = dom->Nr; Nz = dom->Nz; nring = Nr * Nz;
     N = dom->Ncell;
-    if (N > 0x7fffffffL) { disco_set_error("too many cells for int32 indexing"); return DISCO_E_ARG; }
+    // cell-component indices q*N + c are int32: NQ*N must stay below 2^31
+    // (face-component indices use 64-bit products)
+    if ((long long)N * dom->num_q >= 0x7fffffffLL) {
+      disco_set_error("too many cells for int32 cell-component indexing (num_q * Ncell >= 2^31)");
+      return DISCO_E_ARG;
+    }
     // ---- parameters (set*Params pushes, domain.c:259-270)
     P.Nr = Nr; P.Nz = Nz; P.NgRa = dom->NgRa; P.NgRb = dom->NgRb; P.NgZa = dom->NgZa; P.NgZb = dom->NgZb;
     P.Ncell = N; P.num_q = dom->num_q; P.num_c = dom->mod.num_c; P.phi_max = dom->phi_max;

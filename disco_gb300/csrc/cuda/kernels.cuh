@@ -178,7 +178,8 @@ DISCO_D void initial_eval(const DevParams& P, double* prim, const double* x) {
     disco_ic_disk_from_params(&D, P.gamma_law, P.mach, P.ic[0], P.ic[1], P.ic[2], P.ic[3],
                               P.ic[4], P.ic[5]);
     if (P.initial_id == 1) disco_ic_disk_mhd_eval(&D, prim, x, P.num_c, P.num_q);
-    else disco_ic_disk_planet_eval(&D, prim, x, P.num_c, P.num_q);
+    else if (P.initial_id == 2) disco_ic_disk_planet_eval(&D, prim, x, P.num_c, P.num_q);
+    else disco_ic_disk_cbd_eval(&D, prim, x, P.num_c, P.num_q);
   }
   if (P.rot_flag) prim[UPP] -= P.rot_omega;   // subtract_omega, rotframe.c:15
 }
@@ -695,7 +696,7 @@ __global__ void k_plm_slopes(DevParams P, DevState<R> S, int dim) {
     R Sl;
     if constexpr (kMix<R>) Sl = ((WR - WL) + (q == UPP ? dOm : (R)0)) * idxs;   // frames of the rings
     else Sl = (WR - WL) / dxs;
-    S.fslope[q * NF + f] = Sl;
+    S.fslope[(size_t)q * NF + f] = Sl;
   }
 }
 
@@ -771,7 +772,7 @@ __global__ void __launch_bounds__(kTileCells) k_plm_trans(DevParams P, DevState<
         sA[t] = S.fdA[d][f];
 #pragma unroll
         for (int u = 0; u < QPT; ++u)
-          if (q0 + u < NQ) sS[u][t] = S.fslope[(q0 + u) * NF + f];
+          if (q0 + u < NQ) sS[u][t] = S.fslope[(size_t)(q0 + u) * NF + f];
       }
     }
     __syncthreads();
@@ -784,7 +785,7 @@ __global__ void __launch_bounds__(kTileCells) k_plm_trans(DevParams P, DevState<
         for (int t = 0; t < QPT; ++t) {
           const int q = q0 + t;
           if (q >= NQ) break;
-          R Sl = tiled ? sS[t][o] : S.fslope[q * NF + f];
+          R Sl = tiled ? sS[t][o] : S.fslope[(size_t)q * NF + f];
           sum[t] += Sl * dA;
           R ps = PLM * Sl;
           mn[t] = ps < mn[t] ? ps : mn[t];
@@ -1014,7 +1015,7 @@ __global__ void k_flux_trans(DevParams P, DevState<R> S, int dim, int jmin, int 
   if constexpr (kMix<R>) dAdt = S.fdA[d][f] * ((R)fac * dt_r<R>(S.scal));
   else dAdt = S.fdA[d][f] * (R)(fac * S.scal[SC_DT]);
 #pragma unroll
-  for (int q = 0; q < NQ; ++q) out[q * NF + f] = Fw[q] * dAdt;
+  for (int q = 0; q < NQ; ++q) out[(size_t)q * NF + f] = Fw[q] * dAdt;
   if (S.ct) {
     R E1, B1, E2, B2;
     Phys::flux_to_E(Fl, Us, r, &E1, &B1, &E2, &B2, dim);
@@ -1103,14 +1104,14 @@ __global__ void k_update(DevParams P, DevState<R> S, double RK, double fac, int 
         int base = S.face_off[d][pb], Nf = S.face_off[d][pb + 1] - base;
         for_run(S.run_dn_s[d][c], S.run_dn_e[d][c], base, Nf, [&](int f) {
 #pragma unroll
-          for (int q = 0; q < NQ; ++q) add(q, Fb[q * NF + f]);
+          for (int q = 0; q < NQ; ++q) add(q, Fb[(size_t)q * NF + f]);
         });
       }
       if (pa >= 0) {
         int base = S.face_off[d][pa], Nf = S.face_off[d][pa + 1] - base;
         for_run(S.run_up_s[d][c], S.run_up_e[d][c], base, Nf, [&](int f) {
 #pragma unroll
-          for (int q = 0; q < NQ; ++q) add(q, -Fb[q * NF + f]);
+          for (int q = 0; q < NQ; ++q) add(q, -Fb[(size_t)q * NF + f]);
         });
       }
     }
@@ -1342,8 +1343,16 @@ static __global__ void k_dt_finalize(DevParams P, double* scal) {
 static __global__ void k_after_first(DevParams P, double* scal, DevPlanet* pl, int planets_id,
                               DevErrs* errs) {
   double dt = scal[SC_DT];
+  double t = scal[SC_T];   // movePlanets sees the time before the step's update
   scal[SC_T] += dt;
   if (planets_id == 2 && P.Npl > 1) pl[1].phi += pl[1].omega * dt;
+  if (planets_id == 3 && P.Npl > 1) {   // Planets/cm.c:53-59
+    pl[0].phi += pl[0].omega * dt;
+    pl[1].phi += pl[1].omega * dt;
+    double eps = 0.5 / P.mach + exp(-t / 30.);
+    pl[0].eps = eps;
+    pl[1].eps = eps;
+  }
   for (int p = 0; p < P.Npl; ++p) {
     double phi = pl[p].phi;
     while (phi > P.phi_max) phi -= P.phi_max;

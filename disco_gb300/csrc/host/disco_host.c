@@ -228,15 +228,15 @@ int disco_modules_read(const char *path, disco_modules *m)
    if(bad) { disco_set_error("Makefile_opt.in: missing module key"); return DISCO_E_PARFILE; }
 
    static const char *hyd[] = {"euler", "mhd"};
-   static const char *ini[] = {"vortex_gauss", "disk_mhd", "disk_planet"};
+   static const char *ini[] = {"vortex_gauss", "disk_mhd", "disk_planet", "disk_cbd"};
    static const char *bnd[] = {"fixed", "fixed3d", "outflow3d", "zerograd"};
-   static const char *pla[] = {"none", "sun", "circular"};
+   static const char *pla[] = {"none", "sun", "circular", "cm"};
    int i;
    m->hydro = m->initial = m->boundary = m->planets = -1;
    for(i = 0; i < 2; i++) if(!strcmp(m->hydro_name, hyd[i])) m->hydro = i;
-   for(i = 0; i < 3; i++) if(!strcmp(m->initial_name, ini[i])) m->initial = i;
+   for(i = 0; i < 4; i++) if(!strcmp(m->initial_name, ini[i])) m->initial = i;
    for(i = 0; i < 4; i++) if(!strcmp(m->boundary_name, bnd[i])) m->boundary = i;
-   for(i = 0; i < 3; i++) if(!strcmp(m->planets_name, pla[i])) m->planets = i;
+   for(i = 0; i < 4; i++) if(!strcmp(m->planets_name, pla[i])) m->planets = i;
    char msg[256];
    if(m->hydro < 0) { snprintf(msg, sizeof msg, "HYDRO=%s not built", m->hydro_name); disco_set_error(msg); return DISCO_E_MODULE; }
    if(m->initial < 0) { snprintf(msg, sizeof msg, "INITIAL=%s not built", m->initial_name); disco_set_error(msg); return DISCO_E_MODULE; }
@@ -279,6 +279,16 @@ static void setup_planets(disco_host_domain *d)
       d->planets[1].r = 1.0;
       d->planets[1].eps = 0.5/p->Disk_Mach;
       break;
+   case DISCO_PL_CM: {       /* Planets/cm.c:7-50: binary about its centre of mass */
+      double a = 1.0, q = p->Mass_Ratio, mu = q/(1. + q), om = pow(a, -1.5);
+      double smooth = 0.5/p->Disk_Mach;
+      d->Npl = 2;
+      d->planets[0].M = 1. - mu; d->planets[0].omega = om; d->planets[0].r = a*mu;
+      d->planets[0].phi = M_PI; d->planets[0].eps = smooth;
+      d->planets[1].M = mu; d->planets[1].omega = om; d->planets[1].r = a*(1. - mu);
+      d->planets[1].phi = 0.0; d->planets[1].eps = smooth;
+      break;
+   }
    }
 }
 
@@ -321,6 +331,14 @@ static void ic_eval(const disco_host_domain *d, double *prim, const double *x)
                                 p->initPar2, p->initPar3, p->initPar4, p->initPar5,
                                 p->initPar6);
       disco_ic_disk_planet_eval(&P, prim, x, nc, nq);
+      break;
+   }
+   case DISCO_IC_DISK_CBD: {
+      struct disco_ic_disk P;
+      disco_ic_disk_from_params(&P, p->Adiabatic_Index, p->Disk_Mach, p->initPar1,
+                                p->initPar2, p->initPar3, p->initPar4, p->initPar5,
+                                p->initPar6);
+      disco_ic_disk_cbd_eval(&P, prim, x, nc, nq);
       break; }
    }
    if(p->RotFrame) prim[3] -= p->RotOmega;   /* subtract_omega, rotframe.c:15 */

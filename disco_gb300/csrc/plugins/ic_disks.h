@@ -91,4 +91,56 @@ DISCO_HD static inline void disco_ic_disk_planet_eval(
    for(q = num_c; q < num_q; q++) prim[q] = r < P->par3 ? 1.0 : 0.0;
 }
 
+/* splitmix64 (Steele, Lea, Flood 2014), for the seeded phases below. */
+DISCO_HD static inline unsigned long long disco_splitmix64(unsigned long long x)
+{
+   unsigned long long z = x + 0x9E3779B97F4A7C15ULL;
+   z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+   z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+   return z ^ (z >> 31);
+}
+
+/*
+ * disk_cbd: 3D circumbinary MHD disk around a total mass 1.
+ *   rho = max(r^-1 exp(-(r_cav/r)^n) exp(-z^2/(2H^2)) (1 + a dn(phi, r)), rho_atm),
+ *   H = r/Mach, P = rho c_s^2 / gamma with c_s^2 = 1/(r Mach^2),
+ *   Omega^2 = r^-3 (1 - 2/Mach^2), toroidal field B_phi = sqrt(2 P / beta).
+ *   dn is a smooth seeded perturbation: the mean of cos(m phi + p_m) sin(m' ln r + q_m)
+ *   over m = 1..8, with the phases p_m, q_m drawn by splitmix64 seeded m.
+ * Parameters: Init_Par1 = r_cav, Init_Par2 = beta (0 = no field),
+ * Init_Par3 = passive-scalar radius, Init_Par4 = cavity steepness n,
+ * Init_Par5 = perturbation amplitude a, Init_Par6 = rho_atm.
+ */
+DISCO_HD static inline void disco_ic_disk_cbd_eval(
+      const struct disco_ic_disk *P, double *prim, const double *x,
+      int num_c, int num_q)
+{
+   double r = x[0], phi = x[1], z = x[2];
+   double M2 = P->mach*P->mach;
+   double cs2 = 1.0/(r*M2);
+   double H = r/P->mach;
+   double dn = 0.0;
+   int m;
+   for(m = 1; m <= 8; m++) {
+      double pm = 6.283185307179586*(double)(disco_splitmix64((unsigned long long)m) >> 11)*0x1.0p-53;
+      double qm = 6.283185307179586*(double)(disco_splitmix64((unsigned long long)(m + 100)) >> 11)*0x1.0p-53;
+      dn += cos(m*phi + pm)*sin(3.0*m*log(r) + qm);
+   }
+   dn *= 0.125;
+   double rho = exp(-pow(P->par1/r, P->par4))*exp(-0.5*z*z/(H*H))*(1.0 + P->par5*dn)/r;
+   if(rho < P->par6) rho = P->par6;
+   double Pp = rho*cs2/P->gam;
+   double omega = sqrt((1.0 - 2.0/M2)/(r*r*r));
+   double Bp = 0.0;
+   if(P->par2 > 0.0) Bp = sqrt(2.0*Pp/P->par2);
+   prim[0] = rho;
+   prim[1] = Pp;
+   prim[2] = 0.0;
+   prim[3] = omega;
+   prim[4] = 0.0;
+   if(num_c > 5) { prim[5] = 0.0; prim[6] = Bp; prim[7] = 0.0; }
+   int q;
+   for(q = num_c; q < num_q; q++) prim[q] = r < P->par3 ? 1.0 : 0.0;
+}
+
 #endif

@@ -49,11 +49,11 @@ enum disco_status_code {
 /* Module ids selected by name from Makefile_opt.in (Makefile:12-26). */
 enum disco_hydro_id   { DISCO_HYDRO_EULER = 0, DISCO_HYDRO_MHD = 1 };
 enum disco_initial_id { DISCO_IC_VORTEX_GAUSS = 0, DISCO_IC_DISK_MHD = 1,
-                        DISCO_IC_DISK_PLANET = 2 };
+                        DISCO_IC_DISK_PLANET = 2, DISCO_IC_DISK_CBD = 3 };
 enum disco_boundary_id{ DISCO_BC_FIXED = 0, DISCO_BC_FIXED3D = 1,
                         DISCO_BC_OUTFLOW3D = 2, DISCO_BC_ZEROGRAD = 3 };
 enum disco_planets_id { DISCO_PL_NONE = 0, DISCO_PL_SUN = 1,
-                        DISCO_PL_CIRCULAR = 2 };
+                        DISCO_PL_CIRCULAR = 2, DISCO_PL_CM = 3 };
 
 #define DISCO_MAX_PLANETS 4
 #define DISCO_NUM_G 2   /* ghost rings per side: paul.h:20 NUM_G */

@@ -1485,7 +1485,8 @@ static void initial(double *prim, const double *x)
       disco_ic_disk_from_params(&Dk, p->Adiabatic_Index, p->Disk_Mach, p->initPar1, p->initPar2,
                                 p->initPar3, p->initPar4, p->initPar5, p->initPar6);
       if(D->mod.initial == DISCO_IC_DISK_MHD) disco_ic_disk_mhd_eval(&Dk, prim, x, D->nc, D->nq);
-      else disco_ic_disk_planet_eval(&Dk, prim, x, D->nc, D->nq);
+      else if(D->mod.initial == DISCO_IC_DISK_PLANET) disco_ic_disk_planet_eval(&Dk, prim, x, D->nc, D->nq);
+      else disco_ic_disk_cbd_eval(&Dk, prim, x, D->nc, D->nq);
    }
    if(p->RotFrame) prim[UPP] -= p->RotOmega;
 }
@@ -1578,6 +1579,13 @@ static void onestep(double RK, double dt, int first)
       for(c = 0; c < D->N; c++) D->cells[c].piph += D->cells[c].wiph*dt;
       /* movePlanets (Planets/circular.c:44-46) for the analytic orbit */
       if(D->mod.planets == DISCO_PL_CIRCULAR && D->Npl > 1) D->pl[1].phi += D->pl[1].omega*dt;
+      if(D->mod.planets == DISCO_PL_CM && D->Npl > 1) {   /* Planets/cm.c:53-59 */
+         D->pl[0].phi += D->pl[0].omega*dt;
+         D->pl[1].phi += D->pl[1].omega*dt;
+         double eps = 0.5/D->par.Disk_Mach + exp(-D->t/30.);
+         D->pl[0].eps = eps;
+         D->pl[1].eps = eps;
+      }
       if(D->mhd) {
          check_flipped(0); flip_fluxes(0);
          if(D->Nz > 1) { check_flipped(1); flip_fluxes(1); }

@@ -29,6 +29,9 @@ from dumpio import read_dump  # noqa: E402
 CASES = {
     "cfg1_n24": ("configs/cfg1_vortex", {"Num_R": 24}, 10),
     "cfg2_n12": ("configs/cfg2_mhd_disk", {"Num_R": 12, "Num_Z": 6}, 5),
+    # the circumbinary MHD disk (binary about its centre of mass, cavity,
+    # toroidal field, seeded density perturbations) at 16 x 8 rings
+    "cfg5_n16": ("configs/cfg5_cbd_mhd", {"Num_R": 16, "Num_Z": 8}, 5),
     # solver / mesh-motion variants of the vortex: HLL on a static mesh, and
     # HLLC with the exact Keplerian mesh rotation and a different PLM theta
     "cfg1_hll_static": ("configs/cfg1_vortex", {"Num_R": 24, "Riemann_Solver": 0, "Mesh_Motion": 0}, 10),
