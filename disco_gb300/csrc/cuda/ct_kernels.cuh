@@ -25,7 +25,7 @@ struct CtStateT {
 
 // ---- RK adjust of Phi + edge gathers (riemann.c:172-212) --------------------
 template <typename R>
-__global__ void k_ct_gather(DevParams P, DevState<R> S, CtStateT<R> C, double RK, int first) {
+__global__ void __launch_bounds__(256, kMix<R> ? 6 : 1) k_ct_gather(DevParams P, DevState<R> S, CtStateT<R> C, double RK, int first) {
   int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= S.N) return;
   const int N = S.N;

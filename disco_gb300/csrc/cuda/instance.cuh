@@ -481,7 +481,7 @@ struct Instance : InstanceBase {
       LAUNCH("ct_avg", (k_ct_avg<R><<<blocks(N), 256, 0, st>>>(P, S, C)));
       LAUNCH("ct_bflux", (k_ct_bflux<R><<<blocks(N), 256, 0, st>>>(P, S, C, fac)));
       if (Nz > 1)
-        LAUNCH("ct_edge", (k_ct_edge<R><<<(Nr - 1) * (Nz - 1), 256, edge_smem, st>>>(P, S, C, fac)));
+        LAUNCH("ct_edge", (k_ct_edge<R><<<(Nr - 1) * (Nz - 1), 512, edge_smem, st>>>(P, S, C, fac)));
     }
     LAUNCH("update", (k_update<Phys, R, NQ><<<blocks(N), 256, 0, st>>>(P, S, RK, fac, first, ct ? 0 : 1)));
     if (first) {
@@ -659,7 +659,7 @@ struct Instance : InstanceBase {
     if (stage >= 2) LAUNCH("ct_avg", (k_ct_avg<R><<<blocks(N), 256, 0, st>>>(P, S, C)));
     if (stage >= 3) LAUNCH("ct_bflux", (k_ct_bflux<R><<<blocks(N), 256, 0, st>>>(P, S, C, fac)));
     if (stage >= 4 && Nz > 1)
-      LAUNCH("ct_edge", (k_ct_edge<R><<<(Nr - 1) * (Nz - 1), 256, edge_smem, st>>>(P, S, C, fac)));
+      LAUNCH("ct_edge", (k_ct_edge<R><<<(Nr - 1) * (Nz - 1), 512, edge_smem, st>>>(P, S, C, fac)));
     CK(cudaStreamSynchronize(st));
     CK(cudaGetLastError());
     auto fetch = [&](double* dst, const R* src, size_t n) -> int {

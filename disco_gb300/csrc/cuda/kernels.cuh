@@ -701,7 +701,7 @@ __global__ void k_plm_slopes(DevParams P, DevState<R> S, int dim) {
 }
 
 // The components are independent: blockIdx.y selects a group of QPT of them.
-constexpr int kPlmQ = 5;        // components per thread in k_plm_trans
+constexpr int kPlmQ = 9;        // components per thread in k_plm_trans (one group for NQ <= 9)
 constexpr int kTileCells = 128; // cells per block of a tiled face gather
 constexpr int kTileCap = 4 * kTileCells;   // faces staged per side
 template <int NQ>
@@ -856,9 +856,13 @@ __global__ void __launch_bounds__(kTileCells) k_plm_trans(DevParams P, DevState<
   }
 }
 
+// Occupancy: on the mixed path the flux and update kernels are capped at
+// 64 registers per thread (4 blocks of 256 per SM), measured faster than
+// their natural 70+; the FP64 versions would spill, so they are not capped.
+
 // ---- phi fluxes, misc.c:378-436 + riemann_phi, riemann.c:39-112 -------------
 template <typename Phys, typename R, int NQ>
-__global__ void k_flux_phi(DevParams P, DevState<R> S, double fac) {
+__global__ void __launch_bounds__(256, kMix<R> ? 4 : 1) k_flux_phi(DevParams P, DevState<R> S, double fac) {
   int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= S.N) return;
   int jk = S.cell_ring[c];
@@ -947,7 +951,7 @@ __global__ void k_flux_phi(DevParams P, DevState<R> S, double fac) {
 // ---- r/z fluxes, misc.c:441-519 + riemann_trans, riemann.c:114-214 ----------
 // Grid: x = pair within the active range, y = chunk of 256 faces.
 template <typename Phys, typename R, int NQ>
-__global__ void k_flux_trans(DevParams P, DevState<R> S, int dim, int jmin, int jcount, int kmin,
+__global__ void __launch_bounds__(256, kMix<R> ? 4 : 1) k_flux_trans(DevParams P, DevState<R> S, int dim, int jmin, int jcount, int kmin,
                              double fac) {
   const int d = dim - 1;
   int pj = jmin + (int)blockIdx.x % jcount;
@@ -1028,7 +1032,7 @@ __global__ void k_flux_trans(DevParams P, DevState<R> S, int dim, int jmin, int 
 // the reference's order, add_source (misc.c:550), move_cells/clean_pi/calc_dp
 // (misc.c:266, :8, :281), calc_prim (misc.c:300).
 template <typename Phys, typename R, int NQ>
-__global__ void k_update(DevParams P, DevState<R> S, double RK, double fac, int first, int do_c2p) {
+__global__ void __launch_bounds__(256, kMix<R> ? 4 : 1) k_update(DevParams P, DevState<R> S, double RK, double fac, int first, int do_c2p) {
   int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= S.N) return;
   const int N = S.N;
