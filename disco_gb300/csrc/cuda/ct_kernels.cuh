@@ -21,6 +21,14 @@ struct CtStateT {
   R* Ephi;          // [4*N]
   unsigned long long* errs;  // [0] edge-order mismatches
   int last_pair[2]; // index of the last pair of each dimension (skipped by update_B_fluxes)
+  // edge-walk events of the last walk (make_edge_adjust): the four cells,
+  // the branch bits and the edge length, replayed by the next step's first
+  // substep, whose positions are the same (nullptr: no cache)
+  int4* ev_cid;
+  unsigned char* ev_flag;   // bit 0-1 w4, bit 2 LR_alt, bit 3 UD_alt, bit 7 valid
+  R* ev_dl;
+  const int* quad_ev_off;   // [quads + 1]: first event of each quad
+  int* ev_ok;               // device flag: the cache matches the current positions
 };
 
 // ---- RK adjust of Phi + edge gathers (riemann.c:172-212) --------------------
@@ -318,10 +326,64 @@ DISCO_D int get_which4(double phi, double phiR, double phiU, double phiUR, int* 
   return w4;
 }
 
+// The four face fluxes an edge event adjusts and its averaged E_phi
+// (bfields.c:955-1110): from the ring that advanced (w4), the two branch
+// bits and the four current cells (c, cR, cU, cUR).
 template <typename R>
-__global__ void k_ct_edge(DevParams P, DevState<R> S, CtStateT<R> C, double fac) {
+DISCO_D void edge_targets(const CtStateT<R>& C, int N, int w4, int LR_alt, int UD_alt, int c, int cR,
+                          int cU, int cUR, double** PL, double** PR, double** PU, double** PD, R* Eo) {
+  const R* Ep = C.Ephi;
+  R E;
+  double *PhiL, *PhiR, *PhiU, *PhiD;
+  double* Ph = C.Phi;
+  if (w4 == 0) {
+    PhiL = Ph + 4 * N + c; PhiD = Ph + 2 * N + c;
+    E = (R).25 * (Ep[3 * N + c] + Ep[1 * N + c]);
+    if (LR_alt == 0) { PhiU = Ph + 2 * N + cU; E += (R).25 * Ep[1 * N + cU]; }
+    else { PhiU = Ph + 1 * N + cUR; E += (R).25 * Ep[0 * N + cUR]; }
+    if (UD_alt == 0) { PhiR = Ph + 4 * N + cR; E += (R).25 * Ep[3 * N + cR]; }
+    else { PhiR = Ph + 3 * N + cUR; E += (R).25 * Ep[2 * N + cUR]; }
+  } else if (w4 == 1) {
+    PhiR = Ph + 4 * N + cR; PhiD = Ph + 1 * N + cR;
+    E = (R).25 * (Ep[3 * N + cR] + Ep[0 * N + cR]);
+    if (LR_alt == 0) { PhiU = Ph + 2 * N + cU; E += (R).25 * Ep[1 * N + cU]; }
+    else { PhiU = Ph + 1 * N + cUR; E += (R).25 * Ep[0 * N + cUR]; }
+    if (UD_alt == 0) { PhiL = Ph + 4 * N + c; E += (R).25 * Ep[3 * N + c]; }
+    else { PhiL = Ph + 3 * N + cU; E += (R).25 * Ep[2 * N + cU]; }
+  } else if (w4 == 2) {
+    PhiL = Ph + 3 * N + cU; PhiU = Ph + 2 * N + cU;
+    E = (R).25 * (Ep[2 * N + cU] + Ep[1 * N + cU]);
+    if (LR_alt == 0) { PhiD = Ph + 2 * N + c; E += (R).25 * Ep[1 * N + c]; }
+    else { PhiD = Ph + 1 * N + cR; E += (R).25 * Ep[0 * N + cR]; }
+    if (UD_alt == 0) { PhiR = Ph + 4 * N + cR; E += (R).25 * Ep[3 * N + cR]; }
+    else { PhiR = Ph + 3 * N + cUR; E += (R).25 * Ep[2 * N + cUR]; }
+  } else {
+    PhiR = Ph + 3 * N + cUR; PhiU = Ph + 1 * N + cUR;
+    E = (R).25 * (Ep[2 * N + cUR] + Ep[0 * N + cUR]);
+    if (LR_alt == 0) { PhiD = Ph + 2 * N + c; E += (R).25 * Ep[1 * N + c]; }
+    else { PhiD = Ph + 1 * N + cR; E += (R).25 * Ep[0 * N + cR]; }
+    if (UD_alt == 0) { PhiL = Ph + 4 * N + c; E += (R).25 * Ep[3 * N + c]; }
+    else { PhiL = Ph + 3 * N + cU; E += (R).25 * Ep[2 * N + cU]; }
+  }
+  *PL = PhiL; *PR = PhiR; *PU = PhiU; *PD = PhiD; *Eo = E;
+}
+
+// E dl dt of one event (FP64 on the FP64 path, R on the mixed path).
+template <typename R>
+DISCO_D double edge_edldt(R E, R dl, R dtf, double dt) {
+  if constexpr (kMix<R>) return (double)(E * (dl * dtf));
+  else return (double)E * dl * dt;
+}
+
+// mode 0: always walk; mode 1: walk only if the cache is stale (first
+// substep); mode 2: walk and record the events for the next step.
+template <typename R>
+__global__ void k_ct_edge(DevParams P, DevState<R> S, CtStateT<R> C, double fac, int mode) {
   extern __shared__ double sm[];
+  if (mode == 1 && C.ev_ok && *C.ev_ok) return;
+  const bool cache = mode == 2 && C.ev_cid != nullptr;
   int q = blockIdx.x;   // quad (j, k): rings j, j+1 at layers k, k+1
+  const long ev0 = cache ? (long)C.quad_ev_off[q] : 0;
   int k = div_fast(q, P.mul_nr1), j = q - k * (P.Nr - 1);
   const int N = S.N;
   int ring[4] = {j + P.Nr * k, j + 1 + P.Nr * k, j + P.Nr * (k + 1), j + 1 + P.Nr * (k + 1)};
@@ -363,8 +425,8 @@ __global__ void k_ct_edge(DevParams P, DevState<R> S, CtStateT<R> C, double fac)
   };
   double dt = fac * S.scal[SC_DT];
   const double rjj = S.r_jph[j + 1];
-  R dlfac = 0;
-  if constexpr (kMix<R>) dlfac = (R)rjj * ((R)fac * dt_r<R>(S.scal));
+  R dtf = 0;
+  if constexpr (kMix<R>) dtf = (R)fac * dt_r<R>(S.scal);
   for (int t = threadIdx.x; t < tot; t += blockDim.x) {
     int rx = t >= base[3] ? 3 : t >= base[2] ? 2 : t >= base[1] ? 1 : 0;
     int m = t - pick(base, rx);
@@ -431,54 +493,57 @@ __global__ void k_ct_edge(DevParams P, DevState<R> S, CtStateT<R> C, double fac)
       xp1 = w4 == 0 ? pp[0] : w4 == 1 ? pp[1] : w4 == 2 ? pp[2] : pp[3];
       xm1 = w4b == 0 ? pb[0] : w4b == 1 ? pb[1] : w4b == 2 ? pb[2] : pb[3];
     }
-    if (w4 != rx) { atomicAdd(C.errs, 1ull); continue; }
+    if (w4 != rx) {
+      atomicAdd(C.errs, 1ull);
+      if (cache) C.ev_flag[ev0 + t] = 0;
+      continue;
+    }
     int c = cid[0], cR = cid[1], cU = cid[2], cUR = cid[3];
-    const R* Ep = C.Ephi;
     R E;
     double *PhiL, *PhiR, *PhiU, *PhiD;
-    double* Ph = C.Phi;
-    if (w4 == 0) {
-      PhiL = Ph + 4 * N + c; PhiD = Ph + 2 * N + c;
-      E = (R).25 * (Ep[3 * N + c] + Ep[1 * N + c]);
-      if (LR_alt == 0) { PhiU = Ph + 2 * N + cU; E += (R).25 * Ep[1 * N + cU]; }
-      else { PhiU = Ph + 1 * N + cUR; E += (R).25 * Ep[0 * N + cUR]; }
-      if (UD_alt == 0) { PhiR = Ph + 4 * N + cR; E += (R).25 * Ep[3 * N + cR]; }
-      else { PhiR = Ph + 3 * N + cUR; E += (R).25 * Ep[2 * N + cUR]; }
-    } else if (w4 == 1) {
-      PhiR = Ph + 4 * N + cR; PhiD = Ph + 1 * N + cR;
-      E = (R).25 * (Ep[3 * N + cR] + Ep[0 * N + cR]);
-      if (LR_alt == 0) { PhiU = Ph + 2 * N + cU; E += (R).25 * Ep[1 * N + cU]; }
-      else { PhiU = Ph + 1 * N + cUR; E += (R).25 * Ep[0 * N + cUR]; }
-      if (UD_alt == 0) { PhiL = Ph + 4 * N + c; E += (R).25 * Ep[3 * N + c]; }
-      else { PhiL = Ph + 3 * N + cU; E += (R).25 * Ep[2 * N + cU]; }
-    } else if (w4 == 2) {
-      PhiL = Ph + 3 * N + cU; PhiU = Ph + 2 * N + cU;
-      E = (R).25 * (Ep[2 * N + cU] + Ep[1 * N + cU]);
-      if (LR_alt == 0) { PhiD = Ph + 2 * N + c; E += (R).25 * Ep[1 * N + c]; }
-      else { PhiD = Ph + 1 * N + cR; E += (R).25 * Ep[0 * N + cR]; }
-      if (UD_alt == 0) { PhiR = Ph + 4 * N + cR; E += (R).25 * Ep[3 * N + cR]; }
-      else { PhiR = Ph + 3 * N + cUR; E += (R).25 * Ep[2 * N + cUR]; }
-    } else {
-      PhiR = Ph + 3 * N + cUR; PhiU = Ph + 1 * N + cUR;
-      E = (R).25 * (Ep[2 * N + cUR] + Ep[0 * N + cUR]);
-      if (LR_alt == 0) { PhiD = Ph + 2 * N + c; E += (R).25 * Ep[1 * N + c]; }
-      else { PhiD = Ph + 1 * N + cR; E += (R).25 * Ep[0 * N + cR]; }
-      if (UD_alt == 0) { PhiL = Ph + 4 * N + c; E += (R).25 * Ep[3 * N + c]; }
-      else { PhiL = Ph + 3 * N + cU; E += (R).25 * Ep[2 * N + cU]; }
+    edge_targets<R>(C, N, w4, LR_alt, UD_alt, c, cR, cU, cUR, &PhiL, &PhiR, &PhiU, &PhiD, &E);
+    R dl;   // edge length r dphi (the phi extent wrapped in FP64)
+    if constexpr (kMix<R>) dl = (R)rjj * (R)get_dp(xp1, xm1, Pmax);
+    else dl = (.5 * (rjj + rjj)) * get_dp(xp1, xm1, Pmax);
+    if (cache) {
+      long e = ev0 + t;
+      C.ev_cid[e] = make_int4(c, cR, cU, cUR);
+      C.ev_flag[e] = (unsigned char)(w4 | (LR_alt << 2) | (UD_alt << 3) | 0x80);
+      C.ev_dl[e] = dl;
     }
-    double Edldt;
-    if constexpr (kMix<R>) {
-      Edldt = (double)(E * (dlfac * (R)get_dp(xp1, xm1, Pmax)));   // wrapped in FP64, then R
-    } else {
-      double dl = (.5 * (rjj + rjj)) * get_dp(xp1, xm1, Pmax);
-      Edldt = (double)E * dl * dt;
-    }
+    double Edldt = edge_edldt<R>(E, dl, dtf, dt);
     atomicAdd(PhiL, -Edldt);
     atomicAdd(PhiR, Edldt);
     atomicAdd(PhiU, -Edldt);
     atomicAdd(PhiD, Edldt);
   }
 }
+
+// Replay of the recorded edge events (first substep, cache current): the
+// same targets, average and edge length as the walk, from the current E_phi.
+template <typename R>
+__global__ void k_ct_edge_replay(DevParams P, DevState<R> S, CtStateT<R> C, double fac, long nev) {
+  if (!*C.ev_ok) return;
+  long e = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= nev) return;
+  unsigned fl = C.ev_flag[e];
+  if (!(fl & 0x80)) return;
+  int4 cc = C.ev_cid[e];
+  R E;
+  double *PhiL, *PhiR, *PhiU, *PhiD;
+  edge_targets<R>(C, S.N, fl & 3, (fl >> 2) & 1, (fl >> 3) & 1, cc.x, cc.y, cc.z, cc.w,
+                  &PhiL, &PhiR, &PhiU, &PhiD, &E);
+  double dt = fac * S.scal[SC_DT];
+  R dtf = 0;
+  if constexpr (kMix<R>) dtf = (R)fac * dt_r<R>(S.scal);
+  double Edldt = edge_edldt<R>(E, C.ev_dl[e], dtf, dt);
+  atomicAdd(PhiL, -Edldt);
+  atomicAdd(PhiR, Edldt);
+  atomicAdd(PhiU, -Edldt);
+  atomicAdd(PhiD, Edldt);
+}
+
+static __global__ void k_set_flag(int* f, int v) { *f = v; }
 
 // ---- check_flipped + flip_fluxes (bfields.c:693-814), first substep --------------
 // One block per pair; flags in parallel, then the sequential repair (rare).

@@ -128,6 +128,7 @@ struct Instance : InstanceBase {
   int planets_id = 0;
   cudaGraphExec_t graph[2] = {nullptr, nullptr};
   size_t edge_smem = 0;
+  long nev = 0;   // edge-walk events per substep (cache size)
   int maxring = 0;
   int graph_nodes = 0;
   double host_t = 0;
@@ -335,6 +336,33 @@ struct Instance : InstanceBase {
         if (flip_smem(d) > 48 * 1024)
           CK(raise_smem_limit(k_ct_flip<R>, flip_smem(d)));
       edge_smem = (size_t)4 * maxring * 8;
+      // edge-walk event cache: one event per cell of each quad's four rings
+      {
+        std::vector<int> qoff((size_t)(Nr - 1) * (Nz - 1) + 1, 0);
+        long tot = 0;
+        for (int k = 0; k + 1 < Nz; ++k)
+          for (int j = 0; j + 1 < Nr; ++j) {
+            int qd = j + (Nr - 1) * k;
+            qoff[qd] = (int)tot;
+            tot += dom->Np[j + Nr * k] + dom->Np[j + 1 + Nr * k] + dom->Np[j + Nr * (k + 1)] +
+                   dom->Np[j + 1 + Nr * (k + 1)];
+          }
+        qoff.back() = (int)tot;
+        nev = tot;
+        size_t need = (size_t)tot * (sizeof(int4) + 1 + sizeof(R));
+        size_t fr = 0, tt = 0;
+        cudaMemGetInfo(&fr, &tt);
+        A(&C.ev_ok, 1);
+        CK(cudaMemset(C.ev_ok, 0, sizeof(int)));
+        // kept only where it leaves room (8 GB) for the rest of the run
+        if (tot < 0x7fffffffL && fr > need + ((size_t)8 << 30)) {
+          int* d_q;
+          A(&d_q, qoff.size());
+          CK(cudaMemcpy(d_q, qoff.data(), sizeof(int) * qoff.size(), cudaMemcpyHostToDevice));
+          C.quad_ev_off = d_q;
+          A(&C.ev_cid, tot); A(&C.ev_flag, tot); A(&C.ev_dl, tot);
+        }
+      }
       if (edge_smem > 48 * 1024)
         CK(raise_smem_limit(k_ct_edge<R>, edge_smem));
     }
@@ -480,8 +508,16 @@ struct Instance : InstanceBase {
       LAUNCH("ct_gather", (k_ct_gather<R><<<blocks(N), 256, 0, st>>>(P, S, C, RK, first)));
       LAUNCH("ct_avg", (k_ct_avg<R><<<blocks(N), 256, 0, st>>>(P, S, C)));
       LAUNCH("ct_bflux", (k_ct_bflux<R><<<blocks(N), 256, 0, st>>>(P, S, C, fac)));
-      if (Nz > 1)
-        LAUNCH("ct_edge", (k_ct_edge<R><<<(Nr - 1) * (Nz - 1), 512, edge_smem, st>>>(P, S, C, fac)));
+      if (Nz > 1) {
+        // first substep: replay the events the last walk recorded (same
+        // positions) or walk if there are none; second substep: walk and
+        // record them for the next step
+        const int mode = C.ev_cid ? (first ? 1 : 2) : 0;
+        LAUNCH("ct_edge", (k_ct_edge<R><<<(Nr - 1) * (Nz - 1), 512, edge_smem, st>>>(P, S, C, fac, mode)));
+        if (C.ev_cid && first)
+          LAUNCH("ct_edge_replay", (k_ct_edge_replay<R><<<(int)((nev + 255) / 256), 256, 0, st>>>(P, S, C, fac, nev)));
+        if (C.ev_cid && !first) LAUNCH("ct_edge_flag", (k_set_flag<<<1, 1, 0, st>>>(C.ev_ok, 1)));
+      }
     }
     LAUNCH("update", (k_update<Phys, R, NQ><<<blocks(N), 256, 0, st>>>(P, S, RK, fac, first, ct ? 0 : 1)));
     if (first) {
@@ -644,6 +680,7 @@ struct Instance : InstanceBase {
   }
   int debug_ct(int stage, double* E, double* B, double* Ephi, double* Phi) override {
     if (!ct) { disco_set_error("debug_ct: not a CT instance"); return DISCO_E_STATE; }
+    if (C.ev_ok) CK(cudaMemsetAsync(C.ev_ok, 0, sizeof(int), st));
     P.t_end = 0.0;
     launch_mindt();
     const double RK = 0.0, fac = 1.0;
@@ -659,7 +696,7 @@ struct Instance : InstanceBase {
     if (stage >= 2) LAUNCH("ct_avg", (k_ct_avg<R><<<blocks(N), 256, 0, st>>>(P, S, C)));
     if (stage >= 3) LAUNCH("ct_bflux", (k_ct_bflux<R><<<blocks(N), 256, 0, st>>>(P, S, C, fac)));
     if (stage >= 4 && Nz > 1)
-      LAUNCH("ct_edge", (k_ct_edge<R><<<(Nr - 1) * (Nz - 1), 512, edge_smem, st>>>(P, S, C, fac)));
+      LAUNCH("ct_edge", (k_ct_edge<R><<<(Nr - 1) * (Nz - 1), 512, edge_smem, st>>>(P, S, C, fac, 0)));
     CK(cudaStreamSynchronize(st));
     CK(cudaGetLastError());
     auto fetch = [&](double* dst, const R* src, size_t n) -> int {
@@ -721,6 +758,7 @@ struct Instance : InstanceBase {
       CK(cudaMemcpy(S.prim, tmp.data(), sizeof(R) * NQ * N, cudaMemcpyHostToDevice));
     }
     if (v->dphi) sync_dphi_r();
+    if (ct && C.ev_ok) CK(cudaMemsetAsync(C.ev_ok, 0, sizeof(int), st));   // positions changed
     if (v->piph || v->dphi) launch_faces();
     CK(cudaStreamSynchronize(st));
     CK(cudaGetLastError());
