@@ -462,7 +462,7 @@ struct Instance : InstanceBase {
   void launch_plm_trans() {
     for (int d = 0; d < 2; ++d) {
       if (!npair[d]) continue;
-      dim3 grid(npair[d], (maxNf[d] + 255) / 256);
+      dim3 grid(npair[d], (maxNf[d] + 256 * kSlopeFaces - 1) / (256 * kSlopeFaces));
       LAUNCH(d == 0 ? "plm_slopes_r" : "plm_slopes_z",
              (k_plm_slopes<R, NQ><<<grid, 256, 0, st>>>(P, S, d + 1)));
       LAUNCH(d == 0 ? "plm_trans_r" : "plm_trans_z",

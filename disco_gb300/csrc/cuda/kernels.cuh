@@ -675,28 +675,33 @@ __global__ void k_pair_geom(DevParams P, DevState<R> S, int dim, int npair) {
 // (plm.c:146-179) reduces to: zero if any face slope has the opposite sign
 // (or is zero), else the smallest of |g| and |PLM S| -- a function of the
 // extremes of PLM S over the faces only, independent of face order.
+constexpr int kSlopeFaces = 4;   // faces per thread in k_plm_slopes (loads in flight)
+
 template <typename R, int NQ>
 __global__ void k_plm_slopes(DevParams P, DevState<R> S, int dim) {
   const int d = dim - 1;
   int pair = blockIdx.x;
   int base = S.face_off[d][pair], Nf = S.face_off[d][pair + 1] - base;
-  int n = blockIdx.y * blockDim.x + threadIdx.x;
-  if (n >= Nf) return;
-  int f = base + n;
   const int N = S.N, NF = S.nf[d];
-  int cL = S.fL[d][f], cR = S.fR[d][f];
-  R dpL = S.fdpL[d][f], dpR = S.fdpR[d][f];
   R dxs = S.pdxs[d][pair];
   R idxs = kMix<R> ? S.pidxs[d][pair] : (R)0;
   R dOm = kMix<R> ? S.pdOm[d][pair] : (R)0;
 #pragma unroll
-  for (int q = 0; q < NQ; ++q) {
-    R WL = S.prim[q * N + cL] + dpL * S.gradp[q * N + cL];
-    R WR = S.prim[q * N + cR] - dpR * S.gradp[q * N + cR];
-    R Sl;
-    if constexpr (kMix<R>) Sl = ((WR - WL) + (q == UPP ? dOm : (R)0)) * idxs;   // frames of the rings
-    else Sl = (WR - WL) / dxs;
-    S.fslope[(size_t)q * NF + f] = Sl;
+  for (int u = 0; u < kSlopeFaces; ++u) {
+    int n = (blockIdx.y * kSlopeFaces + u) * blockDim.x + threadIdx.x;
+    if (n >= Nf) break;
+    int f = base + n;
+    int cL = S.fL[d][f], cR = S.fR[d][f];
+    R dpL = S.fdpL[d][f], dpR = S.fdpR[d][f];
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) {
+      R WL = S.prim[q * N + cL] + dpL * S.gradp[q * N + cL];
+      R WR = S.prim[q * N + cR] - dpR * S.gradp[q * N + cR];
+      R Sl;
+      if constexpr (kMix<R>) Sl = ((WR - WL) + (q == UPP ? dOm : (R)0)) * idxs;   // frames of the rings
+      else Sl = (WR - WL) / dxs;
+      S.fslope[(size_t)q * NF + f] = Sl;
+    }
   }
 }
 
