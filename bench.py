@@ -177,11 +177,11 @@ def kernel_bytes(name: str, N: int, nf: dict, nq: int, sw: int, ct: bool) -> flo
         d = name[-1]
         return N * 3 * nq * sw + nf[d] * (2 * ix + f8 + 3 * sw + nq * sw + c * 3 * sw)
     if name == "ct_gather":
-        return N * (15 * f8 + 36 * sw + 4 * ix) + nfa * 5 * sw
+        return N * (36 * sw + 4 * ix) + nfa * 5 * sw
     if name == "ct_avg":
         return N * (20 * sw + f8 + 4 * ix) + nfa * 2 * sw
-    if name == "ct_bflux":
-        return N * (4 * sw + 10 * f8 + 4 * ix)
+    if name == "ct_bflux":   # incl. the RK adjustment of Phi (RKPhi read or written)
+        return N * (4 * sw + 15 * f8 + 4 * ix)
     if name == "ct_edge":
         return N * (f8 + 4 * sw + 10 * f8)
     if name == "ct_flip":

@@ -31,18 +31,12 @@ struct CtStateT {
   int* ev_ok;               // device flag: the cache matches the current positions
 };
 
-// ---- RK adjust of Phi + edge gathers (riemann.c:172-212) --------------------
+// ---- edge gathers (riemann.c:172-212) ------------------------------------------
 template <typename R>
-__global__ void __launch_bounds__(256, kMix<R> ? 6 : 1) k_ct_gather(DevParams P, DevState<R> S, CtStateT<R> C, double RK, int first) {
+__global__ void __launch_bounds__(256, kMix<R> ? 6 : 1) k_ct_gather(DevParams P, DevState<R> S, CtStateT<R> C) {
   int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= S.N) return;
   const int N = S.N;
-#pragma unroll
-  for (int q = 0; q < 5; ++q) {
-    double ph = C.Phi[q * N + c];
-    if (first) C.RKPhi[q * N + c] = ph;
-    else C.Phi[q * N + c] = (1. - RK) * ph + RK * C.RKPhi[q * N + c];
-  }
   int jk = S.cell_ring[c];
   int k = div_fast(jk, P.mul_nr), j = jk - k * P.Nr;
   if (!ring_in_phi_range(P, j, k)) return;
@@ -157,8 +151,8 @@ __global__ void k_ct_avg(DevParams P, DevState<R> S, CtStateT<R> C) {
   if constexpr (kMix<R>) {
     // E_lab - h w B = X + s h ((w - Om_own) B_own + (w - Om_other) B_other),
     // all frame differences small and exact to FP32 rounding
-    R wrel = (R)(S.wiph[c] - S.ring_Om[jk]);
-    R hL = (R)rj[j - 1], hR = (R)rj[j], hC = S.ring_rc_r[jk];
+    R wrel = to_r<R>(S.wiph[c] - S.ring_Om[jk]);
+    R hL = to_r<R>(rj[j - 1]), hR = to_r<R>(rj[j]), hC = S.ring_rc_r[jk];
     const R h[4] = {hL, hR, hC, hC};
     const R sg[4] = {(R)-1, (R)-1, (R)1, (R)1};
 #pragma unroll
@@ -192,12 +186,13 @@ DISCO_D R face_emf(const DevState<R>& S, const CtStateT<R>& C, int d, int f) {
 // the FP64 flux once (the FP64 path below keeps the reference's terms).
 template <typename R>
 DISCO_D void ct_bflux_mixed(const DevParams& P, const DevState<R>& S, const CtStateT<R>& C,
-                            double fac, int c) {
+                            double fac, int c, double* ph) {
   const int N = S.N;
   int jk = S.cell_ring[c];
   int k = div_fast(jk, P.mul_nr), j = jk - k * P.Nr;
-  R dtf = (R)fac * dt_r<R>(S.scal);
+  R dtf = to_r<R>(fac) * dt_r<R>(S.scal);
   R dph0 = 0;
+#pragma unroll
   for (int dim = 1; dim <= 2; ++dim) {
     if (dim == 1 && P.Nr <= 1) continue;
     if (dim == 2 && P.Nz <= 1) continue;
@@ -212,7 +207,7 @@ DISCO_D void ct_bflux_mixed(const DevParams& P, const DevState<R>& S, const CtSt
       R Eg = face_emf(S, C, d, g);
       int slot = dim == 1 ? 1 : 3;
       R dv = dim == 1 ? (Eg - Ef) * dldt : (Ef - Eg) * dldt;
-      C.Phi[slot * N + c] += (double)dv;
+      ph[slot] += from_r<R>(dv);
       dph0 += dim == 1 ? -Ef * dldt : Ef * dldt;
     }
     if (pa >= 0 && pa != C.last_pair[d]) {
@@ -223,28 +218,43 @@ DISCO_D void ct_bflux_mixed(const DevParams& P, const DevState<R>& S, const CtSt
       R Eg = face_emf(S, C, d, g);
       int slot = dim == 1 ? 2 : 4;
       R dv = dim == 1 ? (Eg - Ef) * dldt : (Ef - Eg) * dldt;
-      C.Phi[slot * N + c] += (double)dv;
+      ph[slot] += from_r<R>(dv);
       dph0 += dim == 1 ? Ef * dldt : -Ef * dldt;
     }
   }
-  C.Phi[0 * N + c] += (double)dph0;
+  ph[0] += from_r<R>(dph0);
 }
 
+// The RK adjustment of the face fluxes (Phi -> (1 - RK) Phi + RK RKPhi, or
+// RKPhi = Phi on the first substep) is done here, in registers, before the
+// circulation terms: nothing reads Phi between the edge gathers and this
+// kernel, so one pass over Phi serves both.
 template <typename R>
-__global__ void k_ct_bflux(DevParams P, DevState<R> S, CtStateT<R> C, double fac) {
+__global__ void k_ct_bflux(DevParams P, DevState<R> S, CtStateT<R> C, double fac, double RK, int first) {
   int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= S.N) return;
+  const int N = S.N;
+  double ph[5];
+#pragma unroll
+  for (int q = 0; q < 5; ++q) {
+    double v = C.Phi[q * N + c];
+    if (first) C.RKPhi[q * N + c] = v;
+    else v = (1. - RK) * v + RK * C.RKPhi[q * N + c];
+    ph[q] = v;
+  }
   if constexpr (kMix<R>) {
-    ct_bflux_mixed<R>(P, S, C, fac, c);
+    ct_bflux_mixed<R>(P, S, C, fac, c, ph);
+#pragma unroll
+    for (int q = 0; q < 5; ++q) C.Phi[q * N + c] = ph[q];
     return;
   }
-  const int N = S.N;
   int jk = S.cell_ring[c];
   int k = div_fast(jk, P.mul_nr), j = jk - k * P.Nr;
   double dt = fac * S.scal[SC_DT];
   const double* rj = S.r_jph + 1;
   const double* zk = S.z_kph + 1;
-  double ph0 = C.Phi[0 * N + c];
+  double ph0 = ph[0];
+#pragma unroll
   for (int dim = 1; dim <= 2; ++dim) {
     if (dim == 1 && P.Nr <= 1) continue;
     if (dim == 2 && P.Nz <= 1) continue;
@@ -260,7 +270,7 @@ __global__ void k_ct_bflux(DevParams P, DevState<R> S, CtStateT<R> C, double fac
       double Ef = (double)C.Efin[(2 * d + 0) * N + c];
       double Eg = (double)face_emf(S, C, d, g);
       int slot = dim == 1 ? 1 : 3;
-      double v = C.Phi[slot * N + c];
+      double v = ph[slot];
       if (dim == 1) {
         if (f == base) { v -= Ef * dl * dt; v += Eg * dl * dt; }
         else { v += Eg * dl * dt; v -= Ef * dl * dt; }
@@ -269,7 +279,7 @@ __global__ void k_ct_bflux(DevParams P, DevState<R> S, CtStateT<R> C, double fac
         if (f == base) { v += Ef * dl * dt; v -= Eg * dl * dt; }
         else { v -= Eg * dl * dt; v += Ef * dl * dt; }
       }
-      C.Phi[slot * N + c] = v;
+      ph[slot] = v;
       if (dim == 2) ph0 += Ef * dl * dt;
     }
     if (pa >= 0 && pa != C.last_pair[d]) {
@@ -279,7 +289,7 @@ __global__ void k_ct_bflux(DevParams P, DevState<R> S, CtStateT<R> C, double fac
       double Ef = (double)C.Efin[(2 * d + 1) * N + c];
       double Eg = (double)face_emf(S, C, d, g);
       int slot = dim == 1 ? 2 : 4;
-      double v = C.Phi[slot * N + c];
+      double v = ph[slot];
       if (dim == 1) {
         if (f == base) { v -= Ef * dl * dt; v += Eg * dl * dt; }
         else { v += Eg * dl * dt; v -= Ef * dl * dt; }
@@ -289,11 +299,13 @@ __global__ void k_ct_bflux(DevParams P, DevState<R> S, CtStateT<R> C, double fac
         else { v -= Eg * dl * dt; v += Ef * dl * dt; }
         ph0 -= Ef * dl * dt;
       }
-      C.Phi[slot * N + c] = v;
+      ph[slot] = v;
     }
     (void)sgn;
   }
-  C.Phi[0 * N + c] = ph0;
+  ph[0] = ph0;
+#pragma unroll
+  for (int q = 0; q < 5; ++q) C.Phi[q * N + c] = ph[q];
 }
 
 // ---- make_edge_adjust (bfields.c:888-1127) -------------------------------------
@@ -371,7 +383,7 @@ DISCO_D void edge_targets(const CtStateT<R>& C, int N, int w4, int LR_alt, int U
 // E dl dt of one event (FP64 on the FP64 path, R on the mixed path).
 template <typename R>
 DISCO_D double edge_edldt(R E, R dl, R dtf, double dt) {
-  if constexpr (kMix<R>) return (double)(E * (dl * dtf));
+  if constexpr (kMix<R>) return from_r<R>(E * (dl * dtf));
   else return (double)E * dl * dt;
 }
 
@@ -426,7 +438,7 @@ __global__ void k_ct_edge(DevParams P, DevState<R> S, CtStateT<R> C, double fac,
   double dt = fac * S.scal[SC_DT];
   const double rjj = S.r_jph[j + 1];
   R dtf = 0;
-  if constexpr (kMix<R>) dtf = (R)fac * dt_r<R>(S.scal);
+  if constexpr (kMix<R>) dtf = to_r<R>(fac) * dt_r<R>(S.scal);
   for (int t = threadIdx.x; t < tot; t += blockDim.x) {
     int rx = t >= base[3] ? 3 : t >= base[2] ? 2 : t >= base[1] ? 1 : 0;
     int m = t - pick(base, rx);
@@ -535,7 +547,7 @@ __global__ void k_ct_edge_replay(DevParams P, DevState<R> S, CtStateT<R> C, doub
                   &PhiL, &PhiR, &PhiU, &PhiD, &E);
   double dt = fac * S.scal[SC_DT];
   R dtf = 0;
-  if constexpr (kMix<R>) dtf = (R)fac * dt_r<R>(S.scal);
+  if constexpr (kMix<R>) dtf = to_r<R>(fac) * dt_r<R>(S.scal);
   double Edldt = edge_edldt<R>(E, C.ev_dl[e], dtf, dt);
   atomicAdd(PhiL, -Edldt);
   atomicAdd(PhiR, Edldt);
@@ -635,7 +647,7 @@ DISCO_D void ct_b2c_cell(const DevParams& P, const DevState<R>& S, const CtState
       auto visit = [&](int f) {
         double ph = S.fLR[d][f] == 0 ? C.Phi[lo * N + S.fL[d][f]] : C.Phi[hi * N + S.fR[d][f]];
         areas[d] += S.fdA[d][f];
-        sums[d] += (R)ph;
+        sums[d] += to_r<R>(ph);
       };
       if (pb >= 0) {
         int base = S.face_off[d][pb], Nf = S.face_off[d][pb + 1] - base;
@@ -646,7 +658,7 @@ DISCO_D void ct_b2c_cell(const DevParams& P, const DevState<R>& S, const CtState
         for_run(S.run_up_s[d][c], S.run_up_e[d][c], base, Nf, visit);
       }
     }
-    R Bphi = (R).5 * (R)(C.Phi[c] + C.Phi[cm]);
+    R Bphi = (R).5 * to_r<R>(C.Phi[c] + C.Phi[cm]);
     R dA = S.ring_dA_r[jk];
     R x0 = S.ring_rc_r[jk];
     if (prim_out) {
@@ -655,9 +667,9 @@ DISCO_D void ct_b2c_cell(const DevParams& P, const DevState<R>& S, const CtState
       if (P.Nz > 1) S.prim[BZZ * N + c] = sums[1] / areas[1];
     } else {
       R dV = S.ring_vol_r[jk] * S.dphi_r[c];
-      S.cons[BRR * N + c] = (double)(sums[0] * (dV / (areas[0] * x0)));
-      S.cons[BPP * N + c] = (double)(Bphi * dV / (dA * x0));
-      if (P.Nz > 1) S.cons[BZZ * N + c] = (double)(sums[1] * (dV / areas[1]));
+      S.cons[BRR * N + c] = from_r<R>(sums[0] * (dV / (areas[0] * x0)));
+      S.cons[BPP * N + c] = from_r<R>(Bphi * dV / (dA * x0));
+      if (P.Nz > 1) S.cons[BZZ * N + c] = from_r<R>(sums[1] * (dV / areas[1]));
     }
     return;
   }

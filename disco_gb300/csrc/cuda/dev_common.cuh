@@ -55,7 +55,16 @@ struct DevParams {
   // exact division by Nr and Nr - 1 (ring and r-pair indices) by 40-bit
   // reciprocals: ceil(2^40 / d)
   unsigned long long mul_nr, mul_nr1;
+  // FP32 copies of the parameters the mixed-precision kernels use per cell
+  // or face (a conversion from FP64 would issue on the slow FP64 pipe)
+  struct {
+    float gamma_law, rho_floor, p_floor, explicit_viscosity, mach, PLM;
+    float Omega0, om_M, om_r1, om_H0, eps;
+  } f;
 };
+
+// A parameter in the arithmetic type R: the FP32 copy on the mixed path.
+#define PRM(R, P, x) (sizeof(R) < sizeof(double) ? (R)(P).f.x : (R)(P).x)
 
 // n / d for 0 <= n < 2^24 and 1 <= d < 2^16, given m = ceil(2^40 / d): the
 // rounding excess of m is below n / 2^40 < 2^-16 < 1 / d, so the floor is
@@ -63,6 +72,57 @@ struct DevParams {
 DISCO_HD inline int div_fast(int n, unsigned long long m) {
   return (int)(((unsigned long long)n * m) >> 40);
 }
+
+// FP64 <-> FP32 conversions on the integer pipes, without branches.  A
+// hardware conversion to or from FP64 issues on the FP64 pipe, which on this
+// part runs at a small fraction of the FP32 rate.  They are used where they
+// measured faster: conserved-state reads and writes in the update, in
+// cons2prim and in the constrained-transport flux kernels.  In the Riemann
+// flux kernels, whose FP64 pipe is mostly idle, the hardware conversion
+// measured faster and stays.
+//
+// d2f_int: in the normal FP32 range it rounds to nearest, ties away from
+// zero (IEEE's ties-to-even differs on exact ties only; the error is at most
+// half an ulp either way).  Results below the smallest normal FP32 number
+// flush to signed zero; overflow gives infinity, NaN stays NaN.
+#ifdef __CUDACC__
+__device__ inline float d2f_int(double x) {
+  unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  unsigned s = (unsigned)(b >> 32) & 0x80000000u;
+  unsigned long long a = b & 0x7fffffffffffffffull;
+  unsigned e = (unsigned)(a >> 52);
+  // add half an FP32 ulp, drop 29 mantissa bits, rebias the exponent by
+  // 1023 - 127 = 896 (a carry out of the mantissa lands in the exponent;
+  // the arithmetic is modulo 2^32 and the result fits in 31 bits)
+  unsigned m = (unsigned)((a + (1ull << 28)) >> 29) - (896u << 23);
+  unsigned big = (a > 0x7ff0000000000000ull) ? 0x7fc00000u : 0x7f800000u;
+  m = e < 897u ? 0u : (e > 1150u ? big : m);
+  return __uint_as_float(s | m);
+}
+// f2d_int: exact for normal FP32 numbers, zero, infinity and NaN; FP32
+// subnormals flush to signed zero.
+__device__ inline double f2d_int(float x) {
+  unsigned u = __float_as_uint(x);
+  unsigned s = u & 0x80000000u;
+  unsigned a = u & 0x7fffffffu;
+  unsigned e = a >> 23;
+  unsigned hi = (a >> 3) + (e == 255u ? (1792u << 20) : (896u << 20));
+  hi = e == 0u ? 0u : hi;
+  unsigned lo = e == 0u ? 0u : (a << 29);
+  return __hiloint2double((int)(s | hi), (int)lo);
+}
+// to_r: a double into the reconstruction type R (identity for R = double)
+template <typename R>
+__device__ inline R to_r(double x) {
+  if constexpr (sizeof(R) < sizeof(double)) return d2f_int(x);
+  else return x;
+}
+template <typename R>
+__device__ inline double from_r(R x) {
+  if constexpr (sizeof(R) < sizeof(double)) return f2d_int(x);
+  else return x;
+}
+#endif
 
 // ---- cylindrical geometry: Geometry/cylindrical.c ------------------------
 DISCO_HD inline double get_dp(double phip, double phim, double phi_max) {
@@ -85,7 +145,7 @@ DISCO_HD inline double centroid_z(double xp, double xm) { return 0.5 * (xp + xm)
 // ---- omega.c ----------------------------------------------------------------
 template <typename R>
 DISCO_D R mesh_om(const DevParams& P, R r) {           // omega.c:56-74
-  r = sqrt(r * r + (R)P.eps * (R)P.eps);
+  r = sqrt(r * r + PRM(R, P, eps) * PRM(R, P, eps));
   if (P.meshOmChoice == 1) return (R)1.0;
   if (P.meshOmChoice == 2) return pow(r, (R)-1.5);
   if (P.meshOmChoice == 3) { R n = 4.0; return (R)1. / pow(pow(r, (R)1.5 * n) + (R)1., (R)1. / n); }
@@ -93,18 +153,18 @@ DISCO_D R mesh_om(const DevParams& P, R r) {           // omega.c:56-74
 }
 template <typename R>
 DISCO_D R get_om(const DevParams& P, R r) {            // omega.c:76-100
-  if (P.enOmChoice == 0) return (R)0.0 - (R)P.Omega0;
-  r = sqrt(r * r + (R)P.eps * (R)P.eps);
-  if (P.enOmChoice == 1) return (R)1.0 - (R)P.Omega0;
-  if (P.enOmChoice == 2) return (R)1.0 / pow(r, (R)1.5) - (R)P.Omega0;
-  if (P.enOmChoice == 3) { R n = 8.0; return (R)1. / pow(pow(r, (R)1.5 * n) + (R)1., (R)1. / n) - (R)P.Omega0; }
-  if (P.enOmChoice == 4) return (R)10. * exp((R)-.5 * r * r) - (R)P.Omega0;
-  return (R)0.0 - (R)P.Omega0;
+  if (P.enOmChoice == 0) return (R)0.0 - PRM(R, P, Omega0);
+  r = sqrt(r * r + PRM(R, P, eps) * PRM(R, P, eps));
+  if (P.enOmChoice == 1) return (R)1.0 - PRM(R, P, Omega0);
+  if (P.enOmChoice == 2) return (R)1.0 / pow(r, (R)1.5) - PRM(R, P, Omega0);
+  if (P.enOmChoice == 3) { R n = 8.0; return (R)1. / pow(pow(r, (R)1.5 * n) + (R)1., (R)1. / n) - PRM(R, P, Omega0); }
+  if (P.enOmChoice == 4) return (R)10. * exp((R)-.5 * r * r) - PRM(R, P, Omega0);
+  return (R)0.0 - PRM(R, P, Omega0);
 }
 template <typename R>
 DISCO_D R get_om1(const DevParams& P, R r) {           // omega.c:102-126
   if (P.enOmChoice == 0 || P.enOmChoice == 1) return (R)0.0;
-  r = sqrt(r * r + (R)P.eps * (R)P.eps);
+  r = sqrt(r * r + PRM(R, P, eps) * PRM(R, P, eps));
   if (P.enOmChoice == 2) return (R)-1.5 / pow(r, (R)2.5);
   if (P.enOmChoice == 3) {
     R n = 8.0;
@@ -135,13 +195,13 @@ DISCO_D R fgrav(R M, R r, R eps, int type) {            // planet.c:75-112 (poin
 
 template <typename R>
 DISCO_D R get_cs2(const DevParams& P, const DevPlanet* pl, R r, R phi) {  // omega.c:157-209
-  if (P.cs2Choice == 1) return (R)1. / ((R)P.mach * (R)P.mach);
-  if (P.cs2Choice == 2) { R nu = .5; return (R).5 / (R)P.mach / (R)P.mach / pow(r, (R)2. * nu); }
-  if (P.cs2Choice == 3) return (R)P.om_M * (R)P.om_H0 * (R)P.om_H0 / ((R)2 * (R)P.om_r1 * (R)P.om_r1 * (R)P.om_r1);
+  if (P.cs2Choice == 1) return (R)1. / (PRM(R, P, mach) * PRM(R, P, mach));
+  if (P.cs2Choice == 2) { R nu = .5; return (R).5 / PRM(R, P, mach) / PRM(R, P, mach) / pow(r, (R)2. * nu); }
+  if (P.cs2Choice == 3) return PRM(R, P, om_M) * PRM(R, P, om_H0) * PRM(R, P, om_H0) / ((R)2 * PRM(R, P, om_r1) * PRM(R, P, om_r1) * PRM(R, P, om_r1));
   if (P.cs2Choice == 4) {
-    r = sqrt(r * r + (R)P.eps * (R)P.eps);
-    R v2 = (R)P.om_M / r;
-    return v2 / ((R)P.mach * (R)P.mach);
+    r = sqrt(r * r + PRM(R, P, eps) * PRM(R, P, eps));
+    R v2 = PRM(R, P, om_M) / r;
+    return v2 / (PRM(R, P, mach) * PRM(R, P, mach));
   }
   if (P.cs2Choice == 5) {
     R cosp = cos(phi), sinp = sin(phi);
@@ -153,7 +213,7 @@ DISCO_D R get_cs2(const DevParams& P, const DevPlanet* pl, R r, R phi) {  // ome
       R pr = (px - gx) * (px - gx) + (py - gy) * (py - gy);
       phip += phigrav<R>((R)pl[p].M, sqrt(pr), (R)pl[p].eps, pl[p].type);
     }
-    return phip / ((R)P.mach * (R)P.mach);
+    return phip / (PRM(R, P, mach) * PRM(R, P, mach));
   }
   return (R)1.0;
 }

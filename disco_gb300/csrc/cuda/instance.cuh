@@ -189,6 +189,10 @@ struct Instance : InstanceBase {
     }
     P.mul_nr = ((1ull << 40) + (unsigned long long)Nr - 1) / (unsigned long long)Nr;
     P.mul_nr1 = Nr > 1 ? ((1ull << 40) + (unsigned long long)(Nr - 1) - 1) / (unsigned long long)(Nr - 1) : 0;
+    P.f.gamma_law = (float)P.gamma_law; P.f.rho_floor = (float)P.rho_floor; P.f.p_floor = (float)P.p_floor;
+    P.f.explicit_viscosity = (float)P.explicit_viscosity; P.f.mach = (float)P.mach; P.f.PLM = (float)P.PLM;
+    P.f.Omega0 = (float)P.Omega0; P.f.om_M = (float)P.om_M; P.f.om_r1 = (float)P.om_r1;
+    P.f.om_H0 = (float)P.om_H0; P.f.eps = (float)P.eps;
     planets_id = dom->mod.planets;
     if (!Phys::MHD && P.riemann_solver == SOLVER_HLLD) {
       disco_set_error("Riemann_Solver = HLLD with a hydro module (riemann.c:19-22)");
@@ -505,9 +509,9 @@ struct Instance : InstanceBase {
     LAUNCH("flux_phi", (k_flux_phi<Phys, R, NQ><<<blocks(N), 256, 0, st>>>(P, S, fac)));
     launch_trans_fluxes(fac);
     if (ct) {   // avg_Efields, subtract_advective_B_fluxes, update_B_fluxes (onestep.c:261-265)
-      LAUNCH("ct_gather", (k_ct_gather<R><<<blocks(N), 256, 0, st>>>(P, S, C, RK, first)));
+      LAUNCH("ct_gather", (k_ct_gather<R><<<blocks(N), 256, 0, st>>>(P, S, C)));
       LAUNCH("ct_avg", (k_ct_avg<R><<<blocks(N), 256, 0, st>>>(P, S, C)));
-      LAUNCH("ct_bflux", (k_ct_bflux<R><<<blocks(N), 256, 0, st>>>(P, S, C, fac)));
+      LAUNCH("ct_bflux", (k_ct_bflux<R><<<blocks(N), 256, 0, st>>>(P, S, C, fac, RK, first)));
       if (Nz > 1) {
         // first substep: replay the events the last walk recorded (same
         // positions) or walk if there are none; second substep: walk and
@@ -691,10 +695,10 @@ struct Instance : InstanceBase {
     LAUNCH("flux_phi", (k_flux_phi<Phys, R, NQ><<<blocks(N), 256, 0, st>>>(P, S, fac)));
     if (stage >= 1) {
       launch_trans_fluxes(fac);
-      LAUNCH("ct_gather", (k_ct_gather<R><<<blocks(N), 256, 0, st>>>(P, S, C, RK, first)));
+      LAUNCH("ct_gather", (k_ct_gather<R><<<blocks(N), 256, 0, st>>>(P, S, C)));
     }
     if (stage >= 2) LAUNCH("ct_avg", (k_ct_avg<R><<<blocks(N), 256, 0, st>>>(P, S, C)));
-    if (stage >= 3) LAUNCH("ct_bflux", (k_ct_bflux<R><<<blocks(N), 256, 0, st>>>(P, S, C, fac)));
+    if (stage >= 3) LAUNCH("ct_bflux", (k_ct_bflux<R><<<blocks(N), 256, 0, st>>>(P, S, C, fac, RK, first)));
     if (stage >= 4 && Nz > 1)
       LAUNCH("ct_edge", (k_ct_edge<R><<<(Nr - 1) * (Nz - 1), 512, edge_smem, st>>>(P, S, C, fac, 0)));
     CK(cudaStreamSynchronize(st));

@@ -282,7 +282,7 @@ __global__ void k_plm_phi(DevParams P, DevState<R> S) {
   int cm = off + (i == 0 ? Np - 1 : i - 1);
   int cp = off + (i + 1 == Np ? 0 : i + 1);
   R dpL = S.dphi_r[cm], dpC = S.dphi_r[c], dpR = S.dphi_r[cp];
-  R PLM = (R)P.PLM;
+  R PLM = PRM(R, P, PLM);
   const int N = S.N;
   R iL = 0, iR = 0, iC = 0;
   if constexpr (kMix<R>) {   // three reciprocals instead of 3 NQ divisions
@@ -721,11 +721,15 @@ constexpr int plm_groups() { return (NQ + kPlmQ - 1) / kPlmQ; }
 template <typename R, int NQ>
 __global__ void __launch_bounds__(kTileCells) k_plm_trans(DevParams P, DevState<R> S, int dim) {
   constexpr int QPT = kPlmQ;
-  __shared__ R sS[QPT][kTileCap];
+  constexpr int NG = plm_groups<NQ>();
+  // components of this block: [q0, q0 + QPT) within NQ (q0 = 0 at compile
+  // time for a single group)
+  constexpr int QB = NG == 1 ? NQ : QPT;
+  __shared__ R sS[QB][kTileCap];
   __shared__ R sA[kTileCap];
   __shared__ int rng[2];
   const int item = blockIdx.x;
-  const int q0 = blockIdx.y * QPT;
+  const int q0 = NG == 1 ? 0 : (int)blockIdx.y * QPT;
   const int d = dim - 1;
   const int N = S.N, NF = S.nf[d];
   const int jk = S.chunk_ring[item], i0 = S.chunk_i0[item];
@@ -736,23 +740,31 @@ __global__ void __launch_bounds__(kTileCells) k_plm_trans(DevParams P, DevState<
   const int c = off + i;
   const int k = div_fast(jk, P.mul_nr), j = jk - k * P.Nr;
   R* grad = dim == 1 ? S.gradr : S.gradz;
-  R PLM = (R)P.PLM;
-  if (P.PLM == 0.0) {
+  const R PLM = PRM(R, P, PLM);
+  if (PLM == (R)0) {
     if (valid)
 #pragma unroll
-      for (int t = 0; t < QPT; ++t)
+      for (int t = 0; t < QB; ++t)
         if (q0 + t < NQ) grad[(q0 + t) * N + c] = 0;
     return;
   }
-  // the limiter needs only the extremes of PLM S over the faces: for g > 0 it
-  // is zero if any PLM S <= 0, else min(g, min PLM S); for g < 0 symmetric
-  R sum[QPT], mn[QPT], mx[QPT];
+  // The limiter needs only the extremes of PLM S over the faces: for g > 0
+  // it is zero if any PLM S <= 0, else min(g, min PLM S); for g < 0
+  // symmetric.  Rounding is monotonic, so min(PLM S) = PLM min(S) exactly
+  // for PLM > 0 (max for PLM < 0): the extremes of S are tracked and scaled
+  // once.
+  R sum[QB], mn[QB], mx[QB];
 #pragma unroll
-  for (int t = 0; t < QPT; ++t) {
+  for (int t = 0; t < QB; ++t) {
     sum[t] = 0;
     mn[t] = (R)INFINITY;
     mx[t] = -(R)INFINITY;
   }
+  auto take = [&](int t, R Sl, R dA) {
+    sum[t] += Sl * dA;
+    mn[t] = fmin(mn[t], Sl);
+    mx[t] = fmax(mx[t], Sl);
+  };
 
   for (int side = 0; side < 2; ++side) {   // pair below (cell is R), then above (cell is L)
     const int p = side == 0 ? pair_below(P, dim, j, k) : pair_above(P, dim, j, k);
@@ -769,38 +781,43 @@ __global__ void __launch_bounds__(kTileCells) k_plm_trans(DevParams P, DevState<
     }
     __syncthreads();
     const int st = rng[0], cnt = rng[1];
-    const bool tiled = cnt <= kTileCap;
-    if (tiled) {
+    if (cnt <= kTileCap) {   // uniform over the block
       for (int t = threadIdx.x; t < cnt; t += kTileCells) {
         int f = st + t;
         if (f >= base + Nf) f -= Nf;
         sA[t] = S.fdA[d][f];
 #pragma unroll
-        for (int u = 0; u < QPT; ++u)
+        for (int u = 0; u < QB; ++u)
           if (q0 + u < NQ) sS[u][t] = S.fslope[(size_t)(q0 + u) * NF + f];
       }
-    }
-    __syncthreads();
-    if (valid) {
-      for_run(rs[c], re[c], base, Nf, [&](int f) {
-        int o = f - st;
-        if (o < 0) o += Nf;
-        R dA = tiled ? sA[o] : S.fdA[d][f];
+      __syncthreads();
+      if (valid) {
+        for_run(rs[c], re[c], base, Nf, [&](int f) {
+          int o = f - st;
+          if (o < 0) o += Nf;
+          R dA = sA[o];
 #pragma unroll
-        for (int t = 0; t < QPT; ++t) {
-          const int q = q0 + t;
-          if (q >= NQ) break;
-          R Sl = tiled ? sS[t][o] : S.fslope[(size_t)q * NF + f];
-          sum[t] += Sl * dA;
-          R ps = PLM * Sl;
-          mn[t] = ps < mn[t] ? ps : mn[t];
-          mx[t] = ps > mx[t] ? ps : mx[t];
-        }
+          for (int t = 0; t < QB; ++t)
+            if (q0 + t < NQ) take(t, sS[t][o], dA);
+        });
+      }
+    } else if (valid) {
+      for_run(rs[c], re[c], base, Nf, [&](int f) {
+        R dA = S.fdA[d][f];
+#pragma unroll
+        for (int t = 0; t < QB; ++t)
+          if (q0 + t < NQ) take(t, S.fslope[(size_t)(q0 + t) * NF + f], dA);
       });
     }
     __syncthreads();
   }
   if (!valid) return;
+#pragma unroll
+  for (int t = 0; t < QB; ++t) {
+    R a = PLM * mn[t], b = PLM * mx[t];
+    mn[t] = PLM > (R)0 ? a : b;
+    mx[t] = PLM > (R)0 ? b : a;
+  }
 
   // total weight, plm.c:113-143
   R dAt, idAt = 0;
@@ -835,7 +852,7 @@ __global__ void __launch_bounds__(kTileCells) k_plm_trans(DevParams P, DevState<
   bool geom_bd = (dim == 1 && j == 0 && P.NgRa == 0);
   R rcen = kMix<R> ? S.ring_rc_r[jk] : (R)S.ring_rc[jk];
 #pragma unroll
-  for (int t = 0; t < QPT; ++t) {
+  for (int t = 0; t < QB; ++t) {
     const int q = q0 + t;
     if (q >= NQ) break;
     R g;
@@ -1134,18 +1151,18 @@ __global__ void __launch_bounds__(256, kMix<R> ? 4 : 1) k_update(DevParams P, De
     if constexpr (MIX) {   // sources summed in R into dU with the flux terms
       pr[UPP] += S.ring_Om_r[jk];   // lab omega for the source terms
       R dph = S.dphi_r[c];
-      R dVdt_r = S.ring_vol_r[jk] * dph * ((R)fac * dt_r<R>(S.scal));
+      R dVdt_r = S.ring_vol_r[jk] * dph * (to_r<R>(fac) * dt_r<R>(S.scal));
       R rc = S.ring_rc_r[jk];
       Phys::template source<R>(P, pr, dU, dVdt_r, S.ring_r1_r[jk], S.ring_r23_r[jk], rc, dph);
       if (P.Npl) {
-        R phc = (R)piph - (R).5 * dph;
+        R phc = to_r<R>(piph) - (R).5 * dph;
         for (int p = 0; p < P.Npl; ++p)
           if (S.planets[p].M != 0.0)
             planet_src<R, R>(P, S.planets[p], pr, dU, phc, S.ring_zc_r[jk], dVdt_r, rc, dph);
       }
       load_rk();
 #pragma unroll
-      for (int q = 0; q < NQ; ++q) U[q] += (double)dU[q];
+      for (int q = 0; q < NQ; ++q) U[q] += from_r<R>(dU[q]);
       if (P.include_viscosity || P.rot_flag) {
         double dV = (.5 * (xp[0] + xm[0])) * (xp[0] - xm[0]) * get_dp(xp[1], xm[1], Pmax) * (xp[2] - xm[2]);
         dVdt = dV * dt;
@@ -1193,15 +1210,15 @@ __global__ void __launch_bounds__(256, kMix<R> ? 4 : 1) k_update(DevParams P, De
     if constexpr (MIX) {
       if (do_c2p) {   // calc_prim at the post-move geometry, from U in registers
         R pr2[NQ];
-        R dph = first ? (R)dphi_new : S.dphi_r[c];
+        R dph = first ? to_r<R>(dphi_new) : S.dphi_r[c];
         int hits = Phys::cons2prim(P, S.planets, U, pr2, S.ring_rc_r[jk],
-                                   (R)piph_new - (R).5 * dph, S.ring_vol_r[jk] * dph,
+                                   to_r<R>(piph_new) - (R).5 * dph, S.ring_vol_r[jk] * dph,
                                    S.ring_Lsh[jk], S.ring_Om_r[jk]);
         bool bad = false;
 #pragma unroll
         for (int q = 0; q < NQ; ++q) {
           S.prim[q * N + c] = pr2[q];
-          if (!isfinite((double)pr2[q])) bad = true;
+          if (!isfinite(pr2[q])) bad = true;
         }
         if (bad) atomicAdd(&S.errs->nan_cells, 1ull);
         if (hits & 1) atomicAdd(&S.errs->rho_floor_hits, 1ull);
@@ -1215,7 +1232,7 @@ __global__ void __launch_bounds__(256, kMix<R> ? 4 : 1) k_update(DevParams P, De
     dphi = dphi_new;
     S.piph_out[c] = piph;
     S.dphi[c] = dphi;
-    if constexpr (MIX) S.dphi_r[c] = (R)dphi;
+    if constexpr (MIX) S.dphi_r[c] = to_r<R>(dphi);
   }
 
   if (!MIX && real && do_c2p) {  // calc_prim at the post-move geometry
@@ -1236,7 +1253,7 @@ __global__ void __launch_bounds__(256, kMix<R> ? 4 : 1) k_update(DevParams P, De
 #pragma unroll
     for (int q = 0; q < NQ; ++q) {
       S.prim[q * N + c] = pr[q];
-      if (!isfinite((double)pr[q])) bad = true;
+      if (!isfinite(pr[q])) bad = true;
     }
     if (bad) atomicAdd(&S.errs->nan_cells, 1ull);
     if (hits & 1) atomicAdd(&S.errs->rho_floor_hits, 1ull);
@@ -1382,7 +1399,7 @@ DISCO_D void c2p_cell(const DevParams& P, const DevState<R>& S, int c, int jk, i
   int hits;
   if constexpr (kMix<R>) {
     R dph = S.dphi_r[c];
-    hits = Phys::cons2prim(P, S.planets, U, pr, S.ring_rc_r[jk], (R)S.piph[c] - (R).5 * dph,
+    hits = Phys::cons2prim(P, S.planets, U, pr, S.ring_rc_r[jk], to_r<R>(S.piph[c]) - (R).5 * dph,
                            S.ring_vol_r[jk] * dph, S.ring_Lsh[jk], S.ring_Om_r[jk]);
   } else {
     const double* rj = S.r_jph + 1;
@@ -1398,7 +1415,7 @@ DISCO_D void c2p_cell(const DevParams& P, const DevState<R>& S, int c, int jk, i
 #pragma unroll
   for (int q = 0; q < NQ; ++q) {
     S.prim[q * N + c] = pr[q];
-    if (!isfinite((double)pr[q])) bad = true;
+    if (!isfinite(pr[q])) bad = true;
   }
   if (bad) atomicAdd(&S.errs->nan_cells, 1ull);
   if (hits & 1) atomicAdd(&S.errs->rho_floor_hits, 1ull);

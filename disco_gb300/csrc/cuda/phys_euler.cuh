@@ -24,7 +24,7 @@ struct Euler {
     R om = get_om<R>(P, r) - omf;
     R vp_off = vp - om * r;
     R v2 = vr * vr + vp_off * vp_off + vz * vz;
-    R rhoe = Pp / ((R)P.gamma_law - (R)1.);
+    R rhoe = Pp / (PRM(R, P, gamma_law) - (R)1.);
     cons[DDD] = rho * dV;
     cons[TAU] = ((R).5 * rho * v2 + rhoe) * dV;
     cons[SRR] = rho * vr * dV;
@@ -44,7 +44,7 @@ struct Euler {
     R vn = vr * n[0] + vp * n[1] + vz * n[2];
     R vn_off = vn - om * r * n[1];
     R Ss_off = Ss + vn_off - vn;
-    R rhoe = Pp / ((R)P.gamma_law - (R)1.);
+    R rhoe = Pp / (PRM(R, P, gamma_law) - (R)1.);
     R rhostar = rho * (Sk - vn) / (Sk - Ss);
     R Pstar = Pp * (Ss - vn) / (Sk - Ss);
     R Us = rhoe * (Sk - vn) / (Sk - Ss);
@@ -69,15 +69,15 @@ struct Euler {
     R rr = (R)r;
     if (sizeof(R) < sizeof(double)) {   // mixed path: one reciprocal, FP32 products
       R idV = (R)1 / (R)dV;
-      rho = (R)cons[DDD] * idV; Sr = (R)cons[SRR] * idV;
-      Sp = (R)(cons[LLL] - cons[DDD] * Lsh) * idV / rr;
-      Sz = (R)cons[SZZ] * idV; E = (R)cons[TAU] * idV;
+      rho = to_r<R>(cons[DDD]) * idV; Sr = to_r<R>(cons[SRR]) * idV;
+      Sp = to_r<R>(cons[LLL] - cons[DDD] * Lsh) * idV / rr;
+      Sz = to_r<R>(cons[SZZ]) * idV; E = to_r<R>(cons[TAU]) * idV;
     } else {
       rho = (R)(cons[DDD] / dV); Sr = (R)(cons[SRR] / dV); Sp = (R)(cons[LLL] / dV / r);
       Sz = (R)(cons[SZZ] / dV); E = (R)(cons[TAU] / dV);
     }
     R rho0 = rho;
-    if (rho < (R)P.rho_floor) { rho = (R)P.rho_floor; hits |= 1; }
+    if (rho < PRM(R, P, rho_floor)) { rho = PRM(R, P, rho_floor); hits |= 1; }
     R om = get_om<R>(P, rr);
     R vr = Sr / rho;
     R vp = Sp / rho;                       // relative to the frame
@@ -86,11 +86,11 @@ struct Euler {
     R vz = Sz / rho;
     R KE = (R).5 * (Sr * vr + rho * vp_off * vp_off + Sz * vz);
     R rhoe = E - KE;
-    R Pp = ((R)P.gamma_law - (R)1.) * rhoe;
-    if (Pp < (R)P.p_floor * rho) { Pp = (R)P.p_floor * rho; hits |= 2; }
+    R Pp = (PRM(R, P, gamma_law) - (R)1.) * rhoe;
+    if (Pp < PRM(R, P, p_floor) * rho) { Pp = PRM(R, P, p_floor) * rho; hits |= 2; }
     if (P.isothermal) {
       R cs2 = get_cs2<R>(P, pl, rr, (R)phi);
-      Pp = cs2 * rho / (R)P.gamma_law;
+      Pp = cs2 * rho / PRM(R, P, gamma_law);
     }
     prim[RHO] = rho;
     prim[PPP] = Pp;
@@ -99,7 +99,7 @@ struct Euler {
     prim[UZZ] = vz;
 #pragma unroll
     for (int q = NC; q < NQ; ++q)
-      prim[q] = sizeof(R) < sizeof(double) ? (R)cons[q] / (R)cons[DDD] : (R)(cons[q] / cons[DDD]);
+      prim[q] = sizeof(R) < sizeof(double) ? to_r<R>(cons[q]) / to_r<R>(cons[DDD]) : (R)(cons[q] / cons[DDD]);
     return hits;
   }
 
@@ -110,7 +110,7 @@ struct Euler {
     R vn = vr * n[0] + vp * n[1] + vz * n[2];
     R wn = om * r * n[1];
     R vp_off = vp - om * r;
-    R rhoe = Pp / ((R)P.gamma_law - (R)1.);
+    R rhoe = Pp / (PRM(R, P, gamma_law) - (R)1.);
     R v2 = vr * vr + vp_off * vp_off + vz * vz;
     f[DDD] = rho * vn;
     f[SRR] = rho * vr * vn + Pp * n[0];
@@ -126,10 +126,10 @@ struct Euler {
                           const R* n, R r, R* Bpack) {
     R P1 = p1[PPP], rho1 = p1[RHO];
     R vn1 = p1[URR] * n[0] + p1[UPP] * n[1] * r + p1[UZZ] * n[2];
-    R cs1 = sqrt((R)P.gamma_law * P1 / rho1);
+    R cs1 = sqrt(PRM(R, P, gamma_law) * P1 / rho1);
     R P2 = p2[PPP], rho2 = p2[RHO];
     R vn2 = p2[URR] * n[0] + p2[UPP] * n[1] * r + p2[UZZ] * n[2];
-    R cs2 = sqrt((R)P.gamma_law * P2 / rho2);
+    R cs2 = sqrt(PRM(R, P, gamma_law) * P2 / rho2);
     *Ss = (P2 - P1 + rho1 * vn1 * (-cs1) - rho2 * vn2 * cs2) / (rho1 * (-cs1) - rho2 * cs2);
     *Sr = cs1 + vn1;
     *Sl = -cs1 + vn1;
@@ -158,10 +158,10 @@ struct Euler {
 
   // nu for viscosity: explicit, or alpha c^2 / get_height_om (euler.c:220-226).
   DISCO_D static R visc_nu(const DevParams& P, const DevPlanet* pl, const R* prim, R r, R phi) {
-    R nu = (R)P.explicit_viscosity;
+    R nu = PRM(R, P, explicit_viscosity);
     if (P.alpha_flag) {
-      R alpha = (R)P.explicit_viscosity;
-      R c2 = (R)P.gamma_law * prim[PPP] / prim[RHO];
+      R alpha = PRM(R, P, explicit_viscosity);
+      R c2 = PRM(R, P, gamma_law) * prim[PPP] / prim[RHO];
       nu = alpha * c2 / get_height_om<R>(P, pl, r, phi);
     }
     return nu;
@@ -226,7 +226,7 @@ struct Euler {
     R Pp = prim[PPP], rho = prim[RHO];
     R vp = (prim[UPP] - w) * r;
     R vr = prim[URR], vz = prim[UZZ];
-    R cs = sqrt((R)P.gamma_law * Pp / rho);
+    R cs = sqrt(PRM(R, P, gamma_law) * Pp / rho);
     R dt = dL1 / (cs + fabs(vr)), dtp = dL0 / (cs + fabs(vp)), dtz = dL2 / (cs + fabs(vz));
     if (dt > dtp) dt = dtp;
     if (dt > dtz) dt = dtz;
@@ -234,10 +234,10 @@ struct Euler {
       R dx = dL0;
       if (dx > dL1) dx = dL1;
       if (dx > dL2) dx = dL2;
-      R nu = (R)P.explicit_viscosity;
+      R nu = PRM(R, P, explicit_viscosity);
       if (P.alpha_flag) {
-        R c2 = (R)P.gamma_law * prim[PPP] / prim[RHO];
-        nu = (R)P.explicit_viscosity * c2 / get_height_om<R>(P, pl, r, phi);
+        R c2 = PRM(R, P, gamma_law) * prim[PPP] / prim[RHO];
+        nu = PRM(R, P, explicit_viscosity) * c2 / get_height_om<R>(P, pl, r, phi);
       }
       R dt_visc = (R)0.5 * dx * dx / nu;
       if (dt > dt_visc) dt = dt_visc;
@@ -251,7 +251,7 @@ struct Euler {
     R Pp = prim[PPP], rho = prim[RHO];
     R vp = (R)((double)prim[UPP] - w) * (R)r;
     R vr = prim[URR], vz = prim[UZZ];
-    R cs = sqrt((R)P.gamma_law * Pp / rho);
+    R cs = sqrt(PRM(R, P, gamma_law) * Pp / rho);
     R maxvr = cs + fabs(vr), maxvp = cs + fabs(vp), maxvz = cs + fabs(vz);
     double dL1 = xp[0] - xm[0];
     double dL0 = .5 * (xp[0] + xm[0]) * get_dp(xp[1], xm[1], P.phi_max);
@@ -269,10 +269,10 @@ struct Euler {
       double dx = dL0;
       if (dx > dL1) dx = dL1;
       if (dx > dL2) dx = dL2;
-      R nu = (R)P.explicit_viscosity;
+      R nu = PRM(R, P, explicit_viscosity);
       if (P.alpha_flag) {
-        R c2 = (R)P.gamma_law * prim[PPP] / prim[RHO];
-        nu = (R)P.explicit_viscosity * c2 /
+        R c2 = PRM(R, P, gamma_law) * prim[PPP] / prim[RHO];
+        nu = PRM(R, P, explicit_viscosity) * c2 /
              get_height_om<R>(P, pl, (R)r, (R)(0.5 * (xp[1] + xm[1])));
       }
       double dt_visc = 0.5 * dx * dx / (double)nu;

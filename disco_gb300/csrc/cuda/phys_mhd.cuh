@@ -23,7 +23,7 @@ struct Mhd {
     R Br = prim[BRR], Bp = prim[BPP], Bz = prim[BZZ];
     R v2 = vr * vr + vp_off * vp_off + vz * vz;
     R B2 = Br * Br + Bp * Bp + Bz * Bz;
-    R rhoe = Pp / ((R)P.gamma_law - (R)1.);
+    R rhoe = Pp / (PRM(R, P, gamma_law) - (R)1.);
     cons[DDD] = rho * dV;
     cons[TAU] = ((R).5 * rho * v2 + rhoe + (R).5 * B2) * dV;
     cons[SRR] = rho * vr * dV;
@@ -46,17 +46,17 @@ struct Mhd {
     R rr = (R)r;
     if (sizeof(R) < sizeof(double)) {   // mixed path: one reciprocal, FP32 products
       R idV = (R)1 / (R)dV;
-      rho = (R)cons[DDD] * idV; Sr = (R)cons[SRR] * idV;
-      Sp = (R)(cons[LLL] - cons[DDD] * Lsh) * idV / rr;
-      Sz = (R)cons[SZZ] * idV; E = (R)cons[TAU] * idV;
-      Br = (R)cons[BRR] * idV * rr; Bp = (R)cons[BPP] * idV * rr; Bz = (R)cons[BZZ] * idV;
+      rho = to_r<R>(cons[DDD]) * idV; Sr = to_r<R>(cons[SRR]) * idV;
+      Sp = to_r<R>(cons[LLL] - cons[DDD] * Lsh) * idV / rr;
+      Sz = to_r<R>(cons[SZZ]) * idV; E = to_r<R>(cons[TAU]) * idV;
+      Br = to_r<R>(cons[BRR]) * idV * rr; Bp = to_r<R>(cons[BPP]) * idV * rr; Bz = to_r<R>(cons[BZZ]) * idV;
     } else {
       rho = (R)(cons[DDD] / dV); Sr = (R)(cons[SRR] / dV); Sp = (R)(cons[LLL] / dV / r);
       Sz = (R)(cons[SZZ] / dV); E = (R)(cons[TAU] / dV);
       Br = (R)(cons[BRR] / (dV * (1.0 / r))); Bp = (R)(cons[BPP] / dV * r); Bz = (R)(cons[BZZ] / dV);
     }
     R rho0 = rho;
-    if (rho < (R)P.rho_floor) { rho = (R)P.rho_floor; hits |= 1; }
+    if (rho < PRM(R, P, rho_floor)) { rho = PRM(R, P, rho_floor); hits |= 1; }
     R om = get_om<R>(P, rr);
     R vr = Sr / rho, vp = Sp / rho, vz = Sz / rho;   // vp relative to the frame
     if (rho != rho0) vp += Om * rr * (rho0 / rho - (R)1);
@@ -64,17 +64,17 @@ struct Mhd {
     R B2 = Br * Br + Bp * Bp + Bz * Bz;
     R KE = (R).5 * (Sr * vr + rho * vp_off * vp_off + Sz * vz);
     R rhoe = E - KE - (R).5 * B2;
-    R Pp = ((R)P.gamma_law - (R)1.) * rhoe;
-    if (Pp < (R)P.p_floor * rho) { Pp = (R)P.p_floor * rho; hits |= 2; }
+    R Pp = (PRM(R, P, gamma_law) - (R)1.) * rhoe;
+    if (Pp < PRM(R, P, p_floor) * rho) { Pp = PRM(R, P, p_floor) * rho; hits |= 2; }
     if (P.isothermal) {
       R cs2 = get_cs2<R>(P, pl, rr, (R)phi);
-      Pp = cs2 * rho / (R)P.gamma_law;
+      Pp = cs2 * rho / PRM(R, P, gamma_law);
     }
     prim[RHO] = rho; prim[PPP] = Pp; prim[URR] = vr; prim[UPP] = vp / rr; prim[UZZ] = vz;
     prim[BRR] = Br; prim[BPP] = Bp; prim[BZZ] = Bz;
 #pragma unroll
     for (int q = NC; q < NQ; ++q)
-      prim[q] = sizeof(R) < sizeof(double) ? (R)cons[q] / (R)cons[DDD] : (R)(cons[q] / cons[DDD]);
+      prim[q] = sizeof(R) < sizeof(double) ? to_r<R>(cons[q]) / to_r<R>(cons[DDD]) : (R)(cons[q] / cons[DDD]);
     return hits;
   }
 
@@ -87,7 +87,7 @@ struct Mhd {
     R vn = vr * n[0] + vp * n[1] + vz * n[2];
     R Bn = Br * n[0] + Bp * n[1] + Bz * n[2];
     R vB = vr * Br + vp * Bp + vz * Bz;
-    R rhoe = Pp / ((R)P.gamma_law - (R)1.);
+    R rhoe = Pp / (PRM(R, P, gamma_law) - (R)1.);
     R v2 = vr * vr + vp * vp + vz * vz;
     R B2 = Br * Br + Bp * Bp + Bz * Bz;
     f[DDD] = rho * vn;
@@ -282,7 +282,7 @@ struct Mhd {
   // get_Ustar_HLLD, hlld.c:282-401
   DISCO_D static void hlld(const DevParams& P, R w, const R* primL, const R* primR, R* F, R* U, R r,
                            const R* n) {
-    R gam = (R)P.gamma_law;
+    R gam = PRM(R, P, gamma_law);
     R vel[5], Pt_star;
     R hr = 1.0, hp = r, hz = 1.0;
     R pL[NQ], pR[NQ];
@@ -348,7 +348,7 @@ struct Mhd {
     R Pp = prim[PPP], rho = prim[RHO];
     R vp = (prim[UPP] - w) * r;
     R vr = prim[URR], vz = prim[UZZ];
-    R cs = sqrt((R)P.gamma_law * Pp / rho);
+    R cs = sqrt(PRM(R, P, gamma_law) * Pp / rho);
     R Br = prim[BRR], Bp = prim[BPP], Bz = prim[BZZ];
     R b2 = (Br * Br + Bp * Bp + Bz * Bz) / rho;
     R cf = sqrt(cs * cs + b2);
@@ -364,7 +364,7 @@ struct Mhd {
     R Pp = prim[PPP], rho = prim[RHO];
     R vp = (R)((double)prim[UPP] - w) * (R)r;
     R vr = prim[URR], vz = prim[UZZ];
-    R cs = sqrt((R)P.gamma_law * Pp / rho);
+    R cs = sqrt(PRM(R, P, gamma_law) * Pp / rho);
     R Br = prim[BRR], Bp = prim[BPP], Bz = prim[BZZ];
     R b2 = (Br * Br + Bp * Bp + Bz * Bz) / rho;
     R cf = sqrt(cs * cs + b2);
