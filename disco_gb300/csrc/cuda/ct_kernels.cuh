@@ -83,12 +83,13 @@ __global__ void __launch_bounds__(256, kMix<R> ? 6 : 1) k_ct_gather(DevParams P,
 // ---- avg_Efields (bfields.c:392-644) + subtract_advective_B_fluxes (:646-690)
 // d1: neighbour average along phi; d2: face average with the interpolated
 // value from the overlapping cell of the other ring; then E -= h w B.
+//
+// edge_avg_at: slot e of cell x after the phi-neighbour averaging pass, for
+// a cell of the ring whose first cell and size are given (a face
+// neighbour's ring follows from the pair, so its bounds load in parallel
+// with the face lookup instead of after it).
 template <typename R>
-DISCO_D R edge_avg(const DevState<R>& S, const R* A, int e, int x) {
-  // value of slot e of cell x after the phi-neighbour averaging pass
-  const int N = S.N;
-  int jk = S.cell_ring[x];
-  int off = S.ring_off[jk], Np = S.ring_off[jk + 1] - off;
+DISCO_D R edge_avg_at(const R* A, int N, int e, int x, int off, int Np) {
   int i = x - off;
   int xp = off + (i + 1 == Np ? 0 : i + 1), xm = off + (i == 0 ? Np - 1 : i - 1);
   int h = e & 4, s = e & 3;
@@ -105,6 +106,7 @@ __global__ void k_ct_avg(DevParams P, DevState<R> S, CtStateT<R> C) {
   const int N = S.N;
   int jk = S.cell_ring[c];
   int k = div_fast(jk, P.mul_nr), j = jk - k * P.Nr;
+  const int off = S.ring_off[jk], Np = S.ring_off[jk + 1] - off;
   R outE[4], outB[4];
   // mixed path: the B average split by the ring whose frame the EMFs were
   // stored in (own ring / the neighbouring ring across the face)
@@ -112,22 +114,26 @@ __global__ void k_ct_avg(DevParams P, DevState<R> S, CtStateT<R> C) {
   bool has[4] = {false, false, false, false};
   // slots: 0 -> E0 (r lower), 1 -> E1 (r upper), 2 -> E4 (z lower), 3 -> E5 (z upper)
   const int slot_e[4] = {0, 1, 4, 5};
+#pragma unroll
   for (int s = 0; s < 4; ++s) {
-    outE[s] = edge_avg(S, S.Eraw, slot_e[s], c);
-    outB[s] = edge_avg(S, S.Braw, slot_e[s], c);
+    outE[s] = edge_avg_at(S.Eraw, N, slot_e[s], c, off, Np);
+    outB[s] = edge_avg_at(S.Braw, N, slot_e[s], c, off, Np);
     ownB[s] = outB[s]; othB[s] = 0; dOmo[s] = 0;
   }
+#pragma unroll
   for (int dim = 1; dim <= 2; ++dim) {
     if (dim == 1 && P.Nr <= 1) continue;
     if (dim == 2 && P.Nz <= 1) continue;
     const int d = dim - 1, a = 4 * d;
+    const int stride = dim == 1 ? 1 : P.Nr;   // ring index step across the pair
     int pa = pair_above(P, dim, j, k), pb = pair_below(P, dim, j, k);
     if (pa >= 0) {   // LRtype 0 face owned by c (c = L = c1, c2 = R)
+      const int o2 = S.ring_off[jk + stride], n2 = S.ring_off[jk + stride + 1] - o2;
       int f = S.run_up_e[d][c];
       int c2 = S.fR[d][f];
       R dp1 = S.fdp1[d][f], dp2 = S.fdp2[d][f];
-      R Eavg = (dp2 * edge_avg(S, S.Eraw, a + 0, c2) + dp1 * edge_avg(S, S.Eraw, a + 2, c2)) / (dp1 + dp2);
-      R Bavg = (dp2 * edge_avg(S, S.Braw, a + 0, c2) + dp1 * edge_avg(S, S.Braw, a + 2, c2)) / (dp1 + dp2);
+      R Eavg = (dp2 * edge_avg_at(S.Eraw, N, a + 0, c2, o2, n2) + dp1 * edge_avg_at(S.Eraw, N, a + 2, c2, o2, n2)) / (dp1 + dp2);
+      R Bavg = (dp2 * edge_avg_at(S.Braw, N, a + 0, c2, o2, n2) + dp1 * edge_avg_at(S.Braw, N, a + 2, c2, o2, n2)) / (dp1 + dp2);
       const int s = 2 * d + 1;
       outE[s] = (R).5 * (outE[s] + Eavg);
       outB[s] = (R).5 * (outB[s] + Bavg);
@@ -135,11 +141,12 @@ __global__ void k_ct_avg(DevParams P, DevState<R> S, CtStateT<R> C) {
       if constexpr (kMix<R>) dOmo[s] = S.pdOm[d][pa];
     }
     if (pb >= 0) {   // LRtype 1 face owned by c (c = R = c1, c2 = L)
+      const int o2 = S.ring_off[jk - stride], n2 = S.ring_off[jk - stride + 1] - o2;
       int f = S.run_dn_e[d][c];
       int c2 = S.fL[d][f];
       R dp1 = S.fdp1[d][f], dp2 = S.fdp2[d][f];
-      R Eavg = (dp2 * edge_avg(S, S.Eraw, a + 1, c2) + dp1 * edge_avg(S, S.Eraw, a + 3, c2)) / (dp1 + dp2);
-      R Bavg = (dp2 * edge_avg(S, S.Braw, a + 1, c2) + dp1 * edge_avg(S, S.Braw, a + 3, c2)) / (dp1 + dp2);
+      R Eavg = (dp2 * edge_avg_at(S.Eraw, N, a + 1, c2, o2, n2) + dp1 * edge_avg_at(S.Eraw, N, a + 3, c2, o2, n2)) / (dp1 + dp2);
+      R Bavg = (dp2 * edge_avg_at(S.Braw, N, a + 1, c2, o2, n2) + dp1 * edge_avg_at(S.Braw, N, a + 3, c2, o2, n2)) / (dp1 + dp2);
       const int s = 2 * d + 0;
       outE[s] = (R).5 * (outE[s] + Eavg);
       outB[s] = (R).5 * (outB[s] + Bavg);
@@ -182,15 +189,18 @@ DISCO_D R face_emf(const DevState<R>& S, const CtStateT<R>& C, int d, int f) {
   return C.Efin[(2 * d + 0) * N + S.fR[d][f]];
 }
 
-// Mixed path: each slot's circulation E dl dt is formed in R and added to
-// the FP64 flux once (the FP64 path below keeps the reference's terms).
+// Mixed path: each slot's circulation E dl dt is formed in R, summed per
+// slot into dph and added to the FP64 flux once (the FP64 path below keeps
+// the reference's terms).
 template <typename R>
 DISCO_D void ct_bflux_mixed(const DevParams& P, const DevState<R>& S, const CtStateT<R>& C,
-                            double fac, int c, double* ph) {
+                            double fac, int c, R* dph) {
   const int N = S.N;
   int jk = S.cell_ring[c];
   int k = div_fast(jk, P.mul_nr), j = jk - k * P.Nr;
   R dtf = to_r<R>(fac) * dt_r<R>(S.scal);
+#pragma unroll
+  for (int q = 0; q < 5; ++q) dph[q] = 0;
   R dph0 = 0;
 #pragma unroll
   for (int dim = 1; dim <= 2; ++dim) {
@@ -207,7 +217,7 @@ DISCO_D void ct_bflux_mixed(const DevParams& P, const DevState<R>& S, const CtSt
       R Eg = face_emf(S, C, d, g);
       int slot = dim == 1 ? 1 : 3;
       R dv = dim == 1 ? (Eg - Ef) * dldt : (Ef - Eg) * dldt;
-      ph[slot] += from_r<R>(dv);
+      dph[slot] += dv;
       dph0 += dim == 1 ? -Ef * dldt : Ef * dldt;
     }
     if (pa >= 0 && pa != C.last_pair[d]) {
@@ -218,11 +228,11 @@ DISCO_D void ct_bflux_mixed(const DevParams& P, const DevState<R>& S, const CtSt
       R Eg = face_emf(S, C, d, g);
       int slot = dim == 1 ? 2 : 4;
       R dv = dim == 1 ? (Eg - Ef) * dldt : (Ef - Eg) * dldt;
-      ph[slot] += from_r<R>(dv);
+      dph[slot] += dv;
       dph0 += dim == 1 ? Ef * dldt : -Ef * dldt;
     }
   }
-  ph[0] += from_r<R>(dph0);
+  dph[0] += dph0;
 }
 
 // The RK adjustment of the face fluxes (Phi -> (1 - RK) Phi + RK RKPhi, or
@@ -235,18 +245,30 @@ __global__ void k_ct_bflux(DevParams P, DevState<R> S, CtStateT<R> C, double fac
   if (c >= S.N) return;
   const int N = S.N;
   double ph[5];
+  if constexpr (kMix<R>) {
+    // circulation terms summed in R first, then Phi = RK RKPhi + ((1 - RK) Phi + d)
+    R dph[5];
+    ct_bflux_mixed<R>(P, S, C, fac, c, dph);
+    const double a1 = 1. - RK;
+#pragma unroll
+    for (int q = 0; q < 5; ++q) {
+      double v = C.Phi[q * N + c], d = from_r<R>(dph[q]);
+      if (first) {
+        C.RKPhi[q * N + c] = v;
+        v += d;
+      } else {
+        v = fma(RK, C.RKPhi[q * N + c], fma(a1, v, d));
+      }
+      C.Phi[q * N + c] = v;
+    }
+    return;
+  }
 #pragma unroll
   for (int q = 0; q < 5; ++q) {
     double v = C.Phi[q * N + c];
     if (first) C.RKPhi[q * N + c] = v;
     else v = (1. - RK) * v + RK * C.RKPhi[q * N + c];
     ph[q] = v;
-  }
-  if constexpr (kMix<R>) {
-    ct_bflux_mixed<R>(P, S, C, fac, c, ph);
-#pragma unroll
-    for (int q = 0; q < 5; ++q) C.Phi[q * N + c] = ph[q];
-    return;
   }
   int jk = S.cell_ring[c];
   int k = div_fast(jk, P.mul_nr), j = jk - k * P.Nr;
@@ -414,8 +436,11 @@ __global__ void k_ct_edge(DevParams P, DevState<R> S, CtStateT<R> C, double fac,
   // search runs on the integer pipe.
   long long* sp = (long long*)sm;
   for (int x = 0; x < 4; ++x)
-    for (int m = threadIdx.x; m < np[x]; m += blockDim.x)
-      sp[base[x] + m] = __double_as_longlong(S.piph[off[x] + (I0[x] + m) % np[x]]);
+    for (int m = threadIdx.x; m < np[x]; m += blockDim.x) {
+      int t = I0[x] + m;   // I0 < np, m < np: one conditional wrap
+      t -= t >= np[x] ? np[x] : 0;
+      sp[base[x] + m] = __double_as_longlong(S.piph[off[x] + t]);
+    }
   __syncthreads();
   const double Pmax = P.phi_max;
   int lapoff[4];

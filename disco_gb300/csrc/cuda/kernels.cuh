@@ -1007,7 +1007,7 @@ __global__ void __launch_bounds__(256, kMix<R> ? 4 : 1) k_flux_trans(DevParams P
     R dOm = S.pdOm[d][pair];
     primR[UPP] += dOm;
     grad[UPP] += dOm * ridxs;
-    OmL = S.ring_Om_r[S.cell_ring[cL]];
+    OmL = S.ring_Om_r[pj + P.Nr * pk];   // the pair's L ring
   }
   if (P.include_viscosity) {
     const R* go = dim == 1 ? S.gradz : S.gradr;
@@ -1100,6 +1100,7 @@ __global__ void __launch_bounds__(256, kMix<R> ? 4 : 1) k_update(DevParams P, De
       }
     };
     if constexpr (!MIX) load_rk();
+    else (void)load_rk;
     // Mixed path: fluxes and sources are summed in R (FP32) into dU, and dU
     // is added once to the FP64 conserved state.  The FP64 path adds every
     // term to U directly, in the reference's order.
@@ -1160,9 +1161,19 @@ __global__ void __launch_bounds__(256, kMix<R> ? 4 : 1) k_update(DevParams P, De
           if (S.planets[p].M != 0.0)
             planet_src<R, R>(P, S.planets[p], pr, dU, phc, S.ring_zc_r[jk], dVdt_r, rc, dph);
       }
-      load_rk();
+      // adjust_RK_cons and the R sum in two FMAs per component:
+      // U = RK * RKcons + ((1 - RK) * cons + dU)
+      const double a1 = 1. - RK;
 #pragma unroll
-      for (int q = 0; q < NQ; ++q) U[q] += from_r<R>(dU[q]);
+      for (int q = 0; q < NQ; ++q) {
+        double u = S.cons[q * N + c], d = from_r<R>(dU[q]);
+        if (first) {
+          S.RKcons[q * N + c] = u;
+          U[q] = u + d;
+        } else {
+          U[q] = fma(RK, S.RKcons[q * N + c], fma(a1, u, d));
+        }
+      }
       if (P.include_viscosity || P.rot_flag) {
         double dV = (.5 * (xp[0] + xm[0])) * (xp[0] - xm[0]) * get_dp(xp[1], xm[1], Pmax) * (xp[2] - xm[2]);
         dVdt = dV * dt;
