@@ -40,6 +40,7 @@ __global__ void __launch_bounds__(256, kMix<R> ? 6 : 1) k_ct_gather(DevParams P,
   int jk = S.cell_ring[c];
   int k = div_fast(jk, P.mul_nr), j = jk - k * P.Nr;
   if (!ring_in_phi_range(P, j, k)) return;
+#pragma unroll
   for (int dim = 1; dim <= 2; ++dim) {
     if (dim == 1 && P.Nr <= 1) continue;
     if (dim == 2 && P.Nz <= 1) continue;
@@ -53,12 +54,17 @@ __global__ void __launch_bounds__(256, kMix<R> ? 6 : 1) k_ct_gather(DevParams P,
       // mixed path: the face EMF was solved in the L ring's frame; this cell
       // (R) stores it relative to its own ring's frame
       R cX = kMix<R> ? S.pcX[d][pb] : (R)0;
-      for_run(S.run_dn_s[d][c], S.run_dn_e[d][c], base, Nf, [&](int f) {
-        R fr = S.ffrR[d][f];
-        R ef = S.fErz[d][f];
-        if constexpr (kMix<R>) ef += cX * S.fBrz[d][f];
+      auto acc = [&](R fr, R ef, R bz) {
+        if constexpr (kMix<R>) ef += cX * bz;
         e0 += (R).5 * ef * fr; e2 += (R).5 * ef * fr;
-        b0 += (R).5 * S.fBrz[d][f] * fr; b2 += (R).5 * S.fBrz[d][f] * fr;
+        b0 += (R).5 * bz * fr; b2 += (R).5 * bz * fr;
+      };
+      // two faces' loads in flight per iteration, accumulated in run order
+      for_run2(S.run_dn_s[d][c], S.run_dn_e[d][c], base, Nf, [&](int f0, int f1, bool two) {
+        R fr0 = S.ffrR[d][f0], ef0 = S.fErz[d][f0], bz0 = S.fBrz[d][f0];
+        R fr1 = S.ffrR[d][f1], ef1 = S.fErz[d][f1], bz1 = S.fBrz[d][f1];
+        acc(fr0, ef0, bz0);
+        if (two) acc(fr1, ef1, bz1);
       });
       S.Eraw[(a + 0) * N + c] = e0; S.Eraw[(a + 2) * N + c] = e2;
       S.Braw[(a + 0) * N + c] = b0; S.Braw[(a + 2) * N + c] = b2;
@@ -68,10 +74,15 @@ __global__ void __launch_bounds__(256, kMix<R> ? 6 : 1) k_ct_gather(DevParams P,
       R e1 = S.Eraw[(a + 1) * N + c], e3 = S.Eraw[(a + 3) * N + c];
       R b1 = S.Braw[(a + 1) * N + c], b3 = S.Braw[(a + 3) * N + c];
       int base = S.face_off[d][pa], Nf = S.face_off[d][pa + 1] - base;
-      for_run(S.run_up_s[d][c], S.run_up_e[d][c], base, Nf, [&](int f) {
-        R fr = S.ffrL[d][f];
-        e1 += (R).5 * S.fErz[d][f] * fr; e3 += (R).5 * S.fErz[d][f] * fr;
-        b1 += (R).5 * S.fBrz[d][f] * fr; b3 += (R).5 * S.fBrz[d][f] * fr;
+      auto acc = [&](R fr, R ef, R bz) {
+        e1 += (R).5 * ef * fr; e3 += (R).5 * ef * fr;
+        b1 += (R).5 * bz * fr; b3 += (R).5 * bz * fr;
+      };
+      for_run2(S.run_up_s[d][c], S.run_up_e[d][c], base, Nf, [&](int f0, int f1, bool two) {
+        R fr0 = S.ffrL[d][f0], ef0 = S.fErz[d][f0], bz0 = S.fBrz[d][f0];
+        R fr1 = S.ffrL[d][f1], ef1 = S.fErz[d][f1], bz1 = S.fBrz[d][f1];
+        acc(fr0, ef0, bz0);
+        if (two) acc(fr1, ef1, bz1);
       });
       S.Eraw[(a + 1) * N + c] = e1; S.Eraw[(a + 3) * N + c] = e3;
       S.Braw[(a + 1) * N + c] = b1; S.Braw[(a + 3) * N + c] = b3;
@@ -663,24 +674,36 @@ DISCO_D void ct_b2c_cell(const DevParams& P, const DevState<R>& S, const CtState
   int cm = off + (i == 0 ? Np - 1 : i - 1);
   if constexpr (kMix<R>) {   // face fluxes summed in R
     R sums[2] = {0, 0}, areas[2] = {0, 0};
+#pragma unroll
     for (int dim = 1; dim <= 2; ++dim) {
       if (dim == 1 && P.Nr <= 1) continue;
       if (dim == 2 && P.Nz <= 1) continue;
       const int d = dim - 1;
       int lo = d == 0 ? 2 : 4, hi = d == 0 ? 1 : 3;
       int pb = pair_below(P, dim, j, k), pa = pair_above(P, dim, j, k);
-      auto visit = [&](int f) {
-        double ph = S.fLR[d][f] == 0 ? C.Phi[lo * N + S.fL[d][f]] : C.Phi[hi * N + S.fR[d][f]];
-        areas[d] += S.fdA[d][f];
-        sums[d] += to_r<R>(ph);
+      // the owning cell's slot of a face: L's lo slot or R's hi slot
+      auto slot = [&](int f) {
+        return S.fLR[d][f] == 0 ? lo * N + S.fL[d][f] : hi * N + S.fR[d][f];
+      };
+      // two faces' loads in flight per iteration, summed in run order
+      auto visit2 = [&](int f0, int f1, bool two) {
+        int s0 = slot(f0), s1 = slot(f1);
+        R a0 = S.fdA[d][f0], a1 = S.fdA[d][f1];
+        double p0 = C.Phi[s0], p1 = C.Phi[s1];
+        areas[d] += a0;
+        sums[d] += to_r<R>(p0);
+        if (two) {
+          areas[d] += a1;
+          sums[d] += to_r<R>(p1);
+        }
       };
       if (pb >= 0) {
         int base = S.face_off[d][pb], Nf = S.face_off[d][pb + 1] - base;
-        for_run(S.run_dn_s[d][c], S.run_dn_e[d][c], base, Nf, visit);
+        for_run2(S.run_dn_s[d][c], S.run_dn_e[d][c], base, Nf, visit2);
       }
       if (pa >= 0) {
         int base = S.face_off[d][pa], Nf = S.face_off[d][pa + 1] - base;
-        for_run(S.run_up_s[d][c], S.run_up_e[d][c], base, Nf, visit);
+        for_run2(S.run_up_s[d][c], S.run_up_e[d][c], base, Nf, visit2);
       }
     }
     R Bphi = (R).5 * to_r<R>(C.Phi[c] + C.Phi[cm]);

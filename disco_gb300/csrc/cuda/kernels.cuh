@@ -578,6 +578,22 @@ DISCO_D void for_run(int s, int e, int base, int Nf, F&& fn) {
   }
 }
 
+// The faces of a run in for_run's order, two at a time: fn(f0, f1, two),
+// f1 meaningful only when two (else f1 = f0).  The caller issues both faces'
+// loads before it consumes the first, and consumes them in order.
+template <typename F>
+DISCO_D void for_run2(int s, int e, int base, int Nf, F&& fn) {
+  const int first0 = s <= e ? s : base;
+  const int n1 = s <= e ? e - s + 1 : e - base + 1;   // faces before the wrap
+  const int n = s <= e ? n1 : n1 + (base + Nf - s);
+  for (int t = 0; t < n; t += 2) {
+    int f0 = t < n1 ? first0 + t : s + (t - n1);
+    bool two = t + 1 < n;
+    int f1 = t + 1 < n1 ? first0 + t + 1 : s + (t + 1 - n1);
+    fn(f0, two ? f1 : f0, two);
+  }
+}
+
 DISCO_D int pair_above(const DevParams& P, int dim, int j, int k) {
   if (dim == 1) return (j < P.Nr - 1) ? j + (P.Nr - 1) * k : -1;
   return (k < P.Nz - 1) ? j + P.Nr * k : -1;
