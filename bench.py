@@ -193,7 +193,7 @@ def kernel_bytes(name: str, N: int, nf: dict, nq: int, sw: int, ct: bool) -> flo
     if name == "ct_b2c_c2p":
         return kernel_bytes("ct_b2c", N, nf, nq, sw, ct) + kernel_bytes("c2p", N, nf, nq, sw, ct)
     if name == "update":
-        return N * (3 * nq * f8 + 2 * nq * sw + 5 * f8 + sw + 8 * ix) + nfa * nq * sw
+        return N * (2 * nq * f8 + 3 * nq * sw + 5 * f8 + sw + 8 * ix) + nfa * nq * sw
     if name in ("faces_r", "faces_z"):
         d = name[-1]
         return N * (2 * f8 + 4 * ix) + nf[d] * (2 * ix + 1 + f8 + 3 * sw + c * 4 * sw)
@@ -568,9 +568,11 @@ def main():
                                "launch, profiles/%s_dram_per_launch.md" % args.workload) if traffic else None,
             "algorithmic_bytes_per_launch": top_bytes,
             "share_of_step": top[2] / tot_prof}
-    # fused-RK2 compulsory bytes per zone-update: NQ (4 s_W + 6 s_U) + 6 x 8,
-    # plus 25 x 8 for the face fluxes Phi / RK_Phi of constrained transport
-    bz = nq * (4 * sw + 6 * 8) + 6 * 8 + (200 if ct else 0)
+    # fused-RK2 compulsory bytes per zone-update: NQ (6 s_W + 4 s_U) + 6 x 8
+    # (the RK copy of the state is one s_W write and one s_W read: the mixed
+    # path keeps the first substep's increment in R), plus 25 x 8 for the
+    # face fluxes Phi / RK_Phi of constrained transport
+    bz = nq * (6 * sw + 4 * 8) + 6 * 8 + (200 if ct else 0)
     whole = {"algorithmic_bytes_per_zone_update": bz, "achieved_GBps": bz * value / 1e9,
              "frac_of_hbm": bz * value / 1e9 / hbm}
     line = {

@@ -473,6 +473,7 @@ __global__ void k_ct_edge(DevParams P, DevState<R> S, CtStateT<R> C, double fac,
   };
   double dt = fac * S.scal[SC_DT];
   const double rjj = S.r_jph[j + 1];
+  const R rjr = (R)rjj;
   R dtf = 0;
   if constexpr (kMix<R>) dtf = to_r<R>(fac) * dt_r<R>(S.scal);
   for (int t = threadIdx.x; t < tot; t += blockDim.x) {
@@ -551,8 +552,16 @@ __global__ void k_ct_edge(DevParams P, DevState<R> S, CtStateT<R> C, double fac,
     double *PhiL, *PhiR, *PhiU, *PhiD;
     edge_targets<R>(C, N, w4, LR_alt, UD_alt, c, cR, cU, cUR, &PhiL, &PhiR, &PhiU, &PhiD, &E);
     R dl;   // edge length r dphi (the phi extent wrapped in FP64)
-    if constexpr (kMix<R>) dl = (R)rjj * (R)get_dp(xp1, xm1, Pmax);
-    else dl = (.5 * (rjj + rjj)) * get_dp(xp1, xm1, Pmax);
+    if constexpr (kMix<R>) {
+      // xp1, xm1 in [0, Pmax]: one FP64 difference, at most one wrap (the
+      // bits of a negative non-zero double exceed 2^63 as unsigned), converted
+      // on the integer pipe
+      double dp = xp1 - xm1;
+      if ((unsigned long long)__double_as_longlong(dp) > 0x8000000000000000ull) dp += Pmax;
+      dl = rjr * d2f_int(dp);
+    } else {
+      dl = (.5 * (rjj + rjj)) * get_dp(xp1, xm1, Pmax);
+    }
     if (cache) {
       long e = ev0 + t;
       C.ev_cid[e] = make_int4(c, cR, cU, cUR);

@@ -137,6 +137,34 @@ DISCO_HD inline double get_signed_dp(double phip, double phim, double phi_max) {
   while (dp > .5 * phi_max) dp -= phi_max;
   return dp;
 }
+#ifdef __CUDACC__
+// clean_pi (misc.c:8) and get_dp with their comparisons on the bit patterns
+// instead of FP64 compares: the integer order of non-negative doubles is
+// their numeric order, and a negative non-zero double's bits exceed 2^63 as
+// unsigned.  Same results as the FP64-compare loops for finite values;
+// infinities and NaN pass through instead of looping.
+__device__ inline double clean_pi_bits(double p, double pmax) {
+  const long long bmax = __double_as_longlong(pmax);
+  long long b = __double_as_longlong(p);
+  while (b > bmax && b < 0x7ff0000000000000LL) { p -= pmax; b = __double_as_longlong(p); }
+  while ((unsigned long long)b > 0x8000000000000000ull && (unsigned long long)b < 0xfff0000000000000ull) {
+    p += pmax;
+    b = __double_as_longlong(p);
+  }
+  return p;
+}
+__device__ inline double get_dp_bits(double phip, double phim, double pmax) {
+  double dp = phip - phim;
+  long long b = __double_as_longlong(dp);
+  while ((unsigned long long)b > 0x8000000000000000ull && (unsigned long long)b < 0xfff0000000000000ull) {
+    dp += pmax;
+    b = __double_as_longlong(dp);
+  }
+  const long long bmax = __double_as_longlong(pmax);
+  while (b > bmax && b < 0x7ff0000000000000LL) { dp -= pmax; b = __double_as_longlong(dp); }
+  return dp;
+}
+#endif
 DISCO_HD inline double centroid_r(double xp, double xm) {
   return 2.0 * (xp * xp + xp * xm + xm * xm) / (3.0 * (xp + xm));  // cylindrical.c:24-30
 }

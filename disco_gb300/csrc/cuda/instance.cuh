@@ -266,7 +266,9 @@ struct Instance : InstanceBase {
     } else {
       S.dphi_r = (R*)S.dphi;
     }
-    A(&S.prim, (size_t)NQ * N); A(&S.cons, (size_t)NQ * N); A(&S.RKcons, (size_t)NQ * N);
+    A(&S.prim, (size_t)NQ * N); A(&S.cons, (size_t)NQ * N);
+    if (kMix<R>) A(&S.RKdU, (size_t)NQ * N);
+    else A(&S.RKcons, (size_t)NQ * N);
     A(&S.gradp, (size_t)NQ * N); A(&S.gradr, (size_t)NQ * N); A(&S.gradz, (size_t)NQ * N);
     A(&S.fphi, (size_t)NQ * N);
     A(&S.anchor, nring);

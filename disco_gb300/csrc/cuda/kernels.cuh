@@ -2,7 +2,8 @@
 //
 // Layout in HBM (N = cells incl. ghosts, ring jk = j + Nr*k):
 //   cell c of ring jk lives at ring_off[jk] + i;  per-component arrays are
-//   SoA: prim[q*N + c] (R), cons/RKcons[q*N + c] (FP64), gradp/gradr/gradz
+//   SoA: prim[q*N + c] (R), cons/RKcons[q*N + c] (FP64; RKdU in R on the
+//   mixed path), gradp/gradr/gradz
 //   [q*N + c] (R), piph/dphi/wiph[c] (FP64).
 //   Sheared r (dim 1) and z (dim 2) faces are stored per ring pair in a
 //   static block face_off[pair] .. face_off[pair+1] (the count Np_L + Np_R
@@ -28,7 +29,8 @@ struct DevState {
   double* wiph;                // [N]
   R* prim;                     // [NQ*N]
   double* cons;                // [NQ*N]
-  double* RKcons;              // [NQ*N]
+  double* RKcons;              // [NQ*N] FP64 path: conserved state at the substep start
+  R* RKdU;                     // [NQ*N] mixed path: the first substep's increment (R)
   R* gradp;                    // [NQ*N]
   R* gradr;                    // [NQ*N]
   R* gradz;                    // [NQ*N]
@@ -1091,13 +1093,19 @@ __global__ void __launch_bounds__(256, kMix<R> ? 4 : 1) k_update(DevParams P, De
   if (first) {
     int cm = off + (i == 0 ? Np - 1 : i - 1);
     double pn = piph + S.wiph[c] * dt;
-    while (pn > Pmax) pn -= Pmax;
-    while (pn < 0.0) pn += Pmax;
     double pm = S.piph[cm] + S.wiph[cm] * dt;
-    while (pm > Pmax) pm -= Pmax;
-    while (pm < 0.0) pm += Pmax;
+    if constexpr (MIX) {   // the same wraps with integer compares
+      pn = clean_pi_bits(pn, Pmax);
+      pm = clean_pi_bits(pm, Pmax);
+      dphi_new = get_dp_bits(pn, pm, Pmax);
+    } else {
+      while (pn > Pmax) pn -= Pmax;
+      while (pn < 0.0) pn += Pmax;
+      while (pm > Pmax) pm -= Pmax;
+      while (pm < 0.0) pm += Pmax;
+      dphi_new = get_dp(pn, pm, Pmax);
+    }
     piph_new = pn;
-    dphi_new = get_dp(pn, pm, Pmax);
   }
   if (real) {
     double U[NQ];
@@ -1177,18 +1185,23 @@ __global__ void __launch_bounds__(256, kMix<R> ? 4 : 1) k_update(DevParams P, De
           if (S.planets[p].M != 0.0)
             planet_src<R, R>(P, S.planets[p], pr, dU, phc, S.ring_zc_r[jk], dVdt_r, rc, dph);
       }
-      // adjust_RK_cons and the R sum in two FMAs per component:
-      // U = RK * RKcons + ((1 - RK) * cons + dU)
-      const double a1 = 1. - RK;
+      // adjust_RK_cons on the mixed path.  The first substep adds its
+      // increment d1 (summed in R; plus the FP64 viscous / rotating-frame
+      // sources, below) to cons and keeps d1 in R; the second substep's
+      // RK RKcons + (1 - RK) cons is then cons - RK d1 (to FP64 rounding:
+      // nothing else writes the cons of a real cell between the two updates,
+      // except the B components of a CT run, which are rebuilt from the face
+      // fluxes after every update and never read from here).  So
+      // U = cons + (dU - RK d1): one FP64 add per component, and the RK
+      // copy of the state is R instead of FP64.
+      const R rk = to_r<R>(RK);
 #pragma unroll
       for (int q = 0; q < NQ; ++q) {
-        double u = S.cons[q * N + c], d = from_r<R>(dU[q]);
-        if (first) {
-          S.RKcons[q * N + c] = u;
-          U[q] = u + d;
-        } else {
-          U[q] = fma(RK, S.RKcons[q * N + c], fma(a1, u, d));
-        }
+        double u = S.cons[q * N + c];
+        R d = dU[q];
+        if (first) S.RKdU[q * N + c] = d;
+        else d = fma(-rk, S.RKdU[q * N + c], d);
+        U[q] = u + from_r<R>(d);
       }
       if (P.include_viscosity || P.rot_flag) {
         double dV = (.5 * (xp[0] + xm[0])) * (xp[0] - xm[0]) * get_dp(xp[1], xm[1], Pmax) * (xp[2] - xm[2]);
@@ -1231,6 +1244,15 @@ __global__ void __launch_bounds__(256, kMix<R> ? 4 : 1) k_update(DevParams P, De
       U[LLL] += rho * f1 * dVdt;
       U[SZZ] += rho * f2 * dVdt;
       U[TAU] += rho * vf * dVdt;
+    }
+    if constexpr (MIX) {
+      // the viscous and rotating-frame sources go to U in FP64 after the R
+      // sum: the increment kept for the second substep is then the whole
+      // change of this substep
+      if (first && (P.include_viscosity || P.rot_flag)) {
+#pragma unroll
+        for (int q = 0; q < NQ; ++q) S.RKdU[q * N + c] = to_r<R>(U[q] - S.cons[q * N + c]);
+      }
     }
 #pragma unroll
     for (int q = 0; q < NQ; ++q) S.cons[q * N + c] = U[q];
