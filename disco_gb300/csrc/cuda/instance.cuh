@@ -325,6 +325,26 @@ struct Instance : InstanceBase {
       CK(cudaMemcpy(d_ci, ci.data(), sizeof(int) * ci.size(), cudaMemcpyHostToDevice));
       S.chunk_ring = d_cr; S.chunk_i0 = d_ci; S.nchunk = (int)cr.size();
     }
+    {   // ghost cells filled by the boundary plugin (fixed.c: r ghosts;
+        // fixed3d.c: r and z ghosts), as chunks of kTileCells cells per ring
+      std::vector<int> gr, gi;
+      for (int jk = 0; jk < nring; ++jk) {
+        int k = jk / Nr, j = jk - k * Nr;
+        bool rghost = (j < P.NgRa) || (j >= Nr - P.NgRb);
+        bool zghost = (k < P.NgZa) || (k >= Nz - P.NgZb);
+        bool fill = P.boundary_id == 0 ? (rghost && Nr > 1)
+                  : P.boundary_id == 1 ? ((rghost && Nr > 1) || (zghost && Nz > 1)) : false;
+        if (!fill) continue;
+        for (int i0 = 0; i0 < dom->Np[jk]; i0 += kTileCells) { gr.push_back(jk); gi.push_back(i0); }
+      }
+      int *d_gr = nullptr, *d_gi = nullptr;
+      if (!gr.empty()) {
+        A(&d_gr, gr.size()); A(&d_gi, gi.size());
+        CK(cudaMemcpy(d_gr, gr.data(), sizeof(int) * gr.size(), cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(d_gi, gi.data(), sizeof(int) * gi.size(), cudaMemcpyHostToDevice));
+      }
+      S.ghost_ring = d_gr; S.ghost_i0 = d_gi; S.nghost = (int)gr.size();
+    }
     A(&S.planets, MAX_PL); A(&S.scal, SC_COUNT); A(&S.errs, 1);
     S.ct = ct ? 1 : 0;
     if (ct) {
@@ -453,7 +473,8 @@ struct Instance : InstanceBase {
       LAUNCH("wcell_avg", (k_wcell_avg<R><<<nring, 64, (maxring + 1) * sizeof(double), st>>>(P, S)));
   }
   void launch_boundary() {
-    LAUNCH("boundary", (k_boundary<R, NQ><<<blocks(N), 256, 0, st>>>(P, S)));
+    if (S.nghost > 0)
+      LAUNCH("boundary", (k_boundary<R, NQ><<<S.nghost, kTileCells, 0, st>>>(P, S)));
   }
   void launch_faces() {
     if (npair[0] == 0 && npair[1] == 0) return;

@@ -87,6 +87,11 @@ struct DevState {
   const int* chunk_ring;
   const int* chunk_i0;
   int nchunk;
+  // the ghost cells the boundary plugin fills, as chunks of up to
+  // kTileCells consecutive cells of one ring (k_boundary: one block each)
+  const int* ghost_ring;
+  const int* ghost_i0;
+  int nghost;
   int* run_up_s[2];            // per cell: first face where the cell is L (pair above)
   int* run_up_e[2];
   int* run_dn_s[2];            // per cell: first face where the cell is R (pair below)
@@ -330,13 +335,32 @@ __global__ void k_anchor(DevParams P, DevState<R> S, int nring) {
   if (warp >= nring) return;
   int off = S.ring_off[warp], Np = S.ring_off[warp + 1] - off;
   double convert = 2. * M_PI / P.phi_max;
+  // phi_max = 2 pi (convert == 1): th = piph exactly, and the quadrant tests
+  // compare bit patterns (the integer order of finite non-negative doubles
+  // is their numeric order; negative values and NaN fail both tests as the
+  // FP64 compares do)
+  const bool unit = convert == 1.0;
+  const long long kPi2 = 0x3ff921fb54442d18LL;     // bits of quadrant_q1's PI_2_LO
+  const long long k3Pi2 = 0x4012d97c7f3321d2LL;    // bits of quadrant_q4's THREE_PI_2_LO
+  const long long k2Pi = 0x401921fb54442d18LL;     // bits of TWO_PI_LO
+  const long long kInf = 0x7ff0000000000000LL;
+  auto q4 = [&](double p) {
+    if (!unit) return quadrant_q4(p * convert) != 0;
+    long long b = __double_as_longlong(p);
+    return b > k3Pi2 && b <= k2Pi;
+  };
+  auto q1 = [&](double p) {
+    if (!unit) return quadrant_q1(p * convert) != 0;
+    long long b = __double_as_longlong(p);
+    return (b > 0 && b <= kPi2) || (b > k2Pi && b <= kInf);
+  };
   int firstQ4 = 0x7fffffff;
   for (int i = lane; i < Np; i += 32)
-    if (quadrant_q4(S.piph[off + i] * convert)) { firstQ4 = min(firstQ4, i); }
+    if (q4(S.piph[off + i])) { firstQ4 = min(firstQ4, i); }
   for (int o = 16; o > 0; o >>= 1) firstQ4 = min(firstQ4, __shfl_xor_sync(0xffffffffu, firstQ4, o));
   int I0 = 0x7fffffff;
   for (int i = lane; i < Np; i += 32)
-    if (i > firstQ4 && quadrant_q1(S.piph[off + i] * convert)) { I0 = min(I0, i); }
+    if (i > firstQ4 && q1(S.piph[off + i])) { I0 = min(I0, i); }
   for (int o = 16; o > 0; o >>= 1) I0 = min(I0, __shfl_xor_sync(0xffffffffu, I0, o));
   if (lane == 0) S.anchor[warp] = (I0 == 0x7fffffff) ? 0 : I0;
 }
@@ -1315,32 +1339,42 @@ __global__ void __launch_bounds__(256, kMix<R> ? 4 : 1) k_update(DevParams P, De
 // only; fixed3d.c uses set_cell_init (boundary_functions.c:21) on r and z
 // ghosts.  The state after the prim update is position-dependent only.
 template <typename R, int NQ>
-__global__ void k_boundary(DevParams P, DevState<R> S) {
-  int c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= S.N) return;
-  int jk = S.cell_ring[c];
-  int k = div_fast(jk, P.mul_nr), j = jk - k * P.Nr;
-  bool rghost = (j < P.NgRa) || (j >= P.Nr - P.NgRb);
-  bool zghost = (k < P.NgZa) || (k >= P.Nz - P.NgZb);
+__global__ void __launch_bounds__(kTileCells) k_boundary(DevParams P, DevState<R> S) {
+  // one block per chunk of ghost cells (the list holds the rings the plugin
+  // fills: fixed.c r ghosts, fixed3d.c r and z ghosts)
+  const int jk = S.ghost_ring[blockIdx.x], i0 = S.ghost_i0[blockIdx.x];
+  const int k = div_fast(jk, P.mul_nr), j = jk - k * P.Nr;
+  const int off = S.ring_off[jk], Np = S.ring_off[jk + 1] - off;
+  const int i = i0 + threadIdx.x;
   const double* rj = S.r_jph + 1;
   const double* zk = S.z_kph + 1;
-  double x[3];
-  if (P.boundary_id == 0) {          // Boundary/fixed.c
-    if (!rghost || P.Nr <= 1) return;
-    x[0] = .5 * (rj[j] + rj[j - 1]);
-    x[1] = S.piph[c] - .5 * S.dphi[c];
-    x[2] = .5 * (zk[k] + zk[k - 1]);
-  } else if (P.boundary_id == 1) {   // Boundary/fixed3d.c -> set_cell_init
-    if (!((rghost && P.Nr > 1) || (zghost && P.Nz > 1))) return;
-    double xp1 = S.piph[c], xm1 = S.piph[c] - S.dphi[c];
-    x[0] = centroid_r(rj[j], rj[j - 1]);
-    x[1] = .5 * (xp1 + xm1);
-    x[2] = centroid_z(zk[k], zk[k - 1]);
-  } else {
-    return;
+  // r and z of the evaluation point are those of the ring in both plugins
+  const double xr = P.boundary_id == 0 ? .5 * (rj[j] + rj[j - 1]) : centroid_r(rj[j], rj[j - 1]);
+  const double xz = P.boundary_id == 0 ? .5 * (zk[k] + zk[k - 1]) : centroid_z(zk[k], zk[k - 1]);
+  // the disk initial conditions (ids 1, 2) do not depend on phi: one
+  // evaluation serves the whole chunk
+  const bool axisym = P.initial_id == 1 || P.initial_id == 2;
+  __shared__ double sprim[MAX_Q];
+  if (axisym) {
+    if (threadIdx.x == 0) {
+      double x[3] = {xr, 0.0, xz};
+      initial_eval(P, sprim, x);
+    }
+    __syncthreads();
   }
+  if (i >= Np || i >= i0 + kTileCells) return;
+  const int c = off + i;
   double prim[MAX_Q];
-  initial_eval(P, prim, x);
+  if (axisym) {
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) prim[q] = sprim[q];
+  } else {
+    double x[3];
+    x[0] = xr;
+    x[1] = P.boundary_id == 0 ? S.piph[c] - .5 * S.dphi[c] : .5 * (S.piph[c] + (S.piph[c] - S.dphi[c]));
+    x[2] = xz;
+    initial_eval(P, prim, x);
+  }
   if constexpr (kMix<R>) prim[UPP] -= S.ring_Om[jk];   // ring frame
 #pragma unroll
   for (int q = 0; q < NQ; ++q) S.prim[q * S.N + c] = (R)prim[q];
