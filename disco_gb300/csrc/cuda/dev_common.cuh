@@ -164,6 +164,36 @@ __device__ inline double get_dp_bits(double phip, double phim, double pmax) {
   while (b > bmax && b < 0x7ff0000000000000LL) { dp -= pmax; b = __double_as_longlong(dp); }
   return dp;
 }
+// get_signed_dp (cylindrical.c:17-22) with the comparisons against
+// +-pmax/2 on the bit patterns (ordered by magnitude within each sign).
+__device__ inline double get_signed_dp_bits(double phip, double phim, double pmax) {
+  const double half = .5 * pmax;
+  const unsigned long long hb = (unsigned long long)__double_as_longlong(half);
+  double dp = phip - phim;
+  unsigned long long b = (unsigned long long)__double_as_longlong(dp);
+  // dp < -half: negative with magnitude above half (and not NaN)
+  while (b > (0x8000000000000000ull | hb) && b < 0xfff0000000000000ull) {
+    dp += pmax;
+    b = (unsigned long long)__double_as_longlong(dp);
+  }
+  // dp > half: non-negative above half (and not NaN or infinity)
+  while (b > hb && b < 0x7ff0000000000000ull) {
+    dp -= pmax;
+    b = (unsigned long long)__double_as_longlong(dp);
+  }
+  return dp;
+}
+// while (p < 0) p += pmax; while (p > pmax) p -= pmax; on the bit patterns
+__device__ inline double wrap_pos_bits(double p, double pmax) {
+  const long long bmax = __double_as_longlong(pmax);
+  long long b = __double_as_longlong(p);
+  while ((unsigned long long)b > 0x8000000000000000ull && (unsigned long long)b < 0xfff0000000000000ull) {
+    p += pmax;
+    b = __double_as_longlong(p);
+  }
+  while (b > bmax && b < 0x7ff0000000000000LL) { p -= pmax; b = __double_as_longlong(p); }
+  return p;
+}
 #endif
 DISCO_HD inline double centroid_r(double xp, double xm) {
   return 2.0 * (xp * xp + xp * xm + xm * xm) / (3.0 * (xp + xm));  // cylindrical.c:24-30

@@ -513,15 +513,13 @@ __global__ void k_faces(DevParams P, DevState<R> S, int dim) {
       R dLr = S.dphi_r[iL], dRr = S.dphi_r[iR];
       // wrapped in FP64 first: across phi = 0 the raw difference is ~2 pi,
       // where an FP32 rounding would be as large as a sliver face
-      R dLR = (R)get_signed_dp(pR, pL, Pmax);
+      R dLR = d2f_int(get_signed_dp_bits(pR, pL, Pmax));
       int LR_back = wrap_signed<R>(dRr - dLr - dLR, Pm) < (R)0 ? 1 : 0;
       R xp = LR == 0 ? (R)0 : dLR;                  // upper edge - pL
       R xm = LR_back == 0 ? -dLr : dLR - dRr;      // lower edge - pL
       R dpr = wrap_dp<R>(xp - xm, Pm);
       R pc = xp - (R).5 * dpr;                     // face centre - pL
-      double phic = pL + (double)pc;
-      while (phic < 0.0) phic += Pmax;
-      while (phic > Pmax) phic -= Pmax;
+      double phic = wrap_pos_bits(pL + f2d_int(pc), Pmax);
       S.fLR[d][gf] = (signed char)LR;
       S.fphic[d][gf] = phic;
       S.fdA[d][gf] = S.pdA[d][pair] * dpr;
