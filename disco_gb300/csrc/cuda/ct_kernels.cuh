@@ -628,10 +628,19 @@ __global__ void k_ct_flip(DevParams P, DevState<R> S, CtStateT<R> C, int dim) {
     int f = base + n, fp = base + np;
     double pm = lr[n] == 0 ? S.piph[S.fL[d][f]] : S.piph[S.fR[d][f]];
     double pp = lr[np] == 0 ? S.piph[S.fL[d][fp]] : S.piph[S.fR[d][fp]];
-    if (get_signed_dp(pp, pm, P.phi_max) < 0.) { bits |= 1ull << (n - n0); ++mine; }
+    bool flip;
+    if constexpr (kMix<R>) {   // the same test with the wrap on bit patterns
+      double dp = get_signed_dp_bits(pp, pm, P.phi_max);
+      flip = (unsigned long long)__double_as_longlong(dp) > 0x8000000000000000ull &&
+             (unsigned long long)__double_as_longlong(dp) < 0xfff0000000000000ull;
+    } else {
+      flip = get_signed_dp(pp, pm, P.phi_max) < 0.;
+    }
+    if (flip) { bits |= 1ull << (n - n0); ++mine; }
   }
   cnt[threadIdx.x] = mine;
-  __syncthreads();
+  // nothing flagged in this pair (the common case): fLR stays, no repair
+  if (!__syncthreads_or(mine)) return;
   if (threadIdx.x == 0) {   // exclusive scan of 256 counts (cheap, one thread)
     int acc = 0;
     for (int t = 0; t < (int)blockDim.x; ++t) { int v = cnt[t]; cnt[t] = acc; acc += v; }
@@ -643,11 +652,31 @@ __global__ void k_ct_flip(DevParams P, DevState<R> S, CtStateT<R> C, int dim) {
     for (int n = n0; n < n1; ++n)
       if (bits >> (n - n0) & 1ull) list[w++] = n + 1 == Nf ? 0 : n + 1;
   }
-  __syncthreads();
-  int nflag = list[Nf];
-  if (threadIdx.x != 0 || nflag == 0) return;
+  __syncthreads();   // the list is complete before anyone reads it
+  __shared__ int last_start;
+  const int nflag = list[Nf];
   // flip_fluxes in ascending face order (the list holds n + 1 for each n;
-  // the wrap-around face 0 comes from the last chunk, so visit it first)
+  // the wrap-around face 0 comes from the last chunk, so it is visited first)
+  const bool wrap0 = list[nflag - 1] == 0;
+  auto ord = [&](int t) { return wrap0 ? (t == 0 ? 0 : list[t - 1]) : list[t]; };
+  // Faces x < y (the last face one chain touches, the first face the next
+  // chain touches) leave the two chains independent when they are distinct
+  // faces and share neither their L nor their R cell: the cells of a pair's
+  // faces advance monotonically with the face index, so no face up to x then
+  // shares a cell (hence a flux slot) with a face from y on.
+  auto apart = [&](int x, int y) {
+    if (y <= x) return false;
+    int fx = base + (x >= Nf ? x - Nf : x), fy = base + (y >= Nf ? y - Nf : y);
+    return S.fL[d][fx] != S.fL[d][fy] && S.fR[d][fx] != S.fR[d][fy];
+  };
+  // entry t (> 0) starts a chain when it is apart from entry t - 1
+  auto starts = [&](int t) { return apart(ord(t - 1) + 1, ord(t) - 1); };
+  if (threadIdx.x == 0) {   // the last chain's first entry (see below)
+    int t = nflag - 1;
+    while (t > 0 && !starts(t)) --t;
+    last_start = t;
+  }
+  __syncthreads();
   const int N = S.N;
   int lo = d == 0 ? 2 : 4, hi = d == 0 ? 1 : 3;
   auto slot = [&](int n) -> long long {
@@ -664,10 +693,30 @@ __global__ void k_ct_flip(DevParams P, DevState<R> S, CtStateT<R> C, int dim) {
     lr[n] = !lr[n];
     lr[nm] = !lr[nm];
   };
-  if (list[nflag - 1] == 0) repair(0);
-  for (int t = 0; t < nflag; ++t)
-    if (list[t] != 0) repair(list[t]);
-  for (int n = 0; n < Nf; ++n) S.fLR[d][base + n] = lr[n];
+  if (Nf <= 6) {   // every face within two of every other: one serial chain
+    if (threadIdx.x == 0)
+      for (int t = 0; t < nflag; ++t) repair(ord(t));
+  } else {
+    // repair(n) touches the slots of faces n - 1, n, n + 1 and flips lr[n - 1]
+    // and lr[n]: flagged faces that are not apart form a chain and are
+    // repaired in order by one thread; different chains touch disjoint slots
+    // and lr entries, so they run in parallel with the same result.  The
+    // first and the last chain are one chain when they meet across the wrap
+    // (face Nf - 1 next to face 0): the first chain's thread then continues
+    // with the last chain, which keeps the ascending order.
+    const bool linked = nflag > 1 && !apart(ord(nflag - 1) + 1, ord(0) - 1 + Nf);
+    for (int t = threadIdx.x; t < nflag; t += blockDim.x) {
+      if (t > 0 && !starts(t)) continue;                   // not a chain start
+      if (linked && t > 0 && t == last_start) continue;   // done by chain 0
+      int u = t;
+      repair(ord(u));
+      while (u + 1 < nflag && !starts(u + 1)) repair(ord(++u));
+      if (t == 0 && linked && last_start > u)
+        for (int v = last_start; v < nflag; ++v) repair(ord(v));
+    }
+  }
+  __syncthreads();
+  for (int n = threadIdx.x; n < Nf; n += blockDim.x) S.fLR[d][base + n] = lr[n];
 }
 
 // ---- B_faces_to_cells type 1 (bfields.c:88-309): cell B from face fluxes ---------
