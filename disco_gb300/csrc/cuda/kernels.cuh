@@ -947,7 +947,8 @@ __global__ void __launch_bounds__(256, kMix<R> ? 4 : 1) k_flux_phi(DevParams P, 
     double dA = (rp - rm) * (zp - zm);         // get_dA(.., 0) = dr dz
     dAdt = dA * (fac * S.scal[SC_DT]);
   }
-  double phi = S.piph[c];
+  // the face angle enters the Riemann solver through the viscous flux only
+  double phi = P.include_viscosity ? S.piph[c] : 0.0;
   R primL[NQ], primR[NQ], gp[NQ], gLr[NQ], gLz[NQ], gRr[NQ], gRz[NQ];
   R dL = S.dphi_r[c], dR = S.dphi_r[cp];
 #pragma unroll
@@ -1025,7 +1026,8 @@ __global__ void __launch_bounds__(256, kMix<R> ? 4 : 1) k_flux_trans(DevParams P
   int f = base + n;
   const int N = S.N;
   int cL = S.fL[d][f], cR = S.fR[d][f];
-  R phi = (R)S.fphic[d][f];
+  // the face angle enters the Riemann solver through the viscous flux only
+  R phi = P.include_viscosity ? (R)S.fphic[d][f] : (R)0;
   R dpL = S.fdpL[d][f], dpR = S.fdpR[d][f];
   R rdxL = S.pdxL[d][pair], rdxR = S.pdxR[d][pair];
   R ridxs = kMix<R> ? S.pidxs[d][pair] : (R)0;
