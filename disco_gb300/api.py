@@ -62,6 +62,8 @@ class DiscoModules(C.Structure):
         ("num_c", C.c_int), ("num_n", C.c_int), ("ct_mode", C.c_int),
         ("initial_name", C.c_char * 64), ("hydro_name", C.c_char * 64),
         ("boundary_name", C.c_char * 64), ("planets_name", C.c_char * 64),
+        ("metric", C.c_int), ("frame", C.c_int),
+        ("metric_name", C.c_char * 64), ("frame_name", C.c_char * 64),
     ]
 
 

@@ -36,7 +36,8 @@ CUDA_SOURCES = [("cuda/disco_gpu.cu", []),
                 ("cuda/inst_euler_f64.cu", ["--fmad=false"]),
                 ("cuda/inst_euler_f32.cu", F32_FLAGS),
                 ("cuda/inst_mhd_f64.cu", ["--fmad=false"]),
-                ("cuda/inst_mhd_f32.cu", F32_FLAGS)]
+                ("cuda/inst_mhd_f32.cu", F32_FLAGS),
+                ("cuda/inst_grmhd_f64.cu", ["--fmad=false"])]
 
 
 def _nvcc() -> str:

@@ -48,6 +48,8 @@ struct DevParams {
   // planet.c:4-35
   int grav2D, polar_r, polar_p;
   int Npl;
+  // GRMHD: the black-hole mass of the Kerr-Schild metric (Metric_Par2)
+  double gr_M;
   // initial / boundary plugins
   int initial_id, boundary_id;
   double ic[8];

@@ -13,6 +13,7 @@ InstanceBase* make_euler_double(const disco_host_domain* dom, int* rc);
 InstanceBase* make_euler_float(const disco_host_domain* dom, int* rc);
 InstanceBase* make_mhd_double(const disco_host_domain* dom, int* rc);
 InstanceBase* make_mhd_float(const disco_host_domain* dom, int* rc);
+InstanceBase* make_grmhd_double(const disco_host_domain* dom, int* rc);
 }
 using namespace disco_impl;
 
@@ -113,10 +114,17 @@ int disco_gpu_create(const disco_host_domain* dom, int precision, disco_gpu** ou
   }
   int rc = 0;
   InstanceBase* impl;
-  if (dom->mod.hydro == DISCO_HYDRO_EULER)
+  if (dom->mod.hydro == DISCO_HYDRO_EULER) {
     impl = precision ? make_euler_float(dom, &rc) : make_euler_double(dom, &rc);
-  else
+  } else if (dom->mod.hydro == DISCO_HYDRO_GRMHD) {
+    if (precision) {
+      disco_set_error("disco_gpu_create: GRMHD runs on the FP64 path only (precision 0)");
+      return DISCO_E_MODULE;
+    }
+    impl = make_grmhd_double(dom, &rc);
+  } else {
     impl = precision ? make_mhd_float(dom, &rc) : make_mhd_double(dom, &rc);
+  }
   if (!impl) return rc ? rc : DISCO_E_CUDA;
   *out = new disco_gpu{impl};
   return 0;

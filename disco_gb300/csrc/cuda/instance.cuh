@@ -207,8 +207,26 @@ struct Instance : InstanceBase {
       disco_set_error("only Timestep 0 (RK2) is built");
       return DISCO_E_MODULE;
     }
-    ct = Phys::MHD && dom->mod.ct_mode == 2 && p.CT;
-    if (Phys::MHD) {
+    ct = Phys::MHD && !Phys::GR && dom->mod.ct_mode == 2 && p.CT;
+    P.gr_M = p.metricPar2;
+    if constexpr (Phys::GR) {
+      // the GRMHD module as built: FP64, HLL, cell-centred B (CT_MODE 0), a
+      // static mesh, adiabatic, no viscosity, no rotating frame, no planets
+      const char* why = nullptr;
+      if (kMix<R>) why = "GRMHD runs on the FP64 path only (precision 0)";
+      else if (P.riemann_solver != SOLVER_HLL) why = "GRMHD is built with the HLL solver only (Riemann_Solver 0)";
+      else if (dom->mod.ct_mode != 0) why = "GRMHD is built with cell-centred B only (CT_MODE 0)";
+      else if (P.mesh_motion != 0) why = "GRMHD is built on a static mesh only (Mesh_Motion 0)";
+      else if (P.isothermal) why = "GRMHD is built for the adiabatic equation of state only";
+      else if (P.include_viscosity || P.rot_flag) why = "GRMHD with viscosity or a rotating frame is not built";
+      else if (dom->mod.planets != 0) why = "GRMHD takes PLANETS=none";
+      else if (P.gr_M <= 0.0) why = "GRMHD needs Metric_Par2 (the black-hole mass) > 0";
+      if (why) {
+        disco_set_error(why);
+        return DISCO_E_MODULE;
+      }
+    }
+    if (Phys::MHD && !Phys::GR) {
       if (!ct) {
         disco_set_error("MHD is built with constrained transport only (CT_MODE 2, Constrained_Transport 1)");
         return DISCO_E_MODULE;

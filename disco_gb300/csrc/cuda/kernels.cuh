@@ -184,9 +184,16 @@ DISCO_D void initial_eval(const DevParams& P, double* prim, const double* x) {
     disco_ic_disk D;
     disco_ic_disk_from_params(&D, P.gamma_law, P.mach, P.ic[0], P.ic[1], P.ic[2], P.ic[3],
                               P.ic[4], P.ic[5]);
-    if (P.initial_id == 1) disco_ic_disk_mhd_eval(&D, prim, x, P.num_c, P.num_q);
-    else if (P.initial_id == 2) disco_ic_disk_planet_eval(&D, prim, x, P.num_c, P.num_q);
-    else disco_ic_disk_cbd_eval(&D, prim, x, P.num_c, P.num_q);
+    if (P.initial_id == 1) {
+      disco_ic_disk_mhd_eval(&D, prim, x, P.num_c, P.num_q);
+    } else if (P.initial_id == 2) {
+      disco_ic_disk_planet_eval(&D, prim, x, P.num_c, P.num_q);
+    } else if (P.initial_id == 3) {
+      disco_ic_disk_cbd_eval(&D, prim, x, P.num_c, P.num_q);
+    } else {   // 4: gr_disk (Metric_Par2 = M, Init_Par1..4)
+      disco_ic_gr_disk G{P.gamma_law, P.gr_M, P.ic[0], P.ic[1], P.ic[2], P.ic[3]};
+      disco_ic_gr_disk_eval(&G, prim, x, P.num_c, P.num_q);
+    }
   }
   if (P.rot_flag) prim[UPP] -= P.rot_omega;   // subtract_omega, rotframe.c:15
 }
@@ -986,6 +993,13 @@ __global__ void __launch_bounds__(256, kMix<R> ? 4 : 1) k_flux_phi(DevParams P, 
     Fw[LLL] += Omr2 * Fw[DDD];
 #pragma unroll
     for (int q = 0; q < NQ; ++q) S.fphi[q * N + c] = Fw[q] * dAdt_r;
+  } else if constexpr (Phys::GR) {   // x = (centroid r, phi, centroid z), misc.c:396-411
+    const double* zk = S.z_kph + 1;
+    const double xg[3] = {r, S.piph[c], .5 * (zk[k] + zk[k - 1])};
+    const double nd[3] = {0.0, 1.0, 0.0};
+    solve_riemann_gr<Phys, NQ>(P, primL, primR, xg, nd, (double)(hn * S.wiph[c]), Fw);
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) S.fphi[q * N + c] = (R)((double)Fw[q] * dAdt);
   } else {
     R w = hn * (R)S.wiph[c];
     solve_riemann<Phys, R, NQ>(P, S.planets, primL, primR, gLr, gp, gLz, gRr, gp, gRz, (R)r,
@@ -993,7 +1007,7 @@ __global__ void __launch_bounds__(256, kMix<R> ? 4 : 1) k_flux_phi(DevParams P, 
 #pragma unroll
     for (int q = 0; q < NQ; ++q) S.fphi[q * N + c] = (R)((double)Fw[q] * dAdt);
   }
-  if (S.ct) {   // riemann.c:86-111 (NUM_EDGES == 8)
+  if constexpr (!Phys::GR) if (S.ct) {   // riemann.c:86-111 (NUM_EDGES == 8)
     R Ez, Br, Er, Bz;
     Phys::flux_to_E(Fl, Us, (R)r, &Ez, &Br, &Er, &Bz, 0);
     R hEz = (R).5 * Ez, hBr = (R).5 * Br, hEr = (R).5 * Er, hBz = (R).5 * Bz;
@@ -1066,12 +1080,20 @@ __global__ void __launch_bounds__(256, kMix<R> ? 4 : 1) k_flux_trans(DevParams P
   // face x = cm: r is the face radius for r faces, the centroid for z faces
   R r = S.prad[d][pair];
   R Fw[NQ], Fl[NQ], Us[NQ];
-  if (dim == 1)
+  if constexpr (Phys::GR) {
+    // face centre cm (faces_alt.c:10-20): z mid-layer on r faces, the face's z on z faces
+    const double* zk = S.z_kph + 1;
+    const double xg[3] = {r, S.fphic[d][f], dim == 1 ? .5 * (zk[pk] + zk[pk - 1]) : zk[pk]};
+    const double nd[3] = {n3[0], n3[1], n3[2]};
+    solve_riemann_gr<Phys, NQ>(P, primL, primR, xg, nd, 0.0, Fw);
+    (void)Fl; (void)Us;
+  } else if (dim == 1) {
     solve_riemann<Phys, R, NQ>(P, S.planets, primL, primR, grad, gLp, gLo, grad, gRp, gRo, (R)r,
                                phi, n3, (R)0.0, Fw, Fl, Us, OmL);
-  else
+  } else {
     solve_riemann<Phys, R, NQ>(P, S.planets, primL, primR, gLo, gLp, grad, gRo, gRp, grad, (R)r,
                                phi, n3, (R)0.0, Fw, Fl, Us, OmL);
+  }
   if constexpr (kMix<R>) {   // back to the lab frame (fixed face: F = Fw)
     R Omr2 = OmL * r * r;
     if (Phys::MHD) Fw[TAU] += OmL * Fw[LLL] + (R).5 * OmL * Omr2 * Fw[DDD];
@@ -1084,7 +1106,7 @@ __global__ void __launch_bounds__(256, kMix<R> ? 4 : 1) k_flux_trans(DevParams P
   else dAdt = S.fdA[d][f] * (R)(fac * S.scal[SC_DT]);
 #pragma unroll
   for (int q = 0; q < NQ; ++q) out[(size_t)q * NF + f] = Fw[q] * dAdt;
-  if (S.ct) {
+  if constexpr (!Phys::GR) if (S.ct) {
     R E1, B1, E2, B2;
     Phys::flux_to_E(Fl, Us, r, &E1, &B1, &E2, &B2, dim);
     S.fErz[d][f] = E1; S.fBrz[d][f] = B1; S.fEphi[d][f] = E2;
@@ -1234,16 +1256,20 @@ __global__ void __launch_bounds__(256, kMix<R> ? 4 : 1) k_update(DevParams P, De
     } else {
       double dV = (.5 * (xp[0] + xm[0])) * (xp[0] - xm[0]) * get_dp(xp[1], xm[1], Pmax) * (xp[2] - xm[2]);
       dVdt = dV * dt;
-      double dph = get_dp(xp[1], xm[1], Pmax);
-      double rc = S.ring_rc[jk];
-      Phys::template source<double>(P, pr, U, dVdt, (R)(.5 * (xp[0] + xm[0])), (R)S.ring_r23[jk], (R)rc,
-                                    (R)dph);
-      for (int p = 0; p < P.Npl; ++p)
-        if (S.planets[p].M != 0.0)
-          planet_src<R, double>(P, S.planets[p], pr, U, (R)(xm[1] + 0.5 * dph),
-                                (R)centroid_z(xp[2], xm[2]), dVdt, (R)rc, (R)dph);
+      if constexpr (Phys::GR) {   // grmhd.c:339 (metric and frame sources; no planets)
+        Phys::source_x(P, pr, U, xp, xm, dVdt);
+      } else {
+        double dph = get_dp(xp[1], xm[1], Pmax);
+        double rc = S.ring_rc[jk];
+        Phys::template source<double>(P, pr, U, dVdt, (R)(.5 * (xp[0] + xm[0])), (R)S.ring_r23[jk], (R)rc,
+                                      (R)dph);
+        for (int p = 0; p < P.Npl; ++p)
+          if (S.planets[p].M != 0.0)
+            planet_src<R, double>(P, S.planets[p], pr, U, (R)(xm[1] + 0.5 * dph),
+                                  (R)centroid_z(xp[2], xm[2]), dVdt, (R)rc, (R)dph);
+      }
     }
-    if (P.include_viscosity) {
+    if constexpr (!Phys::GR) if (P.include_viscosity) {
       R gr[NQ], gp[NQ], gz[NQ];
 #pragma unroll
       for (int q = 0; q < NQ; ++q) {
@@ -1251,7 +1277,7 @@ __global__ void __launch_bounds__(256, kMix<R> ? 4 : 1) k_update(DevParams P, De
       }
       Phys::visc_source(P, S.planets, pr, gr, gp, gz, U, xp, xm, dVdt);
     }
-    if (P.rot_flag) {  // omega_src, rotframe.c:32-80
+    if constexpr (!Phys::GR) if (P.rot_flag) {  // omega_src, rotframe.c:32-80
       double r = S.ring_rc[jk];
       double ph = .5 * (xp[1] + xm[1]);
       double rho = pr[RHO];
@@ -1320,7 +1346,14 @@ __global__ void __launch_bounds__(256, kMix<R> ? 4 : 1) k_update(DevParams P, De
       double U[NQ];
 #pragma unroll
       for (int q = 0; q < NQ; ++q) U[q] = S.cons[q * N + c];
-      hits = Phys::cons2prim(P, S.planets, U, pr, r, .5 * (phim + piph), dV);
+      if constexpr (Phys::GR) {   // Newton iteration seeded with the previous primitives
+#pragma unroll
+        for (int q = 0; q < NQ; ++q) pr[q] = S.prim[q * N + c];
+        const double xg[3] = {r, .5 * (phim + piph), .5 * (zp + zm)};
+        hits = Phys::cons2prim_x(P, U, pr, xg, dV);
+      } else {
+        hits = Phys::cons2prim(P, S.planets, U, pr, r, .5 * (phim + piph), dV);
+      }
     }
     bool bad = false;
 #pragma unroll
@@ -1408,7 +1441,8 @@ __global__ void k_mindt(DevParams P, DevState<R> S) {
         double xp[3] = {rj[j], phip, zk[k]};
         double xm[3] = {rj[j - 1], phim, zk[k - 1]};
         double w = .5 * (S.wiph[im] + S.wiph[c]);
-        dtc = Phys::mindt(P, S.planets, pr, w, xp, xm, S.ring_rc[jk]);
+        if constexpr (Phys::GR) dtc = Phys::mindt_x(P, pr, w, xp, xm);
+        else dtc = Phys::mindt(P, S.planets, pr, w, xp, xm, S.ring_rc[jk]);
       }
     }
   }
@@ -1492,7 +1526,14 @@ DISCO_D void c2p_cell(const DevParams& P, const DevState<R>& S, int c, int jk, i
     double phim = piph - dphi;
     double dV = (.5 * (rp + rm)) * (rp - rm) * get_dp(piph, phim, P.phi_max) * (zp - zm);
     double r = S.ring_rc[jk];
-    hits = Phys::cons2prim(P, S.planets, U, pr, r, .5 * (phim + piph), dV);
+    if constexpr (Phys::GR) {   // Newton iteration seeded with the previous primitives
+#pragma unroll
+      for (int q = 0; q < NQ; ++q) pr[q] = S.prim[q * N + c];
+      const double xg[3] = {r, .5 * (phim + piph), .5 * (zp + zm)};
+      hits = Phys::cons2prim_x(P, U, pr, xg, dV);
+    } else {
+      hits = Phys::cons2prim(P, S.planets, U, pr, r, .5 * (phim + piph), dV);
+    }
   }
   bool bad = false;
 #pragma unroll
@@ -1537,12 +1578,22 @@ __global__ void k_init_cells(DevParams P, DevState<R> S, const double* prim0, in
   double pr[NQ], U[NQ];
 #pragma unroll
   for (int q = 0; q < NQ; ++q) pr[q] = prim0[q * N + c];
-  using Phys64 = typename Phys::template Rebind<double>;
-  Phys64::template prim2cons<double>(P, pr, U, r, dV);
   R out[NQ];
-  if (do_c2p) {
+  if constexpr (Phys::GR) {
+    // setupCells (domain.c:176-238): prim2cons, then cons2prim seeded with
+    // the initial primitives, both at x = (centroid r, phi, centroid z)
+    const double xg[3] = {r, piph - .5 * dphi, .5 * (zp + zm)};
+    Phys::prim2cons_x(P, pr, U, xg, dV);
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) out[q] = pr[q];
+    if (do_c2p) Phys::cons2prim_x(P, U, out, xg, dV);
+  } else if (do_c2p) {
+    using Phys64 = typename Phys::template Rebind<double>;
+    Phys64::template prim2cons<double>(P, pr, U, r, dV);
     Phys::cons2prim(P, S.planets, U, out, r, piph - .5 * dphi, dV, S.ring_Lsh[jk], (R)S.ring_Om[jk]);
   } else {
+    using Phys64 = typename Phys::template Rebind<double>;
+    Phys64::template prim2cons<double>(P, pr, U, r, dV);
     for (int q = 0; q < NQ; ++q) out[q] = (R)pr[q];
     if constexpr (kMix<R>) out[UPP] = (R)(pr[UPP] - S.ring_Om[jk]);   // ring frame
   }

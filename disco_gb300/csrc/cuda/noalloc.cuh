@@ -64,7 +64,8 @@ __global__ void k_mindt_blocks(DevParams P, DevState<R> S, unsigned long long* p
         double xp[3] = {rj[j], phip, zk[k]};
         double xm[3] = {rj[j - 1], phim, zk[k - 1]};
         double w = .5 * (S.wiph[im] + S.wiph[c]);
-        dtc = Phys::mindt(P, S.planets, pr, w, xp, xm, S.ring_rc[jk]);
+        if constexpr (Phys::GR) dtc = Phys::mindt_x(P, pr, w, xp, xm);
+        else dtc = Phys::mindt(P, S.planets, pr, w, xp, xm, S.ring_rc[jk]);
       }
     }
   }

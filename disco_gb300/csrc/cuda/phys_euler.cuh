@@ -11,6 +11,7 @@ template <typename R, int NQ>
 struct Euler {
   static constexpr int NC = 5;
   static constexpr bool MHD = false;
+  static constexpr bool GR = false;
   template <typename T>
   using Rebind = Euler<T, NQ>;
 

@@ -11,6 +11,7 @@ template <typename R, int NQ>
 struct Mhd {
   static constexpr int NC = 8;
   static constexpr bool MHD = true;
+  static constexpr bool GR = false;
   template <typename T>
   using Rebind = Mhd<T, NQ>;
 

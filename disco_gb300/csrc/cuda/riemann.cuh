@@ -83,4 +83,37 @@ DISCO_D void solve_riemann(const DevParams& P, const DevPlanet* pl, const R* pri
   }
 }
 
+// The HLL branch of solve_riemann (riemann.c:238-271) for the GR module,
+// whose hooks take the face position x = (r, phi, z): Fw = Flux - w U*.
+// No viscous flux and no EMFs (the GR module is built without viscosity
+// and with cell-centred B).
+template <typename Phys, int NQ>
+DISCO_D void solve_riemann_gr(const DevParams& P, const double* primL, const double* primR, const double* x,
+                              const double* n, double w, double* Fw) {
+  double Flux[NQ], Ustr[NQ];
+  double Sl, Sr;
+  Phys::vel_x(P, primL, primR, &Sl, &Sr, n, x);
+  if (w < Sl) {
+    Phys::flux_x(P, primL, Flux, x, n);
+    Phys::prim2cons_x(P, primL, Ustr, x, 1.0);
+  } else if (w > Sr) {
+    Phys::flux_x(P, primR, Flux, x, n);
+    Phys::prim2cons_x(P, primR, Ustr, x, 1.0);
+  } else {
+    double Fl[NQ], Fr[NQ], Ul[NQ], Ur[NQ];
+    const double aL = Sr, aR = -Sl;
+    Phys::prim2cons_x(P, primL, Ul, x, 1.0);
+    Phys::prim2cons_x(P, primR, Ur, x, 1.0);
+    Phys::flux_x(P, primL, Fl, x, n);
+    Phys::flux_x(P, primR, Fr, x, n);
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) {
+      Flux[q] = (aL * Fl[q] + aR * Fr[q] + aL * aR * (Ul[q] - Ur[q])) / (aL + aR);
+      Ustr[q] = (aR * Ul[q] + aL * Ur[q] + Fl[q] - Fr[q]) / (aL + aR);
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < NQ; ++q) Fw[q] = Flux[q] - w * Ustr[q];
+}
+
 }  // namespace disco

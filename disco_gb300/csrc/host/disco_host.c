@@ -219,6 +219,9 @@ int disco_modules_read(const char *path, disco_modules *m)
    if(!mk_value(b, "NUM_C", v, sizeof v)) m->num_c = atoi(v); else bad = 1;
    if(!mk_value(b, "NUM_N", v, sizeof v)) m->num_n = atoi(v); else bad = 1;
    if(!mk_value(b, "CT_MODE", v, sizeof v)) m->ct_mode = atoi(v); else bad = 1;
+   /* METRIC and FRAME matter to GRMHD only; absent keys read as "" */
+   if(mk_value(b, "METRIC", m->metric_name, sizeof m->metric_name)) m->metric_name[0] = 0;
+   if(mk_value(b, "FRAME", m->frame_name, sizeof m->frame_name)) m->frame_name[0] = 0;
    if(!mk_value(b, "GEOMETRY", v, sizeof v) && strcmp(v, "cylindrical") != 0) {
       free(b);
       disco_set_error("GEOMETRY: only cylindrical is built");
@@ -227,14 +230,16 @@ int disco_modules_read(const char *path, disco_modules *m)
    free(b);
    if(bad) { disco_set_error("Makefile_opt.in: missing module key"); return DISCO_E_PARFILE; }
 
-   static const char *hyd[] = {"euler", "mhd"};
-   static const char *ini[] = {"vortex_gauss", "disk_mhd", "disk_planet", "disk_cbd"};
+   static const char *hyd[] = {"euler", "mhd", "grmhd"};
+   static const char *ini[] = {"vortex_gauss", "disk_mhd", "disk_planet", "disk_cbd", "gr_disk"};
    static const char *bnd[] = {"fixed", "fixed3d", "outflow3d", "zerograd"};
    static const char *pla[] = {"none", "sun", "circular", "cm"};
    int i;
    m->hydro = m->initial = m->boundary = m->planets = -1;
-   for(i = 0; i < 2; i++) if(!strcmp(m->hydro_name, hyd[i])) m->hydro = i;
-   for(i = 0; i < 4; i++) if(!strcmp(m->initial_name, ini[i])) m->initial = i;
+   for(i = 0; i < 3; i++) if(!strcmp(m->hydro_name, hyd[i])) m->hydro = i;
+   for(i = 0; i < 5; i++) if(!strcmp(m->initial_name, ini[i])) m->initial = i;
+   m->metric = !strcmp(m->metric_name, "schw_ks_rpz") ? DISCO_METRIC_SCHW_KS_RPZ : DISCO_METRIC_NONE;
+   m->frame = !strcmp(m->frame_name, "normal") ? DISCO_FRAME_NORMAL : DISCO_FRAME_NONE;
    for(i = 0; i < 4; i++) if(!strcmp(m->boundary_name, bnd[i])) m->boundary = i;
    for(i = 0; i < 4; i++) if(!strcmp(m->planets_name, pla[i])) m->planets = i;
    char msg[256];
@@ -247,6 +252,17 @@ int disco_modules_read(const char *path, disco_modules *m)
    }
    if(m->hydro == DISCO_HYDRO_MHD && m->num_c != 8) {
       disco_set_error("mhd needs NUM_C=8"); return DISCO_E_MODULE;
+   }
+   if(m->hydro == DISCO_HYDRO_GRMHD) {
+      if(m->num_c != 8 || m->ct_mode != 0) {
+         disco_set_error("grmhd is built with NUM_C=8 and CT_MODE=0 (cell-centred B)");
+         return DISCO_E_MODULE;
+      }
+      if(m->metric != DISCO_METRIC_SCHW_KS_RPZ || m->frame != DISCO_FRAME_NORMAL) {
+         snprintf(msg, sizeof msg, "grmhd: METRIC=%s FRAME=%s not built (schw_ks_rpz, normal are)",
+                  m->metric_name, m->frame_name);
+         disco_set_error(msg); return DISCO_E_MODULE;
+      }
    }
    if(m->num_n < 0 || m->num_n > 1) { disco_set_error("NUM_N must be 0 or 1"); return DISCO_E_MODULE; }
    return DISCO_OK;
@@ -339,6 +355,11 @@ static void ic_eval(const disco_host_domain *d, double *prim, const double *x)
                                 p->initPar2, p->initPar3, p->initPar4, p->initPar5,
                                 p->initPar6);
       disco_ic_disk_cbd_eval(&P, prim, x, nc, nq);
+      break; }
+   case DISCO_IC_GR_DISK: {
+      struct disco_ic_gr_disk P = { p->Adiabatic_Index, p->metricPar2, p->initPar1,
+                                    p->initPar2, p->initPar3, p->initPar4 };
+      disco_ic_gr_disk_eval(&P, prim, x, nc, nq);
       break; }
    }
    if(p->RotFrame) prim[3] -= p->RotOmega;   /* subtract_omega, rotframe.c:15 */

@@ -143,4 +143,69 @@ DISCO_HD static inline void disco_ic_disk_cbd_eval(
    for(q = num_c; q < num_q; q++) prim[q] = r < P->par3 ? 1.0 : 0.0;
 }
 
+/*
+ * gr_disk: a thin Keplerian GRMHD disk around a Schwarzschild black hole of
+ * mass M, in Kerr-Schild cylindrical coordinates (t, r, phi, z) -- the
+ * coordinates of the reference's Hydro/Metric/schw_ks_rpz.c, where
+ * g = eta + H k k with H = 2M/R, R = sqrt(r^2 + z^2), k = (1, r/R, 0, z/R).
+ *   rho  = max(exp(-z^2 / (2 h^2)), 1e-4),  h = hr r;
+ *   P    = rho cs^2 / gam,  cs = hr sqrt(M / r);
+ *   v^r  = amp sqrt(M / r) sin(3 phi),  v^phi = sqrt(M / r^3),  v^z = 0
+ *          (coordinate velocities dx^i/dt);
+ *   u^0 from g_{mu nu} u^mu u^nu = -1, l_i = u^0 (g_{i0} + g_{ij} v^j);
+ *   prim = {rho, P, l_r, l_phi / r^2, l_z, 0, 0, Bz} with the vertical field
+ *   Bz = sqrt(2 P(z = 0) / beta) (the module's B prim is sqrt(gamma) B^i),
+ *   passive = 1 inside r < rpass.
+ * Parameters: gam = Adiabatic_Index, M = Metric_Par2, hr = Init_Par1,
+ * amp = Init_Par2, beta = Init_Par3, rpass = Init_Par4.
+ */
+struct disco_ic_gr_disk {
+   double gam, M, hr, amp, beta, rpass;
+};
+
+DISCO_HD static inline void disco_ic_gr_disk_eval(
+      const struct disco_ic_gr_disk *P, double *prim, const double *x,
+      int num_c, int num_q)
+{
+   double r = x[0], phi = x[1], z = x[2];
+   double M = P->M;
+   double R2 = r*r + z*z;
+   double R = sqrt(R2);
+   double H = 2.0*M/R;
+   double g00 = -1.0 + H;
+   double g0r = H*r/R, g0z = H*z/R;
+   double grr = 1.0 + H*r*r/R2, grz = H*r*z/R2, gzz = 1.0 + H*z*z/R2;
+   double gpp = r*r;
+
+   double vk = sqrt(M/r);
+   double h = P->hr*r;
+   double rho = exp(-0.5*z*z/(h*h));
+   if(rho < 1.0e-4) rho = 1.0e-4;
+   double cs2 = P->hr*P->hr*vk*vk;
+   double Pp = rho*cs2/P->gam;
+   double vr = P->amp*vk*sin(3.0*phi);
+   double vp = vk/r;
+   double vz = 0.0;
+
+   double norm = g00 + 2.0*g0r*vr + 2.0*g0z*vz + grr*vr*vr + 2.0*grz*vr*vz
+                 + gzz*vz*vz + gpp*vp*vp;
+   double u0 = 1.0/sqrt(-norm);
+   double lr = u0*(g0r + grr*vr + grz*vz);
+   double lp = u0*gpp*vp;
+   double lz = u0*(g0z + grz*vr + gzz*vz);
+
+   prim[0] = rho;
+   prim[1] = Pp;
+   prim[2] = lr;
+   prim[3] = lp/(r*r);
+   prim[4] = lz;
+   if(num_c > 5) {
+      prim[5] = 0.0;
+      prim[6] = 0.0;
+      prim[7] = P->beta > 0.0 ? sqrt(2.0*cs2/P->gam/P->beta) : 0.0;
+   }
+   int q;
+   for(q = num_c; q < num_q; q++) prim[q] = r < P->rpass ? 1.0 : 0.0;
+}
+
 #endif

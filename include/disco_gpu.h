@@ -47,9 +47,13 @@ enum disco_status_code {
 };
 
 /* Module ids selected by name from Makefile_opt.in (Makefile:12-26). */
-enum disco_hydro_id   { DISCO_HYDRO_EULER = 0, DISCO_HYDRO_MHD = 1 };
+enum disco_hydro_id   { DISCO_HYDRO_EULER = 0, DISCO_HYDRO_MHD = 1, DISCO_HYDRO_GRMHD = 2 };
 enum disco_initial_id { DISCO_IC_VORTEX_GAUSS = 0, DISCO_IC_DISK_MHD = 1,
-                        DISCO_IC_DISK_PLANET = 2, DISCO_IC_DISK_CBD = 3 };
+                        DISCO_IC_DISK_PLANET = 2, DISCO_IC_DISK_CBD = 3,
+                        DISCO_IC_GR_DISK = 4 };
+/* GRMHD only: METRIC and FRAME of Makefile_opt.in (Hydro/Metric, Hydro/Frame) */
+enum disco_metric_id  { DISCO_METRIC_NONE = -1, DISCO_METRIC_SCHW_KS_RPZ = 0 };
+enum disco_frame_id   { DISCO_FRAME_NONE = -1, DISCO_FRAME_NORMAL = 0 };
 enum disco_boundary_id{ DISCO_BC_FIXED = 0, DISCO_BC_FIXED3D = 1,
                         DISCO_BC_OUTFLOW3D = 2, DISCO_BC_ZEROGRAD = 3 };
 enum disco_planets_id { DISCO_PL_NONE = 0, DISCO_PL_SUN = 1,
@@ -63,6 +67,8 @@ typedef struct disco_modules {
    int hydro, initial, boundary, planets;
    int num_c, num_n, ct_mode;    /* NUM_C, NUM_N, CT_MODE */
    char initial_name[64], hydro_name[64], boundary_name[64], planets_name[64];
+   int metric, frame;            /* GRMHD: disco_metric_id, disco_frame_id */
+   char metric_name[64], frame_name[64];
 } disco_modules;
 
 /* Run-time parameters: the hot-path subset of struct param_list

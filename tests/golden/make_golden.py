@@ -44,6 +44,9 @@ CASES = {
     # one instance of the planet-disk batch: alpha viscosity, locally
     # isothermal, a planet on a circular orbit
     "cfg3_n24": ("configs/cfg3_planet_disk", {"Num_R": 24}, 10),
+    # GRMHD thin disk around a Schwarzschild black hole (Kerr-Schild
+    # cylindrical metric, HLL, cell-centred B) at 12 x 4 rings
+    "cfg4_n12": ("configs/cfg4_grmhd_disk", {"Num_R": 12, "Num_Z": 4}, 5),
 }
 
 

@@ -32,6 +32,34 @@ def test_grid_and_phases_bit_exact():
     assert np.max(np.abs(h.prim[:, real] - g["init_prim"][:, real])) < 1e-14
 
 
+def test_grmhd_disk_initial_state_bit_exact():
+    """GRMHD disk (Kerr-Schild metric module, gr_disk initial condition):
+    grid and phases equal the reference build's, initial primitives to
+    rounding."""
+    dg = _dg()
+    g = load_golden("cfg4_n12")
+    p = dg.read_params(write_par(g["par_text"]))
+    m = dg.read_modules(os.path.join(ROOT, "configs/cfg4_grmhd_disk/Makefile_opt.in"))
+    assert (m.hydro, m.metric, m.frame, m.ct_mode) == (2, 0, 0, 0)
+    h = dg.HostDomain(p, m)
+    assert np.array_equal(h.Np, g["Np"])
+    assert np.array_equal(h.piph, g["init_piph"])
+    real = g["real"].astype(bool)
+    # initial() prims vs the reference's prims after its prim2cons and the
+    # Newton cons2prim seeded with them
+    assert np.max(np.abs(h.prim[:, real] - g["init_prim"][:, real])) < 1e-14
+
+
+def test_grmhd_unbuilt_metric_rejected(tmp_path):
+    """A metric other than schw_ks_rpz is refused at module selection."""
+    dg = _dg()
+    src = open(os.path.join(ROOT, "configs/cfg4_grmhd_disk/Makefile_opt.in")).read()
+    mk = tmp_path / "Makefile_opt.in"
+    mk.write_text(src.replace("schw_ks_rpz", "schw_sc_rpz"))
+    with pytest.raises(dg.DiscoError):
+        dg.read_modules(str(mk))
+
+
 def test_rand_restatement_matches_libc():
     """The restated glibc rand() stream equals the C library's (where the
     host C library is glibc)."""
