@@ -104,7 +104,7 @@ class DiscoKernelTime(C.Structure):
 class DiscoGpuErrs(C.Structure):
     _fields_ = [("nan_cells", C.c_longlong), ("rho_floor_hits", C.c_longlong),
                 ("p_floor_hits", C.c_longlong), ("face_errors", C.c_longlong),
-                ("steps", C.c_longlong)]
+                ("steps", C.c_longlong), ("c2p_no_converge", C.c_longlong)]
 
 
 # Every symbol include/*.h declares, with its ctypes signature.

@@ -343,6 +343,7 @@ DISCO_D R get_height_om(const DevParams& P, const DevPlanet* pl, R r, R phi) {
 // Health counters written by kernels (never trap).
 struct DevErrs {
   unsigned long long nan_cells, rho_floor_hits, p_floor_hits, face_errors, steps;
+  unsigned long long c2p_no_converge;   // GRMHD Newton cons2prim at its iteration cap
 };
 
 }  // namespace disco

@@ -818,6 +818,7 @@ struct Instance : InstanceBase {
     e->p_floor_hits = (long long)h.p_floor_hits;
     e->face_errors = (long long)h.face_errors;
     e->steps = (long long)h.steps;
+    e->c2p_no_converge = (long long)h.c2p_no_converge;
     if (ct) {
       unsigned long long ce = 0;
       CK(cudaMemcpy(&ce, C.errs, 8, cudaMemcpyDeviceToHost));

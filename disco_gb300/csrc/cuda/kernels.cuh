@@ -1364,6 +1364,7 @@ __global__ void __launch_bounds__(256, kMix<R> ? 4 : 1) k_update(DevParams P, De
     if (bad) atomicAdd(&S.errs->nan_cells, 1ull);
     if (hits & 1) atomicAdd(&S.errs->rho_floor_hits, 1ull);
     if (hits & 2) atomicAdd(&S.errs->p_floor_hits, 1ull);
+    if (hits & 4) atomicAdd(&S.errs->c2p_no_converge, 1ull);
   }
 }
 
@@ -1544,6 +1545,7 @@ DISCO_D void c2p_cell(const DevParams& P, const DevState<R>& S, int c, int jk, i
   if (bad) atomicAdd(&S.errs->nan_cells, 1ull);
   if (hits & 1) atomicAdd(&S.errs->rho_floor_hits, 1ull);
   if (hits & 2) atomicAdd(&S.errs->p_floor_hits, 1ull);
+  if (hits & 4) atomicAdd(&S.errs->c2p_no_converge, 1ull);
 }
 
 template <typename Phys, typename R, int NQ>

@@ -150,6 +150,8 @@ typedef struct disco_gpu_errs {
    long long p_floor_hits;    /* pressure floor applied (euler.c:123) */
    long long face_errors;     /* inconsistent sheared-face merge */
    long long steps;           /* timesteps taken on the device */
+   long long c2p_no_converge; /* GRMHD: Newton cons2prim stopped at max_iter = 30
+                                 (grmhd.c:959-968, which prints and continues) */
 } disco_gpu_errs;
 
 typedef struct disco_gpu disco_gpu;   /* opaque device instance */

@@ -71,7 +71,7 @@ def test_steps_match_reference_fp64(name):
         assert e_c < 1e-11, (q, e_c)
         assert e_p < 1e-11, (q, e_p)
     st = d.status()
-    assert st["nan_cells"] == 0 and st["face_errors"] == 0
+    assert st["nan_cells"] == 0 and st["face_errors"] == 0 and st["c2p_no_converge"] == 0
     d.close()
 
 
