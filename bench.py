@@ -386,20 +386,25 @@ def measure_ours(args, wl, rank):
             # memory, K x (getmindt -> dt to host, timestep(dt) -> dt to
             # device), download
             res["profile"] = d.profile(3)
+            # the whole state: with constrained transport the face fluxes Phi too
+            keys = ("piph", "dphi", "wiph", "prim", "cons") + (("Phi",) if "Phi" in st else ())
             pin = {k: torch.empty(st[k].shape, dtype=torch.float64, pin_memory=True).numpy()
-                   for k in ("piph", "dphi", "wiph", "prim", "cons")}
+                   for k in keys}
             for k in pin:
                 pin[k][...] = st[k]
             del st
+            # the download lands in pinned host buffers as well
+            pout = {k: torch.empty(pin[k].shape, dtype=torch.float64, pin_memory=True).numpy()
+                    for k in pin}
             torch.cuda.synchronize()
             t0 = time.perf_counter()
             d.upload(**pin)
             for _ in range(args.steps):
                 d.timestep(d.getmindt())
-            out = d.state()
+            out = d.state(out=pout)
             t1 = time.perf_counter()
             up = sum(pin[k].nbytes for k in pin)
-            down = sum(out[k].nbytes for k in ("piph", "dphi", "wiph", "prim", "cons"))
+            down = sum(out[k].nbytes for k in keys)
             res["e2e"] = {"value": cells * args.steps / (t1 - t0), "unit": "zone-updates/s",
                           "h2d_bytes_per_step": int(up / args.steps + 8),
                           "d2h_bytes_per_step": int(down / args.steps + 8),

@@ -277,16 +277,24 @@ class Domain:
     def num_real_cells(self) -> int:
         return lib().disco_gpu_num_real_cells(self._g)
 
-    def state(self) -> dict:
+    def state(self, out: dict | None = None) -> dict:
+        """Download the state.  `out` may hold preallocated C-contiguous
+        float64 arrays (e.g. in pinned memory) for any of the keys, of the
+        shapes this method would allocate; they are filled in place."""
         n = self.num_cells
         q = self.host.num_q
-        out = {k: np.empty(n) for k in ("piph", "dphi", "wiph")}
-        out["prim"] = np.empty((q, n))
-        out["cons"] = np.empty((q, n))
+        out = dict(out or {})
+        shapes = {"piph": (n,), "dphi": (n,), "wiph": (n,), "prim": (q, n), "cons": (q, n)}
+        if self.host.num_q >= 8:
+            shapes["Phi"] = (5, n)
+        for k, shp in shapes.items():
+            if k not in out:
+                out[k] = np.zeros(shp) if k == "Phi" else np.empty(shp)
+            a = out[k]
+            if a.shape != shp or a.dtype != np.float64 or not a.flags.c_contiguous:
+                raise ValueError(f"state(out): {k} must be C-contiguous float64 of shape {shp}")
         v = DiscoStateView()
         dp = C.POINTER(C.c_double)
-        if self.host.num_q >= 8:
-            out["Phi"] = np.zeros((5, n))
         for k in ("piph", "dphi", "wiph", "prim", "cons", "Phi"):
             if k in out:
                 setattr(v, k, out[k].ctypes.data_as(dp))
@@ -298,7 +306,7 @@ class Domain:
         v = DiscoStateView()
         dp = C.POINTER(C.c_double)
         keep = []
-        for k in ("piph", "dphi", "wiph", "prim", "cons"):
+        for k in ("piph", "dphi", "wiph", "prim", "cons", "Phi"):
             if k in arrays:
                 a = np.ascontiguousarray(arrays[k], dtype=np.float64)
                 keep.append(a)

@@ -133,7 +133,6 @@ struct Instance : InstanceBase {
   int graph_nodes = 0;
   double host_t = 0;
   std::vector<double> ring_Om_h;   // ring frames (host copy)
-  std::vector<int> cell_ring_h;
 
   ~Instance() override {
     if (flush_buf) cudaFree(flush_buf);
@@ -443,7 +442,6 @@ struct Instance : InstanceBase {
       }
     }
     CK(cudaMemcpy(S.ring_Om, ring_Om_h.data(), sizeof(double) * nring, cudaMemcpyHostToDevice));
-    cell_ring_h = cell_ring;
     LAUNCH("ring_geom", (k_ring_geom<R><<<blocks(nring), 256, 0, st>>>(P, S, nring)));
     for (int d = 0; d < 2; ++d)
       if (npair[d]) LAUNCH("pair_geom", (k_pair_geom<R><<<blocks(npair[d]), 256, 0, st>>>(P, S, d + 1, npair[d])));
@@ -766,6 +764,11 @@ struct Instance : InstanceBase {
     if (Phi) CK(cudaMemcpy(Phi, C.Phi, sizeof(double) * 5 * N, cudaMemcpyDeviceToHost));
     return 0;
   }
+  // grid of the primitive conversion kernels: a few waves over the SMs
+  unsigned prim_grid() const {
+    long want = ((long)NQ * N + 255) / 256;
+    return (unsigned)std::min<long>(std::max<long>(want, 1), 152L * 16);
+  }
   int download(disco_state_view* v) override {
     CK(cudaStreamSynchronize(st));
     if (v->piph) CK(cudaMemcpy(v->piph, S.piph, sizeof(double) * N, cudaMemcpyDeviceToHost));
@@ -776,11 +779,17 @@ struct Instance : InstanceBase {
     if (v->prim) {
       if (sizeof(R) == sizeof(double)) {
         CK(cudaMemcpy(v->prim, S.prim, sizeof(double) * NQ * N, cudaMemcpyDeviceToHost));
-      } else {
-        std::vector<R> tmp((size_t)NQ * N);
-        CK(cudaMemcpy(tmp.data(), S.prim, sizeof(R) * NQ * N, cudaMemcpyDeviceToHost));
-        for (size_t i = 0; i < tmp.size(); ++i) v->prim[i] = (double)tmp[i];
-        for (long c = 0; c < N; ++c) v->prim[(size_t)UPP * N + c] += ring_Om_h[cell_ring_h[c]];
+      } else {   // widened (and back to the lab frame) on the device, then one copy
+        double* stage = nullptr;
+        if (cudaMalloc(&stage, sizeof(double) * NQ * N) != cudaSuccess) {
+          disco_set_error("download: no device memory for the FP64 staging copy");
+          return DISCO_E_NOMEM;
+        }
+        k_prim_out<R, NQ><<<prim_grid(), 256, 0, st>>>(S, stage);
+        cudaError_t e = cudaMemcpyAsync(v->prim, stage, sizeof(double) * NQ * N, cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        cudaFree(stage);
+        CK(e);
       }
     }
     double sc[SC_COUNT];
@@ -794,13 +803,24 @@ struct Instance : InstanceBase {
     if (v->dphi) CK(cudaMemcpy(S.dphi, v->dphi, sizeof(double) * N, cudaMemcpyHostToDevice));
     if (v->wiph) CK(cudaMemcpy(S.wiph, v->wiph, sizeof(double) * N, cudaMemcpyHostToDevice));
     if (v->cons) CK(cudaMemcpy(S.cons, v->cons, sizeof(double) * NQ * N, cudaMemcpyHostToDevice));
+    if (v->Phi && ct) CK(cudaMemcpy(C.Phi, v->Phi, sizeof(double) * 5 * N, cudaMemcpyHostToDevice));
     if (v->prim) {
-      std::vector<R> tmp((size_t)NQ * N);
-      for (size_t i = 0; i < tmp.size(); ++i) tmp[i] = (R)v->prim[i];
-      if (kMix<R>)
-        for (long c = 0; c < N; ++c)
-          tmp[(size_t)UPP * N + c] = (R)(v->prim[(size_t)UPP * N + c] - ring_Om_h[cell_ring_h[c]]);
-      CK(cudaMemcpy(S.prim, tmp.data(), sizeof(R) * NQ * N, cudaMemcpyHostToDevice));
+      if (sizeof(R) == sizeof(double)) {
+        CK(cudaMemcpy(S.prim, v->prim, sizeof(double) * NQ * N, cudaMemcpyHostToDevice));
+      } else {   // one copy of the FP64 view, converted (into the ring frame) on the device
+        double* stage = nullptr;
+        if (cudaMalloc(&stage, sizeof(double) * NQ * N) != cudaSuccess) {
+          disco_set_error("upload: no device memory for the FP64 staging copy");
+          return DISCO_E_NOMEM;
+        }
+        cudaError_t e = cudaMemcpyAsync(stage, v->prim, sizeof(double) * NQ * N, cudaMemcpyHostToDevice, st);
+        if (e == cudaSuccess) {
+          k_prim_in<R, NQ><<<prim_grid(), 256, 0, st>>>(S, stage);
+          e = cudaStreamSynchronize(st);
+        }
+        cudaFree(stage);
+        CK(e);
+      }
     }
     if (v->dphi) sync_dphi_r();
     if (ct && C.ev_ok) CK(cudaMemsetAsync(C.ev_ok, 0, sizeof(int), st));   // positions changed

@@ -1368,6 +1368,34 @@ __global__ void __launch_bounds__(256, kMix<R> ? 4 : 1) k_update(DevParams P, De
   }
 }
 
+// ---- FP64 primitives in and out of the device layout --------------------------
+// The C ABI's views hold FP64 primitives with prim[UPP] the lab omega; the
+// device holds R, relative to the ring frame on the mixed path.  The same
+// arithmetic the host would do (FP64 difference, then one rounding to R; the
+// widening and FP64 sum back), over all NQ * N values in a grid-stride loop.
+template <typename R, int NQ>
+__global__ void k_prim_in(DevState<R> S, const double* src) {
+  const size_t n = (size_t)NQ * S.N;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    double v = src[i];
+    if constexpr (kMix<R>) {
+      if (i / (size_t)S.N == (size_t)UPP) v -= S.ring_Om[S.cell_ring[i - (size_t)UPP * S.N]];
+    }
+    S.prim[i] = (R)v;
+  }
+}
+template <typename R, int NQ>
+__global__ void k_prim_out(DevState<R> S, double* dst) {
+  const size_t n = (size_t)NQ * S.N;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    double v = (double)S.prim[i];
+    if constexpr (kMix<R>) {
+      if (i / (size_t)S.N == (size_t)UPP) v += S.ring_Om[S.cell_ring[i - (size_t)UPP * S.N]];
+    }
+    dst[i] = v;
+  }
+}
+
 // ---- ghost rings: boundary_trans of Boundary/fixed.c and Boundary/fixed3d.c ----
 // fixed.c:11-46 evaluates initial() at the arithmetic-mean radius on r ghosts
 // only; fixed3d.c uses set_cell_init (boundary_functions.c:21) on r and z
