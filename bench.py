@@ -386,6 +386,14 @@ def measure_ours(args, wl, rank):
             # memory, K x (getmindt -> dt to host, timestep(dt) -> dt to
             # device), download
             res["profile"] = d.profile(3)
+            # report.c's domain sums as a device reduction (disco_gpu_report):
+            # host-timed calls, each including its result's copy to the host
+            d.report()
+            t0 = time.perf_counter()
+            for _ in range(10):
+                d.report()
+            rms = (time.perf_counter() - t0) / 10 * 1e3
+            res["report"] = {"ms_per_call": rms, "cells_per_s": cells / (rms / 1e3)}
             # the whole state: with constrained transport the face fluxes Phi too
             keys = ("piph", "dphi", "wiph", "prim", "cons") + (("Phi",) if "Phi" in st else ())
             pin = {k: torch.empty(st[k].shape, dtype=torch.float64, pin_memory=True).numpy()
@@ -619,6 +627,7 @@ def main():
                                     if p[2] > 0 else None)}
                     for p in prof},
         "e2e": res["e2e"],
+        **({"report_reduction": res["report"]} if "report" in res else {}),
         "gpu_launches": int(res[ch]["launches"]),
         "clocks": res[ch]["clocks"],
     }

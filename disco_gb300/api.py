@@ -53,6 +53,7 @@ class DiscoParams(C.Structure):
         ("dampUpperType", C.c_int), ("dampLowerType", C.c_int),
         ("grav_eps", C.c_double),
         ("read_errors", C.c_int),
+        ("sinkPar3", C.c_double),
     ]
 
 
@@ -128,6 +129,7 @@ SIGNATURES = {
     "disco_gpu_debug_ct": (C.c_int, [_P, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double),
                                      C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     "disco_gpu_getmindt_noalloc": (C.c_int, [_P, C.POINTER(C.c_double)]),
+    "disco_gpu_report": (C.c_int, [_P, C.POINTER(C.c_double), C.c_int]),
     "disco_batch_create": (C.c_int, [C.POINTER(_P), C.c_int, C.POINTER(_P)]),
     "disco_batch_run": (C.c_int, [_P, C.c_int]),
     "disco_batch_run_timed": (C.c_int, [_P, C.c_int, C.c_size_t, C.POINTER(C.c_double)]),
@@ -244,6 +246,16 @@ class Domain:
         dt = C.c_double()
         _check(lib().disco_gpu_getmindt_noalloc(self._g, C.byref(dt)), "disco_gpu_getmindt_noalloc")
         return dt.value
+
+    REPORT_KEYS = ("t", "q", "Mass", "Torque", "Torque2") + tuple(
+        f"Torque{i}_cut{n}" for n in range(5) for i in (1, 2))
+
+    def report(self) -> dict:
+        """report.c's domain sums from the device state (disco_gpu_report)."""
+        out = (C.c_double * len(self.REPORT_KEYS))()
+        rc = lib().disco_gpu_report(self._g, out, len(out))
+        _check(rc if rc < 0 else 0, "disco_gpu_report")
+        return {k: out[i] for i, k in enumerate(self.REPORT_KEYS)}
 
     def timestep(self, dt: float) -> None:
         _check(lib().disco_gpu_timestep(self._g, float(dt)), "disco_gpu_timestep")

@@ -278,10 +278,11 @@ DISCO_D R get_cs2(const DevParams& P, const DevPlanet* pl, R r, R phi) {  // ome
   return (R)1.0;
 }
 
-// planetaryForce (planet.c:138-188), mode 0.
+// planetaryForce (planet.c:138-188).  mode 1 (report.c) takes the force
+// components along the planet's direction instead of the cell's.
 template <typename R>
 DISCO_D void planetary_force(const DevParams& P, const DevPlanet& pl, R r, R phi, R z,
-                             R* fr, R* fp, R* fz) {
+                             R* fr, R* fp, R* fz, int mode = 0) {
   R rp = (R)pl.r, pp = (R)pl.phi;
   if (P.grav2D == 1) z = 0.0;
   else if (P.grav2D == 2) { rp = r; pp = phi; z = 1.0; }
@@ -294,6 +295,10 @@ DISCO_D void planetary_force(const DevParams& P, const DevPlanet& pl, R r, R phi
   R cosa = dx / script_r_perp, sina = dy / script_r_perp;
   R cosap = cosa * cosp + sina * sinp;
   R sinap = sina * cosp - cosa * sinp;
+  if (mode == 1) {
+    cosap = cosa * cos(pp) + sina * sin(pp);
+    sinap = sina * cos(pp) - cosa * sin(pp);
+  }
   if (script_r_perp <= (R)0.0) { cosap = 0.0; sinap = 0.0; }
   R sint = script_r_perp / script_r;
   R cost = z / script_r;

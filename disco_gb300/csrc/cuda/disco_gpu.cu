@@ -4,6 +4,7 @@
 #include "disco_gpu_debug.h"
 #include "disco_gpu_noalloc.h"
 #include "disco_gpu_batch.h"
+#include "disco_gpu_report.h"
 
 std::atomic<long long> g_launches{0};
 long long disco_gpu_launch_count(void) { return g_launches.load(); }
@@ -128,6 +129,11 @@ int disco_gpu_create(const disco_host_domain* dom, int precision, disco_gpu** ou
   if (!impl) return rc ? rc : DISCO_E_CUDA;
   *out = new disco_gpu{impl};
   return 0;
+}
+
+int disco_gpu_report(disco_gpu* g, double* out, int nout) {
+  if (!g || !out || nout < 0) { disco_set_error("disco_gpu_report: bad argument"); return DISCO_E_ARG; }
+  return g->impl->report(out, nout);
 }
 
 int disco_gpu_getmindt(disco_gpu* g, double* dt) {

@@ -16,6 +16,7 @@
 #include "kernels.cuh"
 #include "ct_kernels.cuh"
 #include "noalloc.cuh"
+#include "report.cuh"
 
 using namespace disco;
 
@@ -48,6 +49,7 @@ struct InstanceBase {
   virtual double time() = 0;
   virtual int debug_ct(int stage, double* E, double* B, double* Ephi, double* Phi) = 0;
   virtual int getmindt_noalloc(double* dt) = 0;
+  virtual int report(double* out, int nout) = 0;
   // batch support: launch one full step (getmindt + timestep) from piph
   // parity `par` on the instance's stream, then account for nsteps steps
   // taken outside the instance's own run()
@@ -417,6 +419,9 @@ struct Instance : InstanceBase {
       pl[i].eps = dom->planets[i].eps; pl[i].type = dom->planets[i].type;
     }
     CK(cudaMemcpy(S.planets, pl.data(), sizeof(DevPlanet) * MAX_PL, cudaMemcpyHostToDevice));
+    // report.c's mass ratio and the softening behind its torque cut radii
+    report_q = dom->Npl > 1 ? dom->planets[1].M / dom->planets[0].M : 0.0;
+    report_soft = p.sinkPar3;
     double scal[SC_COUNT] = {0, dom->t, 0, 0};
     unsigned long long inf = 0x7ff0000000000000ull;
     memcpy(&scal[SC_MIN], &inf, 8);
@@ -873,6 +878,33 @@ struct Instance : InstanceBase {
 
   // CFL dt with partial minima in the library's static scratch array: no
   // device allocation, no write to the instance (disco_gpu_noalloc.h).
+  // report.c as a device reduction: out = {t, q, Mass, Torque, Torque2,
+  // Torque1_cut[0], Torque2_cut[0], ..., Torque1_cut[4], Torque2_cut[4]}
+  double report_q = 0.0, report_soft = 0.0;
+  double* report_part = nullptr;
+  int report(double* out, int nout) override {
+    const int nb = (int)blocks(N, kReportBlock);
+    if (!report_part) {
+      int rc = dalloc(&report_part, (size_t)nb * kReportSums + kReportSums, keep);
+      if (rc) return rc;
+    }
+    k_report_blocks<R, NQ><<<nb, kReportBlock, 0, st>>>(P, S, report_soft, report_part);
+    k_report_final<<<1, 32, 0, st>>>(report_part, nb, report_part + (size_t)nb * kReportSums);
+    g_launches += 2;
+    CK(cudaGetLastError());
+    double sums[kReportSums], sc[SC_COUNT];
+    CK(cudaMemcpyAsync(sums, report_part + (size_t)nb * kReportSums, sizeof sums, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(sc, S.scal, sizeof sc, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    double all[2 + kReportSums];
+    all[0] = sc[SC_T];
+    all[1] = report_q;
+    all[2] = sums[0]; all[3] = sums[1]; all[4] = sums[2];
+    for (int n = 0; n < 5; ++n) { all[5 + 2 * n] = sums[3 + n]; all[6 + 2 * n] = sums[8 + n]; }
+    const int m = std::min(nout, 2 + kReportSums);
+    for (int i = 0; i < m; ++i) out[i] = all[i];
+    return m;
+  }
   int getmindt_noalloc(double* dt) override {
     long nb = blocks(N, kNoallocBlock);
     if (N > DISCO_NOALLOC_MAX_CELLS || nb > kNoallocMaxBlocks) {

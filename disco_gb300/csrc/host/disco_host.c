@@ -161,6 +161,7 @@ int disco_params_read(const char *path, disco_params *p)
    RI("DampInner_Type", dampInnerType); RI("DampOuter_Type", dampOuterType);
    RI("DampUpper_Type", dampUpperType); RI("DampLower_Type", dampLowerType);
    RD("Softening", grav_eps);
+   RD("Sink_Par3", sinkPar3);
 #undef RI
 #undef RD
    free(b);

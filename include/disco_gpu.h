@@ -105,6 +105,7 @@ typedef struct disco_params {
    int dampInnerType, dampOuterType, dampUpperType, dampLowerType;
    double grav_eps;
    int read_errors;   /* number of keys absent (readpar.c: err count) */
+   double sinkPar3;   /* Sink_Par3: the softening behind report.c's torque cut radii */
 } disco_params;
 
 /* One point mass: the fields of struct planet (paul.h:259-284) the hot path

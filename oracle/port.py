@@ -29,6 +29,7 @@ def _lib():
         L.disco_port_num_real.argtypes = [C.c_void_p]
         L.disco_port_free.argtypes = [C.c_void_p]
         L.disco_port_phi.argtypes = [C.c_void_p, _dp]
+        L.disco_port_report.argtypes = [C.c_void_p, _dp]
         _L = L
     return _L
 
@@ -63,6 +64,15 @@ class PortDomain:
             s["Phi"] = np.empty((5, N))
             _lib().disco_port_phi(self._d, s["Phi"].ctypes.data_as(_dp))
         return s
+
+    REPORT_KEYS = ("t", "q", "Mass", "Torque", "Torque2") + tuple(
+        f"Torque{i}_cut{n}" for n in range(5) for i in (1, 2))
+
+    def report(self) -> dict:
+        """report.c's domain sums (the restatement, serial reference order)."""
+        out = np.empty(len(self.REPORT_KEYS))
+        _lib().disco_port_report(self._d, out.ctypes.data_as(_dp))
+        return dict(zip(self.REPORT_KEYS, out.tolist()))
 
     def __del__(self):
         if getattr(self, "_d", None):

@@ -1741,6 +1741,76 @@ void disco_port_phi(const port_domain *d, double *Phi)
       for(int q = 0; q < 5; q++) Phi[(size_t)q*d->N + c] = d->cells[c].Phi[q];
 }
 
+/* report.c:4-329: the domain sums of one report line, in the reference's
+ * (j, k, i) loop order -- out = {t, q, Mass, Torque, Torque2,
+ * Torque1_cut[0], Torque2_cut[0], ..., Torque1_cut[4], Torque2_cut[4]}.
+ * planetaryForce's mode 1 takes the components along the planet's
+ * direction (planet.c:158-161). */
+static void planetary_force_m1(const disco_planet *pl, double r, double phi, double z,
+                               double *fr, double *fp, double *fz)
+{
+   double rp = pl->r, pp = pl->phi;
+   if(D->par.grav2D == 1) z = 0.0;
+   else if(D->par.grav2D == 2) { rp = r; pp = phi; z = 1.0; }
+   double cosp = cos(phi), sinp = sin(phi);
+   double dx = r*cosp - rp*cos(pp);
+   double dy = r*sinp - rp*sin(pp);
+   double script_r = sqrt(dx*dx + dy*dy + z*z);
+   double script_r_perp = sqrt(dx*dx + dy*dy);
+   double f1 = -fgrav(pl->M, script_r, pl->eps);
+   double cosa = dx/script_r_perp, sina = dy/script_r_perp;
+   double cosap = cosa*cos(pp) + sina*sin(pp);
+   double sinap = sina*cos(pp) - cosa*sin(pp);
+   if(script_r_perp <= 0.0) { cosap = 0.0; sinap = 0.0; }
+   double sint = script_r_perp/script_r, cost = z/script_r;
+   *fr = cosap*f1*sint;
+   *fp = sinap*f1*sint;
+   *fz = f1*cost;
+}
+
+void disco_port_report(port_domain *d, double *out)
+{
+   D = d;
+   double Mass = 0.0, Torque = 0.0, Torque2 = 0.0, T1c[5] = {0}, T2c[5] = {0};
+   double soft = d->par.sinkPar3;
+   for(int j = d->NgRa; j < d->Nr - d->NgRb; j++)
+      for(int k = d->NgZa; k < d->Nz - d->NgZb; k++) {
+         int jk = j + d->Nr*k;
+         for(int i = 0; i < d->Np[jk]; i++) {
+            pcell *c = &d->ring[jk][i];
+            double phi = c->piph - .5*c->dphi;
+            double rho = c->prim[RHO];
+            double phip = c->piph, phim = phip - c->dphi;
+            double xp[3] = {d->rj[j], phip, d->zk[k]};
+            double xm[3] = {d->rj[j - 1], phim, d->zk[k - 1]};
+            double dV = get_dV(xp, xm);
+            double r = centroid(xp[0], xm[0], 1);
+            Mass += rho*dV;
+            if(d->Npl > 1) {
+               double fr, fp, fz, fp2;
+               planetary_force_m1(&d->pl[0], r, phi, 0.0, &fr, &fp2, &fz);
+               planetary_force_m1(&d->pl[1], r, phi, 0.0, &fr, &fp, &fz);
+               double rS = d->pl[0].r, rp = d->pl[1].r, pp = d->pl[1].phi;
+               double dx = r*cos(phi) - rp*cos(pp);
+               double dy = r*sin(phi) - rp*sin(pp);
+               double script_r = sqrt(dx*dx + dy*dy);
+               double t1v = (rho - 1.0)*rp*fp*dV;
+               double t2v = (rho - 1.0)*rS*fp2*dV;
+               Torque -= t1v;
+               Torque2 -= t2v;
+               for(int n = 0; n < 5; n++) {
+                  double r_cut = (double)(n + 1.)*soft;
+                  if(script_r > r_cut) { T1c[n] -= t1v; T2c[n] -= t2v; }
+               }
+            }
+         }
+      }
+   out[0] = d->t;
+   out[1] = d->Npl > 1 ? d->pl[1].M/d->pl[0].M : 0.0;
+   out[2] = Mass; out[3] = Torque; out[4] = Torque2;
+   for(int n = 0; n < 5; n++) { out[5 + 2*n] = T1c[n]; out[6 + 2*n] = T2c[n]; }
+}
+
 long disco_port_num_real(const port_domain *d)
 {
    long n = 0;

@@ -12,7 +12,8 @@
  * Usage (in a directory holding in.par):
  *    disco_ref init  OUT.bin
  *    disco_ref grad  OUT.bin          (plm_phi + faces + plm_trans, then dump)
- *    disco_ref run N OUT.bin          (N full RK steps, then dump)
+ *    disco_ref run N OUT.bin          (N full RK steps, then dump, then the
+ *                                      reference's report() into report.dat)
  *    disco_ref time N                 (N steps, prints zone-updates/s only)
  *
  * Dump format: little-endian raw, see write_state() / write_faces();
@@ -34,6 +35,7 @@ void freeDomain(struct domain *);
 void plm_phi(struct domain *);
 void setup_faces(struct domain *, int);
 void plm_trans(struct domain *, struct face *, int, int);
+void report(struct domain *);
 
 #define DUMP_MAGIC 0x4f435344  /* "DSCO" */
 
@@ -186,6 +188,9 @@ int main(int argc, char **argv)
          FILE *f = fopen(argv[3], "wb");
          write_state(d, f, 0);
          fclose(f);
+         /* the reference's own diagnostics of the final state: one line
+          * appended to report.dat in the working directory */
+         report(d);
       }
    } else {
       fprintf(stderr, "unknown mode %s\n", mode);

@@ -80,7 +80,13 @@ def run_case(name: str, ref: str) -> None:
         ini = read_dump(os.path.join(td, "init.bin"))
         grd = read_dump(os.path.join(td, "grad.bin"))
         run = read_dump(os.path.join(td, "run.bin"))
-    out = {"par_text": np.array(par), "nsteps": nsteps, "cfg": np.array(cfg),
+        # report.c's line for the final state (printed with 7 significant
+        # digits; its "%.7le%le" leaves no space after q, so split on the
+        # exponent form every field has)
+        line = open(os.path.join(td, "report.dat")).read().strip().splitlines()[-1]
+        rep = np.array([float(v) for v in
+                        re.findall(r"[-+]?\d\.\d+e[-+]\d{2}(?:\d(?!\.))?", line)])
+    out = {"par_text": np.array(par), "nsteps": nsteps, "cfg": np.array(cfg), "report": rep,
            "Np": ini["Np"], "r_jph": ini["r_jph"], "z_kph": ini["z_kph"], "real": ini["real"],
            "init_piph": ini["piph"], "init_dphi": ini["dphi"], "init_prim": ini["prim"],
            "init_cons": ini["cons"], "init_wiph": ini["wiph"],

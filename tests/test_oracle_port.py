@@ -92,3 +92,32 @@ def test_port_circumbinary_vs_golden():
     for q in range(s["cons"].shape[0]):
         assert rel_l1(s["cons"][q, real], g["run_cons"][q, real]) < 1e-15, q
 
+
+
+# report.c's line: t, q, then 8 per-body sink accumulators per body (zero
+# here), then Mass, Torque, Torque2 and the five (Torque1_cut, Torque2_cut)
+def _ref_report(g, npl):
+    rep = g["report"]
+    tail = rep[2 + 8 * npl:]
+    keys = ["Mass", "Torque", "Torque2"] + [f"Torque{i}_cut{n}" for n in range(5) for i in (1, 2)]
+    out = {"t": rep[0], "q": rep[1]}
+    out.update(dict(zip(keys, tail)))
+    assert np.all(rep[2:2 + 8 * npl] == 0.0)   # no sinks: the accumulators stay zero
+    return out
+
+
+@pytest.mark.parametrize("name,npl", [("cfg3_n24", 2), ("cfg2_n12", 1)])
+def test_port_report_vs_reference(name, npl):
+    """The restated report sums equal the reference's report line to its
+    7 printed significant digits."""
+    import disco_gb300 as dg
+    from oracle.port import PortDomain
+    g = load_golden(name)
+    h = dg.HostDomain(dg.read_params(write_par(g["par_text"])),
+                      dg.read_modules(os.path.join(ROOT, str(g["cfg"]), "Makefile_opt.in")))
+    d = PortDomain(h)
+    d.run(int(g["nsteps"]))
+    mine = d.report()
+    ref = _ref_report(g, npl)
+    for k, v in ref.items():
+        assert abs(mine[k] - v) <= 6e-7 * abs(v) + 1e-300, (k, mine[k], v)
