@@ -245,8 +245,8 @@ struct Instance : InstanceBase {
         return DISCO_E_MODULE;
       }
     }
-    if (dom->mod.boundary > 1) {
-      disco_set_error("zero-gradient boundaries are not built");
+    if (dom->mod.boundary > 1 && (Phys::MHD || Phys::GR)) {
+      disco_set_error("zero-gradient / outflow boundaries are built for the hydro module only");
       return DISCO_E_MODULE;
     }
 
@@ -494,6 +494,22 @@ struct Instance : InstanceBase {
       LAUNCH("wcell_avg", (k_wcell_avg<R><<<nring, 64, (maxring + 1) * sizeof(double), st>>>(P, S)));
   }
   void launch_boundary() {
+    if (P.boundary_id >= 2) {   // zerograd (3) / outflow3d (2): layer by layer
+      const int diode = P.boundary_id == 2;
+      if (Nr > 1) {   // boundary_trans(dim 1): inner layers inward, then outer outward
+        for (int j = P.NgRa - 1; j >= 0; --j)
+          LAUNCH("boundary", (k_bc_zerograd<R, NQ><<<blocks(Nz, 64), 64, 0, st>>>(P, S, 1, 0, j, diode)));
+        for (int j = Nr - P.NgRb; j < Nr; ++j)
+          LAUNCH("boundary", (k_bc_zerograd<R, NQ><<<blocks(Nz, 64), 64, 0, st>>>(P, S, 1, 1, j, diode)));
+      }
+      if (Nz > 1) {   // boundary_trans(dim 2)
+        for (int k = P.NgZa - 1; k >= 0; --k)
+          LAUNCH("boundary", (k_bc_zerograd<R, NQ><<<blocks(Nr, 64), 64, 0, st>>>(P, S, 2, 0, k, diode)));
+        for (int k = Nz - P.NgZb; k < Nz; ++k)
+          LAUNCH("boundary", (k_bc_zerograd<R, NQ><<<blocks(Nr, 64), 64, 0, st>>>(P, S, 2, 1, k, diode)));
+      }
+      return;
+    }
     if (S.nghost > 0)
       LAUNCH("boundary", (k_boundary<R, NQ><<<S.nghost, kTileCells, 0, st>>>(P, S)));
   }

@@ -1442,6 +1442,88 @@ __global__ void __launch_bounds__(kTileCells) k_boundary(DevParams P, DevState<R
   for (int q = 0; q < NQ; ++q) S.prim[q * S.N + c] = (R)prim[q];
 }
 
+// ---- zero-gradient / outflow ghosts: Boundary/zerograd.c, Boundary/outflow3d.c ----
+// boundary_zerograd_{rinn,rout,zbot,ztop} (boundary_functions.c:269-440) copy
+// the neighbouring ring inward of each ghost ring onto it by phi overlap
+// (set_cells_copy_distant, :90-158), layer by layer from the real domain
+// outward; outflow3d is the same with a diode on the normal velocity.  One
+// thread per ghost ring of a layer walks both rings in the reference's order
+// (the same overlaps summed in the same order); the layers are separate
+// launches.  On the mixed path the copy is made in the lab frame (ring
+// frames added and removed in FP64).
+// dim 1: rings (j, k) for all k, source j + 1 (side 0, inner) or j - 1
+// (side 1, outer); dim 2: rings (j, k) for all j, source k + 1 or k - 1.
+template <typename R, int NQ>
+__global__ void k_bc_zerograd(DevParams P, DevState<R> S, int dim, int side, int layer, int diode) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  int j, k, j1, k1;
+  if (dim == 1) {
+    if (t >= P.Nz) return;
+    k = k1 = t;
+    j = layer;
+    j1 = side == 0 ? j + 1 : j - 1;
+  } else {
+    if (t >= P.Nr) return;
+    j = j1 = t;
+    k = layer;
+    k1 = side == 0 ? k + 1 : k - 1;
+  }
+  const int jk = j + P.Nr * k, jk1 = j1 + P.Nr * k1;
+  const int off = S.ring_off[jk], Np = S.ring_off[jk + 1] - off;
+  const int off1 = S.ring_off[jk1], Np1 = S.ring_off[jk1 + 1] - off1;
+  const double Pmax = P.phi_max;
+  const int N = S.N;
+  const double Om = kMix<R> ? S.ring_Om[jk] : 0.0, Om1 = kMix<R> ? S.ring_Om[jk1] : 0.0;
+  // the first source cell that holds the lower edge of cell 0
+  int i1 = 0;
+  {
+    const double phi0 = S.piph[off] - S.dphi[off];
+    for (i1 = 0; i1 < Np1; ++i1) {
+      const double dphip = get_signed_dp(S.piph[off1 + i1], phi0, Pmax);
+      const double dphim = dphip - S.dphi[off1 + i1];
+      if (dphip > 0 && dphim <= 0.0) break;
+    }
+    if (i1 >= Np1) i1 = 0;
+  }
+  for (int i = 0; i < Np; ++i) {
+    const int c = off + i;
+    const double phip = S.piph[c], phim = S.piph[c] - S.dphi[c];
+    double acc[NQ];
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) acc[q] = 0.0;
+    double phip1, phim1;
+    int walk = 0;   // at most one turn of the source ring (guards a non-finite phi)
+    do {
+      const int c1 = off1 + i1;
+      phip1 = S.piph[c1];
+      phim1 = S.piph[c1] - S.dphi[c1];
+      for (int w = 0; w < 4 && phip1 < phim; ++w) { phip1 += Pmax; phim1 += Pmax; }
+      for (int w = 0; w < 4 && phim1 > phip; ++w) { phip1 -= Pmax; phim1 -= Pmax; }
+      const double p1 = phip < phip1 ? phip : phip1;
+      const double p2 = phim > phim1 ? phim : phim1;
+      const double dphi = p1 - p2;
+#pragma unroll
+      for (int q = 0; q < NQ; ++q) {
+        double v = (double)S.prim[q * N + c1];
+        if (kMix<R> && q == UPP) v += Om1;
+        acc[q] += v * dphi;
+      }
+      i1 = i1 < Np1 - 1 ? i1 + 1 : 0;
+    } while (phip1 < phip && ++walk <= Np1);
+    i1 = i1 > 0 ? i1 - 1 : Np1 - 1;
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) {
+      double v = acc[q] / S.dphi[c];
+      if (diode) {   // outflow3d: no inflow through the boundary
+        const int qn = dim == 1 ? URR : UZZ;
+        if (q == qn && (side == 0 ? v > 0 : v < 0)) v = 0.0;
+      }
+      if (kMix<R> && q == UPP) v -= Om;
+      S.prim[q * N + c] = (R)v;
+    }
+  }
+}
+
 // ---- getmindt, misc.c:39-84 -------------------------------------------------
 template <typename Phys, typename R, int NQ>
 __global__ void k_mindt(DevParams P, DevState<R> S) {

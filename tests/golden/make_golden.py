@@ -44,6 +44,10 @@ CASES = {
     # one instance of the planet-disk batch: alpha viscosity, locally
     # isothermal, a planet on a circular orbit
     "cfg3_n24": ("configs/cfg3_planet_disk", {"Num_R": 24}, 10),
+    # zero-gradient ghosts (Boundary/zerograd.c) on the vortex, in 3D so the
+    # z passes run too; outflow ghosts (Boundary/outflow3d.c) on the planet disk
+    "cfg1_zerograd": ("configs/cfg1_vortex_zerograd", {"Num_R": 16, "Num_Z": 2}, 10),
+    "cfg3_outflow": ("configs/cfg3_planet_disk_outflow", {"Num_R": 24}, 10),
     # GRMHD thin disk around a Schwarzschild black hole (Kerr-Schild
     # cylindrical metric, HLL, cell-centred B) at 12 x 4 rings
     "cfg4_n12": ("configs/cfg4_grmhd_disk", {"Num_R": 12, "Num_Z": 4}, 5),

@@ -16,7 +16,9 @@ CASES = {"cfg1_n24": "configs/cfg1_vortex", "cfg2_n12": "configs/cfg2_mhd_disk",
          "cfg1_hll_static": "configs/cfg1_vortex", "cfg1_exact_mesh": "configs/cfg1_vortex",
          "cfg1_rotframe": "configs/cfg1_vortex",
          "cfg3_n24": "configs/cfg3_planet_disk", "cfg5_n16": "configs/cfg5_cbd_mhd",
-         "cfg4_n12": "configs/cfg4_grmhd_disk"}
+         "cfg4_n12": "configs/cfg4_grmhd_disk",
+         "cfg1_zerograd": "configs/cfg1_vortex_zerograd",
+         "cfg3_outflow": "configs/cfg3_planet_disk_outflow"}
 # GRMHD runs on the FP64 path only
 FP64_ONLY = {"cfg4_n12"}
 
@@ -125,7 +127,7 @@ def test_mixed_precision_error(name):
 # minmod branches in a few cells (the error falls to 9e-7 at 96 rings and
 # 3e-7 at 256, with or without the planet or viscosity); the 1e-6 bar is
 # checked at batch-instance resolution by test_mixed_precision_planet_disk.
-MIXED_BOUND = {"cfg3_n24": 3e-6}
+MIXED_BOUND = {"cfg3_n24": 3e-6, "cfg3_outflow": 3e-6}
 
 
 def test_mixed_precision_planet_disk():
