@@ -230,3 +230,16 @@ def test_mhd_disk_vs_oracle_port():
         assert e < 1e-12, (q, e)
     assert st["nan_cells"] == 0 and st["face_errors"] == 0
     d.close()
+
+
+def test_zerograd_rejected_for_mhd(tmp_path):
+    """Zero-gradient ghosts are built for the hydro module only: an MHD
+    configuration asking for them is refused at create."""
+    import disco_gb300 as dg
+    cfg = os.path.join(ROOT, "configs/cfg2_mhd_disk")
+    src = open(os.path.join(cfg, "Makefile_opt.in")).read()
+    mk = tmp_path / "Makefile_opt.in"
+    mk.write_text(src.replace("fixed3d", "zerograd").replace("BOUNDARY = fixed\n", "BOUNDARY = zerograd\n"))
+    assert "zerograd" in mk.read_text()
+    with pytest.raises(dg.DiscoError, match="hydro module only"):
+        dg.Domain(os.path.join(cfg, "in.par"), str(mk))
