@@ -212,6 +212,8 @@ def kernel_bytes(name: str, N: int, nf: dict, nq: int, sw: int, ct: bool) -> flo
         return N * (sw + f8)
     if name == "boundary":
         return N * 2 * f8
+    if name == "diag":   # ring diagnostics: five primitives and the position of each cell
+        return N * (5 * sw + 2 * f8)
     if name == "anchor":
         return N * f8
     return 0.0

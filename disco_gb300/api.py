@@ -65,6 +65,7 @@ class DiscoModules(C.Structure):
         ("boundary_name", C.c_char * 64), ("planets_name", C.c_char * 64),
         ("metric", C.c_int), ("frame", C.c_int),
         ("metric_name", C.c_char * 64), ("frame_name", C.c_char * 64),
+        ("analysis", C.c_int), ("analysis_name", C.c_char * 64),
     ]
 
 
@@ -130,6 +131,9 @@ SIGNATURES = {
                                      C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     "disco_gpu_getmindt_noalloc": (C.c_int, [_P, C.POINTER(C.c_double)]),
     "disco_gpu_report": (C.c_int, [_P, C.POINTER(C.c_double), C.c_int]),
+    "disco_gpu_diag_count": (C.c_int, [_P]),
+    "disco_gpu_diag_download": (C.c_int, [_P, C.POINTER(C.c_double), C.c_longlong, C.POINTER(C.c_double)]),
+    "disco_gpu_diag_upload": (C.c_int, [_P, C.POINTER(C.c_double), C.c_longlong, C.c_double]),
     "disco_batch_create": (C.c_int, [C.POINTER(_P), C.c_int, C.POINTER(_P)]),
     "disco_batch_run": (C.c_int, [_P, C.c_int]),
     "disco_batch_run_timed": (C.c_int, [_P, C.c_int, C.c_size_t, C.POINTER(C.c_double)]),
@@ -256,6 +260,31 @@ class Domain:
         rc = lib().disco_gpu_report(self._g, out, len(out))
         _check(rc if rc < 0 else 0, "disco_gpu_report")
         return {k: out[i] for i, k in enumerate(self.REPORT_KEYS)}
+
+    def diagnostics(self) -> dict:
+        """analysis.c's ring diagnostics as timestep() accumulated them:
+        Qrz [Nr*Nz, n] (ring jk = k*Nr + j) and t_avg (disco_gpu_diag_download).
+        Qrz / t_avg is what the reference's output step writes."""
+        n = lib().disco_gpu_diag_count(self._g)
+        _check(n if n < 0 else 0, "disco_gpu_diag_count")
+        nring = self.host.Nr * self.host.Nz
+        q = np.zeros((nring, n), dtype=np.float64)
+        t = C.c_double(0.0)
+        rc = lib().disco_gpu_diag_download(self._g, q.ctypes.data_as(C.POINTER(C.c_double)), q.size,
+                                           C.byref(t))
+        _check(rc if rc < 0 else 0, "disco_gpu_diag_download")
+        return {"Qrz": q, "t_avg": t.value}
+
+    def set_diagnostics(self, Qrz=None, t_avg: float = 0.0) -> None:
+        """Replace the accumulators (restart), or zero them when Qrz is None
+        (zero_diagnostics)."""
+        if Qrz is None:
+            rc = lib().disco_gpu_diag_upload(self._g, None, 0, 0.0)
+        else:
+            a = np.ascontiguousarray(Qrz, dtype=np.float64)
+            rc = lib().disco_gpu_diag_upload(self._g, a.ctypes.data_as(C.POINTER(C.c_double)), a.size,
+                                             float(t_avg))
+        _check(rc if rc < 0 else 0, "disco_gpu_diag_upload")
 
     def timestep(self, dt: float) -> None:
         _check(lib().disco_gpu_timestep(self._g, float(dt)), "disco_gpu_timestep")

@@ -5,6 +5,7 @@
 #include "disco_gpu_noalloc.h"
 #include "disco_gpu_batch.h"
 #include "disco_gpu_report.h"
+#include "disco_gpu_diag.h"
 
 std::atomic<long long> g_launches{0};
 long long disco_gpu_launch_count(void) { return g_launches.load(); }
@@ -134,6 +135,21 @@ int disco_gpu_create(const disco_host_domain* dom, int precision, disco_gpu** ou
 int disco_gpu_report(disco_gpu* g, double* out, int nout) {
   if (!g || !out || nout < 0) { disco_set_error("disco_gpu_report: bad argument"); return DISCO_E_ARG; }
   return g->impl->report(out, nout);
+}
+
+int disco_gpu_diag_count(disco_gpu* g) {
+  if (!g) { disco_set_error("disco_gpu_diag_count: null argument"); return DISCO_E_ARG; }
+  return g->impl->diag(0, nullptr, -1, nullptr, nullptr, 0.0);
+}
+
+int disco_gpu_diag_download(disco_gpu* g, double* Qrz, long long len, double* t_avg) {
+  if (!g || (Qrz && len < 0)) { disco_set_error("disco_gpu_diag_download: bad argument"); return DISCO_E_ARG; }
+  return g->impl->diag(0, Qrz, Qrz ? len : -1, t_avg, nullptr, 0.0);
+}
+
+int disco_gpu_diag_upload(disco_gpu* g, const double* Qrz, long long len, double t_avg) {
+  if (!g) { disco_set_error("disco_gpu_diag_upload: null argument"); return DISCO_E_ARG; }
+  return g->impl->diag(Qrz ? 1 : 2, nullptr, len, nullptr, Qrz, t_avg);
 }
 
 int disco_gpu_getmindt(disco_gpu* g, double* dt) {

@@ -17,6 +17,7 @@
 #include "ct_kernels.cuh"
 #include "noalloc.cuh"
 #include "report.cuh"
+#include "diag.cuh"
 
 using namespace disco;
 
@@ -50,6 +51,7 @@ struct InstanceBase {
   virtual int debug_ct(int stage, double* E, double* B, double* Ephi, double* Phi) = 0;
   virtual int getmindt_noalloc(double* dt) = 0;
   virtual int report(double* out, int nout) = 0;
+  virtual int diag(int op, double* Qrz, long long n, double* t_avg, const double* set, double set_t) = 0;
   // batch support: launch one full step (getmindt + timestep) from piph
   // parity `par` on the instance's stream, then account for nsteps steps
   // taken outside the instance's own run()
@@ -365,6 +367,16 @@ struct Instance : InstanceBase {
       S.ghost_ring = d_gr; S.ghost_i0 = d_gi; S.nghost = (int)gr.size();
     }
     A(&S.planets, MAX_PL); A(&S.scal, SC_COUNT); A(&S.errs, 1);
+    diag_id = dom->mod.analysis;
+    diag_n = diag_count(diag_id);
+    if (diag_id == DISCO_DIAG_MHDMRI && NQ < 8) {
+      disco_set_error("ANALYSIS=diag_mhdmri reads magnetic fields: MHD or GRMHD modules only");
+      return DISCO_E_MODULE;
+    }
+    if (diag_n) {
+      A(&diag_Qrz, (size_t)nring * diag_n);
+      CK(cudaMemset(diag_Qrz, 0, sizeof(double) * nring * diag_n));
+    }
     S.ct = ct ? 1 : 0;
     if (ct) {
       A(&S.Eraw, (size_t)8 * N); A(&S.Braw, (size_t)8 * N);
@@ -598,10 +610,53 @@ struct Instance : InstanceBase {
     launch_boundary();
     if (first) launch_faces();
   }
-  // timestep.c:7-54 with Timestep 0 (RK2)
+  // add_diagnostics (analysis.c:52-108) with the ANALYSIS plugin
+  int diag_id = -1, diag_n = 0;
+  double* diag_Qrz = nullptr;
+  void launch_diag() {
+    switch (diag_id) {
+      case 0: LAUNCH("diag", (k_diag<R, NQ, 0><<<nring, kDiagBlock, 0, st>>>(P, S, diag_Qrz))); break;
+      case 1: LAUNCH("diag", (k_diag<R, NQ, 1><<<nring, kDiagBlock, 0, st>>>(P, S, diag_Qrz))); break;
+      case 2: LAUNCH("diag", (k_diag<R, NQ, 2><<<nring, kDiagBlock, 0, st>>>(P, S, diag_Qrz))); break;
+      case 3: LAUNCH("diag", (k_diag<R, NQ, 3><<<nring, kDiagBlock, 0, st>>>(P, S, diag_Qrz))); break;
+      case 4:
+        if constexpr (NQ >= 8)
+          LAUNCH("diag", (k_diag<R, NQ, 4><<<nring, kDiagBlock, 0, st>>>(P, S, diag_Qrz)));
+        break;
+      default: break;
+    }
+  }
+  // timestep.c:7-54 with Timestep 0 (RK2), then add_diagnostics (:51)
   void step_kernels() {
     substep(0.0, 1.0, 1);
     substep(0.5, 0.5, 0);
+    launch_diag();
+  }
+  // Ring diagnostics: Qrz [Nr*Nz][n] and t_avg, as analysis.c keeps them
+  // op 0: read (Qrz may be null); op 1: replace with `set` and set_t
+  // (restart); op 2: zero (zero_diagnostics, analysis.c:9-27)
+  int diag(int op, double* Qrz, long long n, double* t_avg, const double* set, double set_t) override {
+    if (!diag_n) return 0;
+    const size_t tot = (size_t)nring * diag_n;
+    if (op == 1 || op == 2) {
+      if (op == 1) {
+        if (!set || n != (long long)tot) { disco_set_error("disco_gpu_diag_upload: size mismatch"); return DISCO_E_ARG; }
+        CK(cudaMemcpyAsync(diag_Qrz, set, sizeof(double) * tot, cudaMemcpyHostToDevice, st));
+      } else {
+        set_t = 0.0;
+        CK(cudaMemsetAsync(diag_Qrz, 0, sizeof(double) * tot, st));
+      }
+      CK(cudaMemcpyAsync(&S.scal[SC_TAVG], &set_t, sizeof(double), cudaMemcpyHostToDevice, st));
+      CK(cudaStreamSynchronize(st));
+      return diag_n;
+    }
+    if (Qrz && n >= 0) {
+      if (n < (long long)tot) { disco_set_error("disco_gpu_diag_download: buffer too small"); return DISCO_E_ARG; }
+      CK(cudaMemcpyAsync(Qrz, diag_Qrz, sizeof(double) * tot, cudaMemcpyDeviceToHost, st));
+    }
+    if (t_avg) CK(cudaMemcpyAsync(t_avg, &S.scal[SC_TAVG], sizeof(double), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    return diag_n;
   }
 
   int getmindt(double* dt) override {

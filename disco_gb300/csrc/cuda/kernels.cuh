@@ -110,8 +110,9 @@ struct DevState {
 };
 
 // scal: [SC_DT] dt (FP64), [SC_T] t, [SC_MIN] min-dt accumulator (bits),
-// [SC_DTF] dt rounded to FP32, stored in the first 4 bytes of the slot.
-enum { SC_DT = 0, SC_T = 1, SC_MIN = 2, SC_DTF = 3, SC_COUNT = 4 };
+// [SC_DTF] dt rounded to FP32, stored in the first 4 bytes of the slot,
+// [SC_TAVG] the time the ring diagnostics have accumulated over.
+enum { SC_DT = 0, SC_T = 1, SC_MIN = 2, SC_DTF = 3, SC_TAVG = 4, SC_COUNT = 5 };
 
 // The mixed path (R = float) keeps positions, conserved sums and face
 // fluxes of B in FP64 but does every other product in R.

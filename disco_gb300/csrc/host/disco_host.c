@@ -223,6 +223,7 @@ int disco_modules_read(const char *path, disco_modules *m)
    /* METRIC and FRAME matter to GRMHD only; absent keys read as "" */
    if(mk_value(b, "METRIC", m->metric_name, sizeof m->metric_name)) m->metric_name[0] = 0;
    if(mk_value(b, "FRAME", m->frame_name, sizeof m->frame_name)) m->frame_name[0] = 0;
+   if(mk_value(b, "ANALYSIS", m->analysis_name, sizeof m->analysis_name)) m->analysis_name[0] = 0;
    if(!mk_value(b, "GEOMETRY", v, sizeof v) && strcmp(v, "cylindrical") != 0) {
       free(b);
       disco_set_error("GEOMETRY: only cylindrical is built");
@@ -235,6 +236,7 @@ int disco_modules_read(const char *path, disco_modules *m)
    static const char *ini[] = {"vortex_gauss", "disk_mhd", "disk_planet", "disk_cbd", "gr_disk"};
    static const char *bnd[] = {"fixed", "fixed3d", "outflow3d", "zerograd"};
    static const char *pla[] = {"none", "sun", "circular", "cm"};
+   static const char *ana[] = {"diag_euler", "diag_disk2d", "diag_cb", "diag_bl", "diag_mhdmri"};
    int i;
    m->hydro = m->initial = m->boundary = m->planets = -1;
    for(i = 0; i < 3; i++) if(!strcmp(m->hydro_name, hyd[i])) m->hydro = i;
@@ -243,7 +245,10 @@ int disco_modules_read(const char *path, disco_modules *m)
    m->frame = !strcmp(m->frame_name, "normal") ? DISCO_FRAME_NORMAL : DISCO_FRAME_NONE;
    for(i = 0; i < 4; i++) if(!strcmp(m->boundary_name, bnd[i])) m->boundary = i;
    for(i = 0; i < 4; i++) if(!strcmp(m->planets_name, pla[i])) m->planets = i;
+   m->analysis = DISCO_DIAG_NONE;
+   for(i = 0; i < 5; i++) if(!strcmp(m->analysis_name, ana[i])) m->analysis = i;
    char msg[256];
+   if(m->analysis_name[0] && m->analysis < 0) { snprintf(msg, sizeof msg, "ANALYSIS=%s not built", m->analysis_name); disco_set_error(msg); return DISCO_E_MODULE; }
    if(m->hydro < 0) { snprintf(msg, sizeof msg, "HYDRO=%s not built", m->hydro_name); disco_set_error(msg); return DISCO_E_MODULE; }
    if(m->initial < 0) { snprintf(msg, sizeof msg, "INITIAL=%s not built", m->initial_name); disco_set_error(msg); return DISCO_E_MODULE; }
    if(m->boundary < 0) { snprintf(msg, sizeof msg, "BOUNDARY=%s not built", m->boundary_name); disco_set_error(msg); return DISCO_E_MODULE; }

@@ -58,6 +58,11 @@ enum disco_boundary_id{ DISCO_BC_FIXED = 0, DISCO_BC_FIXED3D = 1,
                         DISCO_BC_OUTFLOW3D = 2, DISCO_BC_ZEROGRAD = 3 };
 enum disco_planets_id { DISCO_PL_NONE = 0, DISCO_PL_SUN = 1,
                         DISCO_PL_CIRCULAR = 2, DISCO_PL_CM = 3 };
+/* ANALYSIS of Makefile_opt.in: the Diagnostics/ plugin whose ring averages
+ * timestep() accumulates (analysis.c:52-108, timestep.c:51) */
+enum disco_analysis_id{ DISCO_DIAG_NONE = -1, DISCO_DIAG_EULER = 0,
+                        DISCO_DIAG_DISK2D = 1, DISCO_DIAG_CB = 2,
+                        DISCO_DIAG_BL = 3, DISCO_DIAG_MHDMRI = 4 };
 
 #define DISCO_MAX_PLANETS 4
 #define DISCO_NUM_G 2   /* ghost rings per side: paul.h:20 NUM_G */
@@ -69,6 +74,8 @@ typedef struct disco_modules {
    char initial_name[64], hydro_name[64], boundary_name[64], planets_name[64];
    int metric, frame;            /* GRMHD: disco_metric_id, disco_frame_id */
    char metric_name[64], frame_name[64];
+   int analysis;                 /* ANALYSIS: disco_analysis_id, or -1 when absent */
+   char analysis_name[64];
 } disco_modules;
 
 /* Run-time parameters: the hot-path subset of struct param_list

@@ -30,6 +30,7 @@ def _lib():
         L.disco_port_free.argtypes = [C.c_void_p]
         L.disco_port_phi.argtypes = [C.c_void_p, _dp]
         L.disco_port_report.argtypes = [C.c_void_p, _dp]
+        L.disco_port_diag.argtypes = [C.c_void_p, _dp, _dp]
         _L = L
     return _L
 
@@ -73,6 +74,14 @@ class PortDomain:
         out = np.empty(len(self.REPORT_KEYS))
         _lib().disco_port_report(self._d, out.ctypes.data_as(_dp))
         return dict(zip(self.REPORT_KEYS, out.tolist()))
+
+    def diagnostics(self) -> dict:
+        """analysis.c's ring accumulators: Qrz [Nr*Nz, n] and t_avg."""
+        n = _lib().disco_port_diag(self._d, None, None)
+        q = np.zeros((self.host.Nr * self.host.Nz, n))
+        t = C.c_double()
+        _lib().disco_port_diag(self._d, q.ctypes.data_as(_dp), C.byref(t))
+        return {"Qrz": q, "t_avg": t.value}
 
     def __del__(self):
         if getattr(self, "_d", None):

@@ -60,6 +60,8 @@ typedef struct port_domain {
    int ntracks[2];
    disco_planet pl[DISCO_MAX_PLANETS];
    double gam;
+   int nd;                /* num_diagnostics() of the ANALYSIS plugin */
+   double *Qrz, t_avg;    /* struct diagnostic_avg: Qrz[jk*nd + q] */
 } port_domain;
 
 static port_domain *D;   /* the domain being advanced (module statics in the reference) */
@@ -146,9 +148,10 @@ static double mesh_om(const double *x)  /* omega.c:56-74 */
    return 0.0;
 }
 static double fgrav(double M, double r, double eps);
+extern double disco_port_phi_order;
 static double phigrav(double M, double r, double eps)
 {
-   double n = 2.0;
+   double n = disco_port_phi_order;
    return M/pow(pow(r, n) + pow(eps, n), 1./n);
 }
 static double get_cs2(const double *x)  /* omega.c:157-209 */
@@ -188,9 +191,14 @@ static double get_height_om(const double *x)  /* omega.c:132-155 */
 }
 
 /* ---- planet.c (point masses) ---------------------------------------------- */
+/* planet.c:4 keeps the potential's order in a mutable global, so the
+ * reference's pow() calls stay libm calls; an exported global here keeps
+ * the compiler from folding pow(x, 2.0) into x*x, which can differ from
+ * libm's pow in the last bit. */
+double disco_port_phi_order = 2.0;
 static double fgrav(double M, double r, double eps)
 {
-   double n = 2.0;
+   double n = disco_port_phi_order;
    return M*pow(r, n - 1.)/pow(pow(r, n) + pow(eps, n), 1. + 1./n);
 }
 static void planetary_force(const disco_planet *pl, double r, double phi, double z,
@@ -1491,8 +1499,65 @@ static void initial(double *prim, const double *x)
    if(p->RotFrame) prim[UPP] -= p->RotOmega;
 }
 /* Boundary/fixed.c:11-46 (r ghosts) and fixed3d.c via set_cell_init. */
+/* set_cells_copy_distant (boundary_functions.c:90-158): ring c takes the
+ * phi-overlap average of ring c1's primitives. */
+static void copy_distant(pcell *c, int Np, const pcell *c1, int Np1)
+{
+   double Pmax = D->Pmax;
+   int i, q, i1;
+   for(i = 0; i < Np; i++) for(q = 0; q < D->nq; q++) c[i].prim[q] = 0.0;
+   double phi0 = c[0].piph - c[0].dphi;
+   for(i1 = 0; i1 < Np1; i1++) {
+      double dp = get_signed_dp(c1[i1].piph, phi0);
+      if(dp > 0 && dp - c1[i1].dphi <= 0.0) break;
+   }
+   if(i1 >= Np1) i1 = 0;
+   for(i = 0; i < Np; i++) {
+      double hi = c[i].piph, lo = c[i].piph - c[i].dphi, hi1, lo1;
+      do {
+         hi1 = c1[i1].piph; lo1 = c1[i1].piph - c1[i1].dphi;
+         while(hi1 < lo) { hi1 += Pmax; lo1 += Pmax; }
+         while(lo1 > hi) { hi1 -= Pmax; lo1 -= Pmax; }
+         double w = (hi < hi1 ? hi : hi1) - (lo > lo1 ? lo : lo1);
+         for(q = 0; q < D->nq; q++) c[i].prim[q] += c1[i1].prim[q]*w;
+         i1 = i1 < Np1 - 1 ? i1 + 1 : 0;
+      } while(hi1 < hi);
+      i1 = i1 > 0 ? i1 - 1 : Np1 - 1;
+   }
+   for(i = 0; i < Np; i++) for(q = 0; q < D->nq; q++) c[i].prim[q] /= c[i].dphi;
+}
+
+/* boundary_zerograd_{rinn,rout,zbot,ztop} (boundary_functions.c:269-440):
+ * layer by layer outward from the real domain; outflow3d adds a diode on
+ * the normal velocity (Boundary/outflow3d.c). */
+static void zerograd_ring(int j, int k, int j1, int k1, int vq, int sign, int diode)
+{
+   int jk = j + D->Nr*k, jk1 = j1 + D->Nr*k1;
+   copy_distant(D->ring[jk], D->Np[jk], D->ring[jk1], D->Np[jk1]);
+   if(diode)
+      for(int i = 0; i < D->Np[jk]; i++)
+         if(sign*D->ring[jk][i].prim[vq] > 0) D->ring[jk][i].prim[vq] = 0.0;
+}
+
+static void boundary_zerograd(int diode)
+{
+   int j, k;
+   if(D->Nr > 1) {
+      for(k = 0; k < D->Nz; k++) for(j = D->NgRa - 1; j >= 0; j--) zerograd_ring(j, k, j + 1, k, URR, 1, diode);
+      for(k = 0; k < D->Nz; k++) for(j = D->Nr - D->NgRb; j < D->Nr; j++) zerograd_ring(j, k, j - 1, k, URR, -1, diode);
+   }
+   if(D->Nz > 1) {
+      for(j = 0; j < D->Nr; j++) for(k = D->NgZa - 1; k >= 0; k--) zerograd_ring(j, k, j, k + 1, UZZ, 1, diode);
+      for(j = 0; j < D->Nr; j++) for(k = D->Nz - D->NgZb; k < D->Nz; k++) zerograd_ring(j, k, j, k - 1, UZZ, -1, diode);
+   }
+}
+
 static void boundary(void)
 {
+   if(D->mod.boundary == DISCO_BC_OUTFLOW3D || D->mod.boundary == DISCO_BC_ZEROGRAD) {
+      boundary_zerograd(D->mod.boundary == DISCO_BC_OUTFLOW3D);
+      return;
+   }
    for(int k = 0; k < D->Nz; k++) for(int j = 0; j < D->Nr; j++) {
       int rg = j < D->NgRa || j >= D->Nr - D->NgRb;
       int zg = k < D->NgZa || k >= D->Nz - D->NgZb;
@@ -1640,6 +1705,11 @@ port_domain *disco_port_create(const disco_host_domain *h)
    d->ct = d->mhd && h->mod.ct_mode == 2 && h->par.CT;
    if(d->mhd && (!d->ct || h->par.Riemann_Solver != 2 || h->NgRa == 0 || h->NgRb == 0 ||
                  h->NgZa == 0 || h->NgZb == 0)) { free(d); return NULL; }
+   if(h->mod.hydro == DISCO_HYDRO_GRMHD || (d->mhd && h->mod.boundary > DISCO_BC_FIXED3D) ||
+      (h->mod.analysis == DISCO_DIAG_MHDMRI && !d->mhd)) { free(d); return NULL; }
+   static const int ndiag[] = {8, 5, 6, 5, 18};
+   d->nd = h->mod.analysis >= 0 ? ndiag[h->mod.analysis] : 0;
+   d->Qrz = (double *)calloc((size_t)h->Nr*h->Nz*(d->nd ? d->nd : 1), sizeof(double));
    d->N = h->Ncell; d->Pmax = h->phi_max; d->t = h->t; d->Npl = h->Npl;
    d->gam = h->par.Adiabatic_Index;
    memcpy(d->pl, h->planets, sizeof d->pl);
@@ -1696,6 +1766,8 @@ port_domain *disco_port_create(const disco_host_domain *h)
    return d;
 }
 
+static void add_diagnostics(double dt);
+
 /* timestep.c:7-54 (Timestep 0), preceded by getmindt (main.c:70). */
 double disco_port_step(port_domain *d)
 {
@@ -1708,6 +1780,7 @@ double disco_port_step(port_domain *d)
    onestep(0.0, dt, 1);
    d->t += dt;
    onestep(0.5, 0.5*dt, 0);
+   add_diagnostics(dt);
    return dt;
 }
 
@@ -1811,6 +1884,106 @@ void disco_port_report(port_domain *d, double *out)
    for(int n = 0; n < 5; n++) { out[5 + 2*n] = T1c[n]; out[6 + 2*n] = T2c[n]; }
 }
 
+/* get_diagnostics of the ANALYSIS plugins (Diagnostics/diag_euler.c:18-44,
+ * diag_disk2d.c:18-41, diag_cb.c:18-62, diag_bl.c:17-36,
+ * diag_mhdmri.c:17-62) at the cell centroid x. */
+static void get_diagnostics(const double *x, const double *prim, double *Q)
+{
+   double r = x[0], phi = x[1], z = x[2];
+   double rho = prim[RHO], Pp = prim[PPP], vr = prim[URR], om = prim[UPP], vz = prim[UZZ];
+   double Fr, Fp = 0.0, Fz;
+   switch(D->mod.analysis) {
+   case DISCO_DIAG_EULER:
+      if(D->Npl > 1) planetary_force(&D->pl[1], r, phi, z, &Fr, &Fp, &Fz);
+      Q[0] = rho;
+      Q[1] = 2.*M_PI*r*rho*vr;
+      Q[2] = 2.*M_PI*r*rho*vz;
+      Q[3] = 2.*M_PI*r*rho*(r*Fp);
+      Q[4] = 2.*M_PI*r*rho*(r*r*om*vr);
+      Q[5] = om;
+      Q[6] = 2.*M_PI*r*rho*r*r*om;
+      Q[7] = Pp;
+      break;
+   case DISCO_DIAG_DISK2D:
+      if(D->Npl > 1) planetary_force(&D->pl[1], r, phi, 0.0, &Fr, &Fp, &Fz);
+      Q[0] = rho;
+      Q[1] = 2.*M_PI*r*rho*vr;
+      Q[2] = 2.*M_PI*r*rho*(r*Fp);
+      Q[3] = 2.*M_PI*r*rho*(r*r*om*vr);
+      Q[4] = om;
+      break;
+   case DISCO_DIAG_CB: {
+      double vp = r*om;
+      double gx = r*cos(phi), gy = r*sin(phi);
+      double vx = vr*cos(phi) - vp*sin(phi), vy = vr*sin(phi) + vp*cos(phi);
+      double vm2 = vx*vx + vy*vy, rdv = vx*gx + vy*gy;
+      Q[0] = rho;
+      Q[1] = 2.*M_PI*r*rho*vr;
+      Q[2] = ((vm2 - 1./r)*gx - rdv*vx)*rho;
+      Q[3] = ((vm2 - 1./r)*gy - rdv*vy)*rho;
+      Q[4] = 0.0;
+      Q[5] = rho*vp;
+      for(int p = 0; p < 2 && p < D->Npl; p++) {
+         planetary_force_m1(&D->pl[p], r, phi, z, &Fr, &Fp, &Fz);
+         Q[4] += rho*D->pl[p].r*Fp;
+      }
+      break;
+   }
+   case DISCO_DIAG_BL: {
+      double vp = r*om;
+      Q[0] = rho; Q[1] = rho*om; Q[2] = rho*vp; Q[3] = rho*vr; Q[4] = rho*vp*vr;
+      break;
+   }
+   case DISCO_DIAG_MHDMRI: {
+      double g = D->par.Adiabatic_Index;
+      double Br = prim[BRR], Bp = prim[BPP], Bz = prim[BZZ];
+      double cs2 = g*Pp/rho, B2 = Br*Br + Bp*Bp + Bz*Bz;
+      Q[0] = rho; Q[1] = Pp; Q[2] = vr; Q[3] = om; Q[4] = vz;
+      Q[5] = Br; Q[6] = Bp; Q[7] = Bz; Q[8] = rho;
+      Q[9] = 0.5*rho*(vr*vr + r*r*om*om + vz*vz) + Pp/(g - 1.0) + 0.5*B2;
+      Q[10] = rho*vr; Q[11] = r*r*rho*om; Q[12] = rho*vz;
+      Q[13] = rho*vr*om; Q[14] = Br*Bp; Q[15] = B2;
+      Q[16] = sqrt(cs2); Q[17] = sqrt(B2/rho);
+      break;
+   }
+   default: break;
+   }
+}
+
+/* add_diagnostics (analysis.c:52-108): per ring, every ghost ring included,
+ * Qrz += (sum of Q dV) * dt / (sum of dV); t_avg += dt. */
+static void add_diagnostics(double dt)
+{
+   int nd = D->nd;
+   if(!nd) return;
+   double Q[18];
+   for(int k = 0; k < D->Nz; k++) for(int j = 0; j < D->Nr; j++) {
+      int jk = k*D->Nr + j;
+      double sum[18] = {0}, vol = 0.0;
+      for(int i = 0; i < D->Np[jk]; i++) {
+         pcell *c = &D->ring[jk][i];
+         double xp[3] = {D->rj[j], c->piph, D->zk[k]};
+         double xm[3] = {D->rj[j - 1], c->piph - c->dphi, D->zk[k - 1]};
+         double xc[3];
+         centroid_arr(xp, xm, xc);
+         double dV = get_dV(xp, xm);
+         get_diagnostics(xc, c->prim, Q);
+         for(int q = 0; q < nd; q++) sum[q] += Q[q]*dV;
+         vol += dV;
+      }
+      for(int q = 0; q < nd; q++) D->Qrz[(size_t)jk*nd + q] += sum[q]*dt/vol;
+   }
+   D->t_avg += dt;
+}
+
+/* Qrz [Nr*Nz*nd] (may be NULL) and t_avg; returns nd. */
+int disco_port_diag(const port_domain *d, double *Qrz, double *t_avg)
+{
+   if(Qrz && d->nd) memcpy(Qrz, d->Qrz, sizeof(double)*(size_t)d->Nr*d->Nz*d->nd);
+   if(t_avg) *t_avg = d->t_avg;
+   return d->nd;
+}
+
 long disco_port_num_real(const port_domain *d)
 {
    long n = 0;
@@ -1825,6 +1998,7 @@ void disco_port_free(port_domain *d)
    free(d->Np); free(d->off); free(d->rj - 1); free(d->zk - 1);
    free(d->cells); free(d->ring);
    free(d->faces[0]); free(d->faces[1]); free(d->fI[0]); free(d->fI[1]);
+   free(d->Qrz);
    free(d);
 }
 

@@ -191,6 +191,15 @@ int main(int argc, char **argv)
          /* the reference's own diagnostics of the final state: one line
           * appended to report.dat in the working directory */
          report(d);
+         /* the ring diagnostics timestep() accumulated (analysis.c):
+          * int32 num_tools, int32 Nr*Nz, double t_avg, double Qrz[] */
+         FILE *g = fopen("diag.bin", "wb");
+         int nq = d->num_tools, nring = d->Nr * d->Nz;
+         fwrite(&nq, sizeof nq, 1, g);
+         fwrite(&nring, sizeof nring, 1, g);
+         fwrite(&d->theTools.t_avg, sizeof(double), 1, g);
+         fwrite(d->theTools.Qrz, sizeof(double), (size_t)nq * nring, g);
+         fclose(g);
       }
    } else {
       fprintf(stderr, "unknown mode %s\n", mode);

@@ -90,7 +90,13 @@ def run_case(name: str, ref: str) -> None:
         line = open(os.path.join(td, "report.dat")).read().strip().splitlines()[-1]
         rep = np.array([float(v) for v in
                         re.findall(r"[-+]?\d\.\d+e[-+]\d{2}(?:\d(?!\.))?", line)])
+        # analysis.c's ring diagnostics accumulated over the run
+        raw = open(os.path.join(td, "diag.bin"), "rb").read()
+        nq, nring = np.frombuffer(raw[:8], dtype="<i4")
+        dg = np.frombuffer(raw[8:], dtype="<f8")
+        diag_tavg, diag_Qrz = dg[0], dg[1:1 + nq * nring].reshape(nring, nq)
     out = {"par_text": np.array(par), "nsteps": nsteps, "cfg": np.array(cfg), "report": rep,
+           "diag_tavg": diag_tavg, "diag_Qrz": diag_Qrz,
            "Np": ini["Np"], "r_jph": ini["r_jph"], "z_kph": ini["z_kph"], "real": ini["real"],
            "init_piph": ini["piph"], "init_dphi": ini["dphi"], "init_prim": ini["prim"],
            "init_cons": ini["cons"], "init_wiph": ini["wiph"],

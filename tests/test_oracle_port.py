@@ -22,12 +22,26 @@ def _port_run(par_path, mk, nsteps):
     return h, d.state()
 
 
-@pytest.mark.parametrize("name", ["cfg1_n24", "cfg1_hll_static", "cfg1_exact_mesh", "cfg1_rotframe",
-                                  "cfg3_n24"])
+def _port_domain(g):
+    import disco_gb300 as dg
+    from oracle.port import PortDomain
+    mk = os.path.join(ROOT, str(g["cfg"]), "Makefile_opt.in")
+    h = dg.HostDomain(dg.read_params(write_par(g["par_text"])), dg.read_modules(mk))
+    d = PortDomain(h)
+    d.run(int(g["nsteps"]))
+    return d
+
+
+HYDRO_CASES = ["cfg1_n24", "cfg1_hll_static", "cfg1_exact_mesh", "cfg1_rotframe", "cfg3_n24",
+               "cfg1_zerograd", "cfg3_outflow"]
+
+
+@pytest.mark.parametrize("name", HYDRO_CASES)
 def test_port_bit_exact_vs_golden(name):
     """Hydro cases: HLLC vortex, HLL on a static mesh, exact Keplerian mesh
     rotation, rotating frame with a Keplerian energy frame (HLLC with the
-    centre switch), and the planet disk with alpha viscosity."""
+    centre switch), the planet disk with alpha viscosity, and the
+    zero-gradient / outflow ghost variants."""
     g = load_golden(name)
     h, s = _port_run(write_par(g["par_text"]), os.path.join(ROOT, str(g["cfg"]), "Makefile_opt.in"),
                      int(g["nsteps"]))
@@ -121,3 +135,19 @@ def test_port_report_vs_reference(name, npl):
     ref = _ref_report(g, npl)
     for k, v in ref.items():
         assert abs(mine[k] - v) <= 6e-7 * abs(v) + 1e-300, (k, mine[k], v)
+
+
+@pytest.mark.parametrize("name", HYDRO_CASES + ["cfg2_n12", "cfg5_n16"])
+def test_port_diagnostics_vs_reference(name):
+    """analysis.c's ring accumulators after the fixture's steps: bit for bit
+    where the state is (every case but the circumbinary disk, whose state
+    carries a few ulps)."""
+    from helpers import rel_l1
+    g = load_golden(name)
+    dg = _port_domain(g).diagnostics()
+    assert dg["t_avg"] == float(g["diag_tavg"])
+    if name == "cfg5_n16":
+        for q in range(g["diag_Qrz"].shape[1]):
+            assert rel_l1(dg["Qrz"][:, q], g["diag_Qrz"][:, q]) < 1e-14, q
+    else:
+        assert np.array_equal(dg["Qrz"], g["diag_Qrz"])
