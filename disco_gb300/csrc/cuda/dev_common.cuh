@@ -47,6 +47,9 @@ struct DevParams {
   double rot_omega, rot_d;
   // planet.c:4-35
   int grav2D, polar_r, polar_p;
+  // plm_geom_boundary (plm.c:184-186) acts on the inner ring when it has no
+  // ghosts and geom_grad (cylindrical.c:150-155) finds its edge at r = 0
+  int geom_bd_r;
   int Npl;
   // GRMHD: the black-hole mass of the Kerr-Schild metric (Metric_Par2)
   double gr_M;

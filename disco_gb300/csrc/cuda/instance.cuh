@@ -18,6 +18,7 @@
 #include "noalloc.cuh"
 #include "report.cuh"
 #include "diag.cuh"
+#include "../plugins/bc_plugins.h"
 
 using namespace disco;
 
@@ -181,6 +182,10 @@ struct Instance : InstanceBase {
     P.rot_flag = p.RotFrame; P.rot_omega = p.RotOmega; P.rot_d = p.RotD;
     P.grav2D = p.grav2D;
     P.polar_r = P.polar_p = (p.NoBC_Rmin == 1);    // planet.c:13-18 (cylindrical)
+    {
+      const double rp0 = dom->r_jph[1], rm0 = dom->r_jph[0];   // r_jph[0], r_jph[-1]
+      P.geom_bd_r = dom->NgRa == 0 && !(rp0 < 0.0 || fabs(rm0) > 1.0e-10 * rp0);
+    }
     P.Npl = dom->Npl;
     P.initial_id = dom->mod.initial; P.boundary_id = dom->mod.boundary;
     double icp[8] = {p.initPar1, p.initPar2, p.initPar3, p.initPar4, p.initPar5, p.initPar6, p.initPar7, p.initPar8};
@@ -247,9 +252,24 @@ struct Instance : InstanceBase {
         return DISCO_E_MODULE;
       }
     }
-    if (dom->mod.boundary > 1 && (Phys::MHD || Phys::GR)) {
-      disco_set_error("zero-gradient / outflow boundaries are built for the hydro module only");
+    n_bc_ops = disco_bc_plugin_ops(dom->mod.boundary, bc_ops);
+    if (n_bc_ops < 0) {
+      disco_set_error("BOUNDARY plugin not built");
       return DISCO_E_MODULE;
+    }
+    if (n_bc_ops > 0 && (Phys::MHD || Phys::GR)) {
+      disco_set_error("boundary plugins other than fixed / fixed3d are built for the hydro module only");
+      return DISCO_E_MODULE;
+    }
+    for (int o = 0; o < n_bc_ops; ++o) {   // the source rings of the copies must be real rings
+      const int dim = bc_ops[o].side < 2 ? 1 : 2, side = bc_ops[o].side & 1;
+      const int ng = dim == 1 ? (side ? dom->NgRb : dom->NgRa) : (side ? dom->NgZb : dom->NgZa);
+      const int nreal = dim == 1 ? dom->Nr - dom->NgRa - dom->NgRb : dom->Nz - dom->NgZa - dom->NgZb;
+      const int need = bc_ops[o].op == DISCO_BCOP_ZEROGRAD ? 1 : ng;
+      if (bc_ops[o].op >= DISCO_BCOP_ZEROGRAD && ng > 0 && nreal < need) {
+        disco_set_error("boundary copy needs more real rings than the domain has");
+        return DISCO_E_ARG;
+      }
     }
 
     for (int jk = 0; jk < nring; ++jk) maxring = std::max(maxring, dom->Np[jk]);
@@ -505,20 +525,28 @@ struct Instance : InstanceBase {
     if (P.mesh_motion == 3)
       LAUNCH("wcell_avg", (k_wcell_avg<R><<<nring, 64, (maxring + 1) * sizeof(double), st>>>(P, S)));
   }
+  disco_bc_op bc_ops[DISCO_BC_MAX_OPS];
+  int n_bc_ops = 0;
   void launch_boundary() {
-    if (P.boundary_id >= 2) {   // zerograd (3) / outflow3d (2): layer by layer
-      const int diode = P.boundary_id == 2;
-      if (Nr > 1) {   // boundary_trans(dim 1): inner layers inward, then outer outward
-        for (int j = P.NgRa - 1; j >= 0; --j)
-          LAUNCH("boundary", (k_bc_zerograd<R, NQ><<<blocks(Nz, 64), 64, 0, st>>>(P, S, 1, 0, j, diode)));
-        for (int j = Nr - P.NgRb; j < Nr; ++j)
-          LAUNCH("boundary", (k_bc_zerograd<R, NQ><<<blocks(Nz, 64), 64, 0, st>>>(P, S, 1, 1, j, diode)));
-      }
-      if (Nz > 1) {   // boundary_trans(dim 2)
-        for (int k = P.NgZa - 1; k >= 0; --k)
-          LAUNCH("boundary", (k_bc_zerograd<R, NQ><<<blocks(Nr, 64), 64, 0, st>>>(P, S, 2, 0, k, diode)));
-        for (int k = Nz - P.NgZb; k < Nz; ++k)
-          LAUNCH("boundary", (k_bc_zerograd<R, NQ><<<blocks(Nr, 64), 64, 0, st>>>(P, S, 2, 1, k, diode)));
+    if (n_bc_ops > 0) {   // plugins written as boundary_functions.c primitives
+      for (int o = 0; o < n_bc_ops; ++o) {
+        const disco_bc_op& b = bc_ops[o];
+        const int dim = b.side < 2 ? 1 : 2, side = b.side & 1;
+        if ((dim == 1 && Nr <= 1) || (dim == 2 && Nz <= 1)) continue;
+        const int ng = dim == 1 ? (side ? P.NgRb : P.NgRa) : (side ? P.NgZb : P.NgZa);
+        if (ng == 0) continue;
+        const int per_layer = dim == 1 ? Nz : Nr, n = dim == 1 ? Nr : Nz;
+        if (b.op <= DISCO_BCOP_FIXED_PHI) {
+          LAUNCH("boundary", (k_bc_init<R, NQ><<<ng * per_layer, 128, 0, st>>>(P, S, dim, side, b.op, b.arg,
+                                                                               b.pa, b.pb)));
+        } else {
+          const int mode = b.op - DISCO_BCOP_ZEROGRAD;   // 0 zerograd, 1 reflect, 2 noslip
+          for (int l = 0; l < ng; ++l) {   // from the real domain outward
+            const int layer = side ? n - ng + l : ng - 1 - l;
+            LAUNCH("boundary", (k_bc_copy<R, NQ><<<blocks(per_layer, 64), 64, 0, st>>>(P, S, dim, side, layer,
+                                                                                       mode, b.arg)));
+          }
+        }
       }
       return;
     }

@@ -897,7 +897,7 @@ __global__ void __launch_bounds__(kTileCells) k_plm_trans(DevParams P, DevState<
     dAt = (R)dAtot;
   }
 
-  bool geom_bd = (dim == 1 && j == 0 && P.NgRa == 0);
+  bool geom_bd = (dim == 1 && j == 0 && P.geom_bd_r);
   R rcen = kMix<R> ? S.ring_rc_r[jk] : (R)S.ring_rc[jk];
 #pragma unroll
   for (int t = 0; t < QB; ++t) {
@@ -1443,31 +1443,36 @@ __global__ void __launch_bounds__(kTileCells) k_boundary(DevParams P, DevState<R
   for (int q = 0; q < NQ; ++q) S.prim[q * S.N + c] = (R)prim[q];
 }
 
-// ---- zero-gradient / outflow ghosts: Boundary/zerograd.c, Boundary/outflow3d.c ----
-// boundary_zerograd_{rinn,rout,zbot,ztop} (boundary_functions.c:269-440) copy
-// the neighbouring ring inward of each ghost ring onto it by phi overlap
-// (set_cells_copy_distant, :90-158), layer by layer from the real domain
-// outward; outflow3d is the same with a diode on the normal velocity.  One
-// thread per ghost ring of a layer walks both rings in the reference's order
-// (the same overlaps summed in the same order); the layers are separate
-// launches.  On the mixed path the copy is made in the lab frame (ring
+// ---- ghost rings copied from other rings: boundary_functions.c:90-158 ----
+// boundary_zerograd_* (:269-441) copy the next ring inward onto each ghost
+// ring, layer by layer from the real domain outward (with an optional
+// diode on the normal velocity, as outflow3d.c asks); boundary_reflect_*
+// (:442-621) and boundary_noslip_* (:914-1101) copy the mirror ring and
+// negate the normal velocity (reflect) or every velocity (noslip,
+// reflect_prims in all three directions).  The copy is the phi-overlap
+// average of set_cells_copy_distant.  One thread per ghost ring of a layer
+// walks both rings in the reference's order (the same overlaps summed in
+// the same order); the layers are separate launches.  On the mixed path
+// the copy is made in the frame of the reference's primitives (ring
 // frames added and removed in FP64).
-// dim 1: rings (j, k) for all k, source j + 1 (side 0, inner) or j - 1
-// (side 1, outer); dim 2: rings (j, k) for all j, source k + 1 or k - 1.
+// dim 1: rings (layer, k) for all k; dim 2: rings (j, layer) for all j.
+// mode 0 zerograd (source layer +- 1), 1 reflect, 2 noslip (mirror source).
 template <typename R, int NQ>
-__global__ void k_bc_zerograd(DevParams P, DevState<R> S, int dim, int side, int layer, int diode) {
+__global__ void k_bc_copy(DevParams P, DevState<R> S, int dim, int side, int layer, int mode, int diode) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   int j, k, j1, k1;
   if (dim == 1) {
     if (t >= P.Nz) return;
     k = k1 = t;
     j = layer;
-    j1 = side == 0 ? j + 1 : j - 1;
+    if (mode == 0) j1 = side == 0 ? j + 1 : j - 1;
+    else j1 = side == 0 ? 2 * P.NgRa - j - 1 : 2 * (P.Nr - P.NgRb) - j - 1;
   } else {
     if (t >= P.Nr) return;
     j = j1 = t;
     k = layer;
-    k1 = side == 0 ? k + 1 : k - 1;
+    if (mode == 0) k1 = side == 0 ? k + 1 : k - 1;
+    else k1 = side == 0 ? 2 * P.NgZa - k - 1 : 2 * (P.Nz - P.NgZb) - k - 1;
   }
   const int jk = j + P.Nr * k, jk1 = j1 + P.Nr * k1;
   const int off = S.ring_off[jk], Np = S.ring_off[jk + 1] - off;
@@ -1486,6 +1491,7 @@ __global__ void k_bc_zerograd(DevParams P, DevState<R> S, int dim, int side, int
     }
     if (i1 >= Np1) i1 = 0;
   }
+  const int qn = dim == 1 ? URR : UZZ;
   for (int i = 0; i < Np; ++i) {
     const int c = off + i;
     const double phip = S.piph[c], phim = S.piph[c] - S.dphi[c];
@@ -1515,13 +1521,64 @@ __global__ void k_bc_zerograd(DevParams P, DevState<R> S, int dim, int side, int
 #pragma unroll
     for (int q = 0; q < NQ; ++q) {
       double v = acc[q] / S.dphi[c];
-      if (diode) {   // outflow3d: no inflow through the boundary
-        const int qn = dim == 1 ? URR : UZZ;
-        if (q == qn && (side == 0 ? v > 0 : v < 0)) v = 0.0;
-      }
+      if (mode == 0 && diode && q == qn && (side == 0 ? v > 0 : v < 0)) v = 0.0;
+      if ((mode == 1 && q == qn) || (mode == 2 && (q == URR || q == UPP || q == UZZ))) v = -v;
       if (kMix<R> && q == UPP) v -= Om;
       S.prim[q * N + c] = (R)v;
     }
+  }
+}
+
+// ---- ghost rings from the initial condition, one side at a time ----------
+// boundary_fixed_* (boundary_functions.c:161-268: set_cell_init at the
+// cell centroid), boundary_fixed_q_* (:662-773: set_cell_init_q, at
+// phi = piph - dphi/2, only the primitives in qmask) and
+// boundary_fixed_phi_* (:774-913: set_cell_init where the cell's phi,
+// raised past pa by whole turns, is below pb).  One block per ghost ring:
+// dim 1 rings (j, k) of the side's ng layers for all k, dim 2 (j, k) for
+// all j.  mode 0 fixed, 1 fixed_q, 2 fixed_phi.
+template <typename R, int NQ>
+__global__ void __launch_bounds__(128) k_bc_init(DevParams P, DevState<R> S, int dim, int side, int mode,
+                                                 int qmask, double pa, double pb) {
+  int j, k;
+  if (dim == 1) {
+    const int ng = side ? P.NgRb : P.NgRa;
+    const int l = blockIdx.x % ng;
+    k = blockIdx.x / ng;
+    j = side ? P.Nr - P.NgRb + l : l;
+  } else {
+    const int ng = side ? P.NgZb : P.NgZa;
+    const int l = blockIdx.x % ng;
+    j = blockIdx.x / ng;
+    k = side ? P.Nz - P.NgZb + l : l;
+  }
+  const int jk = j + P.Nr * k;
+  const int off = S.ring_off[jk], Np = S.ring_off[jk + 1] - off;
+  const double* rj = S.r_jph + 1;
+  const double* zk = S.z_kph + 1;
+  const double xr = centroid_r(rj[j], rj[j - 1]);
+  const double xz = centroid_z(zk[k], zk[k - 1]);
+  const int N = S.N;
+  for (int i = threadIdx.x; i < Np; i += blockDim.x) {
+    const int c = off + i;
+    const double phip = S.piph[c], dph = S.dphi[c];
+    double x[3] = {xr, 0.0, xz};
+    if (mode == 1) {
+      x[1] = phip - .5 * dph;
+    } else {
+      if (mode == 2) {
+        double phi = phip - .5 * dph;
+        for (int w = 0; w < 4 && phi < pa; ++w) phi += P.phi_max;
+        if (!(phi < pb)) continue;
+      }
+      x[1] = .5 * (phip + (phip - dph));   // get_centroid(dim 0)
+    }
+    double prim[MAX_Q];
+    initial_eval(P, prim, x);
+    if constexpr (kMix<R>) prim[UPP] -= S.ring_Om[jk];   // ring frame
+#pragma unroll
+    for (int q = 0; q < NQ; ++q)
+      if (mode != 1 || ((qmask >> q) & 1)) S.prim[q * N + c] = (R)prim[q];
   }
 }
 

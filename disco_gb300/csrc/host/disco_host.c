@@ -234,7 +234,9 @@ int disco_modules_read(const char *path, disco_modules *m)
 
    static const char *hyd[] = {"euler", "mhd", "grmhd"};
    static const char *ini[] = {"vortex_gauss", "disk_mhd", "disk_planet", "disk_cbd", "gr_disk"};
-   static const char *bnd[] = {"fixed", "fixed3d", "outflow3d", "zerograd"};
+   static const char *bnd[] = {"fixed", "fixed3d", "outflow3d", "zerograd", "zerograd_omk",
+                               "zerograd_omIN", "accrete3d", "fixRrefZ", "polar3d", "fixed_gap",
+                               "tube", "surfaceGravBox", "flowthrough"};
    static const char *pla[] = {"none", "sun", "circular", "cm"};
    static const char *ana[] = {"diag_euler", "diag_disk2d", "diag_cb", "diag_bl", "diag_mhdmri"};
    int i;
@@ -243,7 +245,7 @@ int disco_modules_read(const char *path, disco_modules *m)
    for(i = 0; i < 5; i++) if(!strcmp(m->initial_name, ini[i])) m->initial = i;
    m->metric = !strcmp(m->metric_name, "schw_ks_rpz") ? DISCO_METRIC_SCHW_KS_RPZ : DISCO_METRIC_NONE;
    m->frame = !strcmp(m->frame_name, "normal") ? DISCO_FRAME_NORMAL : DISCO_FRAME_NONE;
-   for(i = 0; i < 4; i++) if(!strcmp(m->boundary_name, bnd[i])) m->boundary = i;
+   for(i = 0; i < DISCO_BC_COUNT; i++) if(!strcmp(m->boundary_name, bnd[i])) m->boundary = i;
    for(i = 0; i < 4; i++) if(!strcmp(m->planets_name, pla[i])) m->planets = i;
    m->analysis = DISCO_DIAG_NONE;
    for(i = 0; i < 5; i++) if(!strcmp(m->analysis_name, ana[i])) m->analysis = i;

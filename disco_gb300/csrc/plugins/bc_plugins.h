@@ -1,0 +1,123 @@
+/* Ghost-ring boundary plugins (Boundary/*.c) written as the per-side
+ * primitives of boundary_functions.c that each plugin's boundary_trans
+ * calls, in call order: the dim 1 (r) list, run when Nr > 1, then the
+ * dim 2 (z) list, run when Nz > 1.
+ *
+ * Primitives (boundary_functions.c):
+ *   FIXED      boundary_fixed_{rinn,rout,zbot,ztop}     :161-268  set_cell_init (:21)
+ *   FIXED_Q    boundary_fixed_q_*                       :662-773  set_cell_init_q (:33) on the q mask
+ *   FIXED_PHI  boundary_fixed_phi_*                     :774-913  set_cell_init where phi in [pa, pb)
+ *   ZEROGRAD   boundary_zerograd_* (arg: diode)         :269-441  copy of the next ring inward
+ *   REFLECT    boundary_reflect_*                       :442-621  copy of the mirror ring, normal velocity negated
+ *   NOSLIP     boundary_noslip_*                        :914-1101 copy of the mirror ring, all velocities negated
+ * fixed.c and fixed3d.c keep their own kernel (they fill every ghost ring
+ * of their dimensions from initial()).
+ */
+#ifndef DISCO_BC_PLUGINS_H
+#define DISCO_BC_PLUGINS_H
+
+#include <math.h>
+
+#include "disco_gpu.h"
+
+enum { DISCO_BCOP_FIXED = 0, DISCO_BCOP_FIXED_Q = 1, DISCO_BCOP_FIXED_PHI = 2,
+       DISCO_BCOP_ZEROGRAD = 3, DISCO_BCOP_REFLECT = 4, DISCO_BCOP_NOSLIP = 5 };
+enum { DISCO_SIDE_RINN = 0, DISCO_SIDE_ROUT = 1, DISCO_SIDE_ZBOT = 2, DISCO_SIDE_ZTOP = 3 };
+
+typedef struct disco_bc_op {
+   int op, side;
+   int arg;          /* ZEROGRAD: diode; FIXED_Q: bit mask of the primitives set */
+   double pa, pb;    /* FIXED_PHI: the phi range */
+} disco_bc_op;
+
+#define DISCO_BC_MAX_OPS 8
+
+static inline disco_bc_op disco_bc_mk(int op, int side, int arg)
+{
+   disco_bc_op o;
+   o.op = op; o.side = side; o.arg = arg; o.pa = 0.0; o.pb = 0.0;
+   return o;
+}
+
+/* Fills ops (DISCO_BC_MAX_OPS entries) for a plugin that is written as
+ * primitives; returns the count, 0 for fixed / fixed3d (own kernel) and -1
+ * for an unknown id.  UPP = 3 in the primitive order. */
+static inline int disco_bc_plugin_ops(int boundary_id, disco_bc_op *o)
+{
+   const int upp = 1 << 3;
+   int n = 0;
+   switch(boundary_id) {
+   case DISCO_BC_FIXED: case DISCO_BC_FIXED3D:
+      return 0;
+   case DISCO_BC_ZEROGRAD:        /* Boundary/zerograd.c */
+   case DISCO_BC_OUTFLOW3D: {     /* Boundary/outflow3d.c: with the diode */
+      int d = boundary_id == DISCO_BC_OUTFLOW3D;
+      o[n++] = disco_bc_mk(DISCO_BCOP_ZEROGRAD, DISCO_SIDE_RINN, d);
+      o[n++] = disco_bc_mk(DISCO_BCOP_ZEROGRAD, DISCO_SIDE_ROUT, d);
+      o[n++] = disco_bc_mk(DISCO_BCOP_ZEROGRAD, DISCO_SIDE_ZBOT, d);
+      o[n++] = disco_bc_mk(DISCO_BCOP_ZEROGRAD, DISCO_SIDE_ZTOP, d);
+      return n;
+   }
+   case DISCO_BC_ZEROGRAD_OMK:    /* Boundary/zerograd_omk.c */
+      o[n++] = disco_bc_mk(DISCO_BCOP_ZEROGRAD, DISCO_SIDE_RINN, 1);
+      o[n++] = disco_bc_mk(DISCO_BCOP_ZEROGRAD, DISCO_SIDE_ROUT, 1);
+      o[n++] = disco_bc_mk(DISCO_BCOP_FIXED_Q, DISCO_SIDE_RINN, upp);
+      o[n++] = disco_bc_mk(DISCO_BCOP_FIXED_Q, DISCO_SIDE_ROUT, upp);
+      o[n++] = disco_bc_mk(DISCO_BCOP_ZEROGRAD, DISCO_SIDE_ZBOT, 1);
+      o[n++] = disco_bc_mk(DISCO_BCOP_ZEROGRAD, DISCO_SIDE_ZTOP, 1);
+      return n;
+   case DISCO_BC_ZEROGRAD_OMIN:   /* Boundary/zerograd_omIN.c */
+      o[n++] = disco_bc_mk(DISCO_BCOP_ZEROGRAD, DISCO_SIDE_RINN, 1);
+      o[n++] = disco_bc_mk(DISCO_BCOP_FIXED, DISCO_SIDE_ROUT, 0);
+      o[n++] = disco_bc_mk(DISCO_BCOP_FIXED_Q, DISCO_SIDE_RINN, upp);
+      o[n++] = disco_bc_mk(DISCO_BCOP_ZEROGRAD, DISCO_SIDE_ZBOT, 1);
+      o[n++] = disco_bc_mk(DISCO_BCOP_ZEROGRAD, DISCO_SIDE_ZTOP, 1);
+      return n;
+   case DISCO_BC_ACCRETE3D:       /* Boundary/accrete3d.c */
+      o[n++] = disco_bc_mk(DISCO_BCOP_ZEROGRAD, DISCO_SIDE_RINN, 1);
+      o[n++] = disco_bc_mk(DISCO_BCOP_FIXED, DISCO_SIDE_ROUT, 0);
+      o[n++] = disco_bc_mk(DISCO_BCOP_FIXED, DISCO_SIDE_ZBOT, 0);
+      o[n++] = disco_bc_mk(DISCO_BCOP_FIXED, DISCO_SIDE_ZTOP, 0);
+      return n;
+   case DISCO_BC_FIXRREFZ:        /* Boundary/fixRrefZ.c */
+      o[n++] = disco_bc_mk(DISCO_BCOP_FIXED, DISCO_SIDE_RINN, 0);
+      o[n++] = disco_bc_mk(DISCO_BCOP_FIXED, DISCO_SIDE_ROUT, 0);
+      o[n++] = disco_bc_mk(DISCO_BCOP_REFLECT, DISCO_SIDE_ZBOT, 0);
+      o[n++] = disco_bc_mk(DISCO_BCOP_REFLECT, DISCO_SIDE_ZTOP, 0);
+      return n;
+   case DISCO_BC_POLAR3D:         /* Boundary/polar3d.c */
+      o[n++] = disco_bc_mk(DISCO_BCOP_FIXED, DISCO_SIDE_ROUT, 0);
+      o[n++] = disco_bc_mk(DISCO_BCOP_FIXED, DISCO_SIDE_ZBOT, 0);
+      o[n++] = disco_bc_mk(DISCO_BCOP_FIXED, DISCO_SIDE_ZTOP, 0);
+      return n;
+   case DISCO_BC_FIXED_GAP:       /* Boundary/fixed_gap.c */
+      o[n++] = disco_bc_mk(DISCO_BCOP_ZEROGRAD, DISCO_SIDE_RINN, 1);
+      o[n++] = disco_bc_mk(DISCO_BCOP_FIXED, DISCO_SIDE_ROUT, 0);
+      o[n++] = disco_bc_mk(DISCO_BCOP_ZEROGRAD, DISCO_SIDE_ZBOT, 1);
+      o[n++] = disco_bc_mk(DISCO_BCOP_ZEROGRAD, DISCO_SIDE_ZTOP, 1);
+      return n;
+   case DISCO_BC_TUBE:            /* Boundary/tube.c */
+      o[n++] = disco_bc_mk(DISCO_BCOP_REFLECT, DISCO_SIDE_ROUT, 0);
+      o[n++] = disco_bc_mk(DISCO_BCOP_ZEROGRAD, DISCO_SIDE_ZBOT, 0);
+      o[n++] = disco_bc_mk(DISCO_BCOP_ZEROGRAD, DISCO_SIDE_ZTOP, 0);
+      return n;
+   case DISCO_BC_SURFACEGRAVBOX:  /* Boundary/surfaceGravBox.c */
+      o[n++] = disco_bc_mk(DISCO_BCOP_REFLECT, DISCO_SIDE_RINN, 0);
+      o[n++] = disco_bc_mk(DISCO_BCOP_REFLECT, DISCO_SIDE_ROUT, 0);
+      o[n++] = disco_bc_mk(DISCO_BCOP_REFLECT, DISCO_SIDE_ZBOT, 0);
+      o[n++] = disco_bc_mk(DISCO_BCOP_ZEROGRAD, DISCO_SIDE_ZTOP, 1);
+      return n;
+   case DISCO_BC_FLOWTHROUGH:     /* Boundary/flowthrough.c */
+      o[n++] = disco_bc_mk(DISCO_BCOP_NOSLIP, DISCO_SIDE_RINN, 0);
+      o[n++] = disco_bc_mk(DISCO_BCOP_ZEROGRAD, DISCO_SIDE_ROUT, 1);
+      o[n] = disco_bc_mk(DISCO_BCOP_FIXED_PHI, DISCO_SIDE_ROUT, 0);
+      o[n].pa = 0.3*M_PI; o[n].pb = 1.7*M_PI; n++;
+      o[n++] = disco_bc_mk(DISCO_BCOP_FIXED, DISCO_SIDE_ZBOT, 0);
+      o[n++] = disco_bc_mk(DISCO_BCOP_FIXED, DISCO_SIDE_ZTOP, 0);
+      return n;
+   default:
+      return -1;
+   }
+}
+
+#endif

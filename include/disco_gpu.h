@@ -55,7 +55,12 @@ enum disco_initial_id { DISCO_IC_VORTEX_GAUSS = 0, DISCO_IC_DISK_MHD = 1,
 enum disco_metric_id  { DISCO_METRIC_NONE = -1, DISCO_METRIC_SCHW_KS_RPZ = 0 };
 enum disco_frame_id   { DISCO_FRAME_NONE = -1, DISCO_FRAME_NORMAL = 0 };
 enum disco_boundary_id{ DISCO_BC_FIXED = 0, DISCO_BC_FIXED3D = 1,
-                        DISCO_BC_OUTFLOW3D = 2, DISCO_BC_ZEROGRAD = 3 };
+                        DISCO_BC_OUTFLOW3D = 2, DISCO_BC_ZEROGRAD = 3,
+                        DISCO_BC_ZEROGRAD_OMK = 4, DISCO_BC_ZEROGRAD_OMIN = 5,
+                        DISCO_BC_ACCRETE3D = 6, DISCO_BC_FIXRREFZ = 7,
+                        DISCO_BC_POLAR3D = 8, DISCO_BC_FIXED_GAP = 9,
+                        DISCO_BC_TUBE = 10, DISCO_BC_SURFACEGRAVBOX = 11,
+                        DISCO_BC_FLOWTHROUGH = 12, DISCO_BC_COUNT = 13 };
 enum disco_planets_id { DISCO_PL_NONE = 0, DISCO_PL_SUN = 1,
                         DISCO_PL_CIRCULAR = 2, DISCO_PL_CM = 3 };
 /* ANALYSIS of Makefile_opt.in: the Diagnostics/ plugin whose ring averages

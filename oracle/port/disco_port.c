@@ -23,6 +23,7 @@
 #include "disco_gpu.h"
 #include "../../disco_gb300/csrc/plugins/ic_vortex_gauss.h"
 #include "../../disco_gb300/csrc/plugins/ic_disks.h"
+#include "../../disco_gb300/csrc/plugins/bc_plugins.h"
 
 enum { RHO, PPP, URR, UPP, UZZ, BRR, BPP, BZZ };
 enum { DDD, TAU, SRR, LLL, SZZ };
@@ -232,6 +233,10 @@ static void planet_src(const disco_planet *pl, const double *prim, double *cons,
    double F[3];
    planetary_force(pl, x[0], x[1], x[2], &F[0], &F[1], &F[2]);
    double hr = 1.0, hp = x[0], hz = 1.0;
+   if(D->par.NoBC_Rmin == 1) {   /* planet.c:13-18, :205-212: polar vector adjustment */
+      double adjust = sin(0.5*dphi)/(0.5*dphi);
+      F[0] *= adjust; F[1] *= adjust;
+   }
    cons[SRR] += rho*hr*F[0]*dVdt;
    cons[LLL] += rho*hp*F[1]*dVdt;
    cons[SZZ] += rho*hz*F[2]*dVdt;
@@ -335,6 +340,10 @@ static void e_source(const double *prim, double *cons, const double *xp, const d
    double vr = prim[URR], omega = prim[UPP], vz = prim[UZZ];
    double x[3] = {r, 0.5*(xm[1] + xp[1]), z};
    double centrifugal = rho*omega*omega*r;
+   if(D->par.NoBC_Rmin == 1) {   /* polar_sources (euler.c:26, :195-200): geom_polar_vec_adjust */
+      double dphi = get_dp(xp[1], xm[1]);
+      centrifugal *= sin(0.5*dphi)/(0.5*dphi);
+   }
    double press_bal = Pp/r_1;
    cons[SRR] += dVdt*(centrifugal + press_bal);
    double om = get_om(x), om_r = get_om1(x), om_z = 0.0;
@@ -960,6 +969,25 @@ static void plm_trans(int dim)
          if(S*gR[q] < 0.0) gR[q] = 0.0; else if(fabs(PLM*S) < fabs(gR[q])) gR[q] = PLM*S;
       }
    }
+   /* plm_geom_boundary (plm.c:184-232) at a coordinate inner edge: geom_grad
+    * (cylindrical.c:141-173) acts only where the edge is r = 0. */
+   if(dim == 1 && D->NgRa == 0 && !(D->rj[0] < 0.0 || fabs(D->rj[-1]) > 1.0e-10*D->rj[0])) {
+      for(k = 0; k < D->Nz; k++) {
+         double r = centroid(D->rj[0], D->rj[-1], 1);
+         for(i = 0; i < D->Np[k*D->Nr]; i++) {
+            pcell *c = &D->ring[k*D->Nr][i];
+            for(q = 0; q < nq; q++) {
+               if(q == URR || (D->nc > BZZ && q == BRR)) {
+                  double SL = c->prim[q]/r, S = c->gradr[q];
+                  if(S*SL < 0.0) c->gradr[q] = 0.0;
+                  else if(fabs(PLM*SL) < fabs(S)) c->gradr[q] = PLM*SL;
+               } else {
+                  c->gradr[q] = 0.0;
+               }
+            }
+         }
+      }
+   }
 }
 
 /* ---- fluxes: misc.c:378-519, riemann.c:39-214 ------------------------------------- */
@@ -1527,35 +1555,90 @@ static void copy_distant(pcell *c, int Np, const pcell *c1, int Np1)
    for(i = 0; i < Np; i++) for(q = 0; q < D->nq; q++) c[i].prim[q] /= c[i].dphi;
 }
 
-/* boundary_zerograd_{rinn,rout,zbot,ztop} (boundary_functions.c:269-440):
- * layer by layer outward from the real domain; outflow3d adds a diode on
- * the normal velocity (Boundary/outflow3d.c). */
-static void zerograd_ring(int j, int k, int j1, int k1, int vq, int sign, int diode)
+/* The per-side primitives of boundary_functions.c.  copy_side covers
+ * boundary_zerograd_* (:269-441, the next ring inward, layer by layer
+ * outward, with the diode), boundary_reflect_* (:442-621, the mirror ring,
+ * normal velocity negated) and boundary_noslip_* (:914-1101, every
+ * velocity negated); init_side covers boundary_fixed_* (:161-268,
+ * set_cell_init), boundary_fixed_q_* (:662-773, set_cell_init_q) and
+ * boundary_fixed_phi_* (:774-913). */
+static void copy_ring(int jk, int jk1, int op, int vq, int sign, int diode)
 {
-   int jk = j + D->Nr*k, jk1 = j1 + D->Nr*k1;
    copy_distant(D->ring[jk], D->Np[jk], D->ring[jk1], D->Np[jk1]);
-   if(diode)
-      for(int i = 0; i < D->Np[jk]; i++)
-         if(sign*D->ring[jk][i].prim[vq] > 0) D->ring[jk][i].prim[vq] = 0.0;
+   for(int i = 0; i < D->Np[jk]; i++) {
+      double *p = D->ring[jk][i].prim;
+      if(op == DISCO_BCOP_ZEROGRAD && diode && sign*p[vq] > 0) p[vq] = 0.0;
+      if(op == DISCO_BCOP_REFLECT) p[vq] = -p[vq];
+      if(op == DISCO_BCOP_NOSLIP) { p[URR] = -p[URR]; p[UPP] = -p[UPP]; p[UZZ] = -p[UZZ]; }
+   }
 }
 
-static void boundary_zerograd(int diode)
+static void copy_side(const disco_bc_op *o)
 {
-   int j, k;
-   if(D->Nr > 1) {
-      for(k = 0; k < D->Nz; k++) for(j = D->NgRa - 1; j >= 0; j--) zerograd_ring(j, k, j + 1, k, URR, 1, diode);
-      for(k = 0; k < D->Nz; k++) for(j = D->Nr - D->NgRb; j < D->Nr; j++) zerograd_ring(j, k, j - 1, k, URR, -1, diode);
+   int j, k, Nr = D->Nr, Nz = D->Nz, zg = o->op == DISCO_BCOP_ZEROGRAD;
+   switch(o->side) {
+   case DISCO_SIDE_RINN:
+      for(k = 0; k < Nz; k++) for(j = D->NgRa - 1; j >= 0; j--)
+         copy_ring(j + Nr*k, (zg ? j + 1 : 2*D->NgRa - j - 1) + Nr*k, o->op, URR, 1, o->arg);
+      break;
+   case DISCO_SIDE_ROUT:
+      for(k = 0; k < Nz; k++) for(j = Nr - D->NgRb; j < Nr; j++)
+         copy_ring(j + Nr*k, (zg ? j - 1 : 2*(Nr - D->NgRb) - j - 1) + Nr*k, o->op, URR, -1, o->arg);
+      break;
+   case DISCO_SIDE_ZBOT:
+      for(k = D->NgZa - 1; k >= 0; k--) for(j = 0; j < Nr; j++)
+         copy_ring(j + Nr*k, j + Nr*(zg ? k + 1 : 2*D->NgZa - k - 1), o->op, UZZ, 1, o->arg);
+      break;
+   default:
+      for(k = Nz - D->NgZb; k < Nz; k++) for(j = 0; j < Nr; j++)
+         copy_ring(j + Nr*k, j + Nr*(zg ? k - 1 : 2*(Nz - D->NgZb) - k - 1), o->op, UZZ, -1, o->arg);
+      break;
    }
-   if(D->Nz > 1) {
-      for(j = 0; j < D->Nr; j++) for(k = D->NgZa - 1; k >= 0; k--) zerograd_ring(j, k, j, k + 1, UZZ, 1, diode);
-      for(j = 0; j < D->Nr; j++) for(k = D->Nz - D->NgZb; k < D->Nz; k++) zerograd_ring(j, k, j, k - 1, UZZ, -1, diode);
+}
+
+static void init_side(const disco_bc_op *o)
+{
+   int j0, j1, k0, k1;
+   if(o->side == DISCO_SIDE_RINN) { j0 = 0; j1 = D->NgRa; k0 = 0; k1 = D->Nz; }
+   else if(o->side == DISCO_SIDE_ROUT) { j0 = D->Nr - D->NgRb; j1 = D->Nr; k0 = 0; k1 = D->Nz; }
+   else if(o->side == DISCO_SIDE_ZBOT) { j0 = 0; j1 = D->Nr; k0 = 0; k1 = D->NgZa; }
+   else { j0 = 0; j1 = D->Nr; k0 = D->Nz - D->NgZb; k1 = D->Nz; }
+   for(int k = k0; k < k1; k++) for(int j = j0; j < j1; j++) {
+      int jk = j + D->Nr*k;
+      for(int i = 0; i < D->Np[jk]; i++) {
+         pcell *c = &D->ring[jk][i];
+         double xp[3] = {D->rj[j], c->piph, D->zk[k]}, xm[3] = {D->rj[j - 1], c->piph - c->dphi, D->zk[k - 1]};
+         double x[3], prim[MAXQ];
+         if(o->op == DISCO_BCOP_FIXED_Q) {
+            x[0] = centroid(D->rj[j], D->rj[j - 1], 1);
+            x[1] = c->piph - 0.5*c->dphi;
+            x[2] = centroid(D->zk[k], D->zk[k - 1], 2);
+            initial(prim, x);
+            for(int q = 0; q < D->nq; q++) if((o->arg >> q) & 1) c->prim[q] = prim[q];
+            continue;
+         }
+         if(o->op == DISCO_BCOP_FIXED_PHI) {
+            double phi = c->piph - 0.5*c->dphi;
+            while(phi < o->pa) phi += D->Pmax;
+            if(!(phi < o->pb)) continue;
+         }
+         centroid_arr(xp, xm, x);
+         initial(c->prim, x);
+      }
    }
 }
 
 static void boundary(void)
 {
-   if(D->mod.boundary == DISCO_BC_OUTFLOW3D || D->mod.boundary == DISCO_BC_ZEROGRAD) {
-      boundary_zerograd(D->mod.boundary == DISCO_BC_OUTFLOW3D);
+   disco_bc_op ops[DISCO_BC_MAX_OPS];
+   int n = disco_bc_plugin_ops(D->mod.boundary, ops);
+   if(n > 0) {   /* the plugin's primitives in call order: r sides, then z sides */
+      for(int o = 0; o < n; o++) {
+         int dim = ops[o].side < 2 ? 1 : 2;
+         if((dim == 1 && D->Nr <= 1) || (dim == 2 && D->Nz <= 1)) continue;
+         if(ops[o].op >= DISCO_BCOP_ZEROGRAD) copy_side(&ops[o]);
+         else init_side(&ops[o]);
+      }
       return;
    }
    for(int k = 0; k < D->Nz; k++) for(int j = 0; j < D->Nr; j++) {
@@ -1705,6 +1788,8 @@ port_domain *disco_port_create(const disco_host_domain *h)
    d->ct = d->mhd && h->mod.ct_mode == 2 && h->par.CT;
    if(d->mhd && (!d->ct || h->par.Riemann_Solver != 2 || h->NgRa == 0 || h->NgRb == 0 ||
                  h->NgZa == 0 || h->NgZb == 0)) { free(d); return NULL; }
+   disco_bc_op bops[DISCO_BC_MAX_OPS];
+   if(disco_bc_plugin_ops(h->mod.boundary, bops) < 0) { free(d); return NULL; }
    if(h->mod.hydro == DISCO_HYDRO_GRMHD || (d->mhd && h->mod.boundary > DISCO_BC_FIXED3D) ||
       (h->mod.analysis == DISCO_DIAG_MHDMRI && !d->mhd)) { free(d); return NULL; }
    static const int ndiag[] = {8, 5, 6, 5, 18};

@@ -48,6 +48,16 @@ CASES = {
     # z passes run too; outflow ghosts (Boundary/outflow3d.c) on the planet disk
     "cfg1_zerograd": ("configs/cfg1_vortex_zerograd", {"Num_R": 16, "Num_Z": 2}, 10),
     "cfg3_outflow": ("configs/cfg3_planet_disk_outflow", {"Num_R": 24}, 10),
+    # the other ghost-ring plugins (Boundary/*.c), each on the 3D vortex;
+    # polar3d and tube leave the inner ghost rings alone (they are meant for
+    # a domain without them), so their cases have none (NoBC_Rmin): with
+    # stale inner ghosts the reference run stalls (polar3d) or goes
+    # non-finite (tube) within six steps
+    **{f"bc_{b}": ("configs/cfg1_vortex_zerograd",
+                   {"Num_R": 12, "Num_Z": 2, **({"NoBC_Rmin": 1} if b in ("polar3d", "tube") else {})}, 6,
+                   {"BOUNDARY": b})
+       for b in ("zerograd_omk", "zerograd_omIN", "accrete3d", "fixRrefZ", "polar3d", "fixed_gap",
+                 "tube", "surfaceGravBox", "flowthrough")},
     # GRMHD thin disk around a Schwarzschild black hole (Kerr-Schild
     # cylindrical metric, HLL, cell-centred B) at 12 x 4 rings
     "cfg4_n12": ("configs/cfg4_grmhd_disk", {"Num_R": 12, "Num_Z": 4}, 5),
@@ -70,9 +80,34 @@ def build_ref(cfg: str, ref: str) -> str:
     return os.path.join(ROOT, "oracle", "_ref", os.path.basename(cfg), "disco_ref")
 
 
+def patch_mk(text: str, overrides: dict) -> str:
+    for k, v in overrides.items():
+        text, n = re.subn(rf"(?m)^{k}\s*=.*$", f"{k} = {v}", text)
+        if n == 0:
+            text += f"\n{k} = {v}\n"
+    return text
+
+
+def case_config(name: str):
+    """(config dir, in.par overrides, steps, Makefile_opt.in text); a case
+    with module overrides gets a generated config dir under oracle/_ref."""
+    cfg, over, nsteps = CASES[name][:3]
+    mk = open(os.path.join(ROOT, cfg, "Makefile_opt.in")).read()
+    if len(CASES[name]) > 3:
+        mk = patch_mk(mk, CASES[name][3])
+        gen = os.path.join("oracle", "_ref", "cfgs", name)
+        os.makedirs(os.path.join(ROOT, gen), exist_ok=True)
+        with open(os.path.join(ROOT, gen, "Makefile_opt.in"), "w") as f:
+            f.write(mk)
+        with open(os.path.join(ROOT, cfg, "in.par")) as f, open(os.path.join(ROOT, gen, "in.par"), "w") as g:
+            g.write(f.read())
+        return gen, over, nsteps, mk, cfg
+    return cfg, over, nsteps, mk, cfg
+
+
 def run_case(name: str, ref: str) -> None:
-    cfg, over, nsteps = CASES[name]
-    exe = build_ref(cfg, ref)
+    gcfg, over, nsteps, mk_text, cfg = case_config(name)
+    exe = build_ref(gcfg, ref)
     with open(os.path.join(ROOT, cfg, "in.par")) as f:
         par = patch_par(f.read(), over)
     with tempfile.TemporaryDirectory() as td:
@@ -96,6 +131,7 @@ def run_case(name: str, ref: str) -> None:
         dg = np.frombuffer(raw[8:], dtype="<f8")
         diag_tavg, diag_Qrz = dg[0], dg[1:1 + nq * nring].reshape(nring, nq)
     out = {"par_text": np.array(par), "nsteps": nsteps, "cfg": np.array(cfg), "report": rep,
+           "mk_text": np.array(mk_text),
            "diag_tavg": diag_tavg, "diag_Qrz": diag_Qrz,
            "Np": ini["Np"], "r_jph": ini["r_jph"], "z_kph": ini["z_kph"], "real": ini["real"],
            "init_piph": ini["piph"], "init_dphi": ini["dphi"], "init_prim": ini["prim"],

@@ -23,6 +23,18 @@ def write_par(text: str) -> str:
     return p
 
 
+def mk_path(g, cfg=None) -> str:
+    """Makefile_opt.in of a fixture: its own module text when it carries one
+    (cases that swap a module of a configuration), else the configuration's."""
+    if "mk_text" in g:
+        td = tempfile.mkdtemp(prefix="disco_mk_")
+        p = os.path.join(td, "Makefile_opt.in")
+        with open(p, "w") as f:
+            f.write(str(g["mk_text"]))
+        return p
+    return os.path.join(ROOT, str(cfg if cfg is not None else g["cfg"]), "Makefile_opt.in")
+
+
 def rel_l1(a: np.ndarray, b: np.ndarray) -> float:
     """sum |a - b| / sum |b| (relative L1 error of a against b)."""
     den = np.abs(b).sum()

@@ -8,7 +8,7 @@ import os
 import numpy as np
 import pytest
 
-from helpers import ROOT, cell_radius, grouped_rel_l1, load_golden, rel_l1, write_par
+from helpers import ROOT, cell_radius, grouped_rel_l1, load_golden, mk_path, rel_l1, write_par
 
 pytestmark = pytest.mark.gpu
 
@@ -18,7 +18,11 @@ CASES = {"cfg1_n24": "configs/cfg1_vortex", "cfg2_n12": "configs/cfg2_mhd_disk",
          "cfg3_n24": "configs/cfg3_planet_disk", "cfg5_n16": "configs/cfg5_cbd_mhd",
          "cfg4_n12": "configs/cfg4_grmhd_disk",
          "cfg1_zerograd": "configs/cfg1_vortex_zerograd",
-         "cfg3_outflow": "configs/cfg3_planet_disk_outflow"}
+         "cfg3_outflow": "configs/cfg3_planet_disk_outflow",
+         # the other ghost-ring plugins on the 3D vortex (module text in the fixture)
+         **{f"bc_{b}": "configs/cfg1_vortex_zerograd"
+            for b in ("zerograd_omk", "zerograd_omIN", "accrete3d", "fixRrefZ", "polar3d", "fixed_gap",
+                      "tube", "surfaceGravBox", "flowthrough")}}
 # GRMHD runs on the FP64 path only
 FP64_ONLY = {"cfg4_n12"}
 
@@ -27,8 +31,7 @@ def _domain(name, precision=0):
     import disco_gb300 as dg
     g = load_golden(name)
     cfg = CASES[name]
-    d = dg.Domain(write_par(g["par_text"]), os.path.join(ROOT, cfg, "Makefile_opt.in"),
-                  precision=precision)
+    d = dg.Domain(write_par(g["par_text"]), mk_path(g, cfg), precision=precision)
     return d, g
 
 

@@ -10,7 +10,7 @@ import tempfile
 import numpy as np
 import pytest
 
-from helpers import ROOT, load_golden, write_par
+from helpers import ROOT, load_golden, mk_path, write_par
 
 
 def _port_run(par_path, mk, nsteps):
@@ -25,15 +25,16 @@ def _port_run(par_path, mk, nsteps):
 def _port_domain(g):
     import disco_gb300 as dg
     from oracle.port import PortDomain
-    mk = os.path.join(ROOT, str(g["cfg"]), "Makefile_opt.in")
-    h = dg.HostDomain(dg.read_params(write_par(g["par_text"])), dg.read_modules(mk))
+    h = dg.HostDomain(dg.read_params(write_par(g["par_text"])), dg.read_modules(mk_path(g)))
     d = PortDomain(h)
     d.run(int(g["nsteps"]))
     return d
 
 
+BC_CASES = [f"bc_{b}" for b in ("zerograd_omk", "zerograd_omIN", "accrete3d", "fixRrefZ", "polar3d",
+                                 "fixed_gap", "tube", "surfaceGravBox", "flowthrough")]
 HYDRO_CASES = ["cfg1_n24", "cfg1_hll_static", "cfg1_exact_mesh", "cfg1_rotframe", "cfg3_n24",
-               "cfg1_zerograd", "cfg3_outflow"]
+               "cfg1_zerograd", "cfg3_outflow"] + BC_CASES
 
 
 @pytest.mark.parametrize("name", HYDRO_CASES)
@@ -43,8 +44,7 @@ def test_port_bit_exact_vs_golden(name):
     centre switch), the planet disk with alpha viscosity, and the
     zero-gradient / outflow ghost variants."""
     g = load_golden(name)
-    h, s = _port_run(write_par(g["par_text"]), os.path.join(ROOT, str(g["cfg"]), "Makefile_opt.in"),
-                     int(g["nsteps"]))
+    h, s = _port_run(write_par(g["par_text"]), mk_path(g), int(g["nsteps"]))
     real = g["real"].astype(bool)
     assert s["t"] == float(g["run_t"])
     assert np.array_equal(s["piph"], g["run_piph"])
