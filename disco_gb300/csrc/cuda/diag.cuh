@@ -12,11 +12,12 @@
 // share of the ring are formed in R from the R primitives; the tree is FP64.
 #pragma once
 #include "kernels.cuh"
+#include "phys_grmhd.cuh"
 
 namespace disco {
 
 constexpr int kDiagBlock = 128;
-constexpr int kDiagMax = 18;
+constexpr int kDiagMax = 48;
 
 // num_diagnostics() of each plugin
 DISCO_HD inline int diag_count(int id) {
@@ -26,6 +27,7 @@ DISCO_HD inline int diag_count(int id) {
     case 2: return 6;    // diag_cb.c:10
     case 3: return 5;    // diag_bl.c:10
     case 4: return 18;   // diag_mhdmri.c:9
+    case 5: return 48;   // diag_grmhdmri.c:12
     default: return 0;
   }
 }
@@ -161,13 +163,87 @@ DISCO_D void diag_cell(const DevParams& P, const DevState<R>& S, int c, double O
       Q[16] = sqrt(cs2);
       Q[17] = sqrt(B2 / rho);
     }
+  } else if constexpr (D == 5) {   // diag_grmhdmri.c:19-163 (FP64 GRMHD path)
+    if constexpr (NQ >= 8 && !kMix<R>) {
+      const double gl = P.gamma_law;
+      const double x[3] = {rd, phid, zd};
+      const KsMetric g(x, P.gr_M);
+      const double al = g.al, jac = g.jac;
+      const double* be = g.be;
+      const double* gam = g.gam;
+      const double* igam = g.igam;
+      const double sqrtgam = jac / al;
+      const double l[3] = {vr, S.prim[UPP * N + c], vz};
+      const double B[3] = {S.prim[BRR * N + c] / sqrtgam, S.prim[BPP * N + c] / (rd * sqrtgam),
+                           S.prim[BZZ * N + c] / sqrtgam};
+      double U[4];
+      ks_frame_U(g, U);
+      double igaml[3];
+      for (int i = 0; i < 3; ++i) {
+        igaml[i] = 0.0;
+        for (int j = 0; j < 3; ++j) igaml[i] += igam[3 * i + j] * l[j];
+      }
+      const double u2 = l[0] * igaml[0] + l[1] * igaml[1] + l[2] * igaml[2];
+      const double w = sqrt(1.0 + u2);
+      const double u0 = w / al;
+      double u[3];
+      for (int i = 0; i < 3; ++i) u[i] = igaml[i] - be[i] * u0;
+      const double l0 = -al * w + be[0] * l[0] + be[1] * l[1] + be[2] * l[2];
+      const double uU = U[0] * l0 + U[1] * l[0] + U[2] * l[1] + U[3] * l[2];
+      const double uB = l[0] * B[0] + l[1] * B[1] + l[2] * B[2];
+      const double b0 = uB / al;
+      double bd[3], b[3];
+      for (int i = 0; i < 3; ++i) {
+        bd[i] = (gam[3 * i] * B[0] + gam[3 * i + 1] * B[1] + gam[3 * i + 2] * B[2] + l[i] * uB) / w;
+        b[i] = (B[i] + uB * u[i]) / w;
+      }
+      double B2 = 0.0, UB = 0.0;
+      for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) {
+          B2 += gam[3 * i + j] * B[i] * B[j];
+          UB += gam[3 * i + j] * B[i] * (U[0] * be[j] + U[j + 1]);
+        }
+      const double b2 = (B2 + uB * uB) / (w * w);
+      const double Ub = (UB + uU * uB) / w;
+      const double rhoh = rho + gl / (gl - 1.0) * Pp + b2;
+      const double rhoe = Pp / (gl - 1.0);
+      const double rhohs = rhoh + b2;
+      const double tauU = jac * (-(rhoe + 0.5 * b2) * uU * u0 - (Pp + 0.5 * b2) * (uU * u0 + U[0]) -
+                                 rho * (uU + 1.0) * u0 + Ub * b0);
+      const double tau = sqrtgam * ((rhoe + 0.5 * b2) * w * w + (Pp + 0.5 * b2) * u2 + rho * w * u2 / (w + 1) -
+                                    b0 * b0);
+      const double bd0 = -al * al * b0 + be[0] * bd[0] + be[1] * bd[1] + be[2] * bd[2];
+      const double uu[4] = {u0, u[0], u[1], u[2]};
+      const double uud[4] = {l0, l[0], l[1], l[2]};
+      const double bb[4] = {b0, b[0], b[1], b[2]};
+      const double bbd[4] = {bd0, bd[0], bd[1], bd[2]};
+      Q[0] = rho; Q[1] = Pp;
+      Q[2] = l[0]; Q[3] = l[1]; Q[4] = l[2];
+      Q[5] = B[0]; Q[6] = B[1]; Q[7] = B[2];
+      Q[8] = jac * rho * u0;
+      Q[9] = tauU;
+      for (int i = 0; i < 3; ++i) Q[10 + i] = jac * (rhohs * u0 * l[i] - b0 * bd[i]);
+      for (int i = 0; i < 3; ++i) Q[13 + i] = jac * rho * uu[1 + i];
+      for (int i = 1; i < 4; ++i)
+        for (int j = 1; j < 4; ++j) {
+          const int n = 3 * (i - 1) + (j - 1);
+          Q[16 + n] = jac * (rhoh * uud[i] * uu[j]);
+          Q[25 + n] = jac * (b2 * uud[i] * uu[j]);
+          Q[34 + n] = jac * (-bbd[i] * bb[j]);
+        }
+      Q[43] = B2;
+      Q[44] = b2;
+      Q[45] = sqrt(gl * Pp / rhoh);
+      Q[46] = sqrt(b2 / rhohs);
+      Q[47] = tau;
+    }
   }
 }
 
 // One block per ring jk; Qrz is [Nr*Nz][ND], t_avg lives in scal[SC_TAVG].
 template <typename R, int NQ, int D>
 __global__ void __launch_bounds__(kDiagBlock) k_diag(DevParams P, DevState<R> S, double* Qrz) {
-  constexpr int ND = D == 0 ? 8 : D == 1 ? 5 : D == 2 ? 6 : D == 3 ? 5 : 18;
+  constexpr int ND = D == 0 ? 8 : D == 1 ? 5 : D == 2 ? 6 : D == 3 ? 5 : D == 4 ? 18 : 48;
   const int jk = blockIdx.x;
   const int k = jk / P.Nr, j = jk - k * P.Nr;
   const int off = S.ring_off[jk], Np = S.ring_off[jk + 1] - off;
@@ -180,7 +256,7 @@ __global__ void __launch_bounds__(kDiagBlock) k_diag(DevParams P, DevState<R> S,
   // Each thread's share (a few cells) is summed in R: FP32 on the mixed
   // path, whose cell volume is formed from the cell's own width, and FP64
   // with the reference's get_dV otherwise; the tree across threads is FP64.
-  const bool need_phi = D == 2 || ((D == 0 || D == 1) && P.Npl > 1);
+  const bool need_phi = D == 2 || D == 5 || ((D == 0 || D == 1) && P.Npl > 1);
   R sum[ND + 1];
 #pragma unroll
   for (int q = 0; q <= ND; ++q) sum[q] = (R)0.0;

@@ -393,6 +393,10 @@ struct Instance : InstanceBase {
       disco_set_error("ANALYSIS=diag_mhdmri reads magnetic fields: MHD or GRMHD modules only");
       return DISCO_E_MODULE;
     }
+    if (diag_id == DISCO_DIAG_GRMHDMRI && !Phys::GR) {
+      disco_set_error("ANALYSIS=diag_grmhdmri reads the metric: GRMHD module only");
+      return DISCO_E_MODULE;
+    }
     if (diag_n) {
       A(&diag_Qrz, (size_t)nring * diag_n);
       CK(cudaMemset(diag_Qrz, 0, sizeof(double) * nring * diag_n));
@@ -650,6 +654,10 @@ struct Instance : InstanceBase {
       case 4:
         if constexpr (NQ >= 8)
           LAUNCH("diag", (k_diag<R, NQ, 4><<<nring, kDiagBlock, 0, st>>>(P, S, diag_Qrz)));
+        break;
+      case 5:
+        if constexpr (Phys::GR)
+          LAUNCH("diag", (k_diag<R, NQ, 5><<<nring, kDiagBlock, 0, st>>>(P, S, diag_Qrz)));
         break;
       default: break;
     }

@@ -238,7 +238,8 @@ int disco_modules_read(const char *path, disco_modules *m)
                                "zerograd_omIN", "accrete3d", "fixRrefZ", "polar3d", "fixed_gap",
                                "tube", "surfaceGravBox", "flowthrough"};
    static const char *pla[] = {"none", "sun", "circular", "cm"};
-   static const char *ana[] = {"diag_euler", "diag_disk2d", "diag_cb", "diag_bl", "diag_mhdmri"};
+   static const char *ana[] = {"diag_euler", "diag_disk2d", "diag_cb", "diag_bl", "diag_mhdmri",
+                               "diag_grmhdmri"};
    int i;
    m->hydro = m->initial = m->boundary = m->planets = -1;
    for(i = 0; i < 3; i++) if(!strcmp(m->hydro_name, hyd[i])) m->hydro = i;
@@ -248,7 +249,7 @@ int disco_modules_read(const char *path, disco_modules *m)
    for(i = 0; i < DISCO_BC_COUNT; i++) if(!strcmp(m->boundary_name, bnd[i])) m->boundary = i;
    for(i = 0; i < 4; i++) if(!strcmp(m->planets_name, pla[i])) m->planets = i;
    m->analysis = DISCO_DIAG_NONE;
-   for(i = 0; i < 5; i++) if(!strcmp(m->analysis_name, ana[i])) m->analysis = i;
+   for(i = 0; i < 6; i++) if(!strcmp(m->analysis_name, ana[i])) m->analysis = i;
    char msg[256];
    if(m->analysis_name[0] && m->analysis < 0) { snprintf(msg, sizeof msg, "ANALYSIS=%s not built", m->analysis_name); disco_set_error(msg); return DISCO_E_MODULE; }
    if(m->hydro < 0) { snprintf(msg, sizeof msg, "HYDRO=%s not built", m->hydro_name); disco_set_error(msg); return DISCO_E_MODULE; }

@@ -67,7 +67,8 @@ enum disco_planets_id { DISCO_PL_NONE = 0, DISCO_PL_SUN = 1,
  * timestep() accumulates (analysis.c:52-108, timestep.c:51) */
 enum disco_analysis_id{ DISCO_DIAG_NONE = -1, DISCO_DIAG_EULER = 0,
                         DISCO_DIAG_DISK2D = 1, DISCO_DIAG_CB = 2,
-                        DISCO_DIAG_BL = 3, DISCO_DIAG_MHDMRI = 4 };
+                        DISCO_DIAG_BL = 3, DISCO_DIAG_MHDMRI = 4,
+                        DISCO_DIAG_GRMHDMRI = 5 };
 
 #define DISCO_MAX_PLANETS 4
 #define DISCO_NUM_G 2   /* ghost rings per side: paul.h:20 NUM_G */

@@ -25,7 +25,8 @@ extern "C" {
 #endif
 
 /* num_diagnostics() of the configured plugin: 8 (diag_euler), 5
- * (diag_disk2d), 6 (diag_cb), 5 (diag_bl), 18 (diag_mhdmri), 0 when
+ * (diag_disk2d), 6 (diag_cb), 5 (diag_bl), 18 (diag_mhdmri), 48
+ * (diag_grmhdmri, GRMHD only), 0 when
  * Makefile_opt.in names no ANALYSIS.  Negative DISCO_E_* on error. */
 int disco_gpu_diag_count(disco_gpu *g);
 

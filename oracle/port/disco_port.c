@@ -1791,7 +1791,9 @@ port_domain *disco_port_create(const disco_host_domain *h)
    disco_bc_op bops[DISCO_BC_MAX_OPS];
    if(disco_bc_plugin_ops(h->mod.boundary, bops) < 0) { free(d); return NULL; }
    if(h->mod.hydro == DISCO_HYDRO_GRMHD || (d->mhd && h->mod.boundary > DISCO_BC_FIXED3D) ||
-      (h->mod.analysis == DISCO_DIAG_MHDMRI && !d->mhd)) { free(d); return NULL; }
+      (h->mod.analysis == DISCO_DIAG_MHDMRI && !d->mhd) || h->mod.analysis > DISCO_DIAG_MHDMRI) {
+      free(d); return NULL;
+   }
    static const int ndiag[] = {8, 5, 6, 5, 18};
    d->nd = h->mod.analysis >= 0 ? ndiag[h->mod.analysis] : 0;
    d->Qrz = (double *)calloc((size_t)h->Nr*h->Nz*(d->nd ? d->nd : 1), sizeof(double));

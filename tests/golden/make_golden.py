@@ -61,6 +61,8 @@ CASES = {
     # GRMHD thin disk around a Schwarzschild black hole (Kerr-Schild
     # cylindrical metric, HLL, cell-centred B) at 12 x 4 rings
     "cfg4_n12": ("configs/cfg4_grmhd_disk", {"Num_R": 12, "Num_Z": 4}, 5),
+    # the same disk with the GRMHD ring diagnostics (Diagnostics/diag_grmhdmri.c)
+    "cfg4_diag": ("configs/cfg4_grmhd_disk", {"Num_R": 12, "Num_Z": 4}, 5, {"ANALYSIS": "diag_grmhdmri"}),
 }
 
 

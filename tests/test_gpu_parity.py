@@ -17,6 +17,7 @@ CASES = {"cfg1_n24": "configs/cfg1_vortex", "cfg2_n12": "configs/cfg2_mhd_disk",
          "cfg1_rotframe": "configs/cfg1_vortex",
          "cfg3_n24": "configs/cfg3_planet_disk", "cfg5_n16": "configs/cfg5_cbd_mhd",
          "cfg4_n12": "configs/cfg4_grmhd_disk",
+         "cfg4_diag": "configs/cfg4_grmhd_disk",
          "cfg1_zerograd": "configs/cfg1_vortex_zerograd",
          "cfg3_outflow": "configs/cfg3_planet_disk_outflow",
          # the other ghost-ring plugins on the 3D vortex (module text in the fixture)
@@ -24,7 +25,7 @@ CASES = {"cfg1_n24": "configs/cfg1_vortex", "cfg2_n12": "configs/cfg2_mhd_disk",
             for b in ("zerograd_omk", "zerograd_omIN", "accrete3d", "fixRrefZ", "polar3d", "fixed_gap",
                       "tube", "surfaceGravBox", "flowthrough")}}
 # GRMHD runs on the FP64 path only
-FP64_ONLY = {"cfg4_n12"}
+FP64_ONLY = {"cfg4_n12", "cfg4_diag"}
 
 
 def _domain(name, precision=0):
