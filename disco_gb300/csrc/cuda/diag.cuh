@@ -260,6 +260,7 @@ __global__ void __launch_bounds__(kDiagBlock) k_diag(DevParams P, DevState<R> S,
   R sum[ND + 1];
 #pragma unroll
   for (int q = 0; q <= ND; ++q) sum[q] = (R)0.0;
+#pragma unroll 4
   for (int i = threadIdx.x; i < Np; i += kDiagBlock) {
     const int c = off + i;
     double phic = 0.0;

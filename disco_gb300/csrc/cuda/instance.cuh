@@ -385,6 +385,15 @@ struct Instance : InstanceBase {
         CK(cudaMemcpy(d_gi, gi.data(), sizeof(int) * gi.size(), cudaMemcpyHostToDevice));
       }
       S.ghost_ring = d_gr; S.ghost_i0 = d_gi; S.nghost = (int)gr.size();
+      S.ghost_tab = nullptr;
+      if (S.nghost > 0 && (P.initial_id == 1 || P.initial_id == 2)) {   // axisymmetric disks
+        double* tab = nullptr;
+        A(&tab, (size_t)nring * NQ);
+        k_ghost_tab<R, NQ><<<(int)blocks(nring, 128), 128, 0, st>>>(P, nring, tab, S.r_jph, S.z_kph);
+        CK(cudaGetLastError());
+        CK(cudaStreamSynchronize(st));
+        S.ghost_tab = tab;
+      }
     }
     A(&S.planets, MAX_PL); A(&S.scal, SC_COUNT); A(&S.errs, 1);
     diag_id = dom->mod.analysis;

@@ -92,6 +92,7 @@ struct DevState {
   const int* ghost_ring;
   const int* ghost_i0;
   int nghost;
+  const double* ghost_tab;     // [nring][NQ]: fixed ghosts of an axisymmetric initial condition
   int* run_up_s[2];            // per cell: first face where the cell is L (pair above)
   int* run_up_e[2];
   int* run_dn_s[2];            // per cell: first face where the cell is R (pair below)
@@ -1414,23 +1415,14 @@ __global__ void __launch_bounds__(kTileCells) k_boundary(DevParams P, DevState<R
   // r and z of the evaluation point are those of the ring in both plugins
   const double xr = P.boundary_id == 0 ? .5 * (rj[j] + rj[j - 1]) : centroid_r(rj[j], rj[j - 1]);
   const double xz = P.boundary_id == 0 ? .5 * (zk[k] + zk[k - 1]) : centroid_z(zk[k], zk[k - 1]);
-  // the disk initial conditions (ids 1, 2) do not depend on phi: one
-  // evaluation serves the whole chunk
-  const bool axisym = P.initial_id == 1 || P.initial_id == 2;
-  __shared__ double sprim[MAX_Q];
-  if (axisym) {
-    if (threadIdx.x == 0) {
-      double x[3] = {xr, 0.0, xz};
-      initial_eval(P, sprim, x);
-    }
-    __syncthreads();
-  }
+  // the disk initial conditions do not depend on phi (or time): their ghost
+  // values come from the per-ring table made at set-up (k_ghost_tab)
   if (i >= Np || i >= i0 + kTileCells) return;
   const int c = off + i;
   double prim[MAX_Q];
-  if (axisym) {
+  if (S.ghost_tab) {
 #pragma unroll
-    for (int q = 0; q < NQ; ++q) prim[q] = sprim[q];
+    for (int q = 0; q < NQ; ++q) prim[q] = S.ghost_tab[(size_t)jk * NQ + q];
   } else {
     double x[3];
     x[0] = xr;
@@ -1441,6 +1433,25 @@ __global__ void __launch_bounds__(kTileCells) k_boundary(DevParams P, DevState<R
   if constexpr (kMix<R>) prim[UPP] -= S.ring_Om[jk];   // ring frame
 #pragma unroll
   for (int q = 0; q < NQ; ++q) S.prim[q * S.N + c] = (R)prim[q];
+}
+
+// Per-ring ghost values of fixed.c / fixed3d.c for the axisymmetric disk
+// initial conditions (ids 1, 2), evaluated once at set-up at the points
+// k_boundary uses (phi plays no part): one thread per ring.
+template <typename R, int NQ>
+__global__ void k_ghost_tab(DevParams P, int nring, double* tab, const double* r_jph, const double* z_kph) {
+  const int jk = blockIdx.x * blockDim.x + threadIdx.x;
+  if (jk >= nring) return;
+  const int k = jk / P.Nr, j = jk - k * P.Nr;
+  const double* rj = r_jph + 1;
+  const double* zk = z_kph + 1;
+  double x[3];
+  x[0] = P.boundary_id == 0 ? .5 * (rj[j] + rj[j - 1]) : centroid_r(rj[j], rj[j - 1]);
+  x[1] = 0.0;
+  x[2] = P.boundary_id == 0 ? .5 * (zk[k] + zk[k - 1]) : centroid_z(zk[k], zk[k - 1]);
+  double prim[MAX_Q];
+  initial_eval(P, prim, x);
+  for (int q = 0; q < NQ; ++q) tab[(size_t)jk * NQ + q] = prim[q];
 }
 
 // ---- ghost rings copied from other rings: boundary_functions.c:90-158 ----
