@@ -74,6 +74,53 @@ DISCO_D void planetary_force_mix(const DevParams& P, const DevPlanet& pl, double
   *fz = f1_sr * zz;
 }
 
+// The second body seen from one ring, for the mixed path's per-cell torque:
+// everything but the azimuth is a ring constant.
+template <typename R>
+struct RingBody {
+  double pp;          // the body's azimuth (FP64)
+  R rr, rpp, dr, zz;  // ring radius, body radius, their difference (FP64 first), z
+  R M, eps2;
+  int type;
+};
+
+template <typename R>
+DISCO_D RingBody<R> ring_body(const DevParams& P, const DevPlanet& pl, double r, double z) {
+  RingBody<R> b;
+  double rp = pl.r, pp = pl.phi;
+  if (P.grav2D == 1) z = 0.0;
+  b.pp = pp;
+  b.rr = (R)r; b.rpp = (R)rp; b.dr = (R)(r - rp); b.zz = (R)z;
+  b.M = (R)pl.M; b.eps2 = (R)pl.eps * (R)pl.eps;
+  b.type = pl.type;
+  return b;
+}
+
+// planetary_force_mix (mode 0) with the ring constants of RingBody: per cell
+// one FP64 difference piph - phi_p, wrapped to [-pi, pi] in FP64 and
+// rounded to FP32 on the integer pipe; the half width comes off in FP32.
+template <typename R>
+DISCO_D R ring_body_fphi(const RingBody<R>& b, double piph, R dph) {
+  double d = piph - b.pp;
+  if (d > M_PI) d -= 2.0 * M_PI;
+  if (d < -M_PI) d += 2.0 * M_PI;
+  R del = d2f_int(d) - (R)0.5 * dph;
+  if (del < (R)-M_PI) del += (R)(2.0 * M_PI);
+  R sh, ch;
+  sincos((R)0.5 * del, &sh, &ch);
+  const R srp2 = b.dr * b.dr + (R)4.0 * b.rr * b.rpp * sh * sh;
+  const R sr2 = srp2 + b.zz * b.zz;
+  R f1_sr = 0.0;
+  if (b.type == PL_POINTMASS) {
+    const R dd = sr2 + b.eps2;
+    f1_sr = -b.M / (dd * sqrt(dd));
+  } else if (b.type == PL_SURFACEGRAV) {
+    f1_sr = -b.M / sqrt(sr2);
+  }
+  if (!(srp2 > (R)0.0)) return (R)0.0;
+  return b.rpp * ((R)2.0 * sh * ch) * f1_sr;
+}
+
 // planetaryForce at the cell centroid: the reference's operation order on
 // the FP64 path, the planet-frame form above on the mixed path
 template <typename R>
@@ -88,7 +135,7 @@ DISCO_D void diag_force(const DevParams& P, const DevPlanet& pl, double r, doubl
 // azimuthal velocity; 0 on the FP64 path)
 template <typename R, int NQ, int D>
 DISCO_D void diag_cell(const DevParams& P, const DevState<R>& S, int c, double Om, double rd, double phid,
-                       double zd, R* Q) {
+                       double zd, R* Q, const RingBody<R>* rb = nullptr, double piph = 0.0, R dph = 0) {
   const int N = S.N;
   const R r = (R)rd, phi = (R)phid;
   const R rho = S.prim[RHO * N + c], Pp = S.prim[PPP * N + c];
@@ -97,7 +144,10 @@ DISCO_D void diag_cell(const DevParams& P, const DevState<R>& S, int c, double O
   const R twopi = (R)(2. * M_PI);
   if constexpr (D == 0) {   // diag_euler.c:18-44
     R Fr, Fp = 0.0, Fz;
-    if (P.Npl > 1) diag_force<R>(P, S.planets[1], rd, phid, zd, &Fr, &Fp, &Fz, 0);
+    if (P.Npl > 1) {
+      if (kMix<R> && rb) Fp = ring_body_fphi<R>(*rb, piph, dph);
+      else diag_force<R>(P, S.planets[1], rd, phid, zd, &Fr, &Fp, &Fz, 0);
+    }
     Q[0] = rho;
     Q[1] = twopi * r * rho * vr;
     Q[2] = twopi * r * rho * vz;
@@ -108,7 +158,10 @@ DISCO_D void diag_cell(const DevParams& P, const DevState<R>& S, int c, double O
     Q[7] = Pp;
   } else if constexpr (D == 1) {   // diag_disk2d.c:18-41
     R Fr, Fp = 0.0, Fz;
-    if (P.Npl > 1) diag_force<R>(P, S.planets[1], rd, phid, 0.0, &Fr, &Fp, &Fz, 0);
+    if (P.Npl > 1) {
+      if (kMix<R> && rb) Fp = ring_body_fphi<R>(*rb, piph, dph);
+      else diag_force<R>(P, S.planets[1], rd, phid, 0.0, &Fr, &Fp, &Fz, 0);
+    }
     Q[0] = rho;
     Q[1] = twopi * r * rho * vr;
     Q[2] = twopi * r * rho * (r * Fp);
@@ -256,7 +309,12 @@ __global__ void __launch_bounds__(kDiagBlock) k_diag(DevParams P, DevState<R> S,
   // Each thread's share (a few cells) is summed in R: FP32 on the mixed
   // path, whose cell volume is formed from the cell's own width, and FP64
   // with the reference's get_dV otherwise; the tree across threads is FP64.
-  const bool need_phi = D == 2 || D == 5 || ((D == 0 || D == 1) && P.Npl > 1);
+  // the mixed path's torque (diag_euler, diag_disk2d) takes the ring
+  // constants once; the other forms need each cell's centroid azimuth
+  const bool ring_force = kMix<R> && (D == 0 || D == 1) && P.Npl > 1 && P.grav2D != 2;
+  const bool need_phi = !ring_force && (D == 2 || D == 5 || ((D == 0 || D == 1) && P.Npl > 1));
+  RingBody<R> rb;
+  if (ring_force) rb = ring_body<R>(P, S.planets[1], rc, D == 1 ? 0.0 : zc);
   R sum[ND + 1];
 #pragma unroll
   for (int q = 0; q <= ND; ++q) sum[q] = (R)0.0;
@@ -265,10 +323,14 @@ __global__ void __launch_bounds__(kDiagBlock) k_diag(DevParams P, DevState<R> S,
     const int c = off + i;
     double phic = 0.0;
     R dV;
+    double piph = 0.0;
+    R dphf = 0;
     if constexpr (kMix<R>) {
       const double dph = S.dphi[c];
       if (need_phi) phic = S.piph[c] - .5 * dph;
-      dV = (R)rdr * d2f_int(dph) * (R)dz;
+      if (ring_force) piph = S.piph[c];
+      dphf = d2f_int(dph);
+      dV = (R)rdr * dphf * (R)dz;
     } else {
       const double phip = S.piph[c];
       const double phim = phip - S.dphi[c];
@@ -276,7 +338,7 @@ __global__ void __launch_bounds__(kDiagBlock) k_diag(DevParams P, DevState<R> S,
       dV = rdr * get_dp(phip, phim, P.phi_max) * dz;   // get_dV, cylindrical.c:56-63
     }
     R Q[ND];
-    diag_cell<R, NQ, D>(P, S, c, Om, rc, phic, zc, Q);
+    diag_cell<R, NQ, D>(P, S, c, Om, rc, phic, zc, Q, ring_force ? &rb : nullptr, piph, dphf);
 #pragma unroll
     for (int q = 0; q < ND; ++q) sum[q] += Q[q] * dV;
     sum[ND] += dV;
