@@ -116,3 +116,40 @@ def test_missing_files_and_modules_fail_loudly(tmp_path):
                   "BOUNDARY = fixed\nPLANETS = none\nNUM_C = 5\nNUM_N = 1\nCT_MODE = 0\n")
     with pytest.raises(dg.DiscoError, match="HYDRO=grmhd2"):
         dg.read_modules(str(mk))
+
+
+BOUNDARY_PLUGINS = ["fixed", "fixed3d", "outflow3d", "zerograd", "zerograd_omk", "zerograd_omIN",
+                    "accrete3d", "fixRrefZ", "polar3d", "fixed_gap", "tube", "surfaceGravBox",
+                    "flowthrough"]
+ANALYSIS_PLUGINS = ["diag_euler", "diag_disk2d", "diag_cb", "diag_bl", "diag_mhdmri", "diag_grmhdmri"]
+
+
+def _mk(tmp_path, **kw):
+    keys = {"INITIAL": "vortex_gauss", "HYDRO": "euler", "GEOMETRY": "cylindrical", "BOUNDARY": "fixed",
+            "PLANETS": "none", "ANALYSIS": "diag_euler", "NUM_C": 5, "NUM_N": 1, "CT_MODE": 0}
+    keys.update(kw)
+    p = tmp_path / "Makefile_opt.in"
+    p.write_text("".join(f"{k} = {v}\n" for k, v in keys.items() if v is not None))
+    return str(p)
+
+
+def test_boundary_and_analysis_plugins_select(tmp_path):
+    """Every built BOUNDARY and ANALYSIS plugin name maps to its id, in the
+    order of disco_boundary_id / disco_analysis_id; a missing ANALYSIS key
+    selects none (the reference build requires one: no accumulators)."""
+    dg = _dg()
+    for i, b in enumerate(BOUNDARY_PLUGINS):
+        m = dg.read_modules(_mk(tmp_path, BOUNDARY=b))
+        assert m.boundary == i and m.boundary_name.decode() == b
+    for i, a in enumerate(ANALYSIS_PLUGINS):
+        m = dg.read_modules(_mk(tmp_path, ANALYSIS=a))
+        assert m.analysis == i and m.analysis_name.decode() == a
+    assert dg.read_modules(_mk(tmp_path, ANALYSIS=None)).analysis == -1
+
+
+@pytest.mark.parametrize("key,name", [("BOUNDARY", "horizon3d"), ("BOUNDARY", "inflow"),
+                                      ("ANALYSIS", "diag_nonexistent")])
+def test_unbuilt_plugins_fail_loudly(tmp_path, key, name):
+    dg = _dg()
+    with pytest.raises(dg.DiscoError, match=f"{key}={name} not built"):
+        dg.read_modules(_mk(tmp_path, **{key: name}))
