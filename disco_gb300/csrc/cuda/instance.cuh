@@ -211,10 +211,14 @@ struct Instance : InstanceBase {
       disco_set_error("sink/nozzle/cooling/damping source terms are not built");
       return DISCO_E_MODULE;
     }
-    if (p.Timestep != 0) {
-      disco_set_error("only Timestep 0 (RK2) is built");
+    if (p.Timestep != 0 && p.Timestep != 3) {
+      // Timestep 1 runs forward Euler and then the RK2 pair as well
+      // (timestep.c:29-49: the RK2 branch is the else of the RK3 test),
+      // blending against the state before the Euler step
+      disco_set_error("Timestep 0 (RK2) and 3 (RK3) are built");
       return DISCO_E_MODULE;
     }
+    rk3 = p.Timestep == 3;
     ct = Phys::MHD && !Phys::GR && dom->mod.ct_mode == 2 && p.CT;
     P.gr_M = p.metricPar2;
     if constexpr (Phys::GR) {
@@ -614,8 +618,9 @@ struct Instance : InstanceBase {
              (k_flux_trans<Phys, R, NQ><<<grid, 256, 0, st>>>(P, S, dim, jmin, jc, kmin, fac)));
     }
   }
-  // one onestep (onestep.c:86-186)
-  void substep(double RK, double fac, int first) {
+  // one onestep (onestep.c:86-186); mid marks a substep that is neither the
+  // first nor the last (RK3's second)
+  void substep(double RK, double fac, int first, int mid = 0) {
     if (first) launch_wcell();
     LAUNCH("plm_phi", (k_plm_phi<R, NQ><<<blocks(N), 256, 0, st>>>(P, S)));
     launch_plm_trans();
@@ -636,7 +641,8 @@ struct Instance : InstanceBase {
         if (C.ev_cid && !first) LAUNCH("ct_edge_flag", (k_set_flag<<<1, 1, 0, st>>>(C.ev_ok, 1)));
       }
     }
-    LAUNCH("update", (k_update<Phys, R, NQ><<<blocks(N), 256, 0, st>>>(P, S, RK, fac, first, ct ? 0 : 1)));
+    LAUNCH("update", (k_update<Phys, R, NQ><<<blocks(N), 256, 0, st>>>(P, S, RK, fac, first + 2 * mid,
+                                                                      ct ? 0 : 1)));
     if (first) {
       parity ^= 1;
       set_piph(parity);
@@ -671,10 +677,17 @@ struct Instance : InstanceBase {
       default: break;
     }
   }
-  // timestep.c:7-54 with Timestep 0 (RK2), then add_diagnostics (:51)
+  // timestep.c:7-54: Timestep 0 (RK2) or 3 (RK3), then add_diagnostics (:51)
+  int rk3 = 0;
   void step_kernels() {
-    substep(0.0, 1.0, 1);
-    substep(0.5, 0.5, 0);
+    if (rk3) {
+      substep(0.0, 1.0, 1);
+      substep(0.75, 0.25, 0, 1);
+      substep(1. / 3., 2. / 3., 0);
+    } else {
+      substep(0.0, 1.0, 1);
+      substep(0.5, 0.5, 0);
+    }
     launch_diag();
   }
   // Ring diagnostics: Qrz [Nr*Nz][n] and t_avg, as analysis.c keeps them

@@ -1120,7 +1120,9 @@ __global__ void __launch_bounds__(256, kMix<R> ? 4 : 1) k_flux_trans(DevParams P
 // the reference's order, add_source (misc.c:550), move_cells/clean_pi/calc_dp
 // (misc.c:266, :8, :281), calc_prim (misc.c:300).
 template <typename Phys, typename R, int NQ>
-__global__ void __launch_bounds__(256, kMix<R> ? 4 : 1) k_update(DevParams P, DevState<R> S, double RK, double fac, int first, int do_c2p) {
+__global__ void __launch_bounds__(256, kMix<R> ? 4 : 1) k_update(DevParams P, DevState<R> S, double RK, double fac, int stage, int do_c2p) {
+  // stage: 1 the first substep, 2 a middle substep (RK3's second), 0 the last
+  const int first = stage == 1, mid = stage == 2;
   int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= S.N) return;
   const int N = S.N;
@@ -1242,13 +1244,21 @@ __global__ void __launch_bounds__(256, kMix<R> ? 4 : 1) k_update(DevParams P, De
       // fluxes after every update and never read from here).  So
       // U = cons + (dU - RK d1): one FP64 add per component, and the RK
       // copy of the state is R instead of FP64.
+      // A middle substep (RK3's second) keeps the increment since the step
+      // start current for the last one: d_k = d_(k-1) + (U_k - U_(k-1)).
       const R rk = to_r<R>(RK);
+      const bool whole = P.include_viscosity || P.rot_flag;
 #pragma unroll
       for (int q = 0; q < NQ; ++q) {
         double u = S.cons[q * N + c];
         R d = dU[q];
-        if (first) S.RKdU[q * N + c] = d;
-        else d = fma(-rk, S.RKdU[q * N + c], d);
+        if (first) {
+          S.RKdU[q * N + c] = d;
+        } else {
+          const R dold = S.RKdU[q * N + c];
+          d = fma(-rk, dold, d);
+          if (mid && !whole) S.RKdU[q * N + c] = dold + d;
+        }
         U[q] = u + from_r<R>(d);
       }
       if (P.include_viscosity || P.rot_flag) {
@@ -1301,9 +1311,12 @@ __global__ void __launch_bounds__(256, kMix<R> ? 4 : 1) k_update(DevParams P, De
       // the viscous and rotating-frame sources go to U in FP64 after the R
       // sum: the increment kept for the second substep is then the whole
       // change of this substep
-      if (first && (P.include_viscosity || P.rot_flag)) {
+      if ((first || mid) && (P.include_viscosity || P.rot_flag)) {
 #pragma unroll
-        for (int q = 0; q < NQ; ++q) S.RKdU[q * N + c] = to_r<R>(U[q] - S.cons[q * N + c]);
+        for (int q = 0; q < NQ; ++q) {
+          const R dold = first ? (R)0 : S.RKdU[q * N + c];
+          S.RKdU[q * N + c] = dold + to_r<R>(U[q] - S.cons[q * N + c]);
+        }
       }
     }
 #pragma unroll

@@ -1790,6 +1790,7 @@ port_domain *disco_port_create(const disco_host_domain *h)
                  h->NgZa == 0 || h->NgZb == 0)) { free(d); return NULL; }
    disco_bc_op bops[DISCO_BC_MAX_OPS];
    if(disco_bc_plugin_ops(h->mod.boundary, bops) < 0) { free(d); return NULL; }
+   if(h->par.Timestep != 0 && h->par.Timestep != 3) { free(d); return NULL; }
    if(h->mod.hydro == DISCO_HYDRO_GRMHD || (d->mhd && h->mod.boundary > DISCO_BC_FIXED3D) ||
       (h->mod.analysis == DISCO_DIAG_MHDMRI && !d->mhd) || h->mod.analysis > DISCO_DIAG_MHDMRI) {
       free(d); return NULL;
@@ -1864,9 +1865,18 @@ double disco_port_step(port_domain *d)
       memcpy(d->cells[c].RKcons, d->cells[c].cons, sizeof(double)*MAXQ);
       memcpy(d->cells[c].RK_Phi, d->cells[c].Phi, sizeof(double)*5);
    }
-   onestep(0.0, dt, 1);
-   d->t += dt;
-   onestep(0.5, 0.5*dt, 0);
+   if(d->par.Timestep == 3) {   /* timestep.c:35-42 */
+      onestep(0.0, dt, 1);
+      d->t += dt;
+      onestep(0.75, 0.25*dt, 0);
+      d->t -= dt*0.5;
+      onestep(1./3., 2.*dt/3., 0);
+      d->t += dt*0.5;
+   } else {
+      onestep(0.0, dt, 1);
+      d->t += dt;
+      onestep(0.5, 0.5*dt, 0);
+   }
    add_diagnostics(dt);
    return dt;
 }

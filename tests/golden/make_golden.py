@@ -58,6 +58,11 @@ CASES = {
                    {"BOUNDARY": b})
        for b in ("zerograd_omk", "zerograd_omIN", "accrete3d", "fixRrefZ", "polar3d", "fixed_gap",
                  "tube", "surfaceGravBox", "flowthrough")},
+    # third-order Runge-Kutta (Timestep 3, timestep.c:35-42) on the vortex,
+    # the MHD disk and the viscous planet disk
+    "cfg1_rk3": ("configs/cfg1_vortex", {"Num_R": 24, "Timestep": 3}, 10),
+    "cfg2_rk3": ("configs/cfg2_mhd_disk", {"Num_R": 12, "Num_Z": 6, "Timestep": 3}, 5),
+    "cfg3_rk3": ("configs/cfg3_planet_disk", {"Num_R": 24, "Timestep": 3}, 10),
     # GRMHD thin disk around a Schwarzschild black hole (Kerr-Schild
     # cylindrical metric, HLL, cell-centred B) at 12 x 4 rings
     "cfg4_n12": ("configs/cfg4_grmhd_disk", {"Num_R": 12, "Num_Z": 4}, 5),

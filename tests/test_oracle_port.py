@@ -34,7 +34,7 @@ def _port_domain(g):
 BC_CASES = [f"bc_{b}" for b in ("zerograd_omk", "zerograd_omIN", "accrete3d", "fixRrefZ", "polar3d",
                                  "fixed_gap", "tube", "surfaceGravBox", "flowthrough")]
 HYDRO_CASES = ["cfg1_n24", "cfg1_hll_static", "cfg1_exact_mesh", "cfg1_rotframe", "cfg3_n24",
-               "cfg1_zerograd", "cfg3_outflow"] + BC_CASES
+               "cfg1_zerograd", "cfg3_outflow", "cfg1_rk3", "cfg3_rk3"] + BC_CASES
 
 
 @pytest.mark.parametrize("name", HYDRO_CASES)
@@ -78,10 +78,12 @@ def test_port_bit_exact_vs_reference_binary():
     shutil.rmtree(td)
 
 
-def test_port_mhd_ct_bit_exact_vs_golden():
-    """3D MHD disk with HLLD and constrained transport: the oracle equals the
-    reference bit for bit (conserved variables, face fluxes, positions)."""
-    g = load_golden("cfg2_n12")
+@pytest.mark.parametrize("name", ["cfg2_n12", "cfg2_rk3"])
+def test_port_mhd_ct_bit_exact_vs_golden(name):
+    """3D MHD disk with HLLD and constrained transport (RK2 and RK3): the
+    oracle equals the reference bit for bit (conserved variables, face
+    fluxes, positions)."""
+    g = load_golden(name)
     h, s = _port_run(write_par(g["par_text"]), os.path.join(ROOT, "configs/cfg2_mhd_disk/Makefile_opt.in"),
                      int(g["nsteps"]))
     real = g["real"].astype(bool)
