@@ -54,6 +54,10 @@ class DiscoParams(C.Structure):
         ("grav_eps", C.c_double),
         ("read_errors", C.c_int),
         ("sinkPar3", C.c_double),
+        ("coolPar1", C.c_double), ("coolPar2", C.c_double), ("coolPar3", C.c_double), ("coolPar4", C.c_double),
+        ("dampTimeInner", C.c_double), ("dampLenInner", C.c_double), ("dampTimeOuter", C.c_double),
+        ("dampLenOuter", C.c_double), ("dampTimeUpper", C.c_double), ("dampLenUpper", C.c_double),
+        ("dampTimeLower", C.c_double), ("dampLenLower", C.c_double),
     ]
 
 

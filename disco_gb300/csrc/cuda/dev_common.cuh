@@ -50,6 +50,13 @@ struct DevParams {
   // plm_geom_boundary (plm.c:184-186) acts on the inner ring when it has no
   // ghosts and geom_grad (cylindrical.c:150-155) finds its edge at r = 0
   int geom_bd_r;
+  // cooling and damping (sink.c:274-427): Cool_Type, Cool_Par1 (beta);
+  // Damp{Inner,Outer,Upper,Lower}_{Type,Time,Len}; the domain edges they use
+  int cool_type, cool_damp, twoD;
+  double cool_beta;
+  int damp_type[4];
+  double damp_time[4], damp_len[4];
+  double dom_rmin, dom_rmax, dom_zmax;
   int Npl;
   // GRMHD: the black-hole mass of the Kerr-Schild metric (Metric_Par2)
   double gr_M;

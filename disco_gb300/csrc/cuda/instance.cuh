@@ -206,9 +206,24 @@ struct Instance : InstanceBase {
       disco_set_error("Riemann_Solver = HLLD with a hydro module (riemann.c:19-22)");
       return DISCO_E_MODULE;
     }
-    if (p.sinkType || p.nozzleType || p.coolType || p.dampInnerType || p.dampOuterType ||
-        p.dampUpperType || p.dampLowerType) {
-      disco_set_error("sink/nozzle/cooling/damping source terms are not built");
+    if (p.sinkType || p.nozzleType) {
+      disco_set_error("sink/nozzle source terms are not built");
+      return DISCO_E_MODULE;
+    }
+    P.cool_type = p.coolType;
+    P.cool_beta = p.coolPar1;
+    P.damp_type[0] = p.dampInnerType; P.damp_type[1] = p.dampOuterType;
+    P.damp_type[2] = p.dampUpperType; P.damp_type[3] = p.dampLowerType;
+    P.damp_len[0] = p.dampLenInner; P.damp_len[1] = p.dampLenOuter;
+    P.damp_len[2] = p.dampLenUpper; P.damp_len[3] = p.dampLenLower;
+    P.damp_time[0] = p.dampTimeInner; P.damp_time[1] = p.dampTimeOuter;
+    P.damp_time[2] = p.dampTimeUpper; P.damp_time[3] = p.dampTimeLower;
+    P.dom_rmin = p.rmin; P.dom_rmax = p.rmax; P.dom_zmax = p.zmax;
+    P.twoD = dom->Nz == 1;
+    P.cool_damp = (p.coolType == 1 || p.coolType == 2) ||
+                  p.dampInnerType > 0 || p.dampOuterType > 0 || p.dampUpperType > 0 || p.dampLowerType > 0;
+    if (P.cool_damp && Phys::GR) {
+      disco_set_error("cooling/damping are built for the Newtonian modules");
       return DISCO_E_MODULE;
     }
     if (p.Timestep != 0 && p.Timestep != 3) {

@@ -178,7 +178,7 @@ DISCO_D bool pair_in_flux_range(const DevParams& P, int dim, int pair) {
 }
 
 // ---- initial() dispatch (plugin chosen by Makefile_opt.in INITIAL) --------
-DISCO_D void initial_eval(const DevParams& P, double* prim, const double* x) {
+DISCO_D void initial_raw(const DevParams& P, double* prim, const double* x) {
   if (P.initial_id == 0) {
     disco_ic_vortex_gauss V{P.ic[0], P.ic[1], P.ic[2], P.ic[3], P.ic[4], P.gamma_law};
     disco_ic_vortex_gauss_eval(&V, prim, x, P.num_c, P.num_q);
@@ -197,7 +197,11 @@ DISCO_D void initial_eval(const DevParams& P, double* prim, const double* x) {
       disco_ic_gr_disk_eval(&G, prim, x, P.num_c, P.num_q);
     }
   }
-  if (P.rot_flag) prim[UPP] -= P.rot_omega;   // subtract_omega, rotframe.c:15
+}
+// initial() followed by subtract_omega (rotframe.c:15), as set_cell_init does
+DISCO_D void initial_eval(const DevParams& P, double* prim, const double* x) {
+  initial_raw(P, prim, x);
+  if (P.rot_flag) prim[UPP] -= P.rot_omega;
 }
 
 // ---- set_wcell, misc.c:101-168 --------------------------------------------
@@ -927,6 +931,72 @@ __global__ void __launch_bounds__(kTileCells) k_plm_trans(DevParams P, DevState<
   }
 }
 
+// ---- cooling (sink.c:274-326) and damping (sink.c:329-427) of one cell -----
+// add_source runs them first (misc.c:579-580).  x is the cell centroid; the
+// planets' summed |f|/|x - x_p| (mode-1 forces) sets the orbital rate of the
+// beta cooling and of the type-2 damping times.  Damping relaxes DDD, SRR,
+// LLL, SZZ and TAU towards initial() with expm1(-dt f), f the damping
+// factor of the last active side (the reference's ratetot is unused).
+template <typename Phys, typename R, int NQ>
+DISCO_D void cool_damp_src(const DevParams& P, const DevPlanet* pl, const R* prim, double* U,
+                           const double* xp, const double* xm, double dV, double dt) {
+  const double x[3] = {centroid_r(xp[0], xm[0]), .5 * (xp[1] + xm[1]), centroid_z(xp[2], xm[2])};
+  auto orbital = [&]() {
+    const double gx = x[0] * cos(x[1]), gy = x[0] * sin(x[1]);
+    double omtot = 0.0;
+    for (int p = 0; p < P.Npl; ++p) {
+      const double px = pl[p].r * cos(pl[p].phi), py = pl[p].r * sin(pl[p].phi);
+      const double dx = gx - px, dy = gy - py;
+      const double mag = sqrt(dx * dx + dy * dy);
+      double fr, fp, fz;
+      planetary_force<double>(P, pl[p], x[0], x[1], x[2], &fr, &fp, &fz, 1);
+      omtot += sqrt(fr * fr + fp * fp + fz * fz) / mag;
+    }
+    return sqrt(omtot);
+  };
+  if (P.cool_type == 1 || P.cool_type == 2) {   // COOL_BETA, COOL_BETA_RELAX
+    const double press = prim[PPP], rho = prim[RHO];
+    const double gm1 = P.gamma_law - 1.0;
+    const double enTarget = get_cs2<double>(P, pl, x[0], x[1]) / (P.gamma_law * gm1);
+    const double enCurrent = press / (rho * gm1);
+    if (P.cool_type == 2 || enCurrent > enTarget) {
+      const double omtot = orbital();
+      const double Tm1 = expm1(-dt * omtot / P.cool_beta);
+      U[TAU] += rho * dV * (enCurrent - enTarget) * Tm1;
+    }
+  }
+  if (P.damp_type[0] + P.damp_type[1] + P.damp_type[2] + P.damp_type[3] > 0) {
+    // inner, outer, upper, lower (upper and lower only in 3D); both z sides
+    // measure from the upper edge, as the reference does.  The damping times
+    // (and the orbital rate of type 2) enter only the reference's unused
+    // ratetot, so they play no part here.
+    double dampFactor = 0.0;
+    for (int side = 0; side < 4; ++side) {
+      if (P.damp_type[side] <= 0 || (side >= 2 && P.twoD)) continue;
+      const double theta = side == 0 ? (x[0] - P.dom_rmin) / P.damp_len[0]
+                         : side == 1 ? (P.dom_rmax - x[0]) / P.damp_len[1]
+                                     : (P.dom_zmax - x[2]) / P.damp_len[side];
+      const bool rising = side == 1 || side == 2;   // outer, upper: pow(1 - theta^2, 2)
+      if (theta > 1.0) dampFactor = 0.0;
+      else dampFactor = rising ? pow(1.0 - pow(theta, 2.0), 2.0) : 1.0 - pow(1.0 - pow(theta, 2.0), 2.0);
+    }
+    dampFactor = expm1(-dt * dampFactor);
+    double p0[MAX_Q];
+    initial_raw(P, p0, x);
+    R p0r[NQ];
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) p0r[q] = (R)p0[q];
+    double c0[NQ], c1[NQ];
+    Phys::template prim2cons<double>(P, p0r, c0, (R)x[0], (R)dV);
+    Phys::template prim2cons<double>(P, prim, c1, (R)x[0], (R)dV);
+    U[DDD] += (c1[DDD] - c0[DDD]) * dampFactor;
+    U[SRR] += (c1[SRR] - c0[SRR]) * dampFactor;
+    U[LLL] += (c1[LLL] - c0[LLL]) * dampFactor;
+    U[SZZ] += (c1[SZZ] - c0[SZZ]) * dampFactor;
+    U[TAU] += (c1[TAU] - c0[TAU]) * dampFactor;
+  }
+}
+
 // Occupancy: on the mixed path the flux and update kernels are capped at
 // 64 registers per thread (4 blocks of 256 per SM), measured faster than
 // their natural 70+; the FP64 versions would spill, so they are not capped.
@@ -1247,7 +1317,7 @@ __global__ void __launch_bounds__(256, kMix<R> ? 4 : 1) k_update(DevParams P, De
       // A middle substep (RK3's second) keeps the increment since the step
       // start current for the last one: d_k = d_(k-1) + (U_k - U_(k-1)).
       const R rk = to_r<R>(RK);
-      const bool whole = P.include_viscosity || P.rot_flag;
+      const bool whole = P.include_viscosity || P.rot_flag || P.cool_damp;
 #pragma unroll
       for (int q = 0; q < NQ; ++q) {
         double u = S.cons[q * N + c];
@@ -1261,9 +1331,11 @@ __global__ void __launch_bounds__(256, kMix<R> ? 4 : 1) k_update(DevParams P, De
         }
         U[q] = u + from_r<R>(d);
       }
-      if (P.include_viscosity || P.rot_flag) {
+      if (P.include_viscosity || P.rot_flag || P.cool_damp) {
         double dV = (.5 * (xp[0] + xm[0])) * (xp[0] - xm[0]) * get_dp(xp[1], xm[1], Pmax) * (xp[2] - xm[2]);
         dVdt = dV * dt;
+        if constexpr (!Phys::GR)
+          if (P.cool_damp) cool_damp_src<Phys, R, NQ>(P, S.planets, pr, U, xp, xm, dV, dt);
       }
     } else {
       double dV = (.5 * (xp[0] + xm[0])) * (xp[0] - xm[0]) * get_dp(xp[1], xm[1], Pmax) * (xp[2] - xm[2]);
@@ -1271,6 +1343,7 @@ __global__ void __launch_bounds__(256, kMix<R> ? 4 : 1) k_update(DevParams P, De
       if constexpr (Phys::GR) {   // grmhd.c:339 (metric and frame sources; no planets)
         Phys::source_x(P, pr, U, xp, xm, dVdt);
       } else {
+        if (P.cool_damp) cool_damp_src<Phys, R, NQ>(P, S.planets, pr, U, xp, xm, dV, dt);
         double dph = get_dp(xp[1], xm[1], Pmax);
         double rc = S.ring_rc[jk];
         Phys::template source<double>(P, pr, U, dVdt, (R)(.5 * (xp[0] + xm[0])), (R)S.ring_r23[jk], (R)rc,
@@ -1311,7 +1384,7 @@ __global__ void __launch_bounds__(256, kMix<R> ? 4 : 1) k_update(DevParams P, De
       // the viscous and rotating-frame sources go to U in FP64 after the R
       // sum: the increment kept for the second substep is then the whole
       // change of this substep
-      if ((first || mid) && (P.include_viscosity || P.rot_flag)) {
+      if ((first || mid) && (P.include_viscosity || P.rot_flag || P.cool_damp)) {
 #pragma unroll
         for (int q = 0; q < NQ; ++q) {
           const R dold = first ? (R)0 : S.RKdU[q * N + c];

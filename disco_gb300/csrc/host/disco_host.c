@@ -160,6 +160,11 @@ int disco_params_read(const char *path, disco_params *p)
    RI("Sink_Type", sinkType); RI("Nozzle_Type", nozzleType); RI("Cool_Type", coolType);
    RI("DampInner_Type", dampInnerType); RI("DampOuter_Type", dampOuterType);
    RI("DampUpper_Type", dampUpperType); RI("DampLower_Type", dampLowerType);
+   RD("Cool_Par1", coolPar1); RD("Cool_Par2", coolPar2); RD("Cool_Par3", coolPar3); RD("Cool_Par4", coolPar4);
+   RD("DampInner_Time", dampTimeInner); RD("DampInner_Len", dampLenInner);
+   RD("DampOuter_Time", dampTimeOuter); RD("DampOuter_Len", dampLenOuter);
+   RD("DampUpper_Time", dampTimeUpper); RD("DampUpper_Len", dampLenUpper);
+   RD("DampLower_Time", dampTimeLower); RD("DampLower_Len", dampLenLower);
    RD("Softening", grav_eps);
    RD("Sink_Par3", sinkPar3);
 #undef RI

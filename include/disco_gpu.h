@@ -119,6 +119,9 @@ typedef struct disco_params {
    double grav_eps;
    int read_errors;   /* number of keys absent (readpar.c: err count) */
    double sinkPar3;   /* Sink_Par3: the softening behind report.c's torque cut radii */
+   double coolPar1, coolPar2, coolPar3, coolPar4;            /* Cool_Par1..4 (sink.c:274) */
+   double dampTimeInner, dampLenInner, dampTimeOuter, dampLenOuter,
+          dampTimeUpper, dampLenUpper, dampTimeLower, dampLenLower;   /* Damp*_Time/_Len (sink.c:329) */
 } disco_params;
 
 /* One point mass: the fields of struct planet (paul.h:259-284) the hot path

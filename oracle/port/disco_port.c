@@ -1175,6 +1175,7 @@ static void B_faces_to_cells(int type)
 }
 
 static void initial(double *prim, const double *x);
+static void initial_raw(double *prim, const double *x);
 
 static void set_B_fields(void)
 {
@@ -1511,6 +1512,11 @@ static void calc_prim(void)
 }
 static void initial(double *prim, const double *x)
 {
+   initial_raw(prim, x);
+   if(D->par.RotFrame) prim[UPP] -= D->par.RotOmega;
+}
+static void initial_raw(double *prim, const double *x)
+{
    const disco_params *p = &D->par;
    if(D->mod.initial == DISCO_IC_VORTEX_GAUSS) {
       struct disco_ic_vortex_gauss V = {p->initPar1, p->initPar2, p->initPar3, p->initPar4,
@@ -1524,7 +1530,6 @@ static void initial(double *prim, const double *x)
       else if(D->mod.initial == DISCO_IC_DISK_PLANET) disco_ic_disk_planet_eval(&Dk, prim, x, D->nc, D->nq);
       else disco_ic_disk_cbd_eval(&Dk, prim, x, D->nc, D->nq);
    }
-   if(p->RotFrame) prim[UPP] -= p->RotOmega;
 }
 /* Boundary/fixed.c:11-46 (r ghosts) and fixed3d.c via set_cell_init. */
 /* set_cells_copy_distant (boundary_functions.c:90-158): ring c takes the
@@ -1686,6 +1691,66 @@ static void omega_src(const double *prim, double *cons, const double *xp, const 
    cons[SZZ] += rho*f2*dVdt;
    cons[TAU] += rho*vf*dVdt;
 }
+/* cooling (sink.c:274-326) and damping (sink.c:329-427), the first two
+ * terms add_source applies (misc.c:579-580). */
+static void planetary_force_m1(const disco_planet *pl, double r, double phi, double z,
+                               double *fr, double *fp, double *fz);
+static void initial_raw(double *prim, const double *x);
+
+static double orbital_rate(const double *x)
+{
+   double gx = x[0]*cos(x[1]), gy = x[0]*sin(x[1]), omtot = 0.0;
+   for(int p = 0; p < D->Npl; p++) {
+      double px = D->pl[p].r*cos(D->pl[p].phi), py = D->pl[p].r*sin(D->pl[p].phi);
+      double dx = gx - px, dy = gy - py, mag = sqrt(dx*dx + dy*dy), fr, fp, fz;
+      planetary_force_m1(&D->pl[p], x[0], x[1], x[2], &fr, &fp, &fz);
+      omtot += sqrt(fr*fr + fp*fp + fz*fz)/mag;
+   }
+   return sqrt(omtot);
+}
+
+static void cooling(const double *prim, double *cons, const double *xp, const double *xm, double dV, double dt)
+{
+   int type = D->par.coolType;
+   if(type != 1 && type != 2) return;
+   double x[3];
+   centroid_arr(xp, xm, x);
+   double gm1 = D->gam - 1.0;
+   double enTarget = get_cs2(x)/(D->gam*gm1), enCurrent = prim[PPP]/(prim[RHO]*gm1);
+   if(type == 2 || enCurrent > enTarget) {
+      double Tm1 = expm1(-dt*orbital_rate(x)/D->par.coolPar1);
+      cons[TAU] += prim[RHO]*dV*(enCurrent - enTarget)*Tm1;
+   }
+}
+
+static void damping(const double *prim, double *cons, const double *xp, const double *xm, double dV, double dt)
+{
+   const disco_params *p = &D->par;
+   int t[4] = {p->dampInnerType, p->dampOuterType, p->dampUpperType, p->dampLowerType};
+   if(t[0] + t[1] + t[2] + t[3] <= 0) return;
+   double x[3];
+   centroid_arr(xp, xm, x);
+   /* the last active side's factor is the one applied (ratetot, which the
+    * damping times enter, is unused in the reference) */
+   double f = 0.0, th;
+   if(t[0] > 0) { th = (x[0] - p->rmin)/p->dampLenInner; f = th > 1.0 ? 0.0 : 1.0 - pow(1.0 - pow(th, 2.0), 2.0); }
+   if(t[1] > 0) { th = (p->rmax - x[0])/p->dampLenOuter; f = th > 1.0 ? 0.0 : pow(1.0 - pow(th, 2.0), 2.0); }
+   if(D->Nz > 1) {
+      if(t[2] > 0) { th = (p->zmax - x[2])/p->dampLenUpper; f = th > 1.0 ? 0.0 : pow(1.0 - pow(th, 2.0), 2.0); }
+      if(t[3] > 0) { th = (p->zmax - x[2])/p->dampLenLower; f = th > 1.0 ? 0.0 : 1.0 - pow(1.0 - pow(th, 2.0), 2.0); }
+   }
+   f = expm1(-dt*f);
+   double p0[MAXQ], c0[MAXQ], c1[MAXQ];
+   initial_raw(p0, x);
+   prim2cons(p0, c0, x, dV);
+   prim2cons(prim, c1, x, dV);
+   cons[DDD] += (c1[DDD] - c0[DDD])*f;
+   cons[SRR] += (c1[SRR] - c0[SRR])*f;
+   cons[LLL] += (c1[LLL] - c0[LLL])*f;
+   cons[SZZ] += (c1[SZZ] - c0[SZZ])*f;
+   cons[TAU] += (c1[TAU] - c0[TAU])*f;
+}
+
 static void add_source(double dt)
 {
    for(int k = D->NgZa; k < D->Nz - D->NgZb; k++) for(int j = D->NgRa; j < D->Nr - D->NgRb; j++) {
@@ -1695,6 +1760,8 @@ static void add_source(double dt)
          double phip = c->piph, phim = c->piph - c->dphi;
          double xp[3] = {D->rj[j], phip, D->zk[k]}, xm[3] = {D->rj[j - 1], phim, D->zk[k - 1]};
          double dV = get_dV(xp, xm);
+         cooling(c->prim, c->cons, xp, xm, dV, dt);
+         damping(c->prim, c->cons, xp, xm, dV, dt);
          if(D->mhd) m_source(c->prim, c->cons, xp, xm, dV*dt);
          else e_source(c->prim, c->cons, xp, xm, dV*dt);
          for(int p = 0; p < D->Npl; p++) planet_src(&D->pl[p], c->prim, c->cons, xp, xm, dV*dt);
@@ -1791,6 +1858,7 @@ port_domain *disco_port_create(const disco_host_domain *h)
    disco_bc_op bops[DISCO_BC_MAX_OPS];
    if(disco_bc_plugin_ops(h->mod.boundary, bops) < 0) { free(d); return NULL; }
    if(h->par.Timestep != 0 && h->par.Timestep != 3) { free(d); return NULL; }
+   if(h->par.sinkType || h->par.nozzleType) { free(d); return NULL; }
    if(h->mod.hydro == DISCO_HYDRO_GRMHD || (d->mhd && h->mod.boundary > DISCO_BC_FIXED3D) ||
       (h->mod.analysis == DISCO_DIAG_MHDMRI && !d->mhd) || h->mod.analysis > DISCO_DIAG_MHDMRI) {
       free(d); return NULL;

@@ -63,6 +63,15 @@ CASES = {
     "cfg1_rk3": ("configs/cfg1_vortex", {"Num_R": 24, "Timestep": 3}, 10),
     "cfg2_rk3": ("configs/cfg2_mhd_disk", {"Num_R": 12, "Num_Z": 6, "Timestep": 3}, 5),
     "cfg3_rk3": ("configs/cfg3_planet_disk", {"Num_R": 24, "Timestep": 3}, 10),
+    # the planet disk with beta cooling relaxing its energy to the
+    # sound-speed profile and inner / outer damping towards the initial state
+    # (sink.c:274-427); locally isothermal as the disks here are (cooling
+    # then acts on the conserved energy), the adiabatic disk goes non-finite
+    # within six steps even without these terms
+    "cfg3_cooldamp": ("configs/cfg3_planet_disk",
+                      {"Num_R": 24, "Cool_Type": 2, "Cool_Par1": 0.5,
+                       "DampInner_Type": 2, "DampInner_Time": 1.0, "DampInner_Len": 0.3,
+                       "DampOuter_Type": 1, "DampOuter_Time": 2.0, "DampOuter_Len": 0.5}, 10),
     # GRMHD thin disk around a Schwarzschild black hole (Kerr-Schild
     # cylindrical metric, HLL, cell-centred B) at 12 x 4 rings
     "cfg4_n12": ("configs/cfg4_grmhd_disk", {"Num_R": 12, "Num_Z": 4}, 5),

@@ -76,7 +76,7 @@ def _mixed_errors(a, b, g, host):
 # different minmod branches in a few cells at that resolution): their ring
 # means of density and pressure, ghost rings included, sit at 2.9e-6 and
 # 3.2e-6 after ten steps.
-DIAG_MIXED_BOUND = {"cfg3_n24": 4e-6, "cfg3_outflow": 4e-6, "cfg3_rk3": 4e-6,
+DIAG_MIXED_BOUND = {"cfg3_n24": 4e-6, "cfg3_outflow": 4e-6, "cfg3_rk3": 4e-6, "cfg3_cooldamp": 4e-6,
                     # the MHD disk's RK3 run, whose dt collapses after one step
                     # (see the state's bound): its ring mean of Omega sits at 7.8e-6
                     "cfg2_rk3": 1.5e-5}

@@ -17,7 +17,7 @@ CASES = {"cfg1_n24": "configs/cfg1_vortex", "cfg2_n12": "configs/cfg2_mhd_disk",
          "cfg1_rotframe": "configs/cfg1_vortex",
          "cfg3_n24": "configs/cfg3_planet_disk", "cfg5_n16": "configs/cfg5_cbd_mhd",
          "cfg1_rk3": "configs/cfg1_vortex", "cfg2_rk3": "configs/cfg2_mhd_disk",
-         "cfg3_rk3": "configs/cfg3_planet_disk",
+         "cfg3_rk3": "configs/cfg3_planet_disk", "cfg3_cooldamp": "configs/cfg3_planet_disk",
          "cfg4_n12": "configs/cfg4_grmhd_disk",
          "cfg4_diag": "configs/cfg4_grmhd_disk",
          "cfg1_zerograd": "configs/cfg1_vortex_zerograd",
@@ -133,7 +133,8 @@ def test_mixed_precision_error(name):
 # minmod branches in a few cells (the error falls to 9e-7 at 96 rings and
 # 3e-7 at 256, with or without the planet or viscosity); the 1e-6 bar is
 # checked at batch-instance resolution by test_mixed_precision_planet_disk.
-MIXED_BOUND = {"cfg3_n24": 3e-6, "cfg3_outflow": 3e-6, "cfg3_rk3": 3e-6, "cfg2_rk3": 3e-6}
+MIXED_BOUND = {"cfg3_n24": 3e-6, "cfg3_outflow": 3e-6, "cfg3_rk3": 3e-6, "cfg2_rk3": 3e-6,
+               "cfg3_cooldamp": 3e-6}
 # The reference's RK3 run of the MHD disk is not smooth: after its first
 # step the CFL dt falls 2000-fold (8.9e-1 to 4.2e-4), both paths alike.
 # In it the mixed path's mass and momentum stay at 3e-8 while the field's
