@@ -656,8 +656,14 @@ struct Instance : InstanceBase {
         if (C.ev_cid && !first) LAUNCH("ct_edge_flag", (k_set_flag<<<1, 1, 0, st>>>(C.ev_ok, 1)));
       }
     }
-    LAUNCH("update", (k_update<Phys, R, NQ><<<blocks(N), 256, 0, st>>>(P, S, RK, fac, first + 2 * mid,
-                                                                      ct ? 0 : 1)));
+    {
+      const int c2p = ct ? 0 : 1;
+      const dim3 g((unsigned)blocks(N));
+      if (P.cool_damp && mid) LAUNCH("update", (k_update<Phys, R, NQ, true, true><<<g, 256, 0, st>>>(P, S, RK, fac, first, c2p)));
+      else if (P.cool_damp)   LAUNCH("update", (k_update<Phys, R, NQ, true, false><<<g, 256, 0, st>>>(P, S, RK, fac, first, c2p)));
+      else if (mid)           LAUNCH("update", (k_update<Phys, R, NQ, false, true><<<g, 256, 0, st>>>(P, S, RK, fac, first, c2p)));
+      else                    LAUNCH("update", (k_update<Phys, R, NQ, false, false><<<g, 256, 0, st>>>(P, S, RK, fac, first, c2p)));
+    }
     if (first) {
       parity ^= 1;
       set_piph(parity);

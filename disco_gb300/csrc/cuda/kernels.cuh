@@ -1189,10 +1189,13 @@ __global__ void __launch_bounds__(256, kMix<R> ? 4 : 1) k_flux_trans(DevParams P
 // adjust_RK_cons (misc.c:226), flux scatter (riemann.c:314-317) as a gather in
 // the reference's order, add_source (misc.c:550), move_cells/clean_pi/calc_dp
 // (misc.c:266, :8, :281), calc_prim (misc.c:300).
-template <typename Phys, typename R, int NQ>
-__global__ void __launch_bounds__(256, kMix<R> ? 4 : 1) k_update(DevParams P, DevState<R> S, double RK, double fac, int stage, int do_c2p) {
-  // stage: 1 the first substep, 2 a middle substep (RK3's second), 0 the last
-  const int first = stage == 1, mid = stage == 2;
+// Variants kept out of the common instantiation, which runs at the mixed
+// path's 64-register cap with every component's loads in flight: CD with
+// cooling / damping, MID for a middle substep (RK3's second), whose store of
+// the running increment would otherwise sit in the component loop.
+template <typename Phys, typename R, int NQ, bool CD = false, bool MID = false>
+__global__ void __launch_bounds__(256, kMix<R> ? 4 : 1) k_update(DevParams P, DevState<R> S, double RK, double fac, int first, int do_c2p) {
+  constexpr bool mid = MID;
   int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= S.N) return;
   const int N = S.N;
@@ -1317,7 +1320,7 @@ __global__ void __launch_bounds__(256, kMix<R> ? 4 : 1) k_update(DevParams P, De
       // A middle substep (RK3's second) keeps the increment since the step
       // start current for the last one: d_k = d_(k-1) + (U_k - U_(k-1)).
       const R rk = to_r<R>(RK);
-      const bool whole = P.include_viscosity || P.rot_flag || P.cool_damp;
+      const bool whole = P.include_viscosity || P.rot_flag || CD;
 #pragma unroll
       for (int q = 0; q < NQ; ++q) {
         double u = S.cons[q * N + c];
@@ -1327,15 +1330,17 @@ __global__ void __launch_bounds__(256, kMix<R> ? 4 : 1) k_update(DevParams P, De
         } else {
           const R dold = S.RKdU[q * N + c];
           d = fma(-rk, dold, d);
-          if (mid && !whole) S.RKdU[q * N + c] = dold + d;
+          if constexpr (MID) {
+            if (!whole) S.RKdU[q * N + c] = dold + d;
+          }
         }
         U[q] = u + from_r<R>(d);
       }
-      if (P.include_viscosity || P.rot_flag || P.cool_damp) {
+      if (P.include_viscosity || P.rot_flag || CD) {
         double dV = (.5 * (xp[0] + xm[0])) * (xp[0] - xm[0]) * get_dp(xp[1], xm[1], Pmax) * (xp[2] - xm[2]);
         dVdt = dV * dt;
         if constexpr (!Phys::GR)
-          if (P.cool_damp) cool_damp_src<Phys, R, NQ>(P, S.planets, pr, U, xp, xm, dV, dt);
+          if constexpr (CD) cool_damp_src<Phys, R, NQ>(P, S.planets, pr, U, xp, xm, dV, dt);
       }
     } else {
       double dV = (.5 * (xp[0] + xm[0])) * (xp[0] - xm[0]) * get_dp(xp[1], xm[1], Pmax) * (xp[2] - xm[2]);
@@ -1343,7 +1348,7 @@ __global__ void __launch_bounds__(256, kMix<R> ? 4 : 1) k_update(DevParams P, De
       if constexpr (Phys::GR) {   // grmhd.c:339 (metric and frame sources; no planets)
         Phys::source_x(P, pr, U, xp, xm, dVdt);
       } else {
-        if (P.cool_damp) cool_damp_src<Phys, R, NQ>(P, S.planets, pr, U, xp, xm, dV, dt);
+        if constexpr (CD) cool_damp_src<Phys, R, NQ>(P, S.planets, pr, U, xp, xm, dV, dt);
         double dph = get_dp(xp[1], xm[1], Pmax);
         double rc = S.ring_rc[jk];
         Phys::template source<double>(P, pr, U, dVdt, (R)(.5 * (xp[0] + xm[0])), (R)S.ring_r23[jk], (R)rc,
@@ -1384,7 +1389,7 @@ __global__ void __launch_bounds__(256, kMix<R> ? 4 : 1) k_update(DevParams P, De
       // the viscous and rotating-frame sources go to U in FP64 after the R
       // sum: the increment kept for the second substep is then the whole
       // change of this substep
-      if ((first || mid) && (P.include_viscosity || P.rot_flag || P.cool_damp)) {
+      if ((first || mid) && (P.include_viscosity || P.rot_flag || CD)) {
 #pragma unroll
         for (int q = 0; q < NQ; ++q) {
           const R dold = first ? (R)0 : S.RKdU[q * N + c];
