@@ -153,3 +153,16 @@ def test_unbuilt_plugins_fail_loudly(tmp_path, key, name):
     dg = _dg()
     with pytest.raises(dg.DiscoError, match=f"{key}={name} not built"):
         dg.read_modules(_mk(tmp_path, **{key: name}))
+
+
+def test_cooling_damping_keys_read(tmp_path):
+    """Cool_* and Damp*_* keys (readpar.c:155-174) land in disco_params."""
+    dg = _dg()
+    src = open(os.path.join(ROOT, "configs/cfg3_planet_disk/in.par")).read()
+    extra = ("\nCool_Type 2\nCool_Par1 0.5\nDampInner_Type 2\nDampInner_Time 1.0\nDampInner_Len 0.3\n"
+             "DampOuter_Type 1\nDampOuter_Time 2.0\nDampOuter_Len 0.5\nTimestep 3\n")
+    p = dg.read_params(write_par(src + extra))
+    assert (p.coolType, p.coolPar1) == (2, 0.5)
+    assert (p.dampInnerType, p.dampTimeInner, p.dampLenInner) == (2, 1.0, 0.3)
+    assert (p.dampOuterType, p.dampTimeOuter, p.dampLenOuter) == (1, 2.0, 0.5)
+    assert p.Timestep == 3
