@@ -159,8 +159,10 @@ def test_cooling_damping_keys_read(tmp_path):
     """Cool_* and Damp*_* keys (readpar.c:155-174) land in disco_params."""
     dg = _dg()
     src = open(os.path.join(ROOT, "configs/cfg3_planet_disk/in.par")).read()
+    import re
+    src = re.sub(r"(?m)^Timestep\s.*$", "Timestep 3", src)   # readvar takes a key's first line
     extra = ("\nCool_Type 2\nCool_Par1 0.5\nDampInner_Type 2\nDampInner_Time 1.0\nDampInner_Len 0.3\n"
-             "DampOuter_Type 1\nDampOuter_Time 2.0\nDampOuter_Len 0.5\nTimestep 3\n")
+             "DampOuter_Type 1\nDampOuter_Time 2.0\nDampOuter_Len 0.5\n")
     p = dg.read_params(write_par(src + extra))
     assert (p.coolType, p.coolPar1) == (2, 0.5)
     assert (p.dampInnerType, p.dampTimeInner, p.dampLenInner) == (2, 1.0, 0.3)
