@@ -37,7 +37,11 @@ WORKLOADS = {
                            "isothermal c_s=0.05 v_K, beta=400 vertical field",
                    # bounded CPU samples: same physics at reduced resolution
                    "cpu_sample": {"Num_R": 64, "Num_Z": 16},
-                   "ref_sample": {"Num_R": 32, "Num_Z": 8}},
+                   "ref_sample": {"Num_R": 32, "Num_Z": 8},
+                   # reference arm: tiles of 64 rings x 2 layers of the full
+                   # grid (Nr, Nz, r range, z range), one per host core
+                   "ref_tiles": {"grid": (256, 64, 1.0, 4.0, -0.5, 0.5), "tile": (64, 2)},
+                   "cells_full": 22004544},
     # the circumbinary MHD disk at full size: 134 M cells (about 136 GB on the
     # mixed path, 228 GB on the FP64 path, measured one after the other)
     "cbd_large": {"dir": "configs/cfg5_cbd_mhd",
@@ -81,17 +85,39 @@ DEFAULT_WORKLOAD = "mhd_disk3d"
 L2_BYTES = 126 * 1024 * 1024
 
 
-def _traffic_table() -> dict:
-    """DRAM bytes per launch at full size from the committed ncu summary
-    (lines `traffic <kernel> <bytes>` in profiles/*_dram_per_launch.md)."""
-    out = {}
+# profile entry (one per launch site) -> kernel function
+KERNEL_FUNCTION = {"flux_r": "flux_trans", "flux_z": "flux_trans",
+                   "plm_slopes_r": "plm_slopes", "plm_slopes_z": "plm_slopes",
+                   "plm_trans_r": "plm_trans", "plm_trans_z": "plm_trans",
+                   "faces_r": "faces", "faces_z": "faces", "dt_finalize": "mindt"}
+# kernel function -> its symbol in disco_gb300/csrc/cuda
+KERNEL_SYMBOL = {"flux_trans": "k_flux_trans", "plm_slopes": "k_plm_slopes", "plm_trans": "k_plm_trans",
+                 "faces": "k_faces", "update": "k_update", "flux_phi": "k_flux_phi", "plm_phi": "k_plm_phi",
+                 "ct_gather": "k_ct_gather", "ct_avg": "k_ct_avg", "ct_bflux": "k_ct_bflux",
+                 "ct_edge": "k_ct_edge", "ct_edge_replay": "k_ct_edge_replay", "ct_flip": "k_ct_flip",
+                 "ct_b2c_c2p": "k_ct_b2c_c2p", "mindt": "k_mindt", "diag": "k_diag",
+                 "boundary": "k_boundary", "anchor": "k_anchor", "wcell": "k_wcell",
+                 "wcell_ring": "k_wcell_ring", "wcell_avg": "k_wcell_avg", "after_first": "k_after_first",
+                 "ct_edge_flag": "k_set_flag"}
+
+
+def _traffic(workload: str, func: str, N: int, nf: dict):
+    """DRAM bytes per launch of kernel function `func` from a committed ncu
+    summary: lines `traffic_per_unit <func> <bytes per cell> <bytes per
+    face>` of profiles/<func>_<case>_dram.md, captured on a small case and
+    scaled by the units one full launch processes (the kernel's traffic is
+    proportional to its cells and faces).  Returns (bytes, source)."""
     import glob
-    for path in glob.glob(os.path.join(ROOT, "profiles", "*_dram_per_launch.md")):
+    for path in sorted(glob.glob(os.path.join(ROOT, "profiles", f"{func}_*_dram.md"))):
         for ln in open(path):
             parts = ln.split()
-            if len(parts) == 3 and parts[0] == "traffic":
-                out[(os.path.basename(path).split("_dram")[0], parts[1])] = float(parts[2])
-    return out
+            if len(parts) == 4 and parts[0] == "traffic_per_unit" and parts[1] == func:
+                per_cell, per_face = float(parts[2]), float(parts[3])
+                nfa = (nf["r"] + nf["z"]) / 2 if func in ("flux_trans", "plm_slopes", "plm_trans", "faces") else 0
+                return (per_cell * N + per_face * nfa,
+                        f"ncu dram__bytes_read.sum + dram__bytes_write.sum on a small case, per cell "
+                        f"and face, scaled to one full launch ({os.path.relpath(path, ROOT)})")
+    return None, None
 
 
 def _peaks():
@@ -167,8 +193,7 @@ def kernel_bytes(name: str, N: int, nf: dict, nq: int, sw: int, ct: bool) -> flo
     array element the kernel must read or write, moved once (neighbour and
     face re-reads are assumed served on chip).  N = cells incl. ghosts,
     nf[d] = faces of dimension d ("r", "z"), sw = bytes of a reconstruction
-    value (4 mixed, 8 FP64), index = 4 bytes, positions/conserved = 8 bytes.
-    The same table is written out, per unit, in the design doc."""
+    value (4 mixed, 8 FP64), index = 4 bytes, positions/conserved = 8 bytes."""
     ix, f8 = 4, 8
     nfa = nf["r"] + nf["z"]
     c = 1 if ct else 0
@@ -428,18 +453,14 @@ def measure_ours(args, wl, rank):
     h = saved["host"]
     real = h.real_mask()
     sys.path.insert(0, os.path.join(ROOT, "tests"))
-    from helpers import cell_radius, grouped_rel_l1
+    from helpers import cell_radius, component_norms, grouped_rel_l1
     r = cell_radius(h.Np, h.r_jph, h.Nr, h.Nz)[real]
     num_c = 8 if h.num_q >= 8 else 5
     c1, c0 = saved[1]["cons"], saved[0]["cons"]
     grp = grouped_rel_l1(c1[:, real], c0[:, real], r, num_c)
-    percomp = {}
-    for q in range(c0.shape[0]):
-        den = np.abs(c0[q, real]).sum()
-        if den > 0:
-            percomp[q] = float(np.abs(c1[q, real] - c0[q, real]).sum() / den)
+    comp = component_norms(c1[:, real], c0[:, real])
     res["l1_err"] = {"max_over_quantities": max(grp.values()), "per_quantity": grp,
-                     "per_component": percomp}
+                     "per_component": comp["l1"], "linf_per_component": comp["linf"]}
     return res
 
 
@@ -453,10 +474,18 @@ def _sample_domain(wl, key):
 
 
 def cpu_baseline(wl, target_s=12.0):
-    """The oracle (plain-C restatement, bit-exact with the reference build),
-    single thread on the host, on a bounded sample of the workload: the same
-    configuration at the resolution in wl["cpu_sample"], for as many steps as
-    fit in about target_s seconds."""
+    """The reference on one host core, on a bounded sample of the workload:
+    the unmodified reference binary on one tile of the full grid (3 steps
+    after 1 warm-up) where it was built; else the oracle (plain-C
+    restatement, bit-exact with the reference build), single thread, on the
+    same configuration at the resolution in wl["cpu_sample"], for as many
+    steps as fit in about target_s seconds."""
+    exe = os.path.join(ROOT, "oracle", "_ref", os.path.basename(wl["dir"]), "disco_ref")
+    if wl.get("ref_tiles") is not None and os.path.exists(exe):
+        class _A:
+            steps, warmup = 3, 1
+        v, cells, sec, sample, nt = run_reference_binary(_A, wl, exe, 1)
+        return {"value": v, "unit": "zone-updates/s", "cores": 1, "kind": "reference", "sample": sample}
     from oracle.port import PortDomain
     h = _sample_domain(wl, "cpu_sample")
     o = PortDomain(h)
@@ -484,11 +513,97 @@ def _ref_worker(wl_name, warmup, steps, q):
     q.put((o.num_real, time.perf_counter() - t0))
 
 
+def _ref_tiles(wl, ncores):
+    """Tiles of the workload's full grid for the reference arm: (in.par
+    overrides, description) per host core.  A tile is a block of whole rings
+    of the full-resolution grid -- its radial and vertical bounds are the
+    full grid's ring edges, so every ring keeps its Np and every cell its
+    size and initial state -- bounded by the configured boundary plugin at
+    the tile edges, as the reference's own domain decomposition
+    (mpisetup.c, gridsetup.c) cuts the grid, without the halo exchange."""
+    t = wl.get("ref_tiles")
+    if t is None:
+        return None
+    Nr, Nz, rmin, rmax, zmin, zmax = t["grid"]
+    tr, tz = t["tile"]
+    na, nb = Nr // tr, Nz // tz
+    dr, dz = (rmax - rmin) / Nr, (zmax - zmin) / Nz
+    nslab = max(1, (ncores + na - 1) // na)     # vertical positions sampled
+    step = max(1, nb // nslab)
+    out = []
+    for i in range(ncores):
+        a = i % na
+        b = ((i // na) * step + step // 2) % nb
+        ov = {"Num_R": tr, "R_Min": rmin + a * tr * dr, "R_Max": rmin + (a + 1) * tr * dr,
+              "Num_Z": tz, "Z_Min": zmin + b * tz * dz, "Z_Max": zmin + (b + 1) * tz * dz}
+        out.append((ov, f"rings {a * tr}..{(a + 1) * tr - 1}, layers {b * tz}..{(b + 1) * tz - 1}"))
+    return out
+
+
+def run_reference_binary(args, wl, exe, ncores):
+    """The unmodified reference (built from its own sources by
+    oracle/ref/Makefile) on tiles of the full grid, one process per host
+    core, all running at once: each process does W untimed warm-up steps and
+    K timed steps of its tile (getmindt + timestep, the reference's main
+    loop), timed by the harness with clock_gettime."""
+    import tempfile
+    sys.path.insert(0, os.path.join(ROOT, "tests", "golden"))
+    from make_golden import patch_par
+    base = open(os.path.join(ROOT, wl["dir"], "in.par")).read()
+    tiles = _ref_tiles(wl, ncores)
+    procs = []
+    tmp = tempfile.mkdtemp(prefix="disco_refarm_")
+    for i, (ov, _) in enumerate(tiles):
+        td = os.path.join(tmp, f"t{i}")
+        os.makedirs(td)
+        with open(os.path.join(td, "in.par"), "w") as f:
+            f.write(patch_par(base, ov))
+        procs.append(subprocess.Popen([exe, "time", str(args.steps), str(args.warmup)], cwd=td,
+                                      stdout=subprocess.DEVNULL, stderr=subprocess.PIPE, text=True))
+    res = []
+    for p in procs:
+        _, err = p.communicate()
+        if p.returncode != 0:
+            raise RuntimeError(f"reference tile run failed ({p.returncode}): {err[-400:]}")
+        line = [ln for ln in err.splitlines() if ln.startswith("{")][-1]
+        res.append(json.loads(line))
+    cells = sum(r["cells"] for r in res)
+    sec = max(r["seconds"] for r in res)
+    v = cells * args.steps / sec
+    t = wl["ref_tiles"]
+    sample = (f"{len(tiles)} tiles of the full {t['grid'][0]}x{t['grid'][1]} grid at full resolution "
+              f"({t['tile'][0]} rings x {t['tile'][1]} layers each, {cells} cells in all, "
+              f"{cells / wl['cells_full']:.3f} of the grid), one process per host core, "
+              f"{args.steps} RK2 steps after {args.warmup} warm-up; the unmodified reference built "
+              "from its own sources (oracle/ref/Makefile), serial build, clock_gettime around the step loop")
+    return v, cells, sec, sample, len(tiles)
+
+
 def run_reference(args, wl, rank, world):
-    """The reference algorithm on the host CPU: the C restatement (bit-exact
-    with the reference build) as independent replicas, one process per host
-    core, each on a bounded sample of the workload; aggregate zone-updates/s."""
+    """The reference's own CPU implementation of the path on the host cores:
+    the unmodified reference binary on tiles of the full grid (one process
+    per core) where it was built, else the C restatement (bit-exact with the
+    reference build) as independent replicas on a bounded sample."""
     if rank != 0:
+        return
+    ncores = max(1, min(os.cpu_count() or 1, 16))
+    exe = os.path.join(ROOT, "oracle", "_ref", os.path.basename(wl["dir"]), "disco_ref")
+    if wl.get("ref_tiles") is not None and not os.path.exists(exe):
+        from oracle.build_oracle import build_ref
+        build_ref(configs=[wl["dir"]])
+    if wl.get("ref_tiles") is not None and os.path.exists(exe):
+        v, cells, sec, sample, nt = run_reference_binary(args, wl, exe, ncores)
+        line = {"metric": "zone-updates/s", "value": v, "unit": "zone-updates/s", "n_gpus": args.gpus,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": sec * 1e3 / args.steps,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                "data": "synthetic", "impl": "reference",
+                "config": {"workload": wl["desc"], "cells_timed": cells, "tiles": nt,
+                           "same_grid": "tiles of the full-resolution grid"},
+                "cpu_baseline": {"value": v, "unit": "zone-updates/s", "cores": nt, "kind": "reference",
+                                 "sample": sample},
+                "e2e": {"value": v, "unit": "zone-updates/s", "h2d_bytes_per_step": 0,
+                        "d2h_bytes_per_step": 0}}
+        print(json.dumps(line), flush=True)
         return
     if wl.get("ref_sample") is None:
         print(json.dumps({"impl": "reference",
@@ -590,20 +705,22 @@ def main():
             nf["r"] = int((Np[:, :-1] + Np[:, 1:]).sum())
         if hd.Nz > 1:
             nf["z"] = int((Np[:-1, :] + Np[1:, :]).sum())
-    prof = sorted(res["profile"], key=lambda x: -x[2])
-    tot_prof = sum(p[2] for p in prof)
-    top = prof[0]
     ct = nq >= 8 and "precisions" not in wl   # the GRMHD workload has cell-centred B
-    top_bytes = kernel_bytes(top[0], N, nf, nq, sw, ct)
-    top_avg_s = top[2] / top[1] / 1e3
+    # per kernel FUNCTION: the r and z launches of one kernel (flux_r and
+    # flux_z are both k_flux_trans) count together
+    funcs = {}
+    for name, launches, ms_tot in res["profile"]:
+        f = KERNEL_FUNCTION.get(name, name)
+        e = funcs.setdefault(f, {"launches": 0, "ms": 0.0, "bytes": 0.0})
+        e["launches"] += launches
+        e["ms"] += ms_tot
+        e["bytes"] += kernel_bytes(name, N, nf, nq, sw, ct) * launches
+    tot_prof = sum(e["ms"] for e in funcs.values())
+    top_name, top = max(funcs.items(), key=lambda kv: kv[1]["ms"])
+    top_bytes = top["bytes"] / top["launches"]
+    top_avg_s = top["ms"] / top["launches"] / 1e3
     achieved = top_bytes / top_avg_s / 1e9
-    traffic = _traffic_table().get((args.workload, top[0]))
-    roof = {"bound": "hbm", "kernel": top[0], "achieved": achieved, "peak": hbm, "unit": "GB/s",
-            "frac": achieved / hbm, "peak_kind": peak_kind, "traffic": traffic,
-            "traffic_source": ("ncu dram__bytes_read.sum + dram__bytes_write.sum of one full-size "
-                               "launch, profiles/%s_dram_per_launch.md" % args.workload) if traffic else None,
-            "algorithmic_bytes_per_launch": top_bytes,
-            "share_of_step": top[2] / tot_prof}
+    traffic, traffic_src = _traffic(args.workload, top_name, N, nf)
     # fused-RK2 compulsory bytes per zone-update: NQ (6 s_W + 4 s_U) + 6 x 8
     # (the RK copy of the state is one s_W write and one s_W read: the mixed
     # path keeps the first substep's increment in R), plus 25 x 8 for the
@@ -611,6 +728,13 @@ def main():
     bz = nq * (6 * sw + 4 * 8) + 6 * 8 + (200 if ct else 0)
     whole = {"algorithmic_bytes_per_zone_update": bz, "achieved_GBps": bz * value / 1e9,
              "frac_of_hbm": bz * value / 1e9 / hbm}
+    roof = {"bound": "hbm", "kernel": KERNEL_SYMBOL.get(top_name, top_name), "achieved": achieved,
+            "peak": hbm, "unit": "GB/s", "frac": achieved / hbm, "peak_kind": peak_kind,
+            "traffic": traffic, "traffic_source": traffic_src,
+            "algorithmic_bytes_per_launch": top_bytes, "launches_per_step": top["launches"] / 3,
+            "share_of_step": top["ms"] / tot_prof,
+            "step": {"algorithmic_bytes_per_zone_update": bz, "achieved": whole["achieved_GBps"],
+                     "frac": whole["frac_of_hbm"]}}
     line = {
         "metric": "zone-updates/s", "value": value, "unit": "zone-updates/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
@@ -624,10 +748,9 @@ def main():
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "roofline": roof,
         "step_hbm": whole,
-        "kernels": {p[0]: {"ms_per_step": p[2] / 3,
-                           "GBps": (kernel_bytes(p[0], N, nf, nq, sw, ct) * p[1] / (p[2] / 1e3) / 1e9
-                                    if p[2] > 0 else None)}
-                    for p in prof},
+        "kernels": {KERNEL_SYMBOL.get(f, f): {"ms_per_step": e["ms"] / 3, "launches_per_step": e["launches"] / 3,
+                                              "GBps": e["bytes"] / (e["ms"] / 1e3) / 1e9 if e["ms"] > 0 else None}
+                    for f, e in sorted(funcs.items(), key=lambda kv: -kv[1]["ms"])},
         "e2e": res["e2e"],
         **({"report_reduction": res["report"]} if "report" in res else {}),
         "gpu_launches": int(res[ch]["launches"]),
@@ -639,8 +762,11 @@ def main():
     if "l1_err" in res:
         line["l1_err_vs_fp64"] = res["l1_err"]
         line["l1_err_definition"] = ("sum over interior cells of |U_chosen - U_fp64| / sum |U_fp64| per "
-                                     "physical quantity (mass, energy, momentum vector, B vector, passive), "
-                                     "after warmup+steps RK2 steps from the same initial state")
+                                     "physical quantity (mass, energy, momentum vector, B vector, passive; "
+                                     "vectors through the norm of the difference), per conserved component, "
+                                     "and max |U_chosen - U_fp64| / max |U_fp64| per component (Linf), "
+                                     "after warmup+steps RK2 steps from the same initial state, each path "
+                                     "with its own FP64 CFL dt")
     if world == 1 and not args.no_cpu_baseline:
         if wl.get("cpu_sample") is None:
             line["cpu_baseline"] = {"value": None, "unit": "zone-updates/s", "cores": 0, "kind": None,

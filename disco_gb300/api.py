@@ -133,6 +133,15 @@ SIGNATURES = {
                                     C.POINTER(C.c_int)]),
     "disco_gpu_debug_ct": (C.c_int, [_P, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double),
                                      C.POINTER(C.c_double), C.POINTER(C.c_double)]),
+    "disco_gpu_debug_faces": (C.c_int, [_P, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_long),
+                                        C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                        C.POINTER(C.c_int), C.POINTER(C.c_double), C.POINTER(C.c_double)]),
+    "disco_gpu_debug_grad": (C.c_int, [_P, C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                       C.POINTER(C.c_double)]),
+    "disco_gpu_debug_convert": (C.c_int, [C.POINTER(C.c_double), C.POINTER(C.c_float), C.c_long,
+                                          C.POINTER(C.c_float), C.POINTER(C.c_float),
+                                          C.POINTER(C.c_double), C.POINTER(C.c_double)]),
+    "disco_gpu_divb": (C.c_int, [_P, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     "disco_gpu_getmindt_noalloc": (C.c_int, [_P, C.POINTER(C.c_double)]),
     "disco_gpu_report": (C.c_int, [_P, C.POINTER(C.c_double), C.c_int]),
     "disco_gpu_diag_count": (C.c_int, [_P]),
@@ -290,6 +299,47 @@ class Domain:
                                              float(t_avg))
         _check(rc if rc < 0 else 0, "disco_gpu_diag_upload")
 
+    def faces(self, dim: int) -> dict:
+        """The device's sheared-face tables of dimension dim (1 = r, 2 = z):
+        fIndex [npair+1] and per face L, R (global cell ids), LRtype, phic
+        (cm[1]) and dA (disco_gpu_debug_faces)."""
+        npair, nface = C.c_int(), C.c_long()
+        _check(lib().disco_gpu_debug_faces(self._g, int(dim), C.byref(npair), C.byref(nface),
+                                           None, None, None, None, None, None), "disco_gpu_debug_faces")
+        out = {"fIndex": np.zeros(npair.value + 1, np.int32)}
+        for k in ("L", "R", "LRtype"):
+            out[k] = np.zeros(nface.value, np.int32)
+        for k in ("phic", "dA"):
+            out[k] = np.zeros(nface.value, np.float64)
+        if npair.value == 0:
+            return out
+        ip, dp = C.POINTER(C.c_int), C.POINTER(C.c_double)
+        _check(lib().disco_gpu_debug_faces(self._g, int(dim), C.byref(npair), C.byref(nface),
+                                           *(out[k].ctypes.data_as(ip) for k in ("fIndex", "L", "R", "LRtype")),
+                                           *(out[k].ctypes.data_as(dp) for k in ("phic", "dA"))),
+               "disco_gpu_debug_faces")
+        return out
+
+    def gradients(self) -> dict:
+        """plm_phi + plm_trans on the current state: gradp, gradr, gradz
+        [num_q, Ncell] (disco_gpu_debug_grad)."""
+        shp = (self.host.num_q, self.num_cells)
+        out = {k: np.zeros(shp) for k in ("gradp", "gradr", "gradz")}
+        dp = C.POINTER(C.c_double)
+        _check(lib().disco_gpu_debug_grad(self._g, *(out[k].ctypes.data_as(dp) for k in ("gradp", "gradr", "gradz"))),
+               "disco_gpu_debug_grad")
+        return out
+
+    def divb(self) -> tuple:
+        """(div, scale) per cell: net outward face flux of B and the sum of
+        the absolute face fluxes (disco_gpu_divb); scale < 0 marks cells
+        that are not evaluated."""
+        n = self.num_cells
+        div, sc = np.zeros(n), np.zeros(n)
+        dp = C.POINTER(C.c_double)
+        _check(lib().disco_gpu_divb(self._g, div.ctypes.data_as(dp), sc.ctypes.data_as(dp)), "disco_gpu_divb")
+        return div, sc
+
     def timestep(self, dt: float) -> None:
         _check(lib().disco_gpu_timestep(self._g, float(dt)), "disco_gpu_timestep")
 
@@ -373,6 +423,25 @@ class Domain:
             self.close()
         except Exception:
             pass
+
+
+def convert_check(x: np.ndarray, y: np.ndarray) -> dict:
+    """The mixed path's integer-pipe conversions beside the hardware's, on
+    the device: f_int / f_hw from the float64 array x, d_int / d_hw from the
+    float32 array y (same length)."""
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    y = np.ascontiguousarray(y, dtype=np.float32)
+    if x.shape != y.shape:
+        raise ValueError("convert_check: x and y must have the same length")
+    n = x.size
+    out = {"f_int": np.zeros(n, np.float32), "f_hw": np.zeros(n, np.float32),
+           "d_int": np.zeros(n, np.float64), "d_hw": np.zeros(n, np.float64)}
+    fp, dp = C.POINTER(C.c_float), C.POINTER(C.c_double)
+    _check(lib().disco_gpu_debug_convert(x.ctypes.data_as(dp), y.ctypes.data_as(fp), n,
+                                         out["f_int"].ctypes.data_as(fp), out["f_hw"].ctypes.data_as(fp),
+                                         out["d_int"].ctypes.data_as(dp), out["d_hw"].ctypes.data_as(dp)),
+           "disco_gpu_debug_convert")
+    return out
 
 
 class Batch:

@@ -306,18 +306,19 @@ __global__ void __launch_bounds__(kDiagBlock) k_diag(DevParams P, DevState<R> S,
   const double zc = .5 * (zp + zm);
   const double rdr = (.5 * (rp + rm)) * (rp - rm), dz = zp - zm;
   const double Om = kMix<R> ? S.ring_Om[jk] : 0.0;
-  // Each thread's share (a few cells) is summed in R: FP32 on the mixed
-  // path, whose cell volume is formed from the cell's own width, and FP64
-  // with the reference's get_dV otherwise; the tree across threads is FP64.
+  // Each cell's Q dV is formed in R (FP32 on the mixed path, whose cell
+  // volume comes from the cell's own width; FP64 with the reference's get_dV
+  // otherwise); every sum, each thread's share and the tree across threads,
+  // is FP64 on both paths.
   // the mixed path's torque (diag_euler, diag_disk2d) takes the ring
   // constants once; the other forms need each cell's centroid azimuth
   const bool ring_force = kMix<R> && (D == 0 || D == 1) && P.Npl > 1 && P.grav2D != 2;
   const bool need_phi = !ring_force && (D == 2 || D == 5 || ((D == 0 || D == 1) && P.Npl > 1));
   RingBody<R> rb;
   if (ring_force) rb = ring_body<R>(P, S.planets[1], rc, D == 1 ? 0.0 : zc);
-  R sum[ND + 1];
+  double sum[ND + 1];
 #pragma unroll
-  for (int q = 0; q <= ND; ++q) sum[q] = (R)0.0;
+  for (int q = 0; q <= ND; ++q) sum[q] = 0.0;
 #pragma unroll 4
   for (int i = threadIdx.x; i < Np; i += kDiagBlock) {
     const int c = off + i;
@@ -340,14 +341,14 @@ __global__ void __launch_bounds__(kDiagBlock) k_diag(DevParams P, DevState<R> S,
     R Q[ND];
     diag_cell<R, NQ, D>(P, S, c, Om, rc, phic, zc, Q, ring_force ? &rb : nullptr, piph, dphf);
 #pragma unroll
-    for (int q = 0; q < ND; ++q) sum[q] += Q[q] * dV;
-    sum[ND] += dV;
+    for (int q = 0; q < ND; ++q) sum[q] += from_r<R>(Q[q] * dV);
+    sum[ND] += from_r<R>(dV);
   }
   __shared__ double red[ND + 1][kDiagBlock / 32];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
 #pragma unroll
   for (int q = 0; q <= ND; ++q) {
-    double x = (double)sum[q];
+    double x = sum[q];
     for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
     if (lane == 0) red[q][wid] = x;
   }

@@ -189,6 +189,54 @@ int disco_gpu_debug_ct(disco_gpu* g, int stage, double* E, double* B, double* Ep
   if (!g || stage < 0 || stage > 4) { disco_set_error("bad argument"); return DISCO_E_ARG; }
   return g->impl->debug_ct(stage, E, B, Ephi, Phi);
 }
+int disco_gpu_debug_faces(disco_gpu* g, int dim, int* npair, long* nface, int* fIndex, int* L, int* R,
+                          int* LRtype, double* phic, double* dA) {
+  if (!g) { disco_set_error("null argument"); return DISCO_E_ARG; }
+  return g->impl->debug_faces(dim, npair, nface, fIndex, L, R, LRtype, phic, dA);
+}
+int disco_gpu_debug_grad(disco_gpu* g, double* gradp, double* gradr, double* gradz) {
+  if (!g) { disco_set_error("null argument"); return DISCO_E_ARG; }
+  return g->impl->debug_grad(gradp, gradr, gradz);
+}
+int disco_gpu_divb(disco_gpu* g, double* div, double* scale) {
+  if (!g) { disco_set_error("null argument"); return DISCO_E_ARG; }
+  return g->impl->divb(div, scale);
+}
+int disco_gpu_debug_convert(const double* in, const float* fin, long n, float* f_int, float* f_hw,
+                            double* d_int, double* d_hw) {
+  if (!in || !fin || n < 0 || !f_int || !f_hw || !d_int || !d_hw) {
+    disco_set_error("disco_gpu_debug_convert: bad argument");
+    return DISCO_E_ARG;
+  }
+  if (n == 0) return 0;
+  const size_t nb = (size_t)n;
+  double *din = nullptr, *dd_int = nullptr, *dd_hw = nullptr;
+  float *dfin = nullptr, *df_int = nullptr, *df_hw = nullptr;
+  int rc = 0;
+  cudaError_t e = cudaSuccess;
+  if ((e = cudaMalloc(&din, nb * 8)) == cudaSuccess && (e = cudaMalloc(&dd_int, nb * 8)) == cudaSuccess &&
+      (e = cudaMalloc(&dd_hw, nb * 8)) == cudaSuccess && (e = cudaMalloc(&dfin, nb * 4)) == cudaSuccess &&
+      (e = cudaMalloc(&df_int, nb * 4)) == cudaSuccess && (e = cudaMalloc(&df_hw, nb * 4)) == cudaSuccess &&
+      (e = cudaMemcpy(din, in, nb * 8, cudaMemcpyHostToDevice)) == cudaSuccess &&
+      (e = cudaMemcpy(dfin, fin, nb * 4, cudaMemcpyHostToDevice)) == cudaSuccess) {
+    const int grid = (int)std::min<long>((n + 255) / 256, 152L * 8);
+    disco::k_convert_check<<<grid, 256>>>(din, n, df_int, df_hw, dfin, dd_int, dd_hw);
+    ++g_launches;
+    if ((e = cudaGetLastError()) == cudaSuccess && (e = cudaDeviceSynchronize()) == cudaSuccess &&
+        (e = cudaMemcpy(f_int, df_int, nb * 4, cudaMemcpyDeviceToHost)) == cudaSuccess &&
+        (e = cudaMemcpy(f_hw, df_hw, nb * 4, cudaMemcpyDeviceToHost)) == cudaSuccess &&
+        (e = cudaMemcpy(d_int, dd_int, nb * 8, cudaMemcpyDeviceToHost)) == cudaSuccess)
+      e = cudaMemcpy(d_hw, dd_hw, nb * 8, cudaMemcpyDeviceToHost);
+  }
+  if (e != cudaSuccess) {
+    char b[160];
+    snprintf(b, sizeof b, "disco_gpu_debug_convert: CUDA %s", cudaGetErrorString(e));
+    disco_set_error(b);
+    rc = DISCO_E_CUDA;
+  }
+  cudaFree(din); cudaFree(dd_int); cudaFree(dd_hw); cudaFree(dfin); cudaFree(df_int); cudaFree(df_hw);
+  return rc;
+}
 int disco_gpu_getmindt_noalloc(disco_gpu* g, double* dt) {
   if (!g || !dt) { disco_set_error("null argument"); return DISCO_E_ARG; }
   return g->impl->getmindt_noalloc(dt);

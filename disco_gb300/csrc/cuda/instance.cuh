@@ -18,6 +18,7 @@
 #include "noalloc.cuh"
 #include "report.cuh"
 #include "diag.cuh"
+#include "checks.cuh"
 #include "../plugins/bc_plugins.h"
 
 using namespace disco;
@@ -50,6 +51,10 @@ struct InstanceBase {
   virtual int profile(int n, disco_kernel_time* out, int maxo, int* nout) = 0;
   virtual double time() = 0;
   virtual int debug_ct(int stage, double* E, double* B, double* Ephi, double* Phi) = 0;
+  virtual int debug_faces(int dim, int* npair_out, long* nface_out, int* fIndex, int* L, int* Rr,
+                          int* LRtype, double* phic, double* dA) = 0;
+  virtual int debug_grad(double* gp, double* gr, double* gz) = 0;
+  virtual int divb(double* div, double* scale) = 0;
   virtual int getmindt_noalloc(double* dt) = 0;
   virtual int report(double* out, int nout) = 0;
   virtual int diag(int op, double* Qrz, long long n, double* t_avg, const double* set, double set_t) = 0;
@@ -156,8 +161,10 @@ struct Instance : InstanceBase {
     S.piph_out = piph_buf[par ^ 1];
   }
 
+  int device = 0;   // the device current at create: the instance's memory and stream live there
   int create(const disco_host_domain* dom) {
     const disco_params& p = dom->par;
+    CK(cudaGetDevice(&device));
     CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
     Nr = dom->Nr; Nz = dom->Nz; nring = Nr * Nz;
     N = dom->Ncell;
@@ -919,6 +926,71 @@ struct Instance : InstanceBase {
     if (Phi) CK(cudaMemcpy(Phi, C.Phi, sizeof(double) * 5 * N, cudaMemcpyDeviceToHost));
     return 0;
   }
+  // Face tables of one dimension as the device holds them (test access).
+  int debug_faces(int dim, int* npair_out, long* nface_out, int* fIndex, int* L, int* Rr,
+                  int* LRtype, double* phic, double* dA) override {
+    if (dim != 1 && dim != 2) { disco_set_error("debug_faces: dim must be 1 or 2"); return DISCO_E_ARG; }
+    const int d = dim - 1;
+    CK(cudaStreamSynchronize(st));
+    if (npair_out) *npair_out = npair[d];
+    if (nface_out) *nface_out = npair[d] ? S.nf[d] : 0;
+    if (!npair[d]) return 0;
+    const size_t nf = (size_t)S.nf[d];
+    if (fIndex) CK(cudaMemcpy(fIndex, S.face_off[d], sizeof(int) * (npair[d] + 1), cudaMemcpyDeviceToHost));
+    if (L) CK(cudaMemcpy(L, S.fL[d], sizeof(int) * nf, cudaMemcpyDeviceToHost));
+    if (Rr) CK(cudaMemcpy(Rr, S.fR[d], sizeof(int) * nf, cudaMemcpyDeviceToHost));
+    if (LRtype) {
+      std::vector<signed char> t(nf);
+      CK(cudaMemcpy(t.data(), S.fLR[d], nf, cudaMemcpyDeviceToHost));
+      for (size_t f = 0; f < nf; ++f) LRtype[f] = t[f];
+    }
+    if (phic) CK(cudaMemcpy(phic, S.fphic[d], sizeof(double) * nf, cudaMemcpyDeviceToHost));
+    if (dA) {
+      std::vector<R> t(nf);
+      CK(cudaMemcpy(t.data(), S.fdA[d], sizeof(R) * nf, cudaMemcpyDeviceToHost));
+      for (size_t f = 0; f < nf; ++f) dA[f] = (double)t[f];
+    }
+    return 0;
+  }
+  // plm_phi and plm_trans (onestep.c:104-130) on the current state, then the
+  // gradients widened to FP64 (test access; the state is not changed).
+  int debug_grad(double* gp, double* gr, double* gz) override {
+    LAUNCH("plm_phi", (k_plm_phi<R, NQ><<<blocks(N), 256, 0, st>>>(P, S)));
+    launch_plm_trans();
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(st));
+    const size_t n = (size_t)NQ * N;
+    std::vector<R> t(n);
+    const R* src[3] = {S.gradp, S.gradr, S.gradz};
+    double* dst[3] = {gp, gr, gz};
+    for (int a = 0; a < 3; ++a) {
+      if (!dst[a]) continue;
+      CK(cudaMemcpy(t.data(), src[a], sizeof(R) * n, cudaMemcpyDeviceToHost));
+      for (size_t x = 0; x < n; ++x) dst[a][x] = (double)t[x];
+    }
+    return 0;
+  }
+  // Per-cell divergence of the face fluxes of B (constrained transport only).
+  int divb(double* div, double* scale) override {
+    if (!ct) { disco_set_error("divb: the instance does not evolve face fluxes (no constrained transport)"); return DISCO_E_STATE; }
+    double *d_div = nullptr, *d_sc = nullptr;
+    if (cudaMalloc(&d_div, sizeof(double) * N) != cudaSuccess ||
+        cudaMalloc(&d_sc, sizeof(double) * N) != cudaSuccess) {
+      if (d_div) cudaFree(d_div);
+      disco_set_error("divb: no device memory for the per-cell result");
+      return DISCO_E_NOMEM;
+    }
+    k_divb<R><<<blocks(N), 256, 0, st>>>(P, S, C, d_div, d_sc);
+    ++g_launches;
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess && div) e = cudaMemcpyAsync(div, d_div, sizeof(double) * N, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess && scale) e = cudaMemcpyAsync(scale, d_sc, sizeof(double) * N, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    cudaFree(d_div);
+    cudaFree(d_sc);
+    CK(e);
+    return 0;
+  }
   // grid of the primitive conversion kernels: a few waves over the SMs
   unsigned prim_grid() const {
     long want = ((long)NQ * N + 255) / 256;
@@ -1026,8 +1098,6 @@ struct Instance : InstanceBase {
     return 0;
   }
 
-  // CFL dt with partial minima in the library's static scratch array: no
-  // device allocation, no write to the instance (disco_gpu_noalloc.h).
   // report.c as a device reduction: out = {t, q, Mass, Torque, Torque2,
   // Torque1_cut[0], Torque2_cut[0], ..., Torque1_cut[4], Torque2_cut[4]}
   double report_q = 0.0, report_soft = 0.0;
@@ -1055,15 +1125,29 @@ struct Instance : InstanceBase {
     for (int i = 0; i < m; ++i) out[i] = all[i];
     return m;
   }
+  // CFL dt with partial minima in the library's static scratch array: no
+  // device allocation, no write to the instance (disco_gpu_noalloc.h).  The
+  // work runs on the instance's device (the one current at create); the
+  // caller's current device is switched to it for the call and restored.
   int getmindt_noalloc(double* dt) override {
     long nb = blocks(N, kNoallocBlock);
     if (N > DISCO_NOALLOC_MAX_CELLS || nb > kNoallocMaxBlocks) {
       disco_set_error("getmindt_noalloc: instance larger than the static scratch (DISCO_NOALLOC_MAX_CELLS)");
       return DISCO_E_ARG;
     }
-    int dev = 0;
-    CK(cudaGetDevice(&dev));
-    unsigned long long* part = noalloc_scratch(dev);
+    int cur = 0;
+    CK(cudaGetDevice(&cur));
+    if (cur != device) CK(cudaSetDevice(device));
+    int rc = getmindt_noalloc_on_device(dt);
+    if (cur != device) {
+      cudaError_t e = cudaSetDevice(cur);
+      if (!rc && e != cudaSuccess) CK(e);
+    }
+    return rc;
+  }
+  int getmindt_noalloc_on_device(double* dt) {
+    long nb = blocks(N, kNoallocBlock);
+    unsigned long long* part = noalloc_scratch(device);
     if (!part) { disco_set_error("getmindt_noalloc: scratch symbol not available"); return DISCO_E_CUDA; }
     DevParams Pn = P;
     Pn.t_end = 0.0;

@@ -40,47 +40,11 @@ static unsigned long long* noalloc_scratch(int dev) {
 template <typename Phys, typename R, int NQ>
 __global__ void k_mindt_blocks(DevParams P, DevState<R> S, unsigned long long* part) {
   int c = blockIdx.x * blockDim.x + threadIdx.x;
-  double dtc = 1.0e300;
-  float dtf = 3.0e38f;
-  if (c < S.N) {
-    int jk = S.cell_ring[c];
-    int k = div_fast(jk, P.mul_nr), j = jk - k * P.Nr;
-    if (is_real(P, j, k)) {
-      int off = S.ring_off[jk], Np = S.ring_off[jk + 1] - off;
-      int i = c - off;
-      int im = off + (i == 0 ? Np - 1 : i - 1);
-      R pr[NQ];
-#pragma unroll
-      for (int q = 0; q < NQ; ++q) pr[q] = S.prim[q * S.N + c];
-      if constexpr (kMix<R>) {
-        R w = (R)(.5 * (S.wiph[im] + S.wiph[c]) - S.ring_Om[jk]);
-        R dph = S.dphi_r[c];
-        dtf = Phys::mindt_r(P, S.planets, pr, w, S.ring_r1_r[jk] * dph, S.ring_dl_r[1][jk],
-                            S.ring_dl_r[0][jk], S.ring_rc_r[jk], (R)S.piph[c] - (R).5 * dph);
-      } else {
-        const double* rj = S.r_jph + 1;
-        const double* zk = S.z_kph + 1;
-        double phip = S.piph[c], phim = phip - S.dphi[c];
-        double xp[3] = {rj[j], phip, zk[k]};
-        double xm[3] = {rj[j - 1], phim, zk[k - 1]};
-        double w = .5 * (S.wiph[im] + S.wiph[c]);
-        if constexpr (Phys::GR) dtc = Phys::mindt_x(P, pr, w, xp, xm);
-        else dtc = Phys::mindt(P, S.planets, pr, w, xp, xm, S.ring_rc[jk]);
-      }
-    }
-  }
+  double dtc = c < S.N ? cell_mindt<Phys, R, NQ>(P, S, c) : 1.0e300;
   __shared__ unsigned long long red[32];
   int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  unsigned long long b;
-  if constexpr (kMix<R>) {
-    unsigned u = __float_as_uint(dtf);
-    for (int o = 16; o > 0; o >>= 1) u = min(u, __shfl_xor_sync(0xffffffffu, u, o));
-    b = __double_as_longlong(u >= 0x7f000000u ? 1.0e300 : (double)__uint_as_float(u));
-  } else {
-    b = __double_as_longlong(dtc);
-    for (int o = 16; o > 0; o >>= 1) b = min(b, __shfl_xor_sync(0xffffffffu, b, o));
-  }
-  (void)dtc; (void)dtf;
+  unsigned long long b = __double_as_longlong(dtc);
+  for (int o = 16; o > 0; o >>= 1) b = min(b, __shfl_xor_sync(0xffffffffu, b, o));
   if (lane == 0) red[wid] = b;
   __syncthreads();
   if (wid == 0) {
@@ -94,7 +58,9 @@ __global__ void k_mindt_blocks(DevParams P, DevState<R> S, unsigned long long* p
 // as k_dt_finalize does with no end-time clamp; dt goes to part[kNoallocMaxBlocks].
 static __global__ void k_mindt_final(DevParams P, unsigned long long* part, int nb) {
   __shared__ unsigned long long red[32];
-  unsigned long long b = ~0ull;
+  // seeded with +inf as k_dt_finalize's accumulator is, so partials that are
+  // all NaN give the maxDT-capped dt there and here alike
+  unsigned long long b = 0x7ff0000000000000ull;
   for (int i = threadIdx.x; i < nb; i += blockDim.x) b = min(b, part[i]);
   for (int o = 16; o > 0; o >>= 1) b = min(b, __shfl_xor_sync(0xffffffffu, b, o));
   int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;

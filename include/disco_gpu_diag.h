@@ -38,6 +38,16 @@ int disco_gpu_diag_download(disco_gpu *g, double *Qrz, long long len, double *t_
  * zeroes them and t_avg (zero_diagnostics, analysis.c:9-27).  Returns n. */
 int disco_gpu_diag_upload(disco_gpu *g, const double *Qrz, long long len, double t_avg);
 
+/* Divergence of B as constrained transport holds it: per cell, the net
+ * outward flux through its faces, from the face fluxes Phi (the sum of
+ * Python/discopy/geom.py:370-520, calcDivB, which the reference applies to
+ * its checkpoints).  div[c] is that sum and scale[c] the sum of the
+ * absolute face fluxes of cell c, so |div| / scale is the divergence
+ * relative to the flux through the cell; cells without a neighbour ring on
+ * every side get div 0 and scale -1.  Arrays of Ncell (either may be NULL).
+ * Constrained-transport instances only (DISCO_E_STATE otherwise). */
+int disco_gpu_divb(disco_gpu *g, double *div, double *scale);
+
 #ifdef __cplusplus
 }
 #endif

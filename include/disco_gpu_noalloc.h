@@ -37,6 +37,11 @@ extern "C" {
  * within the call.  Returns DISCO_E_ARG (nothing launched) when the instance
  * has more than DISCO_NOALLOC_MAX_CELLS cells.
  *
+ * The call runs on the instance's device (the device that was current when
+ * disco_gpu_create made it): the caller's current device is switched to it
+ * for the call and restored before returning.  The scratch address is
+ * looked up for that device on its first call there.
+ *
  * The scratch array is shared by all instances of the same hydro module and
  * precision on a device: concurrent calls from several host threads or
  * streams race on it and must be serialised by the caller. */

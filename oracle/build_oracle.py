@@ -4,7 +4,9 @@
   compiled with -ffp-contract=off so x86 and Arm hosts round like the
   reference build (no fused multiply-add).
 * oracle/_ref/<config>/disco_ref -- the reference itself, compiled from its
-  unmodified sources by oracle/ref/Makefile, only where those sources exist.
+  unmodified sources by oracle/ref/Makefile, only where those sources exist:
+  the directory named by the environment variable DISCO_REFERENCE, else the
+  copy oracle/stage_reference.py leaves in baseline/_ref/src (git-ignored).
 """
 from __future__ import annotations
 
@@ -33,11 +35,26 @@ def build_port(force: bool = False) -> str:
     return PORT_LIB
 
 
-def build_ref(reference: str = "/root/reference") -> list[str]:
-    if not os.path.isdir(reference):
+STAGED = os.path.join(ROOT, "baseline", "_ref", "src")
+
+
+def reference_dir() -> str | None:
+    """The reference source tree: $DISCO_REFERENCE, else the staged copy in
+    baseline/_ref/src, else None."""
+    env = os.environ.get("DISCO_REFERENCE")
+    if env and os.path.isfile(os.path.join(env, "paul.h")):
+        return env
+    if os.path.isfile(os.path.join(STAGED, "paul.h")):
+        return STAGED
+    return None
+
+
+def build_ref(reference: str | None = None, configs=None) -> list[str]:
+    reference = reference or reference_dir()
+    if not reference:
         return []
     out = []
-    for cfg in REF_CONFIGS:
+    for cfg in configs or REF_CONFIGS:
         subprocess.run(["make", "-s", "-f", "oracle/ref/Makefile", f"CFG={cfg}", f"REF={reference}"],
                        cwd=ROOT, check=True)
         out.append(os.path.join(HERE, "_ref", os.path.basename(cfg), "disco_ref"))

@@ -31,6 +31,11 @@ def _lib():
         L.disco_port_phi.argtypes = [C.c_void_p, _dp]
         L.disco_port_report.argtypes = [C.c_void_p, _dp]
         L.disco_port_diag.argtypes = [C.c_void_p, _dp, _dp]
+        _ip = C.POINTER(C.c_int)
+        L.disco_port_faces.restype = C.c_long
+        L.disco_port_faces.argtypes = [C.c_void_p, C.c_int, _ip, _ip, _ip, _ip, _dp, _dp]
+        L.disco_port_grad.argtypes = [C.c_void_p, _dp, _dp, _dp]
+        L.disco_port_debug_ct.argtypes = [C.c_void_p, C.c_int, _dp, _dp, _dp, _dp]
         _L = L
     return _L
 
@@ -82,6 +87,30 @@ class PortDomain:
         t = C.c_double()
         _lib().disco_port_diag(self._d, q.ctypes.data_as(_dp), C.byref(t))
         return {"Qrz": q, "t_avg": t.value}
+
+    def faces(self, dim: int) -> dict:
+        """The face tables built from the current positions (faces_alt.c),
+        in the layout of disco_gb300.Domain.faces."""
+        h = self.host
+        ntr = (h.Nr - 1) * h.Nz if dim == 1 else h.Nr * (h.Nz - 1)
+        nf = _lib().disco_port_faces(self._d, int(dim), None, None, None, None, None, None)
+        out = {"fIndex": np.zeros(max(ntr, 0) + 1, np.int32)}
+        for k in ("L", "R", "LRtype"):
+            out[k] = np.zeros(nf, np.int32)
+        for k in ("phic", "dA"):
+            out[k] = np.zeros(nf)
+        if nf:
+            ip = C.POINTER(C.c_int)
+            _lib().disco_port_faces(self._d, int(dim), *(out[k].ctypes.data_as(ip) for k in ("fIndex", "L", "R", "LRtype")),
+                                    *(out[k].ctypes.data_as(_dp) for k in ("phic", "dA")))
+        return out
+
+    def gradients(self) -> dict:
+        """plm_phi + plm_trans on the current state (gradp, gradr, gradz)."""
+        shp = (self.host.num_q, self.host.Ncell)
+        out = {k: np.zeros(shp) for k in ("gradp", "gradr", "gradz")}
+        _lib().disco_port_grad(self._d, *(out[k].ctypes.data_as(_dp) for k in ("gradp", "gradr", "gradz")))
+        return out
 
     def __del__(self):
         if getattr(self, "_d", None):

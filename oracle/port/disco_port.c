@@ -2167,6 +2167,46 @@ void disco_port_free(port_domain *d)
    free(d);
 }
 
+/* The face tables of dimension dim built from the current positions
+ * (faces_alt.c:36-179), in the layout of disco_gpu_debug_faces: fIndex
+ * [ntracks + 1], per face L and R as global cell ids, LRtype, cm[1] and dA.
+ * Returns the number of faces (arrays may be NULL to size them). */
+long disco_port_faces(port_domain *d, int dim, int *fIndex, int *L, int *R, int *LRtype,
+                      double *phic, double *dA)
+{
+   D = d;
+   if((dim == 1 && d->Nr <= 1) || (dim == 2 && d->Nz <= 1)) return 0;
+   build_faces(dim);
+   int d0 = dim - 1, nt = d->ntracks[d0];
+   long nf = d->fI[d0][nt];
+   if(fIndex) for(int t = 0; t <= nt; t++) fIndex[t] = d->fI[d0][t];
+   for(long n = 0; n < nf; n++) {
+      const pface *f = &d->faces[d0][n];
+      if(L) L[n] = (int)(f->L - d->cells);
+      if(R) R[n] = (int)(f->R - d->cells);
+      if(LRtype) LRtype[n] = f->LRtype;
+      if(phic) phic[n] = f->cm[1];
+      if(dA) dA[n] = f->dA;
+   }
+   return nf;
+}
+
+/* plm_phi, then the faces and plm_trans of each dimension (onestep.c:104-130)
+ * on the current state; gradp, gradr, gradz as SoA [nq*N] (NULL to skip). */
+void disco_port_grad(port_domain *d, double *gradp, double *gradr, double *gradz)
+{
+   D = d;
+   plm_phi();
+   if(d->Nr > 1) { build_faces(1); plm_trans(1); }
+   if(d->Nz > 1) { build_faces(2); plm_trans(2); }
+   for(long c = 0; c < d->N; c++)
+      for(int q = 0; q < d->nq; q++) {
+         if(gradp) gradp[(size_t)q*d->N + c] = d->cells[c].gradp[q];
+         if(gradr) gradr[(size_t)q*d->N + c] = d->cells[c].gradr[q];
+         if(gradz) gradz[(size_t)q*d->N + c] = d->cells[c].gradz[q];
+      }
+}
+
 /* Stage dumps of the CT chain of the first substep (see disco_gpu_debug_ct). */
 int disco_port_debug_ct(port_domain *d, int stage, double *E, double *B, double *Ephi, double *Phi)
 {

@@ -14,7 +14,8 @@
  *    disco_ref grad  OUT.bin          (plm_phi + faces + plm_trans, then dump)
  *    disco_ref run N OUT.bin          (N full RK steps, then dump, then the
  *                                      reference's report() into report.dat)
- *    disco_ref time N                 (N steps, prints zone-updates/s only)
+ *    disco_ref time N [W]             (W untimed warm-up steps, then N timed
+ *                                      steps; prints zone-updates/s only)
  *
  * Dump format: little-endian raw, see write_state() / write_faces();
  * tests/golden/dumpio.py reads it.
@@ -171,11 +172,17 @@ int main(int argc, char **argv)
    } else if(strcmp(mode, "run") == 0 || strcmp(mode, "time") == 0) {
       int nsteps = atoi(argv[2]);
       long ncells = 0;
-      int j, k;
+      int j, k, s;
       for(k = d->NgZa; k < d->Nz - d->NgZb; k++)
          for(j = d->NgRa; j < d->Nr - d->NgRb; j++) ncells += d->Np[j + d->Nr*k];
+      if(strcmp(mode, "time") == 0 && argc > 3) {
+         int nwarm = atoi(argv[3]);
+         for(s = 0; s < nwarm; s++) {
+            double dt = getmindt(d);
+            timestep(d, dt);
+         }
+      }
       double t0 = now_s();
-      int s;
       for(s = 0; s < nsteps; s++) {
          double dt = getmindt(d);
          timestep(d, dt);

@@ -171,7 +171,11 @@ def run_case(name: str, ref: str) -> None:
 
 
 if __name__ == "__main__":
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    sys.path.insert(0, ROOT)
+    from oracle.build_oracle import reference_dir
+    ref = sys.argv[1] if len(sys.argv) > 1 else reference_dir()
+    if not ref:
+        raise SystemExit("reference sources not found: pass REFERENCE_DIR or set DISCO_REFERENCE")
     names = sys.argv[2:] or list(CASES)
     for n in names:
         run_case(n, ref)

@@ -73,3 +73,39 @@ def grouped_rel_l1(a, b, r, num_c):
     if a.shape[0] > num_c:
         out["passive"] = rel_l1(a[num_c], b[num_c])
     return out
+
+
+def divb_from_faces(Phi, Np, faces):
+    """Net outward face flux of B per cell (the sum of
+    Python/discopy/geom.py:370-520, calcDivB) from the face fluxes Phi
+    [5, N] and face tables {"r": ..., "z": ...} (L, R, LRtype per face): a
+    face's flux lives in L.Phi[2] / L.Phi[4] (LRtype 0) or R.Phi[1] /
+    R.Phi[3] (bfields.c:52-76)."""
+    N = Phi.shape[1]
+    off = np.concatenate([[0], np.cumsum(Np)])
+    div = np.zeros(N)
+    for jk in range(len(Np)):
+        a, b = off[jk], off[jk + 1]
+        div[a:b] += Phi[0, a:b] - np.roll(Phi[0, a:b], 1)
+    for key, up, dn in (("r", 2, 1), ("z", 4, 3)):
+        f = faces.get(key)
+        if f is None or len(f["L"]) == 0:
+            continue
+        L, R = f["L"].astype(np.int64), f["R"].astype(np.int64)
+        flux = np.where(f["LRtype"] == 0, Phi[up, L], Phi[dn, R])
+        np.add.at(div, L, flux)
+        np.add.at(div, R, -flux)
+    return div
+
+
+def component_norms(a, b):
+    """Per conserved component q of a [nq, n] against b: the relative L1
+    error sum|a-b| / sum|b| and the relative Linf error max|a-b| / max|b|
+    (each 0 where b is identically zero and a equals it)."""
+    out = {"l1": {}, "linf": {}}
+    for q in range(b.shape[0]):
+        d = np.abs(a[q] - b[q])
+        s1, m1 = np.abs(b[q]).sum(), np.abs(b[q]).max() if b.shape[1] else 0.0
+        out["l1"][q] = float(d.sum() / s1) if s1 > 0 else float(d.sum())
+        out["linf"][q] = float(d.max() / m1) if m1 > 0 else float(d.max() if d.size else 0.0)
+    return out

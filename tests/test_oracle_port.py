@@ -53,10 +53,15 @@ def test_port_bit_exact_vs_golden(name):
     assert np.array_equal(s["prim"], g["run_prim"]) or np.array_equal(s["prim"][:, real], g["run_prim"][:, real])
 
 
-REF = "/root/reference"
+def _ref_dir():
+    from oracle.build_oracle import reference_dir
+    return reference_dir()
 
 
-@pytest.mark.skipif(not os.path.isdir(REF), reason="reference sources not present")
+REF = _ref_dir()
+
+
+@pytest.mark.skipif(REF is None, reason="reference sources not present")
 def test_port_bit_exact_vs_reference_binary():
     sys_path_golden = os.path.join(ROOT, "tests", "golden")
     import sys
@@ -153,3 +158,27 @@ def test_port_diagnostics_vs_reference(name):
             assert rel_l1(dg["Qrz"][:, q], g["diag_Qrz"][:, q]) < 1e-14, q
     else:
         assert np.array_equal(dg["Qrz"], g["diag_Qrz"])
+
+
+FACE_CASES = ["cfg1_n24", "cfg2_n12", "cfg5_n16", "cfg3_n24", "cfg1_zerograd"] + BC_CASES
+
+
+@pytest.mark.parametrize("name", FACE_CASES)
+def test_port_faces_and_gradients_bit_exact_vs_golden(name):
+    """The restatement's face tables (faces_alt.c) and PLM gradients
+    (plm.c) of the initial state equal the reference's, bit for bit: the
+    checker the device's face and gradient tests rest on."""
+    import disco_gb300 as dg
+    from oracle.port import PortDomain
+    g = load_golden(name)
+    h = dg.HostDomain(dg.read_params(write_par(g["par_text"])), dg.read_modules(mk_path(g)))
+    o = PortDomain(h)
+    for key, dim in (("r", 1), ("z", 2)):
+        if f"faces_{key}_L" not in g:
+            continue
+        f = o.faces(dim)
+        for k in ("fIndex", "L", "R", "LRtype", "phic", "dA"):
+            assert np.array_equal(f[k], g[f"faces_{key}_{k}"]), (key, k)
+    gr = o.gradients()
+    for k in ("gradp", "gradr", "gradz"):
+        assert np.array_equal(gr[k], g[f"grad_{k}"]), k
