@@ -57,6 +57,23 @@ WORKLOADS = {
                          "overrides": {"Num_R": 64, "Num_Z": 16},
                          "cpu_sample": {"Num_R": 32, "Num_Z": 8},
                          "ref_sample": {"Num_R": 32, "Num_Z": 8}},
+    # the same disk at 128 x 32 rings (about 1.9 M cells, 0.8 GB of state,
+    # well above L2): the case for DRAM-traffic captures of single kernels
+    "mhd_disk3d_medium": {"dir": "configs/cfg2_mhd_disk",
+                          "desc": "3D Newtonian MHD Keplerian disk at Nr=128 x Nz=32 (profiling case)",
+                          "overrides": {"Num_R": 128, "Num_Z": 32},
+                          "cpu_sample": {"Num_R": 32, "Num_Z": 8},
+                          "ref_sample": {"Num_R": 32, "Num_Z": 8}},
+    # GRMHD Fishbone-Moncrief torus around a Kerr black hole (a = 0.9):
+    # 192 x 96 rings on r in [2, 40], z in [-20, 20], Np capped at 1024,
+    # 11.9 M cells, FP64
+    "grmhd_torus": {"dir": "configs/cfg4_grmhd_torus",
+                    "desc": "3D GRMHD Fishbone-Moncrief torus (r_in 6, r_pk 12, gamma 4/3, loop field at "
+                            "beta 100, 4% pressure noise) around a Kerr black hole a=0.9 in Kerr-Schild "
+                            "cylindrical coordinates, Nr=192 on r in [2,40], Nz=96 on z in [-20,20], "
+                            "Np capped at 1024, HLL, cell-centred B, Noble 2D cons2prim, PLM 1.5, RK2, FP64",
+                    "precisions": (0,),
+                    "cpu_sample": None, "ref_sample": None},
     # 64 independent planet-disk runs in one graph launch per step: Nr drawn
     # from U{64..512} and the planet mass ratio log-uniform in [1e-5, 1e-3]
     # by splitmix64 seeded 0..63
@@ -101,22 +118,21 @@ KERNEL_SYMBOL = {"flux_trans": "k_flux_trans", "plm_slopes": "k_plm_slopes", "pl
                  "ct_edge_flag": "k_set_flag"}
 
 
-def _traffic(workload: str, func: str, N: int, nf: dict):
-    """DRAM bytes per launch of kernel function `func` from a committed ncu
-    summary: lines `traffic_per_unit <func> <bytes per cell> <bytes per
-    face>` of profiles/<func>_<case>_dram.md, captured on a small case and
-    scaled by the units one full launch processes (the kernel's traffic is
-    proportional to its cells and faces).  Returns (bytes, source)."""
+def _traffic(func: str, alg_bytes: float):
+    """DRAM bytes per launch of kernel function `func`: the ratio of measured
+    to algorithmic bytes from a committed ncu summary (a line
+    `traffic_ratio <func> <ratio>` in profiles/<func>_*_dram.md, captured on a
+    case larger than L2 but a few GB at most), times this launch's
+    algorithmic bytes -- the kernel's traffic grows in proportion to the
+    cells and faces it processes.  Returns (bytes, source)."""
     import glob
     for path in sorted(glob.glob(os.path.join(ROOT, "profiles", f"{func}_*_dram.md"))):
         for ln in open(path):
             parts = ln.split()
-            if len(parts) == 4 and parts[0] == "traffic_per_unit" and parts[1] == func:
-                per_cell, per_face = float(parts[2]), float(parts[3])
-                nfa = (nf["r"] + nf["z"]) / 2 if func in ("flux_trans", "plm_slopes", "plm_trans", "faces") else 0
-                return (per_cell * N + per_face * nfa,
-                        f"ncu dram__bytes_read.sum + dram__bytes_write.sum on a small case, per cell "
-                        f"and face, scaled to one full launch ({os.path.relpath(path, ROOT)})")
+            if len(parts) == 3 and parts[0] == "traffic_ratio" and parts[1] == func:
+                return (float(parts[2]) * alg_bytes,
+                        "ncu dram__bytes_read.sum + dram__bytes_write.sum over algorithmic bytes on a "
+                        f"smaller case, scaled to one full launch ({os.path.relpath(path, ROOT)})")
     return None, None
 
 
@@ -720,7 +736,7 @@ def main():
     top_bytes = top["bytes"] / top["launches"]
     top_avg_s = top["ms"] / top["launches"] / 1e3
     achieved = top_bytes / top_avg_s / 1e9
-    traffic, traffic_src = _traffic(args.workload, top_name, N, nf)
+    traffic, traffic_src = _traffic(top_name, top_bytes)
     # fused-RK2 compulsory bytes per zone-update: NQ (6 s_W + 4 s_U) + 6 x 8
     # (the RK copy of the state is one s_W write and one s_W read: the mixed
     # path keeps the first substep's increment in R), plus 25 x 8 for the

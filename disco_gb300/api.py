@@ -58,6 +58,7 @@ class DiscoParams(C.Structure):
         ("dampTimeInner", C.c_double), ("dampLenInner", C.c_double), ("dampTimeOuter", C.c_double),
         ("dampLenOuter", C.c_double), ("dampTimeUpper", C.c_double), ("dampLenUpper", C.c_double),
         ("dampTimeLower", C.c_double), ("dampLenLower", C.c_double),
+        ("maxNp", C.c_int),
     ]
 
 
@@ -93,6 +94,7 @@ class DiscoHostDomain(C.Structure):
         ("prim", C.POINTER(C.c_double)),
         ("Npl", C.c_int),
         ("planets", DiscoPlanet * 4),
+        ("ic_aux", C.c_double * 4),
     ]
 
 

@@ -60,9 +60,12 @@ struct DevParams {
   int Npl;
   // GRMHD: the black-hole mass of the Kerr-Schild metric (Metric_Par2)
   double gr_M;
+  double gr_a;     // GRMHD: black-hole spin (Metric_Par3) of the Kerr metric
+  int gr_kerr;     // GRMHD: 1 for METRIC kerr_ks_rpz, 0 for schw_ks_rpz
   // initial / boundary plugins
   int initial_id, boundary_id;
   double ic[8];
+  double ic_aux[4];   // constants the initial condition derived at set-up (disco_host_domain)
   double t_end;
   // exact division by Nr and Nr - 1 (ring and r-pair indices) by 40-bit
   // reciprocals: ceil(2^40 / d)

@@ -220,7 +220,7 @@ DISCO_D void diag_cell(const DevParams& P, const DevState<R>& S, int c, double O
     if constexpr (NQ >= 8 && !kMix<R>) {
       const double gl = P.gamma_law;
       const double x[3] = {rd, phid, zd};
-      const KsMetric g(x, P.gr_M);
+      const KsMetric g(x, P.gr_M, P.gr_a, P.gr_kerr);
       const double al = g.al, jac = g.jac;
       const double* be = g.be;
       const double* gam = g.gam;

@@ -197,6 +197,7 @@ struct Instance : InstanceBase {
     P.initial_id = dom->mod.initial; P.boundary_id = dom->mod.boundary;
     double icp[8] = {p.initPar1, p.initPar2, p.initPar3, p.initPar4, p.initPar5, p.initPar6, p.initPar7, p.initPar8};
     for (int i = 0; i < 8; ++i) P.ic[i] = icp[i];
+    for (int i = 0; i < 4; ++i) P.ic_aux[i] = dom->ic_aux[i];
     P.t_end = 0.0;
     if ((long)nring >= (1L << 24) || Nr >= (1 << 16)) {
       disco_set_error("grid too large for the ring index arithmetic (Nr*Nz < 2^24, Nr < 2^16)");
@@ -243,6 +244,8 @@ struct Instance : InstanceBase {
     rk3 = p.Timestep == 3;
     ct = Phys::MHD && !Phys::GR && dom->mod.ct_mode == 2 && p.CT;
     P.gr_M = p.metricPar2;
+    P.gr_kerr = dom->mod.metric == DISCO_METRIC_KERR_KS_RPZ ? 1 : 0;
+    P.gr_a = P.gr_kerr ? p.metricPar3 : 0.0;
     if constexpr (Phys::GR) {
       // the GRMHD module as built: FP64, HLL, cell-centred B (CT_MODE 0), a
       // static mesh, adiabatic, no viscosity, no rotating frame, no planets
@@ -255,6 +258,7 @@ struct Instance : InstanceBase {
       else if (P.include_viscosity || P.rot_flag) why = "GRMHD with viscosity or a rotating frame is not built";
       else if (dom->mod.planets != 0) why = "GRMHD takes PLANETS=none";
       else if (P.gr_M <= 0.0) why = "GRMHD needs Metric_Par2 (the black-hole mass) > 0";
+      else if (P.gr_kerr && !(fabs(P.gr_a) < P.gr_M)) why = "kerr_ks_rpz needs |Metric_Par3| (the spin) < Metric_Par2";
       if (why) {
         disco_set_error(why);
         return DISCO_E_MODULE;
@@ -324,7 +328,7 @@ struct Instance : InstanceBase {
     A(&S.ring_rc_r, nring); A(&S.ring_r1_r, nring); A(&S.ring_vol_r, nring); A(&S.ring_dA_r, nring);
     A(&S.ring_r23_r, nring); A(&S.ring_zc_r, nring);
     A(&S.ring_Om, nring); A(&S.ring_Om_r, nring); A(&S.ring_Lsh, nring);
-    A(&S.ring_gL_r, nring); A(&S.ring_gR_r, nring);
+    A(&S.ring_gL_r, nring); A(&S.ring_gR_r, nring); A(&S.ring_cfl, 3 * (size_t)nring);
     for (int d = 0; d < 2; ++d) { A(&S.ring_At_r[d], nring); A(&S.ring_dl_r[d], nring); }
     A(&piph_buf[0], N); A(&piph_buf[1], N);
     A(&S.dphi, N); A(&S.wiph, N);
@@ -412,7 +416,7 @@ struct Instance : InstanceBase {
       }
       S.ghost_ring = d_gr; S.ghost_i0 = d_gi; S.nghost = (int)gr.size();
       S.ghost_tab = nullptr;
-      if (S.nghost > 0 && (P.initial_id == 1 || P.initial_id == 2)) {   // axisymmetric disks
+      if (S.nghost > 0 && (P.initial_id == 1 || P.initial_id == 2 || P.initial_id == 5)) {   // axisymmetric
         double* tab = nullptr;
         A(&tab, (size_t)nring * NQ);
         k_ghost_tab<R, NQ><<<(int)blocks(nring, 128), 128, 0, st>>>(P, nring, tab, S.r_jph, S.z_kph);

@@ -13,6 +13,7 @@
 #include "riemann.cuh"
 #include "../plugins/ic_vortex_gauss.h"
 #include "../plugins/ic_disks.h"
+#include "../plugins/ic_fm_torus.h"
 
 namespace disco {
 
@@ -64,6 +65,7 @@ struct DevState {
   R* ring_zc_r;
   R* ring_At_r[2];
   R* ring_dl_r[2];
+  double* ring_cfl;            // [3 * Nr*Nz]: .5 (rp + rm), 1 / dr, 1 / dz (CFL bound, FP64)
   R* dphi_r;                   // [N] dphi in R (the same array as dphi when R is double)
   // Ring frame of the mixed path: there prim[UPP] holds omega - Om of the
   // cell's ring, so the FP32 value keeps the precision of the motion
@@ -192,9 +194,13 @@ DISCO_D void initial_raw(const DevParams& P, double* prim, const double* x) {
       disco_ic_disk_planet_eval(&D, prim, x, P.num_c, P.num_q);
     } else if (P.initial_id == 3) {
       disco_ic_disk_cbd_eval(&D, prim, x, P.num_c, P.num_q);
-    } else {   // 4: gr_disk (Metric_Par2 = M, Init_Par1..4)
+    } else if (P.initial_id == 4) {   // gr_disk (Metric_Par2 = M, Init_Par1..4)
       disco_ic_gr_disk G{P.gamma_law, P.gr_M, P.ic[0], P.ic[1], P.ic[2], P.ic[3]};
       disco_ic_gr_disk_eval(&G, prim, x, P.num_c, P.num_q);
+    } else {   // 5: fm_torus (Metric_Par2,3 = M, a; Init_Par1..4; the set-up's derived constants)
+      disco_ic_fm F{P.gamma_law, P.gr_M, P.gr_a, P.ic[0], P.ic[1], P.ic[2], P.ic[3], P.rho_floor,
+                    P.p_floor, P.ic_aux[0], P.ic_aux[1], P.ic_aux[2], P.ic_aux[3]};
+      disco_ic_fm_eval(&F, prim, x, P.num_c, P.num_q);
     }
   }
 }
@@ -691,6 +697,10 @@ __global__ void k_ring_geom(DevParams P, DevState<R> S, int nring) {
   S.ring_At_r[1][jk] = (R)atz;
   S.ring_dl_r[0][jk] = (R)dz;
   S.ring_dl_r[1][jk] = (R)dr;
+  // CFL extents in FP64: .5 (rp + rm) (times dphi: r dphi), 1 / dr, 1 / dz
+  S.ring_cfl[3 * jk + 0] = r1;
+  S.ring_cfl[3 * jk + 1] = 1.0 / dr;
+  S.ring_cfl[3 * jk + 2] = 1.0 / dz;
 }
 
 // Static per-pair geometry (faces_alt.c:112-135, the face radius cm[0]).
@@ -1704,12 +1714,25 @@ DISCO_D double cell_mindt(const DevParams& P, const DevState<R>& S, int c) {
   double xm[3] = {rj[j - 1], phim, zk[k - 1]};
   double w = .5 * (S.wiph[im] + S.wiph[c]);
   if constexpr (kMix<R>) {
-    using Phys64 = typename Phys::template Rebind<double>;
-    double pd[NQ];
+    // the signal speeds are physics and FP32, as in the Riemann solvers;
+    // the cell extents, the rates, their maximum and dt are FP64:
+    // dt = 1 / max(s_r / dr, s_phi / (r dphi), s_z / dz [, 2 nu / dx^2])
+    (void)xp; (void)xm;
+    R pr[NQ];
 #pragma unroll
-    for (int q = 0; q < NQ; ++q) pd[q] = f2d_int(S.prim[q * S.N + c]);
-    pd[UPP] += S.ring_Om[jk];
-    return Phys64::mindt(P, S.planets, pd, w, xp, xm, S.ring_rc[jk]);
+    for (int q = 0; q < NQ; ++q) pr[q] = S.prim[q * S.N + c];
+    R sp[4];
+    const R wr = (R)(w - S.ring_Om[jk]);   // relative to the ring frame, as prim[UPP]
+    const double dph = S.dphi[c];
+    Phys::cfl_speeds_r(P, S.planets, pr, wr, S.ring_rc_r[jk], (R)(phip - .5 * dph), sp);
+    const double* g = S.ring_cfl + 3 * jk;
+    const double iphi = 1.0 / (g[0] * dph);
+    double rate = fmax(f2d_int(sp[0]) * g[1], fmax(f2d_int(sp[1]) * iphi, f2d_int(sp[2]) * g[2]));
+    if (sp[3] > (R)0) {   // explicit viscosity: dt_visc = dx^2 / (2 nu), dx the smallest extent
+      const double ix = fmax(iphi, fmax(g[1], g[2]));
+      rate = fmax(rate, 2.0 * f2d_int(sp[3]) * ix * ix);
+    }
+    return 1.0 / rate;
   } else {
     R pr[NQ];
 #pragma unroll

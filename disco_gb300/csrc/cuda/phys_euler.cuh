@@ -220,6 +220,28 @@ struct Euler {
     for (int q = 0; q < NQ; ++q) { F[q] = 0; U[q] = 0; }
   }
 
+  // Signal speeds of the CFL bound in R (mixed path): sp[0..2] =
+  // cs + |v_r|, cs + |v_phi - w r|, cs + |v_z|; sp[3] = the explicit
+  // viscosity nu, 0 without viscosity (euler.c:328-377).
+  DISCO_D static void cfl_speeds_r(const DevParams& P, const DevPlanet* pl, const R* prim, R w, R r, R phi,
+                                   R* sp) {
+    R Pp = prim[PPP], rho = prim[RHO];
+    R vp = (prim[UPP] - w) * r;
+    R cs = sqrt(PRM(R, P, gamma_law) * Pp / rho);
+    sp[0] = cs + fabs(prim[URR]);
+    sp[1] = cs + fabs(vp);
+    sp[2] = cs + fabs(prim[UZZ]);
+    sp[3] = (R)0;
+    if (P.include_viscosity) {
+      R nu = PRM(R, P, explicit_viscosity);
+      if (P.alpha_flag) {
+        R c2 = PRM(R, P, gamma_law) * Pp / rho;
+        nu = PRM(R, P, explicit_viscosity) * c2 / get_height_om<R>(P, pl, r, phi);
+      }
+      sp[3] = nu;
+    }
+  }
+
   // mindt of the mixed path: the same bound in R, with the cell extents
   // dL0 = r dphi, dL1 = dr, dL2 = dz given.
   DISCO_D static R mindt_r(const DevParams& P, const DevPlanet* pl, const R* prim, R w, R dL0, R dL1,

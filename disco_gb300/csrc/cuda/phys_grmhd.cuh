@@ -1,5 +1,6 @@
 // GRMHD module (Hydro/grmhd.c) on the Schwarzschild metric in Kerr-Schild
-// cylindrical coordinates (Hydro/Metric/schw_ks_rpz.c) with the normal
+// cylindrical coordinates (Hydro/Metric/schw_ks_rpz.c) or the Kerr metric
+// of spin a in the same coordinates (plugins/metric_kerr.h), with the normal
 // observer frame (Hydro/Frame/normal.c).  FP64 only.
 //
 // Unlike the Newtonian modules every hook depends on the full position
@@ -14,6 +15,7 @@
 // u_i: prim[URR] = u_r, prim[UPP] = u_phi / r^2, prim[UZZ] = u_z.
 #pragma once
 #include "dev_common.cuh"
+#include "../plugins/metric_kerr.h"
 
 namespace disco {
 
@@ -21,10 +23,17 @@ namespace disco {
 // metric_lapse :20, metric_shift :26, metric_gam :39, metric_igam :63,
 // metric_jacobian :88, metric_der_g :93, metric_der_lapse :142,
 // metric_der_shift :159, metric_killing :184.
+// kerr != 0 selects the Kerr metric of spin a (metric_kerr.h); else the
+// Schwarzschild formulas of schw_ks_rpz.c in the reference's operation order.
 struct KsMetric {
   double al, be[3], gam[9], igam[9], jac;   // jac = metric_jacobian / r
 
-  DISCO_D KsMetric(const double* x, double M) {
+  DISCO_D KsMetric(const double* x, double M, double a, int kerr) {
+    if (kerr) {
+      disco_kerr_3p1(x, M, a, &al, be, gam, igam);
+      jac = 1.0;   // metric_jacobian (r) / r
+      return;
+    }
     const double r = x[0], z = x[2];
     const double R = sqrt(r * r + z * z);
     al = 1.0 / sqrt(1.0 + 2 * M / R);
@@ -48,7 +57,11 @@ struct KsMetric {
 DISCO_D int ks_killing(int mu) { return (mu == 1 || mu == 3) ? 0 : 1; }
 
 // d g_{mu nu} / d x^i (i = 1: r, i = 3: z; zero otherwise)
-DISCO_D void ks_der_g(const double* x, double M, int i, double* dg) {
+DISCO_D void ks_der_g(const double* x, double M, double a, int kerr, int i, double* dg) {
+  if (kerr) {
+    disco_kerr_der_g(x, M, a, i, dg);
+    return;
+  }
   for (int mu = 0; mu < 16; ++mu) dg[mu] = 0.0;
   if (i != 1 && i != 3) return;
   const double r = x[0], z = x[2];
@@ -86,26 +99,31 @@ DISCO_D void ks_frame_U(const KsMetric& g, double* U) {
 }
 
 // frame_der_U (normal.c:21) with metric_der_lapse / metric_der_shift
-DISCO_D void ks_frame_der_U(const double* x, double M, const KsMetric& g, double* dU) {
-  const double r = x[0], z = x[2];
-  const double R = sqrt(r * r + z * z);
-  const double st = r / R, ct = z / R;
-  // metric_der_lapse
-  const double MoR2 = M / (R * R);
-  const double a = 1.0 / sqrt(1.0 + 2 * M / R);
-  const double da[4] = {0.0, a * a * a * MoR2 * st, 0.0, a * a * a * MoR2 * ct};
-  // metric_der_shift
-  const double denom = 1.0 / (R * R + 2 * M * R);
-  const double d_denom = -denom * denom * 2 * (R + M);
-  double db[12];
-  for (int i = 0; i < 3; ++i) db[i] = 0;
-  db[3] = 2 * M * denom + 2 * M * r * d_denom * st;
-  db[4] = 0.0;
-  db[5] = 2 * M * z * d_denom * st;
-  for (int i = 0; i < 3; ++i) db[6 + i] = 0;
-  db[9] = 2 * M * r * d_denom * ct;
-  db[10] = 0.0;
-  db[11] = 2 * M * denom + 2 * M * z * d_denom * ct;
+DISCO_D void ks_frame_der_U(const double* x, double M, double spin, int kerr, const KsMetric& g, double* dU) {
+  double da[4], db[12];
+  if (kerr) {
+    disco_kerr_der_lapse(x, M, spin, da);
+    disco_kerr_der_shift(x, M, spin, db);
+  } else {
+    const double r = x[0], z = x[2];
+    const double R = sqrt(r * r + z * z);
+    const double st = r / R, ct = z / R;
+    // metric_der_lapse
+    const double MoR2 = M / (R * R);
+    const double a = 1.0 / sqrt(1.0 + 2 * M / R);
+    da[0] = 0.0; da[1] = a * a * a * MoR2 * st; da[2] = 0.0; da[3] = a * a * a * MoR2 * ct;
+    // metric_der_shift
+    const double denom = 1.0 / (R * R + 2 * M * R);
+    const double d_denom = -denom * denom * 2 * (R + M);
+    for (int i = 0; i < 3; ++i) db[i] = 0;
+    db[3] = 2 * M * denom + 2 * M * r * d_denom * st;
+    db[4] = 0.0;
+    db[5] = 2 * M * z * d_denom * st;
+    for (int i = 0; i < 3; ++i) db[6 + i] = 0;
+    db[9] = 2 * M * r * d_denom * ct;
+    db[10] = 0.0;
+    db[11] = 2 * M * denom + 2 * M * z * d_denom * ct;
+  }
   const double ia = 1.0 / g.al;
   for (int i = 0; i < 16; ++i) dU[i] = 0.0;
   for (int i = 0; i < 4; ++i) {
@@ -163,7 +181,7 @@ struct Grmhd {
   DISCO_D static void prim2cons_x(const DevParams& P, const double* prim, double* cons, const double* x,
                                   double dV) {
     const double r = x[0];
-    KsMetric g(x, P.gr_M);
+    KsMetric g(x, P.gr_M, P.gr_a, P.gr_kerr);
     State s;
     state(g, prim, r, s);
     const double gl = P.gamma_law;
@@ -187,7 +205,7 @@ struct Grmhd {
   DISCO_D static void flux_x(const DevParams& P, const double* prim, double* f, const double* x,
                              const double* n) {
     const double r = x[0];
-    KsMetric g(x, P.gr_M);
+    KsMetric g(x, P.gr_M, P.gr_a, P.gr_kerr);
     State s;
     state(g, prim, r, s);
     // u^i and v^i = u^i / u^0 (the reference forms igaml again; same values)
@@ -227,7 +245,7 @@ struct Grmhd {
   DISCO_D static void vel_x(const DevParams& P, const double* p1, const double* p2, double* Sl, double* Sr,
                             const double* n, const double* x) {
     const double r = x[0];
-    KsMetric g(x, P.gr_M);
+    KsMetric g(x, P.gr_M, P.gr_a, P.gr_kerr);
     const double sqrtgam = g.jac * r / (g.al * r);   // metric_jacobian(x) / (al r)
     const double gl = P.gamma_law;
     const double* pr[2] = {p1, p2};
@@ -271,10 +289,10 @@ struct Grmhd {
     const double x[3] = {0.5 * (xm[0] + xp[0]), 0.5 * (xm[1] + xp[1]), 0.5 * (xm[2] + xp[2])};
     const double M = P.gr_M;
     const double r = x[0];
-    KsMetric g(x, M);
+    KsMetric g(x, M, P.gr_a, P.gr_kerr);
     double U[4], dU[16];
     ks_frame_U(g, U);
-    ks_frame_der_U(x, M, g, dU);
+    ks_frame_der_U(x, M, P.gr_a, P.gr_kerr, g, dU);
     const double sqrtgam = g.jac / g.al;
     const double gl = P.gamma_law;
     const double rho = prim[RHO], Pp = prim[PPP];
@@ -327,7 +345,7 @@ struct Grmhd {
       Sk[i] = 0.0;
       if (ks_killing(i + 1)) continue;
       double dg[16];
-      ks_der_g(x, M, i + 1, dg);
+      ks_der_g(x, M, P.gr_a, P.gr_kerr, i + 1, dg);
       for (int mu = 0; mu < 4; ++mu)
         for (int nu = 0; nu < 4; ++nu)
           Sk[i] += (rhoh * u[mu] * u[nu] * rcorr * pcorr + ig[4 * mu + nu] * Pt - b[mu] * b[nu]) *
@@ -366,7 +384,7 @@ struct Grmhd {
     const double D = cons[DDD];
     const double S[3] = {cons[SRR], cons[LLL], cons[SZZ]};
     const double tau = cons[TAU];
-    KsMetric g(x, P.gr_M);
+    KsMetric g(x, P.gr_M, P.gr_a, P.gr_kerr);
     const double sqrtgam = g.jac / g.al;
     double U[4];
     ks_frame_U(g, U);
@@ -455,7 +473,7 @@ struct Grmhd {
                                 const double* xm) {
     const double x[3] = {0.5 * (xm[0] + xp[0]), 0.5 * (xm[1] + xp[1]), 0.5 * (xm[2] + xp[2])};
     const double r = x[0];
-    KsMetric g(x, P.gr_M);
+    KsMetric g(x, P.gr_M, P.gr_a, P.gr_kerr);
     const double sqrtgam = g.jac * r / (r * g.al);   // metric_jacobian(x) / (r al)
     const double gl = P.gamma_law;
     const double rho = prim[RHO], Pp = prim[PPP];

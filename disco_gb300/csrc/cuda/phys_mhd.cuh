@@ -341,6 +341,23 @@ struct Mhd {
     U[BRR] *= brfac / hr; U[BPP] *= bpfac / hp; U[BZZ] *= bzfac / hz;
   }
 
+  // Signal speeds of the CFL bound in R (mixed path): sp[0..2] = c_f + |v|
+  // per direction, c_f the fast speed bound sqrt(cs^2 + B^2 / rho) of
+  // mhd.c:452-483; sp[3] = 0 (no explicit viscosity).
+  DISCO_D static void cfl_speeds_r(const DevParams& P, const DevPlanet*, const R* prim, R w, R r, R phi,
+                                   R* sp) {
+    (void)phi;
+    R Pp = prim[PPP], rho = prim[RHO];
+    R vp = (prim[UPP] - w) * r;
+    R cs2 = PRM(R, P, gamma_law) * Pp / rho;
+    R Br = prim[BRR], Bp = prim[BPP], Bz = prim[BZZ];
+    R cf = sqrt(cs2 + (Br * Br + Bp * Bp + Bz * Bz) / rho);
+    sp[0] = cf + fabs(prim[URR]);
+    sp[1] = cf + fabs(vp);
+    sp[2] = cf + fabs(prim[UZZ]);
+    sp[3] = (R)0;
+  }
+
   // mindt of the mixed path: the same bound in R, with the cell extents
   // dL0 = r dphi, dL1 = dr, dL2 = dz given.
   DISCO_D static R mindt_r(const DevParams& P, const DevPlanet*, const R* prim, R w, R dL0, R dL1,

@@ -19,6 +19,7 @@
 
 #include "../plugins/ic_vortex_gauss.h"
 #include "../plugins/ic_disks.h"
+#include "../plugins/ic_fm_torus.h"
 
 /* ------------------------------------------------------------------------
  * Error string shared by the whole library.
@@ -167,6 +168,8 @@ int disco_params_read(const char *path, disco_params *p)
    RD("DampLower_Time", dampTimeLower); RD("DampLower_Len", dampLenLower);
    RD("Softening", grav_eps);
    RD("Sink_Par3", sinkPar3);
+   /* not a reference key: an upper bound on cells per ring (0 = none) */
+   { int e0 = err; RI("Max_Np", maxNp); err = e0; }
 #undef RI
 #undef RD
    free(b);
@@ -238,7 +241,8 @@ int disco_modules_read(const char *path, disco_modules *m)
    if(bad) { disco_set_error("Makefile_opt.in: missing module key"); return DISCO_E_PARFILE; }
 
    static const char *hyd[] = {"euler", "mhd", "grmhd"};
-   static const char *ini[] = {"vortex_gauss", "disk_mhd", "disk_planet", "disk_cbd", "gr_disk"};
+   static const char *ini[] = {"vortex_gauss", "disk_mhd", "disk_planet", "disk_cbd", "gr_disk",
+                               "fm_torus"};
    static const char *bnd[] = {"fixed", "fixed3d", "outflow3d", "zerograd", "zerograd_omk",
                                "zerograd_omIN", "accrete3d", "fixRrefZ", "polar3d", "fixed_gap",
                                "tube", "surfaceGravBox", "flowthrough"};
@@ -248,8 +252,9 @@ int disco_modules_read(const char *path, disco_modules *m)
    int i;
    m->hydro = m->initial = m->boundary = m->planets = -1;
    for(i = 0; i < 3; i++) if(!strcmp(m->hydro_name, hyd[i])) m->hydro = i;
-   for(i = 0; i < 5; i++) if(!strcmp(m->initial_name, ini[i])) m->initial = i;
-   m->metric = !strcmp(m->metric_name, "schw_ks_rpz") ? DISCO_METRIC_SCHW_KS_RPZ : DISCO_METRIC_NONE;
+   for(i = 0; i < 6; i++) if(!strcmp(m->initial_name, ini[i])) m->initial = i;
+   m->metric = !strcmp(m->metric_name, "schw_ks_rpz") ? DISCO_METRIC_SCHW_KS_RPZ
+             : !strcmp(m->metric_name, "kerr_ks_rpz") ? DISCO_METRIC_KERR_KS_RPZ : DISCO_METRIC_NONE;
    m->frame = !strcmp(m->frame_name, "normal") ? DISCO_FRAME_NORMAL : DISCO_FRAME_NONE;
    for(i = 0; i < DISCO_BC_COUNT; i++) if(!strcmp(m->boundary_name, bnd[i])) m->boundary = i;
    for(i = 0; i < 4; i++) if(!strcmp(m->planets_name, pla[i])) m->planets = i;
@@ -272,9 +277,9 @@ int disco_modules_read(const char *path, disco_modules *m)
          disco_set_error("grmhd is built with NUM_C=8 and CT_MODE=0 (cell-centred B)");
          return DISCO_E_MODULE;
       }
-      if(m->metric != DISCO_METRIC_SCHW_KS_RPZ || m->frame != DISCO_FRAME_NORMAL) {
-         snprintf(msg, sizeof msg, "grmhd: METRIC=%s FRAME=%s not built (schw_ks_rpz, normal are)",
-                  m->metric_name, m->frame_name);
+      if(m->metric == DISCO_METRIC_NONE || m->frame != DISCO_FRAME_NORMAL) {
+         snprintf(msg, sizeof msg, "grmhd: METRIC=%s FRAME=%s not built (schw_ks_rpz or kerr_ks_rpz, "
+                  "normal are)", m->metric_name, m->frame_name);
          disco_set_error(msg); return DISCO_E_MODULE;
       }
    }
@@ -338,6 +343,16 @@ static double get_dp(double phip, double phim, double phi_max)
    return dp;
 }
 
+/* fm_torus: the parameters from in.par and the derived constants of
+ * disco_ic_fm_setup (kept in ic_aux: ell, F_in, h_pk - 1, field scale) */
+static void fm_params(const disco_params *p, const double *aux, struct disco_ic_fm *P)
+{
+   P->gam = p->Adiabatic_Index; P->M = p->metricPar2; P->a = p->metricPar3;
+   P->rin = p->initPar1; P->rpk = p->initPar2; P->beta = p->initPar3; P->acut = p->initPar4;
+   P->rho_atm = p->Density_Floor; P->cs2_atm = p->Pressure_Floor;
+   P->ell = aux[0]; P->F_in = aux[1]; P->hpk1 = aux[2]; P->bscale = aux[3];
+}
+
 static void ic_eval(const disco_host_domain *d, double *prim, const double *x)
 {
    const disco_params *p = &d->par;
@@ -374,6 +389,11 @@ static void ic_eval(const disco_host_domain *d, double *prim, const double *x)
       struct disco_ic_gr_disk P = { p->Adiabatic_Index, p->metricPar2, p->initPar1,
                                     p->initPar2, p->initPar3, p->initPar4 };
       disco_ic_gr_disk_eval(&P, prim, x, nc, nq);
+      break; }
+   case DISCO_IC_FM_TORUS: {
+      struct disco_ic_fm P;
+      fm_params(p, d->ic_aux, &P);
+      disco_ic_fm_eval(&P, prim, x, nc, nq);
       break; }
    }
    if(p->RotFrame) prim[3] -= p->RotOmega;   /* subtract_omega, rotframe.c:15 */
@@ -475,6 +495,7 @@ int disco_host_setup(const disco_params *par, const disco_modules *mod,
          double dp = par->aspect*dr/hp;
          int Np = (int)(Pmax/dp);
          if(Np < 4) Np = 4;
+         if(par->maxNp > 0 && Np > par->maxNp) Np = par->maxNp;
          d->Np[jk] = Np;
       }
    }
@@ -512,6 +533,13 @@ int disco_host_setup(const disco_params *par, const disco_modules *mod,
    }
    d->t = par->t_min;
    setup_planets(d);
+   memset(d->ic_aux, 0, sizeof d->ic_aux);
+   if(d->mod.initial == DISCO_IC_FM_TORUS) {
+      struct disco_ic_fm P;
+      fm_params(par, d->ic_aux, &P);
+      disco_ic_fm_setup(&P);
+      d->ic_aux[0] = P.ell; d->ic_aux[1] = P.F_in; d->ic_aux[2] = P.hpk1; d->ic_aux[3] = P.bscale;
+   }
 
    /* setupCells (domain.c:283-353): calc_dp, then initial()+noise on real
     * cells in (k, j, i) order; prim2cons/cons2prim run on the device. */

@@ -50,9 +50,12 @@ enum disco_status_code {
 enum disco_hydro_id   { DISCO_HYDRO_EULER = 0, DISCO_HYDRO_MHD = 1, DISCO_HYDRO_GRMHD = 2 };
 enum disco_initial_id { DISCO_IC_VORTEX_GAUSS = 0, DISCO_IC_DISK_MHD = 1,
                         DISCO_IC_DISK_PLANET = 2, DISCO_IC_DISK_CBD = 3,
-                        DISCO_IC_GR_DISK = 4 };
-/* GRMHD only: METRIC and FRAME of Makefile_opt.in (Hydro/Metric, Hydro/Frame) */
-enum disco_metric_id  { DISCO_METRIC_NONE = -1, DISCO_METRIC_SCHW_KS_RPZ = 0 };
+                        DISCO_IC_GR_DISK = 4, DISCO_IC_FM_TORUS = 5 };
+/* GRMHD only: METRIC and FRAME of Makefile_opt.in (Hydro/Metric, Hydro/Frame);
+ * kerr_ks_rpz is the Kerr metric (spin Metric_Par3) in the same Kerr-Schild
+ * cylindrical coordinates as the reference's schw_ks_rpz */
+enum disco_metric_id  { DISCO_METRIC_NONE = -1, DISCO_METRIC_SCHW_KS_RPZ = 0,
+                        DISCO_METRIC_KERR_KS_RPZ = 1 };
 enum disco_frame_id   { DISCO_FRAME_NONE = -1, DISCO_FRAME_NORMAL = 0 };
 enum disco_boundary_id{ DISCO_BC_FIXED = 0, DISCO_BC_FIXED3D = 1,
                         DISCO_BC_OUTFLOW3D = 2, DISCO_BC_ZEROGRAD = 3,
@@ -122,6 +125,7 @@ typedef struct disco_params {
    double coolPar1, coolPar2, coolPar3, coolPar4;            /* Cool_Par1..4 (sink.c:274) */
    double dampTimeInner, dampLenInner, dampTimeOuter, dampLenOuter,
           dampTimeUpper, dampLenUpper, dampTimeLower, dampLenLower;   /* Damp*_Time/_Len (sink.c:329) */
+   int maxNp;         /* Max_Np: cap on cells per ring (no reference key; 0 = none) */
 } disco_params;
 
 /* One point mass: the fields of struct planet (paul.h:259-284) the hot path
@@ -149,6 +153,8 @@ typedef struct disco_host_domain {
    double *prim;          /* [num_q*Ncell]: initial() (+ noise) for real cells */
    int Npl;
    disco_planet planets[DISCO_MAX_PLANETS];
+   double ic_aux[4];      /* constants the initial condition derives once at set-up
+                             (fm_torus: ell, F(r_in), h(r_pk) - 1, field scale) */
 } disco_host_domain;
 
 /* Host->device state snapshot, filled by disco_gpu_download(). Any pointer

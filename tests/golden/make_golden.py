@@ -77,6 +77,13 @@ CASES = {
     "cfg4_n12": ("configs/cfg4_grmhd_disk", {"Num_R": 12, "Num_Z": 4}, 5),
     # the same disk with the GRMHD ring diagnostics (Diagnostics/diag_grmhdmri.c)
     "cfg4_diag": ("configs/cfg4_grmhd_disk", {"Num_R": 12, "Num_Z": 4}, 5, {"ANALYSIS": "diag_grmhdmri"}),
+    # the Fishbone-Moncrief torus around a Kerr black hole (a = 0.9, Kerr-Schild
+    # cylindrical): the torus body at 16 x 4 rings, and the whole domain
+    # (atmosphere down to r = 2) at 24 x 12 rings; the reference's own
+    # Hydro/grmhd.c evaluated on the repository's Kerr metric plugin
+    "cfg4t_body": ("configs/cfg4_grmhd_torus", {"Num_R": 16, "Num_Z": 4, "R_Min": 8.0, "R_Max": 16.0,
+                                                "Z_Min": -2.0, "Z_Max": 2.0}, 5),
+    "cfg4t_n24": ("configs/cfg4_grmhd_torus", {"Num_R": 24, "Num_Z": 12}, 5),
 }
 
 

@@ -20,6 +20,9 @@ CASES = {"cfg1_n24": "configs/cfg1_vortex", "cfg2_n12": "configs/cfg2_mhd_disk",
          "cfg3_rk3": "configs/cfg3_planet_disk", "cfg3_cooldamp": "configs/cfg3_planet_disk",
          "cfg4_n12": "configs/cfg4_grmhd_disk",
          "cfg4_diag": "configs/cfg4_grmhd_disk",
+         # Fishbone-Moncrief torus around a Kerr black hole (a = 0.9)
+         "cfg4t_body": "configs/cfg4_grmhd_torus",
+         "cfg4t_n24": "configs/cfg4_grmhd_torus",
          "cfg1_zerograd": "configs/cfg1_vortex_zerograd",
          "cfg3_outflow": "configs/cfg3_planet_disk_outflow",
          # the other ghost-ring plugins on the 3D vortex (module text in the fixture)
@@ -27,7 +30,7 @@ CASES = {"cfg1_n24": "configs/cfg1_vortex", "cfg2_n12": "configs/cfg2_mhd_disk",
             for b in ("zerograd_omk", "zerograd_omIN", "accrete3d", "fixRrefZ", "polar3d", "fixed_gap",
                       "tube", "surfaceGravBox", "flowthrough")}}
 # GRMHD runs on the FP64 path only
-FP64_ONLY = {"cfg4_n12", "cfg4_diag"}
+FP64_ONLY = {"cfg4_n12", "cfg4_diag", "cfg4t_body", "cfg4t_n24"}
 
 
 def _domain(name, precision=0):

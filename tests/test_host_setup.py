@@ -50,8 +50,37 @@ def test_grmhd_disk_initial_state_bit_exact():
     assert np.max(np.abs(h.prim[:, real] - g["init_prim"][:, real])) < 1e-14
 
 
+@pytest.mark.parametrize("name", ["cfg4t_body", "cfg4t_n24"])
+def test_grmhd_torus_initial_state(name):
+    """Fishbone-Moncrief torus on the Kerr metric (kerr_ks_rpz, fm_torus):
+    grid and phases equal the reference build's, and so do the initial
+    primitives with the 4 % pressure noise drawn from the same rand()
+    stream, to the rounding of the reference's prim2cons / Newton
+    cons2prim round trip."""
+    dg = _dg()
+    g = load_golden(name)
+    p = dg.read_params(write_par(g["par_text"]))
+    m = dg.read_modules(os.path.join(ROOT, "configs/cfg4_grmhd_torus/Makefile_opt.in"))
+    assert (m.hydro, m.metric, m.initial) == (2, 1, 5)
+    h = dg.HostDomain(p, m)
+    assert np.array_equal(h.Np, g["Np"])
+    assert np.array_equal(h.piph, g["init_piph"])
+    real = g["real"].astype(bool)
+    # the reference's initial primitives are those of its prim2cons + Newton
+    # cons2prim round trip, which floors the torus-edge cells whose initial
+    # density is below Density_Floor; those are compared on the device
+    floor = float(p.Density_Floor)
+    ok = real & (g["init_prim"][0] > 10 * floor) & (h.prim[0] > 10 * floor)
+    assert ok.sum() > 0.3 * real.sum()
+    for q in range(h.prim.shape[0]):
+        ref = g["init_prim"][q, ok]
+        scale = np.abs(ref).max()
+        assert np.max(np.abs(h.prim[q, ok] - ref)) <= 1e-12 * max(scale, 1e-300), q
+
+
 def test_grmhd_unbuilt_metric_rejected(tmp_path):
-    """A metric other than schw_ks_rpz is refused at module selection."""
+    """A metric other than schw_ks_rpz / kerr_ks_rpz is refused at module
+    selection."""
     dg = _dg()
     src = open(os.path.join(ROOT, "configs/cfg4_grmhd_disk/Makefile_opt.in")).read()
     mk = tmp_path / "Makefile_opt.in"
