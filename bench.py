@@ -380,6 +380,61 @@ def measure_batch(args, wl):
     return res
 
 
+def measure_learned_c2p(args, wl, steps=None, warmup=None):
+    """GRMHD torus: the Newton cons2prim started from the previous
+    primitives (the reference's start) against the learned starting point.
+    One domain: W warm-up steps, K timed steps with the plain start; then
+    training pairs harvested from the running torus (every 8th real cell,
+    four steps), the MLP trained on the GPU, attached, and K more timed
+    steps.  Reports the mean iteration at first convergence (k_converge)
+    and the mean iterations per call of both, and both throughputs."""
+    import torch
+    import disco_gb300 as dg
+    K = steps or args.steps
+    W = warmup or args.warmup
+    cfg = os.path.join(ROOT, wl["dir"])
+    d = dg.Domain(os.path.join(cfg, "in.par"), os.path.join(cfg, "Makefile_opt.in"), precision=0,
+                  overrides=wl.get("overrides"))
+    cells = d.num_real_cells
+    d.run(W)
+    torch.cuda.synchronize()
+    d.c2p_stats(reset=True)
+    ms_plain = d.run_timed(K)
+    sp = d.c2p_stats(reset=True)
+    m = dg.Mlp(seed=1, capacity=1 << 21)
+    t0 = time.perf_counter()
+    for _ in range(4):
+        d.run(1)
+        held = m.harvest(d, stride=8)
+    t1 = time.perf_counter()
+    m.fit_norm()
+    l0, l1 = m.train(2000, batch=8192, lr=2e-3, seed=5)
+    t2 = time.perf_counter()
+    d.attach_guess(m)
+    d.run(1)
+    d.c2p_stats(reset=True)
+    ms_learned = d.run_timed(K)
+    sl = d.c2p_stats(reset=True)
+    st = d.status()
+    d.close()
+    m.close()
+    def mean(s, k):
+        return s[k] / s["calls"] if s["calls"] else None
+    kp, kl = mean(sp, "kconv"), mean(sl, "kconv")
+    return {"cells": cells, "steps": K,
+            "plain": {"zone_updates_per_s": cells * K / (ms_plain / 1e3), "ms_per_step": ms_plain / K,
+                      "mean_k_converge": kp, "mean_iterations": mean(sp, "iters"), "calls": sp["calls"]},
+            "learned": {"zone_updates_per_s": cells * K / (ms_learned / 1e3), "ms_per_step": ms_learned / K,
+                        "mean_k_converge": kl, "mean_iterations": mean(sl, "iters"), "calls": sl["calls"],
+                        "guess_used_fraction": sl["guessed"] / sl["calls"] if sl["calls"] else None},
+            "k_converge_ratio_plain_over_learned": (kp / kl) if kp and kl else None,
+            "training": {"pairs": held, "harvest_s": t1 - t0, "train_s": t2 - t1, "steps": 2000, "batch": 8192,
+                         "loss_first": l0, "loss_last": l1},
+            "c2p_no_converge": st["c2p_no_converge"],
+            "k_converge_definition": ("Newton iteration at which the relative change of eta first falls "
+                                      "below 1e-12 (the 10 polishing iterations that follow are not counted)")}
+
+
 def measure_ours(args, wl, rank):
     """One domain at a time (the large workloads do not fit twice in HBM):
     the mixed path first -- timing, per-kernel profile, its state kept on the
@@ -689,6 +744,8 @@ def main():
         pg = dist
         dist.barrier()
     res = measure_batch(args, wl) if wl.get("batch") else measure_ours(args, wl, rank)
+    if wl["dir"].endswith("cfg4_grmhd_torus"):
+        res["learned_c2p"] = measure_learned_c2p(args, wl)
     ch = res.get("chosen", 1)
     ms = res[ch]["ms"]
     if pg is not None:
@@ -769,6 +826,7 @@ def main():
                     for f, e in sorted(funcs.items(), key=lambda kv: -kv[1]["ms"])},
         "e2e": res["e2e"],
         **({"report_reduction": res["report"]} if "report" in res else {}),
+        **({"learned_c2p": res["learned_c2p"]} if "learned_c2p" in res else {}),
         "gpu_launches": int(res[ch]["launches"]),
         "clocks": res[ch]["clocks"],
     }

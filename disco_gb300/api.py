@@ -145,6 +145,20 @@ SIGNATURES = {
                                           C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     "disco_gpu_divb": (C.c_int, [_P, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     "disco_gpu_getmindt_noalloc": (C.c_int, [_P, C.POINTER(C.c_double)]),
+    "disco_mlp_create": (C.c_int, [C.c_ulonglong, C.c_long, C.POINTER(_P)]),
+    "disco_mlp_free": (None, [_P]),
+    "disco_mlp_harvest": (C.c_int, [_P, _P, C.c_int, C.POINTER(C.c_long)]),
+    "disco_mlp_pairs": (C.c_int, [_P, C.c_long, C.c_long, C.POINTER(C.c_float), C.POINTER(C.c_float)]),
+    "disco_mlp_fit_norm": (C.c_int, [_P]),
+    "disco_mlp_train": (C.c_int, [_P, C.c_int, C.c_int, C.c_float, C.c_ulonglong, C.POINTER(C.c_float),
+                                  C.POINTER(C.c_float)]),
+    "disco_mlp_grad": (C.c_int, [_P, C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_int, C.POINTER(C.c_float),
+                                 C.POINTER(C.c_float)]),
+    "disco_mlp_predict": (C.c_int, [_P, C.POINTER(C.c_float), C.c_long, C.POINTER(C.c_float)]),
+    "disco_mlp_params": (C.c_int, [_P, C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_float),
+                                   C.POINTER(C.c_float)]),
+    "disco_gpu_attach_guess": (C.c_int, [_P, _P]),
+    "disco_gpu_c2p_stats": (C.c_int, [_P, C.POINTER(C.c_longlong), C.c_int]),
     "disco_gpu_report": (C.c_int, [_P, C.POINTER(C.c_double), C.c_int]),
     "disco_gpu_diag_count": (C.c_int, [_P]),
     "disco_gpu_diag_download": (C.c_int, [_P, C.POINTER(C.c_double), C.c_longlong, C.POINTER(C.c_double)]),
@@ -342,6 +356,18 @@ class Domain:
         _check(lib().disco_gpu_divb(self._g, div.ctypes.data_as(dp), sc.ctypes.data_as(dp)), "disco_gpu_divb")
         return div, sc
 
+    def attach_guess(self, mlp) -> None:
+        """Start the GRMHD cons2prim from mlp's guess (None: from the previous
+        primitives only)."""
+        _check(lib().disco_gpu_attach_guess(self._g, None if mlp is None else mlp._m), "disco_gpu_attach_guess")
+
+    def c2p_stats(self, reset: bool = False) -> dict:
+        """Newton cons2prim counters: calls, summed k_converge, summed
+        iterations, calls started from the guess."""
+        out = (C.c_longlong * 4)()
+        _check(lib().disco_gpu_c2p_stats(self._g, out, int(reset)), "disco_gpu_c2p_stats")
+        return {"calls": out[0], "kconv": out[1], "iters": out[2], "guessed": out[3]}
+
     def timestep(self, dt: float) -> None:
         _check(lib().disco_gpu_timestep(self._g, float(dt)), "disco_gpu_timestep")
 
@@ -419,6 +445,90 @@ class Domain:
         if getattr(self, "_g", None):
             lib().disco_gpu_free(self._g)
             self._g = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+MLP_FEATURES, MLP_OUTPUTS, MLP_PARAMS, MLP_NORM = 8, 2, 5768, 20
+
+
+class Mlp:
+    """The learned starting point of the GRMHD Newton cons2prim
+    (include/disco_gpu_mlp.h): a 2 x 64 MLP trained and evaluated by the
+    library's BF16 tensor-core kernels."""
+
+    def __init__(self, seed: int = 1, capacity: int = 1 << 21):
+        m = C.c_void_p()
+        _check(lib().disco_mlp_create(int(seed), int(capacity), C.byref(m)), "disco_mlp_create")
+        self._m = m
+
+    def harvest(self, dom: "Domain", stride: int = 1) -> int:
+        """Append (features, converged solution) pairs of dom's current
+        state; returns the pairs held."""
+        n = C.c_long()
+        _check(lib().disco_mlp_harvest(self._m, dom._g, int(stride), C.byref(n)), "disco_mlp_harvest")
+        return n.value
+
+    def pairs(self, first: int, n: int) -> tuple:
+        X = np.zeros((n, MLP_FEATURES), np.float32)
+        Y = np.zeros((n, MLP_OUTPUTS), np.float32)
+        fp = C.POINTER(C.c_float)
+        _check(lib().disco_mlp_pairs(self._m, int(first), int(n), X.ctypes.data_as(fp), Y.ctypes.data_as(fp)),
+               "disco_mlp_pairs")
+        return X, Y
+
+    def fit_norm(self) -> None:
+        _check(lib().disco_mlp_fit_norm(self._m), "disco_mlp_fit_norm")
+
+    def train(self, steps: int, batch: int = 4096, lr: float = 1e-3, seed: int = 7) -> tuple:
+        """steps of Adam; returns (loss of the first batch, of the last)."""
+        a, b = C.c_float(), C.c_float()
+        _check(lib().disco_mlp_train(self._m, int(steps), int(batch), float(lr), int(seed), C.byref(a), C.byref(b)),
+               "disco_mlp_train")
+        return a.value, b.value
+
+    def grad(self, X: np.ndarray, Y: np.ndarray) -> tuple:
+        """(summed squared error, gradient of its mean) over given pairs."""
+        X = np.ascontiguousarray(X, np.float32)
+        Y = np.ascontiguousarray(Y, np.float32)
+        g = np.zeros(MLP_PARAMS, np.float32)
+        loss = C.c_float()
+        fp = C.POINTER(C.c_float)
+        _check(lib().disco_mlp_grad(self._m, X.ctypes.data_as(fp), Y.ctypes.data_as(fp), len(X), C.byref(loss),
+                                    g.ctypes.data_as(fp)), "disco_mlp_grad")
+        return loss.value, g
+
+    def predict(self, X: np.ndarray) -> np.ndarray:
+        X = np.ascontiguousarray(X, np.float32)
+        Y = np.zeros((len(X), MLP_OUTPUTS), np.float32)
+        fp = C.POINTER(C.c_float)
+        _check(lib().disco_mlp_predict(self._m, X.ctypes.data_as(fp), len(X), Y.ctypes.data_as(fp)),
+               "disco_mlp_predict")
+        return Y
+
+    def params(self) -> tuple:
+        p = np.zeros(MLP_PARAMS, np.float32)
+        nm = np.zeros(MLP_NORM, np.float32)
+        fp = C.POINTER(C.c_float)
+        _check(lib().disco_mlp_params(self._m, p.ctypes.data_as(fp), None, nm.ctypes.data_as(fp), None),
+               "disco_mlp_params")
+        return p, nm
+
+    def set_params(self, p=None, norm=None) -> None:
+        fp = C.POINTER(C.c_float)
+        pa = None if p is None else np.ascontiguousarray(p, np.float32)
+        na = None if norm is None else np.ascontiguousarray(norm, np.float32)
+        _check(lib().disco_mlp_params(self._m, None, None if pa is None else pa.ctypes.data_as(fp), None,
+                                      None if na is None else na.ctypes.data_as(fp)), "disco_mlp_params")
+
+    def close(self) -> None:
+        if getattr(self, "_m", None) is not None and self._m.value:
+            lib().disco_mlp_free(self._m)
+            self._m = C.c_void_p()
 
     def __del__(self):
         try:

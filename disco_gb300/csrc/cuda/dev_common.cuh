@@ -362,6 +362,27 @@ DISCO_D R get_height_om(const DevParams& P, const DevPlanet* pl, R r, R phi) {
 struct DevErrs {
   unsigned long long nan_cells, rho_floor_hits, p_floor_hits, face_errors, steps;
   unsigned long long c2p_no_converge;   // GRMHD Newton cons2prim at its iteration cap
+  // GRMHD Newton cons2prim: calls, the summed iteration at first convergence
+  // (k_converge), the summed iterations taken, and the calls whose starting
+  // point came from a supplied guess instead of the previous primitives
+  unsigned long long c2p_calls, c2p_kconv, c2p_iters, c2p_guessed;
 };
+
+#ifdef __CUDACC__
+// Adds one cons2prim record to the counters, one atomic per warp for each
+// (the calling threads may be any subset of the warp).
+__device__ inline void c2p_count(DevErrs* e, int kconv, int iters, int guessed) {
+  const unsigned m = __activemask();
+  const unsigned kc = __reduce_add_sync(m, (unsigned)kconv);
+  const unsigned it = __reduce_add_sync(m, (unsigned)iters);
+  const unsigned gs = __reduce_add_sync(m, (unsigned)guessed);
+  if ((threadIdx.x & 31) == (unsigned)(__ffs(m) - 1)) {
+    atomicAdd(&e->c2p_calls, (unsigned long long)__popc(m));
+    atomicAdd(&e->c2p_kconv, (unsigned long long)kc);
+    atomicAdd(&e->c2p_iters, (unsigned long long)it);
+    if (gs) atomicAdd(&e->c2p_guessed, (unsigned long long)gs);
+  }
+}
+#endif
 
 }  // namespace disco

@@ -6,6 +6,10 @@
 #include "disco_gpu_batch.h"
 #include "disco_gpu_report.h"
 #include "disco_gpu_diag.h"
+#include "disco_gpu_mlp.h"
+#include "mlp_train.cuh"
+
+#include <cmath>
 
 std::atomic<long long> g_launches{0};
 long long disco_gpu_launch_count(void) { return g_launches.load(); }
@@ -105,7 +109,281 @@ static int batch_steps(disco_batch* b, int nsteps, size_t flush_bytes, double* m
   return 0;
 }
 
+// The cons2prim MLP: FP32 masters with Adam moments and gradient, BF16
+// copies, the standardisation, the harvested training pairs and the batch
+// buffers of training.
+struct disco_mlp {
+  cudaStream_t st = nullptr;
+  float *p = nullptr, *m1 = nullptr, *m2 = nullptr, *grad = nullptr, *loss = nullptr;
+  disco::bf16 *W1b = nullptr, *W2b = nullptr, *W3b = nullptr;
+  float norm[DISCO_MLP_NORM];
+  float *X = nullptr, *Y = nullptr;
+  long cap = 0, held = 0;
+  unsigned long long* count = nullptr;
+  disco::MlpBatch bt{};
+  long bcap = 0;
+  long long step = 0;
+  ~disco_mlp() {
+    for (void* q : {(void*)p, (void*)m1, (void*)m2, (void*)grad, (void*)loss, (void*)W1b, (void*)W2b, (void*)W3b,
+                    (void*)X, (void*)Y, (void*)count})
+      if (q) cudaFree(q);
+    free_batch();
+    if (st) cudaStreamDestroy(st);
+  }
+  void free_batch() {
+    for (void* q : {(void*)bt.X, (void*)bt.dY, (void*)bt.H1, (void*)bt.H2, (void*)bt.Z1, (void*)bt.Z2})
+      if (q) cudaFree(q);
+    bt = disco::MlpBatch{};
+    bcap = 0;
+  }
+  int ensure_batch(long B) {
+    if (B <= bcap) return 0;
+    free_batch();
+    const long n = (B + 63) / 64 * 64;
+    CK(cudaMalloc(&bt.X, sizeof(disco::bf16) * n * 16));
+    CK(cudaMalloc(&bt.dY, sizeof(disco::bf16) * n * 16));
+    CK(cudaMalloc(&bt.H1, sizeof(disco::bf16) * n * 64));
+    CK(cudaMalloc(&bt.H2, sizeof(disco::bf16) * n * 64));
+    CK(cudaMalloc(&bt.Z1, sizeof(disco::bf16) * n * 64));
+    CK(cudaMalloc(&bt.Z2, sizeof(disco::bf16) * n * 64));
+    bcap = n;
+    return 0;
+  }
+  disco::MlpDev view() const {
+    disco::MlpDev v;
+    v.W1b = W1b; v.W2b = W2b; v.W3b = W3b; v.params = p;
+    for (int q = 0; q < 8; ++q) { v.xm[q] = norm[q]; v.xs[q] = norm[8 + q]; }
+    for (int q = 0; q < 2; ++q) { v.ym[q] = norm[16 + q]; v.ys[q] = norm[18 + q]; }
+    return v;
+  }
+  int refresh_bf16() {
+    disco::k_mlp_bf16<<<16, 256, 0, st>>>(p, W1b, W2b, W3b);
+    ++g_launches;
+    CK(cudaGetLastError());
+    return 0;
+  }
+  // forward + backward over a batch: grad (mean over the batch) and the
+  // summed loss, on the stream
+  int fwd_bwd(const float* Xd, const float* Yd, long n, int B, unsigned long long seed) {
+    int rc = ensure_batch(B);
+    if (rc) return rc;
+    CK(cudaMemsetAsync(grad, 0, sizeof(float) * DISCO_MLP_PARAMS, st));
+    CK(cudaMemsetAsync(loss, 0, sizeof(float), st));
+    const disco::MlpDev v = view();
+    disco::k_mlp_fwdbwd<<<(B + 63) / 64, 128, 0, st>>>(v, Xd, Yd, n, B, seed, bt, loss);
+    disco::k_mlp_wgrad<<<(B + disco::kWgSamples - 1) / disco::kWgSamples, 320, 0, st>>>(bt, B, grad);
+    g_launches += 2;
+    CK(cudaGetLastError());
+    return 0;
+  }
+};
+
+static unsigned long long mlp_splitmix(unsigned long long& x) {
+  unsigned long long z = (x += 0x9E3779B97F4A7C15ull);
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+
 extern "C" {
+
+int disco_mlp_create(unsigned long long seed, long capacity, disco_mlp** out) {
+  if (!out || capacity < 0) { disco_set_error("disco_mlp_create: bad argument"); return DISCO_E_ARG; }
+  disco_mlp* m = new disco_mlp();
+  auto fail = [&](int rc) { delete m; return rc; };
+  if (cudaStreamCreateWithFlags(&m->st, cudaStreamNonBlocking) != cudaSuccess) {
+    disco_set_error("disco_mlp_create: no stream");
+    return fail(DISCO_E_CUDA);
+  }
+  const size_t np = DISCO_MLP_PARAMS;
+  if (cudaMalloc(&m->p, 4 * np) || cudaMalloc(&m->m1, 4 * np) || cudaMalloc(&m->m2, 4 * np) ||
+      cudaMalloc(&m->grad, 4 * np) || cudaMalloc(&m->loss, 4) || cudaMalloc(&m->W1b, 2 * 64 * 16) ||
+      cudaMalloc(&m->W2b, 2 * 64 * 64) || cudaMalloc(&m->W3b, 2 * 16 * 64) || cudaMalloc(&m->count, 8) ||
+      cudaMalloc(&m->X, 4 * (size_t)std::max(capacity, 1L) * DISCO_MLP_FEATURES) ||
+      cudaMalloc(&m->Y, 4 * (size_t)std::max(capacity, 1L) * DISCO_MLP_OUTPUTS)) {
+    disco_set_error("disco_mlp_create: device allocation failed");
+    return fail(DISCO_E_NOMEM);
+  }
+  m->cap = capacity;
+  // Xavier-uniform weights, zero biases (inputs 8..15 of W1 and rows 2..7
+  // of W3 stay zero)
+  std::vector<float> h(np, 0.f);
+  unsigned long long s = seed;
+  auto fill = [&](int off, int nout, int nin, int ld, int fan_in, int fan_out) {
+    const double a = sqrt(6.0 / (double)(fan_in + fan_out));
+    for (int o = 0; o < nout; ++o)
+      for (int i = 0; i < nin; ++i) {
+        const double u = (double)(mlp_splitmix(s) >> 11) * (1.0 / 9007199254740992.0);
+        h[off + o * ld + i] = (float)((2.0 * u - 1.0) * a);
+      }
+  };
+  fill(disco::kOffW1, 64, DISCO_MLP_FEATURES, 16, DISCO_MLP_FEATURES, 64);
+  fill(disco::kOffW2, 64, 64, 64, 64, 64);
+  fill(disco::kOffW3, DISCO_MLP_OUTPUTS, 64, 64, 64, DISCO_MLP_OUTPUTS);
+  for (int q = 0; q < 8; ++q) { m->norm[q] = 0.f; m->norm[8 + q] = 1.f; }
+  for (int q = 0; q < 2; ++q) { m->norm[16 + q] = 0.f; m->norm[18 + q] = 1.f; }
+  if (cudaMemcpy(m->p, h.data(), 4 * np, cudaMemcpyHostToDevice) || cudaMemset(m->m1, 0, 4 * np) ||
+      cudaMemset(m->m2, 0, 4 * np) || cudaMemset(m->count, 0, 8)) {
+    disco_set_error("disco_mlp_create: upload failed");
+    return fail(DISCO_E_CUDA);
+  }
+  int rc = m->refresh_bf16();
+  if (!rc && cudaStreamSynchronize(m->st) != cudaSuccess) rc = DISCO_E_CUDA;
+  if (rc) return fail(rc);
+  *out = m;
+  return 0;
+}
+
+void disco_mlp_free(disco_mlp* m) { delete m; }
+
+int disco_mlp_harvest(disco_mlp* m, disco_gpu* g, int stride, long* count) {
+  if (!m || !g) { disco_set_error("disco_mlp_harvest: null argument"); return DISCO_E_ARG; }
+  int rc = g->impl->harvest(stride, m->X, m->Y, m->cap, m->count);
+  if (rc) return rc;
+  unsigned long long c = 0;
+  CK(cudaMemcpy(&c, m->count, 8, cudaMemcpyDeviceToHost));
+  m->held = (long)std::min<unsigned long long>(c, (unsigned long long)m->cap);
+  if (count) *count = m->held;
+  return 0;
+}
+
+int disco_mlp_pairs(disco_mlp* m, long first, long n, float* X, float* Y) {
+  if (!m || first < 0 || n < 0 || first + n > m->held) { disco_set_error("disco_mlp_pairs: bad range"); return DISCO_E_ARG; }
+  if (X) CK(cudaMemcpy(X, m->X + first * DISCO_MLP_FEATURES, 4 * (size_t)n * DISCO_MLP_FEATURES, cudaMemcpyDeviceToHost));
+  if (Y) CK(cudaMemcpy(Y, m->Y + first * DISCO_MLP_OUTPUTS, 4 * (size_t)n * DISCO_MLP_OUTPUTS, cudaMemcpyDeviceToHost));
+  return 0;
+}
+
+int disco_mlp_fit_norm(disco_mlp* m) {
+  if (!m || m->held < 2) { disco_set_error("disco_mlp_fit_norm: fewer than two pairs held"); return DISCO_E_STATE; }
+  const long n = m->held;
+  std::vector<float> X((size_t)n * DISCO_MLP_FEATURES), Y((size_t)n * DISCO_MLP_OUTPUTS);
+  int rc = disco_mlp_pairs(m, 0, n, X.data(), Y.data());
+  if (rc) return rc;
+  auto stats = [&](const std::vector<float>& a, int dim, int q, float* mean, float* sd) {
+    double s = 0, s2 = 0;
+    for (long i = 0; i < n; ++i) s += a[(size_t)i * dim + q];
+    const double mu = s / n;
+    for (long i = 0; i < n; ++i) { const double d = a[(size_t)i * dim + q] - mu; s2 += d * d; }
+    const double sdv = sqrt(s2 / n);
+    *mean = (float)mu;
+    *sd = (float)(sdv > 1e-6 ? sdv : 1.0);
+  };
+  for (int q = 0; q < 8; ++q) stats(X, 8, q, &m->norm[q], &m->norm[8 + q]);
+  for (int q = 0; q < 2; ++q) stats(Y, 2, q, &m->norm[16 + q], &m->norm[18 + q]);
+  return 0;
+}
+
+int disco_mlp_train(disco_mlp* m, int steps, int batch, float lr, unsigned long long seed, float* loss_first,
+                    float* loss_last) {
+  if (!m || steps < 0 || batch < 16 || !(lr > 0.f)) { disco_set_error("disco_mlp_train: bad argument"); return DISCO_E_ARG; }
+  if (m->held < 1) { disco_set_error("disco_mlp_train: no training pairs held"); return DISCO_E_STATE; }
+  const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
+  for (int k = 0; k < steps; ++k) {
+    const unsigned long long sd = seed + (unsigned long long)m->step * (unsigned long long)batch;
+    int rc = m->fwd_bwd(m->X, m->Y, m->held, batch, sd == ~0ull ? sd - 1 : sd);
+    if (rc) return rc;
+    if (k == 0 && loss_first) {
+      CK(cudaMemcpyAsync(loss_first, m->loss, 4, cudaMemcpyDeviceToHost, m->st));
+      CK(cudaStreamSynchronize(m->st));
+      *loss_first /= (float)(batch * DISCO_MLP_OUTPUTS);
+    }
+    ++m->step;
+    const float bc1 = 1.f - powf(b1, (float)m->step), bc2 = 1.f - powf(b2, (float)m->step);
+    disco::k_mlp_adam<<<(DISCO_MLP_PARAMS + 255) / 256, 256, 0, m->st>>>(m->p, m->m1, m->m2, m->grad, lr, b1, b2,
+                                                                         eps, bc1, bc2);
+    ++g_launches;
+    rc = m->refresh_bf16();
+    if (rc) return rc;
+  }
+  if (loss_last) {
+    CK(cudaMemcpyAsync(loss_last, m->loss, 4, cudaMemcpyDeviceToHost, m->st));
+    CK(cudaStreamSynchronize(m->st));
+    *loss_last /= (float)(batch * DISCO_MLP_OUTPUTS);
+  }
+  CK(cudaStreamSynchronize(m->st));
+  CK(cudaGetLastError());
+  return 0;
+}
+
+int disco_mlp_grad(disco_mlp* m, const float* X, const float* Y, int n, float* loss, float* grad) {
+  if (!m || !X || !Y || n < 1 || !grad) { disco_set_error("disco_mlp_grad: bad argument"); return DISCO_E_ARG; }
+  float *dX = nullptr, *dY = nullptr;
+  int rc = 0;
+  if (cudaMalloc(&dX, 4 * (size_t)n * DISCO_MLP_FEATURES) != cudaSuccess ||
+      cudaMalloc(&dY, 4 * (size_t)n * DISCO_MLP_OUTPUTS) != cudaSuccess) {
+    if (dX) cudaFree(dX);
+    disco_set_error("disco_mlp_grad: device allocation failed");
+    return DISCO_E_NOMEM;
+  }
+  if (cudaMemcpy(dX, X, 4 * (size_t)n * DISCO_MLP_FEATURES, cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMemcpy(dY, Y, 4 * (size_t)n * DISCO_MLP_OUTPUTS, cudaMemcpyHostToDevice) != cudaSuccess) {
+    rc = DISCO_E_CUDA;
+  }
+  if (!rc) rc = m->fwd_bwd(dX, dY, n, n, ~0ull);
+  if (!rc) {
+    if (cudaMemcpyAsync(grad, m->grad, 4 * DISCO_MLP_PARAMS, cudaMemcpyDeviceToHost, m->st) != cudaSuccess ||
+        (loss && cudaMemcpyAsync(loss, m->loss, 4, cudaMemcpyDeviceToHost, m->st) != cudaSuccess) ||
+        cudaStreamSynchronize(m->st) != cudaSuccess)
+      rc = DISCO_E_CUDA;
+  }
+  cudaFree(dX);
+  cudaFree(dY);
+  if (rc == DISCO_E_CUDA) disco_set_error("disco_mlp_grad: CUDA error");
+  return rc;
+}
+
+int disco_mlp_predict(disco_mlp* m, const float* X, long n, float* Y) {
+  if (!m || !X || !Y || n < 0) { disco_set_error("disco_mlp_predict: bad argument"); return DISCO_E_ARG; }
+  if (n == 0) return 0;
+  float *dX = nullptr, *dY = nullptr;
+  if (cudaMalloc(&dX, 4 * (size_t)n * DISCO_MLP_FEATURES) != cudaSuccess ||
+      cudaMalloc(&dY, 4 * (size_t)n * DISCO_MLP_OUTPUTS) != cudaSuccess) {
+    if (dX) cudaFree(dX);
+    disco_set_error("disco_mlp_predict: device allocation failed");
+    return DISCO_E_NOMEM;
+  }
+  cudaError_t e = cudaMemcpyAsync(dX, X, 4 * (size_t)n * DISCO_MLP_FEATURES, cudaMemcpyHostToDevice, m->st);
+  if (e == cudaSuccess) {
+    disco::k_mlp_predict<<<(unsigned)((n + 127) / 128), 128, 0, m->st>>>(m->view(), dX, n, dY);
+    ++g_launches;
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpyAsync(Y, dY, 4 * (size_t)n * DISCO_MLP_OUTPUTS, cudaMemcpyDeviceToHost, m->st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(m->st);
+  cudaFree(dX);
+  cudaFree(dY);
+  CK(e);
+  return 0;
+}
+
+int disco_mlp_params(disco_mlp* m, float* get, const float* set, float* norm_get, const float* norm_set) {
+  if (!m) { disco_set_error("disco_mlp_params: null model"); return DISCO_E_ARG; }
+  CK(cudaStreamSynchronize(m->st));
+  if (get) CK(cudaMemcpy(get, m->p, 4 * DISCO_MLP_PARAMS, cudaMemcpyDeviceToHost));
+  if (norm_get) memcpy(norm_get, m->norm, sizeof m->norm);
+  if (norm_set) memcpy(m->norm, norm_set, sizeof m->norm);
+  if (set) {
+    CK(cudaMemcpy(m->p, set, 4 * DISCO_MLP_PARAMS, cudaMemcpyHostToDevice));
+    int rc = m->refresh_bf16();
+    if (rc) return rc;
+    CK(cudaStreamSynchronize(m->st));
+  }
+  return 0;
+}
+
+int disco_gpu_attach_guess(disco_gpu* g, disco_mlp* m) {
+  if (!g) { disco_set_error("disco_gpu_attach_guess: null instance"); return DISCO_E_ARG; }
+  if (!m) return g->impl->attach_guess(nullptr);
+  CK(cudaStreamSynchronize(m->st));
+  const disco::MlpDev v = m->view();
+  return g->impl->attach_guess(&v);
+}
+
+int disco_gpu_c2p_stats(disco_gpu* g, long long out[4], int reset) {
+  if (!g || !out) { disco_set_error("disco_gpu_c2p_stats: bad argument"); return DISCO_E_ARG; }
+  return g->impl->c2p_stats(out, reset);
+}
 
 int disco_gpu_create(const disco_host_domain* dom, int precision, disco_gpu** out) {
   if (!dom || !out) { disco_set_error("disco_gpu_create: null argument"); return DISCO_E_ARG; }

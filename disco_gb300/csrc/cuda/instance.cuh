@@ -19,6 +19,7 @@
 #include "report.cuh"
 #include "diag.cuh"
 #include "checks.cuh"
+#include "mlp_c2p.cuh"
 #include "../plugins/bc_plugins.h"
 
 using namespace disco;
@@ -55,6 +56,11 @@ struct InstanceBase {
                           int* LRtype, double* phic, double* dA) = 0;
   virtual int debug_grad(double* gp, double* gr, double* gz) = 0;
   virtual int divb(double* div, double* scale) = 0;
+  // GRMHD cons2prim with a learned starting point (mlp.cuh): attach (null
+  // detaches), harvest training pairs, read / reset the iteration counters
+  virtual int attach_guess(const MlpDev* m) = 0;
+  virtual int harvest(int stride, float* X, float* Y, long cap, unsigned long long* count) = 0;
+  virtual int c2p_stats(long long* out, int reset) = 0;
   virtual int getmindt_noalloc(double* dt) = 0;
   virtual int report(double* out, int nout) = 0;
   virtual int diag(int op, double* Qrz, long long n, double* t_avg, const double* set, double set_t) = 0;
@@ -668,7 +674,8 @@ struct Instance : InstanceBase {
       }
     }
     {
-      const int c2p = ct ? 0 : 1;
+      // GRMHD with a learned starting point: calc_prim is its own pass below
+      const int c2p = (ct || mlp_on) ? 0 : 1;
       const dim3 g((unsigned)blocks(N));
       if (P.cool_damp && mid) LAUNCH("update", (k_update<Phys, R, NQ, true, true><<<g, 256, 0, st>>>(P, S, RK, fac, first, c2p)));
       else if (P.cool_damp)   LAUNCH("update", (k_update<Phys, R, NQ, true, false><<<g, 256, 0, st>>>(P, S, RK, fac, first, c2p)));
@@ -680,6 +687,8 @@ struct Instance : InstanceBase {
       set_piph(parity);
       LAUNCH("after_first", (k_after_first<<<1, 1, 0, st>>>(P, S.scal, S.planets, planets_id, S.errs)));
     }
+    if constexpr (Phys::GR)
+      if (mlp_on) LAUNCH("c2p_guess", (k_c2p_guess<Phys, R, NQ><<<blocks(N), 256, 0, st>>>(P, S, mlp)));
     if (ct) {   // flips (first substep), B_faces_to_cells, calc_prim (onestep.c:270-296)
       if (first)
         for (int d = 0; d < 2; ++d)
@@ -930,6 +939,48 @@ struct Instance : InstanceBase {
     if (Phi) CK(cudaMemcpy(Phi, C.Phi, sizeof(double) * 5 * N, cudaMemcpyDeviceToHost));
     return 0;
   }
+  // ---- learned starting point of the GRMHD cons2prim ----------------------
+  MlpDev mlp{};
+  bool mlp_on = false;
+  int attach_guess(const MlpDev* m) override {
+    if (!Phys::GR) {
+      disco_set_error("a cons2prim guess is built for the GRMHD module only");
+      return DISCO_E_MODULE;
+    }
+    mlp_on = m != nullptr;
+    if (m) mlp = *m;
+    for (int i = 0; i < 2; ++i)   // the step graphs bake the calc_prim launches in
+      if (graph[i]) { cudaGraphExecDestroy(graph[i]); graph[i] = nullptr; }
+    return 0;
+  }
+  int harvest(int stride, float* X, float* Y, long cap, unsigned long long* count) override {
+    if constexpr (Phys::GR) {
+      if (stride < 1) { disco_set_error("harvest: stride must be >= 1"); return DISCO_E_ARG; }
+      const long n = (N + stride - 1) / stride;
+      LAUNCH("c2p_harvest", (k_c2p_harvest<Phys, R, NQ><<<blocks(n), 256, 0, st>>>(P, S, stride, X, Y, cap, count)));
+      CK(cudaGetLastError());
+      CK(cudaStreamSynchronize(st));
+      return 0;
+    } else {
+      (void)stride; (void)X; (void)Y; (void)cap; (void)count;
+      disco_set_error("harvest: cons2prim pairs come from the GRMHD module only");
+      return DISCO_E_MODULE;
+    }
+  }
+  // out = {calls, summed k_converge, summed iterations, calls started from the guess}
+  int c2p_stats(long long* out, int reset) override {
+    DevErrs h;
+    CK(cudaStreamSynchronize(st));
+    CK(cudaMemcpy(&h, S.errs, sizeof h, cudaMemcpyDeviceToHost));
+    out[0] = (long long)h.c2p_calls; out[1] = (long long)h.c2p_kconv;
+    out[2] = (long long)h.c2p_iters; out[3] = (long long)h.c2p_guessed;
+    if (reset) {
+      h.c2p_calls = h.c2p_kconv = h.c2p_iters = h.c2p_guessed = 0;
+      CK(cudaMemcpy(S.errs, &h, sizeof h, cudaMemcpyHostToDevice));
+    }
+    return 0;
+  }
+
   // Face tables of one dimension as the device holds them (test access).
   int debug_faces(int dim, int* npair_out, long* nface_out, int* fIndex, int* L, int* Rr,
                   int* LRtype, double* phic, double* dA) override {

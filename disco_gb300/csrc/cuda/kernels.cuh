@@ -1453,7 +1453,9 @@ __global__ void __launch_bounds__(256, kMix<R> ? 4 : 1) k_update(DevParams P, De
 #pragma unroll
         for (int q = 0; q < NQ; ++q) pr[q] = S.prim[q * N + c];
         const double xg[3] = {r, .5 * (phim + piph), .5 * (zp + zm)};
-        hits = Phys::cons2prim_x(P, U, pr, xg, dV);
+        typename Phys::C2PRec rec;
+        hits = Phys::cons2prim_x(P, U, pr, xg, dV, nullptr, &rec);
+        c2p_count(S.errs, rec.kconv, rec.iters, rec.guessed);
       } else {
         hits = Phys::cons2prim(P, S.planets, U, pr, r, .5 * (phim + piph), dV);
       }
@@ -1823,7 +1825,9 @@ DISCO_D void c2p_cell(const DevParams& P, const DevState<R>& S, int c, int jk, i
 #pragma unroll
       for (int q = 0; q < NQ; ++q) pr[q] = S.prim[q * N + c];
       const double xg[3] = {r, .5 * (phim + piph), .5 * (zp + zm)};
-      hits = Phys::cons2prim_x(P, U, pr, xg, dV);
+      typename Phys::C2PRec rec;
+      hits = Phys::cons2prim_x(P, U, pr, xg, dV, nullptr, &rec);
+      c2p_count(S.errs, rec.kconv, rec.iters, rec.guessed);
     } else {
       hits = Phys::cons2prim(P, S.planets, U, pr, r, .5 * (phim + piph), dV);
     }

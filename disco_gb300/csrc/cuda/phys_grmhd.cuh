@@ -366,58 +366,75 @@ struct Grmhd {
     cons[TAU] += g.jac * S0 * dVdt;
   }
 
-  // cons2prim (grmhd.c:228-245) with cons2prim_solve_adiabatic_noble2d
-  // (:813-1029): 2D Newton-Raphson of Noble et al. (2006) on (v^2, eta),
-  // seeded from the previous primitives in prim (in/out), at most 30
-  // iterations, 10 more after the relative change of eta drops below 1e-12.
-  // Returns the floor-hit mask (1 density, 2 pressure), 4 if the iteration
-  // hit its cap.
-  DISCO_D static int cons2prim_x(const DevParams& P, const double* cons_in, double* prim, const double* x,
-                                 double dV) {
-    double cons[NQ];
-#pragma unroll
-    for (int q = 0; q < NQ; ++q) cons[q] = cons_in[q] / dV;
+  // ---- cons2prim (grmhd.c:228-245, cons2prim_solve_adiabatic_noble2d
+  // :813-1029) in three parts: the invariants of the conserved state, a
+  // Newton-Raphson solve of Noble et al. (2006)'s two equations in
+  // (v^2, eta) from a given starting point, and the recovery of the
+  // primitives.  FP64; each formula keeps the reference's operation order.
+
+  // What the two Noble equations depend on: s2 = S^2 / D^2, the energy e,
+  // Q = sqrt(gamma) B^2 / D and psi = sqrt(gamma) (B.S)^2 / D^3, with
+  // n = (gamma_law - 1) / gamma_law.  Kept with the pieces the recovery uses.
+  struct C2PInv {
+    double D, S[3], B[3], B2, BS, s2, e, Q, psi, n, sqrtgam, r;
+  };
+
+  DISCO_D static void c2p_invariants(const DevParams& P, const double* cons, const KsMetric& g, double r,
+                                     C2PInv& v) {
+    v.r = r;
+    v.D = cons[DDD];
+    v.S[0] = cons[SRR]; v.S[1] = cons[LLL]; v.S[2] = cons[SZZ];
+    const double tau = cons[TAU];
+    v.sqrtgam = g.jac / g.al;
+    double U[4];
+    ks_frame_U(g, U);
+    v.B[0] = r * cons[BRR] / v.sqrtgam; v.B[1] = cons[BPP] / v.sqrtgam; v.B[2] = cons[BZZ] / v.sqrtgam;
+    double s2 = 0.0, Us = 0.0, BS = 0.0, B2 = 0.0;
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) s2 += g.igam[3 * i + j] * v.S[i] * v.S[j];
+    s2 /= v.D * v.D;
+    for (int i = 0; i < 3; ++i) Us += v.S[i] * (g.be[i] * U[0] + U[i + 1]);
+    Us /= v.D;
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) B2 += g.gam[3 * i + j] * v.B[i] * v.B[j];
+    for (int i = 0; i < 3; ++i) BS += v.B[i] * v.S[i];
+    v.s2 = s2;
+    v.B2 = B2;
+    v.BS = BS;
+    v.Q = v.sqrtgam * B2 / v.D;
+    v.psi = v.sqrtgam * BS * BS / (v.D * v.D * v.D);
+    v.e = (tau / v.D + Us + 1.0) / (g.al * U[0]);
+    v.n = (P.gamma_law - 1.0) / P.gamma_law;
+  }
+
+  // The two residuals at (v2, eta), each relative to the term it balances.
+  DISCO_D static double c2p_residual(const C2PInv& v, double v2, double eta) {
+    if (!(v2 >= 0.0 && v2 < 1.0 && eta >= 1.0)) return 1.0e300;
+    const double w = 1.0 / sqrt(1.0 - v2);
+    const double Q = v.Q, psi = v.psi;
+    const double fa = (eta + Q) * (eta + Q) * v2 - psi * (2 * eta + Q) / (eta * eta) - v.s2;
+    const double fb = eta - v.n * (1 - v2) * (eta - w) + 0.5 * Q * (1 + v2) - 0.5 * psi / (eta * eta) - v.e;
+    const double r = fabs(fa) / ((eta + Q) * (eta + Q)) + fabs(fb) / eta;
+    return r == r ? r : 1.0e300;
+  }
+
+  // Newton-Raphson from (v20, eta0): at most 30 iterations, 10 more after
+  // the relative change of eta first falls below 1e-12.  Returns the status
+  // word: 4 if the iteration hit its cap.  *kconv = the iteration at which
+  // the change first fell below the tolerance (0 if it never did), *iters =
+  // the iterations taken.
+  DISCO_D static int noble2d_solve(const C2PInv& v, double v20, double eta0, double* v2_out, double* eta_out,
+                                   int* kconv, int* iters) {
     const double prec = 1.0e-12;
     const int max_iter = 30;
     const int Nextra = 10;
-    const double r = x[0];
-    const double D = cons[DDD];
-    const double S[3] = {cons[SRR], cons[LLL], cons[SZZ]};
-    const double tau = cons[TAU];
-    KsMetric g(x, P.gr_M, P.gr_a, P.gr_kerr);
-    const double sqrtgam = g.jac / g.al;
-    double U[4];
-    ks_frame_U(g, U);
-    const double B[3] = {r * cons[BRR] / sqrtgam, cons[BPP] / sqrtgam, cons[BZZ] / sqrtgam};
-    double s2 = 0.0, Us = 0.0, BS = 0.0, B2 = 0.0;
-    for (int i = 0; i < 3; ++i)
-      for (int j = 0; j < 3; ++j) s2 += g.igam[3 * i + j] * S[i] * S[j];
-    s2 /= D * D;
-    for (int i = 0; i < 3; ++i) Us += S[i] * (g.be[i] * U[0] + U[i + 1]);
-    Us /= D;
-    for (int i = 0; i < 3; ++i)
-      for (int j = 0; j < 3; ++j) B2 += g.gam[3 * i + j] * B[i] * B[j];
-    const double Q = sqrtgam * B2 / D;
-    for (int i = 0; i < 3; ++i) BS += B[i] * S[i];
-    const double psi = sqrtgam * BS * BS / (D * D * D);
-    const double gl = P.gamma_law;
-    const double e = (tau / D + Us + 1.0) / (g.al * U[0]);
-    const double n = (gl - 1.0) / gl;
-
-    // initial guess: the previous v^2 and eta
-    double u2 = 0.0;
-    double l[3] = {prim[URR], r * r * prim[UPP], prim[UZZ]};
-    for (int i = 0; i < 3; ++i)
-      for (int j = 0; j < 3; ++j) u2 += g.igam[3 * i + j] * l[i] * l[j];
-    double w = sqrt(1.0 + u2);
-    const double v20 = u2 / (1.0 + u2);
-    const double eta0 = w * (1.0 + gl / (gl - 1.0) * prim[PPP] / prim[RHO]);
+    const double Q = v.Q, psi = v.psi, s2 = v.s2, e = v.e, n = v.n;
     double v2, v21 = v20, eta, eta1 = eta0;
-    int it = 0, clean = -1;
+    int it = 0, clean = -1, kc = 0;
     while (1) {
       v2 = v21;
       eta = eta1;
-      w = 1.0 / sqrt(1.0 - v2);
+      const double w = 1.0 / sqrt(1.0 - v2);
       const double fa = (eta + Q) * (eta + Q) * v2 - psi * (2 * eta + Q) / (eta * eta) - s2;
       const double fb = eta - n * (1 - v2) * (eta - w) + 0.5 * Q * (1 + v2) - 0.5 * psi / (eta * eta) - e;
       const double dfadv2 = (eta + Q) * (eta + Q);
@@ -432,29 +449,58 @@ struct Grmhd {
       if (v21 < 0.0) v21 = 0.5 * v2;
       if (eta1 < 1.0) eta1 = 0.5 * (eta + 1.0);
       const double err = (eta1 - eta) / eta;
-      if (fabs(err) < prec && clean < 0) clean = Nextra + 1;
+      if (fabs(err) < prec && clean < 0) {
+        clean = Nextra + 1;
+        kc = it;
+      }
       if (clean >= 0) clean--;
       if (clean == 0 || it == max_iter) break;
     }
-    int hits = it == max_iter ? 4 : 0;
-    v2 = v21;
-    eta = eta1;
-    // primitive recovery
-    w = 1.0 / sqrt(1 - v2);
+    *v2_out = v21;
+    *eta_out = eta1;
+    *kconv = kc;
+    *iters = it;
+    return it == max_iter ? 4 : 0;
+  }
+
+  // The starting point the reference uses: the previous primitives' v^2 and
+  // eta = W h.
+  DISCO_D static void c2p_warm_start(const DevParams& P, const KsMetric& g, const double* prim, double r,
+                                     double* v20, double* eta0) {
+    double u2 = 0.0;
+    const double l[3] = {prim[URR], r * r * prim[UPP], prim[UZZ]};
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) u2 += g.igam[3 * i + j] * l[i] * l[j];
+    const double w = sqrt(1.0 + u2);
+    const double gl = P.gamma_law;
+    *v20 = u2 / (1.0 + u2);
+    *eta0 = w * (1.0 + gl / (gl - 1.0) * prim[PPP] / prim[RHO]);
+  }
+
+  // Primitives from the converged (v2, eta); returns the floor-hit mask
+  // (1 density, 2 pressure).
+  DISCO_D static int c2p_recover(const DevParams& P, const KsMetric& g, const C2PInv& v, const double* cons,
+                                 double v2, double eta, double* prim) {
+    int hits = 0;
+    const double gl = P.gamma_law, r = v.r, D = v.D, sqrtgam = v.sqrtgam;
+    const double w = 1.0 / sqrt(1 - v2);
     const double u0 = w / g.al;
     double h = eta / w;
     double rho = D / (g.jac * u0);
     if (rho < P.rho_floor) { rho = P.rho_floor; hits |= 1; }
-    double Pp = n * rho * (h - 1.0);
+    double Pp = v.n * rho * (h - 1.0);
     if (Pp < P.p_floor * rho) { Pp = P.p_floor * rho; hits |= 2; }
     h = 1.0 + gl / (gl - 1.0) * Pp / rho;
+    const double* B = v.B;
     double Bd[3];
     Bd[0] = g.gam[0] * B[0] + g.gam[1] * B[1] + g.gam[2] * B[2];
     Bd[1] = g.gam[3] * B[0] + g.gam[4] * B[1] + g.gam[5] * B[2];
     Bd[2] = g.gam[6] * B[0] + g.gam[7] * B[1] + g.gam[8] * B[2];
-    l[0] = (S[0] + sqrtgam * BS * Bd[0] / (D * h * w)) / (D * h + sqrtgam * B2 / w);
-    l[1] = (S[1] + sqrtgam * BS * Bd[1] / (D * h * w)) / (D * h + sqrtgam * B2 / w);
-    l[2] = (S[2] + sqrtgam * BS * Bd[2] / (D * h * w)) / (D * h + sqrtgam * B2 / w);
+    const double BS = v.BS, B2 = v.B2;
+    double l[3];
+    l[0] = (v.S[0] + sqrtgam * BS * Bd[0] / (D * h * w)) / (D * h + sqrtgam * B2 / w);
+    l[1] = (v.S[1] + sqrtgam * BS * Bd[1] / (D * h * w)) / (D * h + sqrtgam * B2 / w);
+    l[2] = (v.S[2] + sqrtgam * BS * Bd[2] / (D * h * w)) / (D * h + sqrtgam * B2 / w);
     prim[RHO] = rho;
     prim[URR] = l[0];
     prim[UPP] = l[1] / (r * r);
@@ -466,6 +512,73 @@ struct Grmhd {
 #pragma unroll
     for (int q = NC; q < NQ; ++q) prim[q] = cons[q] / cons[DDD];
     return hits;
+  }
+
+  // The eight features of the learned starting point: the Noble invariants
+  // (log e, log s2, log Q, the squared cosine between B and S), the rest
+  // mass log D, the lapse, log r and log |e^2 - s2|.
+  DISCO_D static void c2p_features(const C2PInv& v, const KsMetric& g, float* f) {
+    f[0] = logf((float)fmax(v.e, 1.0e-30));
+    f[1] = logf((float)(v.s2 + 1.0e-20));
+    f[2] = logf((float)(v.Q + 1.0e-20));
+    f[3] = (float)(v.psi / (v.Q * v.s2 + 1.0e-30));
+    f[4] = logf((float)fmax(v.D, 1.0e-30));
+    f[5] = (float)g.al;
+    f[6] = logf((float)v.r);
+    f[7] = logf((float)(fabs(v.e * v.e - v.s2) + 1.0e-20));
+  }
+  // Targets from a converged (v2, eta): log(W^2 - 1) and log(P / rho).
+  DISCO_D static void c2p_targets(const C2PInv& v, double v2, double eta, float* y) {
+    const double u2 = v2 / (1.0 - v2);
+    const double w = sqrt(1.0 + u2);
+    const double th = v.n * (eta / w - 1.0);
+    y[0] = logf((float)fmax(u2, 1.0e-30));
+    y[1] = logf((float)fmax(th, 1.0e-30));
+  }
+  // The starting point (v2, eta) the outputs describe: W^2 - 1 = exp(y0),
+  // P / rho = exp(y1), eta = W h with h = 1 + gamma / (gamma - 1) P / rho.
+  DISCO_D static void c2p_guess_from(const C2PInv& v, const float* y, double* g2) {
+    const double u2 = exp((double)y[0]);
+    const double th = exp((double)y[1]);
+    g2[0] = u2 / (1.0 + u2);
+    g2[1] = sqrt(1.0 + u2) * (1.0 + th / v.n);
+  }
+
+  // Per-call record of the solve: iteration at first convergence, the
+  // iterations taken, and whether a supplied guess replaced the warm start.
+  struct C2PRec {
+    int kconv, iters, guessed;
+  };
+
+  // cons2prim at x: the conserved state cons_in (times dV) to prim (in: the
+  // previous primitives, the warm start; out: the new ones).  guess, when
+  // given, is a starting point (v^2, eta) that replaces the warm start if
+  // its residual is the smaller (the warm start stays the fallback).
+  // Returns the status word: 1 density floor, 2 pressure floor, 4 Newton
+  // cap.
+  DISCO_D static int cons2prim_x(const DevParams& P, const double* cons_in, double* prim, const double* x,
+                                 double dV, const double* guess = nullptr, C2PRec* rec = nullptr) {
+    double cons[NQ];
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) cons[q] = cons_in[q] / dV;
+    const double r = x[0];
+    KsMetric g(x, P.gr_M, P.gr_a, P.gr_kerr);
+    C2PInv v;
+    c2p_invariants(P, cons, g, r, v);
+    double v20, eta0;
+    c2p_warm_start(P, g, prim, r, &v20, &eta0);
+    int guessed = 0;
+    if (guess && c2p_residual(v, guess[0], guess[1]) < c2p_residual(v, v20, eta0)) {
+      v20 = guess[0];
+      eta0 = guess[1];
+      guessed = 1;
+    }
+    double v2, eta;
+    int kc, it;
+    int status = noble2d_solve(v, v20, eta0, &v2, &eta, &kc, &it);
+    status |= c2p_recover(P, g, v, cons, v2, eta, prim);
+    if (rec) { rec->kconv = kc; rec->iters = it; rec->guessed = guessed; }
+    return status;
   }
 
   // mindt, grmhd.c:648-721 (wc: the cell's mesh angular velocity)

@@ -7,8 +7,10 @@ FP64 centroid phi and area) equal the reference bit for bit; the mixed path
 keeps the integer tables bit-exact too.  Gradients of the initial state and
 the face fluxes Phi after the steps are within 1e-12 relative L1 (FP64).
 Constrained transport keeps the divergence of every cell's face fluxes at
-its initial value to roundoff away from the inner radial boundary, where the
-device reproduces the reference's own change."""
+its initial value to roundoff away from the inner radial boundary (FP64
+roundoff on the plain path, the FP32 rounding of the edge EMFs on the mixed
+path), and next to that boundary the device reproduces the reference's own
+change."""
 import numpy as np
 import pytest
 
@@ -75,6 +77,8 @@ def test_face_tables_after_steps_match_oracle(name):
         # transcendentals (gravity, the exact mesh rotation) differ from
         # glibc's, so a sliver face's area is compared against the largest
         # face's, not its own
+        if len(ref["dA"]) == 0:   # a 2D domain has no z faces
+            continue
         assert np.allclose(dev["phic"], ref["phic"], rtol=0, atol=1e-13), key
         assert np.max(np.abs(dev["dA"] - ref["dA"])) <= 1e-13 * np.abs(ref["dA"]).max(), key
     d.close()
@@ -165,5 +169,7 @@ def test_divb_stays_at_roundoff(name, precision):
     assert np.max(np.abs(change - ochange)) < tol
     jk = np.repeat(np.arange(h.Nr * h.Nz), h.Np)
     away = (jk % h.Nr >= h.NgRa + 3)[ev]
-    assert np.abs(change[away]).max() < (1e-13 if precision == 0 else 1e-12), np.abs(change[away]).max()
+    # the mixed path adds FP32 edge EMFs (times dl dt) to FP64 face fluxes:
+    # its divergence is held to FP32 rounding of those increments
+    assert np.abs(change[away]).max() < (1e-13 if precision == 0 else 1e-8), np.abs(change[away]).max()
     d.close()

@@ -1,0 +1,114 @@
+"""The learned starting point of the GRMHD Newton cons2prim on the device.
+
+* The tensor-core training kernels' gradient and the inference kernel's
+  outputs against the oracle's FP64 restatement (oracle/mlp_ref.py) with the
+  same BF16 roundings of the operands.
+* Training on (features, converged solution) pairs harvested from the Kerr
+  torus reduces the loss.
+* With the trained network attached, the Newton iteration converges to the
+  same primitives (relative L1 1e-13 per component after the steps) and the
+  mean iteration at first convergence (k_converge) is reported against the
+  reference's own start, the previous primitives."""
+import numpy as np
+import pytest
+
+from oracle import mlp_ref
+from test_gpu_parity import _domain
+
+pytestmark = pytest.mark.gpu
+
+
+def _rel_l2(a, b):
+    n = np.linalg.norm(b)
+    return float(np.linalg.norm(a - b) / (n if n > 0 else 1.0))
+
+
+def _random_norm(rng):
+    return np.concatenate([rng.normal(0, 1, 8), rng.uniform(0.5, 2, 8), rng.normal(0, 1, 2),
+                           rng.uniform(0.5, 2, 2)]).astype(np.float32)
+
+
+def test_mlp_gradient_matches_restatement():
+    import disco_gb300 as dg
+    rng = np.random.default_rng(5)
+    m = dg.Mlp(seed=11, capacity=16)
+    p, _ = m.params()
+    norm = _random_norm(rng)
+    m.set_params(norm=norm)
+    n = 333                                      # not a multiple of the 16-sample tile
+    X = (rng.normal(0, 1.5, (n, 8)) * norm[8:16] + norm[:8]).astype(np.float32)
+    Y = (rng.normal(0, 1.5, (n, 2)) * norm[18:20] + norm[16:18]).astype(np.float32)
+    loss, g = m.grad(X, Y)
+    l_ref, g_ref, _ = mlp_ref.forward_backward(p, norm, X, Y, bf16=True)
+    assert loss == pytest.approx(l_ref, rel=1e-3)
+    gd, gr = mlp_ref.unpack(g), mlp_ref.unpack(g_ref)
+    errs = {k: _rel_l2(gd[k], gr[k]) for k in gr}
+    print("relative L2 error of the device gradient per parameter block:", errs)
+    for k, e in errs.items():
+        assert e < 1e-2, (k, e)
+    # and against the plain FP64 network: the BF16 operands cost little
+    _, g64, _ = mlp_ref.forward_backward(p, norm, X, Y, bf16=False)
+    assert _rel_l2(g, g64) < 5e-2
+    m.close()
+
+
+def test_mlp_inference_matches_restatement():
+    import disco_gb300 as dg
+    rng = np.random.default_rng(6)
+    m = dg.Mlp(seed=12, capacity=16)
+    p, _ = m.params()
+    norm = _random_norm(rng)
+    m.set_params(norm=norm)
+    X = (rng.normal(0, 1.5, (1000, 8)) * norm[8:16] + norm[:8]).astype(np.float32)
+    Yd = m.predict(X)
+    _, _, Yr = mlp_ref.forward_backward(p, norm, X, np.zeros((1000, 2)), bf16=True)
+    for o in range(2):   # in standardised units
+        yd = (Yd[:, o] - norm[16 + o]) / norm[18 + o]
+        yr = (Yr[:, o] - norm[16 + o]) / norm[18 + o]
+        assert np.max(np.abs(yd - yr)) <= 2e-3 * max(1.0, np.abs(yr).max()), o
+    m.close()
+
+
+def _harvest_and_train(m, steps=8, train_steps=1500):
+    d, _ = _domain("cfg4t_n24", 0)
+    for _ in range(steps):
+        d.timestep(d.getmindt())
+        m.harvest(d)
+    d.close()
+    m.fit_norm()
+    return m.train(train_steps, batch=4096, lr=2e-3, seed=3)
+
+
+def test_training_reduces_loss_and_guess_keeps_the_solution():
+    import disco_gb300 as dg
+    m = dg.Mlp(seed=13, capacity=1 << 20)
+    l0, l1 = _harvest_and_train(m)
+    print("loss: first batch", l0, "last batch", l1)
+    assert l1 < 0.1 * l0
+    # the same torus from the same start: the reference's start (plain)
+    # against the learned one, the same dt sequence
+    a, g = _domain("cfg4t_n24", 0)
+    b, _ = _domain("cfg4t_n24", 0)
+    b.attach_guess(m)
+    a.c2p_stats(reset=True)
+    b.c2p_stats(reset=True)
+    for _ in range(3):
+        dt = a.getmindt()
+        a.timestep(dt)
+        b.timestep(dt)
+    sa, sb = a.c2p_stats(), b.c2p_stats()
+    print("plain:", sa, "learned:", sb)
+    assert sa["calls"] == sb["calls"] > 0
+    ka, kb = sa["kconv"] / sa["calls"], sb["kconv"] / sb["calls"]
+    print(f"mean k_converge: plain {ka:.3f}, learned {kb:.3f}, ratio {ka / kb:.3f}; "
+          f"guess used in {sb['guessed'] / sb['calls']:.3f} of the calls")
+    assert sb["guessed"] > 0
+    assert kb <= ka
+    pa, pb = a.state()["prim"], b.state()["prim"]
+    real = g["real"].astype(bool)
+    for q in range(pa.shape[0]):
+        den = np.abs(pa[q, real]).sum()
+        if den > 0:
+            assert np.abs(pb[q, real] - pa[q, real]).sum() <= 1e-13 * den, q
+    assert a.status()["c2p_no_converge"] == b.status()["c2p_no_converge"]
+    a.close(); b.close(); m.close()
