@@ -112,7 +112,8 @@ class DiscoKernelTime(C.Structure):
 class DiscoGpuErrs(C.Structure):
     _fields_ = [("nan_cells", C.c_longlong), ("rho_floor_hits", C.c_longlong),
                 ("p_floor_hits", C.c_longlong), ("face_errors", C.c_longlong),
-                ("steps", C.c_longlong), ("c2p_no_converge", C.c_longlong)]
+                ("steps", C.c_longlong), ("c2p_no_converge", C.c_longlong),
+                ("async_timeouts", C.c_longlong)]
 
 
 # Every symbol include/*.h declares, with its ctypes signature.
@@ -130,6 +131,7 @@ SIGNATURES = {
     "disco_gpu_download": (C.c_int, [_P, C.POINTER(DiscoStateView)]),
     "disco_gpu_upload": (C.c_int, [_P, C.POINTER(DiscoStateView)]),
     "disco_gpu_status": (C.c_int, [_P, C.POINTER(DiscoGpuErrs)]),
+    "disco_gpu_planets": (C.c_int, [_P, C.POINTER(DiscoPlanet), C.c_int, C.POINTER(C.c_int)]),
     "disco_gpu_run_timed": (C.c_int, [_P, C.c_int, C.c_double, C.c_size_t, C.POINTER(C.c_double)]),
     "disco_gpu_profile": (C.c_int, [_P, C.c_int, C.POINTER(DiscoKernelTime), C.c_int,
                                     C.POINTER(C.c_int)]),
@@ -144,6 +146,7 @@ SIGNATURES = {
                                           C.POINTER(C.c_float), C.POINTER(C.c_float),
                                           C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     "disco_gpu_divb": (C.c_int, [_P, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
+    "disco_gpu_debug_sweep": (C.c_int, [_P, C.c_int]),
     "disco_gpu_getmindt_noalloc": (C.c_int, [_P, C.POINTER(C.c_double)]),
     "disco_mlp_create": (C.c_int, [C.c_ulonglong, C.c_long, C.POINTER(_P)]),
     "disco_mlp_free": (None, [_P]),
@@ -346,6 +349,13 @@ class Domain:
                "disco_gpu_debug_grad")
         return out
 
+    def set_sweep(self, on: bool) -> bool:
+        """Staged phi sweep (True) or separate plm_phi / flux_phi kernels;
+        returns the setting in force (disco_gpu_debug_sweep)."""
+        rc = lib().disco_gpu_debug_sweep(self._g, int(on))
+        _check(rc if rc < 0 else 0, "disco_gpu_debug_sweep")
+        return bool(rc)
+
     def divb(self) -> tuple:
         """(div, scale) per cell: net outward face flux of B and the sum of
         the absolute face fluxes (disco_gpu_divb); scale < 0 marks cells
@@ -435,6 +445,13 @@ class Domain:
                 keep.append(a)
                 setattr(v, k, a.ctypes.data_as(dp))
         _check(lib().disco_gpu_upload(self._g, C.byref(v)), "disco_gpu_upload")
+
+    def planets(self) -> list:
+        """The point masses as the device has advanced them."""
+        out = (DiscoPlanet * 4)()
+        n = C.c_int()
+        _check(lib().disco_gpu_planets(self._g, out, 4, C.byref(n)), "disco_gpu_planets")
+        return [{k: getattr(out[i], k) for k, _ in DiscoPlanet._fields_} for i in range(min(n.value, 4))]
 
     def status(self) -> dict:
         e = DiscoGpuErrs()

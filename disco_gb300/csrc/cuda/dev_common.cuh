@@ -366,6 +366,7 @@ struct DevErrs {
   // (k_converge), the summed iterations taken, and the calls whose starting
   // point came from a supplied guess instead of the previous primitives
   unsigned long long c2p_calls, c2p_kconv, c2p_iters, c2p_guessed;
+  unsigned long long async_timeouts;   // bounded waits on asynchronous copies that ran out
 };
 
 #ifdef __CUDACC__

@@ -459,6 +459,10 @@ int disco_gpu_profile(disco_gpu* g, int nsteps, disco_kernel_time* out, int max_
   if (!g || !out || !n_out || nsteps < 0) { disco_set_error("bad argument"); return DISCO_E_ARG; }
   return g->impl->profile(nsteps, out, max_out, n_out);
 }
+int disco_gpu_planets(disco_gpu* g, disco_planet* out, int max, int* n) {
+  if (!g || !n || (max > 0 && !out) || max < 0) { disco_set_error("disco_gpu_planets: bad argument"); return DISCO_E_ARG; }
+  return g->impl->planets(out, max, n);
+}
 int disco_gpu_status(disco_gpu* g, disco_gpu_errs* e) {
   if (!g || !e) { disco_set_error("null argument"); return DISCO_E_ARG; }
   return g->impl->status(e);
@@ -475,6 +479,10 @@ int disco_gpu_debug_faces(disco_gpu* g, int dim, int* npair, long* nface, int* f
 int disco_gpu_debug_grad(disco_gpu* g, double* gradp, double* gradr, double* gradz) {
   if (!g) { disco_set_error("null argument"); return DISCO_E_ARG; }
   return g->impl->debug_grad(gradp, gradr, gradz);
+}
+int disco_gpu_debug_sweep(disco_gpu* g, int on) {
+  if (!g) { disco_set_error("null argument"); return DISCO_E_ARG; }
+  return g->impl->set_sweep(on);
 }
 int disco_gpu_divb(disco_gpu* g, double* div, double* scale) {
   if (!g) { disco_set_error("null argument"); return DISCO_E_ARG; }

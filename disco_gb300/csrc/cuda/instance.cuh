@@ -20,6 +20,7 @@
 #include "diag.cuh"
 #include "checks.cuh"
 #include "mlp_c2p.cuh"
+#include "phi_sweep.cuh"
 #include "../plugins/bc_plugins.h"
 
 using namespace disco;
@@ -56,6 +57,8 @@ struct InstanceBase {
                           int* LRtype, double* phic, double* dA) = 0;
   virtual int debug_grad(double* gp, double* gr, double* gz) = 0;
   virtual int divb(double* div, double* scale) = 0;
+  virtual int planets(disco_planet* out, int max, int* n) = 0;
+  virtual int set_sweep(int on) = 0;
   // GRMHD cons2prim with a learned starting point (mlp.cuh): attach (null
   // detaches), harvest training pairs, read / reset the iteration counters
   virtual int attach_guess(const MlpDev* m) = 0;
@@ -558,8 +561,26 @@ struct Instance : InstanceBase {
     launch_faces();
     CK(cudaGetLastError());
     CK(cudaStreamSynchronize(st));
+    // the staged phi sweep of the mixed path (not with explicit viscosity,
+    // whose phi fluxes read the transverse gradients of plm_trans)
+    if (kMix<R> && !P.include_viscosity) {
+      sweep = make_sweep_tmap(&tm_prim, (const float*)S.prim, (unsigned long long)NQ * N) == 0 &&
+              make_sweep_tmap(&tm_dphi, (const float*)S.dphi_r, (unsigned long long)N) == 0;
+      sweep_ok = sweep;
+    }
     return 0;
   }
+  bool sweep_ok = false;   // the tensor maps exist
+  // test access: the staged sweep on (1) or the separate plm_phi / flux_phi
+  // kernels (0); returns the setting in force
+  int set_sweep(int on) override {
+    sweep = on && sweep_ok;
+    for (int i = 0; i < 2; ++i)
+      if (graph[i]) { cudaGraphExecDestroy(graph[i]); graph[i] = nullptr; }
+    return sweep ? 1 : 0;
+  }
+  bool sweep = false;   // k_phi_sweep in place of k_plm_phi + k_flux_phi
+  CUtensorMap tm_prim{}, tm_dphi{};
 
   // ---- launch helpers -----------------------------------------------------
   void sync_dphi_r() {
@@ -654,9 +675,17 @@ struct Instance : InstanceBase {
   // first nor the last (RK3's second)
   void substep(double RK, double fac, int first, int mid = 0) {
     if (first) launch_wcell();
-    LAUNCH("plm_phi", (k_plm_phi<R, NQ><<<blocks(N), 256, 0, st>>>(P, S)));
-    launch_plm_trans();
-    LAUNCH("flux_phi", (k_flux_phi<Phys, R, NQ><<<blocks(N), 256, 0, st>>>(P, S, fac)));
+    if constexpr (kMix<R>) {
+      if (sweep) {   // plm_phi and the phi fluxes from one staged pass
+        LAUNCH("phi_sweep", (k_phi_sweep<Phys, R, NQ><<<S.nchunk, kTileCells, 0, st>>>(P, S, fac, tm_prim, tm_dphi)));
+        launch_plm_trans();
+      }
+    }
+    if (!sweep) {
+      LAUNCH("plm_phi", (k_plm_phi<R, NQ><<<blocks(N), 256, 0, st>>>(P, S)));
+      launch_plm_trans();
+      LAUNCH("flux_phi", (k_flux_phi<Phys, R, NQ><<<blocks(N), 256, 0, st>>>(P, S, fac)));
+    }
     launch_trans_fluxes(fac);
     if (ct) {   // avg_Efields, subtract_advective_B_fluxes, update_B_fluxes (onestep.c:261-265)
       LAUNCH("ct_gather", (k_ct_gather<R><<<blocks(N), 256, 0, st>>>(P, S, C)));
@@ -939,6 +968,18 @@ struct Instance : InstanceBase {
     if (Phi) CK(cudaMemcpy(Phi, C.Phi, sizeof(double) * 5 * N, cudaMemcpyDeviceToHost));
     return 0;
   }
+  int planets(disco_planet* out, int max, int* n) override {
+    std::vector<DevPlanet> pl(MAX_PL);
+    CK(cudaStreamSynchronize(st));
+    CK(cudaMemcpy(pl.data(), S.planets, sizeof(DevPlanet) * MAX_PL, cudaMemcpyDeviceToHost));
+    *n = P.Npl;
+    for (int i = 0; i < P.Npl && i < max && i < MAX_PL; ++i) {
+      out[i].r = pl[i].r; out[i].phi = pl[i].phi; out[i].M = pl[i].M; out[i].omega = pl[i].omega;
+      out[i].vr = pl[i].vr; out[i].eps = pl[i].eps; out[i].type = pl[i].type;
+    }
+    return 0;
+  }
+
   // ---- learned starting point of the GRMHD cons2prim ----------------------
   MlpDev mlp{};
   bool mlp_on = false;
@@ -1121,6 +1162,7 @@ struct Instance : InstanceBase {
     e->face_errors = (long long)h.face_errors;
     e->steps = (long long)h.steps;
     e->c2p_no_converge = (long long)h.c2p_no_converge;
+    e->async_timeouts = (long long)h.async_timeouts;
     if (ct) {
       unsigned long long ce = 0;
       CK(cudaMemcpy(&ce, C.errs, 8, cudaMemcpyDeviceToHost));

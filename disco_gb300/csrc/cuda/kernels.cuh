@@ -1012,17 +1012,15 @@ DISCO_D void cool_damp_src(const DevParams& P, const DevPlanet* pl, const R* pri
 // their natural 70+; the FP64 versions would spill, so they are not capped.
 
 // ---- phi fluxes, misc.c:378-436 + riemann_phi, riemann.c:39-112 -------------
+// The phi face between cell c and its successor cp of ring jk (j, k), from
+// their primitives pC, pP, phi gradients gC, gP and widths dL, dR: the
+// reconstruction, the Riemann solve, the face flux into fphi and, with
+// constrained transport, the edge EMFs.  Shared by k_flux_phi and the
+// staged sweep k_phi_sweep.
 template <typename Phys, typename R, int NQ>
-__global__ void __launch_bounds__(256, kMix<R> ? 4 : 1) k_flux_phi(DevParams P, DevState<R> S, double fac) {
-  int c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= S.N) return;
-  int jk = S.cell_ring[c];
-  int k = div_fast(jk, P.mul_nr), j = jk - k * P.Nr;
-  if (S.ct ? !ring_in_phi_range(P, j, k) : !is_real(P, j, k)) return;
+DISCO_D void flux_phi_face(const DevParams& P, const DevState<R>& S, double fac, int c, int cp, int jk, int j, int k,
+                           const R* pC, const R* pP, const R* gC, const R* gP, R dL, R dR) {
   const int N = S.N;
-  int off = S.ring_off[jk], Np = S.ring_off[jk + 1] - off;
-  int i = c - off;
-  int cp = off + (i < Np - 1 ? i + 1 : 0);
   R r, dAdt_r = 0;
   double dAdt = 0;
   if constexpr (kMix<R>) {
@@ -1039,12 +1037,11 @@ __global__ void __launch_bounds__(256, kMix<R> ? 4 : 1) k_flux_phi(DevParams P, 
   // the face angle enters the Riemann solver through the viscous flux only
   double phi = P.include_viscosity ? S.piph[c] : 0.0;
   R primL[NQ], primR[NQ], gp[NQ], gLr[NQ], gLz[NQ], gRr[NQ], gRz[NQ];
-  R dL = S.dphi_r[c], dR = S.dphi_r[cp];
 #pragma unroll
   for (int q = 0; q < NQ; ++q) {
-    R pL = S.prim[q * N + c], pR = S.prim[q * N + cp];
-    primL[q] = pL + (R).5 * S.gradp[q * N + c] * dL;
-    primR[q] = pR - (R).5 * S.gradp[q * N + cp] * dR;
+    R pL = pC[q], pR = pP[q];
+    primL[q] = pL + (R).5 * gC[q] * dL;
+    primR[q] = pR - (R).5 * gP[q] * dR;
     gp[q] = (pR - pL) / ((R)0.5 * (dR + dL));
   }
   if (P.include_viscosity) {
@@ -1105,6 +1102,26 @@ __global__ void __launch_bounds__(256, kMix<R> ? 4 : 1) k_flux_phi(DevParams P, 
     S.Eraw[4 * N + c] = hEr; S.Eraw[5 * N + c] = hEr; S.Eraw[6 * N + cp] = hEr; S.Eraw[7 * N + cp] = hEr;
     S.Braw[4 * N + c] = hBz; S.Braw[5 * N + c] = hBz; S.Braw[6 * N + cp] = hBz; S.Braw[7 * N + cp] = hBz;
   }
+}
+
+template <typename Phys, typename R, int NQ>
+__global__ void __launch_bounds__(256, kMix<R> ? 4 : 1) k_flux_phi(DevParams P, DevState<R> S, double fac) {
+  int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= S.N) return;
+  int jk = S.cell_ring[c];
+  int k = div_fast(jk, P.mul_nr), j = jk - k * P.Nr;
+  if (S.ct ? !ring_in_phi_range(P, j, k) : !is_real(P, j, k)) return;
+  const int N = S.N;
+  int off = S.ring_off[jk], Np = S.ring_off[jk + 1] - off;
+  int i = c - off;
+  int cp = off + (i < Np - 1 ? i + 1 : 0);
+  R pC[NQ], pP[NQ], gC[NQ], gP[NQ];
+#pragma unroll
+  for (int q = 0; q < NQ; ++q) {
+    pC[q] = S.prim[q * N + c]; pP[q] = S.prim[q * N + cp];
+    gC[q] = S.gradp[q * N + c]; gP[q] = S.gradp[q * N + cp];
+  }
+  flux_phi_face<Phys, R, NQ>(P, S, fac, c, cp, jk, j, k, pC, pP, gC, gP, S.dphi_r[c], S.dphi_r[cp]);
 }
 
 // ---- r/z fluxes, misc.c:441-519 + riemann_trans, riemann.c:114-214 ----------

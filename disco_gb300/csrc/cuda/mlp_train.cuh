@@ -48,7 +48,7 @@ static __global__ void __launch_bounds__(128) k_mlp_fwdbwd(MlpDev m, const float
   const int tile = blockIdx.x * 4 + wid;
   if (tile * 16 >= B) return;   // whole warps leave together
   const int s0 = tile * 16;
-  long row[2] = {0, 0};
+  long row[2] = {0, 0};   // the data rows of this lane's two tile rows (read only below B)
   for (int h = 0; h < 2; ++h) {
     const int s = s0 + g + 8 * h;
     row[h] = seed == ~0ull ? (long)s : (long)(mlp_mix(seed + (unsigned long long)s) % (unsigned long long)n);
@@ -57,8 +57,9 @@ static __global__ void __launch_bounds__(128) k_mlp_fwdbwd(MlpDev m, const float
     const int s = s0 + lane;
     const long r = seed == ~0ull ? (long)s : (long)(mlp_mix(seed + (unsigned long long)s) % (unsigned long long)n);
     float f[kMlpIn];
+    if (s < B)   // a partial last tile's padding rows read nothing
 #pragma unroll
-    for (int q = 0; q < kMlpIn; ++q) f[q] = Xd[r * kMlpIn + q];
+      for (int q = 0; q < kMlpIn; ++q) f[q] = Xd[r * kMlpIn + q];
     mlp_put_row(m, &Xs[wid][lane * kLdX], f, s < B);
     // the BF16 row for the first layer's weight gradient
 #pragma unroll

@@ -175,6 +175,8 @@ typedef struct disco_gpu_errs {
    long long steps;           /* timesteps taken on the device */
    long long c2p_no_converge; /* GRMHD: Newton cons2prim stopped at max_iter = 30
                                  (grmhd.c:959-968, which prints and continues) */
+   long long async_timeouts;  /* bounded waits for asynchronous (TMA) copies
+                                 that ran out; the block then skips its work */
 } disco_gpu_errs;
 
 typedef struct disco_gpu disco_gpu;   /* opaque device instance */
@@ -243,6 +245,12 @@ int disco_gpu_profile(disco_gpu *g, int nsteps, disco_kernel_time *out,
                       int max_out, int *n_out);
 
 int disco_gpu_status(disco_gpu *g, disco_gpu_errs *errs);
+
+/* The point masses as the device has advanced them (the analytic orbits of
+ * planet.c:236-270, Planets/circular.c, Planets/cm.c): copies min(Npl, max)
+ * entries to out; *n = Npl.  The reference keeps them in
+ * theDomain->thePlanets, which report() and the checkpoint read. */
+int disco_gpu_planets(disco_gpu *g, disco_planet *out, int max, int *n);
 double disco_gpu_time(disco_gpu *g);
 long disco_gpu_num_cells(disco_gpu *g);       /* total incl. ghosts */
 long disco_gpu_num_real_cells(disco_gpu *g);  /* interior cells */

@@ -43,6 +43,13 @@ int disco_gpu_debug_faces(disco_gpu *g, int dim, int *npair, long *nface,
  * state is left unchanged, so stepping may continue. */
 int disco_gpu_debug_grad(disco_gpu *g, double *gradp, double *gradr, double *gradz);
 
+/* The mixed path's azimuthal sweep: on != 0 selects the staged single-pass
+ * kernel (k_phi_sweep, the default where it applies), 0 the separate
+ * plm_phi and phi-flux kernels, for tests that compare the two.  Returns
+ * the setting in force (0 where the staged sweep does not apply: the plain
+ * FP64 path, explicit viscosity). */
+int disco_gpu_debug_sweep(disco_gpu *g, int on);
+
 /* Applies the library's integer-pipe FP64 -> FP32 and FP32 -> FP64
  * conversions and the hardware's (cvt.rn.f32.f64, cvt.f64.f32) to n values
  * on the current device: f_int/f_hw[i] from in[i], d_int/d_hw[i] from

@@ -23,6 +23,20 @@
 #include "paul.h"
 #include <time.h>
 
+#ifdef GB300
+/* the reference-side binding of libdisco_gb300 (gb300_shim.c): getmindt
+ * and timestep run on the GPU; these hooks create the device instance and
+ * copy its state back before anything reads theDomain */
+void gb300_init(struct domain *);
+void gb300_sync_to_host(struct domain *);
+void gb300_free(void);
+#define GB300_INIT(d) gb300_init(d)
+#define GB300_SYNC(d) gb300_sync_to_host(d)
+#else
+#define GB300_INIT(d) ((void)0)
+#define GB300_SYNC(d) ((void)0)
+#endif
+
 int mpiSetup(struct domain *, int, char *[]);
 void setupGrid(struct domain *);
 void timestep(struct domain *, double);
@@ -148,6 +162,7 @@ int main(int argc, char **argv)
    struct domain theDomain = {0};
    struct domain *d = &theDomain;
    init_domain(d, 1, argv);
+   GB300_INIT(d);
 
    const char *mode = argv[1];
    if(strcmp(mode, "init") == 0) {
@@ -191,6 +206,7 @@ int main(int argc, char **argv)
       fprintf(stderr, "{\"cells\": %ld, \"steps\": %d, \"seconds\": %.6f, "
               "\"zone_updates_per_s\": %.6e}\n", ncells, nsteps, t1 - t0,
               (double)ncells*nsteps/(t1 - t0));
+      GB300_SYNC(d);
       if(strcmp(mode, "run") == 0) {
          FILE *f = fopen(argv[3], "wb");
          write_state(d, f, 0);
