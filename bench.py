@@ -384,9 +384,9 @@ def measure_learned_c2p(args, wl, steps=None, warmup=None):
     """GRMHD torus: the Newton cons2prim started from the previous
     primitives (the reference's start) against the learned starting point.
     One domain: W warm-up steps, K timed steps with the plain start; then
-    training pairs harvested from the running torus (every 8th real cell,
-    four steps), the MLP trained on the GPU, attached, and K more timed
-    steps.  Reports the mean iteration at first convergence (k_converge)
+    training pairs recorded by the running torus's own cons2prim solves
+    (every 8th real cell, four steps), the MLP trained on the GPU, attached,
+    and K more timed steps.  Reports the mean iteration at first convergence (k_converge)
     and the mean iterations per call of both, and both throughputs."""
     import torch
     import disco_gb300 as dg
@@ -403,9 +403,7 @@ def measure_learned_c2p(args, wl, steps=None, warmup=None):
     sp = d.c2p_stats(reset=True)
     m = dg.Mlp(seed=1, capacity=1 << 21)
     t0 = time.perf_counter()
-    for _ in range(4):
-        d.run(1)
-        held = m.harvest(d, stride=8)
+    held = m.harvest(d, stride=8, steps=4)
     t1 = time.perf_counter()
     m.fit_norm()
     l0, l1 = m.train(2000, batch=8192, lr=2e-3, seed=5)

@@ -150,7 +150,7 @@ SIGNATURES = {
     "disco_gpu_getmindt_noalloc": (C.c_int, [_P, C.POINTER(C.c_double)]),
     "disco_mlp_create": (C.c_int, [C.c_ulonglong, C.c_long, C.POINTER(_P)]),
     "disco_mlp_free": (None, [_P]),
-    "disco_mlp_harvest": (C.c_int, [_P, _P, C.c_int, C.POINTER(C.c_long)]),
+    "disco_mlp_harvest": (C.c_int, [_P, _P, C.c_int, C.c_int, C.POINTER(C.c_long)]),
     "disco_mlp_pairs": (C.c_int, [_P, C.c_long, C.c_long, C.POINTER(C.c_float), C.POINTER(C.c_float)]),
     "disco_mlp_fit_norm": (C.c_int, [_P]),
     "disco_mlp_train": (C.c_int, [_P, C.c_int, C.c_int, C.c_float, C.c_ulonglong, C.POINTER(C.c_float),
@@ -470,7 +470,7 @@ class Domain:
             pass
 
 
-MLP_FEATURES, MLP_OUTPUTS, MLP_PARAMS, MLP_NORM = 8, 2, 5768, 20
+MLP_FEATURES, MLP_OUTPUTS, MLP_PARAMS, MLP_NORM = 10, 2, 5768, 24
 
 
 class Mlp:
@@ -483,11 +483,12 @@ class Mlp:
         _check(lib().disco_mlp_create(int(seed), int(capacity), C.byref(m)), "disco_mlp_create")
         self._m = m
 
-    def harvest(self, dom: "Domain", stride: int = 1) -> int:
-        """Append (features, converged solution) pairs of dom's current
-        state; returns the pairs held."""
+    def harvest(self, dom: "Domain", stride: int = 1, steps: int = 1) -> int:
+        """Advance dom by `steps` steps from the reference's start, recording
+        a training pair for every stride-th real cell at every cons2prim;
+        returns the pairs held."""
         n = C.c_long()
-        _check(lib().disco_mlp_harvest(self._m, dom._g, int(stride), C.byref(n)), "disco_mlp_harvest")
+        _check(lib().disco_mlp_harvest(self._m, dom._g, int(stride), int(steps), C.byref(n)), "disco_mlp_harvest")
         return n.value
 
     def pairs(self, first: int, n: int) -> tuple:

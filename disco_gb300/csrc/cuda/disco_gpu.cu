@@ -152,8 +152,9 @@ struct disco_mlp {
   disco::MlpDev view() const {
     disco::MlpDev v;
     v.W1b = W1b; v.W2b = W2b; v.W3b = W3b; v.params = p;
-    for (int q = 0; q < 8; ++q) { v.xm[q] = norm[q]; v.xs[q] = norm[8 + q]; }
-    for (int q = 0; q < 2; ++q) { v.ym[q] = norm[16 + q]; v.ys[q] = norm[18 + q]; }
+    constexpr int F = DISCO_MLP_FEATURES;
+    for (int q = 0; q < F; ++q) { v.xm[q] = norm[q]; v.xs[q] = norm[F + q]; }
+    for (int q = 0; q < 2; ++q) { v.ym[q] = norm[2 * F + q]; v.ys[q] = norm[2 * F + 2 + q]; }
     return v;
   }
   int refresh_bf16() {
@@ -220,8 +221,9 @@ int disco_mlp_create(unsigned long long seed, long capacity, disco_mlp** out) {
   fill(disco::kOffW1, 64, DISCO_MLP_FEATURES, 16, DISCO_MLP_FEATURES, 64);
   fill(disco::kOffW2, 64, 64, 64, 64, 64);
   fill(disco::kOffW3, DISCO_MLP_OUTPUTS, 64, 64, 64, DISCO_MLP_OUTPUTS);
-  for (int q = 0; q < 8; ++q) { m->norm[q] = 0.f; m->norm[8 + q] = 1.f; }
-  for (int q = 0; q < 2; ++q) { m->norm[16 + q] = 0.f; m->norm[18 + q] = 1.f; }
+  constexpr int F = DISCO_MLP_FEATURES;
+  for (int q = 0; q < F; ++q) { m->norm[q] = 0.f; m->norm[F + q] = 1.f; }
+  for (int q = 0; q < 2; ++q) { m->norm[2 * F + q] = 0.f; m->norm[2 * F + 2 + q] = 1.f; }
   if (cudaMemcpy(m->p, h.data(), 4 * np, cudaMemcpyHostToDevice) || cudaMemset(m->m1, 0, 4 * np) ||
       cudaMemset(m->m2, 0, 4 * np) || cudaMemset(m->count, 0, 8)) {
     disco_set_error("disco_mlp_create: upload failed");
@@ -236,9 +238,12 @@ int disco_mlp_create(unsigned long long seed, long capacity, disco_mlp** out) {
 
 void disco_mlp_free(disco_mlp* m) { delete m; }
 
-int disco_mlp_harvest(disco_mlp* m, disco_gpu* g, int stride, long* count) {
-  if (!m || !g) { disco_set_error("disco_mlp_harvest: null argument"); return DISCO_E_ARG; }
-  int rc = g->impl->harvest(stride, m->X, m->Y, m->cap, m->count);
+int disco_mlp_harvest(disco_mlp* m, disco_gpu* g, int stride, int steps, long* count) {
+  if (!m || !g || stride < 1 || steps < 0) { disco_set_error("disco_mlp_harvest: bad argument"); return DISCO_E_ARG; }
+  CK(cudaStreamSynchronize(m->st));
+  const disco::MlpDev v = m->view();
+  disco::C2PRecord rec{m->X, m->Y, m->cap, m->count, stride};
+  int rc = g->impl->harvest(&v, &rec, steps);
   if (rc) return rc;
   unsigned long long c = 0;
   CK(cudaMemcpy(&c, m->count, 8, cudaMemcpyDeviceToHost));
@@ -269,8 +274,9 @@ int disco_mlp_fit_norm(disco_mlp* m) {
     *mean = (float)mu;
     *sd = (float)(sdv > 1e-6 ? sdv : 1.0);
   };
-  for (int q = 0; q < 8; ++q) stats(X, 8, q, &m->norm[q], &m->norm[8 + q]);
-  for (int q = 0; q < 2; ++q) stats(Y, 2, q, &m->norm[16 + q], &m->norm[18 + q]);
+  constexpr int F = DISCO_MLP_FEATURES;
+  for (int q = 0; q < F; ++q) stats(X, F, q, &m->norm[q], &m->norm[F + q]);
+  for (int q = 0; q < 2; ++q) stats(Y, 2, q, &m->norm[2 * F + q], &m->norm[2 * F + 2 + q]);
   return 0;
 }
 

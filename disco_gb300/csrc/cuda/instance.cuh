@@ -62,7 +62,7 @@ struct InstanceBase {
   // GRMHD cons2prim with a learned starting point (mlp.cuh): attach (null
   // detaches), harvest training pairs, read / reset the iteration counters
   virtual int attach_guess(const MlpDev* m) = 0;
-  virtual int harvest(int stride, float* X, float* Y, long cap, unsigned long long* count) = 0;
+  virtual int harvest(const MlpDev* m, const C2PRecord* rec, int steps) = 0;
   virtual int c2p_stats(long long* out, int reset) = 0;
   virtual int getmindt_noalloc(double* dt) = 0;
   virtual int report(double* out, int nout) = 0;
@@ -704,7 +704,7 @@ struct Instance : InstanceBase {
     }
     {
       // GRMHD with a learned starting point: calc_prim is its own pass below
-      const int c2p = (ct || mlp_on) ? 0 : 1;
+      const int c2p = (ct || mlp_on || rec_on.X) ? 0 : 1;
       const dim3 g((unsigned)blocks(N));
       if (P.cool_damp && mid) LAUNCH("update", (k_update<Phys, R, NQ, true, true><<<g, 256, 0, st>>>(P, S, RK, fac, first, c2p)));
       else if (P.cool_damp)   LAUNCH("update", (k_update<Phys, R, NQ, true, false><<<g, 256, 0, st>>>(P, S, RK, fac, first, c2p)));
@@ -717,7 +717,9 @@ struct Instance : InstanceBase {
       LAUNCH("after_first", (k_after_first<<<1, 1, 0, st>>>(P, S.scal, S.planets, planets_id, S.errs)));
     }
     if constexpr (Phys::GR)
-      if (mlp_on) LAUNCH("c2p_guess", (k_c2p_guess<Phys, R, NQ><<<blocks(N), 256, 0, st>>>(P, S, mlp)));
+      if (mlp_on || rec_on.X)
+        LAUNCH("c2p_guess", (k_c2p_guess<Phys, R, NQ><<<blocks(N), 256, 0, st>>>(P, S, mlp, rec_on.X ? 0 : 1,
+                                                                                 rec_on)));
     if (ct) {   // flips (first substep), B_faces_to_cells, calc_prim (onestep.c:270-296)
       if (first)
         for (int d = 0; d < 2; ++d)
@@ -994,16 +996,25 @@ struct Instance : InstanceBase {
       if (graph[i]) { cudaGraphExecDestroy(graph[i]); graph[i] = nullptr; }
     return 0;
   }
-  int harvest(int stride, float* X, float* Y, long cap, unsigned long long* count) override {
+  // steps of (getmindt, timestep) from the reference's start, every
+  // cons2prim recording training pairs into rec
+  C2PRecord rec_on{};
+  int harvest(const MlpDev* m, const C2PRecord* rec, int steps) override {
     if constexpr (Phys::GR) {
-      if (stride < 1) { disco_set_error("harvest: stride must be >= 1"); return DISCO_E_ARG; }
-      const long n = (N + stride - 1) / stride;
-      LAUNCH("c2p_harvest", (k_c2p_harvest<Phys, R, NQ><<<blocks(n), 256, 0, st>>>(P, S, stride, X, Y, cap, count)));
-      CK(cudaGetLastError());
-      CK(cudaStreamSynchronize(st));
-      return 0;
+      const MlpDev keep = mlp;
+      mlp = *m;
+      rec_on = *rec;
+      int rc = 0;
+      for (int s = 0; s < steps && !rc; ++s) {
+        double dt;
+        rc = getmindt(&dt);
+        if (!rc) rc = timestep(dt);
+      }
+      rec_on = C2PRecord{};
+      mlp = keep;
+      return rc;
     } else {
-      (void)stride; (void)X; (void)Y; (void)cap; (void)count;
+      (void)m; (void)rec; (void)steps;
       disco_set_error("harvest: cons2prim pairs come from the GRMHD module only");
       return DISCO_E_MODULE;
     }

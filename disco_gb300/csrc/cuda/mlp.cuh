@@ -1,6 +1,7 @@
 // The learned starting point of the GRMHD Newton cons2prim: a 2 x 64 MLP
-// (8 features of the conserved state and the metric -> log(W^2 - 1) and
-// log(P / rho)), trained and evaluated on the tensor cores.
+// (10 features: 8 of the conserved state and the metric, 2 of the previous
+// primitives -> the changes of log(W^2 - 1) and log(P / rho) from the
+// previous primitives' values), trained and evaluated on the tensor cores.
 //
 // Arithmetic: BF16 operands (inputs, weights, activations, backpropagated
 // deltas) in mma.sync.m16n8k16 with FP32 accumulation; biases, tanh, the
@@ -18,7 +19,7 @@
 
 namespace disco {
 
-constexpr int kMlpIn = 8;          // features
+constexpr int kMlpIn = 10;         // features
 constexpr int kMlpInPad = 16;      // K of the first layer
 constexpr int kMlpH = 64;          // hidden width
 constexpr int kMlpOut = 2;         // outputs
@@ -153,7 +154,7 @@ __device__ inline void mlp_fwd_tile(const MlpSmem& w, const bf16* X, float (*h1)
   y[2] += w.b3[2 * t]; y[3] += w.b3[2 * t + 1];
 }
 
-// Standardised features of one sample into a BF16 row (8 used of 16).
+// Standardised features of one sample into a BF16 row (10 used of 16).
 __device__ inline void mlp_put_row(const MlpDev& m, bf16* row, const float* f, bool valid) {
 #pragma unroll
   for (int q = 0; q < kMlpInPad; ++q) {

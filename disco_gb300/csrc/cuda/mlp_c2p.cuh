@@ -1,6 +1,6 @@
-// The GRMHD cons2prim passes that use the learned starting point (mlp.cuh):
-// harvesting (features, converged solution) pairs from a running torus, and
-// calc_prim (misc.c:300-335 with grmhd.c:228) with the network's guess.
+// The GRMHD cons2prim pass that uses the learned starting point (mlp.cuh):
+// calc_prim (misc.c:300-335 with grmhd.c:228) with the network's corrected
+// start, or with the reference's start while recording training pairs.
 #pragma once
 #include "kernels.cuh"
 #include "mlp.cuh"
@@ -23,56 +23,28 @@ DISCO_D void c2p_geometry(const DevParams& P, const DevState<R>& S, int c, int j
   x[2] = .5 * (zp + zm);
 }
 
-// Training pairs: for every stride-th cell that is real, the features of its
-// conserved state and the (v^2, eta) the Newton iteration converges to from
-// the stored primitives (the state is not changed).  Pairs whose iteration
-// hits its cap are left out.  count: pairs written so far (capped at cap).
-template <typename Phys, typename R, int NQ>
-__global__ void k_c2p_harvest(DevParams P, DevState<R> S, int stride, float* X, float* Y, long cap,
-                              unsigned long long* count) {
-  const long cl = ((long)blockIdx.x * blockDim.x + threadIdx.x) * stride;
-  if (cl >= S.N) return;
-  const int c = (int)cl, N = S.N;
-  const int jk = S.cell_ring[c];
-  const int k = div_fast(jk, P.mul_nr), j = jk - k * P.Nr;
-  if (!is_real(P, j, k)) return;
-  double dV, x[3], cons[NQ], prim[NQ];
-  c2p_geometry(P, S, c, jk, j, k, &dV, x);
-#pragma unroll
-  for (int q = 0; q < NQ; ++q) {
-    cons[q] = S.cons[q * N + c] / dV;
-    prim[q] = S.prim[q * N + c];
-  }
-  KsMetric g(x, P.gr_M, P.gr_a, P.gr_kerr);
-  typename Phys::C2PInv v;
-  Phys::c2p_invariants(P, cons, g, x[0], v);
-  double v20, eta0, v2, eta;
-  Phys::c2p_warm_start(P, g, prim, x[0], &v20, &eta0);
-  int kc, it;
-  if (Phys::noble2d_solve(v, v20, eta0, &v2, &eta, &kc, &it) & 4) return;
-  float f[kMlpIn], y[kMlpOut];
-  Phys::c2p_features(v, g, f);
-  Phys::c2p_targets(v, v2, eta, y);
-  bool ok = isfinite(y[0]) && isfinite(y[1]);
-#pragma unroll
-  for (int q = 0; q < kMlpIn; ++q) ok = ok && isfinite(f[q]);
-  if (!ok) return;
-  const unsigned long long at = atomicAdd(count, 1ull);
-  if ((long)at >= cap) return;
-#pragma unroll
-  for (int q = 0; q < kMlpIn; ++q) X[at * kMlpIn + q] = f[q];
-  Y[at * kMlpOut + 0] = y[0];
-  Y[at * kMlpOut + 1] = y[1];
-}
+// Where the cons2prim pass records training pairs (X null: nowhere): for
+// every stride-th real cell, the features and the change of log(W^2 - 1)
+// and log(P / rho) from the previous primitives to the converged solution.
+struct C2PRecord {
+  float* X;
+  float* Y;
+  long cap;
+  unsigned long long* count;
+  int stride;
+};
 
 // calc_prim of the GRMHD module with the learned starting point: each warp
 // evaluates the network for its 32 cells on the tensor cores, then every
-// thread solves its cell from the network's (v^2, eta) -- or from the
-// previous primitives where those leave the smaller residual, the
-// reference's own start kept as the fallback -- and recovers its primitives
-// as calc_prim does.  256 threads per block.
+// thread solves its cell from the corrected start -- or from the previous
+// primitives where those leave the smaller residual, the reference's own
+// start kept as the fallback -- and recovers its primitives as calc_prim
+// does.  use_guess 0 starts every cell from the previous primitives (the
+// reference's calc_prim) and may record training pairs.  256 threads per
+// block.
 template <typename Phys, typename R, int NQ>
-__global__ void __launch_bounds__(256) k_c2p_guess(DevParams P, DevState<R> S, MlpDev m) {
+__global__ void __launch_bounds__(256) k_c2p_guess(DevParams P, DevState<R> S, MlpDev m, int use_guess,
+                                                   C2PRecord rec) {
   __shared__ MlpSmem w;
   __shared__ __align__(16) bf16 Xs[8][32 * kLdX];
   __shared__ float Ys[8][32 * kMlpOut];
@@ -89,36 +61,58 @@ __global__ void __launch_bounds__(256) k_c2p_guess(DevParams P, DevState<R> S, M
     j = jk - k * P.Nr;
     valid = is_real(P, j, k);
   }
-  double dV = 1.0, x[3] = {1.0, 0.0, 0.0}, cons[NQ];
+  double dV = 1.0, x[3] = {1.0, 0.0, 0.0}, cons[NQ], prim[NQ], lu2 = 0.0, lth = 0.0;
   float f[kMlpIn];
   typename Phys::C2PInv v;
   if (valid) {
     c2p_geometry(P, S, c, jk, j, k, &dV, x);
 #pragma unroll
-    for (int q = 0; q < NQ; ++q) cons[q] = S.cons[q * N + c] / dV;
+    for (int q = 0; q < NQ; ++q) {
+      cons[q] = S.cons[q * N + c] / dV;
+      prim[q] = S.prim[q * N + c];
+    }
     KsMetric g(x, P.gr_M, P.gr_a, P.gr_kerr);
     Phys::c2p_invariants(P, cons, g, x[0], v);
-    Phys::c2p_features(v, g, f);
+    Phys::c2p_warm_logs(g, prim, x[0], &lu2, &lth);
+    Phys::c2p_features(v, g, lu2, lth, f);
   }
-  mlp_put_row(m, &Xs[wid][lane * kLdX], f, valid);
-  mlp_infer_warp(m, w, Xs[wid], Ys[wid]);   // every lane of the warp takes part
+  if (use_guess) {
+    mlp_put_row(m, &Xs[wid][lane * kLdX], f, valid);
+    mlp_infer_warp(m, w, Xs[wid], Ys[wid]);   // every lane of the warp takes part
+  }
   if (!valid) return;
   KsMetric g(x, P.gr_M, P.gr_a, P.gr_kerr);
-  double prim[NQ];
-#pragma unroll
-  for (int q = 0; q < NQ; ++q) prim[q] = S.prim[q * N + c];
-  double v20, eta0, guess[2];
+  double v20, eta0;
   Phys::c2p_warm_start(P, g, prim, x[0], &v20, &eta0);
-  Phys::c2p_guess_from(v, &Ys[wid][lane * kMlpOut], guess);
   int guessed = 0;
-  if (Phys::c2p_residual(v, guess[0], guess[1]) < Phys::c2p_residual(v, v20, eta0)) {
-    v20 = guess[0];
-    eta0 = guess[1];
-    guessed = 1;
+  if (use_guess) {
+    double guess[2];
+    Phys::c2p_guess_from(v, &Ys[wid][lane * kMlpOut], lu2, lth, guess);
+    if (Phys::c2p_residual(v, guess[0], guess[1]) < Phys::c2p_residual(v, v20, eta0)) {
+      v20 = guess[0];
+      eta0 = guess[1];
+      guessed = 1;
+    }
   }
   double v2, eta;
   int kc, it;
   int hits = Phys::noble2d_solve(v, v20, eta0, &v2, &eta, &kc, &it);
+  if (rec.X && !(hits & 4) && (c % rec.stride) == 0) {   // a training pair from this solve
+    float y[kMlpOut];
+    Phys::c2p_targets(v, v2, eta, lu2, lth, y);
+    bool ok = isfinite(y[0]) && isfinite(y[1]);
+#pragma unroll
+    for (int q = 0; q < kMlpIn; ++q) ok = ok && isfinite(f[q]);
+    if (ok) {
+      const unsigned long long at = atomicAdd(rec.count, 1ull);
+      if ((long)at < rec.cap) {
+#pragma unroll
+        for (int q = 0; q < kMlpIn; ++q) rec.X[at * kMlpIn + q] = f[q];
+        rec.Y[at * kMlpOut + 0] = y[0];
+        rec.Y[at * kMlpOut + 1] = y[1];
+      }
+    }
+  }
   hits |= Phys::c2p_recover(P, g, v, cons, v2, eta, prim);
   c2p_count(S.errs, kc, it, guessed);
   bool bad = false;

@@ -514,10 +514,22 @@ struct Grmhd {
     return hits;
   }
 
-  // The eight features of the learned starting point: the Noble invariants
-  // (log e, log s2, log Q, the squared cosine between B and S), the rest
-  // mass log D, the lapse, log r and log |e^2 - s2|.
-  DISCO_D static void c2p_features(const C2PInv& v, const KsMetric& g, float* f) {
+  // The previous primitives' log(W^2 - 1) and log(P / rho): the point the
+  // reference starts from (v20 = u2 / (1 + u2), eta0 = W h), in the
+  // variables the learned correction uses.
+  DISCO_D static void c2p_warm_logs(const KsMetric& g, const double* prim, double r, double* lu2, double* lth) {
+    double u2 = 0.0;
+    const double l[3] = {prim[URR], r * r * prim[UPP], prim[UZZ]};
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) u2 += g.igam[3 * i + j] * l[i] * l[j];
+    *lu2 = log(fmax(u2, 1.0e-30));
+    *lth = log(fmax(prim[PPP] / prim[RHO], 1.0e-30));
+  }
+  // The ten features of the learned correction: the Noble invariants (log e,
+  // log s2, log Q, the squared cosine between B and S), the rest mass log D,
+  // the lapse, log r, log |e^2 - s2|, and the previous primitives'
+  // log(W^2 - 1) and log(P / rho).
+  DISCO_D static void c2p_features(const C2PInv& v, const KsMetric& g, double lu2, double lth, float* f) {
     f[0] = logf((float)fmax(v.e, 1.0e-30));
     f[1] = logf((float)(v.s2 + 1.0e-20));
     f[2] = logf((float)(v.Q + 1.0e-20));
@@ -526,20 +538,23 @@ struct Grmhd {
     f[5] = (float)g.al;
     f[6] = logf((float)v.r);
     f[7] = logf((float)(fabs(v.e * v.e - v.s2) + 1.0e-20));
+    f[8] = (float)lu2;
+    f[9] = (float)lth;
   }
-  // Targets from a converged (v2, eta): log(W^2 - 1) and log(P / rho).
-  DISCO_D static void c2p_targets(const C2PInv& v, double v2, double eta, float* y) {
+  // Targets from a converged (v2, eta): the changes of log(W^2 - 1) and of
+  // log(P / rho) from the previous primitives' values.
+  DISCO_D static void c2p_targets(const C2PInv& v, double v2, double eta, double lu2, double lth, float* y) {
     const double u2 = v2 / (1.0 - v2);
     const double w = sqrt(1.0 + u2);
     const double th = v.n * (eta / w - 1.0);
-    y[0] = logf((float)fmax(u2, 1.0e-30));
-    y[1] = logf((float)fmax(th, 1.0e-30));
+    y[0] = (float)(log(fmax(u2, 1.0e-30)) - lu2);
+    y[1] = (float)(log(fmax(th, 1.0e-30)) - lth);
   }
-  // The starting point (v2, eta) the outputs describe: W^2 - 1 = exp(y0),
-  // P / rho = exp(y1), eta = W h with h = 1 + gamma / (gamma - 1) P / rho.
-  DISCO_D static void c2p_guess_from(const C2PInv& v, const float* y, double* g2) {
-    const double u2 = exp((double)y[0]);
-    const double th = exp((double)y[1]);
+  // The starting point (v2, eta) of the outputs: W^2 - 1 = exp(lu2 + y0),
+  // P / rho = exp(lth + y1), eta = W h, h = 1 + gamma / (gamma - 1) P / rho.
+  DISCO_D static void c2p_guess_from(const C2PInv& v, const float* y, double lu2, double lth, double* g2) {
+    const double u2 = exp(lu2 + (double)y[0]);
+    const double th = exp(lth + (double)y[1]);
     g2[0] = u2 / (1.0 + u2);
     g2[1] = sqrt(1.0 + u2) * (1.0 + th / v.n);
   }

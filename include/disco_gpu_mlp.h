@@ -5,11 +5,13 @@
  * The reference starts its Noble et al. 2D Newton iteration from the
  * previous primitives (Hydro/grmhd.c:885-893) and iterates to a relative
  * change of 1e-12 plus 10 more iterations (:910-957).  Here a small MLP
- * (8 features of the conserved state and the metric -> log(W^2 - 1) and
- * log(P / rho), two hidden layers of 64, tanh) gives another starting
- * point.  It is trained on the GPU, on (features, converged solution) pairs
- * harvested from the method's own runs, by hand-written BF16 tensor-core
- * forward and backward kernels with FP32 accumulation and FP32 Adam.  The
+ * corrects that start: from 10 features -- the Noble invariants of the new
+ * conserved state, the rest mass, the lapse, r, and log(W^2 - 1) and
+ * log(P / rho) of the previous primitives -- it predicts how much those two
+ * logarithms change (two hidden layers of 64, tanh).  It is trained on the
+ * GPU, on pairs the method harvests from its own solves during torus runs,
+ * by hand-written BF16 tensor-core forward and backward kernels with FP32
+ * accumulation and FP32 Adam.  The
  * Newton solve is unchanged and still runs to the same tolerance; the
  * previous primitives stay the starting point wherever they leave the
  * smaller residual of the two Noble equations, so the converged primitives
@@ -28,14 +30,14 @@ extern "C" {
 
 typedef struct disco_mlp disco_mlp;
 
-#define DISCO_MLP_FEATURES 8
+#define DISCO_MLP_FEATURES 10
 #define DISCO_MLP_OUTPUTS 2
-/* FP32 parameters, flat: W1[64][16] (inputs 8..15 zero), b1[64],
+/* FP32 parameters, flat: W1[64][16] (inputs 10..15 zero), b1[64],
  * W2[64][64], b2[64], W3[8][64] (rows 2..7 zero), b3[8] */
 #define DISCO_MLP_PARAMS 5768
-/* standardisation: feature means[8], feature scales[8], target means[2],
+/* standardisation: feature means[10], feature scales[10], target means[2],
  * target scales[2] */
-#define DISCO_MLP_NORM 20
+#define DISCO_MLP_NORM 24
 
 /* A model with Xavier-uniform weights drawn from splitmix64(seed), zero
  * biases, identity standardisation, and room for `capacity` training pairs
@@ -43,14 +45,15 @@ typedef struct disco_mlp disco_mlp;
 int disco_mlp_create(unsigned long long seed, long capacity, disco_mlp **out);
 void disco_mlp_free(disco_mlp *m);
 
-/* Appends a training pair for every stride-th cell of g's current state that
- * is real: the cell's features and the (v^2, eta) the Newton iteration
- * converges to from its stored primitives (the state is not changed).
+/* Advances g by `steps` timesteps (getmindt + timestep) with the
+ * reference's start, recording a training pair for every stride-th real
+ * cell at every cons2prim: its features and the change of log(W^2 - 1) and
+ * log(P / rho) from the previous primitives to the converged solution.
  * *count = pairs held (at most the capacity).  GRMHD instances only. */
-int disco_mlp_harvest(disco_mlp *m, disco_gpu *g, int stride, long *count);
+int disco_mlp_harvest(disco_mlp *m, disco_gpu *g, int stride, int steps, long *count);
 
 /* Copies held pairs [first, first + n) to the host (either array may be
- * NULL): X [n][8] features, Y [n][2] targets. */
+ * NULL): X [n][10] features, Y [n][2] targets. */
 int disco_mlp_pairs(disco_mlp *m, long first, long n, float *X, float *Y);
 
 /* Sets the standardisation from the mean and standard deviation of the held
@@ -64,12 +67,12 @@ int disco_mlp_fit_norm(disco_mlp *m);
 int disco_mlp_train(disco_mlp *m, int steps, int batch, float lr, unsigned long long seed,
                     float *loss_first, float *loss_last);
 
-/* One forward and backward pass over n given pairs (raw X [n][8], Y [n][2])
+/* One forward and backward pass over n given pairs (raw X [n][10], Y [n][2])
  * without an update: *loss = the summed squared error of the standardised
  * outputs, grad[DISCO_MLP_PARAMS] = the gradient of loss / n. */
 int disco_mlp_grad(disco_mlp *m, const float *X, const float *Y, int n, float *loss, float *grad);
 
-/* The network's raw outputs Y [n][2] for raw features X [n][8]. */
+/* The network's raw outputs Y [n][2] for raw features X [n][10]. */
 int disco_mlp_predict(disco_mlp *m, const float *X, long n, float *Y);
 
 /* Reads (get != NULL) and/or replaces (set != NULL) the FP32 parameters

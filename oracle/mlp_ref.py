@@ -39,19 +39,20 @@ def pack(d: dict) -> np.ndarray:
 
 def forward_backward(p, norm, X, Y, bf16: bool = True):
     """(summed squared error of the standardised outputs, gradient of its
-    mean over the samples, the raw outputs) for raw features X [n][8] and
-    raw targets Y [n][2]; norm = (x mean[8], x scale[8], y mean[2], y
-    scale[2]) as the flat 20 floats of the model."""
+    mean over the samples, the raw outputs) for raw features X [n][F] and
+    raw targets Y [n][2]; norm = (x mean[F], x scale[F], y mean[2], y
+    scale[2]) as the flat 2 F + 4 floats of the model."""
     r = to_bf16 if bf16 else (lambda a: np.asarray(a, dtype=np.float64))
     w = unpack(p)
-    nm = np.asarray(norm, dtype=np.float64)
-    xm, xs, ym, ys = nm[0:8], nm[8:16], nm[16:18], nm[18:20]
     X = np.asarray(X, dtype=np.float64)
     Y = np.asarray(Y, dtype=np.float64)
+    F = X.shape[1]
+    nm = np.asarray(norm, dtype=np.float64)
+    xm, xs, ym, ys = nm[0:F], nm[F:2 * F], nm[2 * F:2 * F + 2], nm[2 * F + 2:2 * F + 4]
     n = len(X)
     xn = (X.astype(np.float32) - xm.astype(np.float32)) / xs.astype(np.float32) if bf16 else (X - xm) / xs
     x = np.zeros((n, 16))
-    x[:, :8] = r(xn)
+    x[:, :F] = r(xn)
     W1, W2, W3 = r(w["W1"]), r(w["W2"]), r(w["W3"])
     h1 = np.tanh(x @ W1.T + w["b1"])
     h1b = r(h1)

@@ -3,8 +3,9 @@
 * The tensor-core training kernels' gradient and the inference kernel's
   outputs against the oracle's FP64 restatement (oracle/mlp_ref.py) with the
   same BF16 roundings of the operands.
-* Training on (features, converged solution) pairs harvested from the Kerr
-  torus reduces the loss.
+* Training on pairs harvested from the Kerr torus's own cons2prim solves
+  (features including the previous primitives; targets the change of
+  log(W^2 - 1) and log(P / rho) to the converged solution) reduces the loss.
 * With the trained network attached, the Newton iteration converges to the
   same primitives (relative L1 1e-13 per component after the steps) and the
   mean iteration at first convergence (k_converge) is reported against the
@@ -23,8 +24,11 @@ def _rel_l2(a, b):
     return float(np.linalg.norm(a - b) / (n if n > 0 else 1.0))
 
 
+F = 10   # features
+
+
 def _random_norm(rng):
-    return np.concatenate([rng.normal(0, 1, 8), rng.uniform(0.5, 2, 8), rng.normal(0, 1, 2),
+    return np.concatenate([rng.normal(0, 1, F), rng.uniform(0.5, 2, F), rng.normal(0, 1, 2),
                            rng.uniform(0.5, 2, 2)]).astype(np.float32)
 
 
@@ -36,8 +40,8 @@ def test_mlp_gradient_matches_restatement():
     norm = _random_norm(rng)
     m.set_params(norm=norm)
     n = 333                                      # not a multiple of the 16-sample tile
-    X = (rng.normal(0, 1.5, (n, 8)) * norm[8:16] + norm[:8]).astype(np.float32)
-    Y = (rng.normal(0, 1.5, (n, 2)) * norm[18:20] + norm[16:18]).astype(np.float32)
+    X = (rng.normal(0, 1.5, (n, F)) * norm[F:2 * F] + norm[:F]).astype(np.float32)
+    Y = (rng.normal(0, 1.5, (n, 2)) * norm[2 * F + 2:] + norm[2 * F:2 * F + 2]).astype(np.float32)
     loss, g = m.grad(X, Y)
     l_ref, g_ref, _ = mlp_ref.forward_backward(p, norm, X, Y, bf16=True)
     assert loss == pytest.approx(l_ref, rel=1e-3)
@@ -59,21 +63,19 @@ def test_mlp_inference_matches_restatement():
     p, _ = m.params()
     norm = _random_norm(rng)
     m.set_params(norm=norm)
-    X = (rng.normal(0, 1.5, (1000, 8)) * norm[8:16] + norm[:8]).astype(np.float32)
+    X = (rng.normal(0, 1.5, (1000, F)) * norm[F:2 * F] + norm[:F]).astype(np.float32)
     Yd = m.predict(X)
     _, _, Yr = mlp_ref.forward_backward(p, norm, X, np.zeros((1000, 2)), bf16=True)
     for o in range(2):   # in standardised units
-        yd = (Yd[:, o] - norm[16 + o]) / norm[18 + o]
-        yr = (Yr[:, o] - norm[16 + o]) / norm[18 + o]
+        yd = (Yd[:, o] - norm[2 * F + o]) / norm[2 * F + 2 + o]
+        yr = (Yr[:, o] - norm[2 * F + o]) / norm[2 * F + 2 + o]
         assert np.max(np.abs(yd - yr)) <= 2e-3 * max(1.0, np.abs(yr).max()), o
     m.close()
 
 
-def _harvest_and_train(m, steps=8, train_steps=1500):
+def _harvest_and_train(m, steps=12, train_steps=3000):
     d, _ = _domain("cfg4t_n24", 0)
-    for _ in range(steps):
-        d.timestep(d.getmindt())
-        m.harvest(d)
+    m.harvest(d, stride=1, steps=steps)
     d.close()
     m.fit_norm()
     return m.train(train_steps, batch=4096, lr=2e-3, seed=3)

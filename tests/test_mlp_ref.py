@@ -11,20 +11,21 @@ from oracle import mlp_ref
 def _random_model(rng):
     p = np.zeros(mlp_ref.NPARAMS)
     w = mlp_ref.unpack(p)
-    w["W1"][:, :8] = rng.normal(0, 0.4, (64, 8))
+    w["W1"][:, :10] = rng.normal(0, 0.4, (64, 10))
     w["W2"][...] = rng.normal(0, 0.2, (64, 64))
     w["W3"][:2] = rng.normal(0, 0.2, (2, 64))
     w["b1"][...] = rng.normal(0, 0.1, 64)
     w["b2"][...] = rng.normal(0, 0.1, 64)
     w["b3"][:2] = rng.normal(0, 0.1, 2)
-    norm = np.concatenate([rng.normal(0, 1, 8), rng.uniform(0.5, 2, 8), rng.normal(0, 1, 2), rng.uniform(0.5, 2, 2)])
+    norm = np.concatenate([rng.normal(0, 1, 10), rng.uniform(0.5, 2, 10), rng.normal(0, 1, 2),
+                           rng.uniform(0.5, 2, 2)])
     return mlp_ref.pack(w), norm
 
 
 def test_fp64_gradient_matches_finite_differences():
     rng = np.random.default_rng(3)
     p, norm = _random_model(rng)
-    X = rng.normal(0, 1.5, (37, 8))
+    X = rng.normal(0, 1.5, (37, 10))
     Y = rng.normal(0, 1.5, (37, 2))
     _, g, _ = mlp_ref.forward_backward(p, norm, X, Y, bf16=False)
     live = np.flatnonzero(g)
@@ -39,9 +40,9 @@ def test_fp64_gradient_matches_finite_differences():
         lm = mlp_ref.forward_backward(pm, norm, X, Y, bf16=False)[0] / n
         fd = (lp - lm) / (2 * h)
         assert abs(fd - g[i]) <= 1e-6 * max(1.0, abs(g[i])), (i, fd, g[i])
-    # the padded parameters (inputs 8..15 of W1, rows 2..7 of W3) get no gradient
+    # the padded parameters (inputs 10..15 of W1, rows 2..7 of W3) get no gradient
     w = mlp_ref.unpack(g)
-    assert not np.any(w["W1"][:, 8:]) and not np.any(w["W3"][2:]) and not np.any(w["b3"][2:])
+    assert not np.any(w["W1"][:, 10:]) and not np.any(w["W3"][2:]) and not np.any(w["b3"][2:])
 
 
 def test_bf16_rounding_is_nearest_even():
