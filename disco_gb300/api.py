@@ -161,6 +161,7 @@ SIGNATURES = {
     "disco_mlp_params": (C.c_int, [_P, C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_float),
                                    C.POINTER(C.c_float)]),
     "disco_gpu_attach_guess": (C.c_int, [_P, _P]),
+    "disco_mlp_set_floor": (C.c_int, [_P, C.c_double]),
     "disco_gpu_c2p_stats": (C.c_int, [_P, C.POINTER(C.c_longlong), C.c_int]),
     "disco_gpu_report": (C.c_int, [_P, C.POINTER(C.c_double), C.c_int]),
     "disco_gpu_diag_count": (C.c_int, [_P]),
@@ -519,6 +520,11 @@ class Mlp:
         _check(lib().disco_mlp_grad(self._m, X.ctypes.data_as(fp), Y.ctypes.data_as(fp), len(X), C.byref(loss),
                                     g.ctypes.data_as(fp)), "disco_mlp_grad")
         return loss.value, g
+
+    def set_floor(self, floor: float) -> None:
+        """Residual of the previous primitives at or below which cons2prim
+        keeps them as the start (used at the next attach)."""
+        _check(lib().disco_mlp_set_floor(self._m, float(floor)), "disco_mlp_set_floor")
 
     def predict(self, X: np.ndarray) -> np.ndarray:
         X = np.ascontiguousarray(X, np.float32)

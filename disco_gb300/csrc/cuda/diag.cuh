@@ -295,9 +295,9 @@ DISCO_D void diag_cell(const DevParams& P, const DevState<R>& S, int c, double O
 
 // One block per ring jk; Qrz is [Nr*Nz][ND], t_avg lives in scal[SC_TAVG].
 template <typename R, int NQ, int D>
-__global__ void __launch_bounds__(kDiagBlock) k_diag(DevParams P, DevState<R> S, double* Qrz) {
+DISCO_D void k_diag_body(const DevParams& P, const DevState<R>& S, double* Qrz, int bx_, int by_) {
   constexpr int ND = D == 0 ? 8 : D == 1 ? 5 : D == 2 ? 6 : D == 3 ? 5 : D == 4 ? 18 : 48;
-  const int jk = blockIdx.x;
+  const int jk = bx_;
   const int k = jk / P.Nr, j = jk - k * P.Nr;
   const int off = S.ring_off[jk], Np = S.ring_off[jk + 1] - off;
   const double rp = S.r_jph[j + 1], rm = S.r_jph[j];   // r_jph[j], r_jph[j-1]
@@ -361,6 +361,10 @@ __global__ void __launch_bounds__(kDiagBlock) k_diag(DevParams P, DevState<R> S,
     Qrz[(size_t)jk * ND + threadIdx.x] += s * dt / v;
   }
   if (jk == 0 && threadIdx.x == 0) S.scal[SC_TAVG] += S.scal[SC_DT];
+}
+template <typename R, int NQ, int D>
+__global__ void __launch_bounds__(kDiagBlock) k_diag(DevParams P, DevState<R> S, double* Qrz) {
+  k_diag_body<R, NQ, D>(P, S, Qrz, (int)blockIdx.x, (int)blockIdx.y);
 }
 
 }  // namespace disco

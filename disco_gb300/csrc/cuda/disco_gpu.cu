@@ -123,6 +123,7 @@ struct disco_mlp {
   disco::MlpBatch bt{};
   long bcap = 0;
   long long step = 0;
+  double warm_floor = 0.0;
   ~disco_mlp() {
     for (void* q : {(void*)p, (void*)m1, (void*)m2, (void*)grad, (void*)loss, (void*)W1b, (void*)W2b, (void*)W3b,
                     (void*)X, (void*)Y, (void*)count})
@@ -155,6 +156,7 @@ struct disco_mlp {
     constexpr int F = DISCO_MLP_FEATURES;
     for (int q = 0; q < F; ++q) { v.xm[q] = norm[q]; v.xs[q] = norm[F + q]; }
     for (int q = 0; q < 2; ++q) { v.ym[q] = norm[2 * F + q]; v.ys[q] = norm[2 * F + 2 + q]; }
+    v.warm_floor = warm_floor;
     return v;
   }
   int refresh_bf16() {
@@ -375,6 +377,12 @@ int disco_mlp_params(disco_mlp* m, float* get, const float* set, float* norm_get
     if (rc) return rc;
     CK(cudaStreamSynchronize(m->st));
   }
+  return 0;
+}
+
+int disco_mlp_set_floor(disco_mlp* m, double floor) {
+  if (!m || !(floor >= 0.0)) { disco_set_error("disco_mlp_set_floor: bad argument"); return DISCO_E_ARG; }
+  m->warm_floor = floor;
   return 0;
 }
 

@@ -212,8 +212,8 @@ DISCO_D void initial_eval(const DevParams& P, double* prim, const double* x) {
 
 // ---- set_wcell, misc.c:101-168 --------------------------------------------
 template <typename R, int NQ>
-__global__ void k_wcell(DevParams P, DevState<R> S) {
-  int c = blockIdx.x * blockDim.x + threadIdx.x;
+DISCO_D void k_wcell_body(const DevParams& P, const DevState<R>& S, int bx_, int by_) {
+  int c = bx_ * blockDim.x + threadIdx.x;
   if (c >= S.N) return;
   int jk = S.cell_ring[c];
   int k = div_fast(jk, P.mul_nr), j = jk - k * P.Nr;
@@ -233,15 +233,19 @@ __global__ void k_wcell(DevParams P, DevState<R> S) {
   (void)k;
   S.wiph[c] = w;
 }
+template <typename R, int NQ>
+__global__ void k_wcell(DevParams P, DevState<R> S) {
+  k_wcell_body<R, NQ>(P, S, (int)blockIdx.x, (int)blockIdx.y);
+}
 
 // Mixed path, Mesh_Motion 3: the ring average of .5 (w_i + w_i+1) is the
 // ring average of w_i = prim[UPP]; one block per ring sums it as an FP64
 // tree (the mesh speed enters F - wU, where its rounding is amplified) and
 // writes the mean to every cell of the ring.
 template <typename R>
-__global__ void k_wcell_ring(DevParams P, DevState<R> S) {
+DISCO_D void k_wcell_ring_body(const DevParams& P, const DevState<R>& S, int bx_, int by_) {
   __shared__ double part[32];
-  int jk = blockIdx.x;
+  int jk = bx_;
   int off = S.ring_off[jk], Np = S.ring_off[jk + 1] - off;
   double s = 0;
   for (int i = threadIdx.x; i < Np; i += blockDim.x) s += (double)S.prim[UPP * S.N + off + i];
@@ -258,15 +262,19 @@ __global__ void k_wcell_ring(DevParams P, DevState<R> S) {
   double w = part[0];
   for (int i = threadIdx.x; i < Np; i += blockDim.x) S.wiph[off + i] = w;
 }
+template <typename R>
+__global__ void k_wcell_ring(DevParams P, DevState<R> S) {
+  k_wcell_ring_body<R>(P, S, (int)blockIdx.x, (int)blockIdx.y);
+}
 
 // Mesh_Motion 3: ring average of w (misc.c:138-152), one block per ring.  The
 // ring is staged in shared memory and summed by one thread in the
 // reference's order, so the mesh speed rounds exactly like the reference's
 // (it can coincide with a contact speed, where HLLD branches on equality).
 template <typename R>
-__global__ void k_wcell_avg(DevParams P, DevState<R> S) {
+DISCO_D void k_wcell_avg_body(const DevParams& P, const DevState<R>& S, int bx_, int by_) {
   extern __shared__ double wsm[];
-  int jk = blockIdx.x;
+  int jk = bx_;
   int off = S.ring_off[jk], Np = S.ring_off[jk + 1] - off;
   for (int i = threadIdx.x; i < Np; i += blockDim.x) wsm[i] = S.wiph[off + i];
   __syncthreads();
@@ -278,6 +286,10 @@ __global__ void k_wcell_avg(DevParams P, DevState<R> S) {
   __syncthreads();
   double w = wsm[Np];
   for (int i = threadIdx.x; i < Np; i += blockDim.x) S.wiph[off + i] = w;
+}
+template <typename R>
+__global__ void k_wcell_avg(DevParams P, DevState<R> S) {
+  k_wcell_avg_body<R>(P, S, (int)blockIdx.x, (int)blockIdx.y);
 }
 
 // dphi in R for the mixed path (after an upload or at set-up).
@@ -299,8 +311,8 @@ DISCO_D R minmod(R a, R b, R c) {
 }
 
 template <typename R, int NQ>
-__global__ void k_plm_phi(DevParams P, DevState<R> S) {
-  int c = blockIdx.x * blockDim.x + threadIdx.x;
+DISCO_D void k_plm_phi_body(const DevParams& P, const DevState<R>& S, int bx_, int by_) {
+  int c = bx_ * blockDim.x + threadIdx.x;
   if (c >= S.N) return;
   int jk = S.cell_ring[c];
   int off = S.ring_off[jk], Np = S.ring_off[jk + 1] - off;
@@ -330,6 +342,10 @@ __global__ void k_plm_phi(DevParams P, DevState<R> S) {
     S.gradp[q * N + c] = minmod<R>(PLM * sL, sC, PLM * sR);
   }
 }
+template <typename R, int NQ>
+__global__ void k_plm_phi(DevParams P, DevState<R> S) {
+  k_plm_phi_body<R, NQ>(P, S, (int)blockIdx.x, (int)blockIdx.y);
+}
 
 // ---- ring anchors, faces_alt.c:57-79 -----------------------------------------
 // Quadrant tests of sin/cos(piph * 2pi/Pmax) done as exact comparisons of the
@@ -348,8 +364,8 @@ DISCO_D int quadrant_q4(double th) {  // sin < 0 && cos > 0
 
 // One warp per ring: I0 = first Q1 cell after the first Q4 cell, else 0.
 template <typename R>
-__global__ void k_anchor(DevParams P, DevState<R> S, int nring) {
-  int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+DISCO_D void k_anchor_body(const DevParams& P, const DevState<R>& S, int nring, int bx_, int by_) {
+  int warp = (bx_ * blockDim.x + threadIdx.x) >> 5;
   int lane = threadIdx.x & 31;
   if (warp >= nring) return;
   int off = S.ring_off[warp], Np = S.ring_off[warp + 1] - off;
@@ -382,6 +398,10 @@ __global__ void k_anchor(DevParams P, DevState<R> S, int nring) {
     if (i > firstQ4 && q1(S.piph[off + i])) { I0 = min(I0, i); }
   for (int o = 16; o > 0; o >>= 1) I0 = min(I0, __shfl_xor_sync(0xffffffffu, I0, o));
   if (lane == 0) S.anchor[warp] = (I0 == 0x7fffffff) ? 0 : I0;
+}
+template <typename R>
+__global__ void k_anchor(DevParams P, DevState<R> S, int nring) {
+  k_anchor_body<R>(P, S, nring, (int)blockIdx.x, (int)blockIdx.y);
 }
 
 // ---- sheared faces, faces_alt.c:36-179 ---------------------------------------
@@ -441,10 +461,10 @@ DISCO_D int gallop_search(int lo0, int hi0, int h, F&& pred) {
 }
 
 template <typename R>
-__global__ void k_faces(DevParams P, DevState<R> S, int dim) {
+DISCO_D void k_faces_body(const DevParams& P, const DevState<R>& S, int dim, int bx_, int by_) {
   extern __shared__ long long fkeys[];
   const int d = dim - 1;
-  int pair = blockIdx.x;
+  int pair = bx_;
   PairInfo pi = pair_info(P, dim, pair);
   int offL = S.ring_off[pi.L], NL = S.ring_off[pi.L + 1] - offL;
   int offR = S.ring_off[pi.R], NR = S.ring_off[pi.R + 1] - offR;
@@ -608,6 +628,10 @@ __global__ void k_faces(DevParams P, DevState<R> S, int dim) {
     if (cur == 1) S.run_dn_e[d][iR] = gf;
   }
 }
+template <typename R>
+__global__ void k_faces(DevParams P, DevState<R> S, int dim) {
+  k_faces_body<R>(P, S, dim, (int)blockIdx.x, (int)blockIdx.y);
+}
 
 // Iterate the faces of a circular run [s, e] of a pair block [base, base+Nf)
 // in ascending face order (the reference's loop order).
@@ -741,9 +765,9 @@ __global__ void k_pair_geom(DevParams P, DevState<R> S, int dim, int npair) {
 constexpr int kSlopeFaces = 4;   // faces per thread in k_plm_slopes (loads in flight)
 
 template <typename R, int NQ>
-__global__ void k_plm_slopes(DevParams P, DevState<R> S, int dim) {
+DISCO_D void k_plm_slopes_body(const DevParams& P, const DevState<R>& S, int dim, int bx_, int by_) {
   const int d = dim - 1;
-  int pair = blockIdx.x;
+  int pair = bx_;
   int base = S.face_off[d][pair], Nf = S.face_off[d][pair + 1] - base;
   const int N = S.N, NF = S.nf[d];
   R dxs = S.pdxs[d][pair];
@@ -751,7 +775,7 @@ __global__ void k_plm_slopes(DevParams P, DevState<R> S, int dim) {
   R dOm = kMix<R> ? S.pdOm[d][pair] : (R)0;
 #pragma unroll
   for (int u = 0; u < kSlopeFaces; ++u) {
-    int n = (blockIdx.y * kSlopeFaces + u) * blockDim.x + threadIdx.x;
+    int n = (by_ * kSlopeFaces + u) * blockDim.x + threadIdx.x;
     if (n >= Nf) break;
     int f = base + n;
     int cL = S.fL[d][f], cR = S.fR[d][f];
@@ -766,6 +790,10 @@ __global__ void k_plm_slopes(DevParams P, DevState<R> S, int dim) {
       S.fslope[(size_t)q * NF + f] = Sl;
     }
   }
+}
+template <typename R, int NQ>
+__global__ void k_plm_slopes(DevParams P, DevState<R> S, int dim) {
+  k_plm_slopes_body<R, NQ>(P, S, dim, (int)blockIdx.x, (int)blockIdx.y);
 }
 
 // The components are independent: blockIdx.y selects a group of QPT of them.
@@ -782,7 +810,7 @@ constexpr int plm_groups() { return (NQ + kPlmQ - 1) / kPlmQ; }
 // coalesced loads, and each thread then walks its own run in the reference's
 // order from shared memory.
 template <typename R, int NQ>
-__global__ void __launch_bounds__(kTileCells) k_plm_trans(DevParams P, DevState<R> S, int dim) {
+DISCO_D void k_plm_trans_body(const DevParams& P, const DevState<R>& S, int dim, int bx_, int by_) {
   constexpr int QPT = kPlmQ;
   constexpr int NG = plm_groups<NQ>();
   // components of this block: [q0, q0 + QPT) within NQ (q0 = 0 at compile
@@ -791,8 +819,8 @@ __global__ void __launch_bounds__(kTileCells) k_plm_trans(DevParams P, DevState<
   __shared__ R sS[QB][kTileCap];
   __shared__ R sA[kTileCap];
   __shared__ int rng[2];
-  const int item = blockIdx.x;
-  const int q0 = NG == 1 ? 0 : (int)blockIdx.y * QPT;
+  const int item = bx_;
+  const int q0 = NG == 1 ? 0 : by_ * QPT;
   const int d = dim - 1;
   const int N = S.N, NF = S.nf[d];
   const int jk = S.chunk_ring[item], i0 = S.chunk_i0[item];
@@ -939,6 +967,10 @@ __global__ void __launch_bounds__(kTileCells) k_plm_trans(DevParams P, DevState<
     }
     grad[q * N + c] = g;
   }
+}
+template <typename R, int NQ>
+__global__ void __launch_bounds__(kTileCells) k_plm_trans(DevParams P, DevState<R> S, int dim) {
+  k_plm_trans_body<R, NQ>(P, S, dim, (int)blockIdx.x, (int)blockIdx.y);
 }
 
 // ---- cooling (sink.c:274-326) and damping (sink.c:329-427) of one cell -----
@@ -1105,8 +1137,8 @@ DISCO_D void flux_phi_face(const DevParams& P, const DevState<R>& S, double fac,
 }
 
 template <typename Phys, typename R, int NQ>
-__global__ void __launch_bounds__(256, kMix<R> ? 4 : 1) k_flux_phi(DevParams P, DevState<R> S, double fac) {
-  int c = blockIdx.x * blockDim.x + threadIdx.x;
+DISCO_D void k_flux_phi_body(const DevParams& P, const DevState<R>& S, double fac, int bx_, int by_) {
+  int c = bx_ * blockDim.x + threadIdx.x;
   if (c >= S.N) return;
   int jk = S.cell_ring[c];
   int k = div_fast(jk, P.mul_nr), j = jk - k * P.Nr;
@@ -1123,18 +1155,21 @@ __global__ void __launch_bounds__(256, kMix<R> ? 4 : 1) k_flux_phi(DevParams P, 
   }
   flux_phi_face<Phys, R, NQ>(P, S, fac, c, cp, jk, j, k, pC, pP, gC, gP, S.dphi_r[c], S.dphi_r[cp]);
 }
+template <typename Phys, typename R, int NQ>
+__global__ void __launch_bounds__(256, kMix<R> ? 4 : 1) k_flux_phi(DevParams P, DevState<R> S, double fac) {
+  k_flux_phi_body<Phys, R, NQ>(P, S, fac, (int)blockIdx.x, (int)blockIdx.y);
+}
 
 // ---- r/z fluxes, misc.c:441-519 + riemann_trans, riemann.c:114-214 ----------
 // Grid: x = pair within the active range, y = chunk of 256 faces.
 template <typename Phys, typename R, int NQ>
-__global__ void __launch_bounds__(256, kMix<R> ? 4 : 1) k_flux_trans(DevParams P, DevState<R> S, int dim, int jmin, int jcount, int kmin,
-                             double fac) {
+DISCO_D void k_flux_trans_body(const DevParams& P, const DevState<R>& S, int dim, int jmin, int jcount, int kmin, double fac, int bx_, int by_) {
   const int d = dim - 1;
-  int pj = jmin + (int)blockIdx.x % jcount;
-  int pk = kmin + (int)blockIdx.x / jcount;
+  int pj = jmin + (int)bx_ % jcount;
+  int pk = kmin + (int)bx_ / jcount;
   int pair = dim == 1 ? pj + (P.Nr - 1) * pk : pj + P.Nr * pk;
   int base = S.face_off[d][pair], Nf = S.face_off[d][pair + 1] - base;
-  int n = blockIdx.y * blockDim.x + threadIdx.x;
+  int n = by_ * blockDim.x + threadIdx.x;
   if (n >= Nf) return;
   int f = base + n;
   const int N = S.N;
@@ -1211,6 +1246,10 @@ __global__ void __launch_bounds__(256, kMix<R> ? 4 : 1) k_flux_trans(DevParams P
     S.fErz[d][f] = E1; S.fBrz[d][f] = B1; S.fEphi[d][f] = E2;
   }
 }
+template <typename Phys, typename R, int NQ>
+__global__ void __launch_bounds__(256, kMix<R> ? 4 : 1) k_flux_trans(DevParams P, DevState<R> S, int dim, int jmin, int jcount, int kmin, double fac) {
+  k_flux_trans_body<Phys, R, NQ>(P, S, dim, jmin, jcount, kmin, fac, (int)blockIdx.x, (int)blockIdx.y);
+}
 
 // ---- conserved update + sources + move + cons2prim -----------------------------
 // adjust_RK_cons (misc.c:226), flux scatter (riemann.c:314-317) as a gather in
@@ -1220,10 +1259,10 @@ __global__ void __launch_bounds__(256, kMix<R> ? 4 : 1) k_flux_trans(DevParams P
 // path's 64-register cap with every component's loads in flight: CD with
 // cooling / damping, MID for a middle substep (RK3's second), whose store of
 // the running increment would otherwise sit in the component loop.
-template <typename Phys, typename R, int NQ, bool CD = false, bool MID = false>
-__global__ void __launch_bounds__(256, kMix<R> ? 4 : 1) k_update(DevParams P, DevState<R> S, double RK, double fac, int first, int do_c2p) {
+template <typename Phys, typename R, int NQ, bool CD, bool MID>
+DISCO_D void k_update_body(const DevParams& P, const DevState<R>& S, double RK, double fac, int first, int do_c2p, int bx_, int by_) {
   constexpr bool mid = MID;
-  int c = blockIdx.x * blockDim.x + threadIdx.x;
+  int c = bx_ * blockDim.x + threadIdx.x;
   if (c >= S.N) return;
   const int N = S.N;
   int jk = S.cell_ring[c];
@@ -1489,6 +1528,10 @@ __global__ void __launch_bounds__(256, kMix<R> ? 4 : 1) k_update(DevParams P, De
     if (hits & 4) atomicAdd(&S.errs->c2p_no_converge, 1ull);
   }
 }
+template <typename Phys, typename R, int NQ, bool CD = false, bool MID = false>
+__global__ void __launch_bounds__(256, kMix<R> ? 4 : 1) k_update(DevParams P, DevState<R> S, double RK, double fac, int first, int do_c2p) {
+  k_update_body<Phys, R, NQ, CD, MID>(P, S, RK, fac, first, do_c2p, (int)blockIdx.x, (int)blockIdx.y);
+}
 
 // ---- FP64 primitives in and out of the device layout --------------------------
 // The C ABI's views hold FP64 primitives with prim[UPP] the lab omega; the
@@ -1523,10 +1566,10 @@ __global__ void k_prim_out(DevState<R> S, double* dst) {
 // only; fixed3d.c uses set_cell_init (boundary_functions.c:21) on r and z
 // ghosts.  The state after the prim update is position-dependent only.
 template <typename R, int NQ>
-__global__ void __launch_bounds__(kTileCells) k_boundary(DevParams P, DevState<R> S) {
+DISCO_D void k_boundary_body(const DevParams& P, const DevState<R>& S, int bx_, int by_) {
   // one block per chunk of ghost cells (the list holds the rings the plugin
   // fills: fixed.c r ghosts, fixed3d.c r and z ghosts)
-  const int jk = S.ghost_ring[blockIdx.x], i0 = S.ghost_i0[blockIdx.x];
+  const int jk = S.ghost_ring[bx_], i0 = S.ghost_i0[bx_];
   const int k = div_fast(jk, P.mul_nr), j = jk - k * P.Nr;
   const int off = S.ring_off[jk], Np = S.ring_off[jk + 1] - off;
   const int i = i0 + threadIdx.x;
@@ -1553,6 +1596,10 @@ __global__ void __launch_bounds__(kTileCells) k_boundary(DevParams P, DevState<R
   if constexpr (kMix<R>) prim[UPP] -= S.ring_Om[jk];   // ring frame
 #pragma unroll
   for (int q = 0; q < NQ; ++q) S.prim[q * S.N + c] = (R)prim[q];
+}
+template <typename R, int NQ>
+__global__ void __launch_bounds__(kTileCells) k_boundary(DevParams P, DevState<R> S) {
+  k_boundary_body<R, NQ>(P, S, (int)blockIdx.x, (int)blockIdx.y);
 }
 
 // Per-ring ghost values of fixed.c / fixed3d.c for the axisymmetric disk
@@ -1762,8 +1809,8 @@ DISCO_D double cell_mindt(const DevParams& P, const DevState<R>& S, int c) {
 }
 
 template <typename Phys, typename R, int NQ>
-__global__ void k_mindt(DevParams P, DevState<R> S) {
-  int c = blockIdx.x * blockDim.x + threadIdx.x;
+DISCO_D void k_mindt_body(const DevParams& P, const DevState<R>& S, int bx_, int by_) {
+  int c = bx_ * blockDim.x + threadIdx.x;
   double dtc = c < S.N ? cell_mindt<Phys, R, NQ>(P, S, c) : 1.0e300;
   // dt > 0: its IEEE bits order like unsigned integers; NaN sorts above.
   __shared__ unsigned long long red[32];
@@ -1779,9 +1826,13 @@ __global__ void k_mindt(DevParams P, DevState<R> S) {
     if (lane == 0) atomicMin((unsigned long long*)&S.scal[SC_MIN], b);
   }
 }
+template <typename Phys, typename R, int NQ>
+__global__ void k_mindt(DevParams P, DevState<R> S) {
+  k_mindt_body<Phys, R, NQ>(P, S, (int)blockIdx.x, (int)blockIdx.y);
+}
 
 // dt = CFL * min (misc.c:52-78); clamp to T_End (check_dt, domain.c:433).
-static __global__ void k_dt_finalize(DevParams P, double* scal) {
+DISCO_D void dt_finalize_one(const DevParams& P, double* scal) {
   double m = __longlong_as_double(*(long long*)&scal[SC_MIN]);
   double dt0 = P.maxDT / P.CFL;
   if (dt0 <= 0.0) dt0 = 1.0e100;
@@ -1792,10 +1843,11 @@ static __global__ void k_dt_finalize(DevParams P, double* scal) {
   *(float*)&scal[SC_DTF] = (float)dt;
   *(unsigned long long*)&scal[SC_MIN] = 0x7ff0000000000000ull;   // +inf
 }
+static __global__ void k_dt_finalize(DevParams P, double* scal) { dt_finalize_one(P, scal); }
 
 // After the first substep: t += dt (timestep.c:136), analytic planet motion
 // (Planets/circular.c:44-46), clean_pi on planets (misc.c:27-34).
-static __global__ void k_after_first(DevParams P, double* scal, DevPlanet* pl, int planets_id,
+DISCO_D void after_first_one(const DevParams& P, double* scal, DevPlanet* pl, int planets_id,
                               DevErrs* errs) {
   double dt = scal[SC_DT];
   double t = scal[SC_T];   // movePlanets sees the time before the step's update
@@ -1816,6 +1868,8 @@ static __global__ void k_after_first(DevParams P, double* scal, DevPlanet* pl, i
   }
   errs->steps += 1;
 }
+static __global__ void k_after_first(DevParams P, double* scal, DevPlanet* pl, int planets_id,
+                              DevErrs* errs) { after_first_one(P, scal, pl, planets_id, errs); }
 
 // ---- calc_prim (misc.c:300-335) as its own pass (after B_faces_to_cells) --------
 template <typename Phys, typename R, int NQ>

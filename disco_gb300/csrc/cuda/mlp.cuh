@@ -42,6 +42,9 @@ struct MlpDev {
   const bf16* W3b;
   const float* params;   // FP32 masters (biases read from here)
   float xm[kMlpIn], xs[kMlpIn], ym[kMlpOut], ys[kMlpOut];
+  // cons2prim considers the learned start only where the previous
+  // primitives leave a residual of the two Noble equations above this
+  double warm_floor;
 };
 
 struct __align__(16) MlpSmem {

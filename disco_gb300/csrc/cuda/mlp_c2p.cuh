@@ -37,9 +37,9 @@ struct C2PRecord {
 // calc_prim of the GRMHD module with the learned starting point: each warp
 // evaluates the network for its 32 cells on the tensor cores, then every
 // thread solves its cell from the corrected start -- or from the previous
-// primitives where those leave the smaller residual, the reference's own
-// start kept as the fallback -- and recovers its primitives as calc_prim
-// does.  use_guess 0 starts every cell from the previous primitives (the
+// primitives where those leave the smaller residual, or a residual at most
+// m.warm_floor: the reference's own start is the fallback -- and recovers
+// its primitives as calc_prim does.  use_guess 0 starts every cell from the previous primitives (the
 // reference's calc_prim) and may record training pairs.  256 threads per
 // block.
 template <typename Phys, typename R, int NQ>
@@ -88,7 +88,8 @@ __global__ void __launch_bounds__(256) k_c2p_guess(DevParams P, DevState<R> S, M
   if (use_guess) {
     double guess[2];
     Phys::c2p_guess_from(v, &Ys[wid][lane * kMlpOut], lu2, lth, guess);
-    if (Phys::c2p_residual(v, guess[0], guess[1]) < Phys::c2p_residual(v, v20, eta0)) {
+    const double rw = Phys::c2p_residual(v, v20, eta0);
+    if (rw > m.warm_floor && Phys::c2p_residual(v, guess[0], guess[1]) < rw) {
       v20 = guess[0];
       eta0 = guess[1];
       guessed = 1;

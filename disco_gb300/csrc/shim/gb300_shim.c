@@ -38,9 +38,10 @@
 static disco_gpu *G = NULL;
 static disco_host_domain *H = NULL;
 
+/* the library returns 0 or a count on success, a negative code on error */
 static void gb300_check(int rc, const char *what)
 {
-   if(rc != 0) {
+   if(rc < 0) {
       fprintf(stderr, "gb300: %s failed (%d): %s\n", what, rc, disco_last_error());
       exit(1);
    }
