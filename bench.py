@@ -118,15 +118,17 @@ KERNEL_SYMBOL = {"flux_trans": "k_flux_trans", "plm_slopes": "k_plm_slopes", "pl
                  "ct_edge_flag": "k_set_flag"}
 
 
-def _traffic(func: str, alg_bytes: float):
+def _traffic(func: str, alg_bytes: float, workload: str):
     """DRAM bytes per launch of kernel function `func`: the ratio of measured
-    to algorithmic bytes from a committed ncu summary (a line
-    `traffic_ratio <func> <ratio>` in profiles/<func>_*_dram.md, captured on a
-    case larger than L2 but a few GB at most), times this launch's
-    algorithmic bytes -- the kernel's traffic grows in proportion to the
-    cells and faces it processes.  Returns (bytes, source)."""
+    to algorithmic bytes from a committed ncu summary of the same workload
+    family and precision (a line `traffic_ratio <func> <ratio>` in
+    profiles/<func>_<workload>*_dram.md, captured on a case larger than L2
+    but a few GB at most), times this launch's algorithmic bytes -- the
+    kernel's traffic grows in proportion to the cells and faces it
+    processes.  (None, None) when no capture of this workload exists.
+    Returns (bytes, source)."""
     import glob
-    for path in sorted(glob.glob(os.path.join(ROOT, "profiles", f"{func}_*_dram.md"))):
+    for path in sorted(glob.glob(os.path.join(ROOT, "profiles", f"{func}_{workload}*_dram.md"))):
         for ln in open(path):
             parts = ln.split()
             if len(parts) == 3 and parts[0] == "traffic_ratio" and parts[1] == func:
@@ -304,6 +306,10 @@ def measure_batch(args, wl):
         state_bytes = N * nq * (4 * 8 + 4 * sw)
         flush = 2 * L2_BYTES if state_bytes < 4 * L2_BYTES else 0
         b.run(args.warmup)
+        tune_steps = 0
+        while b.info()["split"] < 0:   # the split autotuner's steps: more warm-up
+            b.run(1)
+            tune_steps += 1
         torch.cuda.synchronize()
         clk = ClockSampler(dev) if prec == 1 else None
         if clk:
@@ -317,7 +323,9 @@ def measure_batch(args, wl):
         clocks = clk.stop() if clk else None
         res[prec] = {"ms": ms, "cells": cells, "N": N, "nq": nq, "sw": sw, "flush": flush,
                      "launches": launches, "clocks": clocks,
-                     "value": cells * args.steps / (ms / 1e3)}
+                     "value": cells * args.steps / (ms / 1e3),
+                     "batch": {**b.info(), "autotune_warmup_steps": tune_steps,
+                               "launches_per_step": launches / args.steps}}
     sys.path.insert(0, os.path.join(ROOT, "tests"))
     from helpers import cell_radius, grouped_rel_l1
     worst, worst128, per_member = {}, {}, []
@@ -336,6 +344,16 @@ def measure_batch(args, wl):
                      "max_over_quantities_Nr_ge_128": max(worst128.values()) if worst128 else None,
                      "per_member_Nr_and_max": sorted(per_member),
                      "note": "maximum over the batch members of the per-member error"}
+    # the same members with one graph branch each (no multi-instance groups)
+    nb = dg.Batch(sets[1], groups=False)
+    nb.run(args.warmup)
+    l0 = dg.lib().disco_gpu_launch_count()
+    nms = nb.run_timed(args.steps, flush_bytes=res[1]["flush"])
+    res[1]["batch"]["branch_per_member"] = {
+        "ms_per_step": nms / args.steps, "launches_per_step": (dg.lib().disco_gpu_launch_count() - l0) / args.steps,
+        "value": res[1]["cells"] * args.steps / (nms / 1e3)}
+    nb.close()
+    res[1]["batch"]["stages"] = batches[1].profile(2)
     # per-kernel profile of the largest member (its own stream, no graph)
     big = max(range(len(mem)), key=lambda i: sets[1][i].num_cells)
     res["profile"] = sets[1][big].profile(3)
@@ -382,12 +400,15 @@ def measure_batch(args, wl):
 
 def measure_learned_c2p(args, wl, steps=None, warmup=None):
     """GRMHD torus: the Newton cons2prim started from the previous
-    primitives (the reference's start) against the learned starting point.
-    One domain: W warm-up steps, K timed steps with the plain start; then
+    primitives (the reference's start) against the learned starting point,
+    both from the same state.  One domain: W warm-up steps, its state saved;
     training pairs recorded by the running torus's own cons2prim solves
-    (every 8th real cell, four steps), the MLP trained on the GPU, attached,
-    and K more timed steps.  Reports the mean iteration at first convergence (k_converge)
-    and the mean iterations per call of both, and both throughputs."""
+    (every 8th real cell, four steps) and the MLP trained on the GPU; then
+    the saved state restored and K timed steps with the plain start, restored
+    again and K timed steps with the learned start attached.  Reports for
+    both the mean iteration at first convergence (k_converge), the mean
+    iterations per call, the calls that did not converge and the throughput,
+    and the relative L1 difference of the two final states."""
     import torch
     import disco_gb300 as dg
     K = steps or args.steps
@@ -398,9 +419,9 @@ def measure_learned_c2p(args, wl, steps=None, warmup=None):
     cells = d.num_real_cells
     d.run(W)
     torch.cuda.synchronize()
-    d.c2p_stats(reset=True)
-    ms_plain = d.run_timed(K)
-    sp = d.c2p_stats(reset=True)
+    keys = ("piph", "dphi", "wiph", "prim", "cons")
+    s0 = d.state()
+    saved = {k: s0[k].copy() for k in keys}
     m = dg.Mlp(seed=1, capacity=1 << 21)
     t0 = time.perf_counter()
     held = m.harvest(d, stride=8, steps=4)
@@ -408,29 +429,58 @@ def measure_learned_c2p(args, wl, steps=None, warmup=None):
     m.fit_norm()
     l0, l1 = m.train(2000, batch=8192, lr=2e-3, seed=5)
     t2 = time.perf_counter()
-    d.attach_guess(m)
-    d.run(1)
-    d.c2p_stats(reset=True)
-    ms_learned = d.run_timed(K)
-    sl = d.c2p_stats(reset=True)
-    st = d.status()
+
+    def arm(guess, ratio=1.0):
+        d.upload(**saved)
+        m.set_gate(0.0, ratio)
+        d.attach_guess(m if guess else None)
+        nc0 = d.status()["c2p_no_converge"]
+        d.c2p_stats(reset=True)
+        ms = d.run_timed(K)
+        sc = d.c2p_stats(reset=True)
+        nc = d.status()["c2p_no_converge"] - nc0
+        return ms, sc, nc, d.state()["cons"]
+
+    ms_plain, sp, ncp, up = arm(False)
+    ms_learned, sl, ncl, ul = arm(True)
+    gated = arm(True, 1e-2)
+    d.attach_guess(None)
+    real = d.host.real_mask()
+
+    def rdiff(u):
+        return max(float(np.abs(u[q, real] - up[q, real]).sum() / max(np.abs(up[q, real]).sum(), 1e-300))
+                   for q in range(up.shape[0]))
+    diff = rdiff(ul)
     d.close()
     m.close()
+
     def mean(s, k):
         return s[k] / s["calls"] if s["calls"] else None
     kp, kl = mean(sp, "kconv"), mean(sl, "kconv")
+    ms_g, sg, ncg, ug = gated
     return {"cells": cells, "steps": K,
             "plain": {"zone_updates_per_s": cells * K / (ms_plain / 1e3), "ms_per_step": ms_plain / K,
-                      "mean_k_converge": kp, "mean_iterations": mean(sp, "iters"), "calls": sp["calls"]},
+                      "mean_k_converge": kp, "mean_iterations": mean(sp, "iters"), "calls": sp["calls"],
+                      "no_converge": ncp},
             "learned": {"zone_updates_per_s": cells * K / (ms_learned / 1e3), "ms_per_step": ms_learned / K,
                         "mean_k_converge": kl, "mean_iterations": mean(sl, "iters"), "calls": sl["calls"],
+                        "no_converge": ncl,
                         "guess_used_fraction": sl["guessed"] / sl["calls"] if sl["calls"] else None},
             "k_converge_ratio_plain_over_learned": (kp / kl) if kp and kl else None,
+            "final_state_rel_l1_learned_vs_plain": diff,
+            "learned_gate_1e-2": {"zone_updates_per_s": cells * K / (ms_g / 1e3), "ms_per_step": ms_g / K,
+                                  "mean_k_converge": mean(sg, "kconv"), "mean_iterations": mean(sg, "iters"),
+                                  "no_converge": ncg,
+                                  "guess_used_fraction": sg["guessed"] / sg["calls"] if sg["calls"] else None,
+                                  "final_state_rel_l1_vs_plain": rdiff(ug),
+                                  "gate": "learned start taken where its residual is below 1e-2 of the "
+                                          "previous primitives'"},
             "training": {"pairs": held, "harvest_s": t1 - t0, "train_s": t2 - t1, "steps": 2000, "batch": 8192,
                          "loss_first": l0, "loss_last": l1},
-            "c2p_no_converge": st["c2p_no_converge"],
             "k_converge_definition": ("Newton iteration at which the relative change of eta first falls "
-                                      "below 1e-12 (the 10 polishing iterations that follow are not counted)")}
+                                      "below 1e-12 (the 10 polishing iterations that follow are not counted; "
+                                      "0 for a call that never converged; a learned start that did not "
+                                      "converge adds its iterations to the fallback solve's)")}
 
 
 def measure_ours(args, wl, rank):
@@ -791,7 +841,7 @@ def main():
     top_bytes = top["bytes"] / top["launches"]
     top_avg_s = top["ms"] / top["launches"] / 1e3
     achieved = top_bytes / top_avg_s / 1e9
-    traffic, traffic_src = _traffic(top_name, top_bytes)
+    traffic, traffic_src = _traffic(top_name, top_bytes, args.workload)
     # fused-RK2 compulsory bytes per zone-update: NQ (6 s_W + 4 s_U) + 6 x 8
     # (the RK copy of the state is one s_W write and one s_W read: the mixed
     # path keeps the first substep's increment in R), plus 25 x 8 for the
@@ -825,6 +875,8 @@ def main():
         "e2e": res["e2e"],
         **({"report_reduction": res["report"]} if "report" in res else {}),
         **({"learned_c2p": res["learned_c2p"]} if "learned_c2p" in res else {}),
+        **({"batch": {"mixed": res[1]["batch"], "fp64": res[0]["batch"]}}
+           if "profiled" in res else {}),
         "gpu_launches": int(res[ch]["launches"]),
         "clocks": res[ch]["clocks"],
     }

@@ -59,6 +59,10 @@ class DiscoParams(C.Structure):
         ("dampLenOuter", C.c_double), ("dampTimeUpper", C.c_double), ("dampLenUpper", C.c_double),
         ("dampTimeLower", C.c_double), ("dampLenLower", C.c_double),
         ("maxNp", C.c_int),
+        ("sinkNumber", C.c_int),
+        ("sinkPar1", C.c_double), ("sinkPar2", C.c_double), ("sinkPar4", C.c_double), ("sinkPar5", C.c_double),
+        ("nozzlePar1", C.c_double), ("nozzlePar2", C.c_double), ("nozzlePar3", C.c_double),
+        ("nozzlePar4", C.c_double),
     ]
 
 
@@ -161,16 +165,23 @@ SIGNATURES = {
     "disco_mlp_params": (C.c_int, [_P, C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_float),
                                    C.POINTER(C.c_float)]),
     "disco_gpu_attach_guess": (C.c_int, [_P, _P]),
-    "disco_mlp_set_floor": (C.c_int, [_P, C.c_double]),
+    "disco_mlp_set_gate": (C.c_int, [_P, C.c_double, C.c_double]),
     "disco_gpu_c2p_stats": (C.c_int, [_P, C.POINTER(C.c_longlong), C.c_int]),
     "disco_gpu_report": (C.c_int, [_P, C.POINTER(C.c_double), C.c_int]),
     "disco_gpu_diag_count": (C.c_int, [_P]),
+    "disco_gpu_sink_accum": (C.c_int, [_P, C.POINTER(C.c_double), C.c_int, C.c_int]),
     "disco_gpu_diag_download": (C.c_int, [_P, C.POINTER(C.c_double), C.c_longlong, C.POINTER(C.c_double)]),
     "disco_gpu_diag_upload": (C.c_int, [_P, C.POINTER(C.c_double), C.c_longlong, C.c_double]),
     "disco_batch_create": (C.c_int, [C.POINTER(_P), C.c_int, C.POINTER(_P)]),
+    "disco_batch_create_flags": (C.c_int, [C.POINTER(_P), C.c_int, C.c_int, C.POINTER(_P)]),
     "disco_batch_run": (C.c_int, [_P, C.c_int]),
     "disco_batch_run_timed": (C.c_int, [_P, C.c_int, C.c_size_t, C.POINTER(C.c_double)]),
     "disco_batch_free": (None, [_P]),
+    "disco_batch_set_grid": (C.c_int, [_P, C.c_int]),
+    "disco_batch_profile": (C.c_int, [_P, C.c_int, C.POINTER(DiscoKernelTime), C.c_int, C.POINTER(C.c_int)]),
+    "disco_batch_set_split": (C.c_int, [_P, C.c_int]),
+    "disco_batch_info": (C.c_int, [_P, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                   C.POINTER(C.c_int), C.POINTER(C.c_double)]),
     "disco_gpu_time": (C.c_double, [_P]),
     "disco_gpu_num_cells": (C.c_long, [_P]),
     "disco_gpu_num_real_cells": (C.c_long, [_P]),
@@ -293,6 +304,16 @@ class Domain:
         rc = lib().disco_gpu_report(self._g, out, len(out))
         _check(rc if rc < 0 else 0, "disco_gpu_report")
         return {k: out[i] for i, k in enumerate(self.REPORT_KEYS)}
+
+    SINK_KEYS = ("gravL", "dM", "accL", "Ls", "kin", "therm", "linXmom", "linYmom")
+
+    def sink_accum(self, reset: bool = False) -> list:
+        """The sink bodies' accumulators (disco_gpu_sink_accum): one dict per
+        sink body, keys SINK_KEYS; reset zeroes them after the read."""
+        out = (C.c_double * (8 * 4))()
+        n = lib().disco_gpu_sink_accum(self._g, out, 4, int(reset))
+        _check(n if n < 0 else 0, "disco_gpu_sink_accum")
+        return [{k: out[8 * b + i] for i, k in enumerate(self.SINK_KEYS)} for b in range(n)]
 
     def diagnostics(self) -> dict:
         """analysis.c's ring diagnostics as timestep() accumulated them:
@@ -521,10 +542,11 @@ class Mlp:
                                     g.ctypes.data_as(fp)), "disco_mlp_grad")
         return loss.value, g
 
-    def set_floor(self, floor: float) -> None:
-        """Residual of the previous primitives at or below which cons2prim
-        keeps them as the start (used at the next attach)."""
-        _check(lib().disco_mlp_set_floor(self._m, float(floor)), "disco_mlp_set_floor")
+    def set_gate(self, floor: float = 0.0, ratio: float = 1.0) -> None:
+        """cons2prim takes the model's start where the previous primitives'
+        residual is above floor and the model's is below ratio times it
+        (used at the next attach)."""
+        _check(lib().disco_mlp_set_gate(self._m, float(floor), float(ratio)), "disco_mlp_set_gate")
 
     def predict(self, X: np.ndarray) -> np.ndarray:
         X = np.ascontiguousarray(X, np.float32)
@@ -582,14 +604,16 @@ def convert_check(x: np.ndarray, y: np.ndarray) -> dict:
 
 class Batch:
     """Independent domains advanced together (disco_gpu_batch.h): each step is
-    one CUDA-graph launch with one branch per member, every member using its
-    own CFL dt.  The members stay usable on their own (state(), status())."""
+    one CUDA-graph launch, every member using its own CFL dt; members of one
+    module, precision and launch sequence are advanced by multi-instance
+    stage kernels.  The members stay usable on their own (state(), status())."""
 
-    def __init__(self, members: list):
+    def __init__(self, members: list, groups: bool = True):
         self.members = list(members)
         arr = (C.c_void_p * len(self.members))(*[m._g.value for m in self.members])
         b = C.c_void_p()
-        _check(lib().disco_batch_create(arr, len(self.members), C.byref(b)), "disco_batch_create")
+        _check(lib().disco_batch_create_flags(arr, len(self.members), 0 if groups else 1, C.byref(b)),
+               "disco_batch_create")
         self._b = b
 
     @property
@@ -604,6 +628,31 @@ class Batch:
         _check(lib().disco_batch_run_timed(self._b, int(nsteps), int(flush_bytes), C.byref(ms)),
                "disco_batch_run_timed")
         return ms.value
+
+    def set_grid(self, ctas_per_sm: int) -> None:
+        """At most this many blocks per SM in the multi-instance stage kernels."""
+        _check(lib().disco_batch_set_grid(self._b, int(ctas_per_sm)), "disco_batch_set_grid")
+
+    def set_split(self, split: int) -> None:
+        """Sub-groups per group (0: every member on its own sequence; -1:
+        choose by timing the candidates)."""
+        _check(lib().disco_batch_set_split(self._b, int(split)), "disco_batch_set_split")
+
+    def profile(self, nsteps: int) -> list:
+        """Per stage of the groups: (name, launches, summed ms) over nsteps
+        steps launched without the graph (disco_batch_profile)."""
+        out = (DiscoKernelTime * 64)()
+        n = C.c_int()
+        _check(lib().disco_batch_profile(self._b, int(nsteps), out, 64, C.byref(n)), "disco_batch_profile")
+        return [(out[i].name.decode(), out[i].launches, out[i].ms) for i in range(n.value)]
+
+    def info(self) -> dict:
+        g, k, sp, c = C.c_int(), C.c_int(), C.c_int(), C.c_int()
+        t = (C.c_double * 6)()
+        _check(lib().disco_batch_info(self._b, C.byref(g), C.byref(k), C.byref(sp), C.byref(c), t),
+               "disco_batch_info")
+        return {"groups": g.value, "grouped_members": k.value, "split": sp.value, "ctas_per_sm": c.value,
+                "tune_ms": {n: t[i] for i, n in enumerate((1, 2, 4, 8, 16, 0))}}
 
     def close(self) -> None:
         if getattr(self, "_b", None) is not None and self._b.value:

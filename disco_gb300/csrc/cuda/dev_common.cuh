@@ -57,6 +57,11 @@ struct DevParams {
   int damp_type[4];
   double damp_time[4], damp_len[4];
   double dom_rmin, dom_rmax, dom_zmax;
+  // accreting sinks and the nozzle (sink.c:105-247): Sink_Type, the number
+  // of sink bodies (Sink_Number capped at Npl), Sink_Par1..5, Nozzle_Type,
+  // Nozzle_Par1..4
+  int sink_type, sink_bodies, nozzle_type;
+  double sink_par[5], nozzle_par[4];
   int Npl;
   // GRMHD: the black-hole mass of the Kerr-Schild metric (Metric_Par2)
   double gr_M;

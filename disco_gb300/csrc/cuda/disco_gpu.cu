@@ -28,54 +28,147 @@ struct disco_gpu {
   InstanceBase* impl;
 };
 
-// A batch: one graph per piph parity, built by stream capture with a
-// fork/join over the members' own streams, so the captured graph has one
-// branch per member.
+// A batch: members of one module, precision and launch sequence form
+// groups at create (multi_plan.cuh); the other members run their own launch
+// sequences.  A step is one graph launch, captured per piph parity with a
+// fork/join: one branch per sub-group, each sub-group a share of a group
+// advanced by the multi-instance stage kernels (one launch per stage over
+// all its members), and one branch per member that runs its own sequence.
+// The split -- sub-groups per group, from kSplitCand, 0 meaning that every
+// member runs its own sequence -- trades launches against concurrency
+// between the stages of different sub-groups.  It is chosen by timing each
+// candidate on two of the batch's first steps (real steps: the split does
+// not change what is computed).
+constexpr int kSplitCand[] = {1, 2, 4, 8, 16, 0};
+constexpr int kSplitN = 6, kTuneReps = 2;
+struct BatchSplit {
+  bool built = false;
+  std::vector<MultiPlanBase*> plans;
+  std::vector<cudaStream_t> st;        // one per plan
+  std::vector<int> lead;               // the member that counts a plan's launches
+  std::vector<int> solo;               // members on their own sequences
+  std::vector<cudaEvent_t> join;       // one per branch
+  cudaGraphExec_t g[2] = {nullptr, nullptr};
+  std::vector<long long> per;          // launches per step, per member
+  void drop_graphs() {
+    for (auto& x : g) if (x) { cudaGraphExecDestroy(x); x = nullptr; }
+  }
+  void release() {
+    drop_graphs();
+    for (auto p : plans) delete p;
+    for (auto s : st) if (s) cudaStreamDestroy(s);
+    for (auto e : join) if (e) cudaEventDestroy(e);
+    plans.clear(); st.clear(); join.clear(); lead.clear(); solo.clear();
+    built = false;
+  }
+};
 struct disco_batch {
   std::vector<InstanceBase*> m;
+  std::vector<std::vector<int>> groups;   // member indices of each group (two or more)
+  std::vector<int> ungrouped;             // members no group takes
+  BatchSplit sets[kSplitN];
   cudaStream_t root = nullptr;
   cudaEvent_t fork = nullptr;
-  std::vector<cudaEvent_t> join;
-  cudaGraphExec_t graph[2] = {nullptr, nullptr};
-  long long nodes = 0;          // kernel launches per graph
-  std::vector<long long> per;   // per member
   int parity = 0;
+  int split_i = -1;                       // the split in force (-1: timing the candidates)
+  int ctas = 8;                           // blocks per SM of the stage kernels (capped by residency)
+  int tune_i = 0;
+  double tune_ms[kSplitN] = {0, 0, 0, 0, 0, 0};
   void* flush = nullptr;
   size_t flush_size = 0;
   ~disco_batch() {
-    for (auto& g : graph) if (g) cudaGraphExecDestroy(g);
-    for (auto e : join) if (e) cudaEventDestroy(e);
+    for (auto& x : sets) x.release();
     if (fork) cudaEventDestroy(fork);
     if (root) cudaStreamDestroy(root);
     if (flush) cudaFree(flush);
   }
 };
 
-static int batch_build(disco_batch* b, int par) {
+// The plans and streams of split candidate ci (outside any capture).
+static int batch_split_build(disco_batch* b, int ci) {
+  BatchSplit& x = b->sets[ci];
+  if (x.built) return 0;
+  const int split = kSplitCand[ci];
+  x.solo = b->ungrouped;
+  for (auto& grp : b->groups) {
+    if (split == 0) {
+      x.solo.insert(x.solo.end(), grp.begin(), grp.end());
+      continue;
+    }
+    // min(split, size) sub-groups, balanced by cells: largest member first,
+    // each to the sub-group with the fewest cells so far
+    const int k = std::min<int>(split, (int)grp.size());
+    std::vector<int> order = grp;
+    std::stable_sort(order.begin(), order.end(), [&](int u, int v) { return b->m[u]->N > b->m[v]->N; });
+    std::vector<std::vector<int>> sub(k);
+    std::vector<long> load(k, 0);
+    for (int i : order) {
+      const int s = (int)(std::min_element(load.begin(), load.end()) - load.begin());
+      sub[s].push_back(i);
+      load[s] += b->m[i]->N;
+    }
+    for (auto& v : sub) {
+      std::sort(v.begin(), v.end());
+      MultiPlanBase* p = b->m[v[0]]->new_multi_plan();
+      if (!p) { disco_set_error("disco_batch: a grouped member has no multi-instance plan"); return DISCO_E_STATE; }
+      for (size_t t = 1; t < v.size(); ++t) p->add(b->m[v[t]]);
+      x.plans.push_back(p);
+      x.lead.push_back(v[0]);
+      int rc = p->prepare();
+      if (rc) return rc;
+      cudaStream_t s;
+      CK(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+      x.st.push_back(s);
+    }
+  }
+  std::sort(x.solo.begin(), x.solo.end());
+  x.join.assign(x.plans.size() + x.solo.size(), nullptr);
+  for (auto& e : x.join) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+  x.built = true;
+  return 0;
+}
+
+static int batch_build(disco_batch* b, int ci, int par) {
+  BatchSplit& x = b->sets[ci];
   long long before = g_launches.load();
   CK(cudaStreamBeginCapture(b->root, cudaStreamCaptureModeThreadLocal));
   CK(cudaEventRecord(b->fork, b->root));
-  b->per.assign(b->m.size(), 0);
-  for (size_t i = 0; i < b->m.size(); ++i) {
+  x.per.assign(b->m.size(), 0);
+  size_t br = 0;
+  for (size_t p = 0; p < x.plans.size(); ++p, ++br) {
+    long long l0 = g_launches.load();
+    CK(cudaStreamWaitEvent(x.st[p], b->fork, 0));
+    int rc = x.plans[p]->launch_step(par, x.st[p], b->ctas, nullptr);
+    if (rc) {
+      cudaGraph_t g = nullptr;
+      cudaStreamEndCapture(b->root, &g);
+      if (g) cudaGraphDestroy(g);
+      return rc;
+    }
+    CK(cudaEventRecord(x.join[br], x.st[p]));
+    CK(cudaStreamWaitEvent(b->root, x.join[br], 0));
+    x.per[x.lead[p]] += g_launches.load() - l0;
+  }
+  for (int i : x.solo) {
     long long l0 = g_launches.load();
     CK(cudaStreamWaitEvent(b->m[i]->stream(), b->fork, 0));
     b->m[i]->launch_step(par);
-    CK(cudaEventRecord(b->join[i], b->m[i]->stream()));
-    CK(cudaStreamWaitEvent(b->root, b->join[i], 0));
-    b->per[i] = g_launches.load() - l0;
+    CK(cudaEventRecord(x.join[br], b->m[i]->stream()));
+    CK(cudaStreamWaitEvent(b->root, x.join[br], 0));
+    x.per[i] += g_launches.load() - l0;
+    ++br;
   }
   cudaGraph_t g;
   CK(cudaStreamEndCapture(b->root, &g));
-  b->nodes = g_launches.load() - before;
-  g_launches -= b->nodes;   // counted on each replay
-  CK(cudaGraphInstantiate(&b->graph[par], g, 0));
+  g_launches -= g_launches.load() - before;   // counted on each replay
+  cudaError_t e = cudaGraphInstantiate(&x.g[par], g, 0);
   cudaGraphDestroy(g);
+  CK(e);
+  CK(cudaGraphUpload(x.g[par], b->root));
   return 0;
 }
 
 static int batch_steps(disco_batch* b, int nsteps, size_t flush_bytes, double* ms) {
-  for (int p = 0; p < 2; ++p)
-    if (!b->graph[p]) { int rc = batch_build(b, p); if (rc) return rc; }
   if (flush_bytes > b->flush_size) {
     if (b->flush) cudaFree(b->flush);
     b->flush = nullptr; b->flush_size = 0;
@@ -84,13 +177,41 @@ static int batch_steps(disco_batch* b, int nsteps, size_t flush_bytes, double* m
   }
   std::vector<cudaEvent_t> ev(ms ? 2 * (size_t)nsteps : 0);
   for (auto& e : ev) CK(cudaEventCreate(&e));
+  cudaEvent_t te[2] = {nullptr, nullptr};
+  if (b->split_i < 0)
+    for (auto& e : te) CK(cudaEventCreate(&e));
+  std::vector<long long> launched(b->m.size(), 0);
   for (int s = 0; s < nsteps; ++s) {
+    const bool tuning = b->split_i < 0;
+    const int ci = tuning ? b->tune_i / kTuneReps : b->split_i;
+    int rc = batch_split_build(b, ci);
+    if (rc) return rc;
+    BatchSplit& x = b->sets[ci];
+    if (!x.g[b->parity]) { rc = batch_build(b, ci, b->parity); if (rc) return rc; }
+    for (size_t i = 0; i < b->m.size(); ++i) launched[i] += x.per[i];
     if (ms && flush_bytes) CK(cudaMemsetAsync(b->flush, s & 0xff, flush_bytes, b->root));
     if (ms) CK(cudaEventRecord(ev[2 * s], b->root));
-    CK(cudaGraphLaunch(b->graph[b->parity], b->root));
+    if (tuning) CK(cudaEventRecord(te[0], b->root));
+    CK(cudaGraphLaunch(x.g[b->parity], b->root));
+    if (tuning) CK(cudaEventRecord(te[1], b->root));
     if (ms) CK(cudaEventRecord(ev[2 * s + 1], b->root));
     b->parity ^= 1;
+    if (tuning) {
+      float t;
+      CK(cudaEventSynchronize(te[1]));
+      CK(cudaEventElapsedTime(&t, te[0], te[1]));
+      if (b->tune_i % kTuneReps == 0 || t < b->tune_ms[ci]) b->tune_ms[ci] = t;
+      if (++b->tune_i == kSplitN * kTuneReps) {
+        int best = 0;
+        for (int c = 1; c < kSplitN; ++c)
+          if (b->tune_ms[c] < b->tune_ms[best]) best = c;
+        b->split_i = best;
+        for (int c = 0; c < kSplitN; ++c)
+          if (c != best) b->sets[c].release();
+      }
+    }
   }
+  for (auto e : te) if (e) cudaEventDestroy(e);
   CK(cudaStreamSynchronize(b->root));
   if (ms) {
     double tot = 0;
@@ -103,7 +224,7 @@ static int batch_steps(disco_batch* b, int nsteps, size_t flush_bytes, double* m
     for (auto e : ev) cudaEventDestroy(e);
   }
   for (size_t i = 0; i < b->m.size(); ++i) {
-    int rc = b->m[i]->after_external_steps(nsteps, b->per[i] * nsteps);
+    int rc = b->m[i]->after_external_steps(nsteps, launched[i]);
     if (rc) return rc;
   }
   return 0;
@@ -123,7 +244,7 @@ struct disco_mlp {
   disco::MlpBatch bt{};
   long bcap = 0;
   long long step = 0;
-  double warm_floor = 0.0;
+  double warm_floor = 0.0, warm_ratio = 1.0;
   ~disco_mlp() {
     for (void* q : {(void*)p, (void*)m1, (void*)m2, (void*)grad, (void*)loss, (void*)W1b, (void*)W2b, (void*)W3b,
                     (void*)X, (void*)Y, (void*)count})
@@ -157,6 +278,7 @@ struct disco_mlp {
     for (int q = 0; q < F; ++q) { v.xm[q] = norm[q]; v.xs[q] = norm[F + q]; }
     for (int q = 0; q < 2; ++q) { v.ym[q] = norm[2 * F + q]; v.ys[q] = norm[2 * F + 2 + q]; }
     v.warm_floor = warm_floor;
+    v.warm_ratio = warm_ratio;
     return v;
   }
   int refresh_bf16() {
@@ -380,9 +502,13 @@ int disco_mlp_params(disco_mlp* m, float* get, const float* set, float* norm_get
   return 0;
 }
 
-int disco_mlp_set_floor(disco_mlp* m, double floor) {
-  if (!m || !(floor >= 0.0)) { disco_set_error("disco_mlp_set_floor: bad argument"); return DISCO_E_ARG; }
+int disco_mlp_set_gate(disco_mlp* m, double floor, double ratio) {
+  if (!m || !(floor >= 0.0) || !(ratio > 0.0 && ratio <= 1.0)) {
+    disco_set_error("disco_mlp_set_gate: bad argument");
+    return DISCO_E_ARG;
+  }
   m->warm_floor = floor;
+  m->warm_ratio = ratio;
   return 0;
 }
 
@@ -427,6 +553,11 @@ int disco_gpu_create(const disco_host_domain* dom, int precision, disco_gpu** ou
 int disco_gpu_report(disco_gpu* g, double* out, int nout) {
   if (!g || !out || nout < 0) { disco_set_error("disco_gpu_report: bad argument"); return DISCO_E_ARG; }
   return g->impl->report(out, nout);
+}
+
+int disco_gpu_sink_accum(disco_gpu* g, double* out, int max_bodies, int reset) {
+  if (!g || max_bodies < 0) { disco_set_error("disco_gpu_sink_accum: bad argument"); return DISCO_E_ARG; }
+  return g->impl->sink_accum(out, max_bodies, reset);
 }
 
 int disco_gpu_diag_count(disco_gpu* g) {
@@ -542,7 +673,13 @@ int disco_gpu_getmindt_noalloc(disco_gpu* g, double* dt) {
   return g->impl->getmindt_noalloc(dt);
 }
 int disco_batch_create(disco_gpu* const* members, int n, disco_batch** out) {
-  if (!members || n <= 0 || !out) { disco_set_error("disco_batch_create: bad argument"); return DISCO_E_ARG; }
+  return disco_batch_create_flags(members, n, 0, out);
+}
+int disco_batch_create_flags(disco_gpu* const* members, int n, int flags, disco_batch** out) {
+  if (!members || n <= 0 || !out || (flags & ~DISCO_BATCH_NO_GROUPS)) {
+    disco_set_error("disco_batch_create: bad argument");
+    return DISCO_E_ARG;
+  }
   int par = -1;
   for (int i = 0; i < n; ++i) {
     if (!members[i]) { disco_set_error("disco_batch_create: null member"); return DISCO_E_ARG; }
@@ -556,19 +693,33 @@ int disco_batch_create(disco_gpu* const* members, int n, disco_batch** out) {
   disco_batch* b = new disco_batch();
   for (int i = 0; i < n; ++i) b->m.push_back(members[i]->impl);
   b->parity = par;
-  b->join.assign(n, nullptr);
+  // groups: members of one type and launch sequence, in member order (a
+  // probe plan per group decides who joins)
+  std::vector<MultiPlanBase*> probe;
+  for (int i = 0; i < n; ++i) {
+    InstanceBase* x = b->m[i];
+    bool placed = false;
+    for (size_t p = 0; p < probe.size() && !placed; ++p)
+      if (probe[p]->accepts(x)) { probe[p]->add(x); b->groups[p].push_back(i); placed = true; }
+    if (placed) continue;
+    MultiPlanBase* p = (flags & DISCO_BATCH_NO_GROUPS) ? nullptr : x->new_multi_plan();
+    if (p) { probe.push_back(p); b->groups.push_back({i}); }
+    else b->ungrouped.push_back(i);
+  }
+  for (auto p : probe) delete p;
+  for (size_t g = 0; g < b->groups.size();) {   // a group of one is a member of its own
+    if (b->groups[g].size() > 1) { ++g; continue; }
+    b->ungrouped.push_back(b->groups[g][0]);
+    b->groups.erase(b->groups.begin() + g);
+  }
+  std::sort(b->ungrouped.begin(), b->ungrouped.end());
+  if (b->groups.empty()) b->split_i = kSplitN - 1;   // nothing to split: every member on its own
   if (cudaStreamCreateWithFlags(&b->root, cudaStreamNonBlocking) != cudaSuccess ||
       cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming) != cudaSuccess) {
     delete b;
     disco_set_error("disco_batch_create: stream/event creation failed");
     return DISCO_E_CUDA;
   }
-  for (int i = 0; i < n; ++i)
-    if (cudaEventCreateWithFlags(&b->join[i], cudaEventDisableTiming) != cudaSuccess) {
-      delete b;
-      disco_set_error("disco_batch_create: event creation failed");
-      return DISCO_E_CUDA;
-    }
   *out = b;
   return 0;
 }
@@ -579,6 +730,90 @@ int disco_batch_run(disco_batch* b, int nsteps) {
 int disco_batch_run_timed(disco_batch* b, int nsteps, size_t flush_bytes, double* ms) {
   if (!b || nsteps < 0 || !ms) { disco_set_error("bad argument"); return DISCO_E_ARG; }
   return batch_steps(b, nsteps, flush_bytes, ms);
+}
+int disco_batch_profile(disco_batch* b, int nsteps, disco_kernel_time* out, int max_out, int* n_out) {
+  if (!b || nsteps < 0 || !out || !n_out || max_out < 0) { disco_set_error("disco_batch_profile: bad argument"); return DISCO_E_ARG; }
+  // the sub-groups' stages launched one by one on their streams, each
+  // bracketed by events; members on their own sequences step untimed
+  const int ci = b->split_i >= 0 ? b->split_i : 0;
+  int rc = batch_split_build(b, ci);
+  if (rc) return rc;
+  BatchSplit& x = b->sets[ci];
+  std::vector<KTimer> kt(x.plans.size());
+  for (size_t p = 0; p < x.plans.size(); ++p) { kt[p].on = true; kt[p].st = x.st[p]; }
+  for (int s = 0; s < nsteps; ++s) {
+    for (size_t p = 0; p < x.plans.size(); ++p) {
+      rc = x.plans[p]->launch_step(b->parity, x.st[p], b->ctas, &kt[p]);
+      if (rc) return rc;
+    }
+    for (int i : x.solo) b->m[i]->launch_step(b->parity);
+    b->parity ^= 1;
+  }
+  CK(cudaDeviceSynchronize());
+  std::vector<std::string> names;
+  std::vector<long long> cnt;
+  std::vector<double> ms;
+  for (auto& k : kt)
+    for (auto& r : k.recs) {
+      float t = 0;
+      cudaEventElapsedTime(&t, r.a, r.b);
+      cudaEventDestroy(r.a);
+      cudaEventDestroy(r.b);
+      size_t i = 0;
+      for (; i < names.size(); ++i) if (names[i] == r.name) break;
+      if (i == names.size()) { names.push_back(r.name); cnt.push_back(0); ms.push_back(0); }
+      cnt[i] += 1;
+      ms[i] += t;
+    }
+  int k = 0;
+  for (size_t i = 0; i < names.size() && k < max_out; ++i, ++k) {
+    snprintf(out[k].name, sizeof out[k].name, "%s", names[i].c_str());
+    out[k].launches = cnt[i];
+    out[k].ms = ms[i];
+  }
+  *n_out = k;
+  for (auto* m : b->m) {
+    rc = m->after_external_steps(nsteps, 0);
+    if (rc) return rc;
+  }
+  return 0;
+}
+int disco_batch_set_grid(disco_batch* b, int ctas_per_sm) {
+  if (!b || ctas_per_sm < 1 || ctas_per_sm > 64) { disco_set_error("disco_batch_set_grid: bad argument"); return DISCO_E_ARG; }
+  b->ctas = ctas_per_sm;
+  for (auto& x : b->sets) x.drop_graphs();
+  return 0;
+}
+int disco_batch_set_split(disco_batch* b, int split) {
+  if (!b) { disco_set_error("disco_batch_set_split: null batch"); return DISCO_E_ARG; }
+  if (split == -1) {
+    if (b->groups.empty()) return 0;
+    b->split_i = -1;
+    b->tune_i = 0;
+    return 0;
+  }
+  for (int c = 0; c < kSplitN; ++c)
+    if (kSplitCand[c] == split) {
+      b->split_i = b->groups.empty() ? kSplitN - 1 : c;
+      return 0;
+    }
+  disco_set_error("disco_batch_set_split: split must be -1, 0, 1, 2, 4, 8 or 16");
+  return DISCO_E_ARG;
+}
+int disco_batch_info(const disco_batch* b, int* groups, int* grouped, int* split, int* ctas_per_sm,
+                     double* tune_ms) {
+  if (!b) { disco_set_error("disco_batch_info: null batch"); return DISCO_E_ARG; }
+  if (groups) *groups = (int)b->groups.size();
+  if (grouped) {
+    int k = 0;
+    for (auto& g : b->groups) k += (int)g.size();
+    *grouped = k;
+  }
+  if (split) *split = b->split_i >= 0 ? kSplitCand[b->split_i] : -1;
+  if (ctas_per_sm) *ctas_per_sm = b->ctas;
+  if (tune_ms)
+    for (int c = 0; c < kSplitN; ++c) tune_ms[c] = b->tune_i > c * kTuneReps ? b->tune_ms[c] : -1.0;
+  return 0;
 }
 void disco_batch_free(disco_batch* b) { delete b; }
 

@@ -41,6 +41,26 @@ extern std::atomic<long long> g_launches;
 
 namespace disco_impl {
 
+struct InstanceBase;
+struct KTimer;
+
+// A group of instances of one hydro module and precision whose steps launch
+// the same kernel sequence, advanced together by the persistent stage
+// kernels of multi.cuh: each stage is one launch over every member's tiles.
+struct MultiPlanBase {
+  virtual ~MultiPlanBase() {}
+  // x has this group's type and launch sequence (and may join it)
+  virtual bool accepts(InstanceBase* x) const = 0;
+  virtual void add(InstanceBase* x) = 0;
+  virtual int size() const = 0;
+  // device member tables and work lists, from the members as they are now
+  virtual int prepare() = 0;
+  // one full step of every member from piph parity par, on stream st, each
+  // stage kernel a grid of at most ctas_per_sm blocks per SM (and at most
+  // as many as are resident at once); kt, when given, times each stage
+  virtual int launch_step(int par, cudaStream_t st, int ctas_per_sm, KTimer* kt) = 0;
+};
+
 struct InstanceBase {
   virtual ~InstanceBase() {}
   virtual int getmindt(double* dt) = 0;
@@ -65,6 +85,7 @@ struct InstanceBase {
   virtual int harvest(const MlpDev* m, const C2PRecord* rec, int steps) = 0;
   virtual int c2p_stats(long long* out, int reset) = 0;
   virtual int getmindt_noalloc(double* dt) = 0;
+  virtual int sink_accum(double* out, int max_bodies, int reset) = 0;
   virtual int report(double* out, int nout) = 0;
   virtual int diag(int op, double* Qrz, long long n, double* t_avg, const double* set, double set_t) = 0;
   // batch support: launch one full step (getmindt + timestep) from piph
@@ -74,8 +95,14 @@ struct InstanceBase {
   virtual int cur_parity() const = 0;
   virtual cudaStream_t stream() const = 0;
   virtual int after_external_steps(int nsteps, long long nodes) = 0;
+  // a new group holding this instance alone, or null if its launch sequence
+  // has stages the multi-instance kernels do not cover
+  virtual MultiPlanBase* new_multi_plan() { return nullptr; }
   long N = 0, Nreal = 0;
 };
+
+template <class Phys, typename R, int NQ>
+struct MultiPlan;
 
 // The dynamic shared-memory limit is an attribute of the kernel function,
 // shared by every instance in the process: only ever raise it, so a smaller
@@ -142,6 +169,7 @@ struct Instance : InstanceBase {
   cudaStream_t st = nullptr;
   int Nr = 0, Nz = 0, nring = 0, npair[2] = {0, 0};
   int maxNf[2] = {0, 0};
+  std::vector<int> face_off_h[2];   // host copy of face_off
   double* piph_buf[2] = {nullptr, nullptr};
   int parity = 0;  // which piph buffer is current
   int planets_id = 0;
@@ -223,9 +251,19 @@ struct Instance : InstanceBase {
       disco_set_error("Riemann_Solver = HLLD with a hydro module (riemann.c:19-22)");
       return DISCO_E_MODULE;
     }
-    if (p.sinkType || p.nozzleType) {
-      disco_set_error("sink/nozzle source terms are not built");
+    if (p.sinkType < 0 || p.sinkType > 3 || (p.nozzleType != 0 && p.nozzleType != 1)) {
+      disco_set_error("Sink_Type 0-3 and Nozzle_Type 0-1 are the sink.c source terms");
       return DISCO_E_MODULE;
+    }
+    P.sink_type = p.sinkType;
+    P.nozzle_type = p.nozzleType;
+    P.sink_bodies = dom->Npl;
+    if (p.sinkNumber > 0 && p.sinkNumber < dom->Npl) P.sink_bodies = p.sinkNumber;   // sink.c:163
+    {
+      const double sp[5] = {p.sinkPar1, p.sinkPar2, p.sinkPar3, p.sinkPar4, p.sinkPar5};
+      const double np[4] = {p.nozzlePar1, p.nozzlePar2, p.nozzlePar3, p.nozzlePar4};
+      for (int i = 0; i < 5; ++i) P.sink_par[i] = sp[i];
+      for (int i = 0; i < 4; ++i) P.nozzle_par[i] = np[i];
     }
     P.cool_type = p.coolType;
     P.cool_beta = p.coolPar1;
@@ -237,10 +275,12 @@ struct Instance : InstanceBase {
     P.damp_time[2] = p.dampTimeUpper; P.damp_time[3] = p.dampTimeLower;
     P.dom_rmin = p.rmin; P.dom_rmax = p.rmax; P.dom_zmax = p.zmax;
     P.twoD = dom->Nz == 1;
+    // the extra-sources variant of the update: cooling, damping, sinks, nozzle
     P.cool_damp = (p.coolType == 1 || p.coolType == 2) ||
-                  p.dampInnerType > 0 || p.dampOuterType > 0 || p.dampUpperType > 0 || p.dampLowerType > 0;
+                  p.dampInnerType > 0 || p.dampOuterType > 0 || p.dampUpperType > 0 || p.dampLowerType > 0 ||
+                  p.sinkType != 0 || p.nozzleType != 0;
     if (P.cool_damp && Phys::GR) {
-      disco_set_error("cooling/damping are built for the Newtonian modules");
+      disco_set_error("cooling/damping/sinks are built for the Newtonian modules");
       return DISCO_E_MODULE;
     }
     if (p.Timestep != 0 && p.Timestep != 3) {
@@ -379,6 +419,7 @@ struct Instance : InstanceBase {
       A(&d_off, np + 1);
       CK(cudaMemcpy(d_off, off.data(), sizeof(int) * (np + 1), cudaMemcpyHostToDevice));
       S.face_off[d] = d_off;
+      face_off_h[d] = off;
       A(&S.fL[d], nf); A(&S.fR[d], nf); A(&S.fLR[d], nf); A(&S.fphic[d], nf); A(&S.fdA[d], nf);
       A(&S.fdpL[d], nf); A(&S.fdpR[d], nf);
       A(&S.pdxL[d], np); A(&S.pdxR[d], np); A(&S.pdxs[d], np); A(&S.prad[d], np);
@@ -435,6 +476,12 @@ struct Instance : InstanceBase {
       }
     }
     A(&S.planets, MAX_PL); A(&S.scal, SC_COUNT); A(&S.errs, 1);
+    sink_on = P.sink_type != 0 && P.sink_bodies > 0;
+    if (sink_on) {
+      A(&S.sink_acc, 2 * MAX_PL * kSinkAcc);
+      A(&S.sink_part, (size_t)blocks(N) * MAX_PL * kSinkAcc);
+      CK(cudaMemset(S.sink_acc, 0, sizeof(double) * 2 * MAX_PL * kSinkAcc));
+    }
     diag_id = dom->mod.analysis;
     diag_n = diag_count(diag_id);
     if (diag_id == DISCO_DIAG_MHDMRI && NQ < 8) {
@@ -647,25 +694,32 @@ struct Instance : InstanceBase {
     LAUNCH("mindt", (k_mindt<Phys, R, NQ><<<blocks(N), 256, 0, st>>>(P, S)));
     LAUNCH("dt_finalize", (k_dt_finalize<<<1, 1, 0, st>>>(P, S.scal)));
   }
+  // The ring pairs of the flux sweep across dimension d + 1: jcount x kcount
+  // rings from (jmin, kmin); false if there are none (misc.c:464-500; with
+  // CT one more layer across the other dimension)
+  bool trans_range(int d, int* jmin_o, int* jcount_o, int* kmin_o, int* kcount_o) const {
+    if (!npair[d]) return false;
+    const int dim = d + 1;
+    int jmin, jmax, kmin, kmax;
+    if (dim == 1) {
+      jmin = P.NgRa == 0 ? 0 : P.NgRa - 1;
+      jmax = P.NgRb == 0 ? Nr - 1 : Nr - P.NgRb;
+      if (ct) { kmin = P.NgZa == 0 ? 0 : P.NgZa - 1; kmax = P.NgZb == 0 ? Nz : Nz - P.NgZb + 1; }
+      else { kmin = P.NgZa; kmax = Nz - P.NgZb; }
+    } else {
+      if (ct) { jmin = P.NgRa == 0 ? 0 : P.NgRa - 1; jmax = P.NgRb == 0 ? Nr : Nr - P.NgRb + 1; }
+      else { jmin = P.NgRa; jmax = Nr - P.NgRb; }
+      kmin = P.NgZa == 0 ? 0 : P.NgZa - 1;
+      kmax = P.NgZb == 0 ? Nz - 1 : Nz - P.NgZb;
+    }
+    *jmin_o = jmin; *jcount_o = jmax - jmin; *kmin_o = kmin; *kcount_o = kmax - kmin;
+    return *jcount_o > 0 && *kcount_o > 0;
+  }
   void launch_trans_fluxes(double fac) {
     for (int d = 0; d < 2; ++d) {
-      if (!npair[d]) continue;
-      int dim = d + 1;
-      int jmin, jmax, kmin, kmax;
-      // misc.c:464-500; with CT one more layer across the other dimension
-      if (dim == 1) {
-        jmin = P.NgRa == 0 ? 0 : P.NgRa - 1;
-        jmax = P.NgRb == 0 ? Nr - 1 : Nr - P.NgRb;
-        if (ct) { kmin = P.NgZa == 0 ? 0 : P.NgZa - 1; kmax = P.NgZb == 0 ? Nz : Nz - P.NgZb + 1; }
-        else { kmin = P.NgZa; kmax = Nz - P.NgZb; }
-      } else {
-        if (ct) { jmin = P.NgRa == 0 ? 0 : P.NgRa - 1; jmax = P.NgRb == 0 ? Nr : Nr - P.NgRb + 1; }
-        else { jmin = P.NgRa; jmax = Nr - P.NgRb; }
-        kmin = P.NgZa == 0 ? 0 : P.NgZa - 1;
-        kmax = P.NgZb == 0 ? Nz - 1 : Nz - P.NgZb;
-      }
-      int jc = jmax - jmin, kc = kmax - kmin;
-      if (jc <= 0 || kc <= 0) continue;
+      const int dim = d + 1;
+      int jmin, jc, kmin, kc;
+      if (!trans_range(d, &jmin, &jc, &kmin, &kc)) continue;
       dim3 grid(jc * kc, (maxNf[d] + 255) / 256);
       LAUNCH(dim == 1 ? "flux_r" : "flux_z",
              (k_flux_trans<Phys, R, NQ><<<grid, 256, 0, st>>>(P, S, dim, jmin, jc, kmin, fac)));
@@ -701,6 +755,11 @@ struct Instance : InstanceBase {
           LAUNCH("ct_edge_replay", (k_ct_edge_replay<R><<<(int)((nev + 255) / 256), 256, 0, st>>>(P, S, C, fac, nev)));
         if (C.ev_cid && !first) LAUNCH("ct_edge_flag", (k_set_flag<<<1, 1, 0, st>>>(C.ev_ok, 1)));
       }
+    }
+    if (sink_on) {   // the sink bodies' accumulators, from the state add_source sees
+      LAUNCH("sink_acc", (k_sink_acc<Phys, R, NQ><<<blocks(N), 256, 0, st>>>(P, S, fac)));
+      LAUNCH("sink_final", (k_sink_final<<<1, MAX_PL * kSinkAcc, 0, st>>>(S.sink_acc, S.sink_part, (int)blocks(N),
+                                                                            RK, first, P.sink_bodies)));
     }
     {
       // GRMHD with a learned starting point: calc_prim is its own pass below
@@ -1194,6 +1253,19 @@ struct Instance : InstanceBase {
     set_piph(save);
   }
   int cur_parity() const override { return parity; }
+  bool sink_on = false;
+  // the sink bodies' accumulators (report.c:81-100): out[b * kSinkAcc + q]
+  // for the first min(bodies, max_bodies) bodies; reset zeroes them and
+  // their RK copy, as report() does after printing
+  int sink_accum(double* out, int max_bodies, int reset) override {
+    if (!sink_on) return 0;
+    const int nb = std::min(P.sink_bodies, max_bodies);
+    CK(cudaStreamSynchronize(st));
+    if (out && nb > 0) CK(cudaMemcpy(out, S.sink_acc, sizeof(double) * nb * kSinkAcc, cudaMemcpyDeviceToHost));
+    if (reset) CK(cudaMemset(S.sink_acc, 0, sizeof(double) * 2 * MAX_PL * kSinkAcc));
+    return nb;
+  }
+  MultiPlanBase* new_multi_plan() override;
   cudaStream_t stream() const override { return st; }
   int after_external_steps(int nsteps, long long nodes) override {
     g_launches += nodes;
@@ -1268,6 +1340,12 @@ struct Instance : InstanceBase {
     return 0;
   }
 };
+
+}  // namespace disco_impl
+
+#include "multi_plan.cuh"
+
+namespace disco_impl {
 
 template <class Phys, typename R, int NQ>
 InstanceBase* make_instance(const disco_host_domain* dom, int* rc) {

@@ -17,6 +17,9 @@
 
 namespace disco {
 
+// accumulators per sink body, in report.c's column order (report.c:81-88)
+enum { SA_GRAVL = 0, SA_DM, SA_ACCL, SA_LS, SA_KIN, SA_THERM, SA_XMOM, SA_YMOM, kSinkAcc };
+
 template <typename R>
 struct DevState {
   int N;                       // cells incl. ghosts
@@ -108,6 +111,8 @@ struct DevState {
   R* fBrz[2];
   R* fEphi[2];
   DevPlanet* planets;          // [Npl], device copy (moves for analytic orbits)
+  double* sink_acc;            // [2][MAX_PL * kSinkAcc]: the sink bodies' accumulators, then their RK copy
+  double* sink_part;           // [blocks of k_sink_acc][MAX_PL * kSinkAcc]: per-block partial sums
   double* scal;                // [0] dt, [1] t, [2] min-dt accumulator (bits)
   DevErrs* errs;
 };
@@ -1039,6 +1044,166 @@ DISCO_D void cool_damp_src(const DevParams& P, const DevPlanet* pl, const R* pri
   }
 }
 
+// sink_src (sink.c:105-247), the last term of add_source: the gas nozzle
+// (Nozzle_Type 1) and the accreting sinks of the first sink_bodies bodies
+// (Sink_Type 1 compact polynomial, 2 exponential, 3 top hat).  A cell
+// outside the nozzle takes neither term, as in the reference (its early
+// return).  U gets the cell's changes; acc, when given, gets the cell's
+// share of each sink body's accumulators (SA_*).  The reference's
+// fmin(Sink_Par2, 1) is overwritten by fmax(0, Sink_Par2), so delta is the
+// latter.
+template <typename R>
+DISCO_D void sink_src(const DevParams& P, const DevPlanet* pl, const R* prim, double* U, const double* xp,
+                      const double* xm, double dV, double dt, double* acc) {
+  if (P.nozzle_type == 1) {
+    const double r = .5 * (xp[0] + xm[0]);
+    double phi = .5 * (xp[1] + xm[1]);
+    const double z = .5 * (xp[2] + xm[2]);
+    if (phi > M_PI) phi -= 2 * M_PI;
+    const double R0 = P.nozzle_par[0], dR = P.nozzle_par[1], v = P.nozzle_par[2], mach = P.nozzle_par[3];
+    const double d2 = (r - R0) * (r - R0) + r * r * phi * phi + z * z;
+    if (d2 > dR * dR) return;
+    double rhodot = 1.0 * 3.0 / (4.0 * M_PI * dR * dR * dR);
+    if (P.twoD) rhodot *= 2 * sqrt(dR * dR - (r - R0) * (r - R0) - r * r * phi * phi);
+    if (rhodot * dV * dt > U[RHO]) rhodot = U[RHO] / dV * dt;
+    const double om = get_om<double>(P, r);
+    const double cs2 = v * v / (mach * mach);
+    const double eps = cs2 / (P.gamma_law * (P.gamma_law - 1));
+    U[RHO] += rhodot * dV * dt;
+    U[LLL] += rhodot * r * v * dV * dt;
+    U[TAU] += (0.5 * rhodot * (v - r * om) * (v - r * om) + rhodot * eps) * dV * dt;
+    if (P.num_q > P.num_c) U[P.num_c] += rhodot * dV * dt;
+  }
+  if (P.sink_type == 0) return;
+  const double r = centroid_r(xp[0], xm[0]), phi = .5 * (xp[1] + xm[1]);
+  const double rho = prim[RHO], vr = prim[URR], vp = (double)prim[UPP] * r, vz = prim[UZZ], pres = prim[PPP];
+  const double cosg = cos(phi), sing = sin(phi);
+  const double gx = r * cosg, gy = r * sing;
+  const double delta = fmax(0.0, P.sink_par[1]);
+  const double gm1 = P.gamma_law - 1.0;
+  for (int b = 0; b < P.sink_bodies; ++b) {
+    const DevPlanet& q = pl[b];
+    const double cosp = cos(q.phi), sinp = sin(q.phi);
+    const double dx = gx - q.r * cosp, dy = gy - q.r * sinp;
+    const double mag = sqrt(dx * dx + dy * dy);
+    double arg = 0.0;
+    if (P.sink_type == 3) {
+      if (mag <= P.sink_par[2]) arg = 1.0;
+    } else if (P.sink_type == 2) {
+      const double eps = pow(P.sink_par[2], P.sink_par[3]);
+      const double ef = P.sink_par[4] <= 0.0 ? 1.0 : P.sink_par[4];
+      arg = exp(-pow(mag, P.sink_par[3]) / (eps * ef));
+    } else if (P.sink_type == 1) {
+      const double eps = P.sink_par[2];
+      arg = pow(1.0 - pow(mag / eps, P.sink_par[3]), P.sink_par[4]);
+      if (mag >= eps) arg = 0.0;
+    }
+    const double surfdiff = rho * (P.sink_par[0] * q.omega) * arg;
+    // the gas velocity relative to the body, its radial part kept and its
+    // azimuthal part (about the body) removed in proportion delta
+    const double vpp = q.r * q.omega;
+    const double vxp = q.vr * cosp - vpp * sinp, vyp = q.vr * sinp + vpp * cosp;
+    double vxg = vr * cosg - vp * sing, vyg = vr * sing + vp * cosg;
+    const double vxr = vxg - vxp, vyr = vyg - vyp;
+    const double cphi = dx / mag, sphi = dy / mag;
+    const double af = dV * dt * surfdiff;
+    const double vpr = cphi * vyr - sphi * vxr;
+    const double vxn = (cphi * cphi + (1.0 - delta) * sphi * sphi) * vxr + delta * sphi * cphi * vyr;
+    const double vyn = delta * cphi * sphi * vxr + (sphi * sphi + (1.0 - delta) * cphi * cphi) * vyr;
+    vxg = vxn + vxp;
+    vyg = vyn + vyp;
+    double vgr = vxg * cosg + vyg * sing, vgp = -vxg * sing + vyg * cosg;
+    const double accL = vgp * r * af;
+    U[RHO] -= af;
+    if (delta == 0.0) { vgr = vr; vgp = vp; }
+    U[URR] -= vgr * af;
+    U[UPP] -= r * vgp * af;
+    U[UZZ] -= vz * af;
+    const double v2 = vgp * vgp + vgr * vgr + vz * vz;
+    U[PPP] -= af * (0.5 * v2 + pres / (rho * gm1));
+    if (acc) {
+      double fr, fp, fz;
+      planetary_force<double>(P, q, r, phi, 0.0, &fr, &fp, &fz, 1);
+      const double rho0 = 1.0 / (3.0 * M_PI * P.explicit_viscosity);
+      double* a = acc + b * kSinkAcc;
+      a[SA_LS] += (1.0 - delta) * mag * vpr * af;
+      a[SA_ACCL] += accL;
+      a[SA_DM] += af;
+      a[SA_KIN] += 0.5 * v2 * af;
+      a[SA_THERM] += pres * af / (rho * gm1);
+      a[SA_XMOM] += af * vxg;
+      a[SA_YMOM] += af * vyg;
+      a[SA_GRAVL] -= (rho - rho0) * q.r * fp * dV * dt;
+    }
+  }
+}
+
+// The sink bodies' accumulators over this substep's real cells, from the
+// state add_source sees (the primitives and positions before the update):
+// each block's partial sums, by a fixed tree, to part[block].
+template <typename Phys, typename R, int NQ>
+__global__ void __launch_bounds__(256) k_sink_acc(DevParams P, DevState<R> S, double fac) {
+  constexpr int NA = MAX_PL * kSinkAcc;
+  __shared__ double red[8][NA];
+  double acc[NA];
+#pragma unroll
+  for (int q = 0; q < NA; ++q) acc[q] = 0.0;
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c < S.N) {
+    const int jk = S.cell_ring[c];
+    const int k = div_fast(jk, P.mul_nr), j = jk - k * P.Nr;
+    if (is_real(P, j, k)) {
+      const double* rj = S.r_jph + 1;
+      const double* zk = S.z_kph + 1;
+      const double piph = S.piph[c], dphi = S.dphi[c];
+      const double xp[3] = {rj[j], piph, zk[k]};
+      const double xm[3] = {rj[j - 1], piph - dphi, zk[k - 1]};
+      const double dV = (.5 * (xp[0] + xm[0])) * (xp[0] - xm[0]) * get_dp(xp[1], xm[1], P.phi_max) * (xp[2] - xm[2]);
+      const double dt = fac * S.scal[SC_DT];
+      R pr[NQ];
+#pragma unroll
+      for (int q = 0; q < NQ; ++q) pr[q] = S.prim[q * S.N + c];
+      if constexpr (kMix<R>) pr[UPP] += S.ring_Om_r[jk];   // lab omega
+      double U[NQ];
+#pragma unroll
+      for (int q = 0; q < NQ; ++q) U[q] = 0.0;
+      U[RHO] = 1.0e300;   // no nozzle cap from here: only acc is kept
+      sink_src<R>(P, S.planets, pr, U, xp, xm, dV, dt, acc);
+    }
+  }
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+  for (int q = 0; q < NA; ++q) {
+    double v = acc[q];
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if (lane == 0) red[w][q] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < NA) {
+    double v = 0.0;
+    for (int i = 0; i < (int)(blockDim.x >> 5); ++i) v += red[i][threadIdx.x];
+    S.sink_part[(size_t)blockIdx.x * NA + threadIdx.x] = v;
+  }
+}
+
+// adjust_RK_planets_aux (misc.c:258-264, planet.c:261-270) and the sum of
+// this substep's contributions: acc = (1 - RK) acc + RK acc_RK + the block
+// partials in block order.  The first substep first copies acc to acc_RK
+// (planet_RK_copy at the start of timestep, timestep.c:25-27).
+static __global__ void k_sink_final(double* sink_acc, const double* part, int nblocks, double RK, int first,
+                                    int nbody) {
+  constexpr int NA = MAX_PL * kSinkAcc;
+  const int t = threadIdx.x;
+  if (t >= nbody * kSinkAcc) return;
+  double* cur = sink_acc;
+  double* rk = sink_acc + NA;
+  if (first) rk[t] = cur[t];
+  double a = (1. - RK) * cur[t] + RK * rk[t];
+  double s = 0.0;
+  for (int b = 0; b < nblocks; ++b) s += part[(size_t)b * NA + t];
+  cur[t] = a + s;
+}
+
 // Occupancy: on the mixed path the flux and update kernels are capped at
 // 64 registers per thread (4 blocks of 256 per SM), measured faster than
 // their natural 70+; the FP64 versions would spill, so they are not capped.
@@ -1361,7 +1526,7 @@ DISCO_D void k_update_body(const DevParams& P, const DevState<R>& S, double RK, 
     for (int q = 0; q < NQ; ++q) pr[q] = S.prim[q * N + c];
     double xp[3] = {rj[j], piph, zk[k]};
     double xm[3] = {rj[j - 1], piph - dphi, zk[k - 1]};
-    double dVdt = 0;
+    double dVdt = 0, dVc = 0;
     if constexpr (MIX) {   // sources summed in R into dU with the flux terms
       pr[UPP] += S.ring_Om_r[jk];   // lab omega for the source terms
       R dph = S.dphi_r[c];
@@ -1405,12 +1570,14 @@ DISCO_D void k_update_body(const DevParams& P, const DevState<R>& S, double RK, 
       if (P.include_viscosity || P.rot_flag || CD) {
         double dV = (.5 * (xp[0] + xm[0])) * (xp[0] - xm[0]) * get_dp(xp[1], xm[1], Pmax) * (xp[2] - xm[2]);
         dVdt = dV * dt;
+        dVc = dV;
         if constexpr (!Phys::GR)
           if constexpr (CD) cool_damp_src<Phys, R, NQ>(P, S.planets, pr, U, xp, xm, dV, dt);
       }
     } else {
       double dV = (.5 * (xp[0] + xm[0])) * (xp[0] - xm[0]) * get_dp(xp[1], xm[1], Pmax) * (xp[2] - xm[2]);
       dVdt = dV * dt;
+      dVc = dV;
       if constexpr (Phys::GR) {   // grmhd.c:339 (metric and frame sources; no planets)
         Phys::source_x(P, pr, U, xp, xm, dVdt);
       } else {
@@ -1451,6 +1618,8 @@ DISCO_D void k_update_body(const DevParams& P, const DevState<R>& S, double RK, 
       U[SZZ] += rho * f2 * dVdt;
       U[TAU] += rho * vf * dVdt;
     }
+    if constexpr (CD && !Phys::GR)   // sink_src, the last source (misc.c:587)
+      if (P.sink_type || P.nozzle_type) sink_src<R>(P, S.planets, pr, U, xp, xm, dVc, dt, nullptr);
     if constexpr (MIX) {
       // the viscous and rotating-frame sources go to U in FP64 after the R
       // sum: the increment kept for the second substep is then the whole

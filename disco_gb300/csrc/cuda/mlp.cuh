@@ -43,8 +43,10 @@ struct MlpDev {
   const float* params;   // FP32 masters (biases read from here)
   float xm[kMlpIn], xs[kMlpIn], ym[kMlpOut], ys[kMlpOut];
   // cons2prim considers the learned start only where the previous
-  // primitives leave a residual of the two Noble equations above this
-  double warm_floor;
+  // primitives leave a residual of the two Noble equations above
+  // warm_floor, and takes it where its own residual is below warm_ratio
+  // times theirs
+  double warm_floor, warm_ratio;
 };
 
 struct __align__(16) MlpSmem {

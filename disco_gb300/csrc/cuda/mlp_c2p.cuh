@@ -37,9 +37,10 @@ struct C2PRecord {
 // calc_prim of the GRMHD module with the learned starting point: each warp
 // evaluates the network for its 32 cells on the tensor cores, then every
 // thread solves its cell from the corrected start -- or from the previous
-// primitives where those leave the smaller residual, or a residual at most
-// m.warm_floor: the reference's own start is the fallback -- and recovers
-// its primitives as calc_prim does.  use_guess 0 starts every cell from the previous primitives (the
+// primitives where the corrected start's residual is not below m.warm_ratio
+// times theirs, where theirs is at most m.warm_floor, or where Newton from
+// the corrected start does not converge: the reference's own start is the
+// fallback -- and recovers its primitives as calc_prim does.  use_guess 0 starts every cell from the previous primitives (the
 // reference's calc_prim) and may record training pairs.  256 threads per
 // block.
 template <typename Phys, typename R, int NQ>
@@ -82,14 +83,15 @@ __global__ void __launch_bounds__(256) k_c2p_guess(DevParams P, DevState<R> S, M
   }
   if (!valid) return;
   KsMetric g(x, P.gr_M, P.gr_a, P.gr_kerr);
-  double v20, eta0;
-  Phys::c2p_warm_start(P, g, prim, x[0], &v20, &eta0);
+  double v2w, etaw;   // the previous primitives' start
+  Phys::c2p_warm_start(P, g, prim, x[0], &v2w, &etaw);
+  double v20 = v2w, eta0 = etaw;
   int guessed = 0;
   if (use_guess) {
     double guess[2];
     Phys::c2p_guess_from(v, &Ys[wid][lane * kMlpOut], lu2, lth, guess);
     const double rw = Phys::c2p_residual(v, v20, eta0);
-    if (rw > m.warm_floor && Phys::c2p_residual(v, guess[0], guess[1]) < rw) {
+    if (rw > m.warm_floor && Phys::c2p_residual(v, guess[0], guess[1]) < m.warm_ratio * rw) {
       v20 = guess[0];
       eta0 = guess[1];
       guessed = 1;
@@ -98,6 +100,17 @@ __global__ void __launch_bounds__(256) k_c2p_guess(DevParams P, DevState<R> S, M
   double v2, eta;
   int kc, it;
   int hits = Phys::noble2d_solve(v, v20, eta0, &v2, &eta, &kc, &it);
+  if (guessed && (kc == 0 || (hits & 4))) {
+    // Newton from the learned start did not converge: solve again from the
+    // previous primitives, as the reference does.  The wasted iterations
+    // count toward this call's k_converge and iterations, and the call
+    // counts as not guessed.
+    int kc2, it2;
+    hits = Phys::noble2d_solve(v, v2w, etaw, &v2, &eta, &kc2, &it2);
+    kc = kc2 ? it + kc2 : 0;
+    it += it2;
+    guessed = 0;
+  }
   if (rec.X && !(hits & 4) && (c % rec.stride) == 0) {   // a training pair from this solve
     float y[kMlpOut];
     Phys::c2p_targets(v, v2, eta, lu2, lth, y);

@@ -167,7 +167,11 @@ int disco_params_read(const char *path, disco_params *p)
    RD("DampUpper_Time", dampTimeUpper); RD("DampUpper_Len", dampLenUpper);
    RD("DampLower_Time", dampTimeLower); RD("DampLower_Len", dampLenLower);
    RD("Softening", grav_eps);
-   RD("Sink_Par3", sinkPar3);
+   RI("Sink_Number", sinkNumber);
+   RD("Sink_Par1", sinkPar1); RD("Sink_Par2", sinkPar2); RD("Sink_Par3", sinkPar3);
+   RD("Sink_Par4", sinkPar4); RD("Sink_Par5", sinkPar5);
+   RD("Nozzle_Par1", nozzlePar1); RD("Nozzle_Par2", nozzlePar2);
+   RD("Nozzle_Par3", nozzlePar3); RD("Nozzle_Par4", nozzlePar4);
    /* not a reference key: an upper bound on cells per ring (0 = none) */
    { int e0 = err; RI("Max_Np", maxNp); err = e0; }
 #undef RI

@@ -126,6 +126,9 @@ typedef struct disco_params {
    double dampTimeInner, dampLenInner, dampTimeOuter, dampLenOuter,
           dampTimeUpper, dampLenUpper, dampTimeLower, dampLenLower;   /* Damp*_Time/_Len (sink.c:329) */
    int maxNp;         /* Max_Np: cap on cells per ring (no reference key; 0 = none) */
+   int sinkNumber;    /* Sink_Number: sinks on the first n bodies (0: all) */
+   double sinkPar1, sinkPar2, sinkPar4, sinkPar5;             /* Sink_Par1,2,4,5 (sink.c:105) */
+   double nozzlePar1, nozzlePar2, nozzlePar3, nozzlePar4;     /* Nozzle_Par1..4 (sink.c:105) */
 } disco_params;
 
 /* One point mass: the fields of struct planet (paul.h:259-284) the hot path

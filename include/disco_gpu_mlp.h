@@ -79,11 +79,12 @@ int disco_mlp_predict(disco_mlp *m, const float *X, long n, float *Y);
  * (DISCO_MLP_PARAMS floats) and the standardisation (DISCO_MLP_NORM). */
 int disco_mlp_params(disco_mlp *m, float *get, const float *set, float *norm_get, const float *norm_set);
 
-/* The residual of the two Noble equations (each relative to the term it
- * balances) at or below which the previous primitives are kept as the
- * start without consulting the model (default 0).  Takes effect at the
- * next disco_gpu_attach_guess. */
-int disco_mlp_set_floor(disco_mlp *m, double floor);
+/* When cons2prim takes the model's start.  With r_w the residual of the two
+ * Noble equations (each relative to the term it balances) at the previous
+ * primitives and r_g at the model's start, the model's start is taken where
+ * r_w > floor and r_g < ratio r_w (defaults 0 and 1; 0 < ratio <= 1).
+ * Takes effect at the next disco_gpu_attach_guess. */
+int disco_mlp_set_gate(disco_mlp *m, double floor, double ratio);
 
 /* Makes g's cons2prim start from the model's guess (m NULL: from the
  * previous primitives only, the reference's start).  The instance keeps the

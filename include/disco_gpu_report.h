@@ -8,8 +8,7 @@
  * outside five cut radii (n + 1) * Sink_Par3, n = 0..4, around the second
  * body.  This entry point returns those sums from the device state, summed
  * in a fixed order (equal to the reference's serial sums to rounding).  The
- * per-planet sink accumulators are zero in this build (sinks are not
- * built) and are not returned.
+ * per-planet sink accumulators come from disco_gpu_sink_accum.
  */
 #ifndef DISCO_GPU_REPORT_H
 #define DISCO_GPU_REPORT_H
@@ -30,6 +29,18 @@ extern "C" {
  * count, or a negative DISCO_E_* code.  The first call allocates a small
  * device buffer for the block partials (about 100 bytes per 256 cells). */
 int disco_gpu_report(disco_gpu *g, double *out, int nout);
+
+/* The sink bodies' accumulators that report.c prints after the mass ratio
+ * (report.c:81-88, sink.c:189-245), accumulated by every substep's
+ * sink_src since the last reset with the RK blend of the planets'
+ * auxiliary fields (planet.c:261-270).  For sink body b (the first
+ * Sink_Number bodies, or all) out[8 b + k] holds, k = 0..7: gravL, dM,
+ * accL, Ls, kin, therm, linXmom, linYmom.  reset != 0 then zeroes them and
+ * their RK copy, as report() does after printing (report.c:91-108).
+ * Returns the number of bodies written (0 without sinks), at most
+ * max_bodies, or a negative DISCO_E_* code. */
+#define DISCO_SINK_NACC 8
+int disco_gpu_sink_accum(disco_gpu *g, double *out, int max_bodies, int reset);
 
 #ifdef __cplusplus
 }

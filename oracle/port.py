@@ -31,6 +31,7 @@ def _lib():
         L.disco_port_phi.argtypes = [C.c_void_p, _dp]
         L.disco_port_report.argtypes = [C.c_void_p, _dp]
         L.disco_port_diag.argtypes = [C.c_void_p, _dp, _dp]
+        L.disco_port_sink_accum.argtypes = [C.c_void_p, _dp, C.c_int]
         _ip = C.POINTER(C.c_int)
         L.disco_port_faces.restype = C.c_long
         L.disco_port_faces.argtypes = [C.c_void_p, C.c_int, _ip, _ip, _ip, _ip, _dp, _dp]
@@ -79,6 +80,13 @@ class PortDomain:
         out = np.empty(len(self.REPORT_KEYS))
         _lib().disco_port_report(self._d, out.ctypes.data_as(_dp))
         return dict(zip(self.REPORT_KEYS, out.tolist()))
+
+    def sink_accum(self, nbody: int) -> np.ndarray:
+        """The sink accumulators of the first nbody bodies, [nbody, 8]:
+        gravL, dM, accL, Ls, kin, therm, linXmom, linYmom."""
+        out = np.zeros((nbody, 8))
+        _lib().disco_port_sink_accum(self._d, out.ctypes.data_as(_dp), int(nbody))
+        return out
 
     def diagnostics(self) -> dict:
         """analysis.c's ring accumulators: Qrz [Nr*Nz, n] and t_avg."""

@@ -63,6 +63,10 @@ typedef struct port_domain {
    double gam;
    int nd;                /* num_diagnostics() of the ANALYSIS plugin */
    double *Qrz, t_avg;    /* struct diagnostic_avg: Qrz[jk*nd + q] */
+   /* the bodies' sink accumulators (paul.h:258-276) in report.c's column
+    * order: gravL, dM, accL, Ls, kin, therm, linXmom, linYmom; and their RK
+    * copies */
+   double sacc[DISCO_MAX_PLANETS][8], sacc_rk[DISCO_MAX_PLANETS][8];
 } port_domain;
 
 static port_domain *D;   /* the domain being advanced (module statics in the reference) */
@@ -1751,6 +1755,91 @@ static void damping(const double *prim, double *cons, const double *xp, const do
    cons[TAU] += (c1[TAU] - c0[TAU])*f;
 }
 
+/* sink_src (sink.c:105-247): the nozzle, then the accreting sinks of the
+ * first Sink_Number bodies (all if 0 or not fewer than Npl), accumulating
+ * into the bodies' sink accumulators in cell order as the reference does.
+ * A cell outside the nozzle returns before the sinks, as in the reference;
+ * delta is fmax(0, Sink_Par2), the reference's fmin being overwritten. */
+static void sink_src(const double *prim, double *cons, const double *xp, const double *xm, double dV, double dt)
+{
+   const disco_params *p = &D->par;
+   if(p->nozzleType == 1) {
+      double R0 = p->nozzlePar1, dR = p->nozzlePar2, v = p->nozzlePar3, mach = p->nozzlePar4;
+      double r = 0.5*(xp[0] + xm[0]), phi = 0.5*(xp[1] + xm[1]), z = 0.5*(xp[2] + xm[2]);
+      if(phi > M_PI) phi -= 2*M_PI;
+      if((r - R0)*(r - R0) + r*r*phi*phi + z*z > dR*dR) return;
+      double rhodot = 1.0*3.0/(4.0*M_PI*dR*dR*dR);
+      if(D->Nz == 1) rhodot *= 2*sqrt(dR*dR - (r - R0)*(r - R0) - r*r*phi*phi);
+      if(rhodot*dV*dt > cons[RHO]) rhodot = cons[RHO]/dV*dt;
+      double x[3] = {r, phi, z};
+      double om = get_om(x);
+      double cs2 = v*v/(mach*mach);
+      double eps = cs2/(D->gam*(D->gam - 1));
+      cons[RHO] += rhodot*dV*dt;
+      cons[LLL] += rhodot*r*v*dV*dt;
+      cons[TAU] += (0.5*rhodot*(v - r*om)*(v - r*om) + rhodot*eps)*dV*dt;
+      if(D->nq > D->nc) cons[D->nc] += rhodot*dV*dt;
+   }
+   if(p->sinkType == 0) return;
+   double x[3];
+   centroid_arr(xp, xm, x);
+   double r = x[0], phi = x[1];
+   double rho = prim[RHO], vr = prim[URR], vp = prim[UPP]*r, vz = prim[UZZ];
+   double cosg = cos(phi), sing = sin(phi), gx = r*cosg, gy = r*sing;
+   int ns = D->Npl;
+   if(p->sinkNumber > 0 && p->sinkNumber < ns) ns = p->sinkNumber;
+   for(int b = 0; b < ns; b++) {
+      const disco_planet *q = &D->pl[b];
+      double *a = D->sacc[b];
+      double cosp = cos(q->phi), sinp = sin(q->phi);
+      double dx = gx - q->r*cosp, dy = gy - q->r*sinp;
+      double mag = sqrt(dx*dx + dy*dy);
+      double arg = 0.0;
+      if(p->sinkType == 3) {
+         if(mag <= p->sinkPar3) arg = 1.0;
+      } else if(p->sinkType == 2) {
+         double eps = pow(p->sinkPar3, p->sinkPar4);
+         double ef = p->sinkPar5 <= 0.0 ? 1.0 : p->sinkPar5;
+         arg = exp(-pow(mag, p->sinkPar4)/(eps*ef));
+      } else if(p->sinkType == 1) {
+         arg = pow(1.0 - pow(mag/p->sinkPar3, p->sinkPar4), p->sinkPar5);
+         if(mag >= p->sinkPar3) arg = 0.0;
+      }
+      double surfdiff = rho*(p->sinkPar1*q->omega)*arg;
+      double delta = fmax(0.0, p->sinkPar2);
+      double vpp = q->r*q->omega;
+      double vxp = q->vr*cosp - vpp*sinp, vyp = q->vr*sinp + vpp*cosp;
+      double vxg = vr*cosg - vp*sing, vyg = vr*sing + vp*cosg;
+      double vxr = vxg - vxp, vyr = vyg - vyp;
+      double cphi = dx/mag, sphi = dy/mag;
+      double af = dV*dt*surfdiff;
+      double vpr = cphi*vyr - sphi*vxr;
+      a[3] += (1.0 - delta)*mag*vpr*af;
+      double vxn = (cphi*cphi + (1.0 - delta)*sphi*sphi)*vxr + delta*sphi*cphi*vyr;
+      double vyn = delta*cphi*sphi*vxr + (sphi*sphi + (1.0 - delta)*cphi*cphi)*vyr;
+      vxg = vxn + vxp;
+      vyg = vyn + vyp;
+      double vgr = vxg*cosg + vyg*sing, vgp = -vxg*sing + vyg*cosg;
+      a[2] += vgp*r*af;
+      cons[DDD] -= af;
+      if(delta == 0.0) { vgr = vr; vgp = vp; }
+      cons[SRR] -= vgr*af;
+      cons[LLL] -= r*vgp*af;
+      cons[SZZ] -= vz*af;
+      double v2 = vgp*vgp + vgr*vgr + vz*vz;
+      cons[TAU] -= af*(0.5*v2 + prim[PPP]/(rho*(D->gam - 1.0)));
+      a[1] += af;
+      a[4] += 0.5*v2*af;
+      a[5] += prim[PPP]*af/(rho*(D->gam - 1.0));
+      a[6] += af*vxg;
+      a[7] += af*vyg;
+      double fr, fp, fz;
+      double rho0 = 1.0/(3.0*M_PI*p->viscosity);
+      planetary_force_m1(q, r, phi, 0.0, &fr, &fp, &fz);
+      a[0] -= (rho - rho0)*q->r*fp*dV*dt;
+   }
+}
+
 static void add_source(double dt)
 {
    for(int k = D->NgZa; k < D->Nz - D->NgZb; k++) for(int j = D->NgRa; j < D->Nr - D->NgRb; j++) {
@@ -1768,6 +1857,7 @@ static void add_source(double dt)
          if(D->par.visc_flag && !D->mhd)
             e_visc_source(c->prim, c->gradr, c->gradp, c->gradz, c->cons, xp, xm, dV*dt);
          if(D->par.RotFrame) omega_src(c->prim, c->cons, xp, xm, dV*dt);
+         if(D->par.sinkType || D->par.nozzleType) sink_src(c->prim, c->cons, xp, xm, dV, dt);
       }
    }
 }
@@ -1782,6 +1872,8 @@ static void onestep(double RK, double dt, int first)
       for(q = 0; q < D->nq; q++) x->cons[q] = (1. - RK)*x->cons[q] + RK*x->RKcons[q];
       if(D->mhd) for(q = 0; q < 5; q++) x->Phi[q] = (1. - RK)*x->Phi[q] + RK*x->RK_Phi[q];
    }
+   for(int p = 0; p < D->Npl; p++)   /* adjust_RK_planets_aux, misc.c:258-264 */
+      for(q = 0; q < 8; q++) D->sacc[p][q] = (1. - RK)*D->sacc[p][q] + RK*D->sacc_rk[p][q];
    plm_phi();
    if(D->Nr > 1) { build_faces(1); plm_trans(1); }
    if(D->Nz > 1) { build_faces(2); plm_trans(2); }
@@ -1858,7 +1950,10 @@ port_domain *disco_port_create(const disco_host_domain *h)
    disco_bc_op bops[DISCO_BC_MAX_OPS];
    if(disco_bc_plugin_ops(h->mod.boundary, bops) < 0) { free(d); return NULL; }
    if(h->par.Timestep != 0 && h->par.Timestep != 3) { free(d); return NULL; }
-   if(h->par.sinkType || h->par.nozzleType) { free(d); return NULL; }
+   if(h->par.sinkType < 0 || h->par.sinkType > 3 || (h->par.nozzleType != 0 && h->par.nozzleType != 1)) {
+      free(d);
+      return NULL;
+   }
    if(h->mod.hydro == DISCO_HYDRO_GRMHD || (d->mhd && h->mod.boundary > DISCO_BC_FIXED3D) ||
       (h->mod.analysis == DISCO_DIAG_MHDMRI && !d->mhd) || h->mod.analysis > DISCO_DIAG_MHDMRI) {
       free(d); return NULL;
@@ -1933,6 +2028,7 @@ double disco_port_step(port_domain *d)
       memcpy(d->cells[c].RKcons, d->cells[c].cons, sizeof(double)*MAXQ);
       memcpy(d->cells[c].RK_Phi, d->cells[c].Phi, sizeof(double)*5);
    }
+   memcpy(d->sacc_rk, d->sacc, sizeof d->sacc);   /* planet_RK_copy, timestep.c:25-27 */
    if(d->par.Timestep == 3) {   /* timestep.c:35-42 */
       onestep(0.0, dt, 1);
       d->t += dt;
@@ -1947,6 +2043,13 @@ double disco_port_step(port_domain *d)
    }
    add_diagnostics(dt);
    return dt;
+}
+
+/* The sink accumulators of the first nbody bodies, out[8 b + k]. */
+void disco_port_sink_accum(const port_domain *d, double *out, int nbody)
+{
+   for(int b = 0; b < nbody && b < d->Npl; b++)
+      for(int k = 0; k < 8; k++) out[8*b + k] = d->sacc[b][k];
 }
 
 int disco_port_run(port_domain *d, int nsteps)

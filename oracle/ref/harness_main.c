@@ -211,6 +211,19 @@ int main(int argc, char **argv)
          FILE *f = fopen(argv[3], "wb");
          write_state(d, f, 0);
          fclose(f);
+         /* the bodies and their sink accumulators, before report() prints
+          * and zeroes them: int32 Npl, then per body r, phi, M, omega, vr,
+          * eps, gravL, dM, accL, Ls, kin, therm, linXmom, linYmom */
+         FILE *pf = fopen("planets.bin", "wb");
+         int npl = d->Npl, p;
+         fwrite(&npl, sizeof npl, 1, pf);
+         for(p = 0; p < npl; p++) {
+            struct planet *b = d->thePlanets + p;
+            double v[14] = {b->r, b->phi, b->M, b->omega, b->vr, b->eps, b->gravL, b->dM, b->accL,
+                            b->Ls, b->kin, b->therm, b->linXmom, b->linYmom};
+            fwrite(v, sizeof(double), 14, pf);
+         }
+         fclose(pf);
          /* the reference's own diagnostics of the final state: one line
           * appended to report.dat in the working directory */
          report(d);

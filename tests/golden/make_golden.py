@@ -84,6 +84,21 @@ CASES = {
     "cfg4t_body": ("configs/cfg4_grmhd_torus", {"Num_R": 16, "Num_Z": 4, "R_Min": 8.0, "R_Max": 16.0,
                                                 "Z_Min": -2.0, "Z_Max": 2.0}, 5),
     "cfg4t_n24": ("configs/cfg4_grmhd_torus", {"Num_R": 24, "Num_Z": 12}, 5),
+    # accreting sinks and the gas nozzle (sink.c:105-247) on the planet disk
+    # (dt is about 0.5 here, so the accretion rate Sink_Par1 x omega_p stays
+    # well below 1 per step; the central body has omega 0 and accretes
+    # nothing): polynomial sinks (Sink_Type 1) with delta 0.5, an
+    # exponential sink (Sink_Type 2) with delta 0, and the nozzle
+    # (Nozzle_Type 1) feeding gas at r = 1.5
+    "cfg3_sink": ("configs/cfg3_planet_disk",
+                  {"Num_R": 24, "Sink_Type": 1, "Sink_Number": 0, "Sink_Par1": 0.2, "Sink_Par2": 0.5,
+                   "Sink_Par3": 0.15, "Sink_Par4": 2.0, "Sink_Par5": 2.0}, 10),
+    "cfg3_sink_exp": ("configs/cfg3_planet_disk",
+                      {"Num_R": 24, "Sink_Type": 2, "Sink_Number": 0, "Sink_Par1": 0.2, "Sink_Par2": 0.0,
+                       "Sink_Par3": 0.1, "Sink_Par4": 2.0, "Sink_Par5": 1.0}, 10),
+    "cfg3_nozzle": ("configs/cfg3_planet_disk",
+                    {"Num_R": 24, "Nozzle_Type": 1, "Nozzle_Par1": 1.5, "Nozzle_Par2": 0.5,
+                     "Nozzle_Par3": 0.8, "Nozzle_Par4": 20.0}, 10),
 }
 
 
@@ -153,9 +168,13 @@ def run_case(name: str, ref: str) -> None:
         nq, nring = np.frombuffer(raw[:8], dtype="<i4")
         dg = np.frombuffer(raw[8:], dtype="<f8")
         diag_tavg, diag_Qrz = dg[0], dg[1:1 + nq * nring].reshape(nring, nq)
+        # the bodies and their sink accumulators before report() zeroed them
+        praw = open(os.path.join(td, "planets.bin"), "rb").read()
+        npl = int(np.frombuffer(praw[:4], dtype="<i4")[0])
+        planets = np.frombuffer(praw[4:], dtype="<f8")[:14 * npl].reshape(npl, 14)
     out = {"par_text": np.array(par), "nsteps": nsteps, "cfg": np.array(cfg), "report": rep,
            "mk_text": np.array(mk_text),
-           "diag_tavg": diag_tavg, "diag_Qrz": diag_Qrz,
+           "diag_tavg": diag_tavg, "diag_Qrz": diag_Qrz, "planets": planets,
            "Np": ini["Np"], "r_jph": ini["r_jph"], "z_kph": ini["z_kph"], "real": ini["real"],
            "init_piph": ini["piph"], "init_dphi": ini["dphi"], "init_prim": ini["prim"],
            "init_cons": ini["cons"], "init_wiph": ini["wiph"],

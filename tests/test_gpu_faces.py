@@ -76,12 +76,17 @@ def test_face_tables_after_steps_match_oracle(name):
         # positions can differ from the oracle's in the last bits where FP64
         # transcendentals (the planet disk's gravity and alpha scale height,
         # the exact mesh rotation) differ from glibc's -- within 1e-12 of a
-        # turn, the bar of the position check -- and a sliver face's area is
-        # compared against the largest face's, not its own
+        # turn, the bar of the position check.  Each of a face's two phi
+        # edges may move by that angle, which changes its area by at most
+        # the angle times the face's extent across phi (r dz for an r face,
+        # r dr for a z face): the area bar, for the largest extent
         if len(ref["dA"]) == 0:   # a 2D domain has no z faces
             continue
-        assert np.allclose(dev["phic"], ref["phic"], rtol=0, atol=1e-12 * 2 * np.pi), key
-        assert np.max(np.abs(dev["dA"] - ref["dA"])) <= 1e-12 * np.abs(ref["dA"]).max(), key
+        atol_phi = 1e-12 * 2 * np.pi
+        assert np.allclose(dev["phic"], ref["phic"], rtol=0, atol=atol_phi), key
+        rj, zk = np.asarray(h.r_jph, dtype=float), np.asarray(h.z_kph, dtype=float)
+        ext = np.abs(rj).max() * max(np.diff(rj).max(initial=0.0), np.diff(zk).max(initial=0.0))
+        assert np.max(np.abs(dev["dA"] - ref["dA"])) <= 2 * atol_phi * ext, key
     d.close()
 
 

@@ -18,6 +18,9 @@ CASES = {"cfg1_n24": "configs/cfg1_vortex", "cfg2_n12": "configs/cfg2_mhd_disk",
          "cfg3_n24": "configs/cfg3_planet_disk", "cfg5_n16": "configs/cfg5_cbd_mhd",
          "cfg1_rk3": "configs/cfg1_vortex", "cfg2_rk3": "configs/cfg2_mhd_disk",
          "cfg3_rk3": "configs/cfg3_planet_disk", "cfg3_cooldamp": "configs/cfg3_planet_disk",
+         # accreting sinks (polynomial, exponential) and the gas nozzle
+         "cfg3_sink": "configs/cfg3_planet_disk", "cfg3_sink_exp": "configs/cfg3_planet_disk",
+         "cfg3_nozzle": "configs/cfg3_planet_disk",
          "cfg4_n12": "configs/cfg4_grmhd_disk",
          "cfg4_diag": "configs/cfg4_grmhd_disk",
          # Fishbone-Moncrief torus around a Kerr black hole (a = 0.9)
@@ -144,7 +147,7 @@ def test_mixed_precision_error(name):
 # 3e-7 at 256, with or without the planet or viscosity); the 1e-6 bar is
 # checked at batch-instance resolution by test_mixed_precision_planet_disk.
 MIXED_BOUND = {"cfg3_n24": 3e-6, "cfg3_outflow": 3e-6, "cfg3_rk3": 3e-6, "cfg2_rk3": 3e-6,
-               "cfg3_cooldamp": 3e-6}
+               "cfg3_cooldamp": 3e-6, "cfg3_sink": 3e-6, "cfg3_sink_exp": 3e-6, "cfg3_nozzle": 3e-6}
 # The reference's RK3 run of the MHD disk is not smooth: after its first
 # step the CFL dt falls 2000-fold (8.9e-1 to 4.2e-4), both paths alike.
 # In it the mixed path's mass and momentum stay at 3e-8 while the field's
