@@ -84,6 +84,16 @@ WORKLOADS = {
                      "batch": 64,
                      "cpu_sample": {"Num_R": 128},
                      "ref_sample": {"Num_R": 64}},
+    # the same disks at survey resolution: 512 members with Nr ~ U{16..64}
+    # (a few thousand cells each), where a member's own step is bound by
+    # its launches rather than its cells
+    "planet_batch_small": {"dir": "configs/cfg3_planet_disk",
+                           "desc": "512 independent 2D locally isothermal disk + planet runs (alpha 1e-3, "
+                                   "h/r 0.05, r in [0.4,2.5], Nr ~ U{16..64}, q ~ logU[1e-5,1e-3]), "
+                                   "one CUDA graph per step",
+                           "batch": 512, "nr_range": (16, 64),
+                           "cpu_sample": {"Num_R": 32},
+                           "ref_sample": {"Num_R": 32}},
     # GRMHD (FP64 only): thin disk around a Schwarzschild black hole in
     # Kerr-Schild cylindrical coordinates, about 4.9 M cells
     "grmhd_disk": {"dir": "configs/cfg4_grmhd_disk",
@@ -115,7 +125,8 @@ KERNEL_SYMBOL = {"flux_trans": "k_flux_trans", "plm_slopes": "k_plm_slopes", "pl
                  "ct_b2c_c2p": "k_ct_b2c_c2p", "mindt": "k_mindt", "diag": "k_diag",
                  "boundary": "k_boundary", "anchor": "k_anchor", "wcell": "k_wcell",
                  "wcell_ring": "k_wcell_ring", "wcell_avg": "k_wcell_avg", "after_first": "k_after_first",
-                 "ct_edge_flag": "k_set_flag"}
+                 "ct_edge_flag": "k_set_flag", "phi_sweep": "k_phi_sweep", "sink_acc": "k_sink_acc",
+                 "sink_final": "k_sink_final", "c2p_guess": "k_c2p_guess"}
 
 
 def _traffic(func: str, alg_bytes: float, workload: str):
@@ -223,7 +234,10 @@ def kernel_bytes(name: str, N: int, nf: dict, nq: int, sw: int, ct: bool) -> flo
     if name.startswith("plm_trans"):    # per cell: runs, gradient out; per face: slopes, area
         d = name[-1]
         return N * (nq * sw + sw + 4 * ix) + nf[d] * (nq * sw + sw)
-    if name == "flux_phi":
+    if name in ("flux_phi", "phi_sweep"):
+        # the staged sweep (plm_phi + flux_phi from one stage) reads the
+        # primitives and widths once and writes the gradients it forms: the
+        # same compulsory bytes as flux_phi alone
         return N * (3 * nq * sw + sw + 2 * f8 + c * 16 * sw)
     if name in ("flux_r", "flux_z"):
         d = name[-1]
@@ -273,13 +287,14 @@ def splitmix64(x: int):
     return x, z ^ (z >> 31)
 
 
-def batch_members(n: int):
+def batch_members(n: int, nr_range=(64, 512)):
     """(Num_R, Mass_Ratio) of batch member i, drawn from splitmix64 seeded i."""
     out = []
+    lo, hi = nr_range
     for i in range(n):
         st, a = splitmix64(i)
         st, b = splitmix64(st)
-        nr = 64 + a % 449
+        nr = lo + a % (hi - lo + 1)
         q = 10.0 ** (-5.0 + 2.0 * (b / 2.0 ** 64))
         out.append({"Num_R": int(nr), "Mass_Ratio": float(q)})
     return out
@@ -293,7 +308,7 @@ def measure_batch(args, wl):
     torch.cuda.set_device(dev)
     cfg = os.path.join(ROOT, wl["dir"])
     par, mk = os.path.join(cfg, "in.par"), os.path.join(cfg, "Makefile_opt.in")
-    mem = batch_members(wl["batch"])
+    mem = batch_members(wl["batch"], wl.get("nr_range", (64, 512)))
     res, sets, batches = {}, {}, {}
     for prec in (1, 0):
         doms = [dg.Domain(par, mk, precision=prec, overrides=m) for m in mem]
@@ -434,12 +449,13 @@ def measure_learned_c2p(args, wl, steps=None, warmup=None):
         d.upload(**saved)
         m.set_gate(0.0, ratio)
         d.attach_guess(m if guess else None)
-        nc0 = d.status()["c2p_no_converge"]
+        st0 = d.status()
         d.c2p_stats(reset=True)
         ms = d.run_timed(K)
         sc = d.c2p_stats(reset=True)
-        nc = d.status()["c2p_no_converge"] - nc0
-        return ms, sc, nc, d.state()["cons"]
+        st1 = d.status()
+        sc["nan_cells"] = st1["nan_cells"] - st0["nan_cells"]
+        return ms, sc, st1["c2p_no_converge"] - st0["c2p_no_converge"], d.state()["cons"]
 
     ms_plain, sp, ncp, up = arm(False)
     ms_learned, sl, ncl, ul = arm(True)
@@ -448,7 +464,10 @@ def measure_learned_c2p(args, wl, steps=None, warmup=None):
     real = d.host.real_mask()
 
     def rdiff(u):
-        return max(float(np.abs(u[q, real] - up[q, real]).sum() / max(np.abs(up[q, real]).sum(), 1e-300))
+        # over the cells finite in both states (the non-finite ones are
+        # counted per arm: nan_cells)
+        ok = real & np.isfinite(u).all(0) & np.isfinite(up).all(0)
+        return max(float(np.abs(u[q, ok] - up[q, ok]).sum() / max(np.abs(up[q, ok]).sum(), 1e-300))
                    for q in range(up.shape[0]))
     diff = rdiff(ul)
     d.close()
@@ -461,16 +480,16 @@ def measure_learned_c2p(args, wl, steps=None, warmup=None):
     return {"cells": cells, "steps": K,
             "plain": {"zone_updates_per_s": cells * K / (ms_plain / 1e3), "ms_per_step": ms_plain / K,
                       "mean_k_converge": kp, "mean_iterations": mean(sp, "iters"), "calls": sp["calls"],
-                      "no_converge": ncp},
+                      "no_converge": ncp, "nan_cells": sp["nan_cells"]},
             "learned": {"zone_updates_per_s": cells * K / (ms_learned / 1e3), "ms_per_step": ms_learned / K,
                         "mean_k_converge": kl, "mean_iterations": mean(sl, "iters"), "calls": sl["calls"],
-                        "no_converge": ncl,
+                        "no_converge": ncl, "nan_cells": sl["nan_cells"],
                         "guess_used_fraction": sl["guessed"] / sl["calls"] if sl["calls"] else None},
             "k_converge_ratio_plain_over_learned": (kp / kl) if kp and kl else None,
             "final_state_rel_l1_learned_vs_plain": diff,
             "learned_gate_1e-2": {"zone_updates_per_s": cells * K / (ms_g / 1e3), "ms_per_step": ms_g / K,
                                   "mean_k_converge": mean(sg, "kconv"), "mean_iterations": mean(sg, "iters"),
-                                  "no_converge": ncg,
+                                  "no_converge": ncg, "nan_cells": sg["nan_cells"],
                                   "guess_used_fraction": sg["guessed"] / sg["calls"] if sg["calls"] else None,
                                   "final_state_rel_l1_vs_plain": rdiff(ug),
                                   "gate": "learned start taken where its residual is below 1e-2 of the "

@@ -374,7 +374,7 @@ class Domain:
     def set_sweep(self, on: bool) -> bool:
         """Staged phi sweep (True) or separate plm_phi / flux_phi kernels;
         returns the setting in force (disco_gpu_debug_sweep)."""
-        rc = lib().disco_gpu_debug_sweep(self._g, int(on))
+        rc = lib().disco_gpu_debug_sweep(self._g, int(on))   # 2: copies withheld (timeout test)
         _check(rc if rc < 0 else 0, "disco_gpu_debug_sweep")
         return bool(rc)
 

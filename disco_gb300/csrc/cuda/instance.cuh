@@ -622,11 +622,13 @@ struct Instance : InstanceBase {
   // kernels (0); returns the setting in force
   int set_sweep(int on) override {
     sweep = on && sweep_ok;
+    sweep_no_copies = sweep && on == 2;
     for (int i = 0; i < 2; ++i)
       if (graph[i]) { cudaGraphExecDestroy(graph[i]); graph[i] = nullptr; }
     return sweep ? 1 : 0;
   }
   bool sweep = false;   // k_phi_sweep in place of k_plm_phi + k_flux_phi
+  bool sweep_no_copies = false;   // debug: the sweep issues no copies (its waits run out)
   CUtensorMap tm_prim{}, tm_dphi{};
 
   // ---- launch helpers -----------------------------------------------------
@@ -731,7 +733,8 @@ struct Instance : InstanceBase {
     if (first) launch_wcell();
     if constexpr (kMix<R>) {
       if (sweep) {   // plm_phi and the phi fluxes from one staged pass
-        LAUNCH("phi_sweep", (k_phi_sweep<Phys, R, NQ><<<S.nchunk, kTileCells, 0, st>>>(P, S, fac, tm_prim, tm_dphi)));
+        LAUNCH("phi_sweep", (k_phi_sweep<Phys, R, NQ><<<S.nchunk, kTileCells, 0, st>>>(P, S, fac, tm_prim, tm_dphi,
+                                                                                    sweep_no_copies ? 1 : 0)));
         launch_plm_trans();
       }
     }

@@ -13,8 +13,10 @@
 // that wrap around the ring's ends (i0 = 0 on the left, the ring's last
 // chunk on the right) are patched with plain loads after the wait.
 //
-// Every wait is bounded: on a timeout the block counts it in the health
-// counters, waits (again bounded) for its copies in flight and returns.
+// Every wait is bounded in time (about a second of SM clock): on a timeout
+// the block counts it in the health counters, waits (again bounded) for its
+// copies in flight and returns.  A debug mode issues no copies, so that a
+// test can make the wait run out and read the count.
 #pragma once
 #include <cuda.h>
 #include <cudaTypedefs.h>
@@ -26,7 +28,7 @@ namespace disco {
 
 constexpr int kSweepBox = 136;    // elements per staged row: 128 + 3 halo, + up to 3 of alignment, 16-byte multiple
 constexpr int kSweepSlot = 160;   // floats per shared-memory row slot (640 B, a multiple of 128 B)
-constexpr int kSweepMaxWait = 1 << 22;
+constexpr long long kSweepMaxCycles = 1LL << 31;   // about 1 s at 2 GHz
 
 #ifdef __CUDACC__
 __device__ inline void tma_load_1d(void* dst, const CUtensorMap* map, int x, unsigned long long* bar) {
@@ -54,15 +56,17 @@ __device__ inline bool mbar_try_wait(unsigned long long* bar, unsigned parity) {
   return ok != 0;
 }
 __device__ inline bool mbar_wait_bounded(unsigned long long* bar, unsigned parity) {
-  for (int it = 0; it < kSweepMaxWait; ++it)
-    if (mbar_try_wait(bar, parity)) return true;
-  return false;
+  const long long t0 = clock64();
+  while (!mbar_try_wait(bar, parity))
+    if (clock64() - t0 > kSweepMaxCycles) return false;
+  return true;
 }
 
 template <typename Phys, typename R, int NQ>
 __global__ void __launch_bounds__(kTileCells) k_phi_sweep(DevParams P, DevState<R> S, double fac,
                                                          const __grid_constant__ CUtensorMap tm_prim,
-                                                         const __grid_constant__ CUtensorMap tm_dphi) {
+                                                         const __grid_constant__ CUtensorMap tm_dphi,
+                                                         int no_copies) {
   static_assert(sizeof(R) == 4, "the staged sweep is the mixed path's");
   __shared__ __align__(128) float stage[(NQ + 1) * kSweepSlot];
   __shared__ float gsh[NQ][kTileCells + 2];   // gradp of window cells w = 1 .. T+1
@@ -81,7 +85,7 @@ __global__ void __launch_bounds__(kTileCells) k_phi_sweep(DevParams P, DevState<
     mbar_fence_init();
   }
   __syncthreads();
-  if (t == 0) {
+  if (t == 0 && !no_copies) {
     mbar_expect_tx(&bar, (unsigned)((NQ + 1) * kSweepBox * sizeof(float)));
 #pragma unroll
     for (int q = 0; q < NQ; ++q) {

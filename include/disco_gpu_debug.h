@@ -43,11 +43,15 @@ int disco_gpu_debug_faces(disco_gpu *g, int dim, int *npair, long *nface,
  * state is left unchanged, so stepping may continue. */
 int disco_gpu_debug_grad(disco_gpu *g, double *gradp, double *gradr, double *gradz);
 
-/* The mixed path's azimuthal sweep: on != 0 selects the staged single-pass
+/* The mixed path's azimuthal sweep: on = 1 selects the staged single-pass
  * kernel (k_phi_sweep, the default where it applies), 0 the separate
- * plm_phi and phi-flux kernels, for tests that compare the two.  Returns
- * the setting in force (0 where the staged sweep does not apply: the plain
- * FP64 path, explicit viscosity). */
+ * plm_phi and phi-flux kernels, for tests that compare the two; 2 the
+ * staged kernel with its tensor copies withheld, so that its bounded
+ * waits (about a second each) run out: every block then counts a timeout
+ * in disco_gpu_status's async_timeouts and returns without its fluxes
+ * (the state of that step is not meaningful).  Returns the setting in
+ * force (0 where the staged sweep does not apply: the plain FP64 path,
+ * explicit viscosity). */
 int disco_gpu_debug_sweep(disco_gpu *g, int on);
 
 /* Applies the library's integer-pipe FP64 -> FP32 and FP32 -> FP64

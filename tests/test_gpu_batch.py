@@ -104,7 +104,12 @@ def _same(d1, d2, tag):
     differently inside a multi-instance kernel than inside its own kernel,
     so they agree to FP32 rounding: within 1e-9 relative L1 per physical
     quantity (vectors through their norm), positions within 1e-9 of a turn,
-    time exactly."""
+    time exactly.  An isothermal run's energy is the exception: its
+    pressure comes from the sound-speed profile, so the energy never feeds
+    back, and FP32 rounding differences in its own flux accumulate there
+    undamped (1.4e-7 after 13 steps of the planet disk, with mass,
+    momentum and passive scalar exactly equal); it is held to the mixed
+    path's 1e-6."""
     s1, s2 = d1.state(), d2.state()
     assert s1["t"] == s2["t"], tag
     if tag[1] == 0:
@@ -118,8 +123,10 @@ def _same(d1, d2, tag):
         real = h.real_mask()
         r = cell_radius(h.Np, h.r_jph, h.Nr, h.Nz)[real]
         e = grouped_rel_l1(s2["cons"][:, real], s1["cons"][:, real], r, 8 if h.num_q >= 8 else 5)
-        print(tag, "max relative L1 per quantity", max(e.values()))
-        assert max(e.values()) < 1e-9, (tag, e)
+        print(tag, "relative L1 per quantity", e)
+        iso = bool(d1.params.isothermal_flag)
+        for k, v in e.items():
+            assert v < (1e-6 if (iso and k == "energy") else 1e-9), (tag, k, e)
         dp = np.abs((s1["piph"] - s2["piph"] + np.pi) % (2 * np.pi) - np.pi)
         assert dp.max() < 1e-9 * 2 * np.pi, tag
     st = d2.status()

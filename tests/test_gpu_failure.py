@@ -78,3 +78,27 @@ def test_grmhd_newton_cap_is_counted():
     p = d.state()["prim"]
     assert np.all(np.isfinite(p[:, c]))
     d.close()
+
+
+def test_sweep_wait_timeout_is_counted():
+    """The staged phi sweep's waits on its tensor copies are bounded (about
+    a second of SM clock).  With the copies withheld (a debug mode of
+    disco_gpu_debug_sweep) no wait can complete: every block counts the
+    timeout, waits once more (bounded) and returns, the call returns 0, and
+    the context stays usable -- the domain steps on with the copies back,
+    and so does a new one."""
+    d, g = _domain("cfg1_n24", 1)
+    assert d.set_sweep(True)
+    assert d.status()["async_timeouts"] == 0
+    assert d.set_sweep(2)
+    d.timestep(d.getmindt())
+    assert d.status()["async_timeouts"] >= 1
+    n0 = d.status()["async_timeouts"]
+    assert d.set_sweep(True)
+    d.timestep(d.getmindt())
+    assert d.status()["async_timeouts"] == n0
+    d.close()
+    e, _ = _domain("cfg1_n24", 1)
+    e.run(2)
+    assert np.isfinite(e.state()["cons"]).all() and e.status()["async_timeouts"] == 0
+    e.close()
