@@ -84,14 +84,14 @@ WORKLOADS = {
                      "batch": 64,
                      "cpu_sample": {"Num_R": 128},
                      "ref_sample": {"Num_R": 64}},
-    # the same disks at survey resolution: 512 members with Nr ~ U{16..64}
+    # the same disks at survey resolution: 256 members with Nr ~ U{16..64}
     # (a few thousand cells each), where a member's own step is bound by
     # its launches rather than its cells
     "planet_batch_small": {"dir": "configs/cfg3_planet_disk",
-                           "desc": "512 independent 2D locally isothermal disk + planet runs (alpha 1e-3, "
+                           "desc": "256 independent 2D locally isothermal disk + planet runs (alpha 1e-3, "
                                    "h/r 0.05, r in [0.4,2.5], Nr ~ U{16..64}, q ~ logU[1e-5,1e-3]), "
                                    "one CUDA graph per step",
-                           "batch": 512, "nr_range": (16, 64),
+                           "batch": 256, "nr_range": (16, 64),
                            "cpu_sample": {"Num_R": 32},
                            "ref_sample": {"Num_R": 32}},
     # GRMHD (FP64 only): thin disk around a Schwarzschild black hole in
