@@ -448,13 +448,16 @@ struct Instance : InstanceBase {
     }
     {   // ghost cells filled by the boundary plugin (fixed.c: r ghosts;
         // fixed3d.c: r and z ghosts), as chunks of kTileCells cells per ring
+      // a periodic dimension's ghosts come from the ring copy instead
+      // (R_Periodic, Z_Periodic: onestep.c:166-172 skips that dimension's
+      // boundary_trans)
       std::vector<int> gr, gi;
       for (int jk = 0; jk < nring; ++jk) {
         int k = jk / Nr, j = jk - k * Nr;
         bool rghost = (j < P.NgRa) || (j >= Nr - P.NgRb);
         bool zghost = (k < P.NgZa) || (k >= Nz - P.NgZb);
-        bool fill = P.boundary_id == 0 ? (rghost && Nr > 1)
-                  : P.boundary_id == 1 ? ((rghost && Nr > 1) || (zghost && Nz > 1)) : false;
+        bool rfill = rghost && Nr > 1 && !p.R_Periodic, zfill = zghost && Nz > 1 && !p.Z_Periodic;
+        bool fill = P.boundary_id == 0 ? rfill : P.boundary_id == 1 ? (rfill || zfill) : false;
         if (!fill) continue;
         for (int i0 = 0; i0 < dom->Np[jk]; i0 += kTileCells) { gr.push_back(jk); gi.push_back(i0); }
       }
@@ -473,6 +476,24 @@ struct Instance : InstanceBase {
         CK(cudaGetLastError());
         CK(cudaStreamSynchronize(st));
         S.ghost_tab = tab;
+      }
+    }
+    {   // periodic ghost rings and their sources, r then z (exchange.c)
+      std::vector<int> dst, src;
+      for (int dim = 1; dim <= 2; ++dim) {
+        for (int k = 0; k < Nz; ++k)
+          for (int j = 0; j < Nr; ++j) {
+            const int s = disco_periodic_source(dom, dim, j, k);
+            if (s < 0) continue;
+            dst.push_back(j + Nr * k);
+            src.push_back(s);
+          }
+        n_pcopy[dim - 1] = (int)dst.size() - (dim == 2 ? n_pcopy[0] : 0);
+      }
+      if (!dst.empty()) {
+        A(&pc_dst, dst.size()); A(&pc_src, src.size());
+        CK(cudaMemcpy(pc_dst, dst.data(), sizeof(int) * dst.size(), cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(pc_src, src.data(), sizeof(int) * src.size(), cudaMemcpyHostToDevice));
       }
     }
     A(&S.planets, MAX_PL); A(&S.scal, SC_COUNT); A(&S.errs, 1);
@@ -576,6 +597,12 @@ struct Instance : InstanceBase {
         long np_ = dom->ring_off[src + 1] - dom->ring_off[src];
         ring_Om_h[jk] = np_ > 0 ? sum / (double)np_ : 0.0;
       }
+      // a periodic ghost ring takes its source ring's frame (r, then z)
+      for (int dim = 1; dim <= 2; ++dim)
+        for (int jk = 0; jk < nring; ++jk) {
+          const int s = disco_periodic_source(dom, dim, jk % Nr, jk / Nr);
+          if (s >= 0) ring_Om_h[jk] = ring_Om_h[s];
+        }
     }
     CK(cudaMemcpy(S.ring_Om, ring_Om_h.data(), sizeof(double) * nring, cudaMemcpyHostToDevice));
     LAUNCH("ring_geom", (k_ring_geom<R><<<blocks(nring), 256, 0, st>>>(P, S, nring)));
@@ -646,12 +673,31 @@ struct Instance : InstanceBase {
   }
   disco_bc_op bc_ops[DISCO_BC_MAX_OPS];
   int n_bc_ops = 0;
+  // R_Periodic / Z_Periodic: the ghost rings of that dimension take their
+  // source rings' cells (k_periodic_copy)
+  int n_pcopy[2] = {0, 0};
+  int* pc_dst = nullptr;
+  int* pc_src = nullptr;
+  void launch_periodic(int dim) {
+    const int n = n_pcopy[dim - 1];
+    if (!n) return;
+    const int o = dim == 1 ? 0 : n_pcopy[0];
+    LAUNCH("periodic", (k_periodic_copy<R, NQ><<<n, kTileCells, 0, st>>>(P, S, ct ? C.Phi : nullptr,
+                                                                       ct ? C.RKPhi : nullptr, pc_dst + o,
+                                                                       pc_src + o)));
+  }
+  // onestep.c:166-172: exchangeData(r); boundary_trans(r) unless
+  // R_Periodic; exchangeData(z); boundary_trans(z) unless Z_Periodic
   void launch_boundary() {
     if (n_bc_ops > 0) {   // plugins written as boundary_functions.c primitives
+      launch_periodic(1);
+      bool z_started = false;
       for (int o = 0; o < n_bc_ops; ++o) {
         const disco_bc_op& b = bc_ops[o];
         const int dim = b.side < 2 ? 1 : 2, side = b.side & 1;
+        if (dim == 2 && !z_started) { launch_periodic(2); z_started = true; }
         if ((dim == 1 && Nr <= 1) || (dim == 2 && Nz <= 1)) continue;
+        if ((dim == 1 && n_pcopy[0]) || (dim == 2 && n_pcopy[1])) continue;
         const int ng = dim == 1 ? (side ? P.NgRb : P.NgRa) : (side ? P.NgZb : P.NgZa);
         if (ng == 0) continue;
         const int per_layer = dim == 1 ? Nz : Nr, n = dim == 1 ? Nr : Nz;
@@ -667,10 +713,17 @@ struct Instance : InstanceBase {
           }
         }
       }
+      if (!z_started) launch_periodic(2);
       return;
     }
+    // fixed / fixed3d fill the non-periodic ghosts in one kernel: after the
+    // r copy (its corners then come from the z boundary, as boundary_trans
+    // dimension 2 rewrites them) and before the z copy (which rewrites the
+    // corners from the source layers)
+    launch_periodic(1);
     if (S.nghost > 0)
       LAUNCH("boundary", (k_boundary<R, NQ><<<S.nghost, kTileCells, 0, st>>>(P, S)));
+    launch_periodic(2);
   }
   void launch_faces() {
     if (npair[0] == 0 && npair[1] == 0) return;

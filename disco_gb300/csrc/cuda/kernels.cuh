@@ -1766,6 +1766,46 @@ DISCO_D void k_boundary_body(const DevParams& P, const DevState<R>& S, int bx_, 
 #pragma unroll
   for (int q = 0; q < NQ; ++q) S.prim[q * S.N + c] = (R)prim[q];
 }
+// exchangeData with one rank and a periodic dimension (exchange.c:173-279:
+// the cartesian communicator wraps around, so the rank is its own left and
+// right neighbour): every cell of ghost ring dst[b] takes the state of the
+// same cell of ring src[b] -- primitives, conserved state and its RK copy,
+// position, width and mesh speed, and with CT the face fluxes and their RK
+// copy (struct cell_lite, exchange.c:6-15).  The two rings have the same Np
+// (set at set-up, as the exchange's Np message does), and on the mixed path
+// the same ring frame, so the frame-relative omega copies as it is.
+template <typename R, int NQ>
+__global__ void __launch_bounds__(kTileCells) k_periodic_copy(DevParams P, DevState<R> S, double* Phi,
+                                                              double* RKPhi, const int* dst, const int* src) {
+  (void)P;
+  const int jd = dst[blockIdx.x], js = src[blockIdx.x];
+  const int od = S.ring_off[jd], os = S.ring_off[js];
+  const int np = S.ring_off[js + 1] - os;
+  const int N = S.N;
+  double* piph = const_cast<double*>(S.piph);
+  for (int i = threadIdx.x; i < np; i += blockDim.x) {
+    const int cd = od + i, cs = os + i;
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) {
+      S.prim[q * N + cd] = S.prim[q * N + cs];
+      S.cons[q * N + cd] = S.cons[q * N + cs];
+      if constexpr (kMix<R>) S.RKdU[q * N + cd] = S.RKdU[q * N + cs];
+      else S.RKcons[q * N + cd] = S.RKcons[q * N + cs];
+    }
+    piph[cd] = piph[cs];
+    S.dphi[cd] = S.dphi[cs];
+    S.wiph[cd] = S.wiph[cs];
+    if constexpr (kMix<R>) S.dphi_r[cd] = S.dphi_r[cs];
+    if (Phi) {
+#pragma unroll
+      for (int f = 0; f < 5; ++f) {
+        Phi[f * N + cd] = Phi[f * N + cs];
+        RKPhi[f * N + cd] = RKPhi[f * N + cs];
+      }
+    }
+  }
+}
+
 template <typename R, int NQ>
 __global__ void __launch_bounds__(kTileCells) k_boundary(DevParams P, DevState<R> S) {
   k_boundary_body<R, NQ>(P, S, (int)blockIdx.x, (int)blockIdx.y);

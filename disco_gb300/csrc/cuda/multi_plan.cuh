@@ -8,7 +8,7 @@
 //
 // The group takes the sequence of an instance without constrained
 // transport, boundary plugins, the staged phi sweep, a learned cons2prim
-// start, sinks or the nozzle; such instances stay outside (a batch gives them their own graph
+// start, sinks, the nozzle or periodic ghosts; such instances stay outside (a batch gives them their own graph
 // branch).  Included by instance.cuh after the Instance template.
 #pragma once
 #include "multi.cuh"
@@ -38,7 +38,7 @@ struct MultiPlan : MultiPlanBase {
 
   static bool covered(const Inst* x) {
     return !x->ct && x->n_bc_ops == 0 && !x->sweep && !x->mlp_on && !x->rec_on.X && !x->sink_on &&
-           x->P.nozzle_type == 0;
+           x->P.nozzle_type == 0 && !x->n_pcopy[0] && !x->n_pcopy[1];
   }
   bool accepts(InstanceBase* b) const override {
     auto* x = dynamic_cast<Inst*>(b);

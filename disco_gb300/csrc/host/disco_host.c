@@ -442,10 +442,6 @@ int disco_host_setup(const disco_params *par, const disco_modules *mod,
    if(par->LogZoning != 0) {
       disco_set_error("disco_host_setup: only Log_Zoning 0 is built"); return DISCO_E_MODULE;
    }
-   if(par->R_Periodic || par->Z_Periodic) {
-      disco_set_error("disco_host_setup: periodic r/z boundaries are not built");
-      return DISCO_E_MODULE;
-   }
    disco_host_domain *d = (disco_host_domain *)calloc(1, sizeof(*d));
    if(!d) return DISCO_E_NOMEM;
    d->par = *par;
@@ -503,6 +499,18 @@ int disco_host_setup(const disco_params *par, const disco_modules *mod,
          d->Np[jk] = Np;
       }
    }
+   /* periodic dimensions: a ghost ring holds the cells of its source ring,
+    * Np included (exchange.c:123-171 sends Np with the cells) */
+   for(k = 0; k < Nz; k++)
+      for(j = 0; j < Nr; j++) {
+         int src = disco_periodic_source(d, 1, j, k);
+         if(src >= 0) d->Np[j + Nr*k] = d->Np[src];
+      }
+   for(k = 0; k < Nz; k++)
+      for(j = 0; j < Nr; j++) {
+         int src = disco_periodic_source(d, 2, j, k);
+         if(src >= 0) d->Np[j + Nr*k] = d->Np[src];
+      }
    for(k = 0; k < Nr*Nz; k++) { d->ring_off[k] = off; off += d->Np[k]; }
    d->ring_off[Nr*Nz] = off;
    d->Ncell = off;
@@ -576,8 +584,45 @@ int disco_host_setup(const disco_params *par, const disco_modules *mod,
          }
       }
    }
+   /* the first exchange of a periodic run (main.c:53-61): r ghost rings,
+    * then whole z ghost layers, take their source rings' cells */
+   for(int dim = 1; dim <= 2; dim++)
+      for(k = 0; k < Nz; k++)
+         for(j = 0; j < Nr; j++) {
+            int src = disco_periodic_source(d, dim, j, k);
+            if(src < 0) continue;
+            long c0 = d->ring_off[j + Nr*k], s0 = d->ring_off[src];
+            int i, q;
+            for(i = 0; i < d->Np[src]; i++) {
+               d->piph[c0 + i] = d->piph[s0 + i];
+               d->dphi[c0 + i] = d->dphi[s0 + i];
+               for(q = 0; q < nq; q++) d->prim[(size_t)q*N + c0 + i] = d->prim[(size_t)q*N + s0 + i];
+            }
+         }
    *out = d;
    return DISCO_OK;
+}
+
+/* The ring whose cells a periodic ghost ring holds, or -1: with R_Periodic
+ * (dim 1) ghost ring j < NgRa takes real ring j + Nr_real and ring
+ * j >= Nr - NgRb takes j - Nr_real, in every layer; with Z_Periodic (dim 2)
+ * likewise in k, for every j.  With one rank, the cartesian communicator's
+ * wrap-around makes exchangeData (exchange.c:173-279) exactly this copy. */
+int disco_periodic_source(const disco_host_domain *d, int dim, int j, int k)
+{
+   int Nr = d->Nr, Nz = d->Nz;
+   if(dim == 1) {
+      if(!d->par.R_Periodic || Nr <= 1) return -1;
+      int nreal = Nr - d->NgRa - d->NgRb;
+      if(j < d->NgRa) return (j + nreal) + Nr*k;
+      if(j >= Nr - d->NgRb) return (j - nreal) + Nr*k;
+      return -1;
+   }
+   if(!d->par.Z_Periodic || Nz <= 1) return -1;
+   int nreal = Nz - d->NgZa - d->NgZb;
+   if(k < d->NgZa) return j + Nr*(k + nreal);
+   if(k >= Nz - d->NgZb) return j + Nr*(k - nreal);
+   return -1;
 }
 
 void disco_host_free(disco_host_domain *d)

@@ -20,6 +20,10 @@ void disco_set_error(const char *msg);
 /* Exposed for tests of the glibc-rand restatement. */
 int disco_rand_sequence(unsigned int seed, int n, int *out);
 
+/* The ring whose cells a periodic ghost ring (j, k) holds for dimension
+ * dim (1: r, 2: z), or -1 when (j, k) is not a periodic ghost of dim. */
+int disco_periodic_source(const disco_host_domain *d, int dim, int j, int k);
+
 #ifdef __cplusplus
 }
 #endif

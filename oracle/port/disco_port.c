@@ -1637,22 +1637,68 @@ static void init_side(const disco_bc_op *o)
    }
 }
 
+/* exchangeData (exchange.c:173-279) of a run on one rank with a periodic
+ * dimension: the cartesian communicator wraps around, so the rank is its
+ * own neighbour on both sides, and ghost ring j < Ng (k < Ng) takes the
+ * cells of real ring j + Nreal (k + Nreal), ghost ring j >= N - Ng those of
+ * j - Nreal: every field of struct cell_lite (exchange.c:6-15). */
+static int periodic_dim(int dim)
+{
+   return dim == 1 ? (D->par.R_Periodic && D->Nr > 1) : (D->par.Z_Periodic && D->Nz > 1);
+}
+static void exchange(int dim)
+{
+   if(!periodic_dim(dim)) return;
+   int nreal = dim == 1 ? D->Nr - D->NgRa - D->NgRb : D->Nz - D->NgZa - D->NgZb;
+   int ga = dim == 1 ? D->NgRa : D->NgZa, gb = dim == 1 ? D->NgRb : D->NgZb;
+   int n = dim == 1 ? D->Nr : D->Nz;
+   for(int k = 0; k < D->Nz; k++) for(int j = 0; j < D->Nr; j++) {
+      int a = dim == 1 ? j : k, s;
+      if(a < ga) s = a + nreal;
+      else if(a >= n - gb) s = a - nreal;
+      else continue;
+      int src = dim == 1 ? s + D->Nr*k : j + D->Nr*s;
+      int jk = j + D->Nr*k;
+      for(int i = 0; i < D->Np[jk]; i++) {
+         pcell *c = &D->ring[jk][i];
+         const pcell *o = &D->ring[src][i];
+         memcpy(c->prim, o->prim, sizeof c->prim);
+         memcpy(c->cons, o->cons, sizeof c->cons);
+         memcpy(c->RKcons, o->RKcons, sizeof c->RKcons);
+         memcpy(c->Phi, o->Phi, sizeof c->Phi);
+         memcpy(c->RK_Phi, o->RK_Phi, sizeof c->RK_Phi);
+         c->piph = o->piph;
+         c->dphi = o->dphi;
+         c->wiph = o->wiph;
+      }
+   }
+}
+
+/* onestep.c:166-172: exchangeData(r); boundary_trans(r) unless R_Periodic;
+ * exchangeData(z); boundary_trans(z) unless Z_Periodic */
 static void boundary(void)
 {
    disco_bc_op ops[DISCO_BC_MAX_OPS];
    int n = disco_bc_plugin_ops(D->mod.boundary, ops);
+   exchange(1);
    if(n > 0) {   /* the plugin's primitives in call order: r sides, then z sides */
+      int zdone = 0;
       for(int o = 0; o < n; o++) {
          int dim = ops[o].side < 2 ? 1 : 2;
+         if(dim == 2 && !zdone) { exchange(2); zdone = 1; }
          if((dim == 1 && D->Nr <= 1) || (dim == 2 && D->Nz <= 1)) continue;
+         if(periodic_dim(dim)) continue;
          if(ops[o].op >= DISCO_BCOP_ZEROGRAD) copy_side(&ops[o]);
          else init_side(&ops[o]);
       }
+      if(!zdone) exchange(2);
       return;
    }
    for(int k = 0; k < D->Nz; k++) for(int j = 0; j < D->Nr; j++) {
       int rg = j < D->NgRa || j >= D->Nr - D->NgRb;
       int zg = k < D->NgZa || k >= D->Nz - D->NgZb;
+      if(periodic_dim(1)) rg = 0;
+      if(periodic_dim(2)) zg = 0;
       int jk = j + D->Nr*k;
       for(int i = 0; i < D->Np[jk]; i++) {
          pcell *c = &D->ring[jk][i];
@@ -1670,6 +1716,7 @@ static void boundary(void)
          initial(c->prim, x);
       }
    }
+   exchange(2);
 }
 /* rotframe.c:32-80 (cylindrical: the rpz / orthonormal conversions reduce
  * to the scale factor r on the phi component) */
