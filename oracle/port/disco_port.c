@@ -2001,7 +2001,7 @@ port_domain *disco_port_create(const disco_host_domain *h)
       free(d);
       return NULL;
    }
-   if(h->mod.hydro == DISCO_HYDRO_GRMHD || (d->mhd && h->mod.boundary > DISCO_BC_FIXED3D) ||
+   if(h->mod.hydro == DISCO_HYDRO_GRMHD ||
       (h->mod.analysis == DISCO_DIAG_MHDMRI && !d->mhd) || h->mod.analysis > DISCO_DIAG_MHDMRI) {
       free(d); return NULL;
    }

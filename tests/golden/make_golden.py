@@ -96,6 +96,11 @@ CASES = {
     "cfg3_sink_exp": ("configs/cfg3_planet_disk",
                       {"Num_R": 24, "Sink_Type": 2, "Sink_Number": 0, "Sink_Par1": 0.2, "Sink_Par2": 0.0,
                        "Sink_Par3": 0.1, "Sink_Par4": 2.0, "Sink_Par5": 1.0}, 10),
+    # the MHD disk (HLLD + CT) with zero-gradient and outflow ghosts: the
+    # boundary primitives copy the ghost rings' primitives, B included, and
+    # leave the CT face fluxes to the CT update, as with fixed ghosts
+    "cfg2_outflow": ("configs/cfg2_mhd_disk", {"Num_R": 12, "Num_Z": 6}, 5, {"BOUNDARY": "outflow3d"}),
+    "cfg2_zerograd": ("configs/cfg2_mhd_disk", {"Num_R": 12, "Num_Z": 6}, 5, {"BOUNDARY": "zerograd"}),
     "cfg3_nozzle": ("configs/cfg3_planet_disk",
                     {"Num_R": 24, "Nozzle_Type": 1, "Nozzle_Par1": 1.5, "Nozzle_Par2": 0.5,
                      "Nozzle_Par3": 0.8, "Nozzle_Par4": 20.0}, 10),

@@ -27,6 +27,8 @@ CASES = {"cfg1_n24": "configs/cfg1_vortex", "cfg2_n12": "configs/cfg2_mhd_disk",
          "cfg4t_body": "configs/cfg4_grmhd_torus",
          "cfg4t_n24": "configs/cfg4_grmhd_torus",
          "cfg1_zerograd": "configs/cfg1_vortex_zerograd",
+         # the MHD disk with zero-gradient and outflow ghosts (module text in the fixture)
+         "cfg2_outflow": "configs/cfg2_mhd_disk", "cfg2_zerograd": "configs/cfg2_mhd_disk",
          "cfg3_outflow": "configs/cfg3_planet_disk_outflow",
          # the other ghost-ring plugins on the 3D vortex (module text in the fixture)
          **{f"bc_{b}": "configs/cfg1_vortex_zerograd"

@@ -31,8 +31,11 @@ def test_periodic_ghosts_match_restatement(name, precision):
     d, o = _pair(name, precision)
     n = 6
     for _ in range(n):
-        d.timestep(d.getmindt())
-    o.run(n)
+        if precision == 0:   # the device's own dt
+            d.timestep(d.getmindt())
+            o.step()
+        else:                # the mixed path takes the restatement's dt: one clock
+            d.timestep(o.step())
     s, so = d.state(), o.state()
     h = d.host
     real = h.real_mask()

@@ -99,14 +99,13 @@ def test_port_bit_exact_vs_reference_binary():
     shutil.rmtree(td)
 
 
-@pytest.mark.parametrize("name", ["cfg2_n12", "cfg2_rk3"])
+@pytest.mark.parametrize("name", ["cfg2_n12", "cfg2_rk3", "cfg2_outflow", "cfg2_zerograd"])
 def test_port_mhd_ct_bit_exact_vs_golden(name):
-    """3D MHD disk with HLLD and constrained transport (RK2 and RK3): the
-    oracle equals the reference bit for bit (conserved variables, face
-    fluxes, positions)."""
+    """3D MHD disk with HLLD and constrained transport (RK2 and RK3, fixed,
+    outflow and zero-gradient ghosts): the oracle equals the reference bit
+    for bit (conserved variables, face fluxes, positions)."""
     g = load_golden(name)
-    h, s = _port_run(write_par(g["par_text"]), os.path.join(ROOT, "configs/cfg2_mhd_disk/Makefile_opt.in"),
-                     int(g["nsteps"]))
+    h, s = _port_run(write_par(g["par_text"]), mk_path(g), int(g["nsteps"]))
     real = g["real"].astype(bool)
     assert s["t"] == float(g["run_t"])
     assert np.array_equal(s["piph"], g["run_piph"])
