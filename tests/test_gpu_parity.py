@@ -295,14 +295,15 @@ def test_mhd_disk_vs_oracle_port():
     d.close()
 
 
-def test_zerograd_rejected_for_mhd(tmp_path):
-    """Zero-gradient ghosts are built for the hydro module only: an MHD
-    configuration asking for them is refused at create."""
+def test_zerograd_rejected_for_grmhd(tmp_path):
+    """Zero-gradient ghosts are built for the Newtonian modules (hydro and
+    MHD, against reference fixtures): a GRMHD configuration asking for them
+    is refused at create."""
     import disco_gb300 as dg
-    cfg = os.path.join(ROOT, "configs/cfg2_mhd_disk")
+    cfg = os.path.join(ROOT, "configs/cfg4_grmhd_disk")
     src = open(os.path.join(cfg, "Makefile_opt.in")).read()
     mk = tmp_path / "Makefile_opt.in"
-    mk.write_text(src.replace("fixed3d", "zerograd").replace("BOUNDARY = fixed\n", "BOUNDARY = zerograd\n"))
+    mk.write_text(src.replace("fixed3d", "zerograd"))
     assert "zerograd" in mk.read_text()
-    with pytest.raises(dg.DiscoError, match="hydro module only"):
-        dg.Domain(os.path.join(cfg, "in.par"), str(mk))
+    with pytest.raises(dg.DiscoError, match="Newtonian modules"):
+        dg.Domain(os.path.join(cfg, "in.par"), str(mk), overrides={"Num_R": 12, "Num_Z": 4})
