@@ -868,7 +868,8 @@ def main():
     bz = nq * (6 * sw + 4 * 8) + 6 * 8 + (200 if ct else 0)
     whole = {"algorithmic_bytes_per_zone_update": bz, "achieved_GBps": bz * value / 1e9,
              "frac_of_hbm": bz * value / 1e9 / hbm}
-    roof = {"bound": "hbm", "kernel": KERNEL_SYMBOL.get(top_name, top_name), "achieved": achieved,
+    symbols = KERNEL_SYMBOL
+    roof = {"bound": "hbm", "kernel": symbols.get(top_name, top_name), "achieved": achieved,
             "peak": hbm, "unit": "GB/s", "frac": achieved / hbm, "peak_kind": peak_kind,
             "traffic": traffic, "traffic_source": traffic_src,
             "algorithmic_bytes_per_launch": top_bytes, "launches_per_step": top["launches"] / 3,
@@ -888,7 +889,7 @@ def main():
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "roofline": roof,
         "step_hbm": whole,
-        "kernels": {KERNEL_SYMBOL.get(f, f): {"ms_per_step": e["ms"] / 3, "launches_per_step": e["launches"] / 3,
+        "kernels": {symbols.get(f, f): {"ms_per_step": e["ms"] / 3, "launches_per_step": e["launches"] / 3,
                                               "GBps": e["bytes"] / (e["ms"] / 1e3) / 1e9 if e["ms"] > 0 else None}
                     for f, e in sorted(funcs.items(), key=lambda kv: -kv[1]["ms"])},
         "e2e": res["e2e"],

@@ -1327,32 +1327,30 @@ __global__ void __launch_bounds__(256, kMix<R> ? 4 : 1) k_flux_phi(DevParams P, 
 
 // ---- r/z fluxes, misc.c:441-519 + riemann_trans, riemann.c:114-214 ----------
 // Grid: x = pair within the active range, y = chunk of 256 faces.
-template <typename Phys, typename R, int NQ>
-DISCO_D void k_flux_trans_body(const DevParams& P, const DevState<R>& S, int dim, int jmin, int jcount, int kmin, double fac, int bx_, int by_) {
+// One face of the r / z flux sweep (misc.c:441-519, riemann.c:114-214):
+// reconstruction at the face from the two cells' primitives and gradients,
+// the Riemann solve, the fluxes times dA dt, and the CT face terms.  ld(s, q,
+// &p, &gp, &gd) gives cell s's (0: L, 1: R) component q: primitive, phi
+// gradient and gradient across the face.
+template <typename Phys, typename R, int NQ, typename Load>
+DISCO_D void flux_trans_face(const DevParams& P, const DevState<R>& S, int dim, int pair, int pj, int pk, int f,
+                             int cL, int cR, double fac, Load&& ld) {
   const int d = dim - 1;
-  int pj = jmin + (int)bx_ % jcount;
-  int pk = kmin + (int)bx_ / jcount;
-  int pair = dim == 1 ? pj + (P.Nr - 1) * pk : pj + P.Nr * pk;
-  int base = S.face_off[d][pair], Nf = S.face_off[d][pair + 1] - base;
-  int n = by_ * blockDim.x + threadIdx.x;
-  if (n >= Nf) return;
-  int f = base + n;
   const int N = S.N;
-  int cL = S.fL[d][f], cR = S.fR[d][f];
   // the face angle enters the Riemann solver through the viscous flux only
   R phi = P.include_viscosity ? (R)S.fphic[d][f] : (R)0;
   R dpL = S.fdpL[d][f], dpR = S.fdpR[d][f];
   R rdxL = S.pdxL[d][pair], rdxR = S.pdxR[d][pair];
   R ridxs = kMix<R> ? S.pidxs[d][pair] : (R)0;
-  const R* gradL = (dim == 1 ? S.gradr : S.gradz);
   R primL[NQ], primR[NQ], grad[NQ];
   R gLp[NQ], gRp[NQ], gLo[NQ], gRo[NQ];
 #pragma unroll
   for (int q = 0; q < NQ; ++q) {
-    R pL = S.prim[q * N + cL], pR = S.prim[q * N + cR];
-    R gpL = S.gradp[q * N + cL], gpR = S.gradp[q * N + cR];
-    primL[q] = pL + gradL[q * N + cL] * rdxL + gpL * dpL;
-    primR[q] = pR - gradL[q * N + cR] * rdxR - gpR * dpR;
+    R pL, gpL, gdL, pR, gpR, gdR;
+    ld(0, q, &pL, &gpL, &gdL);
+    ld(1, q, &pR, &gpR, &gdR);
+    primL[q] = pL + gdL * rdxL + gpL * dpL;
+    primR[q] = pR - gdR * rdxR - gpR * dpR;
     if constexpr (kMix<R>) grad[q] = ((pR - gpR * dpR) - (pL + gpL * dpL)) * ridxs;
     else grad[q] = ((pR - gpR * dpR) - (pL + gpL * dpL)) / (rdxL + rdxR);
     gLp[q] = gpL; gRp[q] = gpR;
@@ -1411,6 +1409,28 @@ DISCO_D void k_flux_trans_body(const DevParams& P, const DevState<R>& S, int dim
     S.fErz[d][f] = E1; S.fBrz[d][f] = B1; S.fEphi[d][f] = E2;
   }
 }
+
+template <typename Phys, typename R, int NQ>
+DISCO_D void k_flux_trans_body(const DevParams& P, const DevState<R>& S, int dim, int jmin, int jcount, int kmin, double fac, int bx_, int by_) {
+  const int d = dim - 1;
+  int pj = jmin + (int)bx_ % jcount;
+  int pk = kmin + (int)bx_ / jcount;
+  int pair = dim == 1 ? pj + (P.Nr - 1) * pk : pj + P.Nr * pk;
+  int base = S.face_off[d][pair], Nf = S.face_off[d][pair + 1] - base;
+  int n = by_ * blockDim.x + threadIdx.x;
+  if (n >= Nf) return;
+  int f = base + n;
+  const int N = S.N;
+  const int cL = S.fL[d][f], cR = S.fR[d][f];
+  const R* gradD = dim == 1 ? S.gradr : S.gradz;
+  flux_trans_face<Phys, R, NQ>(P, S, dim, pair, pj, pk, f, cL, cR, fac, [&](int s, int q, R* p, R* gp, R* gd) {
+    const int c = s ? cR : cL;
+    *p = S.prim[q * N + c];
+    *gp = S.gradp[q * N + c];
+    *gd = gradD[q * N + c];
+  });
+}
+
 template <typename Phys, typename R, int NQ>
 __global__ void __launch_bounds__(256, kMix<R> ? 4 : 1) k_flux_trans(DevParams P, DevState<R> S, int dim, int jmin, int jcount, int kmin, double fac) {
   k_flux_trans_body<Phys, R, NQ>(P, S, dim, jmin, jcount, kmin, fac, (int)blockIdx.x, (int)blockIdx.y);
