@@ -336,10 +336,6 @@ struct Instance : InstanceBase {
       disco_set_error("BOUNDARY plugin not built");
       return DISCO_E_MODULE;
     }
-    if (n_bc_ops > 0 && Phys::GR) {
-      disco_set_error("boundary plugins other than fixed / fixed3d are built for the Newtonian modules");
-      return DISCO_E_MODULE;
-    }
     for (int o = 0; o < n_bc_ops; ++o) {   // the source rings of the copies must be real rings
       const int dim = bc_ops[o].side < 2 ? 1 : 2, side = bc_ops[o].side & 1;
       const int ng = dim == 1 ? (side ? dom->NgRb : dom->NgRa) : (side ? dom->NgZb : dom->NgZa);

@@ -101,6 +101,9 @@ CASES = {
     # leave the CT face fluxes to the CT update, as with fixed ghosts
     "cfg2_outflow": ("configs/cfg2_mhd_disk", {"Num_R": 12, "Num_Z": 6}, 5, {"BOUNDARY": "outflow3d"}),
     "cfg2_zerograd": ("configs/cfg2_mhd_disk", {"Num_R": 12, "Num_Z": 6}, 5, {"BOUNDARY": "zerograd"}),
+    # the GRMHD disk with outflow and zero-gradient ghosts
+    "cfg4_outflow": ("configs/cfg4_grmhd_disk", {"Num_R": 12, "Num_Z": 4}, 5, {"BOUNDARY": "outflow3d"}),
+    "cfg4_zerograd": ("configs/cfg4_grmhd_disk", {"Num_R": 12, "Num_Z": 4}, 5, {"BOUNDARY": "zerograd"}),
     "cfg3_nozzle": ("configs/cfg3_planet_disk",
                     {"Num_R": 24, "Nozzle_Type": 1, "Nozzle_Par1": 1.5, "Nozzle_Par2": 0.5,
                      "Nozzle_Par3": 0.8, "Nozzle_Par4": 20.0}, 10),

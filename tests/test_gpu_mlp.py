@@ -127,7 +127,10 @@ def test_training_reduces_loss_and_guess_keeps_the_solution():
             den = np.abs(pa[q, real]).sum()
             if den > 0:
                 assert np.abs(pb[q, real] - pa[q, real]).sum() <= 1e-13 * den, (f, q)
-        assert a.status()["c2p_no_converge"] == b.status()["c2p_no_converge"]
+        # a learned start may converge where the previous primitives stop at
+        # the iteration cap (the atmosphere at the density floor), never the
+        # other way round: a start that does not converge falls back
+        assert b.status()["c2p_no_converge"] <= a.status()["c2p_no_converge"]
     assert bs[0].c2p_stats()["guessed"] > 0
     assert min(kbs) <= 1.05 * ka
     a.close(); m.close()

@@ -29,13 +29,14 @@ CASES = {"cfg1_n24": "configs/cfg1_vortex", "cfg2_n12": "configs/cfg2_mhd_disk",
          "cfg1_zerograd": "configs/cfg1_vortex_zerograd",
          # the MHD disk with zero-gradient and outflow ghosts (module text in the fixture)
          "cfg2_outflow": "configs/cfg2_mhd_disk", "cfg2_zerograd": "configs/cfg2_mhd_disk",
+         "cfg4_outflow": "configs/cfg4_grmhd_disk", "cfg4_zerograd": "configs/cfg4_grmhd_disk",
          "cfg3_outflow": "configs/cfg3_planet_disk_outflow",
          # the other ghost-ring plugins on the 3D vortex (module text in the fixture)
          **{f"bc_{b}": "configs/cfg1_vortex_zerograd"
             for b in ("zerograd_omk", "zerograd_omIN", "accrete3d", "fixRrefZ", "polar3d", "fixed_gap",
                       "tube", "surfaceGravBox", "flowthrough")}}
 # GRMHD runs on the FP64 path only
-FP64_ONLY = {"cfg4_n12", "cfg4_diag", "cfg4t_body", "cfg4t_n24"}
+FP64_ONLY = {"cfg4_n12", "cfg4_diag", "cfg4t_body", "cfg4t_n24", "cfg4_outflow", "cfg4_zerograd"}
 
 
 def _domain(name, precision=0):
@@ -295,15 +296,11 @@ def test_mhd_disk_vs_oracle_port():
     d.close()
 
 
-def test_zerograd_rejected_for_grmhd(tmp_path):
-    """Zero-gradient ghosts are built for the Newtonian modules (hydro and
-    MHD, against reference fixtures): a GRMHD configuration asking for them
-    is refused at create."""
+def test_cooling_rejected_for_grmhd():
+    """Cooling, damping and sinks are built for the Newtonian modules: a
+    GRMHD configuration asking for them is refused at create."""
     import disco_gb300 as dg
     cfg = os.path.join(ROOT, "configs/cfg4_grmhd_disk")
-    src = open(os.path.join(cfg, "Makefile_opt.in")).read()
-    mk = tmp_path / "Makefile_opt.in"
-    mk.write_text(src.replace("fixed3d", "zerograd"))
-    assert "zerograd" in mk.read_text()
     with pytest.raises(dg.DiscoError, match="Newtonian modules"):
-        dg.Domain(os.path.join(cfg, "in.par"), str(mk), overrides={"Num_R": 12, "Num_Z": 4})
+        dg.Domain(os.path.join(cfg, "in.par"), os.path.join(cfg, "Makefile_opt.in"),
+                  overrides={"Num_R": 12, "Num_Z": 4, "coolType": 1, "coolPar1": 1.0})
