@@ -10,8 +10,18 @@
 #include "mlp_train.cuh"
 
 #include <cmath>
+#include <nvtx3/nvToolsExt.h>
 
 std::atomic<long long> g_launches{0};
+
+// A named NVTX range over one C-ABI call (header-only NVTX3: a no-op unless
+// a profiler is attached), so that a timeline shows the host's calls --
+// getmindt, timestep, run, the batch's steps, training -- around the
+// kernels they launch.
+struct NvtxRange {
+  explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+  ~NvtxRange() { nvtxRangePop(); }
+};
 long long disco_gpu_launch_count(void) { return g_launches.load(); }
 
 namespace disco_impl {
@@ -408,6 +418,7 @@ int disco_mlp_train(disco_mlp* m, int steps, int batch, float lr, unsigned long 
                     float* loss_last) {
   if (!m || steps < 0 || batch < 16 || !(lr > 0.f)) { disco_set_error("disco_mlp_train: bad argument"); return DISCO_E_ARG; }
   if (m->held < 1) { disco_set_error("disco_mlp_train: no training pairs held"); return DISCO_E_STATE; }
+  NvtxRange r("disco_mlp_train");
   const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
   for (int k = 0; k < steps; ++k) {
     const unsigned long long sd = seed + (unsigned long long)m->step * (unsigned long long)batch;
@@ -577,15 +588,18 @@ int disco_gpu_diag_upload(disco_gpu* g, const double* Qrz, long long len, double
 
 int disco_gpu_getmindt(disco_gpu* g, double* dt) {
   if (!g || !dt) { disco_set_error("null argument"); return DISCO_E_ARG; }
+  NvtxRange r("disco_gpu_getmindt");
   return g->impl->getmindt(dt);
 }
 int disco_gpu_timestep(disco_gpu* g, double dt) {
   if (!g) { disco_set_error("null argument"); return DISCO_E_ARG; }
   if (!(dt > 0.0)) { disco_set_error("timestep: dt must be positive"); return DISCO_E_ARG; }
+  NvtxRange r("disco_gpu_timestep");
   return g->impl->timestep(dt);
 }
 int disco_gpu_run(disco_gpu* g, int nsteps, double t_end) {
   if (!g || nsteps < 0) { disco_set_error("bad argument"); return DISCO_E_ARG; }
+  NvtxRange r("disco_gpu_run");
   return g->impl->run(nsteps, t_end);
 }
 int disco_gpu_download(disco_gpu* g, disco_state_view* v) {
@@ -725,6 +739,7 @@ int disco_batch_create_flags(disco_gpu* const* members, int n, int flags, disco_
 }
 int disco_batch_run(disco_batch* b, int nsteps) {
   if (!b || nsteps < 0) { disco_set_error("bad argument"); return DISCO_E_ARG; }
+  NvtxRange r("disco_batch_run");
   return batch_steps(b, nsteps, 0, nullptr);
 }
 int disco_batch_run_timed(disco_batch* b, int nsteps, size_t flush_bytes, double* ms) {
