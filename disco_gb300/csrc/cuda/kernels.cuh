@@ -785,13 +785,20 @@ DISCO_D void k_plm_slopes_body(const DevParams& P, const DevState<R>& S, int dim
     int f = base + n;
     int cL = S.fL[d][f], cR = S.fR[d][f];
     R dpL = S.fdpL[d][f], dpR = S.fdpR[d][f];
+    // every component's reconstructed pair before the first store: the
+    // stores may alias the inputs as far as the compiler knows, so loads
+    // placed after one would wait for it
+    R WL[NQ], WR[NQ];
 #pragma unroll
     for (int q = 0; q < NQ; ++q) {
-      R WL = S.prim[q * N + cL] + dpL * S.gradp[q * N + cL];
-      R WR = S.prim[q * N + cR] - dpR * S.gradp[q * N + cR];
+      WL[q] = S.prim[q * N + cL] + dpL * S.gradp[q * N + cL];
+      WR[q] = S.prim[q * N + cR] - dpR * S.gradp[q * N + cR];
+    }
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) {
       R Sl;
-      if constexpr (kMix<R>) Sl = ((WR - WL) + (q == UPP ? dOm : (R)0)) * idxs;   // frames of the rings
-      else Sl = (WR - WL) / dxs;
+      if constexpr (kMix<R>) Sl = ((WR[q] - WL[q]) + (q == UPP ? dOm : (R)0)) * idxs;   // frames of the rings
+      else Sl = (WR[q] - WL[q]) / dxs;
       S.fslope[(size_t)q * NF + f] = Sl;
     }
   }
