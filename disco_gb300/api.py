@@ -63,6 +63,11 @@ class DiscoParams(C.Structure):
         ("sinkPar1", C.c_double), ("sinkPar2", C.c_double), ("sinkPar4", C.c_double), ("sinkPar5", C.c_double),
         ("nozzlePar1", C.c_double), ("nozzlePar2", C.c_double), ("nozzlePar3", C.c_double),
         ("nozzlePar4", C.c_double),
+        ("NumRepts", C.c_int), ("NumSnaps", C.c_int), ("NumChecks", C.c_int),
+        ("Out_LogTime", C.c_int), ("Initial_Regrid", C.c_int), ("restart_flag", C.c_int),
+        ("include_atmos", C.c_int),
+        ("MaxShort", C.c_double), ("MaxLong", C.c_double), ("Eccentricity", C.c_double),
+        ("Drift_Rate", C.c_double), ("Drift_Exp", C.c_double),
     ]
 
 
@@ -75,6 +80,8 @@ class DiscoModules(C.Structure):
         ("metric", C.c_int), ("frame", C.c_int),
         ("metric_name", C.c_char * 64), ("frame_name", C.c_char * 64),
         ("analysis", C.c_int), ("analysis_name", C.c_char * 64),
+        ("geometry_name", C.c_char * 64), ("output_name", C.c_char * 64),
+        ("restart_name", C.c_char * 64), ("hlld_name", C.c_char * 64),
     ]
 
 
@@ -99,6 +106,7 @@ class DiscoHostDomain(C.Structure):
         ("Npl", C.c_int),
         ("planets", DiscoPlanet * 4),
         ("ic_aux", C.c_double * 4),
+        ("Phi", C.POINTER(C.c_double)),
     ]
 
 
@@ -128,6 +136,10 @@ SIGNATURES = {
     "disco_host_setup": (C.c_int, [C.POINTER(DiscoParams), C.POINTER(DiscoModules),
                                    C.POINTER(C.POINTER(DiscoHostDomain))]),
     "disco_host_free": (None, [C.POINTER(DiscoHostDomain)]),
+    "disco_host_restart": (C.c_int, [C.POINTER(DiscoParams), C.POINTER(DiscoModules), C.c_char_p,
+                                     C.POINTER(C.POINTER(DiscoHostDomain))]),
+    "disco_host_checkpoint": (C.c_int, [C.POINTER(DiscoHostDomain), C.c_char_p]),
+    "disco_gpu_checkpoint": (C.c_int, [_P, C.POINTER(DiscoHostDomain), C.c_char_p]),
     "disco_gpu_create": (C.c_int, [C.POINTER(DiscoHostDomain), C.c_int, C.POINTER(_P)]),
     "disco_gpu_getmindt": (C.c_int, [_P, C.POINTER(C.c_double)]),
     "disco_gpu_timestep": (C.c_int, [_P, C.c_double]),
@@ -233,12 +245,17 @@ def read_modules(makefile_opt: str) -> DiscoModules:
 
 
 class HostDomain:
-    """Host-side grid + initial state (disco_host_setup), no GPU needed."""
+    """Host-side grid + initial state (disco_host_setup), no GPU needed; with
+    `restart` the grid and state of that checkpoint file (disco_host_restart)."""
 
-    def __init__(self, params: DiscoParams, modules: DiscoModules):
+    def __init__(self, params: DiscoParams, modules: DiscoModules, restart: str | None = None):
         ptr = C.POINTER(DiscoHostDomain)()
-        _check(lib().disco_host_setup(C.byref(params), C.byref(modules), C.byref(ptr)),
-               "disco_host_setup")
+        if restart is None:
+            _check(lib().disco_host_setup(C.byref(params), C.byref(modules), C.byref(ptr)),
+                   "disco_host_setup")
+        else:
+            _check(lib().disco_host_restart(C.byref(params), C.byref(modules), restart.encode(),
+                                            C.byref(ptr)), "disco_host_restart")
         self._ptr = ptr
         d = ptr.contents
         self.Nr, self.Nz = d.Nr, d.Nz
@@ -255,6 +272,16 @@ class HostDomain:
         self.piph = np.ctypeslib.as_array(d.piph, (n,)).copy()
         self.dphi = np.ctypeslib.as_array(d.dphi, (n,)).copy()
         self.prim = np.ctypeslib.as_array(d.prim, (self.num_q * n,)).copy().reshape(self.num_q, n)
+        self.num_faces = d.num_faces
+        self.Phi = (np.ctypeslib.as_array(d.Phi, (self.num_faces * n,)).copy().reshape(self.num_faces, n)
+                    if d.Phi else None)
+        self.Npl = d.Npl
+        self.planets = [{k: getattr(d.planets[i], k) for k, _ in DiscoPlanet._fields_} for i in range(d.Npl)]
+        self.params = d.par
+
+    def checkpoint(self, path: str) -> None:
+        """The checkpoint file of this host state (disco_host_checkpoint)."""
+        _check(lib().disco_host_checkpoint(self._ptr, path.encode()), "disco_host_checkpoint")
 
     def real_mask(self) -> np.ndarray:
         jk = np.repeat(np.arange(self.Nr * self.Nz), self.Np)
@@ -272,12 +299,12 @@ class Domain:
     """A domain resident on the GPU: the reference's getmindt/timestep pair."""
 
     def __init__(self, in_par: str, makefile_opt: str, precision: int = 0,
-                 overrides: dict | None = None):
+                 overrides: dict | None = None, restart: str | None = None):
         self.params = read_params(in_par)
         for k, v in (overrides or {}).items():
             setattr(self.params, k, v)
         self.modules = read_modules(makefile_opt)
-        self.host = HostDomain(self.params, self.modules)
+        self.host = HostDomain(self.params, self.modules, restart=restart)
         g = C.c_void_p()
         _check(lib().disco_gpu_create(self.host._ptr, int(precision), C.byref(g)), "disco_gpu_create")
         self._g = g
@@ -431,6 +458,12 @@ class Domain:
     @property
     def num_real_cells(self) -> int:
         return lib().disco_gpu_num_real_cells(self._g)
+
+    def checkpoint(self, path: str) -> None:
+        """Write the checkpoint file of the device state (disco_gpu_checkpoint):
+        the layout of the reference's h5out.c output(); the ring diagnostics
+        are averaged into the file and zeroed, as output() does."""
+        _check(lib().disco_gpu_checkpoint(self._g, self.host._ptr, path.encode()), "disco_gpu_checkpoint")
 
     def state(self, out: dict | None = None) -> dict:
         """Download the state.  `out` may hold preallocated C-contiguous

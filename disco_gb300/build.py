@@ -25,7 +25,7 @@ NVCC_FLAGS = ["-std=c++17", "-O3", GENCODE, "-lineinfo", "-Xcompiler", "-fPIC",
               "--expt-relaxed-constexpr"]
 CC_FLAGS = ["-std=gnu11", "-O2", "-fPIC", "-Wall", "-ffp-contract=off"]
 
-HOST_SOURCES = ["host/disco_host.c"]
+HOST_SOURCES = ["host/disco_host.c", "host/h5lite.c", "host/checkpoint.c"]
 # (source, extra nvcc flags): the plain-FP64 instances are compiled without
 # FMA contraction so their FP64 arithmetic rounds like the reference's C build.
 # FP64 path: no FMA contraction (it must round like the reference build).

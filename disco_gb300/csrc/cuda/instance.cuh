@@ -613,12 +613,18 @@ struct Instance : InstanceBase {
     double* d_prim0;
     CK(cudaMalloc(&d_prim0, sizeof(double) * NQ * N));
     CK(cudaMemcpy(d_prim0, dom->prim, sizeof(double) * NQ * N, cudaMemcpyHostToDevice));
-    k_init_cells<Phys, R, NQ><<<blocks(N), 256, 0, st>>>(P, S, d_prim0, ct ? 0 : 1);
+    // a restarted domain carries its face fluxes: setupCells then skips
+    // set_B_fields and runs prim2cons + cons2prim on the file's primitives
+    // (domain.c:211-238)
+    const bool phi_in = ct && dom->Phi && dom->num_faces == 5;
+    k_init_cells<Phys, R, NQ><<<blocks(N), 256, 0, st>>>(P, S, d_prim0, (ct && !phi_in) ? 0 : 1);
     ++g_launches;
     CK(cudaGetLastError());
     CK(cudaStreamSynchronize(st));
     cudaFree(d_prim0);
-    if (ct) {   // set_B_fields (bfields.c:13-86), then cons2prim (domain.c:365-382)
+    if (phi_in) {
+      CK(cudaMemcpy(C.Phi, dom->Phi, sizeof(double) * 5 * N, cudaMemcpyHostToDevice));
+    } else if (ct) {   // set_B_fields (bfields.c:13-86), then cons2prim (domain.c:365-382)
       launch_faces();
       LAUNCH("ct_init", (k_ct_init_phi0<R><<<blocks(N), 256, 0, st>>>(P, S, C)));
       for (int d = 0; d < 2; ++d)

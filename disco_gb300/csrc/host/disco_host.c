@@ -172,6 +172,10 @@ int disco_params_read(const char *path, disco_params *p)
    RD("Sink_Par4", sinkPar4); RD("Sink_Par5", sinkPar5);
    RD("Nozzle_Par1", nozzlePar1); RD("Nozzle_Par2", nozzlePar2);
    RD("Nozzle_Par3", nozzlePar3); RD("Nozzle_Par4", nozzlePar4);
+   RI("Num_Reports", NumRepts); RI("Num_Snapshots", NumSnaps); RI("Num_Checkpoints", NumChecks);
+   RI("Use_Logtime", Out_LogTime); RD("Max_Aspect_Short", MaxShort); RD("Max_Aspect_Long", MaxLong);
+   RI("Initial_Regrid", Initial_Regrid); RI("Restart", restart_flag); RI("Include_Atmos", include_atmos);
+   RD("Eccentricity", Eccentricity); RD("Drift_Rate", Drift_Rate); RD("Drift_Exp", Drift_Exp);
    /* not a reference key: an upper bound on cells per ring (0 = none) */
    { int e0 = err; RI("Max_Np", maxNp); err = e0; }
 #undef RI
@@ -236,6 +240,10 @@ int disco_modules_read(const char *path, disco_modules *m)
    if(mk_value(b, "METRIC", m->metric_name, sizeof m->metric_name)) m->metric_name[0] = 0;
    if(mk_value(b, "FRAME", m->frame_name, sizeof m->frame_name)) m->frame_name[0] = 0;
    if(mk_value(b, "ANALYSIS", m->analysis_name, sizeof m->analysis_name)) m->analysis_name[0] = 0;
+   if(mk_value(b, "GEOMETRY", m->geometry_name, sizeof m->geometry_name)) m->geometry_name[0] = 0;
+   if(mk_value(b, "OUTPUT", m->output_name, sizeof m->output_name)) m->output_name[0] = 0;
+   if(mk_value(b, "RESTART", m->restart_name, sizeof m->restart_name)) m->restart_name[0] = 0;
+   if(mk_value(b, "HLLD", m->hlld_name, sizeof m->hlld_name)) m->hlld_name[0] = 0;
    if(!mk_value(b, "GEOMETRY", v, sizeof v) && strcmp(v, "cylindrical") != 0) {
       free(b);
       disco_set_error("GEOMETRY: only cylindrical is built");
@@ -431,10 +439,14 @@ static void add_noise(const disco_params *p, disco_rand_state *rs, double *prim,
    }
 }
 
-int disco_host_setup(const disco_params *par, const disco_modules *mod,
-                     disco_host_domain **out)
+/* The grid of main.c:34-47 up to the ring phases: gridsetup.c (r_jph,
+ * z_kph, Np), setupDomain's phases from rand() after srand(314159)
+ * (domain.c:172-233), the planets, and calc_dp.  *rs is left where the
+ * reference's rand() stream stands when setupCells begins. */
+int disco_host_grid(const disco_params *par, const disco_modules *mod,
+                    disco_host_domain **out, disco_rand_state *rs_out)
 {
-   if(!par || !mod || !out) { disco_set_error("disco_host_setup: null argument"); return DISCO_E_ARG; }
+   if(!par || !mod || !out || !rs_out) { disco_set_error("disco_host_setup: null argument"); return DISCO_E_ARG; }
    if(par->Num_R < 1 || par->Num_Z < 1 || par->aspect <= 0.0 || par->phimax <= 0.0) {
       disco_set_error("disco_host_setup: Num_R, Num_Z, aspect, Phi_Max must be positive");
       return DISCO_E_ARG;
@@ -553,8 +565,7 @@ int disco_host_setup(const disco_params *par, const disco_modules *mod,
       d->ic_aux[0] = P.ell; d->ic_aux[1] = P.F_in; d->ic_aux[2] = P.hpk1; d->ic_aux[3] = P.bscale;
    }
 
-   /* setupCells (domain.c:283-353): calc_dp, then initial()+noise on real
-    * cells in (k, j, i) order; prim2cons/cons2prim run on the device. */
+   /* setupCells (domain.c:283-353) begins with calc_dp */
    int jk;
    for(jk = 0; jk < Nr*Nz; jk++) {
       long c0 = d->ring_off[jk];
@@ -564,8 +575,22 @@ int disco_host_setup(const disco_params *par, const disco_modules *mod,
          d->dphi[c0 + i] = get_dp(d->piph[c0 + i], d->piph[c0 + im], Pmax);
       }
    }
+   *rs_out = rs;
+   *out = d;
+   return DISCO_OK;
+}
+
+/* The rest of setupCells (domain.c:319-353) on the real cells in (k, j, i)
+ * order: initial() when from_ic (a restart keeps the primitives it read),
+ * then the noise, drawn from *rs; prim2cons/cons2prim run on the device.
+ * Then the first exchange of a periodic run (main.c:53-61): r ghost rings,
+ * then whole z ghost layers, take their source rings' cells. */
+void disco_host_cells(disco_host_domain *d, disco_rand_state *rs, int from_ic)
+{
+   const disco_params *par = &d->par;
+   const int Nr = d->Nr, Nz = d->Nz, NgRa = d->NgRa, NgRb = d->NgRb, NgZa = d->NgZa, NgZb = d->NgZb;
    long N = d->Ncell;
-   int nq = d->num_q;
+   int nq = d->num_q, j, k;
    for(k = NgZa; k < Nz - NgZb; k++) {
       double z = 0.5*(d->z_kph[k + 1] + d->z_kph[k]);
       for(j = NgRa; j < Nr - NgRb; j++) {
@@ -578,14 +603,13 @@ int disco_host_setup(const disco_params *par, const disco_modules *mod,
             double phi = d->piph[c] - .5*d->dphi[c];
             double x[3] = {r, phi, z};
             double prim[16];
-            ic_eval(d, prim, x);
-            if(par->noiseType != 0) add_noise(par, &rs, prim, x);
+            if(from_ic) ic_eval(d, prim, x);
+            else for(q = 0; q < nq; q++) prim[q] = d->prim[(size_t)q*N + c];
+            if(par->noiseType != 0) add_noise(par, rs, prim, x);
             for(q = 0; q < nq; q++) d->prim[(size_t)q*N + c] = prim[q];
          }
       }
    }
-   /* the first exchange of a periodic run (main.c:53-61): r ghost rings,
-    * then whole z ghost layers, take their source rings' cells */
    for(int dim = 1; dim <= 2; dim++)
       for(k = 0; k < Nz; k++)
          for(j = 0; j < Nr; j++) {
@@ -597,8 +621,20 @@ int disco_host_setup(const disco_params *par, const disco_modules *mod,
                d->piph[c0 + i] = d->piph[s0 + i];
                d->dphi[c0 + i] = d->dphi[s0 + i];
                for(q = 0; q < nq; q++) d->prim[(size_t)q*N + c0 + i] = d->prim[(size_t)q*N + s0 + i];
+               for(q = 0; d->Phi && q < d->num_faces; q++)
+                  d->Phi[(size_t)q*N + c0 + i] = d->Phi[(size_t)q*N + s0 + i];
             }
          }
+}
+
+int disco_host_setup(const disco_params *par, const disco_modules *mod,
+                     disco_host_domain **out)
+{
+   disco_rand_state rs;
+   disco_host_domain *d = NULL;
+   int rc = disco_host_grid(par, mod, &d, &rs);
+   if(rc) return rc;
+   disco_host_cells(d, &rs, 1);
    *out = d;
    return DISCO_OK;
 }
@@ -629,7 +665,7 @@ void disco_host_free(disco_host_domain *d)
 {
    if(!d) return;
    free(d->Np); free(d->ring_off); free(d->r_jph); free(d->z_kph);
-   free(d->piph); free(d->dphi); free(d->prim);
+   free(d->piph); free(d->dphi); free(d->prim); free(d->Phi);
    free(d);
 }
 

@@ -24,6 +24,14 @@ int disco_rand_sequence(unsigned int seed, int n, int *out);
  * dim (1: r, 2: z), or -1 when (j, k) is not a periodic ghost of dim. */
 int disco_periodic_source(const disco_host_domain *d, int dim, int j, int k);
 
+/* The two halves of disco_host_setup: the grid, ring phases and planets
+ * (leaving *rs where setupCells draws its noise), then the real cells'
+ * primitives (initial() when from_ic, else the ones already in d) with the
+ * noise, and the periodic ghosts' first exchange. */
+int disco_host_grid(const disco_params *par, const disco_modules *mod,
+                    disco_host_domain **out, disco_rand_state *rs);
+void disco_host_cells(disco_host_domain *d, disco_rand_state *rs, int from_ic);
+
 #ifdef __cplusplus
 }
 #endif

@@ -16,7 +16,15 @@
  *                                  face fluxes (CT), the point masses and the
  *                                  ring diagnostics into theDomain
  *   gb300_zero_diagnostics()       after the output step's zero_diagnostics
+ *   gb300_output(theDomain, name)  in place of output() (h5out.c:366) when
+ *                                  the build has no HDF5 library: writes
+ *                                  <name>.h5 in output()'s layout from the
+ *                                  device state
  *   gb300_free()                   before freeDomain
+ *
+ * With Restart = 1 in in.par, gb300_init builds the device instance from
+ * input.h5 (the file restart() reads, h5in.c:116) as the library's
+ * checkpoint reader understands it.
  *
  * The build compiles the reference's misc.c and timestep.c with their own
  * definitions renamed out of the way (-Dgetmindt=... for misc.c,
@@ -30,6 +38,7 @@
 #include "paul.h"
 #include "disco_gpu.h"
 #include "disco_gpu_diag.h"
+#include "disco_gpu_checkpoint.h"
 
 #ifndef GB300_PRECISION
 #define GB300_PRECISION 0
@@ -53,7 +62,10 @@ void gb300_init(struct domain *theDomain)
    disco_modules m;
    gb300_check(disco_params_read("in.par", &p), "disco_params_read");
    gb300_check(disco_modules_read("Makefile_opt.in", &m), "disco_modules_read");
-   gb300_check(disco_host_setup(&p, &m, &H), "disco_host_setup");
+   if(p.restart_flag)
+      gb300_check(disco_host_restart(&p, &m, "input.h5", &H), "disco_host_restart");
+   else
+      gb300_check(disco_host_setup(&p, &m, &H), "disco_host_setup");
    if(H->Nr != theDomain->Nr || H->Nz != theDomain->Nz) {
       fprintf(stderr, "gb300: grid differs from the reference's set-up\n");
       exit(1);
@@ -118,6 +130,14 @@ void gb300_sync_to_host(struct domain *theDomain)
       gb300_check(disco_gpu_diag_download(G, theDomain->theTools.Qrz,
                                           (long long)theDomain->Nr*theDomain->Nz*nd,
                                           &theDomain->theTools.t_avg), "disco_gpu_diag_download");
+}
+
+void gb300_output(struct domain *theDomain, const char *filestart)
+{
+   char fname[512];
+   (void)theDomain;
+   snprintf(fname, sizeof fname, "%s.h5", filestart);   /* h5out.c:392 */
+   gb300_check(disco_gpu_checkpoint(G, H, fname), "disco_gpu_checkpoint");
 }
 
 void gb300_zero_diagnostics(void)

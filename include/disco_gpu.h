@@ -85,6 +85,8 @@ typedef struct disco_modules {
    char metric_name[64], frame_name[64];
    int analysis;                 /* ANALYSIS: disco_analysis_id, or -1 when absent */
    char analysis_name[64];
+   /* the remaining names the checkpoint records (h5out.c:98-160); "" when absent */
+   char geometry_name[64], output_name[64], restart_name[64], hlld_name[64];
 } disco_modules;
 
 /* Run-time parameters: the hot-path subset of struct param_list
@@ -129,6 +131,10 @@ typedef struct disco_params {
    int sinkNumber;    /* Sink_Number: sinks on the first n bodies (0: all) */
    double sinkPar1, sinkPar2, sinkPar4, sinkPar5;             /* Sink_Par1,2,4,5 (sink.c:105) */
    double nozzlePar1, nozzlePar2, nozzlePar3, nozzlePar4;     /* Nozzle_Par1..4 (sink.c:105) */
+   /* keys the hot path does not read but the checkpoint records
+    * (readpar.c:73-126, h5out.c:168-366) */
+   int NumRepts, NumSnaps, NumChecks, Out_LogTime, Initial_Regrid, restart_flag, include_atmos;
+   double MaxShort, MaxLong, Eccentricity, Drift_Rate, Drift_Exp;
 } disco_params;
 
 /* One point mass: the fields of struct planet (paul.h:259-284) the hot path
@@ -158,6 +164,9 @@ typedef struct disco_host_domain {
    disco_planet planets[DISCO_MAX_PLANETS];
    double ic_aux[4];      /* constants the initial condition derives once at set-up
                              (fm_torus: ell, F(r_in), h(r_pk) - 1, field scale) */
+   double *Phi;           /* [num_faces*Ncell] face fluxes read from a checkpoint
+                             (disco_host_restart), else NULL: disco_gpu_create then
+                             takes them instead of the initial field's */
 } disco_host_domain;
 
 /* Host->device state snapshot, filled by disco_gpu_download(). Any pointer
