@@ -623,11 +623,16 @@ __global__ void k_ct_flip(DevParams P, DevState<R> S, CtStateT<R> C, int dim) {
   const int n0 = threadIdx.x * chunk, n1 = min(Nf, n0 + chunk);
   unsigned long long bits = 0;   // chunk <= 64 (Nf <= 16384)
   int mine = 0;
+  // the end edge of face n: piph of its L cell (LRtype 0) or of its R cell
+  auto edge = [&](int n) {
+    const int f = base + n;
+    return S.piph[lr[n] == 0 ? S.fL[d][f] : S.fR[d][f]];
+  };
+  double pm = n0 < n1 ? edge(n0) : 0.0;   // carried from face to face: one gather each
+#pragma unroll 4
   for (int n = n0; n < n1; ++n) {
     int np = n + 1 == Nf ? 0 : n + 1;   // face np is flagged when its end edge precedes face n's
-    int f = base + n, fp = base + np;
-    double pm = lr[n] == 0 ? S.piph[S.fL[d][f]] : S.piph[S.fR[d][f]];
-    double pp = lr[np] == 0 ? S.piph[S.fL[d][fp]] : S.piph[S.fR[d][fp]];
+    const double pp = edge(np);
     bool flip;
     if constexpr (kMix<R>) {   // the same test with the wrap on bit patterns
       double dp = get_signed_dp_bits(pp, pm, P.phi_max);
@@ -637,6 +642,7 @@ __global__ void k_ct_flip(DevParams P, DevState<R> S, CtStateT<R> C, int dim) {
       flip = get_signed_dp(pp, pm, P.phi_max) < 0.;
     }
     if (flip) { bits |= 1ull << (n - n0); ++mine; }
+    pm = pp;
   }
   cnt[threadIdx.x] = mine;
   // nothing flagged in this pair (the common case): fLR stays, no repair
