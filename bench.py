@@ -572,8 +572,10 @@ def measure_ours(args, wl, rank):
             torch.cuda.synchronize()
             t0 = time.perf_counter()
             d.upload(**pin)
+            tu = time.perf_counter()
             for _ in range(args.steps):
                 d.timestep(d.getmindt())
+            ts = time.perf_counter()
             out = d.state(out=pout)
             t1 = time.perf_counter()
             up = sum(pin[k].nbytes for k in pin)
@@ -581,7 +583,9 @@ def measure_ours(args, wl, rank):
             res["e2e"] = {"value": cells * args.steps / (t1 - t0), "unit": "zone-updates/s",
                           "h2d_bytes_per_step": int(up / args.steps + 8),
                           "d2h_bytes_per_step": int(down / args.steps + 8),
-                          "timed": "upload of the full state, K x (getmindt, timestep), download"}
+                          "timed": "upload of the full state, K x (getmindt, timestep), download",
+                          "phases_ms": {"upload": (tu - t0) * 1e3, "steps": (ts - tu) * 1e3,
+                                        "download": (t1 - ts) * 1e3}}
             del out, pin
         d.close()
         del d

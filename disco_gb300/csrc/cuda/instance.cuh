@@ -181,7 +181,20 @@ struct Instance : InstanceBase {
   double host_t = 0;
   std::vector<double> ring_Om_h;   // ring frames (host copy)
 
+  // FP64 staging of the primitives for download / upload on the mixed path
+  // (NQ N doubles), allocated at the first transfer and kept: a per-call
+  // allocation and release of this size cost more than the copy itself
+  double* stage64 = nullptr;
+  double* staging() {
+    if (!stage64 && cudaMalloc(&stage64, sizeof(double) * NQ * N) != cudaSuccess) {
+      cudaGetLastError();
+      stage64 = nullptr;
+    }
+    return stage64;
+  }
+
   ~Instance() override {
+    if (stage64) cudaFree(stage64);
     if (flush_buf) cudaFree(flush_buf);
     for (int i = 0; i < 2; ++i)
       if (graph[i]) cudaGraphExecDestroy(graph[i]);
@@ -1231,16 +1244,14 @@ struct Instance : InstanceBase {
       if (sizeof(R) == sizeof(double)) {
         CK(cudaMemcpy(v->prim, S.prim, sizeof(double) * NQ * N, cudaMemcpyDeviceToHost));
       } else {   // widened (and back to the lab frame) on the device, then one copy
-        double* stage = nullptr;
-        if (cudaMalloc(&stage, sizeof(double) * NQ * N) != cudaSuccess) {
+        double* stage = staging();
+        if (!stage) {
           disco_set_error("download: no device memory for the FP64 staging copy");
           return DISCO_E_NOMEM;
         }
         k_prim_out<R, NQ><<<prim_grid(), 256, 0, st>>>(S, stage);
-        cudaError_t e = cudaMemcpyAsync(v->prim, stage, sizeof(double) * NQ * N, cudaMemcpyDeviceToHost, st);
-        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-        cudaFree(stage);
-        CK(e);
+        CK(cudaMemcpyAsync(v->prim, stage, sizeof(double) * NQ * N, cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
       }
     }
     double sc[SC_COUNT];
@@ -1259,18 +1270,14 @@ struct Instance : InstanceBase {
       if (sizeof(R) == sizeof(double)) {
         CK(cudaMemcpy(S.prim, v->prim, sizeof(double) * NQ * N, cudaMemcpyHostToDevice));
       } else {   // one copy of the FP64 view, converted (into the ring frame) on the device
-        double* stage = nullptr;
-        if (cudaMalloc(&stage, sizeof(double) * NQ * N) != cudaSuccess) {
+        double* stage = staging();
+        if (!stage) {
           disco_set_error("upload: no device memory for the FP64 staging copy");
           return DISCO_E_NOMEM;
         }
-        cudaError_t e = cudaMemcpyAsync(stage, v->prim, sizeof(double) * NQ * N, cudaMemcpyHostToDevice, st);
-        if (e == cudaSuccess) {
-          k_prim_in<R, NQ><<<prim_grid(), 256, 0, st>>>(S, stage);
-          e = cudaStreamSynchronize(st);
-        }
-        cudaFree(stage);
-        CK(e);
+        CK(cudaMemcpyAsync(stage, v->prim, sizeof(double) * NQ * N, cudaMemcpyHostToDevice, st));
+        k_prim_in<R, NQ><<<prim_grid(), 256, 0, st>>>(S, stage);
+        CK(cudaStreamSynchronize(st));
       }
     }
     if (v->dphi) sync_dphi_r();
