@@ -566,9 +566,14 @@ def measure_ours(args, wl, rank):
             for k in pin:
                 pin[k][...] = st[k]
             del st
-            # the download lands in pinned host buffers as well
+            # the download lands in pinned host buffers as well, written once
+            # before the timed region as the reused buffers of a running
+            # program are (the first write to fresh pages costs more than
+            # the copy and varies between hosts)
             pout = {k: torch.empty(pin[k].shape, dtype=torch.float64, pin_memory=True).numpy()
                     for k in pin}
+            for k in pout:
+                pout[k].fill(0.0)
             torch.cuda.synchronize()
             t0 = time.perf_counter()
             d.upload(**pin)

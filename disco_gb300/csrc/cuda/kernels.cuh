@@ -1997,45 +1997,29 @@ __global__ void __launch_bounds__(128) k_bc_init(DevParams P, DevState<R> S, int
 }
 
 // ---- getmindt, misc.c:39-84 -------------------------------------------------
-// The CFL bound of cell c (the module's mindt hook), +1e300 for ghost cells.
-// Both paths evaluate it in FP64: the mixed path's primitives are widened
-// (omega back in the lab frame) and go through the FP64 bound with FP64 cell
-// extents, so the global timestep is an FP64 quantity everywhere.
+// The CFL bound of cell c, +1e300 for ghost cells: the module's mindt hook
+// on the FP64 path, 1 / cell_rate on the mixed path (FP64 extents and dt).
+template <typename Phys, typename R, int NQ>
+DISCO_D double cell_rate(const DevParams& P, const DevState<R>& S, int c);
+
 template <typename Phys, typename R, int NQ>
 DISCO_D double cell_mindt(const DevParams& P, const DevState<R>& S, int c) {
-  int jk = S.cell_ring[c];
-  int k = div_fast(jk, P.mul_nr), j = jk - k * P.Nr;
-  if (!is_real(P, j, k)) return 1.0e300;
-  int off = S.ring_off[jk], Np = S.ring_off[jk + 1] - off;
-  int i = c - off;
-  int im = off + (i == 0 ? Np - 1 : i - 1);
-  const double* rj = S.r_jph + 1;
-  const double* zk = S.z_kph + 1;
-  double phip = S.piph[c], phim = phip - S.dphi[c];
-  double xp[3] = {rj[j], phip, zk[k]};
-  double xm[3] = {rj[j - 1], phim, zk[k - 1]};
-  double w = .5 * (S.wiph[im] + S.wiph[c]);
   if constexpr (kMix<R>) {
-    // the signal speeds are physics and FP32, as in the Riemann solvers;
-    // the cell extents, the rates, their maximum and dt are FP64:
-    // dt = 1 / max(s_r / dr, s_phi / (r dphi), s_z / dz [, 2 nu / dx^2])
-    (void)xp; (void)xm;
-    R pr[NQ];
-#pragma unroll
-    for (int q = 0; q < NQ; ++q) pr[q] = S.prim[q * S.N + c];
-    R sp[4];
-    const R wr = (R)(w - S.ring_Om[jk]);   // relative to the ring frame, as prim[UPP]
-    const double dph = S.dphi[c];
-    Phys::cfl_speeds_r(P, S.planets, pr, wr, S.ring_rc_r[jk], (R)(phip - .5 * dph), sp);
-    const double* g = S.ring_cfl + 3 * jk;
-    const double iphi = 1.0 / (g[0] * dph);
-    double rate = fmax(f2d_int(sp[0]) * g[1], fmax(f2d_int(sp[1]) * iphi, f2d_int(sp[2]) * g[2]));
-    if (sp[3] > (R)0) {   // explicit viscosity: dt_visc = dx^2 / (2 nu), dx the smallest extent
-      const double ix = fmax(iphi, fmax(g[1], g[2]));
-      rate = fmax(rate, 2.0 * f2d_int(sp[3]) * ix * ix);
-    }
-    return 1.0 / rate;
+    const double rate = cell_rate<Phys, R, NQ>(P, S, c);
+    return rate > 0.0 ? 1.0 / rate : 1.0e300;
   } else {
+    int jk = S.cell_ring[c];
+    int k = div_fast(jk, P.mul_nr), j = jk - k * P.Nr;
+    if (!is_real(P, j, k)) return 1.0e300;
+    int off = S.ring_off[jk], Np = S.ring_off[jk + 1] - off;
+    int i = c - off;
+    int im = off + (i == 0 ? Np - 1 : i - 1);
+    const double* rj = S.r_jph + 1;
+    const double* zk = S.z_kph + 1;
+    double phip = S.piph[c], phim = phip - S.dphi[c];
+    double xp[3] = {rj[j], phip, zk[k]};
+    double xm[3] = {rj[j - 1], phim, zk[k - 1]};
+    double w = .5 * (S.wiph[im] + S.wiph[c]);
     R pr[NQ];
 #pragma unroll
     for (int q = 0; q < NQ; ++q) pr[q] = S.prim[q * S.N + c];
@@ -2044,21 +2028,67 @@ DISCO_D double cell_mindt(const DevParams& P, const DevState<R>& S, int c) {
   }
 }
 
+// Mixed path: the cell's inverse time step.  The signal speeds are physics
+// and FP32, as in the Riemann solvers; the cell extents, the rates, their
+// maximum and dt are FP64: dt = 1 / max(s_r / dr, s_phi / (r dphi),
+// s_z / dz [, 2 nu / dx^2]).  0 for a ghost cell, and for a rate that is
+// not a number (such a cell drops out of the minimum, as in getmindt).
+template <typename Phys, typename R, int NQ>
+DISCO_D double cell_rate(const DevParams& P, const DevState<R>& S, int c) {
+  int jk = S.cell_ring[c];
+  int k = div_fast(jk, P.mul_nr), j = jk - k * P.Nr;
+  if (!is_real(P, j, k)) return 0.0;
+  int off = S.ring_off[jk], Np = S.ring_off[jk + 1] - off;
+  int i = c - off;
+  int im = off + (i == 0 ? Np - 1 : i - 1);
+  const double phip = S.piph[c];
+  const double w = .5 * (S.wiph[im] + S.wiph[c]);
+  R pr[NQ];
+#pragma unroll
+  for (int q = 0; q < NQ; ++q) pr[q] = S.prim[q * S.N + c];
+  R sp[4];
+  const R wr = (R)(w - S.ring_Om[jk]);   // relative to the ring frame, as prim[UPP]
+  const double dph = S.dphi[c];
+  Phys::cfl_speeds_r(P, S.planets, pr, wr, S.ring_rc_r[jk], (R)(phip - .5 * dph), sp);
+  const double* g = S.ring_cfl + 3 * jk;
+  const double iphi = 1.0 / (g[0] * dph);
+  double rate = fmax(f2d_int(sp[0]) * g[1], fmax(f2d_int(sp[1]) * iphi, f2d_int(sp[2]) * g[2]));
+  if (sp[3] > (R)0) {   // explicit viscosity: dt_visc = dx^2 / (2 nu), dx the smallest extent
+    const double ix = fmax(iphi, fmax(g[1], g[2]));
+    rate = fmax(rate, 2.0 * f2d_int(sp[3]) * ix * ix);
+  }
+  return rate >= 0.0 ? rate : 0.0;
+}
+
 template <typename Phys, typename R, int NQ>
 DISCO_D void k_mindt_body(const DevParams& P, const DevState<R>& S, int bx_, int by_) {
   int c = bx_ * blockDim.x + threadIdx.x;
-  double dtc = c < S.N ? cell_mindt<Phys, R, NQ>(P, S, c) : 1.0e300;
   // dt > 0: its IEEE bits order like unsigned integers; NaN sorts above.
+  // The mixed path reduces the largest rate instead and divides once per
+  // block: 1 / x rounds monotonically, so 1 / max(rate) is the smallest
+  // 1 / rate bit for bit.
   __shared__ unsigned long long red[32];
   int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   unsigned long long b;
-  b = __double_as_longlong(dtc);
-  for (int o = 16; o > 0; o >>= 1) b = min(b, __shfl_xor_sync(0xffffffffu, b, o));
+  if constexpr (kMix<R>) {
+    b = __double_as_longlong(c < S.N ? cell_rate<Phys, R, NQ>(P, S, c) : 0.0);
+    for (int o = 16; o > 0; o >>= 1) b = max(b, __shfl_xor_sync(0xffffffffu, b, o));
+  } else {
+    b = __double_as_longlong(c < S.N ? cell_mindt<Phys, R, NQ>(P, S, c) : 1.0e300);
+    for (int o = 16; o > 0; o >>= 1) b = min(b, __shfl_xor_sync(0xffffffffu, b, o));
+  }
   if (lane == 0) red[wid] = b;
   __syncthreads();
   if (wid == 0) {
-    b = lane < (int)(blockDim.x >> 5) ? red[lane] : ~0ull;
-    for (int o = 16; o > 0; o >>= 1) b = min(b, __shfl_xor_sync(0xffffffffu, b, o));
+    if constexpr (kMix<R>) {
+      b = lane < (int)(blockDim.x >> 5) ? red[lane] : 0ull;
+      for (int o = 16; o > 0; o >>= 1) b = max(b, __shfl_xor_sync(0xffffffffu, b, o));
+      const double rmax = __longlong_as_double(b);
+      b = __double_as_longlong(rmax > 0.0 ? 1.0 / rmax : 1.0e300);
+    } else {
+      b = lane < (int)(blockDim.x >> 5) ? red[lane] : ~0ull;
+      for (int o = 16; o > 0; o >>= 1) b = min(b, __shfl_xor_sync(0xffffffffu, b, o));
+    }
     if (lane == 0) atomicMin((unsigned long long*)&S.scal[SC_MIN], b);
   }
 }
