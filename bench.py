@@ -566,20 +566,22 @@ def measure_ours(args, wl, rank):
             for k in pin:
                 pin[k][...] = st[k]
             del st
-            # the download lands in pinned host buffers as well, written once
-            # before the timed region as the reused buffers of a running
-            # program are (the first write to fresh pages costs more than
-            # the copy and varies between hosts)
+            # the download lands in pinned host buffers as well.  One untimed
+            # round trip through both sets of buffers first, as a running
+            # program reuses its transfer buffers: the first device write to
+            # fresh pinned pages costs up to several times the copy itself
+            # (54 against 26 ms for the same download measured back to back)
             pout = {k: torch.empty(pin[k].shape, dtype=torch.float64, pin_memory=True).numpy()
                     for k in pin}
-            for k in pout:
-                pout[k].fill(0.0)
+            d.upload(**pin)
+            d.state(out=pout)
             torch.cuda.synchronize()
             t0 = time.perf_counter()
             d.upload(**pin)
             tu = time.perf_counter()
             for _ in range(args.steps):
                 d.timestep(d.getmindt())
+            torch.cuda.synchronize()   # the last step's kernels count as steps
             ts = time.perf_counter()
             out = d.state(out=pout)
             t1 = time.perf_counter()
