@@ -29,12 +29,15 @@
  * copy its state back before anything reads theDomain */
 void gb300_init(struct domain *);
 void gb300_sync_to_host(struct domain *);
+void gb300_output(struct domain *, const char *);
 void gb300_free(void);
 #define GB300_INIT(d) gb300_init(d)
 #define GB300_SYNC(d) gb300_sync_to_host(d)
+#define GB300_OUTPUT(d, name) gb300_output(d, name)
 #else
 #define GB300_INIT(d) ((void)0)
 #define GB300_SYNC(d) ((void)0)
+#define GB300_OUTPUT(d, name) ((void)0)
 #endif
 
 int mpiSetup(struct domain *, int, char *[]);
@@ -236,6 +239,9 @@ int main(int argc, char **argv)
          fwrite(&d->theTools.t_avg, sizeof(double), 1, g);
          fwrite(d->theTools.Qrz, sizeof(double), (size_t)nq * nring, g);
          fclose(g);
+         /* with the binding: the checkpoint of output() written by the
+          * library from the device state (checkpoint_gb300.h5) */
+         GB300_OUTPUT(d, "checkpoint_gb300");
       }
    } else {
       fprintf(stderr, "unknown mode %s\n", mode);

@@ -64,4 +64,15 @@ def test_reference_harness_on_the_shim(name):
     rep = np.array([float(v) for v in re.findall(r"[-+]?\d\.\d+e[-+]\d{2}(?:\d(?!\.))?", line)])
     assert rep.shape == g["report"].shape
     assert np.allclose(rep, g["report"], rtol=2e-6, atol=1e-30)
+    # the shim's gb300_output in place of output(): the checkpoint file of
+    # the same final state, read by the specification reader
+    import h5spec
+    f = h5spec.File(os.path.join(td, "checkpoint_gb300.h5"))
+    cells = f.dataset("Data/Cells")
+    nq, nf = out["prim"].shape[0], out["Phi"].shape[0]
+    assert cells.shape == (out["prim"].shape[1], nq + nf + 1)
+    assert np.array_equal(cells[:, :nq].T, out["prim"])
+    assert np.array_equal(cells[:, nq:nq + nf].T, out["Phi"])
+    assert np.array_equal(cells[:, -1], out["piph"])
+    assert f.dataset("Grid/T").tolist() == [out["t"]]
     shutil.rmtree(td)
