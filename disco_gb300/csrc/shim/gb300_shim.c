@@ -62,10 +62,19 @@ void gb300_init(struct domain *theDomain)
    disco_modules m;
    gb300_check(disco_params_read("in.par", &p), "disco_params_read");
    gb300_check(disco_modules_read("Makefile_opt.in", &m), "disco_modules_read");
-   if(p.restart_flag)
+   if(p.restart_flag) {
       gb300_check(disco_host_restart(&p, &m, "input.h5", &H), "disco_host_restart");
-   else
+      /* what restart() sets in theDomain (h5in.c:135-160, :303-318); the
+       * cells follow at the first gb300_sync_to_host */
+      theDomain->t = H->t;
+      for(int q = 0; q < H->Npl && q < theDomain->Npl; ++q) {
+         struct planet *P = &theDomain->thePlanets[q];
+         P->r = H->planets[q].r; P->phi = H->planets[q].phi; P->M = H->planets[q].M;
+         P->omega = H->planets[q].omega; P->vr = H->planets[q].vr; P->eps = H->planets[q].eps;
+      }
+   } else {
       gb300_check(disco_host_setup(&p, &m, &H), "disco_host_setup");
+   }
    if(H->Nr != theDomain->Nr || H->Nz != theDomain->Nz) {
       fprintf(stderr, "gb300: grid differs from the reference's set-up\n");
       exit(1);

@@ -28,6 +28,50 @@ CASES = {"cfg1_n24": "configs/cfg1_vortex", "cfg2_n12": "configs/cfg2_mhd_disk",
          "cfg3_n24": "configs/cfg3_planet_disk"}
 
 
+def _run_harness(exe, td, par_text, makefile_opt, nsteps, out="out.bin"):
+    with open(os.path.join(td, "in.par"), "w") as f:
+        f.write(par_text)
+    shutil.copy(makefile_opt, os.path.join(td, "Makefile_opt.in"))
+    r = subprocess.run([exe, "run", str(nsteps), out], cwd=td, capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr[-2000:]
+
+
+@pytest.mark.skipif(_ref() is None, reason="reference sources not present")
+def test_restart_on_the_shim_continues_the_reference_run():
+    """Half the vortex run, its checkpoint through gb300_output, then the
+    reference's main loop with Restart 1 from that file (input.h5) for the
+    other half: the final state equals the unmodified reference's
+    uninterrupted run (the fixture) within 1e-12, the time exactly."""
+    import sys
+    sys.path.insert(0, os.path.join(ROOT, "tests", "golden"))
+    from dumpio import read_dump
+    from disco_gb300 import build
+    build.build()
+    name, cfg = "cfg1_n24", CASES["cfg1_n24"]
+    subprocess.run(["make", "-s", "-f", "oracle/ref/Makefile", f"CFG={cfg}", f"REF={_ref()}", "gb300"],
+                   cwd=ROOT, check=True)
+    exe = os.path.join(ROOT, "oracle", "_ref", os.path.basename(cfg), "disco_ref_gb300")
+    g = load_golden(name)
+    n = int(g["nsteps"])
+    par = str(g["par_text"])
+    mk = os.path.join(ROOT, cfg, "Makefile_opt.in")
+    td1, td2 = tempfile.mkdtemp(prefix="disco_shim_"), tempfile.mkdtemp(prefix="disco_shim_")
+    _run_harness(exe, td1, par, mk, n // 2)
+    shutil.copy(os.path.join(td1, "checkpoint_gb300.h5"), os.path.join(td2, "input.h5"))
+    par2 = re.sub(r"^Restart\s+\d+", "Restart\t1", par, flags=re.M)
+    assert par2 != par
+    _run_harness(exe, td2, par2, mk, n - n // 2)
+    out = read_dump(os.path.join(td2, "out.bin"))
+    real = g["real"].astype(bool)
+    assert abs(out["t"] - float(g["run_t"])) <= 1e-14 * abs(float(g["run_t"]))
+    assert np.max(np.abs(out["piph"] - g["run_piph"])) < 1e-12 * 2 * np.pi
+    for q in range(out["cons"].shape[0]):
+        assert rel_l1(out["cons"][q, real], g["run_cons"][q, real]) < 1e-11, q
+        assert rel_l1(out["prim"][q, real], g["run_prim"][q, real]) < 1e-11, q
+    shutil.rmtree(td1)
+    shutil.rmtree(td2)
+
+
 @pytest.mark.skipif(_ref() is None, reason="reference sources not present")
 @pytest.mark.parametrize("name", list(CASES))
 def test_reference_harness_on_the_shim(name):
