@@ -141,7 +141,7 @@ __global__ void k_ct_avg(DevParams P, DevState<R> S, CtStateT<R> C) {
     if (pa >= 0) {   // LRtype 0 face owned by c (c = L = c1, c2 = R)
       const int o2 = S.ring_off[jk + stride], n2 = S.ring_off[jk + stride + 1] - o2;
       int f = S.run_up_e[d][c];
-      int c2 = S.fR[d][f];
+      int c2 = S.nb_up[d][c];   // = fR of face f, loaded beside f
       R dp1 = S.fdp1[d][f], dp2 = S.fdp2[d][f];
       R Eavg = (dp2 * edge_avg_at(S.Eraw, N, a + 0, c2, o2, n2) + dp1 * edge_avg_at(S.Eraw, N, a + 2, c2, o2, n2)) / (dp1 + dp2);
       R Bavg = (dp2 * edge_avg_at(S.Braw, N, a + 0, c2, o2, n2) + dp1 * edge_avg_at(S.Braw, N, a + 2, c2, o2, n2)) / (dp1 + dp2);
@@ -154,7 +154,7 @@ __global__ void k_ct_avg(DevParams P, DevState<R> S, CtStateT<R> C) {
     if (pb >= 0) {   // LRtype 1 face owned by c (c = R = c1, c2 = L)
       const int o2 = S.ring_off[jk - stride], n2 = S.ring_off[jk - stride + 1] - o2;
       int f = S.run_dn_e[d][c];
-      int c2 = S.fL[d][f];
+      int c2 = S.nb_dn[d][c];   // = fL of face f, loaded beside f
       R dp1 = S.fdp1[d][f], dp2 = S.fdp2[d][f];
       R Eavg = (dp2 * edge_avg_at(S.Eraw, N, a + 1, c2, o2, n2) + dp1 * edge_avg_at(S.Eraw, N, a + 3, c2, o2, n2)) / (dp1 + dp2);
       R Bavg = (dp2 * edge_avg_at(S.Braw, N, a + 1, c2, o2, n2) + dp1 * edge_avg_at(S.Braw, N, a + 3, c2, o2, n2)) / (dp1 + dp2);

@@ -435,6 +435,7 @@ struct Instance : InstanceBase {
       A(&S.pidxs[d], np); A(&S.pdA[d], np); A(&S.pdOm[d], np); A(&S.pcX[d], np);
       A(&S.fflux[d], (size_t)NQ * nf);
       A(&S.run_up_s[d], N); A(&S.run_up_e[d], N); A(&S.run_dn_s[d], N); A(&S.run_dn_e[d], N);
+      A(&S.nb_up[d], N); A(&S.nb_dn[d], N);
       if (ct) {
         A(&S.fErz[d], nf); A(&S.fBrz[d], nf); A(&S.fEphi[d], nf);
         A(&S.ffrL[d], nf); A(&S.ffrR[d], nf); A(&S.fdp1[d], nf); A(&S.fdp2[d], nf);

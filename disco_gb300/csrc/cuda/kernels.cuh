@@ -102,6 +102,8 @@ struct DevState {
   int* run_up_e[2];
   int* run_dn_s[2];            // per cell: first face where the cell is R (pair below)
   int* run_dn_e[2];
+  int* nb_up[2];               // per cell: the R cell of its last face in the pair above
+  int* nb_dn[2];               // per cell: the L cell of its last face in the pair below
   int nf[2];
   // constrained transport (MHD): edge EMFs written by the flux kernels
   int ct;
@@ -628,9 +630,9 @@ DISCO_D void k_faces_body(const DevParams& P, const DevState<R>& S, int dim, int
     int cur = sLR[n];
     int iL = S.fL[d][gf], iR = S.fR[d][gf];
     if (prev == 0) S.run_up_s[d][iL] = gf;
-    if (cur == 0) S.run_up_e[d][iL] = gf;
+    if (cur == 0) { S.run_up_e[d][iL] = gf; S.nb_up[d][iL] = iR; }
     if (prev == 1) S.run_dn_s[d][iR] = gf;
-    if (cur == 1) S.run_dn_e[d][iR] = gf;
+    if (cur == 1) { S.run_dn_e[d][iR] = gf; S.nb_dn[d][iR] = iL; }
   }
 }
 template <typename R>
