@@ -90,6 +90,13 @@ static inline int disco_bc_plugin_ops(int boundary_id, disco_bc_op *o)
       o[n++] = disco_bc_mk(DISCO_BCOP_FIXED, DISCO_SIDE_ZBOT, 0);
       o[n++] = disco_bc_mk(DISCO_BCOP_FIXED, DISCO_SIDE_ZTOP, 0);
       return n;
+   case DISCO_BC_POLAR:           /* Boundary/polar.c: initial() at (centroid r, piph - dphi/2,
+                                     centroid z), which is set_cell_init_q's position, on every
+                                     primitive; without subtract_omega (RotFrame is rejected) */
+      o[n++] = disco_bc_mk(DISCO_BCOP_FIXED_Q, DISCO_SIDE_ROUT, 0xffff);
+      o[n++] = disco_bc_mk(DISCO_BCOP_FIXED_Q, DISCO_SIDE_ZBOT, 0xffff);
+      o[n++] = disco_bc_mk(DISCO_BCOP_FIXED_Q, DISCO_SIDE_ZTOP, 0xffff);
+      return n;
    case DISCO_BC_FIXED_GAP:       /* Boundary/fixed_gap.c */
       o[n++] = disco_bc_mk(DISCO_BCOP_ZEROGRAD, DISCO_SIDE_RINN, 1);
       o[n++] = disco_bc_mk(DISCO_BCOP_FIXED, DISCO_SIDE_ROUT, 0);

@@ -54,10 +54,11 @@ CASES = {
     # stale inner ghosts the reference run stalls (polar3d) or goes
     # non-finite (tube) within six steps
     **{f"bc_{b}": ("configs/cfg1_vortex_zerograd",
-                   {"Num_R": 12, "Num_Z": 2, **({"NoBC_Rmin": 1} if b in ("polar3d", "tube") else {})}, 6,
+                   {"Num_R": 12, "Num_Z": 2,
+                    **({"NoBC_Rmin": 1} if b in ("polar3d", "polar", "tube") else {})}, 6,
                    {"BOUNDARY": b})
        for b in ("zerograd_omk", "zerograd_omIN", "accrete3d", "fixRrefZ", "polar3d", "fixed_gap",
-                 "tube", "surfaceGravBox", "flowthrough")},
+                 "tube", "surfaceGravBox", "flowthrough", "polar")},
     # third-order Runge-Kutta (Timestep 3, timestep.c:35-42) on the vortex,
     # the MHD disk and the viscous planet disk
     "cfg1_rk3": ("configs/cfg1_vortex", {"Num_R": 24, "Timestep": 3}, 10),

@@ -149,7 +149,7 @@ def test_missing_files_and_modules_fail_loudly(tmp_path):
 
 BOUNDARY_PLUGINS = ["fixed", "fixed3d", "outflow3d", "zerograd", "zerograd_omk", "zerograd_omIN",
                     "accrete3d", "fixRrefZ", "polar3d", "fixed_gap", "tube", "surfaceGravBox",
-                    "flowthrough"]
+                    "flowthrough", "polar"]
 ANALYSIS_PLUGINS = ["diag_euler", "diag_disk2d", "diag_cb", "diag_bl", "diag_mhdmri", "diag_grmhdmri"]
 
 
@@ -182,6 +182,18 @@ def test_unbuilt_plugins_fail_loudly(tmp_path, key, name):
     dg = _dg()
     with pytest.raises(dg.DiscoError, match=f"{key}={name} not built"):
         dg.read_modules(_mk(tmp_path, **{key: name}))
+
+
+def test_polar_with_rotating_frame_rejected(tmp_path):
+    """Boundary/polar.c fills its ghosts without subtract_omega; with RotFrame
+    that differs from the built ghost fill, so the set-up refuses it."""
+    dg = _dg()
+    p = dg.read_params(os.path.join(ROOT, "configs/cfg1_vortex/in.par"))
+    m = dg.read_modules(_mk(tmp_path, BOUNDARY="polar"))
+    dg.HostDomain(p, m)   # without RotFrame: built
+    p.RotFrame = 1
+    with pytest.raises(dg.DiscoError, match="polar with RotFrame"):
+        dg.HostDomain(p, m)
 
 
 def test_cooling_damping_keys_read(tmp_path):
