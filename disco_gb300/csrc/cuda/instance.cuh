@@ -478,6 +478,26 @@ struct Instance : InstanceBase {
         CK(cudaMemcpy(d_gi, gi.data(), sizeof(int) * gi.size(), cudaMemcpyHostToDevice));
       }
       S.ghost_ring = d_gr; S.ghost_i0 = d_gi; S.nghost = (int)gr.size();
+      // horizon3d: the rings boundary_fixed_horizon excises, when its r
+      // pass runs at all (Nr > 1, not R_Periodic: main.c:53-61)
+      std::vector<int> hr;
+      std::vector<unsigned char> hx(nring, 0);
+      bool hor = false;
+      for (int o = 0; o < n_bc_ops; ++o) hor = hor || bc_ops[o].op == DISCO_BCOP_HORIZON;
+      if (hor && Nr > 1 && !p.R_Periodic)
+        for (int jk = 0; jk < nring; ++jk) {
+          const int k = jk / Nr, j = jk - k * Nr;
+          if (disco_bc_horizon_ring(dom->r_jph + 1, dom->z_kph + 1, j, k)) { hr.push_back(jk); hx[jk] = 1; }
+        }
+      S.hor_rings = nullptr; S.ring_excised = nullptr; S.nhor = (int)hr.size();
+      if (!hr.empty()) {
+        int* d_hr;
+        unsigned char* d_hx;
+        A(&d_hr, hr.size()); A(&d_hx, (size_t)nring);
+        CK(cudaMemcpy(d_hr, hr.data(), sizeof(int) * hr.size(), cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(d_hx, hx.data(), (size_t)nring, cudaMemcpyHostToDevice));
+        S.hor_rings = d_hr; S.ring_excised = d_hx;
+      }
       S.ghost_tab = nullptr;
       if (S.nghost > 0 && (P.initial_id == 1 || P.initial_id == 2 || P.initial_id == 5)) {   // axisymmetric
         double* tab = nullptr;
@@ -714,6 +734,10 @@ struct Instance : InstanceBase {
         if (dim == 2 && !z_started) { launch_periodic(2); z_started = true; }
         if ((dim == 1 && Nr <= 1) || (dim == 2 && Nz <= 1)) continue;
         if ((dim == 1 && n_pcopy[0]) || (dim == 2 && n_pcopy[1])) continue;
+        if (b.op == DISCO_BCOP_HORIZON) {   // every excised ring, ghosts or not
+          if (S.nhor) LAUNCH("boundary", (k_bc_horizon<R, NQ><<<S.nhor, 128, 0, st>>>(P, S)));
+          continue;
+        }
         const int ng = dim == 1 ? (side ? P.NgRb : P.NgRa) : (side ? P.NgZb : P.NgZa);
         if (ng == 0) continue;
         const int per_layer = dim == 1 ? Nz : Nr, n = dim == 1 ? Nr : Nz;

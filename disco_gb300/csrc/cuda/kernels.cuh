@@ -102,6 +102,12 @@ struct DevState {
   int* run_up_e[2];
   int* run_dn_s[2];            // per cell: first face where the cell is R (pair below)
   int* run_dn_e[2];
+  // Boundary/horizon3d.c: rings boundary_fixed_horizon resets (list) and
+  // the same as a per-ring flag, which drops their cells from the CFL
+  // minimum; null / 0 without that plugin
+  const int* hor_rings;
+  const unsigned char* ring_excised;
+  int nhor;
   int* nb_up[2];               // per cell: the R cell of its last face in the pair above
   int* nb_dn[2];               // per cell: the L cell of its last face in the pair below
   int nf[2];
@@ -1954,20 +1960,8 @@ __global__ void k_bc_copy(DevParams P, DevState<R> S, int dim, int side, int lay
 // dim 1 rings (j, k) of the side's ng layers for all k, dim 2 (j, k) for
 // all j.  mode 0 fixed, 1 fixed_q, 2 fixed_phi.
 template <typename R, int NQ>
-__global__ void __launch_bounds__(128) k_bc_init(DevParams P, DevState<R> S, int dim, int side, int mode,
-                                                 int qmask, double pa, double pb) {
-  int j, k;
-  if (dim == 1) {
-    const int ng = side ? P.NgRb : P.NgRa;
-    const int l = blockIdx.x % ng;
-    k = blockIdx.x / ng;
-    j = side ? P.Nr - P.NgRb + l : l;
-  } else {
-    const int ng = side ? P.NgZb : P.NgZa;
-    const int l = blockIdx.x % ng;
-    j = blockIdx.x / ng;
-    k = side ? P.Nz - P.NgZb + l : l;
-  }
+DISCO_D void bc_init_ring(const DevParams& P, const DevState<R>& S, int j, int k, int mode, int qmask,
+                          double pa, double pb) {
   const int jk = j + P.Nr * k;
   const int off = S.ring_off[jk], Np = S.ring_off[jk + 1] - off;
   const double* rj = S.r_jph + 1;
@@ -1997,6 +1991,31 @@ __global__ void __launch_bounds__(128) k_bc_init(DevParams P, DevState<R> S, int
       if (mode != 1 || ((qmask >> q) & 1)) S.prim[q * N + c] = (R)prim[q];
   }
 }
+template <typename R, int NQ>
+__global__ void __launch_bounds__(128) k_bc_init(DevParams P, DevState<R> S, int dim, int side, int mode,
+                                                 int qmask, double pa, double pb) {
+  int j, k;
+  if (dim == 1) {
+    const int ng = side ? P.NgRb : P.NgRa;
+    const int l = blockIdx.x % ng;
+    k = blockIdx.x / ng;
+    j = side ? P.Nr - P.NgRb + l : l;
+  } else {
+    const int ng = side ? P.NgZb : P.NgZa;
+    const int l = blockIdx.x % ng;
+    j = blockIdx.x / ng;
+    k = side ? P.Nz - P.NgZb + l : l;
+  }
+  bc_init_ring<R, NQ>(P, S, j, k, mode, qmask, pa, pb);
+}
+// boundary_fixed_horizon (boundary_functions.c:622-660): set_cell_init on
+// every cell of the excised rings, real and ghost alike (one block a ring)
+template <typename R, int NQ>
+__global__ void __launch_bounds__(128) k_bc_horizon(DevParams P, DevState<R> S) {
+  const int jk = S.hor_rings[blockIdx.x];
+  const int k = jk / P.Nr, j = jk - k * P.Nr;
+  bc_init_ring<R, NQ>(P, S, j, k, 0, 0, 0.0, 0.0);
+}
 
 // ---- getmindt, misc.c:39-84 -------------------------------------------------
 // The CFL bound of cell c, +1e300 for ghost cells: the module's mindt hook
@@ -2012,7 +2031,7 @@ DISCO_D double cell_mindt(const DevParams& P, const DevState<R>& S, int c) {
   } else {
     int jk = S.cell_ring[c];
     int k = div_fast(jk, P.mul_nr), j = jk - k * P.Nr;
-    if (!is_real(P, j, k)) return 1.0e300;
+    if (!is_real(P, j, k) || (S.ring_excised && S.ring_excised[jk])) return 1.0e300;
     int off = S.ring_off[jk], Np = S.ring_off[jk + 1] - off;
     int i = c - off;
     int im = off + (i == 0 ? Np - 1 : i - 1);
@@ -2039,7 +2058,7 @@ template <typename Phys, typename R, int NQ>
 DISCO_D double cell_rate(const DevParams& P, const DevState<R>& S, int c) {
   int jk = S.cell_ring[c];
   int k = div_fast(jk, P.mul_nr), j = jk - k * P.Nr;
-  if (!is_real(P, j, k)) return 0.0;
+  if (!is_real(P, j, k) || (S.ring_excised && S.ring_excised[jk])) return 0.0;
   int off = S.ring_off[jk], Np = S.ring_off[jk + 1] - off;
   int i = c - off;
   int im = off + (i == 0 ? Np - 1 : i - 1);

@@ -257,7 +257,7 @@ int disco_modules_read(const char *path, disco_modules *m)
                                "fm_torus"};
    static const char *bnd[] = {"fixed", "fixed3d", "outflow3d", "zerograd", "zerograd_omk",
                                "zerograd_omIN", "accrete3d", "fixRrefZ", "polar3d", "fixed_gap",
-                               "tube", "surfaceGravBox", "flowthrough", "polar"};
+                               "tube", "surfaceGravBox", "flowthrough", "polar", "horizon3d"};
    static const char *pla[] = {"none", "sun", "circular", "cm"};
    static const char *ana[] = {"diag_euler", "diag_disk2d", "diag_cb", "diag_bl", "diag_mhdmri",
                                "diag_grmhdmri"};

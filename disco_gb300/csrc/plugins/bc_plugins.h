@@ -10,6 +10,9 @@
  *   ZEROGRAD   boundary_zerograd_* (arg: diode)         :269-441  copy of the next ring inward
  *   REFLECT    boundary_reflect_*                       :442-621  copy of the mirror ring, normal velocity negated
  *   NOSLIP     boundary_noslip_*                        :914-1101 copy of the mirror ring, all velocities negated
+ *   HORIZON    boundary_fixed_horizon                   :622-660  set_cell_init on every ring within
+ *                                                                  R_HOR of the origin, which then leaves
+ *                                                                  the CFL minimum (real = 0)
  * fixed.c and fixed3d.c keep their own kernel (they fill every ghost ring
  * of their dimensions from initial()).
  */
@@ -21,7 +24,8 @@
 #include "disco_gpu.h"
 
 enum { DISCO_BCOP_FIXED = 0, DISCO_BCOP_FIXED_Q = 1, DISCO_BCOP_FIXED_PHI = 2,
-       DISCO_BCOP_ZEROGRAD = 3, DISCO_BCOP_REFLECT = 4, DISCO_BCOP_NOSLIP = 5 };
+       DISCO_BCOP_ZEROGRAD = 3, DISCO_BCOP_REFLECT = 4, DISCO_BCOP_NOSLIP = 5,
+       DISCO_BCOP_HORIZON = 6 };
 enum { DISCO_SIDE_RINN = 0, DISCO_SIDE_ROUT = 1, DISCO_SIDE_ZBOT = 2, DISCO_SIDE_ZTOP = 3 };
 
 typedef struct disco_bc_op {
@@ -31,6 +35,20 @@ typedef struct disco_bc_op {
 } disco_bc_op;
 
 #define DISCO_BC_MAX_OPS 8
+
+/* boundary_fixed_horizon's ring test (boundary_functions.c:634-651, R_HOR
+ * = 1 at :8): ring (j, k) is excised when its outer edge r_jph[j] and the
+ * larger-|z| edge of its layer lie within R_HOR of the origin.  rj and zk
+ * are indexed as the reference's r_jph and z_kph (rj[-1] is valid). */
+#define DISCO_R_HOR 1.0
+static inline int disco_bc_horizon_ring(const double *rj, const double *zk, int j, int k)
+{
+   double zm = zk[k - 1], zp = zk[k];
+   double zo = fabs(zp) > fabs(zm) ? zp : zm;
+   if(fabs(zo) > DISCO_R_HOR) return 0;
+   double ro = rj[j];
+   return sqrt(zo*zo + ro*ro) < DISCO_R_HOR;
+}
 
 static inline disco_bc_op disco_bc_mk(int op, int side, int arg)
 {
@@ -96,6 +114,12 @@ static inline int disco_bc_plugin_ops(int boundary_id, disco_bc_op *o)
       o[n++] = disco_bc_mk(DISCO_BCOP_FIXED_Q, DISCO_SIDE_ROUT, 0xffff);
       o[n++] = disco_bc_mk(DISCO_BCOP_FIXED_Q, DISCO_SIDE_ZBOT, 0xffff);
       o[n++] = disco_bc_mk(DISCO_BCOP_FIXED_Q, DISCO_SIDE_ZTOP, 0xffff);
+      return n;
+   case DISCO_BC_HORIZON3D:       /* Boundary/horizon3d.c */
+      o[n++] = disco_bc_mk(DISCO_BCOP_HORIZON, DISCO_SIDE_RINN, 0);
+      o[n++] = disco_bc_mk(DISCO_BCOP_FIXED, DISCO_SIDE_ROUT, 0);
+      o[n++] = disco_bc_mk(DISCO_BCOP_FIXED, DISCO_SIDE_ZBOT, 0);
+      o[n++] = disco_bc_mk(DISCO_BCOP_FIXED, DISCO_SIDE_ZTOP, 0);
       return n;
    case DISCO_BC_FIXED_GAP:       /* Boundary/fixed_gap.c */
       o[n++] = disco_bc_mk(DISCO_BCOP_ZEROGRAD, DISCO_SIDE_RINN, 1);

@@ -1676,6 +1676,25 @@ static void exchange(int dim)
 
 /* onestep.c:166-172: exchangeData(r); boundary_trans(r) unless R_Periodic;
  * exchangeData(z); boundary_trans(z) unless Z_Periodic */
+/* boundary_fixed_horizon (boundary_functions.c:622-660): every ring within
+ * R_HOR of the origin, ghost or real, back to initial() at the cell
+ * centroid (set_cell_init, :21-31), and out of getmindt (real = 0) */
+static void horizon_rings(void)
+{
+   for(int k = 0; k < D->Nz; k++) for(int j = 0; j < D->Nr; j++) {
+      if(!disco_bc_horizon_ring(D->rj, D->zk, j, k)) continue;
+      int jk = j + D->Nr*k;
+      for(int i = 0; i < D->Np[jk]; i++) {
+         pcell *c = &D->ring[jk][i];
+         double xp[3] = {D->rj[j], c->piph, D->zk[k]}, xm[3] = {D->rj[j - 1], c->piph - c->dphi, D->zk[k - 1]};
+         double x[3];
+         centroid_arr(xp, xm, x);
+         initial(c->prim, x);
+         c->real = 0;
+      }
+   }
+}
+
 static void boundary(void)
 {
    disco_bc_op ops[DISCO_BC_MAX_OPS];
@@ -1688,7 +1707,8 @@ static void boundary(void)
          if(dim == 2 && !zdone) { exchange(2); zdone = 1; }
          if((dim == 1 && D->Nr <= 1) || (dim == 2 && D->Nz <= 1)) continue;
          if(periodic_dim(dim)) continue;
-         if(ops[o].op >= DISCO_BCOP_ZEROGRAD) copy_side(&ops[o]);
+         if(ops[o].op == DISCO_BCOP_HORIZON) horizon_rings();
+         else if(ops[o].op >= DISCO_BCOP_ZEROGRAD) copy_side(&ops[o]);
          else init_side(&ops[o]);
       }
       if(!zdone) exchange(2);

@@ -59,6 +59,10 @@ CASES = {
                    {"BOUNDARY": b})
        for b in ("zerograd_omk", "zerograd_omIN", "accrete3d", "fixRrefZ", "polar3d", "fixed_gap",
                  "tube", "surfaceGravBox", "flowthrough", "polar")},
+    # Boundary/horizon3d.c on the 2D vortex (r from 0.5): boundary_fixed_horizon
+    # resets the rings within R_HOR = 1 of the origin to initial() at every
+    # r boundary pass and drops them from the CFL minimum; fixed outer ghosts
+    "bc_horizon3d": ("configs/cfg1_vortex", {"Num_R": 24}, 10, {"BOUNDARY": "horizon3d"}),
     # third-order Runge-Kutta (Timestep 3, timestep.c:35-42) on the vortex,
     # the MHD disk and the viscous planet disk
     "cfg1_rk3": ("configs/cfg1_vortex", {"Num_R": 24, "Timestep": 3}, 10),
