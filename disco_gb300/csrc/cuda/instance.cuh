@@ -354,7 +354,8 @@ struct Instance : InstanceBase {
       const int ng = dim == 1 ? (side ? dom->NgRb : dom->NgRa) : (side ? dom->NgZb : dom->NgZa);
       const int nreal = dim == 1 ? dom->Nr - dom->NgRa - dom->NgRb : dom->Nz - dom->NgZa - dom->NgZb;
       const int need = bc_ops[o].op == DISCO_BCOP_ZEROGRAD ? 1 : ng;
-      if (bc_ops[o].op >= DISCO_BCOP_ZEROGRAD && ng > 0 && nreal < need) {
+      const bool copy = bc_ops[o].op >= DISCO_BCOP_ZEROGRAD && bc_ops[o].op <= DISCO_BCOP_NOSLIP;
+      if (copy && ng > 0 && nreal < need) {
         disco_set_error("boundary copy needs more real rings than the domain has");
         return DISCO_E_ARG;
       }
@@ -478,16 +479,26 @@ struct Instance : InstanceBase {
         CK(cudaMemcpy(d_gi, gi.data(), sizeof(int) * gi.size(), cudaMemcpyHostToDevice));
       }
       S.ghost_ring = d_gr; S.ghost_i0 = d_gi; S.nghost = (int)gr.size();
-      // horizon3d: the rings boundary_fixed_horizon excises, when its r
-      // pass runs at all (Nr > 1, not R_Periodic: main.c:53-61)
+      // horizon3d / horizon: the rings the plugin excises, when a pass
+      // that excises runs at all (main.c:53-61: r when Nr > 1 and not
+      // R_Periodic; horizon.c also after the z pass, when Nz > 1 and not
+      // Z_Periodic)
       std::vector<int> hr;
       std::vector<unsigned char> hx(nring, 0);
-      bool hor = false;
-      for (int o = 0; o < n_bc_ops; ++o) hor = hor || bc_ops[o].op == DISCO_BCOP_HORIZON;
-      if (hor && Nr > 1 && !p.R_Periodic)
+      bool hor = false, cut = false, rpass = Nr > 1 && !p.R_Periodic, zpass = Nz > 1 && !p.Z_Periodic;
+      for (int o = 0; o < n_bc_ops; ++o)
+        if (bc_ops[o].op == DISCO_BCOP_HORIZON) {
+          const bool zop = bc_ops[o].side >= 2;
+          if ((zop && zpass) || (!zop && rpass)) { hor = true; cut = bc_ops[o].arg == 1; }
+        }
+      if (hor)
         for (int jk = 0; jk < nring; ++jk) {
           const int k = jk / Nr, j = jk - k * Nr;
-          if (disco_bc_horizon_ring(dom->r_jph + 1, dom->z_kph + 1, j, k)) { hr.push_back(jk); hx[jk] = 1; }
+          const double *rj = dom->r_jph + 1, *zk = dom->z_kph + 1;
+          if (cut ? disco_bc_horizon_cut_ring(rj, zk, Nz, j, k) : disco_bc_horizon_ring(rj, zk, j, k)) {
+            hr.push_back(jk);
+            hx[jk] = 1;
+          }
         }
       S.hor_rings = nullptr; S.ring_excised = nullptr; S.nhor = (int)hr.size();
       if (!hr.empty()) {
@@ -735,14 +746,15 @@ struct Instance : InstanceBase {
         if ((dim == 1 && Nr <= 1) || (dim == 2 && Nz <= 1)) continue;
         if ((dim == 1 && n_pcopy[0]) || (dim == 2 && n_pcopy[1])) continue;
         if (b.op == DISCO_BCOP_HORIZON) {   // every excised ring, ghosts or not
-          if (S.nhor) LAUNCH("boundary", (k_bc_horizon<R, NQ><<<S.nhor, 128, 0, st>>>(P, S)));
+          if (S.nhor) LAUNCH("boundary", (k_bc_horizon<R, NQ><<<S.nhor, 128, 0, st>>>(P, S, b.arg ? 3 : 0)));
           continue;
         }
         const int ng = dim == 1 ? (side ? P.NgRb : P.NgRa) : (side ? P.NgZb : P.NgZa);
         if (ng == 0) continue;
         const int per_layer = dim == 1 ? Nz : Nr, n = dim == 1 ? Nr : Nz;
-        if (b.op <= DISCO_BCOP_FIXED_PHI) {
-          LAUNCH("boundary", (k_bc_init<R, NQ><<<ng * per_layer, 128, 0, st>>>(P, S, dim, side, b.op, b.arg,
+        if (b.op <= DISCO_BCOP_FIXED_PHI || b.op == DISCO_BCOP_FIXED_MEAN) {
+          const int mode = b.op == DISCO_BCOP_FIXED_MEAN ? 3 : b.op;
+          LAUNCH("boundary", (k_bc_init<R, NQ><<<ng * per_layer, 128, 0, st>>>(P, S, dim, side, mode, b.arg,
                                                                                b.pa, b.pb)));
         } else {
           const int mode = b.op - DISCO_BCOP_ZEROGRAD;   // 0 zerograd, 1 reflect, 2 noslip

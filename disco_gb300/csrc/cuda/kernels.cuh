@@ -1966,14 +1966,15 @@ DISCO_D void bc_init_ring(const DevParams& P, const DevState<R>& S, int j, int k
   const int off = S.ring_off[jk], Np = S.ring_off[jk + 1] - off;
   const double* rj = S.r_jph + 1;
   const double* zk = S.z_kph + 1;
-  const double xr = centroid_r(rj[j], rj[j - 1]);
-  const double xz = centroid_z(zk[k], zk[k - 1]);
+  // mode 3 (Boundary/horizon.c): arithmetic-mean r and z
+  const double xr = mode == 3 ? .5 * (rj[j] + rj[j - 1]) : centroid_r(rj[j], rj[j - 1]);
+  const double xz = mode == 3 ? .5 * (zk[k] + zk[k - 1]) : centroid_z(zk[k], zk[k - 1]);
   const int N = S.N;
   for (int i = threadIdx.x; i < Np; i += blockDim.x) {
     const int c = off + i;
     const double phip = S.piph[c], dph = S.dphi[c];
     double x[3] = {xr, 0.0, xz};
-    if (mode == 1) {
+    if (mode == 1 || mode == 3) {
       x[1] = phip - .5 * dph;
     } else {
       if (mode == 2) {
@@ -2009,12 +2010,13 @@ __global__ void __launch_bounds__(128) k_bc_init(DevParams P, DevState<R> S, int
   bc_init_ring<R, NQ>(P, S, j, k, mode, qmask, pa, pb);
 }
 // boundary_fixed_horizon (boundary_functions.c:622-660): set_cell_init on
-// every cell of the excised rings, real and ghost alike (one block a ring)
+// every cell of the excised rings, real and ghost alike (one block a ring);
+// mode 3 for Boundary/horizon.c's cut-out (arithmetic-mean positions)
 template <typename R, int NQ>
-__global__ void __launch_bounds__(128) k_bc_horizon(DevParams P, DevState<R> S) {
+__global__ void __launch_bounds__(128) k_bc_horizon(DevParams P, DevState<R> S, int mode) {
   const int jk = S.hor_rings[blockIdx.x];
   const int k = jk / P.Nr, j = jk - k * P.Nr;
-  bc_init_ring<R, NQ>(P, S, j, k, 0, 0, 0.0, 0.0);
+  bc_init_ring<R, NQ>(P, S, j, k, mode, 0, 0.0, 0.0);
 }
 
 // ---- getmindt, misc.c:39-84 -------------------------------------------------

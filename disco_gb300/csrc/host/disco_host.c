@@ -257,7 +257,8 @@ int disco_modules_read(const char *path, disco_modules *m)
                                "fm_torus"};
    static const char *bnd[] = {"fixed", "fixed3d", "outflow3d", "zerograd", "zerograd_omk",
                                "zerograd_omIN", "accrete3d", "fixRrefZ", "polar3d", "fixed_gap",
-                               "tube", "surfaceGravBox", "flowthrough", "polar", "horizon3d"};
+                               "tube", "surfaceGravBox", "flowthrough", "polar", "horizon3d",
+                               "horizon"};
    static const char *pla[] = {"none", "sun", "circular", "cm"};
    static const char *ana[] = {"diag_euler", "diag_disk2d", "diag_cb", "diag_bl", "diag_mhdmri",
                                "diag_grmhdmri"};
@@ -454,10 +455,12 @@ int disco_host_grid(const disco_params *par, const disco_modules *mod,
    if(par->LogZoning != 0) {
       disco_set_error("disco_host_setup: only Log_Zoning 0 is built"); return DISCO_E_MODULE;
    }
-   if(mod->boundary == DISCO_BC_POLAR && par->RotFrame) {
-      /* Boundary/polar.c fills its ghosts without subtract_omega; the
-       * ghost fill here is written for the non-rotating frame */
-      disco_set_error("BOUNDARY=polar with RotFrame is not built"); return DISCO_E_MODULE;
+   if((mod->boundary == DISCO_BC_POLAR || mod->boundary == DISCO_BC_HORIZON) && par->RotFrame) {
+      /* Boundary/polar.c and horizon.c fill their cells without
+       * subtract_omega; the fill here is written for the non-rotating frame */
+      disco_set_error(mod->boundary == DISCO_BC_POLAR ? "BOUNDARY=polar with RotFrame is not built"
+                                                      : "BOUNDARY=horizon with RotFrame is not built");
+      return DISCO_E_MODULE;
    }
    disco_host_domain *d = (disco_host_domain *)calloc(1, sizeof(*d));
    if(!d) return DISCO_E_NOMEM;

@@ -12,7 +12,10 @@
  *   NOSLIP     boundary_noslip_*                        :914-1101 copy of the mirror ring, all velocities negated
  *   HORIZON    boundary_fixed_horizon                   :622-660  set_cell_init on every ring within
  *                                                                  R_HOR of the origin, which then leaves
- *                                                                  the CFL minimum (real = 0)
+ *                                                                  the CFL minimum (real = 0); arg 1: the
+ *                                                                  cut-out of Boundary/horizon.c instead
+ *   FIXED_MEAN (Boundary/horizon.c's own fixed sides)             initial() at the arithmetic-mean r, z
+ *                                                                  and piph - dphi / 2
  * fixed.c and fixed3d.c keep their own kernel (they fill every ghost ring
  * of their dimensions from initial()).
  */
@@ -25,7 +28,7 @@
 
 enum { DISCO_BCOP_FIXED = 0, DISCO_BCOP_FIXED_Q = 1, DISCO_BCOP_FIXED_PHI = 2,
        DISCO_BCOP_ZEROGRAD = 3, DISCO_BCOP_REFLECT = 4, DISCO_BCOP_NOSLIP = 5,
-       DISCO_BCOP_HORIZON = 6 };
+       DISCO_BCOP_HORIZON = 6, DISCO_BCOP_FIXED_MEAN = 7 };
 enum { DISCO_SIDE_RINN = 0, DISCO_SIDE_ROUT = 1, DISCO_SIDE_ZBOT = 2, DISCO_SIDE_ZTOP = 3 };
 
 typedef struct disco_bc_op {
@@ -48,6 +51,27 @@ static inline int disco_bc_horizon_ring(const double *rj, const double *zk, int 
    if(fabs(zo) > DISCO_R_HOR) return 0;
    double ro = rj[j];
    return sqrt(zo*zo + ro*ro) < DISCO_R_HOR;
+}
+
+/* Boundary/horizon.c's cut-out (:73-109): M = 1, cut = 0.7 * 2M; the
+ * domain must reach inside the cut, then ring (j, k) is cut when the
+ * smaller-|z| edge of its layer and its inner edge lie within it (in 2D,
+ * the inner edge alone).  The reference's early exit from the j loop
+ * changes nothing: the test only grows stricter with j. */
+#define DISCO_HORIZON_CUT (0.7 * 2.0)
+static inline int disco_bc_horizon_cut_ring(const double *rj, const double *zk, int Nz, int j, int k)
+{
+   const double cut = DISCO_HORIZON_CUT;
+   if(!(rj[-1] < cut && zk[-1] < cut && zk[Nz - 1] > -cut)) return 0;
+   double zp = zk[k], zm = zk[k - 1];
+   double zc = fabs(zp) < fabs(zm) ? zp : zm;
+   if(fabs(zc) > cut && Nz > 1) return 0;
+   for(int jj = 0; jj <= j; jj++) {
+      double rp = rj[jj], rm = rj[jj - 1];
+      double rc = fabs(rp) < fabs(rm) ? rp : rm;
+      if((rc*rc + zc*zc > cut*cut && Nz > 1) || rc > cut) return 0;
+   }
+   return 1;
 }
 
 static inline disco_bc_op disco_bc_mk(int op, int side, int arg)
@@ -120,6 +144,13 @@ static inline int disco_bc_plugin_ops(int boundary_id, disco_bc_op *o)
       o[n++] = disco_bc_mk(DISCO_BCOP_FIXED, DISCO_SIDE_ROUT, 0);
       o[n++] = disco_bc_mk(DISCO_BCOP_FIXED, DISCO_SIDE_ZBOT, 0);
       o[n++] = disco_bc_mk(DISCO_BCOP_FIXED, DISCO_SIDE_ZTOP, 0);
+      return n;
+   case DISCO_BC_HORIZON:         /* Boundary/horizon.c: the cut-out after each pass */
+      o[n++] = disco_bc_mk(DISCO_BCOP_FIXED_MEAN, DISCO_SIDE_ROUT, 0);
+      o[n++] = disco_bc_mk(DISCO_BCOP_HORIZON, DISCO_SIDE_RINN, 1);
+      o[n++] = disco_bc_mk(DISCO_BCOP_FIXED_MEAN, DISCO_SIDE_ZBOT, 0);
+      o[n++] = disco_bc_mk(DISCO_BCOP_FIXED_MEAN, DISCO_SIDE_ZTOP, 0);
+      o[n++] = disco_bc_mk(DISCO_BCOP_HORIZON, DISCO_SIDE_ZBOT, 1);
       return n;
    case DISCO_BC_FIXED_GAP:       /* Boundary/fixed_gap.c */
       o[n++] = disco_bc_mk(DISCO_BCOP_ZEROGRAD, DISCO_SIDE_RINN, 1);

@@ -1626,6 +1626,13 @@ static void init_side(const disco_bc_op *o)
             for(int q = 0; q < D->nq; q++) if((o->arg >> q) & 1) c->prim[q] = prim[q];
             continue;
          }
+         if(o->op == DISCO_BCOP_FIXED_MEAN) {   /* Boundary/horizon.c's fixed sides */
+            x[0] = .5*(D->rj[j] + D->rj[j - 1]);
+            x[1] = c->piph - .5*c->dphi;
+            x[2] = .5*(D->zk[k] + D->zk[k - 1]);
+            initial(c->prim, x);
+            continue;
+         }
          if(o->op == DISCO_BCOP_FIXED_PHI) {
             double phi = c->piph - 0.5*c->dphi;
             while(phi < o->pa) phi += D->Pmax;
@@ -1678,17 +1685,26 @@ static void exchange(int dim)
  * exchangeData(z); boundary_trans(z) unless Z_Periodic */
 /* boundary_fixed_horizon (boundary_functions.c:622-660): every ring within
  * R_HOR of the origin, ghost or real, back to initial() at the cell
- * centroid (set_cell_init, :21-31), and out of getmindt (real = 0) */
-static void horizon_rings(void)
+ * centroid (set_cell_init, :21-31), and out of getmindt (real = 0).
+ * cut != 0: Boundary/horizon.c's own cut-out (:73-109), initial() at the
+ * arithmetic-mean r, z and the cell's mid phi. */
+static void horizon_rings(int cut)
 {
    for(int k = 0; k < D->Nz; k++) for(int j = 0; j < D->Nr; j++) {
-      if(!disco_bc_horizon_ring(D->rj, D->zk, j, k)) continue;
+      if(cut ? !disco_bc_horizon_cut_ring(D->rj, D->zk, D->Nz, j, k)
+             : !disco_bc_horizon_ring(D->rj, D->zk, j, k)) continue;
       int jk = j + D->Nr*k;
       for(int i = 0; i < D->Np[jk]; i++) {
          pcell *c = &D->ring[jk][i];
-         double xp[3] = {D->rj[j], c->piph, D->zk[k]}, xm[3] = {D->rj[j - 1], c->piph - c->dphi, D->zk[k - 1]};
          double x[3];
-         centroid_arr(xp, xm, x);
+         if(cut) {
+            x[0] = 0.5*(D->rj[j - 1] + D->rj[j]);
+            x[1] = c->piph - .5*c->dphi;
+            x[2] = 0.5*(D->zk[k - 1] + D->zk[k]);
+         } else {
+            double xp[3] = {D->rj[j], c->piph, D->zk[k]}, xm[3] = {D->rj[j - 1], c->piph - c->dphi, D->zk[k - 1]};
+            centroid_arr(xp, xm, x);
+         }
          initial(c->prim, x);
          c->real = 0;
       }
@@ -1707,8 +1723,8 @@ static void boundary(void)
          if(dim == 2 && !zdone) { exchange(2); zdone = 1; }
          if((dim == 1 && D->Nr <= 1) || (dim == 2 && D->Nz <= 1)) continue;
          if(periodic_dim(dim)) continue;
-         if(ops[o].op == DISCO_BCOP_HORIZON) horizon_rings();
-         else if(ops[o].op >= DISCO_BCOP_ZEROGRAD) copy_side(&ops[o]);
+         if(ops[o].op == DISCO_BCOP_HORIZON) horizon_rings(ops[o].arg);
+         else if(ops[o].op >= DISCO_BCOP_ZEROGRAD && ops[o].op <= DISCO_BCOP_NOSLIP) copy_side(&ops[o]);
          else init_side(&ops[o]);
       }
       if(!zdone) exchange(2);

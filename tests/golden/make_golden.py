@@ -63,6 +63,9 @@ CASES = {
     # resets the rings within R_HOR = 1 of the origin to initial() at every
     # r boundary pass and drops them from the CFL minimum; fixed outer ghosts
     "bc_horizon3d": ("configs/cfg1_vortex", {"Num_R": 24}, 10, {"BOUNDARY": "horizon3d"}),
+    # Boundary/horizon.c on the same disk: its own cut (0.7 of 2M, M = 1) with
+    # arithmetic-mean positions, after both the r and the z boundary pass
+    "bc_horizon": ("configs/cfg1_vortex", {"Num_R": 24}, 10, {"BOUNDARY": "horizon"}),
     # third-order Runge-Kutta (Timestep 3, timestep.c:35-42) on the vortex,
     # the MHD disk and the viscous planet disk
     "cfg1_rk3": ("configs/cfg1_vortex", {"Num_R": 24, "Timestep": 3}, 10),

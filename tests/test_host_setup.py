@@ -149,7 +149,7 @@ def test_missing_files_and_modules_fail_loudly(tmp_path):
 
 BOUNDARY_PLUGINS = ["fixed", "fixed3d", "outflow3d", "zerograd", "zerograd_omk", "zerograd_omIN",
                     "accrete3d", "fixRrefZ", "polar3d", "fixed_gap", "tube", "surfaceGravBox",
-                    "flowthrough", "polar", "horizon3d"]
+                    "flowthrough", "polar", "horizon3d", "horizon"]
 ANALYSIS_PLUGINS = ["diag_euler", "diag_disk2d", "diag_cb", "diag_bl", "diag_mhdmri", "diag_grmhdmri"]
 
 
@@ -176,7 +176,7 @@ def test_boundary_and_analysis_plugins_select(tmp_path):
     assert dg.read_modules(_mk(tmp_path, ANALYSIS=None)).analysis == -1
 
 
-@pytest.mark.parametrize("key,name", [("BOUNDARY", "horizon"), ("BOUNDARY", "inflow"),
+@pytest.mark.parametrize("key,name", [("BOUNDARY", "horizon_bin"), ("BOUNDARY", "inflow"),
                                       ("ANALYSIS", "diag_nonexistent")])
 def test_unbuilt_plugins_fail_loudly(tmp_path, key, name):
     dg = _dg()
@@ -184,15 +184,16 @@ def test_unbuilt_plugins_fail_loudly(tmp_path, key, name):
         dg.read_modules(_mk(tmp_path, **{key: name}))
 
 
-def test_polar_with_rotating_frame_rejected(tmp_path):
-    """Boundary/polar.c fills its ghosts without subtract_omega; with RotFrame
-    that differs from the built ghost fill, so the set-up refuses it."""
+@pytest.mark.parametrize("plugin", ["polar", "horizon"])
+def test_frame_free_plugins_with_rotating_frame_rejected(tmp_path, plugin):
+    """Boundary/polar.c and horizon.c fill cells without subtract_omega; with
+    RotFrame that differs from the built fill, so the set-up refuses it."""
     dg = _dg()
     p = dg.read_params(os.path.join(ROOT, "configs/cfg1_vortex/in.par"))
-    m = dg.read_modules(_mk(tmp_path, BOUNDARY="polar"))
+    m = dg.read_modules(_mk(tmp_path, BOUNDARY=plugin))
     dg.HostDomain(p, m)   # without RotFrame: built
     p.RotFrame = 1
-    with pytest.raises(dg.DiscoError, match="polar with RotFrame"):
+    with pytest.raises(dg.DiscoError, match=f"{plugin} with RotFrame"):
         dg.HostDomain(p, m)
 
 
