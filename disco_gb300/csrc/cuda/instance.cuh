@@ -501,6 +501,36 @@ struct Instance : InstanceBase {
           }
         }
       S.hor_rings = nullptr; S.ring_excised = nullptr; S.nhor = (int)hr.size();
+      // horizon_bin: the candidate rings of its two holes, for each pass
+      // that runs, and the per-cell flag its cut-outs set
+      std::vector<int> hl;
+      bool holes = false;
+      for (int o = 0; o < n_bc_ops; ++o)
+        if (bc_ops[o].op == DISCO_BCOP_HOLES) {
+          const bool zop = bc_ops[o].side >= 2;
+          holes = holes || (zop && zpass) || (!zop && rpass);
+        }
+      if (holes)
+        for (int h = 0; h < 2; ++h)
+          for (int jk = 0; jk < nring; ++jk) {
+            const int k = jk / Nr, j = jk - k * Nr;
+            double rc, zc;
+            if (disco_bc_hole_ring(dom->r_jph + 1, dom->z_kph + 1, Nr, Nz, j, k, h, &rc, &zc))
+              hl.push_back(2 * jk + h);
+          }
+      S.hole_list = nullptr; S.cell_excised = nullptr; S.nhole = (int)hl.size();
+      if (holes) {
+        unsigned char* d_cx;
+        A(&d_cx, (size_t)N);
+        CK(cudaMemset(d_cx, 0, (size_t)N));
+        S.cell_excised = d_cx;
+        if (!hl.empty()) {
+          int* d_hl;
+          A(&d_hl, hl.size());
+          CK(cudaMemcpy(d_hl, hl.data(), sizeof(int) * hl.size(), cudaMemcpyHostToDevice));
+          S.hole_list = d_hl;
+        }
+      }
       if (!hr.empty()) {
         int* d_hr;
         unsigned char* d_hx;
@@ -745,6 +775,10 @@ struct Instance : InstanceBase {
         if (dim == 2 && !z_started) { launch_periodic(2); z_started = true; }
         if ((dim == 1 && Nr <= 1) || (dim == 2 && Nz <= 1)) continue;
         if ((dim == 1 && n_pcopy[0]) || (dim == 2 && n_pcopy[1])) continue;
+        if (b.op == DISCO_BCOP_HOLES) {
+          if (S.nhole) LAUNCH("boundary", (k_bc_holes<R, NQ><<<S.nhole, 128, 0, st>>>(P, S)));
+          continue;
+        }
         if (b.op == DISCO_BCOP_HORIZON) {   // every excised ring, ghosts or not
           if (S.nhor) LAUNCH("boundary", (k_bc_horizon<R, NQ><<<S.nhor, 128, 0, st>>>(P, S, b.arg ? 3 : 0)));
           continue;

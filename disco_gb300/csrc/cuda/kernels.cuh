@@ -14,6 +14,7 @@
 #include "../plugins/ic_vortex_gauss.h"
 #include "../plugins/ic_disks.h"
 #include "../plugins/ic_fm_torus.h"
+#include "../plugins/bc_plugins.h"
 
 namespace disco {
 
@@ -108,6 +109,11 @@ struct DevState {
   const int* hor_rings;
   const unsigned char* ring_excised;
   int nhor;
+  // Boundary/horizon_bin.c: candidate (ring, hole) entries, 2 jk + hole,
+  // and the per-cell flag its cut-outs set for good (real = 0)
+  const int* hole_list;
+  unsigned char* cell_excised;
+  int nhole;
   int* nb_up[2];               // per cell: the R cell of its last face in the pair above
   int* nb_dn[2];               // per cell: the L cell of its last face in the pair below
   int nf[2];
@@ -2009,6 +2015,33 @@ __global__ void __launch_bounds__(128) k_bc_init(DevParams P, DevState<R> S, int
   }
   bc_init_ring<R, NQ>(P, S, j, k, mode, qmask, pa, pb);
 }
+// Boundary/horizon_bin.c's cut-outs (:79-179): on a candidate ring of hole
+// h, every cell whose point (rc, mid phi, zc) lies within the hole goes back
+// to initial() at the arithmetic-mean r, z and its mid phi, and leaves the
+// CFL minimum for good (one block a candidate entry)
+template <typename R, int NQ>
+__global__ void __launch_bounds__(128) k_bc_holes(DevParams P, DevState<R> S) {
+  const int e = S.hole_list[blockIdx.x], jk = e >> 1, h = e & 1;
+  const int k = jk / P.Nr, j = jk - k * P.Nr;
+  const double* rj = S.r_jph + 1;
+  const double* zk = S.z_kph + 1;
+  double rc, zc;
+  if (!disco_bc_hole_ring(rj, zk, P.Nr, P.Nz, j, k, h, &rc, &zc)) return;
+  const int off = S.ring_off[jk], Np = S.ring_off[jk + 1] - off, N = S.N;
+  for (int i = threadIdx.x; i < Np; i += blockDim.x) {
+    const int c = off + i;
+    const double phi = S.piph[c] - .5 * S.dphi[c];
+    if (!disco_bc_hole_cell(rc, zc, P.Nz, phi, h)) continue;
+    double x[3] = {.5 * (rj[j - 1] + rj[j]), phi, .5 * (zk[k - 1] + zk[k])};
+    double prim[MAX_Q];
+    initial_eval(P, prim, x);
+    if constexpr (kMix<R>) prim[UPP] -= S.ring_Om[jk];   // ring frame
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) S.prim[q * N + c] = (R)prim[q];
+    S.cell_excised[c] = 1;
+  }
+}
+
 // boundary_fixed_horizon (boundary_functions.c:622-660): set_cell_init on
 // every cell of the excised rings, real and ghost alike (one block a ring);
 // mode 3 for Boundary/horizon.c's cut-out (arithmetic-mean positions)
@@ -2033,7 +2066,8 @@ DISCO_D double cell_mindt(const DevParams& P, const DevState<R>& S, int c) {
   } else {
     int jk = S.cell_ring[c];
     int k = div_fast(jk, P.mul_nr), j = jk - k * P.Nr;
-    if (!is_real(P, j, k) || (S.ring_excised && S.ring_excised[jk])) return 1.0e300;
+    if (!is_real(P, j, k) || (S.ring_excised && S.ring_excised[jk]) || (S.cell_excised && S.cell_excised[c]))
+      return 1.0e300;
     int off = S.ring_off[jk], Np = S.ring_off[jk + 1] - off;
     int i = c - off;
     int im = off + (i == 0 ? Np - 1 : i - 1);
@@ -2060,7 +2094,8 @@ template <typename Phys, typename R, int NQ>
 DISCO_D double cell_rate(const DevParams& P, const DevState<R>& S, int c) {
   int jk = S.cell_ring[c];
   int k = div_fast(jk, P.mul_nr), j = jk - k * P.Nr;
-  if (!is_real(P, j, k) || (S.ring_excised && S.ring_excised[jk])) return 0.0;
+  if (!is_real(P, j, k) || (S.ring_excised && S.ring_excised[jk]) || (S.cell_excised && S.cell_excised[c]))
+    return 0.0;
   int off = S.ring_off[jk], Np = S.ring_off[jk + 1] - off;
   int i = c - off;
   int im = off + (i == 0 ? Np - 1 : i - 1);

@@ -258,7 +258,7 @@ int disco_modules_read(const char *path, disco_modules *m)
    static const char *bnd[] = {"fixed", "fixed3d", "outflow3d", "zerograd", "zerograd_omk",
                                "zerograd_omIN", "accrete3d", "fixRrefZ", "polar3d", "fixed_gap",
                                "tube", "surfaceGravBox", "flowthrough", "polar", "horizon3d",
-                               "horizon"};
+                               "horizon", "horizon_bin"};
    static const char *pla[] = {"none", "sun", "circular", "cm"};
    static const char *ana[] = {"diag_euler", "diag_disk2d", "diag_cb", "diag_bl", "diag_mhdmri",
                                "diag_grmhdmri"};
@@ -455,11 +455,14 @@ int disco_host_grid(const disco_params *par, const disco_modules *mod,
    if(par->LogZoning != 0) {
       disco_set_error("disco_host_setup: only Log_Zoning 0 is built"); return DISCO_E_MODULE;
    }
-   if((mod->boundary == DISCO_BC_POLAR || mod->boundary == DISCO_BC_HORIZON) && par->RotFrame) {
-      /* Boundary/polar.c and horizon.c fill their cells without
-       * subtract_omega; the fill here is written for the non-rotating frame */
-      disco_set_error(mod->boundary == DISCO_BC_POLAR ? "BOUNDARY=polar with RotFrame is not built"
-                                                      : "BOUNDARY=horizon with RotFrame is not built");
+   if((mod->boundary == DISCO_BC_POLAR || mod->boundary == DISCO_BC_HORIZON ||
+       mod->boundary == DISCO_BC_HORIZON_BIN) && par->RotFrame) {
+      /* Boundary/polar.c, horizon.c and horizon_bin.c fill their cells
+       * without subtract_omega; the fill here is written for the
+       * non-rotating frame */
+      char msg[96];
+      snprintf(msg, sizeof msg, "BOUNDARY=%s with RotFrame is not built", mod->boundary_name);
+      disco_set_error(msg);
       return DISCO_E_MODULE;
    }
    disco_host_domain *d = (disco_host_domain *)calloc(1, sizeof(*d));

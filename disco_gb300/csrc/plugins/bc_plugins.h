@@ -16,6 +16,8 @@
  *                                                                  cut-out of Boundary/horizon.c instead
  *   FIXED_MEAN (Boundary/horizon.c's own fixed sides)             initial() at the arithmetic-mean r, z
  *                                                                  and piph - dphi / 2
+ *   HOLES      (Boundary/horizon_bin.c's two cut-outs)            the cells within 0.8 of x = +-5 back to
+ *                                                                  initial(), and out of the CFL minimum
  * fixed.c and fixed3d.c keep their own kernel (they fill every ghost ring
  * of their dimensions from initial()).
  */
@@ -28,7 +30,13 @@
 
 enum { DISCO_BCOP_FIXED = 0, DISCO_BCOP_FIXED_Q = 1, DISCO_BCOP_FIXED_PHI = 2,
        DISCO_BCOP_ZEROGRAD = 3, DISCO_BCOP_REFLECT = 4, DISCO_BCOP_NOSLIP = 5,
-       DISCO_BCOP_HORIZON = 6, DISCO_BCOP_FIXED_MEAN = 7 };
+       DISCO_BCOP_HORIZON = 6, DISCO_BCOP_FIXED_MEAN = 7, DISCO_BCOP_HOLES = 8 };
+
+#ifdef __CUDACC__
+#define DISCO_BC_HD __host__ __device__
+#else
+#define DISCO_BC_HD
+#endif
 enum { DISCO_SIDE_RINN = 0, DISCO_SIDE_ROUT = 1, DISCO_SIDE_ZBOT = 2, DISCO_SIDE_ZTOP = 3 };
 
 typedef struct disco_bc_op {
@@ -58,6 +66,51 @@ static inline int disco_bc_horizon_ring(const double *rj, const double *zk, int 
  * smaller-|z| edge of its layer and its inner edge lie within it (in 2D,
  * the inner edge alone).  The reference's early exit from the j loop
  * changes nothing: the test only grows stricter with j. */
+/* Boundary/horizon_bin.c (:24-31, :79-179): hole h (0, 1) of a binary of
+ * total mass M = 1, separation a = 10, mass ratio q = 1 sits at x = a_h
+ * (a_0 = q a / (1 + q), a_1 = -a / (1 + q)) with radius 0.8 * 2 M_h.  Ring
+ * (j, k) is a candidate when the domain reaches the hole and the ring's
+ * nearer edges lie within the cut; *rc and *zc receive those edges.  The
+ * reference walks candidate rings cell by cell (disco_bc_hole_cell). */
+DISCO_BC_HD static inline int disco_bc_hole_ring(const double *rj, const double *zk, int Nr, int Nz,
+                                                 int j, int k, int h, double *rc, double *zc)
+{
+   const double M = 1.0, a = 1.0e1, q = 1.0;
+   const double Mh = h == 0 ? M / (1 + q) : q * M / (1 + q);
+   const double ah = h == 0 ? q * a / (1 + q) : -a / (1 + q);
+   const double cut = 0.8 * (2 * Mh);
+   /* the region test: hole 0 at r ~ a_0, hole 1 at r ~ -a_1 */
+   const double s = h == 0 ? ah : -ah;
+   if(!(rj[-1] < s + cut && rj[Nr - 1] > s - cut && zk[-1] < cut && zk[Nz - 1] > -cut)) return 0;
+   double zp = zk[k], zm = zk[k - 1];
+   double z = fabs(zp) < fabs(zm) ? zp : zm;
+   if(fabs(z) > cut && Nz > 1) return 0;
+   double rp = rj[j], rm = rj[j - 1];
+   double r;
+   if(h == 0) {
+      r = fabs(rp - ah) < fabs(rm - ah) ? rp : rm;
+      if(((r - ah)*(r - ah) + z*z > cut*cut && Nz > 1) || fabs(r - ah) > cut) return 0;
+   } else {
+      r = fabs(rp + ah) < fabs(rm + ah) ? rp : rm;
+      if(((r + ah)*(r + ah) + z*z > cut*cut && Nz > 1) || fabs(r + ah) > cut) return 0;
+   }
+   *rc = r;
+   *zc = z;
+   return 1;
+}
+/* the cell test of a candidate ring: the point (rc, phi, zc) within the cut
+ * of hole h (phi = piph - dphi / 2) */
+DISCO_BC_HD static inline int disco_bc_hole_cell(double rc, double zc, int Nz, double phi, int h)
+{
+   const double M = 1.0, a = 1.0e1, q = 1.0;
+   const double Mh = h == 0 ? M / (1 + q) : q * M / (1 + q);
+   const double ah = h == 0 ? q * a / (1 + q) : -a / (1 + q);
+   const double cut = 0.8 * (2 * Mh);
+   double xc = rc * cos(phi), yc = rc * sin(phi);
+   double d2 = Nz > 1 ? (xc - ah)*(xc - ah) + yc*yc + zc*zc : (xc - ah)*(xc - ah) + yc*yc;
+   return d2 < cut*cut;
+}
+
 #define DISCO_HORIZON_CUT (0.7 * 2.0)
 static inline int disco_bc_horizon_cut_ring(const double *rj, const double *zk, int Nz, int j, int k)
 {
@@ -151,6 +204,13 @@ static inline int disco_bc_plugin_ops(int boundary_id, disco_bc_op *o)
       o[n++] = disco_bc_mk(DISCO_BCOP_FIXED_MEAN, DISCO_SIDE_ZBOT, 0);
       o[n++] = disco_bc_mk(DISCO_BCOP_FIXED_MEAN, DISCO_SIDE_ZTOP, 0);
       o[n++] = disco_bc_mk(DISCO_BCOP_HORIZON, DISCO_SIDE_ZBOT, 1);
+      return n;
+   case DISCO_BC_HORIZON_BIN:     /* Boundary/horizon_bin.c: the holes after each pass */
+      o[n++] = disco_bc_mk(DISCO_BCOP_FIXED_MEAN, DISCO_SIDE_ROUT, 0);
+      o[n++] = disco_bc_mk(DISCO_BCOP_HOLES, DISCO_SIDE_RINN, 0);
+      o[n++] = disco_bc_mk(DISCO_BCOP_FIXED_MEAN, DISCO_SIDE_ZBOT, 0);
+      o[n++] = disco_bc_mk(DISCO_BCOP_FIXED_MEAN, DISCO_SIDE_ZTOP, 0);
+      o[n++] = disco_bc_mk(DISCO_BCOP_HOLES, DISCO_SIDE_ZBOT, 0);
       return n;
    case DISCO_BC_FIXED_GAP:       /* Boundary/fixed_gap.c */
       o[n++] = disco_bc_mk(DISCO_BCOP_ZEROGRAD, DISCO_SIDE_RINN, 1);

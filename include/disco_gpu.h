@@ -65,7 +65,7 @@ enum disco_boundary_id{ DISCO_BC_FIXED = 0, DISCO_BC_FIXED3D = 1,
                         DISCO_BC_TUBE = 10, DISCO_BC_SURFACEGRAVBOX = 11,
                         DISCO_BC_FLOWTHROUGH = 12, DISCO_BC_POLAR = 13,
                         DISCO_BC_HORIZON3D = 14, DISCO_BC_HORIZON = 15,
-                        DISCO_BC_COUNT = 16 };
+                        DISCO_BC_HORIZON_BIN = 16, DISCO_BC_COUNT = 17 };
 enum disco_planets_id { DISCO_PL_NONE = 0, DISCO_PL_SUN = 1,
                         DISCO_PL_CIRCULAR = 2, DISCO_PL_CM = 3 };
 /* ANALYSIS of Makefile_opt.in: the Diagnostics/ plugin whose ring averages

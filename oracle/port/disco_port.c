@@ -1711,6 +1711,28 @@ static void horizon_rings(int cut)
    }
 }
 
+/* Boundary/horizon_bin.c's cut-outs (:79-179): hole 0, then hole 1; on a
+ * candidate ring, a cell whose point (rc, mid phi, zc) lies within the hole
+ * goes back to initial() at the arithmetic-mean r, z and its mid phi, and
+ * out of getmindt for good (real = 0) */
+static void hole_cells(void)
+{
+   for(int h = 0; h < 2; h++)
+      for(int k = 0; k < D->Nz; k++) for(int j = 0; j < D->Nr; j++) {
+         double rc, zc;
+         if(!disco_bc_hole_ring(D->rj, D->zk, D->Nr, D->Nz, j, k, h, &rc, &zc)) continue;
+         int jk = j + D->Nr*k;
+         for(int i = 0; i < D->Np[jk]; i++) {
+            pcell *c = &D->ring[jk][i];
+            double phi = c->piph - .5*c->dphi;
+            if(!disco_bc_hole_cell(rc, zc, D->Nz, phi, h)) continue;
+            double x[3] = {0.5*(D->rj[j - 1] + D->rj[j]), phi, 0.5*(D->zk[k - 1] + D->zk[k])};
+            initial(c->prim, x);
+            c->real = 0;
+         }
+      }
+}
+
 static void boundary(void)
 {
    disco_bc_op ops[DISCO_BC_MAX_OPS];
@@ -1724,6 +1746,7 @@ static void boundary(void)
          if((dim == 1 && D->Nr <= 1) || (dim == 2 && D->Nz <= 1)) continue;
          if(periodic_dim(dim)) continue;
          if(ops[o].op == DISCO_BCOP_HORIZON) horizon_rings(ops[o].arg);
+         else if(ops[o].op == DISCO_BCOP_HOLES) hole_cells();
          else if(ops[o].op >= DISCO_BCOP_ZEROGRAD && ops[o].op <= DISCO_BCOP_NOSLIP) copy_side(&ops[o]);
          else init_side(&ops[o]);
       }

@@ -66,6 +66,11 @@ CASES = {
     # Boundary/horizon.c on the same disk: its own cut (0.7 of 2M, M = 1) with
     # arithmetic-mean positions, after both the r and the z boundary pass
     "bc_horizon": ("configs/cfg1_vortex", {"Num_R": 24}, 10, {"BOUNDARY": "horizon"}),
+    # Boundary/horizon_bin.c: two holes of radius 0.8 at x = +-5 (its fixed
+    # M = 1, a = 10, q = 1), cell by cell; the vortex out to r = 6 reaches them
+    # (no inner ghost rings: the plugin never fills them)
+    "bc_horizon_bin": ("configs/cfg1_vortex", {"Num_R": 48, "R_Max": 6.0, "NoBC_Rmin": 1}, 10,
+                       {"BOUNDARY": "horizon_bin"}),
     # third-order Runge-Kutta (Timestep 3, timestep.c:35-42) on the vortex,
     # the MHD disk and the viscous planet disk
     "cfg1_rk3": ("configs/cfg1_vortex", {"Num_R": 24, "Timestep": 3}, 10),

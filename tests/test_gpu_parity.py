@@ -38,7 +38,9 @@ CASES = {"cfg1_n24": "configs/cfg1_vortex", "cfg2_n12": "configs/cfg2_mhd_disk",
          # Boundary/horizon3d.c on the 2D vortex: rings within R_HOR reset and out of the CFL
          "bc_horizon3d": "configs/cfg1_vortex",
          # Boundary/horizon.c: its own cut-out after the r and z passes
-         "bc_horizon": "configs/cfg1_vortex"}
+         "bc_horizon": "configs/cfg1_vortex",
+         # Boundary/horizon_bin.c: two holes at x = +-5, cell by cell, on the vortex out to r = 6
+         "bc_horizon_bin": "configs/cfg1_vortex"}
 # GRMHD runs on the FP64 path only
 FP64_ONLY = {"cfg4_n12", "cfg4_diag", "cfg4t_body", "cfg4t_n24", "cfg4_outflow", "cfg4_zerograd"}
 

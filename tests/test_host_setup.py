@@ -149,7 +149,7 @@ def test_missing_files_and_modules_fail_loudly(tmp_path):
 
 BOUNDARY_PLUGINS = ["fixed", "fixed3d", "outflow3d", "zerograd", "zerograd_omk", "zerograd_omIN",
                     "accrete3d", "fixRrefZ", "polar3d", "fixed_gap", "tube", "surfaceGravBox",
-                    "flowthrough", "polar", "horizon3d", "horizon"]
+                    "flowthrough", "polar", "horizon3d", "horizon", "horizon_bin"]
 ANALYSIS_PLUGINS = ["diag_euler", "diag_disk2d", "diag_cb", "diag_bl", "diag_mhdmri", "diag_grmhdmri"]
 
 
@@ -176,7 +176,7 @@ def test_boundary_and_analysis_plugins_select(tmp_path):
     assert dg.read_modules(_mk(tmp_path, ANALYSIS=None)).analysis == -1
 
 
-@pytest.mark.parametrize("key,name", [("BOUNDARY", "horizon_bin"), ("BOUNDARY", "inflow"),
+@pytest.mark.parametrize("key,name", [("BOUNDARY", "wedge"), ("BOUNDARY", "inflow"),
                                       ("ANALYSIS", "diag_nonexistent")])
 def test_unbuilt_plugins_fail_loudly(tmp_path, key, name):
     dg = _dg()
@@ -184,7 +184,7 @@ def test_unbuilt_plugins_fail_loudly(tmp_path, key, name):
         dg.read_modules(_mk(tmp_path, **{key: name}))
 
 
-@pytest.mark.parametrize("plugin", ["polar", "horizon"])
+@pytest.mark.parametrize("plugin", ["polar", "horizon", "horizon_bin"])
 def test_frame_free_plugins_with_rotating_frame_rejected(tmp_path, plugin):
     """Boundary/polar.c and horizon.c fill cells without subtract_omega; with
     RotFrame that differs from the built fill, so the set-up refuses it."""

@@ -33,7 +33,7 @@ def _port_domain(g):
 
 BC_CASES = [f"bc_{b}" for b in ("zerograd_omk", "zerograd_omIN", "accrete3d", "fixRrefZ", "polar3d",
                                  "fixed_gap", "tube", "surfaceGravBox", "flowthrough", "polar",
-                                 "horizon3d", "horizon")]
+                                 "horizon3d", "horizon", "horizon_bin")]
 SINK_CASES = ["cfg3_sink", "cfg3_sink_exp", "cfg3_nozzle"]
 HYDRO_CASES = ["cfg1_n24", "cfg1_hll_static", "cfg1_exact_mesh", "cfg1_rotframe", "cfg3_n24",
                "cfg1_zerograd", "cfg3_outflow", "cfg1_rk3", "cfg3_rk3", "cfg3_cooldamp"] + BC_CASES + SINK_CASES
