@@ -331,8 +331,10 @@ struct Instance : InstanceBase {
         disco_set_error("MHD is built with constrained transport only (CT_MODE 2, Constrained_Transport 1)");
         return DISCO_E_MODULE;
       }
-      if (P.riemann_solver != SOLVER_HLLD) {
-        disco_set_error("MHD is built with the HLLD solver only (Riemann_Solver 2)");
+      const bool hll_hllc = P.riemann_solver == SOLVER_HLL || P.riemann_solver == SOLVER_HLLC;
+      if (P.riemann_solver != SOLVER_HLLD && !(hll_hllc && !kMix<R>)) {
+        disco_set_error("MHD is built with HLLD (Riemann_Solver 2), and with HLL / HLLC (0, 1) on the "
+                        "FP64 path");
         return DISCO_E_MODULE;
       }
       if (dom->NgRa == 0 || dom->NgRb == 0 || (dom->Nz > 1 && (dom->NgZa == 0 || dom->NgZb == 0))) {

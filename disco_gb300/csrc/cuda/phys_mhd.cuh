@@ -147,13 +147,90 @@ struct Mhd {
     }
   }
 
-  // HLL/HLLC paths of solve_riemann are not used with this module here
-  // (configurations select HLLD, Riemann_Solver 2); rejected at set-up.
-  DISCO_D static void vel(const DevParams&, const R*, const R*, R* Sl, R* Sr, R* Ss, const R*, R,
-                          R*) { *Sl = -1; *Sr = 1; *Ss = 0; }
-  DISCO_D static void getUstar(const DevParams&, const R*, R* U, R, R, R, const R*, const R*, R = 0) {
+  // ---- mhd.c's HLL/HLLC hooks (FP64 path; the mixed path rejects these
+  // solvers at set-up) ----------------------------------------------------
+  // vel (mhd.c:318-450): fast magnetosonic bounds of both states, the
+  // contact speed from the total-pressure balance, and in Bpack the HLL
+  // average of B (normal, r, phi, z) and v.B for the star state.
+  DISCO_D static void vel(const DevParams& P, const R* p1, const R* p2, R* Sl, R* Sr, R* Ss, const R* n,
+                          R r, R* Bpack) {
+    const R gam = PRM(R, P, gamma_law);
+    const R* pp[2] = {p1, p2};
+    R v[2][3], B[2][3], rho[2], Pr[2], vn[2], Bn[2], B2[2], cf[2], m[2][3], Fm[2][3], FB[2][3];
 #pragma unroll
-    for (int q = 0; q < NQ; ++q) U[q] = 0;
+    for (int s = 0; s < 2; ++s) {
+      const R* p = pp[s];
+      rho[s] = p[RHO]; Pr[s] = p[PPP];
+      v[s][0] = p[URR]; v[s][1] = r * p[UPP]; v[s][2] = p[UZZ];
+      B[s][0] = p[BRR]; B[s][1] = p[BPP]; B[s][2] = p[BZZ];
+      vn[s] = v[s][0] * n[0] + v[s][1] * n[1] + v[s][2] * n[2];
+      Bn[s] = B[s][0] * n[0] + B[s][1] * n[1] + B[s][2] * n[2];
+      B2[s] = B[s][0] * B[s][0] + B[s][1] * B[s][1] + B[s][2] * B[s][2];
+      R cs = sqrt(gam * (Pr[s] / rho[s])), b2 = B2[s] / rho[s];
+      R a = cs * cs + b2;
+      cf[s] = (R).5 * (cs * cs + b2 + sqrt(fabs(a * a - (R)4.0 * cs * cs * Bn[s] * Bn[s] / rho[s])));
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        FB[s][c] = vn[s] * B[s][c] - Bn[s] * v[s][c];
+        m[s][c] = rho[s] * v[s][c];
+        Fm[s][c] = rho[s] * v[s][c] * vn[s] + (Pr[s] + (R).5 * B2[s]) * n[c] - B[s][c] * Bn[s];
+      }
+    }
+    R Lm = vn[0] - sqrt(cf[0]), Lp = vn[0] + sqrt(cf[0]);
+    if (Lm > vn[1] - sqrt(cf[1])) Lm = vn[1] - sqrt(cf[1]);
+    if (Lp < vn[1] + sqrt(cf[1])) Lp = vn[1] + sqrt(cf[1]);
+    const R aL = Lp, aR = -Lm;
+    R Bh[3], mh[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      Bh[c] = (aR * B[0][c] + aL * B[1][c] + FB[0][c] - FB[1][c]) / (aL + aR);
+      mh[c] = (aR * m[0][c] + aL * m[1][c] + Fm[0][c] - Fm[1][c]) / (aL + aR);
+    }
+    R Bnh = Bh[0] * n[0] + Bh[1] * n[1] + Bh[2] * n[2];
+    R mnL = m[0][0] * n[0] + m[0][1] * n[1] + m[0][2] * n[2];
+    R mnR = m[1][0] * n[0] + m[1][1] * n[1] + m[1][2] * n[2];
+    R rhoh = (aR * rho[0] + aL * rho[1] + mnL - mnR) / (aL + aR);
+    *Ss = (rho[1] * vn[1] * (Lp - vn[1]) - rho[0] * vn[0] * (Lm - vn[0]) +
+           (Pr[0] + (R).5 * B2[0] - Bn[0] * Bn[0]) - (Pr[1] + (R).5 * B2[1] - Bn[1] * Bn[1])) /
+          (rho[1] * (Lp - vn[1]) - rho[0] * (Lm - vn[0]));
+    R vh0 = mh[0] / rhoh, vh1 = mh[1] / rhoh, vh2 = mh[2] / rhoh;
+    Bpack[0] = Bnh; Bpack[1] = Bh[0]; Bpack[2] = Bh[1]; Bpack[3] = Bh[2];
+    Bpack[4] = vh0 * Bh[0] + vh1 * Bh[1] + vh2 * Bh[2];
+    *Sl = Lm;
+    *Sr = Lp;
+  }
+  // getUstar (mhd.c:71-137): the HLLC star state of the side with wave
+  // speed Sk and contact Ss, with the HLL field Bpack of vel
+  DISCO_D static void getUstar(const DevParams& P, const R* prim, R* Us, R r, R Sk, R Ss, const R* n,
+                               const R* Bpack, R = 0) {
+    const R gam = PRM(R, P, gamma_law);
+    const R Bsn = Bpack[0], Bs[3] = {Bpack[1], Bpack[2], Bpack[3]}, vBs = Bpack[4];
+    const R rho = prim[RHO], Pp = prim[PPP];
+    const R v[3] = {prim[URR], prim[UPP] * r, prim[UZZ]};
+    const R B[3] = {prim[BRR], prim[BPP], prim[BZZ]};
+    R v2 = v[0] * v[0] + v[1] * v[1] + v[2] * v[2], B2 = B[0] * B[0] + B[1] * B[1] + B[2] * B[2];
+    R vn = v[0] * n[0] + v[1] * n[1] + v[2] * n[2], Bn = B[0] * n[0] + B[1] * n[1] + B[2] * n[2];
+    R vB = v[0] * B[0] + v[1] * B[1] + v[2] * B[2];
+    R E = (R).5 * rho * v2 + Pp / (gam - (R)1.) + (R).5 * B2;
+    R Bs2 = Bs[0] * Bs[0] + Bs[1] * Bs[1] + Bs[2] * Bs[2];
+    R Ps = rho * (Sk - vn) * (Ss - vn) + (Pp + (R).5 * B2 - Bn * Bn) - (R).5 * Bs2 + Bsn * Bsn;
+    R Ds = (Sk - vn) * rho / (Sk - Ss);
+    R Ms[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const R mc = rho * v[c];
+      Ms[c] = ((Sk - vn) * mc + (B[c] * Bn - Bs[c] * Bsn)) / (Sk - Ss);
+    }
+    R Es = ((Sk - vn) * E + (Ps + (R).5 * Bs2) * Ss - (Pp + (R).5 * B2) * vn - vBs * Bsn + vB * Bn) / (Sk - Ss);
+    R Msn = Ds * Ss, mn = Ms[0] * n[0] + Ms[1] * n[1] + Ms[2] * n[2];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) Ms[c] += n[c] * (Msn - mn);
+    Us[DDD] = Ds; Us[SRR] = Ms[0]; Us[LLL] = r * Ms[1]; Us[SZZ] = Ms[2]; Us[TAU] = Es;
+    Us[BRR] = Bs[0] * ((R)1.0 / r);   // bfield_scale_factor(r, 0) = 1 / r (mhd.c:518)
+    Us[BPP] = Bs[1] / r;
+    Us[BZZ] = Bs[2];
+#pragma unroll
+    for (int q = 8; q < NQ; ++q) Us[q] = prim[q] * Us[DDD];
   }
 
   // ---- hlld.c ----------------------------------------------------------------

@@ -749,6 +749,89 @@ static double mindt(const double *p, double w, const double *xp, const double *x
 { return D->mhd ? m_mindt(p, w, xp, xm) : e_mindt(p, w, xp, xm); }
 
 /* ---- riemann.c:216-320 ------------------------------------------------------- */
+/* mhd.c's wave-speed bounds for HLL/HLLC (vel, :318-450): the fast
+ * magnetosonic speeds of both states bound the fan, the contact speed comes
+ * from the total-pressure balance, and Bpack carries the HLL average of B
+ * (normal component, r, phi, z) and v.B for the star state. */
+static void m_vel(const double *p1, const double *p2, double *Sl, double *Sr, double *Ss,
+                  const double *n, const double *x, double *Bpack)
+{
+   const double r = x[0], gam = D->par.Adiabatic_Index;
+   const double *pp[2] = {p1, p2};
+   double v[2][3], B[2][3], rho[2], P[2], vn[2], Bn[2], B2[2], cf[2];
+   double m[2][3], Fm[2][3], FB[2][3];
+   for(int s = 0; s < 2; s++) {
+      const double *p = pp[s];
+      rho[s] = p[RHO]; P[s] = p[PPP];
+      v[s][0] = p[URR]; v[s][1] = r*p[UPP]; v[s][2] = p[UZZ];
+      B[s][0] = p[BRR]; B[s][1] = p[BPP]; B[s][2] = p[BZZ];
+      vn[s] = v[s][0]*n[0] + v[s][1]*n[1] + v[s][2]*n[2];
+      Bn[s] = B[s][0]*n[0] + B[s][1]*n[1] + B[s][2]*n[2];
+      B2[s] = B[s][0]*B[s][0] + B[s][1]*B[s][1] + B[s][2]*B[s][2];
+      double cs = sqrt(gam*(P[s]/rho[s])), b2 = B2[s]/rho[s];
+      double a = cs*cs + b2;
+      cf[s] = .5*(cs*cs + b2 + sqrt(fabs(a*a - 4.0*cs*cs*Bn[s]*Bn[s]/rho[s])));
+      for(int c = 0; c < 3; c++) {
+         FB[s][c] = vn[s]*B[s][c] - Bn[s]*v[s][c];
+         m[s][c] = rho[s]*v[s][c];
+         Fm[s][c] = rho[s]*v[s][c]*vn[s] + (P[s] + .5*B2[s])*n[c] - B[s][c]*Bn[s];
+      }
+   }
+   double Lm = vn[0] - sqrt(cf[0]), Lp = vn[0] + sqrt(cf[0]);
+   if(Lm > vn[1] - sqrt(cf[1])) Lm = vn[1] - sqrt(cf[1]);
+   if(Lp < vn[1] + sqrt(cf[1])) Lp = vn[1] + sqrt(cf[1]);
+   const double aL = Lp, aR = -Lm;
+   double Bh[3], mh[3];
+   for(int c = 0; c < 3; c++) {
+      Bh[c] = (aR*B[0][c] + aL*B[1][c] + FB[0][c] - FB[1][c])/(aL + aR);
+      mh[c] = (aR*m[0][c] + aL*m[1][c] + Fm[0][c] - Fm[1][c])/(aL + aR);
+   }
+   double Bnh = Bh[0]*n[0] + Bh[1]*n[1] + Bh[2]*n[2];
+   double mnL = m[0][0]*n[0] + m[0][1]*n[1] + m[0][2]*n[2];
+   double mnR = m[1][0]*n[0] + m[1][1]*n[1] + m[1][2]*n[2];
+   double rhoh = (aR*rho[0] + aL*rho[1] + mnL - mnR)/(aL + aR);
+   *Ss = (rho[1]*vn[1]*(Lp - vn[1]) - rho[0]*vn[0]*(Lm - vn[0])
+          + (P[0] + .5*B2[0] - Bn[0]*Bn[0]) - (P[1] + .5*B2[1] - Bn[1]*Bn[1]))
+         /(rho[1]*(Lp - vn[1]) - rho[0]*(Lm - vn[0]));
+   double vh[3] = {mh[0]/rhoh, mh[1]/rhoh, mh[2]/rhoh};
+   Bpack[0] = Bnh; Bpack[1] = Bh[0]; Bpack[2] = Bh[1]; Bpack[3] = Bh[2];
+   Bpack[4] = vh[0]*Bh[0] + vh[1]*Bh[1] + vh[2]*Bh[2];
+   *Sl = Lm;
+   *Sr = Lp;
+}
+
+/* mhd.c's HLLC star state (getUstar, :71-137) of the side with wave speed
+ * Sk, contact Ss and the HLL field Bpack of m_vel */
+static void m_getUstar(const double *prim, double *Us, const double *x, double Sk, double Ss,
+                       const double *n, const double *Bpack)
+{
+   const double r = x[0], gam = D->par.Adiabatic_Index;
+   const double Bsn = Bpack[0], Bs[3] = {Bpack[1], Bpack[2], Bpack[3]}, vBs = Bpack[4];
+   const double rho = prim[RHO], Pp = prim[PPP];
+   const double v[3] = {prim[URR], prim[UPP]*r, prim[UZZ]};
+   const double B[3] = {prim[BRR], prim[BPP], prim[BZZ]};
+   double v2 = v[0]*v[0] + v[1]*v[1] + v[2]*v[2], B2 = B[0]*B[0] + B[1]*B[1] + B[2]*B[2];
+   double vn = v[0]*n[0] + v[1]*n[1] + v[2]*n[2], Bn = B[0]*n[0] + B[1]*n[1] + B[2]*n[2];
+   double vB = v[0]*B[0] + v[1]*B[1] + v[2]*B[2];
+   double E = .5*rho*v2 + Pp/(gam - 1.) + .5*B2;
+   double Bs2 = Bs[0]*Bs[0] + Bs[1]*Bs[1] + Bs[2]*Bs[2];
+   double Ps = rho*(Sk - vn)*(Ss - vn) + (Pp + .5*B2 - Bn*Bn) - .5*Bs2 + Bsn*Bsn;
+   double Ds = (Sk - vn)*rho/(Sk - Ss);
+   double Ms[3];
+   for(int c = 0; c < 3; c++) {
+      const double mc = rho*v[c];   /* the momentum first, as mhd.c forms it */
+      Ms[c] = ((Sk - vn)*mc + (B[c]*Bn - Bs[c]*Bsn))/(Sk - Ss);
+   }
+   double Es = ((Sk - vn)*E + (Ps + .5*Bs2)*Ss - (Pp + .5*B2)*vn - vBs*Bsn + vB*Bn)/(Sk - Ss);
+   double Msn = Ds*Ss, mn = Ms[0]*n[0] + Ms[1]*n[1] + Ms[2]*n[2];
+   for(int c = 0; c < 3; c++) Ms[c] += n[c]*(Msn - mn);
+   Us[DDD] = Ds; Us[SRR] = Ms[0]; Us[LLL] = r*Ms[1]; Us[SZZ] = Ms[2]; Us[TAU] = Es;
+   Us[BRR] = Bs[0]*(1.0/r);   /* bfield_scale_factor(r, 0) = 1 / r (mhd.c:518) */
+   Us[BPP] = Bs[1]/r;
+   Us[BZZ] = Bs[2];
+   for(int q = D->nc; q < D->nq; q++) Us[q] = prim[q]*Us[DDD];
+}
+
 static void solve_riemann(const double *primL, const double *primR, double *consL, double *consR,
                           const double *gLr, const double *gLp, const double *gLz,
                           const double *gRr, const double *gRp, const double *gRz,
@@ -759,8 +842,9 @@ static void solve_riemann(const double *primL, const double *primR, double *cons
    double Flux[MAXQ] = {0}, Ustr[MAXQ] = {0};
    int solver = D->par.Riemann_Solver;   /* 0 HLL, 1 HLLC, 2 HLLD, 3 HLLC with HLL for r < 0.1 */
    if(solver == 0 || solver == 1 || solver == 3) {
-      double Sl, Sr, Ss;
-      e_vel(primL, primR, &Sl, &Sr, &Ss, n, x);
+      double Sl, Sr, Ss, Bpack[5];
+      if(D->mhd) m_vel(primL, primR, &Sl, &Sr, &Ss, n, x, Bpack);
+      else e_vel(primL, primR, &Sl, &Sr, &Ss, n, x);
       if(w < Sl) {
          flux(primL, Flux, x, n);
          prim2cons(primL, Ustr, x, 1.0);
@@ -782,12 +866,14 @@ static void solve_riemann(const double *primL, const double *primR, double *cons
          double Uk[MAXQ], Fk[MAXQ];
          if(w < Ss) {
             prim2cons(primL, Uk, x, 1.0);
-            e_getUstar(primL, Ustr, x, Sl, Ss, n);
+            if(D->mhd) m_getUstar(primL, Ustr, x, Sl, Ss, n, Bpack);
+            else e_getUstar(primL, Ustr, x, Sl, Ss, n);
             flux(primL, Fk, x, n);
             for(q = 0; q < nq; q++) Flux[q] = Fk[q] + Sl*(Ustr[q] - Uk[q]);
          } else {
             prim2cons(primR, Uk, x, 1.0);
-            e_getUstar(primR, Ustr, x, Sr, Ss, n);
+            if(D->mhd) m_getUstar(primR, Ustr, x, Sr, Ss, n, Bpack);
+            else e_getUstar(primR, Ustr, x, Sr, Ss, n);
             flux(primR, Fk, x, n);
             for(q = 0; q < nq; q++) Flux[q] = Fk[q] + Sr*(Ustr[q] - Uk[q]);
          }
@@ -2051,7 +2137,8 @@ port_domain *disco_port_create(const disco_host_domain *h)
    d->NgZa = h->NgZa; d->NgZb = h->NgZb; d->nq = h->num_q; d->nc = h->mod.num_c;
    d->mhd = h->mod.hydro == DISCO_HYDRO_MHD;
    d->ct = d->mhd && h->mod.ct_mode == 2 && h->par.CT;
-   if(d->mhd && (!d->ct || h->par.Riemann_Solver != 2 || h->NgRa == 0 || h->NgRb == 0 ||
+   if(d->mhd && (!d->ct || (h->par.Riemann_Solver != 0 && h->par.Riemann_Solver != 1 &&
+                             h->par.Riemann_Solver != 2) || h->NgRa == 0 || h->NgRb == 0 ||
                  h->NgZa == 0 || h->NgZb == 0)) { free(d); return NULL; }
    disco_bc_op bops[DISCO_BC_MAX_OPS];
    if(disco_bc_plugin_ops(h->mod.boundary, bops) < 0) { free(d); return NULL; }

@@ -71,6 +71,10 @@ CASES = {
     # (no inner ghost rings: the plugin never fills them)
     "bc_horizon_bin": ("configs/cfg1_vortex", {"Num_R": 48, "R_Max": 6.0, "NoBC_Rmin": 1}, 10,
                        {"BOUNDARY": "horizon_bin"}),
+    # the MHD disk with the HLL and HLLC solvers (Riemann_Solver 0, 1):
+    # mhd.c's vel (fast magnetosonic bounds) and getUstar, with CT
+    "cfg2_hll": ("configs/cfg2_mhd_disk", {"Num_R": 12, "Num_Z": 6, "Riemann_Solver": 0}, 5),
+    "cfg2_hllc": ("configs/cfg2_mhd_disk", {"Num_R": 12, "Num_Z": 6, "Riemann_Solver": 1}, 5),
     # third-order Runge-Kutta (Timestep 3, timestep.c:35-42) on the vortex,
     # the MHD disk and the viscous planet disk
     "cfg1_rk3": ("configs/cfg1_vortex", {"Num_R": 24, "Timestep": 3}, 10),

@@ -146,6 +146,8 @@ def test_divb_stays_at_roundoff(name, precision):
     for bit)."""
     import disco_gb300 as dg
     from oracle.port import PortDomain
+    if precision and name in FP64_ONLY:
+        pytest.skip("FP64 path only")
     d, g = _domain(name, precision)
     h = d.host
     real = g["real"].astype(bool)

@@ -29,6 +29,8 @@ CASES = {"cfg1_n24": "configs/cfg1_vortex", "cfg2_n12": "configs/cfg2_mhd_disk",
          "cfg1_zerograd": "configs/cfg1_vortex_zerograd",
          # the MHD disk with zero-gradient and outflow ghosts (module text in the fixture)
          "cfg2_outflow": "configs/cfg2_mhd_disk", "cfg2_zerograd": "configs/cfg2_mhd_disk",
+         # the MHD disk with HLL and HLLC (mhd.c's vel and getUstar), FP64 path
+         "cfg2_hll": "configs/cfg2_mhd_disk", "cfg2_hllc": "configs/cfg2_mhd_disk",
          "cfg4_outflow": "configs/cfg4_grmhd_disk", "cfg4_zerograd": "configs/cfg4_grmhd_disk",
          "cfg3_outflow": "configs/cfg3_planet_disk_outflow",
          # the other ghost-ring plugins on the 3D vortex (module text in the fixture)
@@ -42,7 +44,8 @@ CASES = {"cfg1_n24": "configs/cfg1_vortex", "cfg2_n12": "configs/cfg2_mhd_disk",
          # Boundary/horizon_bin.c: two holes at x = +-5, cell by cell, on the vortex out to r = 6
          "bc_horizon_bin": "configs/cfg1_vortex"}
 # GRMHD runs on the FP64 path only
-FP64_ONLY = {"cfg4_n12", "cfg4_diag", "cfg4t_body", "cfg4t_n24", "cfg4_outflow", "cfg4_zerograd"}
+FP64_ONLY = {"cfg4_n12", "cfg4_diag", "cfg4t_body", "cfg4t_n24", "cfg4_outflow", "cfg4_zerograd",
+             "cfg2_hll", "cfg2_hllc"}
 
 
 def _domain(name, precision=0):

@@ -100,11 +100,13 @@ def test_port_bit_exact_vs_reference_binary():
     shutil.rmtree(td)
 
 
-@pytest.mark.parametrize("name", ["cfg2_n12", "cfg2_rk3", "cfg2_outflow", "cfg2_zerograd"])
+@pytest.mark.parametrize("name", ["cfg2_n12", "cfg2_rk3", "cfg2_outflow", "cfg2_zerograd", "cfg2_hll",
+                                  "cfg2_hllc"])
 def test_port_mhd_ct_bit_exact_vs_golden(name):
-    """3D MHD disk with HLLD and constrained transport (RK2 and RK3, fixed,
-    outflow and zero-gradient ghosts): the oracle equals the reference bit
-    for bit (conserved variables, face fluxes, positions)."""
+    """3D MHD disk with constrained transport (HLLD; HLL and HLLC with
+    mhd.c's vel and getUstar; RK2 and RK3, fixed, outflow and zero-gradient
+    ghosts): the oracle equals the reference bit for bit (conserved
+    variables, face fluxes, positions)."""
     g = load_golden(name)
     h, s = _port_run(write_par(g["par_text"]), mk_path(g), int(g["nsteps"]))
     real = g["real"].astype(bool)
