@@ -313,3 +313,20 @@ def test_cooling_rejected_for_grmhd():
     with pytest.raises(dg.DiscoError, match="Newtonian modules"):
         dg.Domain(os.path.join(cfg, "in.par"), os.path.join(cfg, "Makefile_opt.in"),
                   overrides={"Num_R": 12, "Num_Z": 4, "coolType": 1, "coolPar1": 1.0})
+
+
+@pytest.mark.parametrize("solver", [0, 1])
+def test_mhd_hll_hllc_rejected_on_mixed_path(solver):
+    """MHD with HLL or HLLC (Riemann_Solver 0, 1) is built on the FP64 path;
+    the mixed path refuses it at create rather than run it without the
+    ring-frame offset those solvers would need."""
+    import disco_gb300 as dg
+    cfg = os.path.join(ROOT, "configs/cfg2_mhd_disk")
+    args = (os.path.join(cfg, "in.par"), os.path.join(cfg, "Makefile_opt.in"))
+    ov = {"Num_R": 12, "Num_Z": 6, "Riemann_Solver": solver}
+    with pytest.raises(dg.DiscoError, match="FP64 path"):
+        dg.Domain(*args, precision=1, overrides=ov)
+    d = dg.Domain(*args, precision=0, overrides=ov)
+    d.timestep(d.getmindt())
+    assert d.status()["nan_cells"] == 0
+    d.close()
