@@ -214,6 +214,36 @@ def test_restart_rejects_bad_files(tmp_path):
         api.HostDomain(pe, me, restart=path)
 
 
+def test_restart_survives_any_flipped_byte(tmp_path):
+    """The reader checks every offset, size and checksum it takes from the
+    file: a checkpoint with one byte flipped anywhere in its metadata (every
+    byte of the superblock and root header, every fifth byte of the rest of
+    the first 8 KB and of the last 16 KB, where the headers, the global heap
+    and the parameter tables lie) or in its data either restarts or raises
+    DiscoError -- it never crashes the process or reads out of bounds."""
+    import disco_gb300.api as api
+    h, p, m = _host("mhd", noiseType=0)
+    path = str(tmp_path / "ck.h5")
+    h.checkpoint(path)
+    raw = bytearray(open(path, "rb").read())
+    n = len(raw)
+    where = [*range(0, 2048), *range(2048, 8192, 5), *range(n - 16384, n, 5),
+             *range(8192, n - 16384, 4099)]
+    bp = str(tmp_path / "bad.h5")
+    errors = 0
+    for w in where:
+        bad = bytearray(raw)
+        bad[w] ^= 0xff
+        open(bp, "wb").write(bad)
+        try:
+            api.HostDomain(p, m, restart=bp)
+        except api.DiscoError:
+            errors += 1
+    # the superblock's 48 bytes end in a checksum over the first 44: a flip
+    # of any of them is caught
+    assert errors >= 48
+
+
 def test_checkpoint_abi_symbols():
     """The checkpoint entry points are exported with the header's names."""
     import disco_gb300.api as api
